@@ -1,0 +1,170 @@
+/*
+ * ocrt_gb300.h — C ABI of the GB300 successive-orders-of-scattering (SOS)
+ * vector radiative-transfer solve path.
+ *
+ * Drop-in boundary for the solve API of the OCRT C solver
+ * (code/OCRT_C/src/rt_solver.h).  Plain C types only: no CUDA or torch types
+ * cross this boundary, so the library can be bound from C, ctypes, cgo or JNI.
+ *
+ * Conventions kept from the reference (rt_types.h:7-50, rt_solver.h):
+ *   - F_sun = pi normalisation ("Convention B"): rho = I_TOA / mu_sun.
+ *   - Fourier reconstruction X(phi) = X_0 + 2 sum_m X_m cos m(phi+pi),
+ *     U(phi) = 2 sum_m U_m sin m(phi+pi)           (rt_fourier.c:9-33).
+ *   - Return codes: 0 ok, -1 invalid arguments, -2 non-finite field,
+ *     -3 allocation failure, -7 bottom-source shape (rt_solver.h:7-11).
+ *     Non-convergence is not an error: converged = 0 and
+ *     n_orders_used = max_orders (rt_solver.c:2193-2211).
+ *   - Callers own every input and output buffer.
+ */
+#ifndef OCRT_GB300_H
+#define OCRT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ------------------------------------------------------ */
+#define OCRT_OK                        0
+#define OCRT_ERR_ARGS                 -1
+#define OCRT_ERR_NONFINITE            -2
+#define OCRT_ERR_ALLOC                -3
+#define OCRT_ERR_DEVICE               -4   /* CUDA launch/runtime failure (no reference counterpart) */
+#define OCRT_ERR_UNSUPPORTED          -5   /* surface/mode outside the GB300 solve path */
+#define OCRT_ERR_BOTTOM_SOURCE_SHAPE  -7
+
+/* ---- enumerations (values identical to rt_types.h:59-65, 181-184) ------ */
+enum {
+    OCRT_SURFACE_BLACK = 0,
+    OCRT_SURFACE_LAMBERT = 1,               /* not on the solve path: -5 */
+    OCRT_SURFACE_BLACK_FRESNEL_OCEAN = 2,   /* rough (wind>0) or flat (wind<=0) Fresnel over a black ocean */
+    OCRT_SURFACE_FLAT = 3,                  /* exact flat Fresnel */
+    OCRT_SURFACE_OCEAN = 4                  /* coupled in-water solve: -5 (not built) */
+};
+enum { OCRT_TAU_R_AUTO = 0, OCRT_TAU_R_FROM_INPUT = 1 };
+/* Altitude mapping of the uniform-optical-depth level grid.  The plane-parallel
+ * solve does not depend on it; IPSS ray tracing does (rt_atm.c:205-232). */
+enum { OCRT_PROFILE_US62 = 0, OCRT_PROFILE_EXPONENTIAL = 1 };
+
+/* ---- per-case input (solve-relevant fields of rt_case_t, rt_types.h:321-360) */
+typedef struct {
+    double sza_deg;          /* [0, 90) */
+    double vza_deg;          /* [0, 90) */
+    double raa_deg;          /* public relative azimuth, degrees */
+    double wavelength_nm;    /* [330, 1100] */
+    int    surface;          /* OCRT_SURFACE_* */
+    double pressure_hpa;     /* <= 0 => no Rayleigh (rt_types.h:327-330) */
+    double tau_r_input;      /* column Rayleigh depth for OCRT_TAU_R_FROM_INPUT */
+    double n_water;          /* default 1.34 */
+    double wind_speed;       /* m/s; <= 0 => flat Fresnel for BLACK_FRESNEL_OCEAN */
+    int    sigma_type;       /* 0 Nakajima-Tanaka, 1 OCRT floor law (default 1) */
+    int    q_convention;     /* 0 legacy (Rs-Rp)/2, 1 Mishchenko (Rp-Rs)/2 (default 1) */
+    int    decouple_sunglint;/* 1 => direct sunglint not added to rho */
+} ocrt_case;
+
+/* ---- solver options (solve-relevant fields of rt_options_t, rt_types.h:654-795) */
+typedef struct {
+    int    n_mu;             /* Gauss nodes per hemisphere, default 24, max 64 */
+    int    n_layers;         /* default 40, max 1024 */
+    int    fourier_m_max;    /* default 2; the reference caps this at 32, this library at 255 */
+    int    max_orders;       /* SOS max_iterations, default 20 */
+    double tolerance;        /* SOS relative sup-norm tolerance, default 1e-7 */
+    int    tau_r_source;     /* OCRT_TAU_R_* */
+    int    pssa;             /* 1 => IPSS spherical correction (rt_ipss.h) */
+    int    view_as_node;     /* 1 (default) => mu_view is a zero-weight ring node */
+    double aer_h_km;         /* aerosol scale height, default 2 km */
+    int    rayleigh_profile; /* OCRT_PROFILE_* (default US62, the reference's mapping) */
+    double rayleigh_h_km;    /* scale height for OCRT_PROFILE_EXPONENTIAL */
+    int    n_phi_surface;    /* Cox-Munk azimuth quadrature, default 1024 */
+} ocrt_opts;
+
+/* ---- aerosol expansion (rt_aerosol_input_t moment path, rt_solver.h:94-114) */
+typedef struct {
+    double tau_a;            /* column AOD at the wavelength */
+    double ssa_a;            /* aerosol single-scattering albedo [0,1] */
+    int    L_max;            /* >= 2 */
+    const double *beta;      /* [L_max+1], beta_0 = 1 */
+    const double *gamma;     /* [L_max+1] */
+    const double *alpha;     /* [L_max+1] */
+    const double *zeta;      /* [L_max+1] */
+} ocrt_aerosol;
+
+/* ---- per-case output (solve-path fields of rt_result_t, rt_types.h:496-651) */
+typedef struct {
+    double rho_I, rho_Q, rho_U;
+    double I_TOA, Q_TOA, U_TOA;
+    double tau_R_total;
+    int    n_orders_used;     /* max over Fourier modes */
+    int    converged;         /* AND over Fourier modes */
+    int    order_modes;       /* sum over modes of orders executed (work actually done) */
+    double kappa_ipss;        /* IPSS factor applied (1 when off) */
+    double T_dir_dn;
+    double T_diff_dn_hemi;
+    double T_total_dn_hemi;
+    double T_diff_dn_dir;
+    double T_total_up_dir;
+    double T_sg_up_dir;
+    double T_dir_up_view;
+    double rho_glint_direct_I, rho_glint_direct_Q, rho_glint_direct_U;
+} ocrt_result;
+
+/* Optional per-mode diagnostics; every non-NULL array holds fourier_m_max+1
+ * entries (sos_orders_per_m / sos_residual_per_m of rt_result_t). */
+typedef struct {
+    int    *orders_per_m;
+    double *residual_per_m;
+    double *view_I_m, *view_Q_m, *view_U_m;   /* TOA upwelling at mu_view per mode */
+} ocrt_diag;
+
+/* Fill defaults identical to rt_options_default() (rt_types.h:760-795) plus
+ * the CLI case defaults of main.c:1826-1840. */
+void ocrt_opts_default(ocrt_opts *opts);
+void ocrt_case_default(ocrt_case *cs);
+
+/* ---- device lifetime -------------------------------------------------- */
+/* Select the CUDA device and create the library's streams, CUDA graphs cache
+ * and workspace arena.  Idempotent.  Replaces no reference call (the
+ * reference allocates per solve, rt_solver.h:45-48). */
+int         ocrt_gb_init(int device);
+void        ocrt_gb_shutdown(void);
+const char *ocrt_gb_last_error(void);
+
+/* ---- single solve ------------------------------------------------------
+ * Replaces rt_solve_case_pol (rt_solver.h:84-85) when aer == NULL or
+ * aer->tau_a == 0, and rt_solve_case_pol_aerosol (rt_solver.h:119-121)
+ * otherwise.  Host buffers in, host result out. */
+int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts,
+                       const ocrt_aerosol *aer, ocrt_result *out,
+                       ocrt_diag *diag);
+
+/* ---- batched solve -----------------------------------------------------
+ * n independent pixels in one device pass.  opts / aer are either one shared
+ * object (*_per_case = 0) or arrays of n (*_per_case = 1); aer may be NULL.
+ * Each pixel's result equals ocrt_gb_solve_case on the same inputs.  This is
+ * the GPU form of the reference's OpenMP row loop (rt_io.c:197-199).
+ * stream: a cudaStream_t passed as void* (NULL = the library's stream). */
+int ocrt_gb_solve_batch(int n, const ocrt_case *cases,
+                        const ocrt_opts *opts, int opts_per_case,
+                        const ocrt_aerosol *aer, int aer_per_case,
+                        ocrt_result *out, void *stream);
+
+/* ---- resident plans (inputs uploaded once, solved many times) -----------
+ * A plan holds the device copy of a batch.  ocrt_gb_plan_execute runs the
+ * full solve on device-resident inputs (no host traffic); results stay on the
+ * device until ocrt_gb_plan_results copies them out. */
+typedef struct ocrt_plan ocrt_plan;
+int  ocrt_gb_plan_create(int n, const ocrt_case *cases,
+                         const ocrt_opts *opts, int opts_per_case,
+                         const ocrt_aerosol *aer, int aer_per_case,
+                         ocrt_plan **plan);
+int  ocrt_gb_plan_execute(ocrt_plan *plan, void *stream);
+int  ocrt_gb_plan_results(ocrt_plan *plan, ocrt_result *out, void *stream);
+/* Device time of the last execute's kernels, and how many of this library's
+ * kernels it launched. */
+int  ocrt_gb_plan_stats(const ocrt_plan *plan, double *order_modes_total,
+                        long long *kernel_launches);
+void ocrt_gb_plan_destroy(ocrt_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCRT_GB300_H */

@@ -1,0 +1,139 @@
+"""ctypes mirror of include/ocrt_gb300.h.
+
+The structures below must stay field-for-field identical to the C header;
+tests/test_abi.py checks the sizes against the compiled library.
+"""
+import ctypes as C
+
+OCRT_OK = 0
+OCRT_ERR_ARGS = -1
+OCRT_ERR_NONFINITE = -2
+OCRT_ERR_ALLOC = -3
+OCRT_ERR_DEVICE = -4
+OCRT_ERR_UNSUPPORTED = -5
+OCRT_ERR_BOTTOM_SOURCE_SHAPE = -7
+
+SURFACE_BLACK = 0
+SURFACE_LAMBERT = 1
+SURFACE_BLACK_FRESNEL_OCEAN = 2
+SURFACE_FLAT = 3
+SURFACE_OCEAN = 4
+
+SURFACE_NAMES = {
+    "black": SURFACE_BLACK,
+    "lambert": SURFACE_LAMBERT,
+    "black_fresnel_ocean": SURFACE_BLACK_FRESNEL_OCEAN,
+    "coxmunk": SURFACE_BLACK_FRESNEL_OCEAN,
+    "flat": SURFACE_FLAT,
+    "ocean": SURFACE_OCEAN,
+}
+
+TAU_R_AUTO = 0
+TAU_R_FROM_INPUT = 1
+PROFILE_US62 = 0
+PROFILE_EXPONENTIAL = 1
+
+
+class Case(C.Structure):
+    _fields_ = [
+        ("sza_deg", C.c_double), ("vza_deg", C.c_double), ("raa_deg", C.c_double),
+        ("wavelength_nm", C.c_double), ("surface", C.c_int), ("pressure_hpa", C.c_double),
+        ("tau_r_input", C.c_double), ("n_water", C.c_double), ("wind_speed", C.c_double),
+        ("sigma_type", C.c_int), ("q_convention", C.c_int), ("decouple_sunglint", C.c_int),
+    ]
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("n_mu", C.c_int), ("n_layers", C.c_int), ("fourier_m_max", C.c_int),
+        ("max_orders", C.c_int), ("tolerance", C.c_double), ("tau_r_source", C.c_int),
+        ("pssa", C.c_int), ("view_as_node", C.c_int), ("aer_h_km", C.c_double),
+        ("rayleigh_profile", C.c_int), ("rayleigh_h_km", C.c_double),
+        ("n_phi_surface", C.c_int),
+    ]
+
+
+class Aerosol(C.Structure):
+    _fields_ = [
+        ("tau_a", C.c_double), ("ssa_a", C.c_double), ("L_max", C.c_int),
+        ("beta", C.POINTER(C.c_double)), ("gamma", C.POINTER(C.c_double)),
+        ("alpha", C.POINTER(C.c_double)), ("zeta", C.POINTER(C.c_double)),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("rho_I", C.c_double), ("rho_Q", C.c_double), ("rho_U", C.c_double),
+        ("I_TOA", C.c_double), ("Q_TOA", C.c_double), ("U_TOA", C.c_double),
+        ("tau_R_total", C.c_double), ("n_orders_used", C.c_int), ("converged", C.c_int),
+        ("order_modes", C.c_int), ("kappa_ipss", C.c_double),
+        ("T_dir_dn", C.c_double), ("T_diff_dn_hemi", C.c_double),
+        ("T_total_dn_hemi", C.c_double), ("T_diff_dn_dir", C.c_double),
+        ("T_total_up_dir", C.c_double), ("T_sg_up_dir", C.c_double),
+        ("T_dir_up_view", C.c_double),
+        ("rho_glint_direct_I", C.c_double), ("rho_glint_direct_Q", C.c_double),
+        ("rho_glint_direct_U", C.c_double),
+    ]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("orders_per_m", C.POINTER(C.c_int)), ("residual_per_m", C.POINTER(C.c_double)),
+        ("view_I_m", C.POINTER(C.c_double)), ("view_Q_m", C.POINTER(C.c_double)),
+        ("view_U_m", C.POINTER(C.c_double)),
+    ]
+
+
+RESULT_FIELDS = [f for f, _ in Result._fields_]
+
+
+def default_case(**kw):
+    """CLI defaults of the reference (main.c:1826-1840)."""
+    c = Case(sza_deg=40.0, vza_deg=30.0, raa_deg=90.0, wavelength_nm=555.0,
+             surface=SURFACE_BLACK, pressure_hpa=1013.25, tau_r_input=0.0, n_water=1.34,
+             wind_speed=0.0, sigma_type=1, q_convention=1, decouple_sunglint=0)
+    for k, v in kw.items():
+        if k == "surface" and isinstance(v, str):
+            v = SURFACE_NAMES[v]
+        setattr(c, k, v)
+    return c
+
+
+def default_opts(**kw):
+    """rt_options_default() (rt_types.h:760-795)."""
+    o = Opts(n_mu=24, n_layers=40, fourier_m_max=2, max_orders=20, tolerance=1e-7,
+             tau_r_source=TAU_R_AUTO, pssa=0, view_as_node=1, aer_h_km=2.0,
+             rayleigh_profile=PROFILE_US62, rayleigh_h_km=8.0, n_phi_surface=1024)
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class AerosolHolder:
+    """Keeps the moment arrays alive while an Aerosol struct points into them."""
+
+    def __init__(self, tau_a, ssa_a, beta, gamma, alpha, zeta):
+        import numpy as np
+        self.arrays = [np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+                       for a in (beta, gamma, alpha, zeta)]
+        L = len(self.arrays[0]) - 1
+        ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self.arrays]
+        self.struct = Aerosol(tau_a=float(tau_a), ssa_a=float(ssa_a), L_max=L,
+                              beta=ptrs[0], gamma=ptrs[1], alpha=ptrs[2], zeta=ptrs[3])
+
+    @property
+    def L_max(self):
+        return self.struct.L_max
+
+
+def result_dict(r):
+    return {f: getattr(r, f) for f in RESULT_FIELDS}
+
+
+def bind_solver(lib, prefix):
+    """Declare argtypes for <prefix>_solve_case / <prefix>_solve_batch."""
+    f = getattr(lib, prefix + "_solve_case")
+    f.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol), C.POINTER(Result),
+                  C.POINTER(Diag)]
+    f.restype = C.c_int
+    return f

@@ -1,0 +1,1411 @@
+/*
+ * ocrt_oracle.c — FP64 CPU restatement of the OCRT SOS solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the GB300
+ * library and the timed CPU "port" baseline; the product never links it.
+ * It is pinned against the reference C solver built from its own sources
+ * (oracle/Makefile -> oracle/_ref) and against the reference's published
+ * golden values (tests/golden/).
+ *
+ * Every routine restates one reference routine; the reference file:line is
+ * given beside it (paths relative to code/OCRT_C/src/).  The layout is this
+ * oracle's own: directions are kept in signed-ring arrays indexed j+n, fields
+ * as [level][signed direction], exactly the mathematical objects of the
+ * reference, not its packing.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdio.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/ocrt_gb300.h"
+
+#define PI 3.14159265358979323846
+#define DEPOL 0.0279                  /* rt_solver.c:646 */
+#define Z_TOP_KM 100.0                /* rt_atm.c:219, 306 */
+#define MAX_RING 130
+#define DEDUP_TOL 1.0e-12             /* rt_angle_grid.h:12 */
+
+/* ======================================================================
+ * Quadrature: Gauss-Legendre positive nodes, Newton from a Tricomi guess
+ * (rt_quadrature.c:20-61).  Nodes ascending, weights sum to 1.
+ * ==================================================================== */
+static void legendre_pair(int order, double t, double *p_n, double *p_nm1)
+{
+    double a = 1.0, b = t;
+    for (int k = 1; k < order; ++k) {
+        const double c = ((2.0 * k + 1.0) * t * b - (double)k * a) / (double)(k + 1);
+        a = b;
+        b = c;
+    }
+    *p_n = b;
+    *p_nm1 = a;
+}
+
+int ocrt_oracle_gauss(int n, double *mu, double *w)
+{
+    if (n < 1 || !mu || !w) return -1;
+    const int order = 2 * n;
+    for (int k = 1; k <= n; ++k) {
+        double t = cos(PI * ((double)k - 0.25) / ((double)order + 0.5));
+        double pn = 0.0, pm = 0.0, dp = 1.0;
+        int ok = 0;
+        for (int it = 0; it < 100; ++it) {
+            legendre_pair(order, t, &pn, &pm);
+            dp = (double)order * (t * pn - pm) / (t * t - 1.0);
+            const double step = -pn / dp;
+            t += step;
+            if (fabs(step) < 1.0e-15 * (fabs(t) + 1.0)) { ok = 1; break; }
+        }
+        if (!ok) return -2;
+        legendre_pair(order, t, &pn, &pm);
+        dp = (double)order * (t * pn - pm) / (t * t - 1.0);
+        mu[n - k] = t;
+        w[n - k] = 2.0 / ((1.0 - t * t) * dp * dp);
+    }
+    return 0;
+}
+
+/* Sorted insertion of a zero-weight node with de-duplication
+ * (rt_angle_grid.c:37-73).  Returns the ring index (0-based) of mu_new. */
+static int ring_insert(double *mu, double *w, int *n_total, double mu_new)
+{
+    int lo = 0, hi = *n_total;
+    while (lo < hi) {
+        const int mid = lo + (hi - lo) / 2;
+        if (mu[mid] < mu_new) lo = mid + 1; else hi = mid;
+    }
+    if (lo > 0 && fabs(mu[lo - 1] - mu_new) < DEDUP_TOL) return lo - 1;
+    if (lo < *n_total && fabs(mu[lo] - mu_new) < DEDUP_TOL) return lo;
+    for (int i = *n_total; i > lo; --i) { mu[i] = mu[i - 1]; w[i] = w[i - 1]; }
+    mu[lo] = mu_new;
+    w[lo] = 0.0;
+    *n_total += 1;
+    return lo;
+}
+
+/* ======================================================================
+ * Rayleigh optical depth, Bodhaine et al. 1999 (rt_rayleigh.c:46-52,
+ * 84-96, 137-146, 198-238): CO2 360 ppm, latitude 45 deg, sea level.
+ * ==================================================================== */
+static double gravity_wgs84(double lat_deg, double z_m)
+{
+    const double lat = lat_deg * PI / 180.0;
+    const double s1 = sin(lat) * sin(lat);
+    const double s2 = sin(2.0 * lat) * sin(2.0 * lat);
+    return 9.780327 * (1.0 + 0.0053024 * s1 - 0.0000058 * s2) - 3.086e-6 * z_m;
+}
+
+double ocrt_oracle_tau_rayleigh(double wl_nm, double p_hpa)
+{
+    const double co2 = 360.0;
+    const double um = wl_nm / 1000.0;
+    const double inv2 = 1.0 / (um * um);
+    const double fn2 = 1.034 + 3.17e-4 * inv2;
+    const double fo2 = 1.096 + 1.385e-3 * inv2 + 1.448e-4 * inv2 * inv2;
+    const double xc = co2 / 1.0e4;
+    const double king = (78.084 * fn2 + 20.946 * fo2 + 0.934 * 1.0 + xc * 1.15) /
+                        (78.084 + 20.946 + 0.934 + xc);
+    const double n300 = (8060.51 + 2480990.0 / (132.274 - inv2) +
+                         17455.7 / (39.32957 - inv2)) * 1.0e-8;
+    const double nm1 = n300 * (1.0 + 0.54 * (co2 * 1.0e-6 - 0.0003));
+    const double nn = (1.0 + nm1) * (1.0 + nm1);
+    const double avo = 6.0221367e23;
+    const double ns = (avo / 22.4141) * (273.15 / 288.15) * 1.0e-3;
+    const double wl_cm = wl_nm * 1.0e-7;
+    const double wl4 = wl_cm * wl_cm * wl_cm * wl_cm;
+    const double sigma = 24.0 * PI * PI * PI * (nn - 1.0) * (nn - 1.0) /
+                         (wl4 * ns * ns * (nn + 2.0) * (nn + 2.0)) * king;
+    const double ma = 15.0556 * (co2 * 1.0e-6) + 28.9595;
+    const double g = 100.0 * gravity_wgs84(45.0, 5517.56);
+    return sigma * (p_hpa * 1000.0) * avo / (ma * g);
+}
+
+/* ======================================================================
+ * Altitude mapping: US Standard Atmosphere 1962 column fractions
+ * (rt_molecular_profile.c:9-105) and the finite exponential aerosol profile
+ * (rt_atm.c:44-51).
+ * ==================================================================== */
+static const double US62_Z[8] = {0.0, 11.0, 20.0, 32.0, 47.0, 51.0, 71.0, 84.852};
+static const double US62_P[8] = {101325.0, 22632.1, 5474.89, 868.019,
+                                 110.906, 66.9389, 3.95642, 0.3734};
+
+static double us62_pressure(double z)
+{
+    if (z <= US62_Z[0]) return US62_P[0];
+    if (z >= US62_Z[7]) return US62_P[7];
+    int lo = 0, hi = 7;
+    while (hi - lo > 1) {
+        const int mid = lo + (hi - lo) / 2;
+        if (z < US62_Z[mid]) hi = mid; else lo = mid;
+    }
+    const double t = (z - US62_Z[lo]) / (US62_Z[hi] - US62_Z[lo]);
+    const double a = log(US62_P[lo]), b = log(US62_P[hi]);
+    return exp(a + t * (b - a));
+}
+
+static double clamp01(double x) { return x <= 0.0 ? 0.0 : (x >= 1.0 ? 1.0 : x); }
+
+static double us62_fraction_above_raw(double z)
+{
+    if (z <= 0.0) return 1.0;
+    const double g0 = gravity_wgs84(45.0, 0.0);
+    if (z >= US62_Z[7]) {
+        const double gt = gravity_wgs84(45.0, US62_Z[7] * 1000.0);
+        return clamp01((US62_P[7] / gt) / (US62_P[0] / g0));
+    }
+    const double gz = gravity_wgs84(45.0, z * 1000.0);
+    return clamp01((us62_pressure(z) / gz) / (US62_P[0] / g0));
+}
+
+static double us62_grid_fraction_above(double z)
+{
+    if (z <= 0.0) return 1.0;
+    if (z >= US62_Z[7]) return 0.0;
+    const double ft = us62_fraction_above_raw(US62_Z[7]);
+    return clamp01((us62_fraction_above_raw(z) - ft) / (1.0 - ft));
+}
+
+static double exp_fraction_above(double z, double z_top, double h)
+{
+    if (z <= 0.0) return 1.0;
+    if (z >= z_top) return 0.0;
+    const double et = exp(-z_top / h);
+    return (exp(-z / h) - et) / (1.0 - et);
+}
+
+/* Molecular column fraction above z for the selected profile. */
+static double ray_fraction_above(double z, int profile, double h_km)
+{
+    return profile == OCRT_PROFILE_EXPONENTIAL ? exp_fraction_above(z, Z_TOP_KM, h_km)
+                                               : us62_grid_fraction_above(z);
+}
+
+static double altitude_from_ray_fraction(double f, int profile, double h_km)
+{
+    const double ztop = profile == OCRT_PROFILE_EXPONENTIAL ? Z_TOP_KM : US62_Z[7];
+    if (f >= 1.0) return 0.0;
+    if (f <= 0.0) return ztop;
+    double lo = 0.0, hi = ztop;
+    for (int it = 0; it < 64; ++it) {       /* rt_molecular_profile.c:92-102 */
+        const double mid = 0.5 * (lo + hi);
+        if (ray_fraction_above(mid, profile, h_km) > f) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+/* ======================================================================
+ * Medium: uniform-tau levels with direct-beam attenuation and the aerosol /
+ * molecular scattering fractions per level (rt_atm.c:177-400).
+ * ==================================================================== */
+typedef struct {
+    int nt;
+    double tau_total;
+    double *h, *ch, *xdel, *ydel, *z;
+} medium_t;
+
+static void medium_free(medium_t *md)
+{
+    free(md->h); free(md->ch); free(md->xdel); free(md->ydel); free(md->z);
+    memset(md, 0, sizeof(*md));
+}
+
+static int medium_build(medium_t *md, int nt, double tau_r, double tau_a,
+                        double ssa_a, double mu0, double aer_h_km,
+                        int profile, double ray_h_km)
+{
+    memset(md, 0, sizeof(*md));
+    md->nt = nt;
+    md->h = calloc(nt + 1, sizeof(double));
+    md->ch = calloc(nt + 1, sizeof(double));
+    md->xdel = calloc(nt + 1, sizeof(double));
+    md->ydel = calloc(nt + 1, sizeof(double));
+    md->z = calloc(nt + 1, sizeof(double));
+    if (!md->h || !md->ch || !md->xdel || !md->ydel || !md->z) { medium_free(md); return -3; }
+    const double tau = tau_r + tau_a;
+    md->tau_total = tau;
+    for (int k = 0; k <= nt; ++k) {
+        md->h[k] = (double)k * tau / (double)nt;
+        md->ch[k] = 0.5 * exp(-md->h[k] / mu0);
+        md->xdel[k] = 0.0;
+        md->ydel[k] = 1.0;
+        md->z[k] = k == 0 ? Z_TOP_KM
+                          : altitude_from_ray_fraction(md->h[k] / tau, profile, ray_h_km);
+    }
+    if (tau_a <= 0.0) return 0;
+
+    /* Aerosol + Rayleigh: altitude of every level by bisection on the mixed
+     * column above, then per-layer scattering fractions (rt_atm.c:313-383). */
+    const double ah = aer_h_km > 0.0 ? aer_h_km : 2.0;
+    if (tau_r == 0.0) { md->xdel[0] = ssa_a; md->ydel[0] = 0.0; }
+    else { md->xdel[0] = 0.0; md->ydel[0] = 1.0; }
+    double z_prev = Z_TOP_KM, ray_prev = 0.0, aer_prev = 0.0;
+    md->z[0] = Z_TOP_KM;
+    for (int j = 1; j <= nt; ++j) {
+        double zj = 0.0;
+        if (j < nt) {
+            double lo = 0.0, hi = z_prev;
+            for (int it = 0; it < 64; ++it) {
+                const double mid = 0.5 * (lo + hi);
+                const double above = tau_r * ray_fraction_above(mid, profile, ray_h_km) +
+                                     tau_a * exp_fraction_above(mid, Z_TOP_KM, ah);
+                if (above > md->h[j]) lo = mid; else hi = mid;
+            }
+            zj = 0.5 * (lo + hi);
+        }
+        md->z[j] = zj;
+        const double ray_j = tau_r * ray_fraction_above(zj, profile, ray_h_km);
+        const double aer_j = tau_a * exp_fraction_above(zj, Z_TOP_KM, ah);
+        const double dr = ray_j - ray_prev, da = aer_j - aer_prev, dt = dr + da;
+        if (dt > 0.0) { md->xdel[j] = da * ssa_a / dt; md->ydel[j] = dr / dt; }
+        else { md->xdel[j] = 0.0; md->ydel[j] = tau_r > 0.0 ? 1.0 : 0.0; }
+        z_prev = zj; ray_prev = ray_j; aer_prev = aer_j;
+    }
+    return 0;
+}
+
+/* ======================================================================
+ * Angular basis: normalised associated Legendre P_l^m and the spin-2 pair
+ * R_l^m, T_l^m by three-term recurrence (rt_angular_basis.c:19-124).
+ * Arrays are [l] for one direction cosine.
+ * ==================================================================== */
+static double diag_norm(int m)
+{
+    double v = 1.0;
+    for (int i = 1; i <= m; ++i) v *= sqrt((double)(i + m) / (double)i) * 0.5;
+    return v;
+}
+
+static void basis_scalar(int L, int m, double x, double *p)
+{
+    for (int l = 0; l <= L; ++l) p[l] = 0.0;
+    if (m == 0) { p[0] = 1.0; p[1] = x; p[2] = 0.5 * (3.0 * x * x - 1.0); }
+    else if (m == 1) { p[1] = sqrt(0.5 * (1.0 - x * x)); p[2] = x * p[1] * sqrt(3.0); }
+    else { p[m - 1] = 0.0; p[m] = diag_norm(m) * pow(1.0 - x * x, 0.5 * (double)m); }
+    const int l0 = m < 2 ? 2 : m;
+    for (int l = l0; l < L; ++l) {
+        const double f = (2.0 * l + 1.0) / sqrt((double)(l + m + 1) * (double)(l - m + 1));
+        const double b = sqrt((double)(l + m) * (double)(l - m)) / (2.0 * l + 1.0);
+        p[l + 1] = f * (x * p[l] - b * p[l - 1]);
+    }
+}
+
+static void basis_spin2(int L, int m, double x, double *r, double *t)
+{
+    for (int l = 0; l <= L; ++l) { r[l] = 0.0; t[l] = 0.0; }
+    if (m == 0) {
+        r[2] = 3.0 * (1.0 - x * x) / (2.0 * sqrt(6.0));
+    } else if (m == 1) {
+        const double s = sqrt(1.0 - x * x);
+        r[2] = -x * s * 0.5;
+        t[2] = -s * 0.5;
+    } else {
+        const double sn = diag_norm(m) * sqrt((double)m / (double)(m + 1)) *
+                          sqrt((double)(m - 1) / (double)(m + 2));
+        const double env = pow(1.0 - x * x, 0.5 * (double)m - 1.0);
+        r[m] = sn * (1.0 + x * x) * env;
+        t[m] = sn * 2.0 * x * env;
+    }
+    const int l0 = m < 2 ? 2 : m;
+    for (int l = l0; l < L; ++l) {
+        const double sc = (double)(l + 1) * (double)(2 * l + 1) /
+            sqrt((double)(l + 3) * (double)(l - 1) * (double)(l + m + 1) * (double)(l - m + 1));
+        const double dc = sqrt((double)(l + 2) * (double)(l - 2) * (double)(l + m) * (double)(l - m)) /
+                          ((double)l * (double)(2 * l + 1));
+        const double cc = 2.0 * (double)m / ((double)l * (double)(l + 1));
+        r[l + 1] = sc * (x * r[l] - cc * t[l] - dc * r[l - 1]);
+        t[l + 1] = sc * (x * t[l] - cc * r[l] - dc * t[l - 1]);
+    }
+}
+
+/* ======================================================================
+ * Per-mode angular state: the six particle phase tables over
+ * (row j in 0..n) x (column k in -n..n) (rt_angular_basis.c:278-357) and the
+ * molecular l=2 basis values xpl/xrl/xtl (rt_angular_basis.c:366-396).
+ * Row 0 / column 0 is the solar slot mu = -mu0.
+ * ==================================================================== */
+typedef struct {
+    int n, L, m;
+    double *P, *R, *T;              /* [(L+1)][2n+1] basis at the signed ring */
+    double *pfm, *gr, *gt, *arr, *art, *att;   /* [(n+1)][2n+1] */
+    double *xpl, *xrl, *xtl;        /* [2n+1] */
+} mode_t_;
+
+#define RIDX(n, j) ((j) + (n))
+#define TAB(tab, n, j, k) ((tab)[(size_t)(j) * (size_t)(2 * (n) + 1) + (size_t)((k) + (n))])
+
+static void mode_free(mode_t_ *md)
+{
+    free(md->P); free(md->R); free(md->T);
+    free(md->pfm); free(md->gr); free(md->gt); free(md->arr); free(md->art); free(md->att);
+    free(md->xpl); free(md->xrl); free(md->xtl);
+    memset(md, 0, sizeof(*md));
+}
+
+static int mode_alloc(mode_t_ *md, int n, int L)
+{
+    memset(md, 0, sizeof(*md));
+    md->n = n; md->L = L;
+    const size_t nd = (size_t)(2 * n + 1);
+    const size_t nb = (size_t)(L + 1) * nd, nk = (size_t)(n + 1) * nd;
+    md->P = calloc(nb, sizeof(double)); md->R = calloc(nb, sizeof(double));
+    md->T = calloc(nb, sizeof(double));
+    md->pfm = calloc(nk, sizeof(double)); md->gr = calloc(nk, sizeof(double));
+    md->gt = calloc(nk, sizeof(double)); md->arr = calloc(nk, sizeof(double));
+    md->art = calloc(nk, sizeof(double)); md->att = calloc(nk, sizeof(double));
+    md->xpl = calloc(nd, sizeof(double)); md->xrl = calloc(nd, sizeof(double));
+    md->xtl = calloc(nd, sizeof(double));
+    if (!md->P || !md->R || !md->T || !md->pfm || !md->gr || !md->gt || !md->arr ||
+        !md->art || !md->att || !md->xpl || !md->xrl || !md->xtl) { mode_free(md); return -3; }
+    return 0;
+}
+
+/* rm: signed ring [2n+1] (index j+n), moments may be NULL (pure Rayleigh). */
+static void mode_build(mode_t_ *md, int m, const double *rm,
+                       const ocrt_aerosol *aer)
+{
+    const int n = md->n, L = md->L, nd = 2 * n + 1;
+    md->m = m;
+    double *bp = malloc(sizeof(double) * 3 * (L + 1));
+    double *br = bp + (L + 1), *bt = br + (L + 1);
+    for (int j = -n; j <= n; ++j) {
+        basis_scalar(L, m, rm[RIDX(n, j)], bp);
+        basis_spin2(L, m, rm[RIDX(n, j)], br, bt);
+        for (int l = 0; l <= L; ++l) {
+            md->P[(size_t)l * nd + RIDX(n, j)] = bp[l];
+            md->R[(size_t)l * nd + RIDX(n, j)] = br[l];
+            md->T[(size_t)l * nd + RIDX(n, j)] = bt[l];
+        }
+        md->xpl[RIDX(n, j)] = bp[2];
+        md->xrl[RIDX(n, j)] = br[2];
+        md->xtl[RIDX(n, j)] = bt[2];
+    }
+    free(bp);
+    const size_t nk = (size_t)(n + 1) * nd;
+    memset(md->pfm, 0, nk * sizeof(double)); memset(md->gr, 0, nk * sizeof(double));
+    memset(md->gt, 0, nk * sizeof(double)); memset(md->arr, 0, nk * sizeof(double));
+    memset(md->art, 0, nk * sizeof(double)); memset(md->att, 0, nk * sizeof(double));
+    if (!aer) return;
+    const int La = aer->L_max;
+    for (int j = 0; j <= n; ++j) {
+        for (int k = -n; k <= n; ++k) {
+            double s_p = 0, s_r = 0, s_t = 0, s_rr = 0, s_rt = 0, s_tt = 0;
+            for (int l = m; l <= L; ++l) {
+                const double be = l <= La ? aer->beta[l] : 0.0;
+                const double ga = l <= La ? aer->gamma[l] : 0.0;
+                const double al = l <= La ? aer->alpha[l] : 0.0;
+                const double ze = l <= La ? aer->zeta[l] : 0.0;
+                const double pj = md->P[(size_t)l * nd + RIDX(n, j)], pk = md->P[(size_t)l * nd + RIDX(n, k)];
+                const double rj = md->R[(size_t)l * nd + RIDX(n, j)], rk = md->R[(size_t)l * nd + RIDX(n, k)];
+                const double tj = md->T[(size_t)l * nd + RIDX(n, j)], tk = md->T[(size_t)l * nd + RIDX(n, k)];
+                s_p += pj * pk * be;
+                s_r += pj * rk * ga;
+                s_t += pj * tk * ga;
+                s_tt += tj * tk * al + rj * rk * ze;
+                s_rr += tj * tk * ze + rj * rk * al;
+                s_rt += tj * rk * al + rj * tk * ze;
+            }
+            TAB(md->pfm, n, j, k) = s_p; TAB(md->gr, n, j, k) = s_r; TAB(md->gt, n, j, k) = s_t;
+            TAB(md->arr, n, j, k) = s_rr; TAB(md->art, n, j, k) = s_rt; TAB(md->att, n, j, k) = s_tt;
+        }
+    }
+}
+
+/* ======================================================================
+ * Solve context for one pixel.
+ * ==================================================================== */
+typedef struct {
+    int n;                 /* ring size (positive directions) */
+    int view_idx;          /* 1-based ring index of mu_view, 0 if interpolated */
+    double mu0, mu_view;
+    double rm[2 * MAX_RING + 1], gb[2 * MAX_RING + 1];
+    double beta0, beta2, gamma2, alpha2;
+    medium_t md;
+    double *Tr;            /* [2n+1][nt] layer transmission */
+    double *Ca, *Cb;       /* [2n+1][nt] linear-source weights on J_out, J_in */
+} ctx_t;
+
+#define F(buf, c, k, j) ((buf)[(size_t)(k) * (size_t)(2 * (c)->n + 1) + (size_t)((j) + (c)->n)])
+
+/* Transport coefficients of the linear-in-tau formal solution
+ * (rt_layer_transport.c:36-99, 107-208), regrouped as
+ *   I_k = T I_up + Ca J_k + Cb J_up,
+ *   G = (1-T)|mu|/dtau - T,  Ca = (1-T-G)/2,  Cb = G/2,
+ * which is the reference's slope/intercept expression expanded. */
+static int transport_prepare(ctx_t *c)
+{
+    const int n = c->n, nt = c->md.nt, nd = 2 * n + 1;
+    c->Tr = malloc(sizeof(double) * (size_t)nd * nt);
+    c->Ca = malloc(sizeof(double) * (size_t)nd * nt);
+    c->Cb = malloc(sizeof(double) * (size_t)nd * nt);
+    if (!c->Tr || !c->Ca || !c->Cb) return -3;
+    for (int j = -n; j <= n; ++j) {
+        for (int l = 0; l < nt; ++l) {
+            const size_t i = (size_t)RIDX(n, j) * nt + l;
+            if (j == 0) { c->Tr[i] = c->Ca[i] = c->Cb[i] = 0.0; continue; }
+            const double am = fabs(c->rm[RIDX(n, j)]);
+            const double dtau = c->md.h[l + 1] - c->md.h[l];
+            const double T = exp(-dtau / am);
+            const double G = (1.0 - T) * am / dtau - T;
+            c->Tr[i] = T;
+            c->Ca[i] = 0.5 * (1.0 - T - G);
+            c->Cb[i] = 0.5 * G;
+        }
+    }
+    return 0;
+}
+
+/* Up sweep from the surface BC, down sweep from a zero top BC. */
+static int transport(const ctx_t *c, const double *J, const double *bc, double *I)
+{
+    const int n = c->n, nt = c->md.nt;
+    for (int k = 0; k <= nt; ++k) F(I, c, k, 0) = NAN;
+    for (int j = -n; j <= n; ++j) {
+        if (j == 0) continue;
+        const double *T = c->Tr + (size_t)RIDX(n, j) * nt;
+        const double *A = c->Ca + (size_t)RIDX(n, j) * nt;
+        const double *B = c->Cb + (size_t)RIDX(n, j) * nt;
+        if (j > 0) {
+            double run = bc ? bc[j - 1] : 0.0;
+            F(I, c, nt, j) = run;
+            for (int k = nt - 1; k >= 0; --k) {
+                const double jo = F(J, c, k, j), ji = F(J, c, k + 1, j);
+                if (!isfinite(jo) || !isfinite(ji)) return -2;
+                run = T[k] * run + A[k] * jo + B[k] * ji;
+                F(I, c, k, j) = run;
+            }
+        } else {
+            double run = 0.0;
+            F(I, c, 0, j) = run;
+            for (int k = 1; k <= nt; ++k) {
+                const double jo = F(J, c, k, j), ji = F(J, c, k - 1, j);
+                if (!isfinite(jo) || !isfinite(ji)) return -2;
+                run = T[k - 1] * run + A[k - 1] * jo + B[k - 1] * ji;
+                F(I, c, k, j) = run;
+            }
+        }
+    }
+    return 0;
+}
+
+/* Direct-beam primary source (rt_primary_source.c:17-198; beam_q = 0). */
+static void primary_source(const ctx_t *c, const mode_t_ *md, double *JI, double *JQ, double *JU)
+{
+    const int n = c->n, nt = c->md.nt, m = md->m;
+    const int mol = m <= 2;
+    const double b0 = m == 0 ? c->beta0 : 0.0;
+    const double p0 = md->xpl[RIDX(n, 0)];
+    for (int k = 0; k <= nt; ++k) {
+        const double beam = c->md.ch[k], x = c->md.xdel[k], y = c->md.ydel[k];
+        for (int j = -n; j <= n; ++j) {
+            const double pj = md->xpl[RIDX(n, j)];
+            const double mi = b0 + c->beta2 * pj * p0;
+            const double mq = mol ? c->gamma2 * md->xrl[RIDX(n, j)] * p0 : 0.0;
+            const double mu = mol ? c->gamma2 * md->xtl[RIDX(n, j)] * p0 : 0.0;
+            F(JI, c, k, j) = beam * (x * TAB(md->pfm, n, 0, j) + y * mi);
+            F(JQ, c, k, j) = beam * (x * TAB(md->gr, n, 0, j) + y * mq);
+            F(JU, c, k, j) = -beam * (x * TAB(md->gt, n, 0, j) + y * mu);
+        }
+        F(JI, c, k, 0) = F(JQ, c, k, 0) = F(JU, c, k, 0) = NAN;
+    }
+}
+
+/* Multiple-scattering source: the vector contraction of
+ * rt_sos_operator.c:206-424 written directly on the phase tables. */
+static int ms_source(const ctx_t *c, const mode_t_ *md,
+                     const double *I, const double *Q, const double *U,
+                     double *JI, double *JQ, double *JU)
+{
+    const int n = c->n, nt = c->md.nt, m = md->m;
+    const int mol = m <= 2;
+    const double b0 = m == 0 ? c->beta0 : 0.0, b2 = c->beta2, g2 = c->gamma2, a2 = c->alpha2;
+    const double *xp = md->xpl + n, *xr = md->xrl + n, *xt = md->xtl + n;
+    for (int k = 0; k <= nt; ++k)
+        for (int j = -n; j <= n; ++j)
+            if (j != 0 && (!isfinite(F(I, c, k, j)) || !isfinite(F(Q, c, k, j)) ||
+                           !isfinite(F(U, c, k, j)))) return -2;
+    for (int k = 0; k <= nt; ++k) {
+        const double x = c->md.xdel[k], y = c->md.ydel[k];
+        for (int o = 1; o <= n; ++o) {
+            double Iu = 0, Id = 0, Qu = 0, Qd = 0, Uu = 0, Ud = 0;
+            for (int i = 1; i <= n; ++i) {
+                const double w = c->gb[RIDX(n, i)];
+                if (w == 0.0) continue;
+                /* aerosol tables + molecular l=2 (and l=0 at m=0) terms */
+                const double ii_s = x * TAB(md->pfm, n, i, o) + y * (mol ? b0 + b2 * xp[i] * xp[o] : 0.0);
+                const double ii_c = x * TAB(md->pfm, n, i, -o) + y * (mol ? b0 + b2 * xp[i] * xp[-o] : 0.0);
+                const double iu_s = x * TAB(md->gt, n, i, o) + y * (mol ? g2 * xp[i] * xt[o] : 0.0);
+                const double iu_c = x * TAB(md->gt, n, i, -o) + y * (mol ? g2 * xp[i] * xt[-o] : 0.0);
+                const double iuT_s = x * TAB(md->gt, n, o, i) + y * (mol ? g2 * xp[o] * xt[i] : 0.0);
+                const double iuT_c = x * TAB(md->gt, n, o, -i) + y * (mol ? g2 * xp[o] * xt[-i] : 0.0);
+                const double iq_s = x * TAB(md->gr, n, i, o) + y * (mol ? g2 * xp[i] * xr[o] : 0.0);
+                const double iq_c = x * TAB(md->gr, n, i, -o) + y * (mol ? g2 * xp[i] * xr[-o] : 0.0);
+                const double iqT_s = x * TAB(md->gr, n, o, i) + y * (mol ? g2 * xp[o] * xr[i] : 0.0);
+                const double iqT_c = x * TAB(md->gr, n, o, -i) + y * (mol ? g2 * xp[o] * xr[-i] : 0.0);
+                const double qq_s = x * TAB(md->arr, n, i, o) + y * (mol ? a2 * xr[i] * xr[o] : 0.0);
+                const double qq_c = x * TAB(md->arr, n, i, -o) + y * (mol ? a2 * xr[i] * xr[-o] : 0.0);
+                const double qu_s = x * TAB(md->art, n, i, o) + y * (mol ? a2 * xt[i] * xr[o] : 0.0);
+                const double qu_c = x * TAB(md->art, n, i, -o) + y * (mol ? a2 * xt[i] * xr[-o] : 0.0);
+                const double quT_s = x * TAB(md->art, n, o, i) + y * (mol ? a2 * xt[o] * xr[i] : 0.0);
+                const double quT_c = x * TAB(md->art, n, o, -i) + y * (mol ? a2 * xt[o] * xr[-i] : 0.0);
+                const double uu_s = x * TAB(md->att, n, i, o) + y * (mol ? a2 * xt[i] * xt[o] : 0.0);
+                const double uu_c = x * TAB(md->att, n, i, -o) + y * (mol ? a2 * xt[i] * xt[-o] : 0.0);
+                const double iu = F(I, c, k, i), id = F(I, c, k, -i);
+                const double qu = F(Q, c, k, i), qd = F(Q, c, k, -i);
+                const double uu = F(U, c, k, i), ud = F(U, c, k, -i);
+                Iu += w * (iu * ii_s + qu * iqT_s - uu * iuT_s + id * ii_c + qd * iqT_c - ud * iuT_c);
+                Id += w * (iu * ii_c + qu * iqT_c + uu * iuT_c + id * ii_s + qd * iqT_s + ud * iuT_s);
+                Qu += w * (iu * iq_s + qu * qq_s - uu * qu_s + id * iq_c + qd * qq_c + ud * qu_c);
+                Qd += w * (iu * iq_c + qu * qq_c - uu * qu_c + id * iq_s + qd * qq_s + ud * qu_s);
+                Uu -= w * (iu * iu_s + qu * quT_s - uu * uu_s - id * iu_c + qd * quT_c - ud * uu_c);
+                Ud -= w * (iu * iu_c - qu * quT_c - uu * uu_c - id * iu_s - qd * quT_s - ud * uu_s);
+            }
+            F(JI, c, k, o) = Iu; F(JI, c, k, -o) = Id;
+            F(JQ, c, k, o) = Qu; F(JQ, c, k, -o) = Qd;
+            F(JU, c, k, o) = Uu; F(JU, c, k, -o) = Ud;
+        }
+        F(JI, c, k, 0) = F(JQ, c, k, 0) = F(JU, c, k, 0) = NAN;
+    }
+    return 0;
+}
+
+/* ======================================================================
+ * Surface: Fresnel core and Cox-Munk Mueller BRDF (shared/surface.c:57-64,
+ * 385-455, 514-619), rotations (shared/mat3.h:45-55).
+ * ==================================================================== */
+static double slope_variance(double ws, int sigma_type)
+{
+    if (sigma_type == 1) return 0.003 + 0.00512 * fmax(0.01, ws);
+    const double s = 0.0731 * sqrt(fmax(0.0, ws));
+    return fmax(s * s, 1e-10);
+}
+
+static void fresnel_R(double mu_i, double nw, int qconv, double *M)
+{
+    for (int i = 0; i < 9; ++i) M[i] = 0.0;
+    const double st2 = (1.0 / nw) * (1.0 / nw) * fmax(0.0, 1.0 - mu_i * mu_i);
+    if (st2 >= 1.0) { M[0] = M[4] = M[8] = 1.0; return; }
+    const double mt = sqrt(1.0 - st2);
+    const double rs = (mu_i - nw * mt) / (mu_i + nw * mt);
+    const double rp = (nw * mu_i - mt) / (nw * mu_i + mt);
+    const double Rs = rs * rs, Rp = rp * rp;
+    const double q = qconv == 1 ? 0.5 * (Rp - Rs) : 0.5 * (Rs - Rp);
+    M[0] = 0.5 * (Rs + Rp); M[1] = q; M[3] = q; M[4] = 0.5 * (Rs + Rp); M[8] = rs * rp;
+}
+
+static void rot_L(double c, double s, double *L)
+{
+    const double c2 = c * c - s * s, s2 = 2.0 * c * s;
+    for (int i = 0; i < 9; ++i) L[i] = 0.0;
+    L[0] = 1.0; L[4] = c2; L[5] = -s2; L[7] = s2; L[8] = c2;
+}
+
+static void mul3(const double *A, const double *B, double *C)
+{
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 3; ++k) s += A[i * 3 + k] * B[k * 3 + j];
+            C[i * 3 + j] = s;
+        }
+}
+
+void ocrt_oracle_coxmunk_R(double mu_out, double mu_in_dn, double cphi, double sphi,
+                           double ws, int sigma_type, double nw, int qconv, double *R)
+{
+    for (int i = 0; i < 9; ++i) R[i] = 0.0;
+    const double s2v = slope_variance(ws, sigma_type);
+    const double mi = -mu_in_dn;
+    const double s1 = sqrt(fmax(0.0, 1.0 - mu_out * mu_out));
+    const double s2 = sqrt(fmax(0.0, 1.0 - mi * mi));
+    double cT = mu_out * mi + s1 * s2 * cphi;
+    cT = cT > 1.0 ? 1.0 : (cT < -1.0 ? -1.0 : cT);
+    const double cw = sqrt(fmax(0.0, 0.5 * (1.0 - cT)));
+    if (cw <= 1e-6) return;
+    const double cb = (mu_out + mu_in_dn) / (2.0 * cw);
+    if (cb <= 1e-6) return;
+    const double sT = sqrt(fmax(0.0, 1.0 - cT * cT));
+    const double den = fmax(1e-12, sT);
+    const double pole = 1.0e-8;        /* surface.c:57 pole limit */
+    double c1, si1, c2, si2;
+    if (s2 <= pole) { c1 = -copysign(1.0, mi) * cphi; si1 = sphi; }
+    else {
+        c1 = (mu_out - mi * cT) / (den * fmax(1e-12, s2));
+        si1 = s1 * sphi / den;
+        const double nn = sqrt(c1 * c1 + si1 * si1);
+        if (nn < 1e-12) { c1 = 1.0; si1 = 0.0; } else { c1 /= nn; si1 /= nn; }
+    }
+    if (s1 <= pole) { c2 = -copysign(1.0, mu_out) * cphi; si2 = sphi; }
+    else {
+        c2 = (mi - mu_out * cT) / (den * fmax(1e-12, s1));
+        si2 = s2 * sphi / den;
+        const double nn = sqrt(c2 * c2 + si2 * si2);
+        if (nn < 1e-12) { c2 = 1.0; si2 = 0.0; } else { c2 /= nn; si2 /= nn; }
+    }
+    double MF[9];
+    fresnel_R(cw, nw, qconv, MF);
+    const double cb2 = cb * cb;
+    const double tb2 = (1.0 - cb2) / fmax(cb2, 1e-8);
+    const double Pslope = (1.0 / (PI * s2v)) * exp(-tb2 / s2v);
+    const double sl = sqrt(s2v);
+    double li = 0.0, lv = 0.0;
+    if (mu_in_dn < 1.0 - 1e-10) {
+        const double si = sqrt(fmax(1e-20, 1.0 - mu_in_dn * mu_in_dn));
+        const double nu = (mu_in_dn / si) / sl;
+        if (nu <= 20.0) li = 0.5 * (exp(-nu * nu) / (nu * sqrt(PI)) - erfc(nu));
+    }
+    if (mu_out < 1.0 - 1e-10) {
+        const double sv = sqrt(fmax(1e-20, 1.0 - mu_out * mu_out));
+        const double nu = (mu_out / sv) / sl;
+        if (nu <= 20.0) lv = 0.5 * (exp(-nu * nu) / (nu * sqrt(PI)) - erfc(nu));
+    }
+    const double S = 1.0 / (1.0 + li + lv);
+    const double brdf = (Pslope * S) / (4.0 * mu_in_dn * mu_out * cb2 * cb2);
+    double L1[9], L2[9], A[9], B[9];
+    rot_L(c1, si1, L1);
+    rot_L(c2, si2, L2);
+    mul3(MF, L1, A);
+    mul3(L2, A, B);
+    for (int i = 0; i < 9; ++i) R[i] = B[i] * brdf;
+}
+
+/* Azimuthal Fourier projection of the Cox-Munk Mueller kernel for all modes
+ * 0..M at once (shared/surface.c:839-909; the all-mode build of
+ * surface.c:1005-1057).  out[m][o][i][9]. */
+static void coxmunk_fourier_allm(const double *mu_o, int no, const double *mu_i, int ni,
+                                 int M, int nphi, double ws, int st, double nw, int qc,
+                                 double *out)
+{
+    static const int cos_entry[9] = {1, 1, 0, 1, 1, 0, 0, 0, 1};
+    const double dphi = 2.0 * PI / (double)nphi;
+    double *cm = malloc(sizeof(double) * (size_t)nphi * (M + 1) * 2);
+    double *sm = cm + (size_t)nphi * (M + 1);
+    for (int p = 0; p < nphi; ++p) {
+        const double phi = (p + 0.5) * dphi;
+        for (int m = 0; m <= M; ++m) {
+            cm[(size_t)p * (M + 1) + m] = cos(m * phi);
+            sm[(size_t)p * (M + 1) + m] = sin(m * phi);
+        }
+    }
+    const size_t slab = (size_t)no * ni * 9;
+    memset(out, 0, sizeof(double) * slab * (M + 1));
+    for (int o = 0; o < no; ++o)
+        for (int i = 0; i < ni; ++i) {
+            for (int p = 0; p < nphi; ++p) {
+                const double phi = (p + 0.5) * dphi;
+                double R[9];
+                ocrt_oracle_coxmunk_R(mu_o[o], mu_i[i], cos(phi), sin(phi), ws, st, nw, qc, R);
+                for (int m = 0; m <= M; ++m) {
+                    double *dst = out + (size_t)m * slab + ((size_t)o * ni + i) * 9;
+                    const double cw = cm[(size_t)p * (M + 1) + m], sw = sm[(size_t)p * (M + 1) + m];
+                    for (int e = 0; e < 9; ++e) dst[e] += R[e] * (cos_entry[e] ? cw : sw);
+                }
+            }
+            for (int m = 0; m <= M; ++m) {
+                const double norm = m == 0 ? 1.0 / (2.0 * PI) : 1.0 / PI;
+                double *dst = out + (size_t)m * slab + ((size_t)o * ni + i) * 9;
+                for (int e = 0; e < 9; ++e) dst[e] *= dphi * norm;
+                if (m > 0) { dst[2] = -dst[2]; dst[5] = -dst[5]; }
+            }
+        }
+    free(cm);
+}
+
+/* Direct sunglint reflectance (shared/surface.c:1813-1907). */
+static void sunglint_rho(double mu_v, double phi_v, double mu0, double ws, int st,
+                         double nw, double tau, int qc, double *g)
+{
+    const double dphi = phi_v;
+    const double trans = exp(-tau / mu0) * exp(-tau / mu_v);
+    if (ws < 1e-6) {
+        const double fov = 0.5 * PI / 180.0;
+        const double s0 = sqrt(fmax(0.0, 1.0 - mu0 * mu0));
+        const double smu = fov * fmax(s0, 1e-3), sph = fov;
+        double de = dphi;
+        while (de > PI) de -= 2.0 * PI;
+        while (de < -PI) de += 2.0 * PI;
+        const double dm = mu_v - mu0;
+        const double ex = -0.5 * (dm * dm / (smu * smu) + de * de / (sph * sph));
+        if (ex < -50.0) { g[0] = g[1] = g[2] = 0.0; return; }
+        double MF[9];
+        fresnel_R(mu0, nw, qc, MF);
+        const double den = fmax(2.0 * mu0 * s0 * mu0 * mu_v, 1e-12);
+        const double r = 4.0 * PI * trans / den * exp(ex);
+        g[0] = MF[0] * r; g[1] = MF[3] * r; g[2] = MF[6] * r;
+        return;
+    }
+    double R[9];
+    ocrt_oracle_coxmunk_R(mu_v, mu0, cos(dphi), sin(dphi), ws, st, nw, qc, R);
+    g[0] = PI * R[0] * trans; g[1] = PI * R[3] * trans; g[2] = PI * R[6] * trans;
+}
+
+/* ======================================================================
+ * IPSS spherical single-scatter correction (rt_ipss.c:24-644), surface
+ * anchor, phase-weighted source when aerosol scatters.
+ * ==================================================================== */
+typedef struct {
+    int nl;
+    double Re, H, mu0, depol;
+    double *he, *beta, *wsrc, *wray, *waer, *above;
+    double *seg, *ts, *lt, *ltau;
+    int *llay, ln;
+    const ocrt_aerosol *aer;
+} ipss_t;
+
+static void ipss_free(ipss_t *g)
+{
+    free(g->he); free(g->beta); free(g->wsrc); free(g->wray); free(g->waer); free(g->above);
+    free(g->seg); free(g->ts); free(g->lt); free(g->ltau); free(g->llay);
+    memset(g, 0, sizeof(*g));
+}
+
+static int ipss_init(ipss_t *g, const medium_t *md, double mu0, const ocrt_aerosol *aer)
+{
+    memset(g, 0, sizeof(*g));
+    const int nt = md->nt;
+    g->nl = nt; g->Re = 6371.0; g->mu0 = mu0; g->depol = DEPOL;
+    g->he = malloc(sizeof(double) * (nt + 1));
+    g->beta = malloc(sizeof(double) * nt);
+    g->wsrc = malloc(sizeof(double) * nt);
+    g->wray = malloc(sizeof(double) * nt);
+    g->waer = malloc(sizeof(double) * nt);
+    g->above = malloc(sizeof(double) * (nt + 1));
+    g->seg = malloc(sizeof(double) * nt);
+    g->ts = malloc(sizeof(double) * (2 * nt + 8));
+    g->lt = malloc(sizeof(double) * (2 * nt + 8));
+    g->ltau = malloc(sizeof(double) * (2 * nt + 8));
+    g->llay = malloc(sizeof(int) * (2 * nt + 8));
+    for (int k = 0; k <= nt; ++k) g->he[k] = md->z[nt - k];
+    g->H = g->he[nt];
+    int have_aer = 0;
+    for (int j = 0; j < nt; ++j) {
+        const int k = nt - 1 - j;
+        const double dz = g->he[j + 1] - g->he[j];
+        const double dtau = md->h[k + 1] - md->h[k];
+        if (!(dz > 0.0)) return -2;
+        g->beta[j] = dtau > 0.0 ? dtau / dz : 0.0;
+        g->wray[j] = md->ydel[k + 1] > 0.0 ? md->ydel[k + 1] : 0.0;
+        g->waer[j] = md->xdel[k + 1] > 0.0 ? md->xdel[k + 1] : 0.0;
+        if (md->xdel[k + 1] > 0.0) have_aer = 1;
+        g->wsrc[j] = 1.0;                  /* phase-free omega (no gas absorption) */
+    }
+    g->aer = (have_aer && aer) ? aer : NULL;
+    g->above[nt] = 0.0;
+    for (int j = nt - 1; j >= 0; --j) g->above[j] = g->above[j + 1] + g->beta[j] * (g->he[j + 1] - g->he[j]);
+    return 0;
+}
+
+static int ipss_layer_of(const ipss_t *g, double h)
+{
+    if (h <= g->he[0]) return 0;
+    if (h >= g->he[g->nl]) return g->nl - 1;
+    int lo = 0, hi = g->nl;
+    while (hi - lo > 1) { const int mid = (lo + hi) / 2; if (g->he[mid] <= h) lo = mid; else hi = mid; }
+    return lo > g->nl - 1 ? g->nl - 1 : lo;
+}
+
+/* Slant depth toward the sun from rB; INFINITY when shadowed (rt_ipss.c:233-329). */
+static double ipss_tau_sun(ipss_t *g, const double *r0)
+{
+    const int nl = g->nl;
+    const double sn = sqrt(fmax(0.0, 1.0 - g->mu0 * g->mu0));
+    double u[3] = {-sn, 0.0, g->mu0};
+    const double un = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    u[0] /= un; u[1] /= un; u[2] /= un;
+    const double b = r0[0] * u[0] + r0[1] * u[1] + r0[2] * u[2];
+    const double c0 = r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2];
+    double tstop = INFINITY;
+    int hit = 0;
+    const double dg = b * b - (c0 - g->Re * g->Re);
+    if (dg >= 0.0) {
+        const double sq = sqrt(dg);
+        const double cand[2] = {-b - sq, -b + sq};
+        for (int i = 0; i < 2; ++i)
+            if (cand[i] > 1e-9 && cand[i] < tstop) { tstop = cand[i]; hit = 1; }
+    }
+    if (hit) return INFINITY;
+    const int cap = 2 * nl + 8;
+    int cnt = 0;
+    g->ts[cnt++] = 0.0;
+    for (int k = nl; k >= 0; --k) {
+        const double R = g->Re + g->he[k], d = b * b - (c0 - R * R);
+        if (d < 0.0) continue;
+        const double t = -b - sqrt(d);
+        if (t > 1e-9 && t <= tstop && cnt < cap) g->ts[cnt++] = t;
+    }
+    for (int k = 0; k <= nl; ++k) {
+        const double R = g->Re + g->he[k], d = b * b - (c0 - R * R);
+        if (d < 0.0) continue;
+        const double t = -b + sqrt(d);
+        if (t > 1e-9 && t <= tstop && cnt < cap) g->ts[cnt++] = t;
+    }
+    int mm = 0;
+    for (int i = 0; i < cnt; ++i)
+        if (i == 0 || g->ts[i] > g->ts[mm - 1] + 1e-12) g->ts[mm++] = g->ts[i];
+    double tau = 0.0;
+    for (int i = 0; i + 1 < mm; ++i) {
+        const double ta = g->ts[i], tb = g->ts[i + 1], tm = 0.5 * (ta + tb);
+        const double hm = sqrt(tm * tm + 2.0 * b * tm + c0) - g->Re;
+        if (hm < 0.0 || hm > g->he[nl]) continue;
+        int lo = 0, hi = nl;
+        while (hi - lo > 1) { const int mid = (lo + hi) / 2; if (g->he[mid] <= hm) lo = mid; else hi = mid; }
+        if (lo > nl - 1) lo = nl - 1;
+        tau += (tb - ta) * g->beta[lo];
+    }
+    return tau;
+}
+
+static double ipss_phase_aer(const ipss_t *g, double ct)
+{
+    const ocrt_aerosol *a = g->aer;
+    double p0 = 1.0, p1 = ct, s = a->beta[0];
+    if (a->L_max >= 1) s += a->beta[1] * p1;
+    for (int l = 2; l <= a->L_max; ++l) {
+        const double p2 = ((2.0 * l - 1.0) * ct * p1 - (l - 1.0) * p0) / l;
+        s += a->beta[l] * p2; p0 = p1; p1 = p2;
+    }
+    return s > 0.0 ? s : 0.0;
+}
+
+static double ipss_kappa(ipss_t *g, double vza, double raa)
+{
+    const int nl = g->nl;
+    const double tv = vza * PI / 180.0, fp = (180.0 - raa) * PI / 180.0;
+    if (g->aer) {
+        const double sn = sqrt(fmax(0.0, 1.0 - g->mu0 * g->mu0));
+        const double ct = sn * sin(tv) * cos(fp) - g->mu0 * cos(tv);
+        const double d = (g->depol >= 0.0 && g->depol < 1.0) ? g->depol : 0.0;
+        const double PR = 1.0 + (1.0 - d) / (2.0 + d) * 0.5 * (3.0 * ct * ct - 1.0);
+        const double PA = ipss_phase_aer(g, ct);
+        for (int j = 0; j < nl; ++j) g->wsrc[j] = g->wray[j] * PR + g->waer[j] * PA;
+    }
+    /* plane-parallel single scatter (rt_ipss.c:595-615) */
+    const double mv = cos(tv);
+    double Ipp = 0.0;
+    if (mv > 0.0) {
+        const double C = 1.0 / mv + 1.0 / g->mu0;
+        for (int j = 0; j < nl; ++j) {
+            if (!(g->beta[j] > 0.0)) continue;
+            Ipp += g->wsrc[j] / (mv * C) * (exp(-C * g->above[j + 1]) - exp(-C * g->above[j]));
+        }
+    }
+    /* spherical single scatter along the pixel-anchored line of sight */
+    const double u[3] = {sin(tv) * cos(fp), sin(tv) * sin(fp), cos(tv)};
+    const double Rt = g->Re + g->H;
+    const double bq = g->Re * u[2];
+    const double disc = bq * bq + Rt * Rt - g->Re * g->Re;
+    double Iss = 0.0;
+    if (disc > 0.0) {
+        const double s = -bq + sqrt(disc);
+        if (s > 0.0) {
+            const double rA[3] = {s * u[0], s * u[1], g->Re + s * u[2]};
+            const double dmax = s;
+            const double b = -(rA[0] * u[0] + rA[1] * u[1] + rA[2] * u[2]);
+            const double c0 = rA[0] * rA[0] + rA[1] * rA[1] + rA[2] * rA[2];
+            const int cap = 2 * nl + 8;
+            int cnt = 0;
+            g->lt[cnt++] = 0.0;
+            for (int k = nl; k >= 0; --k) {
+                const double R = g->Re + g->he[k], d = b * b - (c0 - R * R);
+                if (d < 0.0) continue;
+                const double t = -b - sqrt(d);
+                if (t > 1e-12 && t <= dmax && cnt < cap) g->lt[cnt++] = t;
+            }
+            for (int k = 0; k <= nl; ++k) {
+                const double R = g->Re + g->he[k], d = b * b - (c0 - R * R);
+                if (d < 0.0) continue;
+                const double t = -b + sqrt(d);
+                if (t > 1e-12 && t <= dmax && cnt < cap) g->lt[cnt++] = t;
+            }
+            if (cnt < cap) g->lt[cnt++] = dmax;
+            int mm = 0;
+            for (int i = 0; i < cnt; ++i)
+                if (i == 0 || g->lt[i] > g->lt[mm - 1] + 1e-12) g->lt[mm++] = g->lt[i];
+            double tau = 0.0;
+            for (int i = 0; i + 1 < mm; ++i) {
+                const double tm = 0.5 * (g->lt[i] + g->lt[i + 1]);
+                const double rmid = sqrt(tm * tm + 2.0 * b * tm + c0);
+                const int j = ipss_layer_of(g, rmid - g->Re);
+                g->llay[i] = j; g->ltau[i] = tau;
+                tau += (g->lt[i + 1] - g->lt[i]) * g->beta[j];
+            }
+            g->ln = mm;
+            const double xq = 1.0 / sqrt(3.0);     /* 2-point Gauss-Legendre per panel */
+            for (int i = 0; i + 1 < mm; ++i) {
+                const int j = g->llay[i];
+                if (!(g->beta[j] > 0.0)) continue;
+                const double sa = g->lt[i], sb = g->lt[i + 1];
+                const double half = 0.5 * (sb - sa), mid = 0.5 * (sa + sb);
+                for (int q = 0; q < 2; ++q) {
+                    const double sq = mid + half * (q == 0 ? -xq : xq);
+                    const double rB[3] = {rA[0] - sq * u[0], rA[1] - sq * u[1], rA[2] - sq * u[2]};
+                    const double hB = sqrt(rB[0] * rB[0] + rB[1] * rB[1] + rB[2] * rB[2]) - g->Re;
+                    if (hB < 0.0 || hB > g->H) continue;
+                    const double tview = g->ltau[i] + (sq - sa) * g->beta[j];
+                    const double tsun = ipss_tau_sun(g, rB);
+                    if (!isfinite(tsun)) continue;
+                    Iss += half * g->beta[j] * g->wsrc[j] * exp(-tview - tsun);
+                }
+            }
+        }
+    }
+    if (!(Ipp > 1.0e-300) || !isfinite(Iss)) return 1.0;
+    return Iss / Ipp;
+}
+
+/* ======================================================================
+ * Single-pixel solve (rt_solver.c:618-1436 with rt_solver_sos_pol
+ * :1987-2212 and rt_solver_sos_pol_with_surface :2923-3150).
+ * ==================================================================== */
+static double sup_norm(const ctx_t *c, const double *X)
+{
+    double mx = 0.0;
+    for (int k = 0; k <= c->md.nt; ++k)
+        for (int j = -c->n; j <= c->n; ++j) {
+            if (j == 0) continue;
+            const double a = fabs(F(X, c, k, j));
+            if (a > mx) mx = a;
+        }
+    return mx;
+}
+
+static double interp_pos(const double *mu_pos, const double *vals, int n, double mu)
+{
+    int jh = 1;
+    while (jh < n && mu_pos[jh - 1] < mu) jh++;
+    int jl = jh - 1;
+    if (jl < 1) { jl = 1; jh = 2; }
+    if (jh > n) { jh = n; jl = n - 1; }
+    const double t = (mu - mu_pos[jl - 1]) / (mu_pos[jh - 1] - mu_pos[jl - 1]);
+    return (1.0 - t) * vals[jl - 1] + t * vals[jh - 1];
+}
+
+static double recon_cos(const double *v, int M, double dphi)
+{
+    const double phi = dphi + PI;
+    double s = v[0];
+    for (int m = 1; m <= M; ++m) s += 2.0 * v[m] * cos((double)m * phi);
+    return s;
+}
+
+static double recon_sin(const double *v, int M, double dphi)
+{
+    if (M < 1) return 0.0;
+    const double phi = dphi + PI;
+    double s = 0.0;
+    for (int m = 1; m <= M; ++m) s += 2.0 * v[m] * sin((double)m * phi);
+    return s;
+}
+
+/* Flat-Fresnel reflected direct beam scattered once by the atmosphere
+ * (rt_surface_boundary.c:210-428). */
+static int flat_reflected_beam(const ctx_t *c, const mode_t_ *md, const ocrt_aerosol *aer,
+                               double nw, int qc, double *tot[3], double *o1[3])
+{
+    const int n = c->n, nt = c->md.nt, m = md->m, nd = 2 * n + 1;
+    const size_t cnt = (size_t)(nt + 1) * nd;
+    const double mu0 = c->mu0, n2 = nw * nw;
+    const double tn = sqrt(n2 - 1.0 + mu0 * mu0);
+    const double rp = (n2 * mu0 - tn) / (n2 * mu0 + tn), rs = (mu0 - tn) / (mu0 + tn);
+    const double RI = (rp * rp + rs * rs) / 2.0;
+    const double RQ = qc == 1 ? (rp * rp - rs * rs) / 2.0 : (rs * rs - rp * rp) / 2.0;
+    const double sb = 0.5 * exp(-2.0 * c->md.h[nt] / mu0);
+    const double bP = md->xpl[RIDX(n, 0)], bR = md->xrl[RIDX(n, 0)];
+    const double b0 = m == 0 ? c->beta0 : 0.0;
+    const int mol = m <= 2;
+    double *S = calloc(cnt * 6, sizeof(double));
+    if (!S) return -3;
+    double *SI = S, *SQ = S + cnt, *SU = S + 2 * cnt, *FI = S + 3 * cnt, *FQ = S + 4 * cnt, *FU = S + 5 * cnt;
+    const int L = md->L;
+    for (int layer = 0; layer < nt; ++layer) {
+        const double yt = c->md.ydel[layer], xt_ = c->md.xdel[layer];
+        const double yb = c->md.ydel[layer + 1], xb = c->md.xdel[layer + 1];
+        const double btop = sb * exp(c->md.h[layer] / mu0), bbot = sb * exp(c->md.h[layer + 1] / mu0);
+        for (int d = 1; d <= n; ++d) {
+            double K[2][6];
+            for (int side = 0; side < 2; ++side) {
+                const int jd = side == 0 ? -d : d;     /* top kernel uses the mirrored direction */
+                const double p = md->xpl[RIDX(n, jd)], r = md->xrl[RIDX(n, jd)], t = md->xtl[RIDX(n, jd)];
+                double pRT = 0.0, pTR = 0.0;
+                if (aer) {
+                    for (int l = m; l <= L; ++l) {
+                        const double Pj = md->P[(size_t)l * nd + RIDX(n, jd)];
+                        const double Rj = md->R[(size_t)l * nd + RIDX(n, jd)];
+                        const double Tj = md->T[(size_t)l * nd + RIDX(n, jd)];
+                        const double R0 = md->R[(size_t)l * nd + RIDX(n, 0)];
+                        const double T0 = md->T[(size_t)l * nd + RIDX(n, 0)];
+                        const double ga = l <= aer->L_max ? aer->gamma[l] : 0.0;
+                        const double al = l <= aer->L_max ? aer->alpha[l] : 0.0;
+                        const double ze = l <= aer->L_max ? aer->zeta[l] : 0.0;
+                        pRT += Pj * R0 * ga;
+                        pTR += Tj * R0 * al + Rj * T0 * ze;
+                    }
+                }
+                const double xx = side == 0 ? xt_ : xb, yy = side == 0 ? yt : yb;
+                K[side][0] = TAB(md->pfm, n, 0, jd) * xx + (mol ? b0 + c->beta2 * p * bP : 0.0) * yy;
+                K[side][1] = TAB(md->gr, n, 0, jd) * xx + (mol ? c->gamma2 * r * bP : 0.0) * yy;
+                K[side][2] = TAB(md->gt, n, 0, jd) * xx + (mol ? c->gamma2 * t * bP : 0.0) * yy;
+                K[side][3] = pRT * xx + (mol ? c->gamma2 * bR * p : 0.0) * yy;
+                K[side][4] = TAB(md->arr, n, 0, jd) * xx + (mol ? c->alpha2 * bR * r : 0.0) * yy;
+                K[side][5] = pTR * xx + (mol ? c->alpha2 * t * bR : 0.0) * yy;
+            }
+            F(SI, c, layer, d) = btop * (RI * K[0][0] + RQ * K[0][3]);
+            F(SQ, c, layer, d) = btop * (RI * K[0][1] + RQ * K[0][4]);
+            F(SU, c, layer, d) = btop * (RI * K[0][2] + RQ * K[0][5]);
+            F(SI, c, layer + 1, -d) = bbot * (RI * K[1][0] + RQ * K[1][3]);
+            F(SQ, c, layer + 1, -d) = bbot * (RI * K[1][1] + RQ * K[1][4]);
+            F(SU, c, layer + 1, -d) = bbot * (RI * K[1][2] + RQ * K[1][5]);
+        }
+    }
+    for (int k = 0; k <= nt; ++k) F(SI, c, k, 0) = F(SQ, c, k, 0) = F(SU, c, k, 0) = NAN;
+    int rc = transport(c, SI, NULL, FI);
+    if (!rc) rc = transport(c, SQ, NULL, FQ);
+    if (!rc) rc = transport(c, SU, NULL, FU);
+    if (!rc) {
+        double *fs[3] = {FI, FQ, FU};
+        for (int s = 0; s < 3; ++s)
+            for (int k = 0; k <= nt; ++k)
+                for (int j = -n; j <= n; ++j) {
+                    if (j == 0) continue;
+                    F(tot[s], c, k, j) += F(fs[s], c, k, j);
+                    F(o1[s], c, k, j) += F(fs[s], c, k, j);
+                }
+    }
+    free(S);
+    return rc ? -2 : 0;
+}
+
+static int check_args(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer)
+{
+    if (!cs || !op) return -1;
+    if (!(cs->wavelength_nm >= 330.0 - 1e-9 && cs->wavelength_nm <= 1100.0 + 1e-9)) return -1;
+    if (cs->sza_deg < 0.0 || cs->sza_deg >= 90.0) return -1;
+    if (cs->vza_deg < 0.0 || cs->vza_deg >= 90.0) return -1;
+    if (op->fourier_m_max < 0 || op->fourier_m_max > 255) return -1;
+    if (op->n_mu < 2 || op->n_mu > 64 || op->n_layers < 2) return -1;
+    if (op->max_orders < 1 || !(op->tolerance > 0.0)) return -1;
+    if (aer) {
+        if (aer->tau_a < 0.0 || aer->ssa_a < 0.0 || aer->ssa_a > 1.0 || aer->L_max < 2) return -1;
+        if (!aer->beta || !aer->gamma || !aer->alpha || !aer->zeta) return -1;
+    }
+    if (cs->surface != OCRT_SURFACE_BLACK && cs->surface != OCRT_SURFACE_BLACK_FRESNEL_OCEAN &&
+        cs->surface != OCRT_SURFACE_FLAT) return -5;
+    if ((cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN || cs->surface == OCRT_SURFACE_FLAT) &&
+        !(cs->n_water > 0.0)) return -1;
+    return 0;
+}
+
+int ocrt_oracle_solve_case(const ocrt_case *cs, const ocrt_opts *op,
+                           const ocrt_aerosol *aer_in, ocrt_result *out, ocrt_diag *diag)
+{
+    int rc = check_args(cs, op, aer_in);
+    if (rc) return rc;
+    if (!out) return -1;
+    memset(out, 0, sizeof(*out));
+    const ocrt_aerosol *aer = (aer_in && aer_in->tau_a > 0.0) ? aer_in : NULL;
+
+    ctx_t *c = calloc(1, sizeof(ctx_t));
+    if (!c) return -3;
+    c->mu0 = cos(cs->sza_deg * PI / 180.0);
+    c->mu_view = cos(cs->vza_deg * PI / 180.0);
+    const double dphi = cs->raa_deg * PI / 180.0;
+
+    double tau_r;
+    if (!(cs->pressure_hpa > 0.0)) tau_r = 0.0;
+    else if (op->tau_r_source == OCRT_TAU_R_FROM_INPUT) {
+        if (cs->tau_r_input <= 0.0) { free(c); return -1; }
+        tau_r = cs->tau_r_input;
+    } else tau_r = ocrt_oracle_tau_rayleigh(cs->wavelength_nm, cs->pressure_hpa);
+    out->tau_R_total = tau_r;
+
+    /* ring: Gauss nodes plus the view direction as a zero-weight node */
+    double mu_r[MAX_RING], w_r[MAX_RING];
+    int nr = op->n_mu;
+    if (ocrt_oracle_gauss(op->n_mu, mu_r, w_r)) { free(c); return -1; }
+    c->view_idx = 0;
+    if (op->view_as_node) c->view_idx = ring_insert(mu_r, w_r, &nr, c->mu_view) + 1;
+    const int n = nr, nt = op->n_layers, nd = 2 * n + 1, M = op->fourier_m_max;
+    c->n = n;
+    c->rm[RIDX(n, 0)] = -c->mu0; c->gb[RIDX(n, 0)] = 0.0;
+    for (int j = 1; j <= n; ++j) {
+        c->rm[RIDX(n, j)] = mu_r[j - 1]; c->rm[RIDX(n, -j)] = -mu_r[j - 1];
+        c->gb[RIDX(n, j)] = c->gb[RIDX(n, -j)] = w_r[j - 1];
+    }
+    /* molecular moments (rt_molecular_phase.c:5-20) */
+    const double A = 2.0 * (1.0 - DEPOL) / (2.0 + DEPOL);
+    c->beta0 = 1.0; c->beta2 = 0.5 * A; c->gamma2 = -A * sqrt(1.5); c->alpha2 = 3.0 * A;
+
+    if (aer) {
+        if (!(tau_r >= 0.0 && tau_r + aer->tau_a > 0.0)) { free(c); return -1; }
+        rc = medium_build(&c->md, nt, tau_r, aer->tau_a, aer->ssa_a, c->mu0, op->aer_h_km,
+                          op->rayleigh_profile, op->rayleigh_h_km);
+    } else {
+        if (!(tau_r > 0.0)) { free(c); return -1; }
+        rc = medium_build(&c->md, nt, tau_r, 0.0, 1.0, c->mu0, op->aer_h_km,
+                          op->rayleigh_profile, op->rayleigh_h_km);
+    }
+    if (rc) { free(c); return rc; }
+    if ((rc = transport_prepare(c))) goto done;
+
+    int L = M > 2 ? M : 2;
+    if (aer && aer->L_max > L) L = aer->L_max;
+    mode_t_ md;
+    if ((rc = mode_alloc(&md, n, L))) goto done;
+
+    const size_t cnt = (size_t)(nt + 1) * nd;
+    double *buf = calloc(cnt * 18, sizeof(double));
+    if (!buf) { mode_free(&md); rc = -3; goto done; }
+    double *Js[3] = {buf, buf + cnt, buf + 2 * cnt};
+    double *Pr[3] = {buf + 3 * cnt, buf + 4 * cnt, buf + 5 * cnt};
+    double *Tt[3] = {buf + 6 * cnt, buf + 7 * cnt, buf + 8 * cnt};
+    double *Ip[3] = {buf + 9 * cnt, buf + 10 * cnt, buf + 11 * cnt};
+    double *Ic[3] = {buf + 12 * cnt, buf + 13 * cnt, buf + 14 * cnt};
+    double *O1[3] = {buf + 15 * cnt, buf + 16 * cnt, buf + 17 * cnt};
+
+    const int surf_on = cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN || cs->surface == OCRT_SURFACE_FLAT;
+    const int flat = cs->surface == OCRT_SURFACE_FLAT ||
+                     (cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && cs->wind_speed <= 0.0);
+    const int rough = surf_on && !flat;
+    double *mu_pos = malloc(sizeof(double) * n);
+    for (int j = 1; j <= n; ++j) mu_pos[j - 1] = c->rm[RIDX(n, j)];
+    /* rough-surface Fourier kernels for all modes: ring x ring and ring x sun */
+    double *Kr = NULL, *Ks = NULL;
+    const int nphi = op->n_phi_surface > 0 ? op->n_phi_surface : 1024;
+    if (rough) {
+        Kr = malloc(sizeof(double) * (size_t)(M + 1) * n * n * 9);
+        Ks = malloc(sizeof(double) * (size_t)(M + 1) * n * 9);
+        coxmunk_fourier_allm(mu_pos, n, mu_pos, n, M, nphi, cs->wind_speed, cs->sigma_type,
+                             cs->n_water, cs->q_convention, Kr);
+        coxmunk_fourier_allm(mu_pos, n, &c->mu0, 1, M, nphi, cs->wind_speed, cs->sigma_type,
+                             cs->n_water, cs->q_convention, Ks);
+    }
+    double *I_dn_boa = calloc((size_t)(M + 1) * n, sizeof(double));
+    double *vI = calloc((size_t)(M + 1) * 3, sizeof(double));
+    double *vQ = vI + (M + 1), *vU = vQ + (M + 1);
+    double *seed = rough ? calloc(cnt * 3, sizeof(double)) : NULL;
+    int max_orders_seen = 0, all_conv = 1, order_modes = 0;
+
+    for (int m = 0; m <= M && !rc; ++m) {
+        mode_build(&md, m, c->rm, aer);
+        primary_source(c, &md, Js[0], Js[1], Js[2]);
+        for (int s = 0; s < 3 && !rc; ++s) if (transport(c, Js[s], NULL, Pr[s])) rc = -2;
+        if (rc) break;
+        for (int s = 0; s < 3; ++s) { memcpy(Tt[s], Pr[s], cnt * sizeof(double)); memset(O1[s], 0, cnt * sizeof(double)); }
+        int orders = 1, conv = 0;
+        double resid = 0.0;
+        const double *Krm = rough ? Kr + (size_t)m * n * n * 9 : NULL;
+        if (surf_on) {
+            if (flat) {
+                if ((rc = flat_reflected_beam(c, &md, aer, cs->n_water, cs->q_convention, Tt, O1))) break;
+            } else {
+                /* rough direct-beam seed (rt_surface_boundary.c:430-493) */
+                const double *Ksm = Ks + (size_t)m * n * 9;
+                const double tdn = exp(-c->md.h[nt] / c->mu0);
+                const double fs = (m == 0 ? PI : 0.5 * PI) * c->mu0;
+                for (int k = 0; k <= nt; ++k) {
+                    const double up = c->md.h[nt] - c->md.h[k];
+                    for (int o = 1; o <= n; ++o) {
+                        const double f = fs * tdn * exp(-up / mu_pos[o - 1]);
+                        const double v[3] = {Ksm[(o - 1) * 9 + 0] * f, Ksm[(o - 1) * 9 + 3] * f,
+                                             Ksm[(o - 1) * 9 + 6] * f};
+                        for (int s = 0; s < 3; ++s) {
+                            F(Tt[s], c, k, o) += v[s];
+                            F(O1[s], c, k, o) += v[s];
+                            seed[(size_t)s * cnt + (size_t)k * nd + RIDX(n, o)] = v[s];
+                        }
+                    }
+                }
+            }
+        }
+        if (op->max_orders > 1) {
+            for (int s = 0; s < 3; ++s)
+                for (size_t i = 0; i < cnt; ++i) Ip[s][i] = Pr[s][i] + O1[s][i];
+            double bc[3][MAX_RING];
+            for (int it = 2; it <= op->max_orders; ++it) {
+                if ((rc = ms_source(c, &md, Ip[0], Ip[1], Ip[2], Js[0], Js[1], Js[2]))) break;
+                if (surf_on) {
+                    /* surface boundary operator (rt_surface_boundary.c:137-208) */
+                    const double fw = flat ? 2.0 * PI : (m == 0 ? 2.0 * PI : PI);
+                    for (int o = 1; o <= n; ++o) {
+                        double si = 0, sq = 0, su = 0;
+                        if (flat) {
+                            const double wo = c->gb[RIDX(n, o)];
+                            double MF[9];
+                            fresnel_R(mu_pos[o - 1], cs->n_water, cs->q_convention, MF);
+                            const double ii = F(Ip[0], c, nt, -o), qq = F(Ip[1], c, nt, -o), uu = F(Ip[2], c, nt, -o);
+                            if (wo == 0.0) {
+                                si = MF[0] * ii + MF[1] * qq + MF[2] * uu;
+                                sq = MF[3] * ii + MF[4] * qq + MF[5] * uu;
+                                su = MF[6] * ii + MF[7] * qq + MF[8] * uu;
+                            } else {
+                                const double dd = 1.0 / (2.0 * PI * mu_pos[o - 1] * wo);
+                                const double pw = fw * mu_pos[o - 1] * wo;
+                                si = pw * (dd * MF[0] * ii + dd * MF[1] * qq + dd * MF[2] * uu);
+                                sq = pw * (dd * MF[3] * ii + dd * MF[4] * qq + dd * MF[5] * uu);
+                                su = pw * (dd * MF[6] * ii + dd * MF[7] * qq + dd * MF[8] * uu);
+                            }
+                        } else {
+                            for (int i = 1; i <= n; ++i) {
+                                const double wi = c->gb[RIDX(n, i)];
+                                if (wi == 0.0) continue;
+                                const double pw = fw * mu_pos[i - 1] * wi;
+                                const double *R = Krm + ((size_t)(o - 1) * n + (i - 1)) * 9;
+                                const double ii = F(Ip[0], c, nt, -i), qq = F(Ip[1], c, nt, -i), uu = F(Ip[2], c, nt, -i);
+                                si += pw * (R[0] * ii + R[1] * qq + R[2] * uu);
+                                sq += pw * (R[3] * ii + R[4] * qq + R[5] * uu);
+                                su += pw * (R[6] * ii + R[7] * qq + R[8] * uu);
+                            }
+                        }
+                        bc[0][o - 1] = si; bc[1][o - 1] = sq; bc[2][o - 1] = su;
+                    }
+                }
+                for (int s = 0; s < 3 && !rc; ++s)
+                    if (transport(c, Js[s], surf_on ? bc[s] : NULL, Ic[s])) rc = -2;
+                if (rc) break;
+                for (int s = 0; s < 3; ++s)
+                    for (int k = 0; k <= nt; ++k)
+                        for (int j = -n; j <= n; ++j)
+                            if (j) F(Tt[s], c, k, j) += F(Ic[s], c, k, j);
+                orders = it;
+                double mi = 0, mt = 0;
+                for (int s = 0; s < 3; ++s) {
+                    const double a = sup_norm(c, Ic[s]), b = sup_norm(c, Tt[s]);
+                    if (a > mi) mi = a;
+                    if (b > mt) mt = b;
+                }
+                resid = mt > 0.0 ? mi / mt : 0.0;
+                if (resid < op->tolerance) { conv = 1; break; }
+                for (int s = 0; s < 3; ++s) memcpy(Ip[s], Ic[s], cnt * sizeof(double));
+            }
+        } else {
+            conv = 1;
+        }
+        if (rc) break;
+        if (rough)
+            for (int s = 0; s < 3; ++s)
+                for (int k = 0; k <= nt; ++k)
+                    for (int o = 1; o <= n; ++o)
+                        F(Tt[s], c, k, o) -= seed[(size_t)s * cnt + (size_t)k * nd + RIDX(n, o)];
+        if (orders > max_orders_seen) max_orders_seen = orders;
+        if (!conv) all_conv = 0;
+        order_modes += orders;
+        if (diag) {
+            if (diag->orders_per_m) diag->orders_per_m[m] = orders;
+            if (diag->residual_per_m) diag->residual_per_m[m] = resid;
+        }
+        /* TOA sample at the view (rt_solver.c:1010-1024) */
+        if (c->view_idx > 0) {
+            vI[m] = F(Tt[0], c, 0, c->view_idx); vQ[m] = F(Tt[1], c, 0, c->view_idx);
+            vU[m] = F(Tt[2], c, 0, c->view_idx);
+        } else {
+            double tmp[3][MAX_RING];
+            for (int s = 0; s < 3; ++s) for (int j = 1; j <= n; ++j) tmp[s][j - 1] = F(Tt[s], c, 0, j);
+            vI[m] = interp_pos(mu_pos, tmp[0], n, c->mu_view);
+            vQ[m] = interp_pos(mu_pos, tmp[1], n, c->mu_view);
+            vU[m] = interp_pos(mu_pos, tmp[2], n, c->mu_view);
+        }
+        for (int j = 1; j <= n; ++j) I_dn_boa[(size_t)m * n + j - 1] = F(Tt[0], c, nt, -j);
+        if (diag) {
+            if (diag->view_I_m) diag->view_I_m[m] = vI[m];
+            if (diag->view_Q_m) diag->view_Q_m[m] = vQ[m];
+            if (diag->view_U_m) diag->view_U_m[m] = vU[m];
+        }
+    }
+    if (!rc) {
+        const double I = recon_cos(vI, M, dphi), Q = recon_cos(vQ, M, dphi), U = recon_sin(vU, M, dphi);
+        out->I_TOA = I; out->Q_TOA = Q; out->U_TOA = U;
+        out->rho_I = I / c->mu0; out->rho_Q = Q / c->mu0; out->rho_U = U / c->mu0;
+        out->kappa_ipss = 1.0;
+        double tau_dir = -1.0;
+        if (op->pssa) {
+            ipss_t g;
+            if (ipss_init(&g, &c->md, c->mu0, aer) == 0) {
+                const double rB[3] = {0.0, 0.0, g.Re};
+                const double ts = ipss_tau_sun(&g, rB);
+                tau_dir = isfinite(ts) ? ts : -1.0;
+                const double kap = ipss_kappa(&g, cs->vza_deg, cs->raa_deg);
+                out->kappa_ipss = kap;
+                out->rho_I *= kap; out->rho_Q *= kap; out->rho_U *= kap;
+                out->I_TOA *= kap; out->Q_TOA *= kap; out->U_TOA *= kap;
+            } else rc = -1;
+            ipss_free(&g);
+        }
+        const double tau_t = c->md.h[nt];
+        if (!rc && cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN) {
+            const double phi_v = (cs->raa_deg - 180.0) * PI / 180.0;
+            const double mv = cs->vza_deg > 0.0 ? c->mu_view : 1.0;
+            double g[3];
+            sunglint_rho(mv, phi_v, c->mu0, cs->wind_speed, cs->sigma_type, cs->n_water, tau_t,
+                         cs->q_convention, g);
+            if (tau_dir >= 0.0) {
+                const double cg = exp(-(tau_dir - tau_t / c->mu0));
+                g[0] *= cg; g[1] *= cg; g[2] *= cg;
+            }
+            if (cs->decouple_sunglint == 0) { out->rho_I += g[0]; out->rho_Q += g[1]; out->rho_U += -g[2]; }
+            if (cs->wind_speed > 0.0) {
+                out->T_sg_up_dir = g[0] * c->mu0;
+                out->rho_glint_direct_I = g[0]; out->rho_glint_direct_Q = g[1]; out->rho_glint_direct_U = g[2];
+            }
+        }
+        out->n_orders_used = max_orders_seen;
+        out->converged = all_conv;
+        out->order_modes = order_modes;
+        /* transmittances (rt_solver.c:1195-1275) */
+        out->T_dir_dn = tau_dir >= 0.0 ? exp(-tau_dir) : exp(-tau_t / c->mu0);
+        double fd = 0.0;
+        for (int j = 1; j <= n; ++j) fd += mu_pos[j - 1] * c->gb[RIDX(n, j)] * I_dn_boa[j - 1];
+        fd *= 2.0 * PI;
+        out->T_diff_dn_hemi = fd / (PI * c->mu0);
+        out->T_total_dn_hemi = out->T_dir_dn + out->T_diff_dn_hemi;
+        double *vdn = calloc(M + 1, sizeof(double));
+        for (int m = 0; m <= M; ++m) vdn[m] = interp_pos(mu_pos, I_dn_boa + (size_t)m * n, n, c->mu_view);
+        out->T_diff_dn_dir = 2.0 * PI * c->mu_view * recon_cos(vdn, M, dphi) / (PI * c->mu0);
+        free(vdn);
+        out->T_total_up_dir = out->rho_I * c->mu0;
+        out->T_dir_up_view = exp(-tau_t / (c->mu_view > 0.0 ? c->mu_view : 1.0));
+    }
+    free(seed); free(vI); free(I_dn_boa); free(Kr); free(Ks); free(mu_pos); free(buf);
+    mode_free(&md);
+done:
+    free(c->Tr); free(c->Ca); free(c->Cb);
+    medium_free(&c->md);
+    free(c);
+    return rc;
+}
+
+/* OpenMP pixel loop (the reference's batch pattern rt_io.c:197-199). */
+int ocrt_oracle_solve_batch(int n, const ocrt_case *cases, const ocrt_opts *opts, int opts_per_case,
+                            const ocrt_aerosol *aer, int aer_per_case, ocrt_result *out,
+                            int n_threads)
+{
+    if (n < 0 || (n > 0 && (!cases || !opts || !out))) return -1;
+    int rc_all = 0;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n; ++i) {
+        const ocrt_opts *o = opts_per_case ? opts + i : opts;
+        const ocrt_aerosol *a = aer ? (aer_per_case ? aer + i : aer) : NULL;
+        const int rc = ocrt_oracle_solve_case(cases + i, o, a, out + i, NULL);
+        if (rc) {
+#pragma omp critical
+            rc_all = rc;
+        }
+    }
+    return rc_all;
+}
+
+int ocrt_oracle_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
