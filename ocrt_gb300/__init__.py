@@ -1,0 +1,154 @@
+"""GB300 successive-orders-of-scattering vector radiative-transfer solver.
+
+Python face of the C-ABI library ``libocrt_gb300.so`` (include/ocrt_gb300.h).
+Every solve runs in the CUDA library; there is no CPU fallback: if the shared
+library is missing or no CUDA device is present, the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (Aerosol, AerosolHolder, Case, Diag, Opts, Result, default_case, default_opts,
+                   result_dict, RESULT_FIELDS)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libocrt_gb300.so")
+_lib = None
+
+EXPORTS = [
+    "ocrt_opts_default", "ocrt_case_default", "ocrt_gb_init", "ocrt_gb_shutdown", "ocrt_gb_last_error",
+    "ocrt_gb_solve_case", "ocrt_gb_solve_batch", "ocrt_gb_plan_create", "ocrt_gb_plan_execute",
+    "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy",
+]
+
+
+class OcrtError(RuntimeError):
+    def __init__(self, rc, msg):
+        super().__init__(f"ocrt error {rc}: {msg}")
+        self.rc = rc
+
+
+def lib():
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OcrtError(_abi.OCRT_ERR_DEVICE,
+                        f"{LIB_PATH} not built; run python -m ocrt_gb300.build")
+    L = C.CDLL(LIB_PATH)
+    L.ocrt_gb_init.argtypes = [C.c_int]
+    L.ocrt_gb_last_error.restype = C.c_char_p
+    L.ocrt_gb_solve_case.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol),
+                                     C.POINTER(Result), C.POINTER(Diag)]
+    L.ocrt_gb_solve_batch.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int,
+                                      C.POINTER(Aerosol), C.c_int, C.POINTER(Result), C.c_void_p]
+    L.ocrt_gb_plan_create.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int,
+                                      C.POINTER(Aerosol), C.c_int, C.POINTER(C.c_void_p)]
+    L.ocrt_gb_plan_execute.argtypes = [C.c_void_p, C.c_void_p]
+    L.ocrt_gb_plan_results.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p]
+    L.ocrt_gb_plan_stats.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    L.ocrt_gb_plan_destroy.argtypes = [C.c_void_p]
+    L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
+    L.ocrt_case_default.argtypes = [C.POINTER(Case)]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise OcrtError(rc, lib().ocrt_gb_last_error().decode())
+
+
+def solve_case(case, opts=None, aerosol=None, diag=False):
+    """One pixel; returns a dict of ocrt_result fields (plus per-mode arrays if diag)."""
+    L = lib()
+    opts = opts or default_opts()
+    r = Result()
+    d = None
+    arrs = None
+    if diag:
+        n = opts.fourier_m_max + 1
+        arrs = {"orders_per_m": (C.c_int * n)(), "residual_per_m": (C.c_double * n)(),
+                "view_I_m": (C.c_double * n)(), "view_Q_m": (C.c_double * n)(),
+                "view_U_m": (C.c_double * n)()}
+        d = Diag(**{k: C.cast(v, Diag._fields_[i][1]) for i, (k, v) in enumerate(arrs.items())})
+    a = aerosol.struct if isinstance(aerosol, AerosolHolder) else aerosol
+    _check(L.ocrt_gb_solve_case(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
+                                C.byref(r), C.byref(d) if d is not None else None))
+    out = result_dict(r)
+    if diag:
+        out.update({k: np.array(v[:]) for k, v in arrs.items()})
+    return out
+
+
+def _arrays(cases, opts, aerosols):
+    n = len(cases)
+    ca = (Case * n)(*cases)
+    if isinstance(opts, (list, tuple)):
+        oa, opp = (Opts * n)(*opts), 1
+    else:
+        oa, opp = (Opts * 1)(opts), 0
+    if aerosols is None:
+        aa, app = None, 0
+    elif isinstance(aerosols, (list, tuple)):
+        structs = [a.struct if isinstance(a, AerosolHolder) else a for a in aerosols]
+        aa, app = (Aerosol * n)(*structs), 1
+    else:
+        s = aerosols.struct if isinstance(aerosols, AerosolHolder) else aerosols
+        aa, app = (Aerosol * 1)(s), 0
+    return n, ca, oa, opp, aa, app
+
+
+def solve_batch(cases, opts, aerosols=None):
+    """n pixels in one device pass; returns a numpy structured view of ocrt_result."""
+    L = lib()
+    n, ca, oa, opp, aa, app = _arrays(cases, opts, aerosols)
+    out = (Result * n)()
+    _check(L.ocrt_gb_solve_batch(n, ca, oa, opp, aa, app, out, None))
+    return results_to_numpy(out)
+
+
+def results_to_numpy(out):
+    dt = np.dtype([(f, np.float64 if t is C.c_double else np.int32) for f, t in Result._fields_],
+                  align=True)
+    arr = np.frombuffer(out, dtype=dt, count=len(out)).copy()
+    return arr
+
+
+class Plan:
+    """Device-resident batch: upload once, execute many times."""
+
+    def __init__(self, cases, opts, aerosols=None):
+        L = lib()
+        self._keep = _arrays(cases, opts, aerosols)
+        n, ca, oa, opp, aa, app = self._keep
+        self.n = n
+        self._h = C.c_void_p()
+        _check(L.ocrt_gb_plan_create(n, ca, oa, opp, aa, app, C.byref(self._h)))
+
+    def execute(self, stream=None):
+        _check(lib().ocrt_gb_plan_execute(self._h, stream))
+
+    def results(self, stream=None):
+        out = (Result * self.n)()
+        _check(lib().ocrt_gb_plan_results(self._h, out, stream))
+        return results_to_numpy(out)
+
+    def stats(self):
+        om, nl = C.c_double(), C.c_longlong()
+        _check(lib().ocrt_gb_plan_stats(self._h, C.byref(om), C.byref(nl)))
+        return {"order_modes": om.value, "kernel_launches": nl.value}
+
+    def close(self):
+        if self._h:
+            lib().ocrt_gb_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,574 @@
+// api.cu — host side of the C ABI (include/ocrt_gb300.h).
+//
+// A plan uploads a batch, groups pixels by Gauss order N, and splits each
+// group into waves of whole pixels whose per-(pixel, mode) working set fits
+// the workspace budget.  Execution is asynchronous on one stream; the order
+// loop polls the device-side active-task count every few orders, which is the
+// only host synchronisation inside a solve.
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "kernels.cuh"
+#include "physics.cuh"
+
+namespace {
+
+std::mutex g_mu;
+thread_local std::string g_err;
+int g_device = -1;
+cudaStream_t g_stream = nullptr;
+std::multimap<size_t, void *> g_free;      // caching allocator: size -> block
+std::map<void *, size_t> g_live;
+int *g_pinned = nullptr;
+
+int fail(int rc, const std::string &msg)
+{
+    g_err = msg;
+    return rc;
+}
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(OCRT_ERR_DEVICE, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+void *dalloc(size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    bytes = (bytes + 255) & ~size_t(255);
+    auto it = g_free.lower_bound(bytes);
+    if (it != g_free.end() && it->first <= bytes * 2) {
+        void *p = it->second;
+        const size_t sz = it->first;
+        g_free.erase(it);
+        g_live[p] = sz;
+        return p;
+    }
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        for (auto &kv : g_free) cudaFree(kv.second);
+        g_free.clear();
+        if (cudaMalloc(&p, bytes) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    }
+    g_live[p] = bytes;
+    return p;
+}
+
+void dfree(void *p)
+{
+    if (!p) return;
+    auto it = g_live.find(p);
+    if (it == g_live.end()) return;
+    g_free.insert({it->second, p});
+    g_live.erase(it);
+}
+
+int ensure_init()
+{
+    if (g_device >= 0) return OCRT_OK;
+    return ocrt_gb_init(0);
+}
+
+int validate(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer)
+{
+    // rt_solver.c:627-638 plus the documented limits of this library
+    if (!cs || !op) return fail(OCRT_ERR_ARGS, "null case or options");
+    if (!(cs->wavelength_nm >= 330.0 - 1e-9 && cs->wavelength_nm <= 1100.0 + 1e-9))
+        return fail(OCRT_ERR_ARGS, "wavelength outside [330, 1100] nm");
+    if (!(cs->sza_deg >= 0.0 && cs->sza_deg < 90.0)) return fail(OCRT_ERR_ARGS, "sza outside [0, 90)");
+    if (!(cs->vza_deg >= 0.0 && cs->vza_deg < 90.0)) return fail(OCRT_ERR_ARGS, "vza outside [0, 90)");
+    if (!std::isfinite(cs->raa_deg)) return fail(OCRT_ERR_ARGS, "raa not finite");
+    if (op->fourier_m_max < 0 || op->fourier_m_max > OCRT_MAX_M) return fail(OCRT_ERR_ARGS, "fourier_m_max outside [0, 255]");
+    if (op->n_mu < 2 || op->n_mu > OCRT_MAX_N) return fail(OCRT_ERR_ARGS, "n_mu outside [2, 64]");
+    if (op->n_layers < 2 || op->n_layers > 1024) return fail(OCRT_ERR_ARGS, "n_layers outside [2, 1024]");
+    if (op->max_orders < 1 || !(op->tolerance > 0.0)) return fail(OCRT_ERR_ARGS, "bad SOS iteration control");
+    const int nphi = op->n_phi_surface > 0 ? op->n_phi_surface : 1024;
+    if (nphi < 64 || nphi > 4096 || (nphi & 1)) return fail(OCRT_ERR_ARGS, "n_phi_surface outside [64, 4096] or odd");
+    if (cs->surface == OCRT_SURFACE_LAMBERT || cs->surface == OCRT_SURFACE_OCEAN)
+        return fail(OCRT_ERR_UNSUPPORTED, "surface kind not on the GB300 solve path");
+    if (cs->surface != OCRT_SURFACE_BLACK && cs->surface != OCRT_SURFACE_BLACK_FRESNEL_OCEAN &&
+        cs->surface != OCRT_SURFACE_FLAT) return fail(OCRT_ERR_ARGS, "unknown surface kind");
+    if ((cs->surface != OCRT_SURFACE_BLACK) && !(cs->n_water > 0.0)) return fail(OCRT_ERR_ARGS, "n_water <= 0");
+    const bool has_aer = aer && aer->tau_a > 0.0;
+    if (aer) {
+        if (aer->tau_a < 0.0 || aer->ssa_a < 0.0 || aer->ssa_a > 1.0 || aer->L_max < 2 || aer->L_max > 1024)
+            return fail(OCRT_ERR_ARGS, "bad aerosol expansion");
+        if (!aer->beta || !aer->gamma || !aer->alpha || !aer->zeta) return fail(OCRT_ERR_ARGS, "null moment array");
+        for (int l = 0; l <= aer->L_max; ++l)
+            if (!std::isfinite(aer->beta[l]) || !std::isfinite(aer->gamma[l]) || !std::isfinite(aer->alpha[l]) ||
+                !std::isfinite(aer->zeta[l])) return fail(OCRT_ERR_NONFINITE, "non-finite aerosol moment");
+    }
+    double tau_r;
+    if (!(cs->pressure_hpa > 0.0)) tau_r = 0.0;
+    else if (op->tau_r_source == OCRT_TAU_R_FROM_INPUT) {
+        if (cs->tau_r_input <= 0.0) return fail(OCRT_ERR_ARGS, "tau_r_input <= 0 with FROM_INPUT");
+        tau_r = cs->tau_r_input;
+    } else tau_r = bodhaine_tau(cs->wavelength_nm, cs->pressure_hpa);
+    if (has_aer) { if (!(tau_r + aer->tau_a > 0.0)) return fail(OCRT_ERR_ARGS, "zero column"); }
+    else if (!(tau_r > 0.0)) return fail(OCRT_ERR_ARGS, "no scattering column (pressure <= 0 and no aerosol)");
+    if (op->pssa && op->rayleigh_profile == OCRT_PROFILE_EXPONENTIAL && !(op->rayleigh_h_km > 0.0))
+        return fail(OCRT_ERR_ARGS, "rayleigh_h_km <= 0");
+    return OCRT_OK;
+}
+
+struct Wave {
+    int p0, p1;            // pixel range within the group
+    int t0, t1;            // task range
+    int Kmax;
+    size_t fld, ops, srf;  // element counts of the wave buffers
+    bool any_rough, any_flat;
+};
+
+struct Group {
+    int N = 0, P = 0, T = 0;
+    Geom G{};
+    std::vector<int> idx;                 // case index of each pixel
+    std::vector<PixDev> hpx;
+    std::vector<TaskDev> htask;
+    std::vector<int> hpix_task0;
+    std::vector<Wave> waves;
+    int Lmax = 2, Mmax = 0, max_orders = 1, nphi = 1024;
+    bool any_pssa = false, any_rough = false, any_flat = false;
+    size_t nlev = 0, ncoef = 0, nmom = 0;
+    size_t wave_fld = 0, wave_ops = 0, wave_srf = 0;
+    int wave_tasks = 0;
+    // device
+    PixDev *px = nullptr; TaskDev *tasks = nullptr; TaskState *state = nullptr; TaskOut *tout = nullptr;
+    ocrt_result *res = nullptr; int *pix_task0 = nullptr;
+    double *gmu = nullptr, *gw = nullptr;
+    double *h = nullptr, *ch = nullptr, *xd = nullptr, *yd = nullptr, *z = nullptr;
+    float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
+    float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
+    double *mb = nullptr, *mg = nullptr, *ma = nullptr, *mz = nullptr;
+    double *kappa = nullptr, *taudir = nullptr;
+    int *active_cnt = nullptr, *err = nullptr;
+    float *F = nullptr, *J = nullptr, *ops = nullptr, *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
+    double *Tot = nullptr;
+};
+
+size_t wave_budget_bytes()
+{
+    const char *e = getenv("OCRT_GB_WAVE_BYTES");
+    if (e && *e) return (size_t)strtoull(e, nullptr, 10);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 0) return (size_t)(fr * 0.45);
+    return (size_t)8 << 30;
+}
+
+} // namespace
+
+struct ocrt_plan {
+    int n = 0;
+    std::vector<Group> groups;
+    long long launches = 0;
+    double order_modes = 0;
+};
+
+namespace {
+
+template <class T> int up(T *&dst, const std::vector<T> &src)
+{
+    dst = (T *)dalloc(sizeof(T) * std::max<size_t>(src.size(), 1));
+    if (!dst) return fail(OCRT_ERR_ALLOC, "device allocation failed");
+    if (!src.empty()) CK(cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, g_stream));
+    return OCRT_OK;
+}
+
+template <class T> int alloc(T *&dst, size_t n)
+{
+    dst = (T *)dalloc(sizeof(T) * std::max<size_t>(n, 1));
+    return dst ? OCRT_OK : fail(OCRT_ERR_ALLOC, "device allocation failed");
+}
+
+void free_group(Group &g)
+{
+    void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.h, g.ch, g.xd, g.yd, g.z,
+                    g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
+                    g.active_cnt, g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot};
+    for (void *p : ptrs) dfree(p);
+}
+
+int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app)
+{
+    const Geom G = make_geom(g.N);
+    g.G = G;
+    g.P = (int)g.idx.size();
+    std::vector<double> mb, mgv, ma, mz;
+    size_t lev = 0, coef = 0;
+    int task = 0;
+    for (int q = 0; q < g.P; ++q) {
+        const int i = g.idx[q];
+        const ocrt_case &c = cases[i];
+        const ocrt_opts &o = opp ? opts[i] : opts[0];
+        const ocrt_aerosol *a = aer ? (app ? &aer[i] : &aer[0]) : nullptr;
+        PixDev d;
+        memset(&d, 0, sizeof(d));
+        d.sza_deg = c.sza_deg; d.vza_deg = c.vza_deg; d.raa_deg = c.raa_deg; d.wavelength_nm = c.wavelength_nm;
+        d.pressure_hpa = c.pressure_hpa; d.tau_r_input = c.tau_r_input;
+        d.n_water = c.n_water; d.wind = c.wind_speed; d.surface = c.surface;
+        d.sigma_type = c.sigma_type; d.q_conv = c.q_convention; d.decouple = c.decouple_sunglint;
+        d.nt = o.n_layers; d.M = o.fourier_m_max; d.max_orders = o.max_orders; d.tol = o.tolerance;
+        d.tau_r_source = o.tau_r_source; d.pssa = o.pssa; d.view_as_node = o.view_as_node;
+        d.aer_h_km = o.aer_h_km; d.profile = o.rayleigh_profile; d.ray_h_km = o.rayleigh_h_km;
+        d.nphi = o.n_phi_surface > 0 ? o.n_phi_surface : 1024;
+        d.mom_off = -1; d.L_aer = -1;
+        if (a && a->tau_a > 0.0) {
+            d.mom_off = (int)mb.size(); d.L_aer = a->L_max; d.tau_a = a->tau_a; d.ssa_a = a->ssa_a;
+            for (int l = 0; l <= a->L_max; ++l) {
+                mb.push_back(a->beta[l]); mgv.push_back(a->gamma[l]); ma.push_back(a->alpha[l]); mz.push_back(a->zeta[l]);
+            }
+        }
+        d.L = std::max(std::max(d.M, 2), d.L_aer);
+        d.lev_off = (long long)lev; lev += d.nt + 1;
+        d.coef_off = (long long)coef; coef += (size_t)d.nt * G.NR;
+        d.task0 = task;
+        g.hpix_task0.push_back(task);
+        for (int m = 0; m <= d.M; ++m) {
+            TaskDev t;
+            memset(&t, 0, sizeof(t));
+            t.pix = q; t.m = m; t.K = d.nt + 1; t.has_mol = m <= 2;
+            g.htask.push_back(t);
+        }
+        task += d.M + 1;
+        g.Lmax = std::max(g.Lmax, d.L);
+        g.Mmax = std::max(g.Mmax, d.M);
+        g.max_orders = std::max(g.max_orders, d.max_orders);
+        g.nphi = std::max(g.nphi, d.nphi);
+        const bool surf = c.surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN || c.surface == OCRT_SURFACE_FLAT;
+        const bool flat = c.surface == OCRT_SURFACE_FLAT || (c.surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && c.wind_speed <= 0.0);
+        g.any_rough |= surf && !flat;
+        g.any_flat |= flat;
+        g.any_pssa |= o.pssa != 0;
+        g.hpx.push_back(d);
+    }
+    g.T = task;
+    g.nlev = lev; g.ncoef = coef; g.nmom = mb.size();
+    // ---- waves of whole pixels under the workspace budget ----
+    const size_t budget = wave_budget_bytes();
+    const size_t op_elems = (size_t)G.CIN * G.LDO;
+    Wave w{0, 0, 0, 0, 0, 0, 0, 0, false, false};
+    size_t bytes = 0;
+    auto close = [&](int pend) {
+        w.p1 = pend;
+        w.t1 = pend < g.P ? g.hpx[pend].task0 : g.T;
+        g.waves.push_back(w);
+        g.wave_fld = std::max(g.wave_fld, w.fld); g.wave_ops = std::max(g.wave_ops, w.ops);
+        g.wave_srf = std::max(g.wave_srf, w.srf); g.wave_tasks = std::max(g.wave_tasks, w.t1 - w.t0);
+    };
+    for (int q = 0; q < g.P; ++q) {
+        const PixDev &d = g.hpx[q];
+        const size_t K = d.nt + 1, nm = d.M + 1;
+        const bool rough = (d.surface == 2 && d.wind > 0.0);
+        const size_t pf = nm * K * G.LDC;
+        const size_t po = (nm + std::min<size_t>(nm, 3)) * op_elems;
+        const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
+        const size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        if (q > w.p0 && bytes + pb > budget) {
+            close(q);
+            w = Wave{q, 0, d.task0, 0, 0, 0, 0, 0, false, false};
+            bytes = 0;
+        }
+        TaskDev *tk = &g.htask[d.task0];
+        for (size_t m = 0; m < nm; ++m) {
+            tk[m].fld_off = (long long)w.fld; w.fld += K * G.LDC;
+            tk[m].op_off = (long long)w.ops; w.ops += op_elems;
+            if (m <= 2) { tk[m].mol_off = (long long)w.ops; w.ops += op_elems; } else tk[m].mol_off = -1;
+            if (rough) { tk[m].srf_off = (long long)w.srf; w.srf += (size_t)G.NR * G.N * 9 + (size_t)G.NR * 9; }
+            else tk[m].srf_off = -1;
+            tk[m].has_mol = m <= 2;
+        }
+        w.Kmax = std::max(w.Kmax, (int)K);
+        w.any_rough |= rough;
+        w.any_flat |= (d.surface == 3 || (d.surface == 2 && d.wind <= 0.0));
+        bytes += pb;
+    }
+    close(g.P);
+    // ---- device buffers ----
+    int rc;
+    if ((rc = up(g.px, g.hpx)) || (rc = up(g.tasks, g.htask)) || (rc = up(g.pix_task0, g.hpix_task0)) ||
+        (rc = up(g.mb, mb)) || (rc = up(g.mg, mgv)) || (rc = up(g.ma, ma)) || (rc = up(g.mz, mz)) ||
+        (rc = alloc(g.state, g.T)) || (rc = alloc(g.tout, g.T)) || (rc = alloc(g.res, g.P)) ||
+        (rc = alloc(g.gmu, g.N)) || (rc = alloc(g.gw, g.N)) ||
+        (rc = alloc(g.h, g.nlev)) || (rc = alloc(g.ch, g.nlev)) || (rc = alloc(g.xd, g.nlev)) ||
+        (rc = alloc(g.yd, g.nlev)) || (rc = alloc(g.z, g.nlev)) ||
+        (rc = alloc(g.Tc, g.ncoef)) || (rc = alloc(g.Ca, g.ncoef)) || (rc = alloc(g.Cb, g.ncoef)) ||
+        (rc = alloc(g.Bp, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
+        (rc = alloc(g.Br, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
+        (rc = alloc(g.Bt, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
+        (rc = alloc(g.cs, (size_t)(g.Mmax + 1) * 2 * (g.nphi / 2))) ||
+        (rc = alloc(g.frs, (size_t)g.P * G.NR * 9)) ||
+        (rc = alloc(g.kappa, g.P)) || (rc = alloc(g.taudir, g.P)) ||
+        (rc = alloc(g.active_cnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.err, 1)) ||
+        (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) || (rc = alloc(g.Tot, g.wave_fld)) ||
+        (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
+        (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
+        (rc = alloc(g.srf, g.wave_srf)) ||
+        (rc = alloc(g.Bx, (size_t)g.wave_tasks * 6 * (g.Lmax + 1))))
+        return rc;
+    return OCRT_OK;
+}
+
+#define LAUNCH(plan, ...)                                                             \
+    do {                                                                              \
+        __VA_ARGS__;                                                                  \
+        (plan)->launches++;                                                           \
+        cudaError_t e_ = cudaGetLastError();                                          \
+        if (e_ != cudaSuccess) return fail(OCRT_ERR_DEVICE, std::string("launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
+{
+    const Geom G = g.G;
+    const int P = g.P;
+    CK(cudaMemsetAsync(g.err, 0, sizeof(int), st));
+    LAUNCH(plan, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw));
+    LAUNCH(plan, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
+    LAUNCH(plan, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
+    LAUNCH(plan, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
+    LAUNCH(plan, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
+    LAUNCH(plan, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
+    if (g.any_rough) LAUNCH(plan, k_cs_table<<<g.Mmax + 1, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
+    if (g.any_flat) LAUNCH(plan, k_flat_fresnel<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.frs));
+
+    BatchBufs B;
+    B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
+    B.gmu = g.gmu; B.gw = g.gw; B.h = g.h; B.ch = g.ch; B.xd = g.xd; B.yd = g.yd; B.z = g.z;
+    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.active_cnt = g.active_cnt; B.err = g.err;
+    WaveBufs W;
+    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.pvec = g.pvec;
+    W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
+    const int scan_threads = ((G.COUT + 31) / 32) * 32;
+    const int poll = 4;
+    for (const Wave &w : g.waves) {
+        const int nw = w.t1 - w.t0;
+        CK(cudaMemsetAsync(g.ops, 0, sizeof(float) * w.ops, st));
+        CK(cudaMemsetAsync(g.pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
+        if (g.any_flat) CK(cudaMemsetAsync(g.fvec, 0, sizeof(float) * (size_t)nw * 24 * G.NR, st));
+        CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+        LAUNCH(plan, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
+        LAUNCH(plan, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
+                                                   g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
+        if (w.any_rough) {
+            const size_t smem = sizeof(float) * 9 * (g.nphi / 2 + 1);
+            LAUNCH(plan, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
+                       g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.srf));
+        }
+        LAUNCH(plan, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+        const dim3 sgrid(nw, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
+        for (int it = 2; it <= g.max_orders; ++it) {
+            LAUNCH(plan, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
+            LAUNCH(plan, k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0, it));
+            if ((it - 1) % poll == 0 || it == g.max_orders) {
+                CK(cudaMemcpyAsync(g_pinned, g.active_cnt + it, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (*g_pinned == 0) break;
+            }
+        }
+        LAUNCH(plan, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
+    }
+    if (g.any_pssa) {
+        int maxnt = 0;
+        for (const PixDev &d : g.hpx) maxnt = std::max(maxnt, d.nt);
+        const size_t smem = sizeof(double) * (6 * (size_t)maxnt + 6) + sizeof(int) * ((size_t)maxnt + 1);
+        LAUNCH(plan, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.kappa, g.taudir));
+    }
+    LAUNCH(plan, k_finalize<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.state, g.tout, g.gmu, g.gw, g.h,
+                                                              g.kappa, g.taudir, g.res));
+    return OCRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+void ocrt_opts_default(ocrt_opts *o)
+{
+    if (!o) return;
+    o->n_mu = 24; o->n_layers = 40; o->fourier_m_max = 2; o->max_orders = 20; o->tolerance = 1e-7;
+    o->tau_r_source = OCRT_TAU_R_AUTO; o->pssa = 0; o->view_as_node = 1; o->aer_h_km = 2.0;
+    o->rayleigh_profile = OCRT_PROFILE_US62; o->rayleigh_h_km = 8.0; o->n_phi_surface = 1024;
+}
+
+void ocrt_case_default(ocrt_case *c)
+{
+    if (!c) return;
+    c->sza_deg = 40.0; c->vza_deg = 30.0; c->raa_deg = 90.0; c->wavelength_nm = 555.0;
+    c->surface = OCRT_SURFACE_BLACK; c->pressure_hpa = 1013.25; c->tau_r_input = 0.0;
+    c->n_water = 1.34; c->wind_speed = 0.0; c->sigma_type = 1; c->q_convention = 1; c->decouple_sunglint = 0;
+}
+
+int ocrt_gb_init(int device)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_device >= 0) return OCRT_OK;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) { cudaGetLastError(); return fail(OCRT_ERR_DEVICE, "no CUDA device"); }
+    if (device < 0 || device >= n) return fail(OCRT_ERR_ARGS, "device index out of range");
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&g_pinned, sizeof(int) * 16));
+    g_device = device;
+    return OCRT_OK;
+}
+
+void ocrt_gb_shutdown(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_device < 0) return;
+    cudaStreamSynchronize(g_stream);
+    for (auto &kv : g_free) cudaFree(kv.second);
+    for (auto &kv : g_live) cudaFree(kv.first);
+    g_free.clear(); g_live.clear();
+    cudaFreeHost(g_pinned); g_pinned = nullptr;
+    cudaStreamDestroy(g_stream); g_stream = nullptr;
+    g_device = -1;
+}
+
+const char *ocrt_gb_last_error(void) { return g_err.c_str(); }
+
+int ocrt_gb_plan_create(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
+                        const ocrt_aerosol *aer, int app, ocrt_plan **out)
+{
+    if (!out) return fail(OCRT_ERR_ARGS, "null plan pointer");
+    *out = nullptr;
+    if (n < 0 || (n > 0 && (!cases || !opts))) return fail(OCRT_ERR_ARGS, "bad batch arguments");
+    for (int i = 0; i < n; ++i) {
+        const int rc = validate(&cases[i], opp ? &opts[i] : &opts[0], aer ? (app ? &aer[i] : &aer[0]) : nullptr);
+        if (rc) return rc;
+    }
+    int rc = ensure_init();
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_mu);
+    ocrt_plan *plan = new ocrt_plan();
+    plan->n = n;
+    std::map<int, int> gid;
+    for (int i = 0; i < n; ++i) {
+        const int N = (opp ? opts[i] : opts[0]).n_mu;
+        auto it = gid.find(N);
+        if (it == gid.end()) { gid[N] = (int)plan->groups.size(); plan->groups.emplace_back(); plan->groups.back().N = N; it = gid.find(N); }
+        plan->groups[it->second].idx.push_back(i);
+    }
+    for (Group &g : plan->groups) {
+        rc = build_group(g, cases, opts, opp, aer, app);
+        if (rc) {
+            for (Group &h : plan->groups) free_group(h);
+            delete plan;
+            return rc;
+        }
+    }
+    if (cudaStreamSynchronize(g_stream) != cudaSuccess) {
+        for (Group &h : plan->groups) free_group(h);
+        delete plan;
+        return fail(OCRT_ERR_DEVICE, "upload failed");
+    }
+    *out = plan;
+    return OCRT_OK;
+}
+
+int ocrt_gb_plan_execute(ocrt_plan *plan, void *stream)
+{
+    if (!plan) return fail(OCRT_ERR_ARGS, "null plan");
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
+    plan->launches = 0;
+    for (Group &g : plan->groups) {
+        const int rc = run_group(plan, g, st);
+        if (rc) return rc;
+    }
+    return OCRT_OK;
+}
+
+int ocrt_gb_plan_results(ocrt_plan *plan, ocrt_result *out, void *stream)
+{
+    if (!plan || (!out && plan->n > 0)) return fail(OCRT_ERR_ARGS, "null plan or output");
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
+    double om = 0;
+    for (Group &g : plan->groups) {
+        std::vector<ocrt_result> r(g.P);
+        int err = 0;
+        CK(cudaMemcpyAsync(r.data(), g.res, sizeof(ocrt_result) * g.P, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&err, g.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (err) return fail(err, "non-finite field during the SOS iteration");
+        for (int q = 0; q < g.P; ++q) { out[g.idx[q]] = r[q]; om += r[q].order_modes; }
+    }
+    plan->order_modes = om;
+    return OCRT_OK;
+}
+
+int ocrt_gb_plan_stats(const ocrt_plan *plan, double *order_modes_total, long long *kernel_launches)
+{
+    if (!plan) return fail(OCRT_ERR_ARGS, "null plan");
+    if (order_modes_total) *order_modes_total = plan->order_modes;
+    if (kernel_launches) *kernel_launches = plan->launches;
+    return OCRT_OK;
+}
+
+void ocrt_gb_plan_destroy(ocrt_plan *plan)
+{
+    if (!plan) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_stream) cudaStreamSynchronize(g_stream);
+    for (Group &g : plan->groups) free_group(g);
+    delete plan;
+}
+
+int ocrt_gb_solve_batch(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
+                        const ocrt_aerosol *aer, int app, ocrt_result *out, void *stream)
+{
+    if (n == 0) return OCRT_OK;
+    if (!out) return fail(OCRT_ERR_ARGS, "null output");
+    ocrt_plan *plan = nullptr;
+    int rc = ocrt_gb_plan_create(n, cases, opts, opp, aer, app, &plan);
+    if (rc) return rc;
+    rc = ocrt_gb_plan_execute(plan, stream);
+    if (!rc) rc = ocrt_gb_plan_results(plan, out, stream);
+    ocrt_gb_plan_destroy(plan);
+    return rc;
+}
+
+int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                       ocrt_result *out, ocrt_diag *diag)
+{
+    if (!cs || !out) return fail(OCRT_ERR_ARGS, "null case or output");
+    ocrt_opts def;
+    if (!opts) { ocrt_opts_default(&def); opts = &def; }
+    ocrt_plan *plan = nullptr;
+    int rc = ocrt_gb_plan_create(1, cs, opts, 0, aer, 0, &plan);
+    if (rc) return rc;
+    rc = ocrt_gb_plan_execute(plan, nullptr);
+    if (!rc) rc = ocrt_gb_plan_results(plan, out, nullptr);
+    if (!rc && diag) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        Group &g = plan->groups[0];
+        std::vector<TaskState> st(g.T);
+        std::vector<TaskOut> to(g.T);
+        if (cudaMemcpy(st.data(), g.state, sizeof(TaskState) * g.T, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(to.data(), g.tout, sizeof(TaskOut) * g.T, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = fail(OCRT_ERR_DEVICE, "diagnostic copy failed");
+        else
+            for (int m = 0; m < g.T; ++m) {
+                if (diag->orders_per_m) diag->orders_per_m[m] = st[m].orders;
+                if (diag->residual_per_m) diag->residual_per_m[m] = st[m].resid;
+                if (diag->view_I_m) diag->view_I_m[m] = to[m].vI;
+                if (diag->view_Q_m) diag->view_Q_m[m] = to[m].vQ;
+                if (diag->view_U_m) diag->view_U_m[m] = to[m].vU;
+            }
+    }
+    ocrt_gb_plan_destroy(plan);
+    return rc;
+}
+
+} // extern "C"

@@ -1,0 +1,94 @@
+// common.cuh — device data model shared by the GB300 SOS kernels.
+//
+// Work decomposition: a batch holds P pixels that share the Gauss order N.
+// Every (pixel, Fourier mode m) pair is an independent SOS problem ("task").
+// Tasks are processed in waves sized to the workspace; a wave is a contiguous
+// pixel range, so all setup that is per pixel-and-mode is built per wave.
+//
+// Direction ring of a pixel (internal order, not the reference's sorted
+// order): slots 0..N-1 are the Gauss nodes in ascending mu, slot N is the
+// zero-weight view node when one is inserted (rt_angle_grid.c:37-73).
+// NR = N + 1 is the padded ring width.  Field columns:
+//     c = s * 2*NR + h * NR + g,   s in {I,Q,U}, h = 0 up / 1 down, g = slot
+// so the weighted (Gauss) inputs of the source contraction are six
+// contiguous blocks of N columns.  Field rows are levels k = 0 (TOA) .. nt.
+#pragma once
+#include <cstdint>
+
+#define OCRT_PI 3.14159265358979323846
+#define OCRT_MAX_N 64
+#define OCRT_MAX_M 255
+#define OCRT_DEPOL 0.0279
+#define OCRT_ZTOP_KM 100.0
+
+struct PixDev {
+    // ---- inputs (host) ----
+    double sza_deg, vza_deg, raa_deg, wavelength_nm;
+    double pressure_hpa, tau_r_input;
+    double tau_a, ssa_a, aer_h_km, ray_h_km;
+    double n_water, wind;
+    double tol;
+    int surface, sigma_type, q_conv, decouple;
+    int nt, M, L, L_aer, max_orders;
+    int tau_r_source, profile, pssa, view_as_node, nphi;
+    int mom_off;            // offset into the moment arrays, -1 without aerosol
+    int task0;              // first task of this pixel
+    long long lev_off;      // offset of level arrays (nt+1 entries)
+    long long coef_off;     // offset of transport coefficients (nt * NR entries)
+    // ---- derived on device (k_pixel_setup) ----
+    double mu0, mu_view, tau_r, tau_total;
+    int n_ring, view_slot;  // view_slot: ring slot holding mu_view, -1 = interpolate
+    int flat, rough, surf_on;
+    int pad_;
+};
+
+struct TaskDev {
+    int pix, m, K, has_mol;
+    long long fld_off;      // wave-relative offset of F/J/Tot (K * LDC entries)
+    long long op_off;       // wave-relative offset of the aerosol operator (6N * LDO)
+    long long mol_off;      // wave-relative offset of the molecular operator, -1 if none
+    long long srf_off;      // wave-relative offset of the surface kernels (NR*N*9 + NR*9), -1 if none
+};
+
+// Per-task mutable SOS state.
+struct TaskState {
+    int active, orders, converged, pad_;
+    double resid;
+};
+
+// Per-task extracted outputs (TOA view up, BOA down) for the finaliser.
+struct TaskOut {
+    double vI, vQ, vU;      // TOA upwelling at mu_view (seed removed)
+    double dn_view;         // BOA diffuse downward I at mu_view
+    double fdn;             // sum_g mu_g w_g I_dn(BOA, g): hemispheric diffuse flux / 2pi
+};
+
+struct Geom {
+    int N, NR, LDC, LDO;    // LDC: field row stride, LDO: operator row stride
+    int CIN;                // 6N weighted input columns
+    int COUT;               // 6NR output columns
+};
+
+__host__ __device__ inline Geom make_geom(int N)
+{
+    Geom g;
+    g.N = N;
+    g.NR = N + 1;
+    g.COUT = 6 * g.NR;
+    g.LDC = (g.COUT + 7) & ~7;
+    g.LDO = g.LDC;
+    g.CIN = 6 * N;
+    return g;
+}
+
+__host__ __device__ inline int col_of(const Geom &g, int s, int h, int slot)
+{
+    return s * 2 * g.NR + h * g.NR + slot;
+}
+
+// Input column (weighted Gauss direction) -> field column.
+__host__ __device__ inline int in_to_col(const Geom &g, int cin)
+{
+    const int blk = cin / g.N, gi = cin - blk * g.N;   // blk = s*2 + h
+    return blk * g.NR + gi;
+}

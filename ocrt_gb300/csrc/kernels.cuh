@@ -1,0 +1,59 @@
+// kernels.cuh — kernel declarations shared by the host orchestration.
+#pragma once
+#include "common.cuh"
+#include "../../include/ocrt_gb300.h"
+
+// setup.cu
+__global__ void k_gauss(int N, double *mu, double *w);
+__global__ void k_pixel_setup(PixDev *px, int P, int N, const double *gmu);
+__global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double *xd, double *yd, double *z);
+__global__ void k_level_mix(const PixDev *px, int P, const double *z, double *xd, double *yd);
+__global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const double *h,
+                       float *Tc, float *Ca, float *Cb);
+__global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt);
+__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx);
+__global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
+                         const float *Bp, const float *Br, const float *Bt, const float *Bx,
+                         const double *gw,
+                         const double *mb, const double *mg, const double *ma, const double *mz,
+                         float *ops, float *pvec, float *fvec);
+__global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
+                          Geom G, const double *gmu, const float *cs_tab, float *srf);
+__global__ void k_cs_table(int M, int nphi, float *cs);
+__global__ void k_flat_fresnel(const PixDev *px, int P, int N, const double *gmu, float *frs);
+
+// sos.cu
+#define ST_M_TILE 64
+#define ST_N_TILE 64
+struct WaveBufs {
+    float *F, *J;          // fields, wave-relative by TaskDev::fld_off
+    double *Tot;
+    float *ops;            // operators, wave-relative
+    float *pvec, *fvec;    // per wave-task primary and flat-beam vectors
+    float *srf;            // rough surface kernels, wave-relative
+};
+struct BatchBufs {
+    const PixDev *px;
+    const TaskDev *tasks;
+    TaskState *state;
+    TaskOut *tout;
+    const double *gmu, *gw;
+    const double *h, *ch, *xd, *yd, *z;
+    const float *Tc, *Ca, *Cb;
+    const float *frs;
+    int *active_cnt;       // [max_orders + 2]
+    int *err;              // device error word
+};
+
+__global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
+__global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
+__global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
+__global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks);
+
+// post.cu
+__global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
+                       const double *xd, const double *yd,
+                       const double *mb, double *kappa, double *tau_dir);
+__global__ void k_finalize(const PixDev *px, int P, const TaskState *state, const TaskOut *tout,
+                           const double *gmu, const double *gw, const double *h,
+                           const double *kappa, const double *tau_dir, ocrt_result *res);

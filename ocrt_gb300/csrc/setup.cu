@@ -1,0 +1,495 @@
+// setup.cu — per-batch and per-wave setup kernels.
+//
+//   k_gauss          Gauss-Legendre nodes, FP64 Newton       (rt_quadrature.c:20-61)
+//   k_pixel_setup    mu0, view slot, Rayleigh depth           (rt_solver.c:618-677)
+//   k_levels         h, ch, xdel, ydel, z per level, FP64     (rt_atm.c:177-400)
+//   k_coef           linear-source transport weights          (rt_layer_transport.c:36-99)
+//   k_basis_gauss    GSF basis at the Gauss nodes per m, FP64 (rt_angular_basis.c:126-276)
+//   k_basis_pix      GSF basis at -mu0 and mu_view per task, FP64
+//   k_tables         phase tables -> packed source operators  (rt_angular_basis.c:278-357,
+//                    rt_sos_operator.c:50-182, rt_primary_source.c:17-198)
+//   k_coxmunk        rough-surface Fourier kernels, all m     (shared/surface.c:514-909)
+//   k_flat_fresnel   flat-surface diagonal Mueller kernels    (rt_surface_boundary.c:86-103)
+#include "kernels.cuh"
+#include "physics.cuh"
+
+__global__ void k_gauss(int N, double *mu, double *w)
+{
+    const int k = threadIdx.x + 1;               // 1..N (largest root first)
+    if (k > N) return;
+    const int order = 2 * N;
+    double t = cos(OCRT_PI * ((double)k - 0.25) / ((double)order + 0.5));
+    double pn = 0, pm = 0, dp = 1;
+    for (int it = 0; it < 100; ++it) {
+        double a = 1.0, b = t;
+        for (int q = 1; q < order; ++q) { const double c = ((2.0 * q + 1.0) * t * b - (double)q * a) / (double)(q + 1); a = b; b = c; }
+        pn = b; pm = a;
+        dp = (double)order * (t * pn - pm) / (t * t - 1.0);
+        const double step = -pn / dp;
+        t += step;
+        if (fabs(step) < 1.0e-15 * (fabs(t) + 1.0)) break;
+    }
+    double a = 1.0, b = t;
+    for (int q = 1; q < order; ++q) { const double c = ((2.0 * q + 1.0) * t * b - (double)q * a) / (double)(q + 1); a = b; b = c; }
+    dp = (double)order * (t * b - a) / (t * t - 1.0);
+    mu[N - k] = t;
+    w[N - k] = 2.0 / ((1.0 - t * t) * dp * dp);
+}
+
+__global__ void k_pixel_setup(PixDev *px, int P, int N, const double *gmu)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    PixDev &d = px[p];
+    d.mu0 = cos(d.sza_deg * OCRT_PI / 180.0);
+    d.mu_view = cos(d.vza_deg * OCRT_PI / 180.0);
+    double tr;
+    if (!(d.pressure_hpa > 0.0)) tr = 0.0;
+    else if (d.tau_r_source == 1) tr = d.tau_r_input;
+    else tr = bodhaine_tau(d.wavelength_nm, d.pressure_hpa);
+    d.tau_r = tr;
+    d.tau_total = tr + (d.mom_off >= 0 ? d.tau_a : 0.0);
+    // view node: sorted insertion with de-duplication (rt_angle_grid.c:37-73)
+    d.view_slot = -1;
+    d.n_ring = N;
+    if (d.view_as_node) {
+        int lo = 0, hi = N;
+        while (lo < hi) { const int mid = (lo + hi) >> 1; if (gmu[mid] < d.mu_view) lo = mid + 1; else hi = mid; }
+        if (lo > 0 && fabs(gmu[lo - 1] - d.mu_view) < 1.0e-12) d.view_slot = lo - 1;
+        else if (lo < N && fabs(gmu[lo] - d.mu_view) < 1.0e-12) d.view_slot = lo;
+        else { d.view_slot = N; d.n_ring = N + 1; }
+    }
+    const int bfo = d.surface == 2, flat_s = d.surface == 3;
+    d.surf_on = bfo || flat_s;
+    d.flat = flat_s || (bfo && d.wind <= 0.0);
+    d.rough = d.surf_on && !d.flat;
+}
+
+// One thread per (pixel, level).  Altitude of each level by 64-step
+// bisection on the column above (rt_molecular_profile.c:84-105, rt_atm.c:313-355);
+// every level brackets [0, 100 km] independently.
+__global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double *xd, double *yd, double *z)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    const int nt = d.nt;
+    const double tau = d.tau_total, tr = d.tau_r;
+    const int aer = d.mom_off >= 0 && d.tau_a > 0.0;
+    const double ta = aer ? d.tau_a : 0.0;
+    const double ah = d.aer_h_km > 0.0 ? d.aer_h_km : 2.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= nt; k += gridDim.x * blockDim.x) {
+        const long long o = d.lev_off + k;
+        const double hk = (double)k * tau / (double)nt;
+        h[o] = hk;
+        ch[o] = 0.5 * exp(-hk / d.mu0);
+        double zk;
+        if (k == 0) zk = OCRT_ZTOP_KM;
+        else if (k == nt && aer) zk = 0.0;
+        else {
+            const double ztop = (!aer && d.profile == 0) ? 84.852 : OCRT_ZTOP_KM;
+            const double f = hk / tau;
+            if (!aer && f >= 1.0) zk = 0.0;
+            else {
+                double lo = 0.0, hi = aer ? OCRT_ZTOP_KM : ztop;
+                for (int it = 0; it < 64; ++it) {
+                    const double mid = 0.5 * (lo + hi);
+                    const double above = aer ? tr * ray_above(mid, d.profile, d.ray_h_km) +
+                                                   ta * exp_above(mid, OCRT_ZTOP_KM, ah)
+                                             : ray_above(mid, d.profile, d.ray_h_km);
+                    const double target = aer ? hk : f;
+                    if (above > target) lo = mid; else hi = mid;
+                }
+                zk = 0.5 * (lo + hi);
+            }
+        }
+        z[o] = zk;
+        double x = 0.0, y = 1.0;
+        if (aer) {
+            if (k == 0) { x = tr == 0.0 ? d.ssa_a : 0.0; y = tr == 0.0 ? 0.0 : 1.0; }
+        }
+        xd[o] = x;
+        yd[o] = y;
+    }
+}
+
+// Layer scattering fractions once every level altitude is known.
+__global__ void k_level_mix(const PixDev *px, int P, const double *z, double *xd, double *yd)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    if (!(d.mom_off >= 0 && d.tau_a > 0.0)) return;
+    const double tr = d.tau_r, ta = d.tau_a, ah = d.aer_h_km > 0.0 ? d.aer_h_km : 2.0;
+    for (int k = 1 + blockIdx.x * blockDim.x + threadIdx.x; k <= d.nt; k += gridDim.x * blockDim.x) {
+        const long long o = d.lev_off + k;
+        const double zj = z[o], zp = z[o - 1];
+        const double rj = tr * ray_above(zj, d.profile, d.ray_h_km);
+        const double aj = ta * exp_above(zj, OCRT_ZTOP_KM, ah);
+        const double rp = k == 1 ? 0.0 : tr * ray_above(zp, d.profile, d.ray_h_km);
+        const double ap = k == 1 ? 0.0 : ta * exp_above(zp, OCRT_ZTOP_KM, ah);
+        const double dr = rj - rp, da = aj - ap, dt = dr + da;
+        if (dt > 0.0) { xd[o] = da * d.ssa_a / dt; yd[o] = dr / dt; }
+        else { xd[o] = 0.0; yd[o] = tr > 0.0 ? 1.0 : 0.0; }
+    }
+}
+
+// Transport weights per (pixel, layer, ring slot):
+//   I_k = T I_up + Ca J_k + Cb J_up,  G = (1-T)|mu|/dtau - T, Ca = (1-T-G)/2, Cb = G/2
+// (the reference's slope/intercept form of rt_layer_transport.c:89-99 expanded,
+// which keeps every weight non-negative).  Computed in FP64, stored FP32.
+__global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const double *h,
+                       float *Tc, float *Ca, float *Cb)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    const int NR = N + 1;
+    const int total = d.nt * NR;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int layer = e / NR, g = e - layer * NR;
+        const long long o = d.coef_off + e;
+        double am = g < N ? gmu[g] : d.mu_view;
+        if (g >= d.n_ring) am = 1.0;
+        const double dtau = h[d.lev_off + layer + 1] - h[d.lev_off + layer];
+        const double x = dtau / am;
+        const double T = exp(-x);
+        const double G = -expm1(-x) / x - T;
+        Tc[o] = (float)T;
+        Ca[o] = (float)(0.5 * (1.0 - T - G));
+        Cb[o] = (float)(0.5 * G);
+    }
+}
+
+// GSF basis at the Gauss nodes for every mode: B[(m*(L+1) + l)*N + g], 3 arrays.
+__global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt)
+{
+    const int m = blockIdx.x, g = threadIdx.x;
+    if (m > M || g >= N) return;
+    const size_t base = (size_t)m * (L + 1) * N;
+    gsf_recur(L, m, gmu[g], [&](int l, double P, double R, double T) {
+        Bp[base + (size_t)l * N + g] = (float)P;
+        Br[base + (size_t)l * N + g] = (float)R;
+        Bt[base + (size_t)l * N + g] = (float)T;
+    });
+}
+
+// GSF basis at the solar direction (-mu0) and at mu_view for every task of a
+// wave: Bx[((t*2 + which)*3 + comp)*(L+1) + l].
+__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx)
+{
+    const int tl = blockIdx.x * (blockDim.x / 2) + threadIdx.x / 2;
+    const int which = threadIdx.x & 1;
+    if (tl >= nt_tasks) return;
+    const TaskDev tk = tasks[t0 + tl];
+    const PixDev &d = px[tk.pix];
+    const double x = which == 0 ? -d.mu0 : d.mu_view;
+    float *dst = Bx + ((size_t)tl * 2 + which) * 3 * (L + 1);
+    for (int l = 0; l <= L; ++l) { dst[l] = 0.f; dst[L + 1 + l] = 0.f; dst[2 * (L + 1) + l] = 0.f; }
+    gsf_recur(d.L, tk.m, x, [&](int l, double P, double R, double T) {
+        dst[l] = (float)P; dst[L + 1 + l] = (float)R; dst[2 * (L + 1) + l] = (float)T;
+    });
+}
+
+// Writes the 36 operator entries of one (outgoing o, incoming Gauss i) pair
+// from the 18 direction-pair coefficients of rt_sos_operator.c:54-72
+// (order: ii_s ii_c iu_s iu_c iuT_s iuT_c iq_s iq_c iqT_s iqT_c qq_s qq_c
+//  qu_s qu_c quT_s quT_c uu_s uu_c), with the quadrature weight folded in.
+// The signs are those of the contraction in rt_sos_operator.c:387-406.
+__device__ inline void put_pair(float *A, const Geom &G, int o, int i, float w, const float *c)
+{
+    enum { II_S, II_C, IU_S, IU_C, IUT_S, IUT_C, IQ_S, IQ_C, IQT_S, IQT_C, QQ_S, QQ_C,
+           QU_S, QU_C, QUT_S, QUT_C, UU_S, UU_C };
+    auto at = [&](int so, int ho, int si, int hi) -> float & {
+        const int cin = (si * 2 + hi) * G.N + i;
+        return A[(size_t)cin * G.LDO + col_of(G, so, ho, o)];
+    };
+    // I up / down
+    at(0, 0, 0, 0) = w * c[II_S];   at(0, 0, 1, 0) = w * c[IQT_S];  at(0, 0, 2, 0) = -w * c[IUT_S];
+    at(0, 0, 0, 1) = w * c[II_C];   at(0, 0, 1, 1) = w * c[IQT_C];  at(0, 0, 2, 1) = -w * c[IUT_C];
+    at(0, 1, 0, 0) = w * c[II_C];   at(0, 1, 1, 0) = w * c[IQT_C];  at(0, 1, 2, 0) = w * c[IUT_C];
+    at(0, 1, 0, 1) = w * c[II_S];   at(0, 1, 1, 1) = w * c[IQT_S];  at(0, 1, 2, 1) = w * c[IUT_S];
+    // Q up / down
+    at(1, 0, 0, 0) = w * c[IQ_S];   at(1, 0, 1, 0) = w * c[QQ_S];   at(1, 0, 2, 0) = -w * c[QU_S];
+    at(1, 0, 0, 1) = w * c[IQ_C];   at(1, 0, 1, 1) = w * c[QQ_C];   at(1, 0, 2, 1) = w * c[QU_C];
+    at(1, 1, 0, 0) = w * c[IQ_C];   at(1, 1, 1, 0) = w * c[QQ_C];   at(1, 1, 2, 0) = -w * c[QU_C];
+    at(1, 1, 0, 1) = w * c[IQ_S];   at(1, 1, 1, 1) = w * c[QQ_S];   at(1, 1, 2, 1) = w * c[QU_S];
+    // U up / down (leading minus of rt_sos_operator.c:399-406 folded in)
+    at(2, 0, 0, 0) = -w * c[IU_S];  at(2, 0, 1, 0) = -w * c[QUT_S]; at(2, 0, 2, 0) = w * c[UU_S];
+    at(2, 0, 0, 1) = w * c[IU_C];   at(2, 0, 1, 1) = -w * c[QUT_C]; at(2, 0, 2, 1) = w * c[UU_C];
+    at(2, 1, 0, 0) = -w * c[IU_C];  at(2, 1, 1, 0) = w * c[QUT_C];  at(2, 1, 2, 0) = w * c[UU_C];
+    at(2, 1, 0, 1) = w * c[IU_S];   at(2, 1, 1, 1) = w * c[QUT_S];  at(2, 1, 2, 1) = w * c[UU_S];
+}
+
+// One block per task.  Phase tables by contraction over l in FP32 with the
+// even/odd parity split giving the mirrored columns; then the packed aerosol
+// operator (and molecular operator for m <= 2), the primary-source vectors and
+// the flat-surface reflected-beam vectors.
+__global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
+                         const float *Bp, const float *Br, const float *Bt, const float *Bx,
+                         const double *gw,
+                         const double *mb, const double *mg, const double *ma, const double *mz,
+                         float *ops, float *pvec, float *fvec)
+{
+    const int tl = blockIdx.x;
+    if (tl >= nt_tasks) return;
+    const TaskDev tk = tasks[t0 + tl];
+    const PixDev &d = px[tk.pix];
+    const int m = tk.m, N = G.N, n = d.n_ring, Lp = d.L;
+    const int aer = d.mom_off >= 0 && d.tau_a > 0.0;
+    const int La = aer ? d.L_aer : -1;
+    const float *bx = Bx + (size_t)tl * 2 * 3 * (L + 1);        // [which][comp][l]
+    const size_t gb = (size_t)m * (L + 1) * N;
+    const int vs = d.view_slot;
+    // basis accessor: slot s in 0..N-1 Gauss, s == N view, s == -1 solar
+    auto basis = [&](int comp, int s, int l) -> float {
+        if (s < 0) return bx[(size_t)(0 * 3 + comp) * (L + 1) + l];
+        if (s >= N) return bx[(size_t)(1 * 3 + comp) * (L + 1) + l];
+        const float *B = comp == 0 ? Bp : (comp == 1 ? Br : Bt);
+        return B[gb + (size_t)l * N + s];
+    };
+    // molecular l = 2 basis with mirror parity p(-x) = (-1)^m p(x), t(-x) = -(-1)^m t(x)
+    const float par = (m & 1) ? -1.f : 1.f;
+    const double A = 2.0 * (1.0 - OCRT_DEPOL) / (2.0 + OCRT_DEPOL);
+    const float b0 = m == 0 ? 1.f : 0.f, b2 = (float)(0.5 * A), g2 = (float)(-A * sqrt(1.5)), a2 = (float)(3.0 * A);
+    const int mol = m <= 2;
+    float *Aop = ops + tk.op_off;
+    float *Bop = tk.mol_off >= 0 ? ops + tk.mol_off : nullptr;
+
+    // ---- operator pairs (o ring slot, i Gauss) ----
+    for (int e = threadIdx.x; e < n * N; e += blockDim.x) {
+        const int o = e / N, i = e - o * N;
+        const int os = o;    // ring slot (the view node, when inserted, is slot N)
+        // accumulators: [row i, col o] products, even (E) / odd (O) in l+m
+        float E[9] = {0}, O[9] = {0}, Et[4] = {0}, Ot[4] = {0};
+        for (int l = m; l <= Lp; ++l) {
+            const float be = l <= La ? (float)mb[d.mom_off + l] : 0.f;
+            const float ga = l <= La ? (float)mg[d.mom_off + l] : 0.f;
+            const float al = l <= La ? (float)ma[d.mom_off + l] : 0.f;
+            const float ze = l <= La ? (float)mz[d.mom_off + l] : 0.f;
+            const float Pi = basis(0, i, l), Ri = basis(1, i, l), Ti = basis(2, i, l);
+            const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
+            float v[9] = {Pi * Po * be, Pi * Ro * ga, Pi * To * ga, Ti * To * ze, Ri * Ro * al,
+                          Ti * Ro * al, Ri * To * ze, Ti * To * al, Ri * Ro * ze};
+            float vt[4] = {Po * Ti * ga, Po * Ri * ga, To * Ri * al, Ro * Ti * ze};
+            if (((l + m) & 1) == 0) {
+#pragma unroll
+                for (int q = 0; q < 9; ++q) E[q] += v[q];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) Et[q] += vt[q];
+            } else {
+#pragma unroll
+                for (int q = 0; q < 9; ++q) O[q] += v[q];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) Ot[q] += vt[q];
+            }
+        }
+        float S[9], D[9], St[4], Dt[4];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) { S[q] = E[q] + O[q]; D[q] = E[q] - O[q]; }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { St[q] = Et[q] + Ot[q]; Dt[q] = Et[q] - Ot[q]; }
+        // tables: value at +col = S, at -col = sigma * D with sigma from the column basis
+        float c[18];
+        c[0] = S[0];             c[1] = D[0];               // pfm[i][+-o]
+        c[2] = S[2];             c[3] = -D[2];              // gt[i][+-o]
+        c[4] = St[0];            c[5] = -Dt[0];             // gt[o][+-i]
+        c[6] = S[1];             c[7] = D[1];               // gr[i][+-o]
+        c[8] = St[1];            c[9] = Dt[1];              // gr[o][+-i]
+        c[10] = S[3] + S[4];     c[11] = -D[3] + D[4];      // arr[i][+-o]
+        c[12] = S[5] + S[6];     c[13] = D[5] - D[6];       // art[i][+-o]
+        c[14] = St[2] + St[3];   c[15] = Dt[2] - Dt[3];     // art[o][+-i]
+        c[16] = S[7] + S[8];     c[17] = -D[7] + D[8];      // att[i][+-o]
+        const float w = (float)gw[i];
+        put_pair(Aop, G, os, i, w, c);
+        if (Bop && mol) {
+            const float pi = basis(0, i, 2), ri = basis(1, i, 2), ti = basis(2, i, 2);
+            const float po = basis(0, os, 2), ro = basis(1, os, 2), to = basis(2, os, 2);
+            const float pmo = par * po, rmo = par * ro, tmo = -par * to;    // at -o
+            const float pmi = par * pi, rmi = par * ri, tmi = -par * ti;    // at -i
+            (void)pmi;
+            float cm[18];
+            cm[0] = b0 + b2 * pi * po;  cm[1] = b0 + b2 * pi * pmo;
+            cm[2] = g2 * pi * to;       cm[3] = g2 * pi * tmo;
+            cm[4] = g2 * po * ti;       cm[5] = g2 * po * tmi;
+            cm[6] = g2 * pi * ro;       cm[7] = g2 * pi * rmo;
+            cm[8] = g2 * po * ri;       cm[9] = g2 * po * rmi;
+            cm[10] = a2 * ri * ro;      cm[11] = a2 * ri * rmo;
+            cm[12] = a2 * ti * ro;      cm[13] = a2 * ti * rmo;
+            cm[14] = a2 * to * ri;      cm[15] = a2 * to * rmi;
+            cm[16] = a2 * ti * to;      cm[17] = a2 * ti * tmo;
+            put_pair(Bop, G, os, i, w, cm);
+        }
+    }
+
+    // ---- solar row: primary-source vectors and flat reflected-beam vectors ----
+    // pvec[tl][2][LDC]: [0] aerosol part, [1] molecular part of J1 / (ch * fraction)
+    float *pv = pvec + (size_t)tl * 2 * G.LDC;
+    float *fv = fvec ? fvec + (size_t)tl * 2 * 2 * 6 * G.NR : nullptr;   // [side][aer/mol][6][NR]
+    for (int o = threadIdx.x; o < n; o += blockDim.x) {
+        const int os = o;
+        float E[6] = {0}, O[6] = {0};      // PP b, PR g, PT g, TT z, RR a, TR a | plus transposed pair
+        float Ex[3] = {0}, Ox[3] = {0};    // RT z, TT a, RR z
+        float Ey[2] = {0}, Oy[2] = {0};    // P_o R_0 g  (gr pair),  T_o R_0 a + R_o T_0 z (art pair)
+        for (int l = m; l <= Lp; ++l) {
+            const float be = l <= La ? (float)mb[d.mom_off + l] : 0.f;
+            const float ga = l <= La ? (float)mg[d.mom_off + l] : 0.f;
+            const float al = l <= La ? (float)ma[d.mom_off + l] : 0.f;
+            const float ze = l <= La ? (float)mz[d.mom_off + l] : 0.f;
+            const float P0 = basis(0, -1, l), R0 = basis(1, -1, l), T0 = basis(2, -1, l);
+            const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
+            const float v[6] = {P0 * Po * be, P0 * Ro * ga, P0 * To * ga, T0 * To * ze, R0 * Ro * al, T0 * Ro * al};
+            const float vx[3] = {R0 * To * ze, T0 * To * al, R0 * Ro * ze};
+            const float vy[2] = {Po * R0 * ga, To * R0 * al + Ro * T0 * ze};
+            const bool ev = ((l + m) & 1) == 0;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) (ev ? E[q] : O[q]) += v[q];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) (ev ? Ex[q] : Ox[q]) += vx[q];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) (ev ? Ey[q] : Oy[q]) += vy[q];
+        }
+        // row 0 (solar) tables at column +o (S) and -o (sigma D)
+        const float pfmP = E[0] + O[0], pfmM = E[0] - O[0];
+        const float grP = E[1] + O[1], grM = E[1] - O[1];
+        const float gtP = E[2] + O[2], gtM = -(E[2] - O[2]);
+        const float arrP = (E[3] + O[3]) + (E[4] + O[4]), arrM = -(E[3] - O[3]) + (E[4] - O[4]);
+        // primary source (rt_primary_source.c:59-77, 163-177), U sign folded in
+        const float p0 = basis(0, -1, 2);
+        const float po = basis(0, os, 2), ro = basis(1, os, 2), to = basis(2, os, 2);
+        const float pmo = par * po, rmo = par * ro, tmo = -par * to;
+        pv[col_of(G, 0, 0, os)] = pfmP;  pv[col_of(G, 0, 1, os)] = pfmM;
+        pv[col_of(G, 1, 0, os)] = grP;   pv[col_of(G, 1, 1, os)] = grM;
+        pv[col_of(G, 2, 0, os)] = -gtP;  pv[col_of(G, 2, 1, os)] = -gtM;
+        float *pm = pv + G.LDC;
+        pm[col_of(G, 0, 0, os)] = b0 + b2 * po * p0;
+        pm[col_of(G, 0, 1, os)] = b0 + b2 * pmo * p0;
+        pm[col_of(G, 1, 0, os)] = mol ? g2 * ro * p0 : 0.f;
+        pm[col_of(G, 1, 1, os)] = mol ? g2 * rmo * p0 : 0.f;
+        pm[col_of(G, 2, 0, os)] = mol ? -g2 * to * p0 : 0.f;
+        pm[col_of(G, 2, 1, os)] = mol ? -g2 * tmo * p0 : 0.f;
+        if (fv) {
+            // flat-surface reflected beam kernels (rt_surface_boundary.c:246-360):
+            // side 0 ("top", upward outputs) uses column -o, side 1 uses +o.
+            // comps: P, R, T, RT(transpose gr), RR, TR(transpose art)
+            const float r0 = basis(1, -1, 2);
+            const float gyP = Ey[0] + Oy[0], gyM = Ey[0] - Oy[0];          // P_o R0 g: col basis P_o -> sigma +
+            // T_o R0 a (sigma -) + R_o T0 z (sigma +): need separate parity -> recompute below
+            float tr_p = 0.f, tr_m = 0.f;
+            {
+                float e1 = 0, o1 = 0, e2 = 0, o2 = 0;
+                for (int l = m; l <= Lp; ++l) {
+                    const float al = l <= La ? (float)ma[d.mom_off + l] : 0.f;
+                    const float ze = l <= La ? (float)mz[d.mom_off + l] : 0.f;
+                    const float a1 = basis(2, os, l) * basis(1, -1, l) * al;
+                    const float a2_ = basis(1, os, l) * basis(2, -1, l) * ze;
+                    if (((l + m) & 1) == 0) { e1 += a1; e2 += a2_; } else { o1 += a1; o2 += a2_; }
+                }
+                tr_p = (e1 + o1) + (e2 + o2);
+                tr_m = -(e1 - o1) + (e2 - o2);
+            }
+            for (int side = 0; side < 2; ++side) {
+                const bool neg = side == 0;
+                float *fa = fv + ((size_t)(side * 2 + 0) * 6) * G.NR;
+                float *fm = fv + ((size_t)(side * 2 + 1) * 6) * G.NR;
+                fa[0 * G.NR + os] = neg ? pfmM : pfmP;
+                fa[1 * G.NR + os] = neg ? grM : grP;
+                fa[2 * G.NR + os] = neg ? gtM : gtP;
+                fa[3 * G.NR + os] = neg ? gyM : gyP;
+                fa[4 * G.NR + os] = neg ? arrM : arrP;
+                fa[5 * G.NR + os] = neg ? tr_m : tr_p;
+                const float pd = neg ? pmo : po, rd = neg ? rmo : ro, td = neg ? tmo : to;
+                fm[0 * G.NR + os] = mol ? b0 + b2 * pd * p0 : 0.f;
+                fm[1 * G.NR + os] = mol ? g2 * rd * p0 : 0.f;
+                fm[2 * G.NR + os] = mol ? g2 * td * p0 : 0.f;
+                fm[3 * G.NR + os] = mol ? g2 * r0 * pd : 0.f;
+                fm[4 * G.NR + os] = mol ? a2 * r0 * rd : 0.f;
+                fm[5 * G.NR + os] = mol ? a2 * td * r0 : 0.f;
+            }
+        }
+    }
+}
+
+// Rough-surface Fourier kernels for one (pixel, outgoing slot o, incoming
+// slot i) per block, all modes at once.  Incoming slot N is the sun.
+// Mueller values on the azimuth grid in FP32 (half grid: the mirror symmetry
+// phi -> 2pi - phi flips exactly the sin entries), projection onto cos/sin
+// mphi in FP32, normalisation dphi/(2pi or pi) and the m>0 IU/QU sign of
+// shared/surface.c:896-906 applied at the end.
+__global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
+                          Geom G, const double *gmu, const float *cs_tab, float *srf)
+{
+    extern __shared__ float sm_R[];                 // [9][nphi/2 + 1]
+    const int p = p0 + blockIdx.z;
+    const PixDev &d = px[p];
+    if (!d.rough) return;
+    const int o = blockIdx.y, i = blockIdx.x;       // o: 0..NR-1, i: 0..N (N = sun)
+    if (o >= d.n_ring) return;
+    const int N = G.N;
+    const int os = o;
+    const double mo = os < N ? gmu[os] : d.mu_view;
+    const double mi = i < N ? gmu[i] : d.mu0;
+    const double s2v = slope_variance(d.wind, d.sigma_type);
+    const double lam = sancer_lambda(mi, sqrt(s2v)) + sancer_lambda(mo, sqrt(s2v));
+    const int nphi = d.nphi, half = nphi / 2, hs = half + 1;
+    const double dphi = 2.0 * OCRT_PI / (double)nphi;
+    for (int q = threadIdx.x; q < half; q += blockDim.x) {
+        const double phi = (q + 0.5) * dphi;
+        float R[9];
+        coxmunk_R<float>((float)mo, (float)mi, (float)cos(phi), (float)sin(phi), (float)s2v, (float)lam,
+                         (float)d.n_water, d.q_conv, R);
+#pragma unroll
+        for (int e = 0; e < 9; ++e) sm_R[e * hs + q] = R[e];
+    }
+    __syncthreads();
+    const int M = d.M;
+    const int nout = (M + 1) * 9;
+    const int task_first = pix_task0[p];
+    for (int e2 = threadIdx.x; e2 < nout; e2 += blockDim.x) {
+        const int m = e2 / 9, e = e2 - m * 9;
+        const bool is_cos = (e == 0 || e == 1 || e == 3 || e == 4 || e == 8);
+        const float *tab = cs_tab + ((size_t)m * 2 + (is_cos ? 0 : 1)) * half;
+        const float *rv = sm_R + e * hs;
+        float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+        int q = 0;
+        for (; q + 3 < half; q += 4) {
+            acc0 += rv[q] * tab[q]; acc1 += rv[q + 1] * tab[q + 1];
+            acc2 += rv[q + 2] * tab[q + 2]; acc3 += rv[q + 3] * tab[q + 3];
+        }
+        for (; q < half; ++q) acc0 += rv[q] * tab[q];
+        double v = 2.0 * (((double)acc0 + (double)acc1) + ((double)acc2 + (double)acc3));
+        v *= dphi * (m == 0 ? 1.0 / (2.0 * OCRT_PI) : 1.0 / OCRT_PI);
+        if (m > 0 && (e == 2 || e == 5)) v = -v;
+        const TaskDev &tk = tasks[task_first + m];
+        float *dst = srf + tk.srf_off;
+        if (i < N) dst[((size_t)os * N + i) * 9 + e] = (float)v;
+        else dst[(size_t)G.NR * N * 9 + (size_t)os * 9 + e] = (float)v;
+    }
+}
+
+// cos / sin(m phi_q) on the half azimuth grid, FP64 evaluated.
+__global__ void k_cs_table(int M, int nphi, float *cs)
+{
+    const int half = nphi / 2;
+    const int m = blockIdx.x;
+    const double dphi = 2.0 * OCRT_PI / (double)nphi;
+    for (int q = threadIdx.x; q < half; q += blockDim.x) {
+        const double phi = (q + 0.5) * dphi;
+        cs[((size_t)m * 2 + 0) * half + q] = (float)cos(m * phi);
+        cs[((size_t)m * 2 + 1) * half + q] = (float)sin(m * phi);
+    }
+}
+
+// Flat Fresnel Mueller per ring slot of every pixel: frs[(p*NR + slot)*9].
+__global__ void k_flat_fresnel(const PixDev *px, int P, int N, const double *gmu, float *frs)
+{
+    const int p = blockIdx.x, s = threadIdx.x;
+    if (p >= P || s > N) return;
+    const PixDev &d = px[p];
+    if (!d.flat || s >= d.n_ring) return;
+    const int os = s;
+    const double mu = os < N ? gmu[os] : d.mu_view;
+    double M[9];
+    fresnel_R<double>(mu, d.n_water, d.q_conv, M);
+    for (int e = 0; e < 9; ++e) frs[((size_t)p * (N + 1) + os) * 9 + e] = (float)M[e];
+}

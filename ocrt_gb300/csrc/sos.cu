@@ -1,0 +1,343 @@
+// sos.cu — the successive-orders loop on the GPU.
+//
+//   k_primary      direct-beam source (rt_primary_source.c:17-198), flat-surface
+//                  reflected-beam source (rt_surface_boundary.c:210-428) and the
+//                  rough direct-beam seed (rt_surface_boundary.c:430-493), then
+//                  the formal solution of order 1 (rt_layer_transport.c:107-208).
+//   k_source_simt  multiple-scattering source J = x*(A F) + y*(B F) over all levels
+//                  (rt_sos_operator.c:206-424) as a tiled FP32 GEMM on CUDA cores.
+//   k_scan         surface boundary condition (rt_surface_boundary.c:137-208),
+//                  up/down formal solution, FP64 order totals, sup-norm residual and
+//                  the convergence test (rt_solver.c:2923-3150).
+//   k_extract      TOA view sample and BOA downward samples (rt_solver.c:1010-1076).
+#include "kernels.cuh"
+#include "physics.cuh"
+
+__device__ inline void decode_col(const Geom &G, int c, int &s, int &h, int &g)
+{
+    s = c / (2 * G.NR);
+    const int r = c - s * 2 * G.NR;
+    h = r / G.NR;
+    g = r - h * G.NR;
+}
+
+__device__ inline double ring_mu(const PixDev &d, const double *gmu, int N, int g)
+{
+    return g < N ? gmu[g] : d.mu_view;
+}
+
+// Rough direct-beam seed at level k for upward slot g, Stokes s (FP64).
+__device__ inline double rough_seed(const PixDev &d, const TaskDev &tk, const WaveBufs &W, const Geom &G,
+                                    const double *gmu, double hk, int g, int s)
+{
+    const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * G.N * 9;
+    const double tdn = exp(-d.tau_total / d.mu0);
+    const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
+    return fs * tdn * exp(-(d.tau_total - hk) / ring_mu(d, gmu, G.N, g)) * (double)Rs[g * 9 + s * 3];
+}
+
+__global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
+{
+    const int tl = blockIdx.x, tg = t0 + tl;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int c = threadIdx.x;
+    if (c == 0) {
+        TaskState st;
+        st.orders = 1;
+        st.active = d.max_orders > 1;
+        st.converged = d.max_orders <= 1;
+        st.pad_ = 0;
+        st.resid = 0.0;
+        B.state[tg] = st;
+    }
+    if (c >= G.COUT) return;
+    int s, h, g;
+    decode_col(G, c, s, h, g);
+    if (g >= d.n_ring) return;
+    const int nt = d.nt;
+    const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
+    const double aP = pv[c], mP = pv[G.LDC + c];
+    float *F = W.F + tk.fld_off;
+    double *Tot = W.Tot + tk.fld_off;
+    const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off, *hh = B.h + d.lev_off;
+    const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+    const int NR = G.NR;
+    // flat reflected beam: Stokes s uses kernel components (s, s+3)
+    double RI = 0, RQ = 0, sb = 0, fa1 = 0, fa2 = 0, fm1 = 0, fm2 = 0;
+    if (d.flat) {
+        const double n2 = d.n_water * d.n_water, mu0 = d.mu0;
+        const double tn = sqrt(n2 - 1.0 + mu0 * mu0);
+        const double rp = (n2 * mu0 - tn) / (n2 * mu0 + tn), rs = (mu0 - tn) / (mu0 + tn);
+        RI = (rp * rp + rs * rs) / 2.0;
+        RQ = d.q_conv == 1 ? (rp * rp - rs * rs) / 2.0 : (rs * rs - rp * rp) / 2.0;
+        sb = 0.5 * exp(-2.0 * d.tau_total / mu0);
+        const int side = h == 0 ? 0 : 1;
+        const float *fv = W.fvec + (size_t)tl * 2 * 2 * 6 * NR;
+        const float *fa = fv + (size_t)(side * 2 + 0) * 6 * NR;
+        const float *fm = fv + (size_t)(side * 2 + 1) * 6 * NR;
+        fa1 = fa[s * NR + g]; fa2 = fa[(s + 3) * NR + g];
+        fm1 = fm[s * NR + g]; fm2 = fm[(s + 3) * NR + g];
+    }
+    int bad = 0;
+    auto Jat = [&](int k) -> float {
+        const double x = xd[k], y = yd[k];
+        double v = ch[k] * (x * aP + y * mP);
+        if (d.flat && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
+            const double beam = sb * exp(hh[k] / d.mu0);
+            v += beam * (RI * (x * fa1 + y * fm1) + RQ * (x * fa2 + y * fm2));
+        }
+        if (!isfinite(v)) bad = 1;
+        return (float)v;
+    };
+    auto store = [&](int k, float I) {
+        double seed = 0.0;
+        if (d.rough && h == 0) seed = rough_seed(d, tk, W, G, B.gmu, hh[k], g, s);
+        F[(size_t)k * G.LDC + c] = (float)((double)I + seed);
+        Tot[(size_t)k * G.LDC + c] = (double)I + seed;
+    };
+    if (h == 0) {
+        float Jn = Jat(nt), I = 0.f;
+        store(nt, I);
+        for (int k = nt - 1; k >= 0; --k) {
+            const float Jk = Jat(k);
+            const int e = k * NR + g;
+            I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jn;
+            store(k, I);
+            Jn = Jk;
+        }
+    } else {
+        float Jp = Jat(0), I = 0.f;
+        store(0, I);
+        for (int k = 1; k <= nt; ++k) {
+            const float Jk = Jat(k);
+            const int e = (k - 1) * NR + g;
+            I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jp;
+            store(k, I);
+            Jp = Jk;
+        }
+    }
+    if (bad) atomicExch(B.err, -2);
+}
+
+// Tiled SIMT GEMM: per task, J[k][c] = x_k * sum_i F[k][col(i)] A[i][c] + y_k * (... B ...).
+// Tile 64 levels x 64 output columns, 256 threads, 4x4 outputs per thread.
+#define ST_K 16
+#define ST_M 64
+#define ST_N 64
+__global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
+{
+    const int tl = blockIdx.x, tg = t0 + tl;
+    if (!B.state[tg].active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt;
+    const int k0 = blockIdx.y * ST_M, c0 = blockIdx.z * ST_N;
+    if (k0 > nt || c0 >= G.COUT) return;
+    __shared__ float Fs[ST_K][ST_M + 4];
+    __shared__ float As[ST_K][ST_N + 4];
+    __shared__ float Bs[ST_K][ST_N + 4];
+    const float *F = W.F + tk.fld_off;
+    const float *A = W.ops + tk.op_off;
+    const float *Bm = tk.has_mol ? W.ops + tk.mol_off : nullptr;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float accA[4][4] = {{0}}, accB[4][4] = {{0}};
+    for (int kc = 0; kc < G.CIN; kc += ST_K) {
+        for (int idx = threadIdx.x; idx < ST_M * ST_K; idx += 256) {
+            const int lv = idx / ST_K, kk = idx - lv * ST_K;
+            const int k = k0 + lv, ci = kc + kk;
+            Fs[kk][lv] = (k <= nt && ci < G.CIN) ? F[(size_t)k * G.LDC + in_to_col(G, ci)] : 0.f;
+        }
+        for (int idx = threadIdx.x; idx < ST_K * ST_N; idx += 256) {
+            const int kk = idx / ST_N, cc = idx - kk * ST_N;
+            const int ci = kc + kk, co = c0 + cc;
+            const bool ok = ci < G.CIN && co < G.LDO;
+            As[kk][cc] = ok ? A[(size_t)ci * G.LDO + co] : 0.f;
+            if (Bm) Bs[kk][cc] = ok ? Bm[(size_t)ci * G.LDO + co] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < ST_K; ++kk) {
+            float fr[4], ar[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) fr[i] = Fs[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) ar[j] = As[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) accA[i][j] = fmaf(fr[i], ar[j], accA[i][j]);
+            if (Bm) {
+                float br[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) br[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) accB[i][j] = fmaf(fr[i], br[j], accB[i][j]);
+            }
+        }
+        __syncthreads();
+    }
+    float *J = W.J + tk.fld_off;
+    const double *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int k = k0 + ty + 16 * i;
+        if (k > nt) continue;
+        const float x = (float)xd[k], y = (float)yd[k];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + tx + 16 * j;
+            if (c < G.COUT) J[(size_t)k * G.LDC + c] = x * accA[i][j] + y * accB[i][j];
+        }
+    }
+}
+
+__device__ inline double block_max(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = l < nw ? red[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+__global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
+{
+    __shared__ double red[32];
+    const int tl = blockIdx.x, tg = t0 + tl;
+    const TaskState st = B.state[tg];
+    if (!st.active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int c = threadIdx.x, nt = d.nt, N = G.N, NR = G.NR;
+    int s = 0, h = 0, g = 0;
+    if (c < G.COUT) decode_col(G, c, s, h, g);
+    const bool valid = c < G.COUT && g < d.n_ring;
+    float *F = W.F + tk.fld_off;
+    const float *J = W.J + tk.fld_off;
+    double *Tot = W.Tot + tk.fld_off;
+    // ---- surface boundary condition from the previous order's BOA downward field
+    float bc = 0.f;
+    if (valid && h == 0 && d.surf_on) {
+        const float *Fb = F + (size_t)nt * G.LDC;
+        if (d.rough) {
+            const float *R = W.srf + tk.srf_off + (size_t)g * N * 9 + s * 3;
+            const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
+            float acc = 0.f;
+            for (int i = 0; i < N; ++i) {
+                const float pw = (float)(fw * B.gmu[i] * B.gw[i]);
+                const float *Ri = R + (size_t)i * 9;
+                acc += pw * (Ri[0] * Fb[col_of(G, 0, 1, i)] + Ri[1] * Fb[col_of(G, 1, 1, i)] +
+                             Ri[2] * Fb[col_of(G, 2, 1, i)]);
+            }
+            bc = acc;
+        } else {
+            const float *MF = B.frs + ((size_t)tk.pix * NR + g) * 9 + s * 3;
+            bc = MF[0] * Fb[col_of(G, 0, 1, g)] + MF[1] * Fb[col_of(G, 1, 1, g)] + MF[2] * Fb[col_of(G, 2, 1, g)];
+        }
+    }
+    __syncthreads();
+    double mi = 0.0, mt = 0.0;
+    int bad = 0;
+    if (valid) {
+        const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+        auto put = [&](int k, float I) {
+            const size_t o = (size_t)k * G.LDC + c;
+            F[o] = I;
+            const double t = Tot[o] + (double)I;
+            Tot[o] = t;
+            mi = fmax(mi, fabs((double)I));
+            mt = fmax(mt, fabs(t));
+        };
+        if (h == 0) {
+            float I = bc, Jn = J[(size_t)nt * G.LDC + c];
+            put(nt, I);
+            for (int k = nt - 1; k >= 0; --k) {
+                const float Jk = J[(size_t)k * G.LDC + c];
+                const int e = k * NR + g;
+                I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jn;
+                put(k, I);
+                Jn = Jk;
+            }
+            bad = !isfinite(I);
+        } else {
+            float I = 0.f, Jp = J[c];
+            put(0, I);
+            for (int k = 1; k <= nt; ++k) {
+                const float Jk = J[(size_t)k * G.LDC + c];
+                const int e = (k - 1) * NR + g;
+                I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jp;
+                put(k, I);
+                Jp = Jk;
+            }
+            bad = !isfinite(I);
+        }
+    }
+    if (bad) atomicExch(B.err, -2);
+    mi = block_max(mi, red);
+    __syncthreads();
+    mt = block_max(mt, red);
+    if (threadIdx.x == 0) {
+        TaskState ns = st;
+        ns.orders = it;
+        ns.resid = mt > 0.0 ? mi / mt : 0.0;
+        if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
+        else if (it >= d.max_orders) ns.active = 0;
+        B.state[tg] = ns;
+        if (ns.active) atomicAdd(&B.active_cnt[it], 1);
+    }
+}
+
+// Linear interpolation between the bracketing Gauss nodes (rt_solver.c:386-403).
+__device__ inline void bracket(const double *gmu, int n, double mu, int &lo, int &hi, double &t)
+{
+    int jh = 1;
+    while (jh < n && gmu[jh - 1] < mu) jh++;
+    int jl = jh - 1;
+    if (jl < 1) { jl = 1; jh = 2; }
+    if (jh > n) { jh = n; jl = n - 1; }
+    lo = jl - 1; hi = jh - 1;
+    t = (mu - gmu[lo]) / (gmu[hi] - gmu[lo]);
+}
+
+__global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
+{
+    const int tl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tl >= nt_tasks) return;
+    const int tg = t0 + tl;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const double *Tot = W.Tot + tk.fld_off;
+    const int nt = d.nt, N = G.N, vs = d.view_slot;
+    const double *hh = B.h + d.lev_off;
+    auto up0 = [&](int s, int g) -> double {
+        double v = Tot[col_of(G, s, 0, g)];
+        if (d.rough) v -= rough_seed(d, tk, W, G, B.gmu, hh[0], g, s);
+        return v;
+    };
+    auto dn = [&](int g) -> double { return Tot[(size_t)nt * G.LDC + col_of(G, 0, 1, g)]; };
+    TaskOut o;
+    if (vs >= 0) {
+        o.vI = up0(0, vs); o.vQ = up0(1, vs); o.vU = up0(2, vs);
+        o.dn_view = dn(vs);
+    } else {
+        int lo, hi; double t;
+        bracket(B.gmu, N, d.mu_view, lo, hi, t);
+        o.vI = (1.0 - t) * up0(0, lo) + t * up0(0, hi);
+        o.vQ = (1.0 - t) * up0(1, lo) + t * up0(1, hi);
+        o.vU = (1.0 - t) * up0(2, lo) + t * up0(2, hi);
+        o.dn_view = (1.0 - t) * dn(lo) + t * dn(hi);
+    }
+    double f = 0.0;
+    for (int g = 0; g < N; ++g) f += B.gmu[g] * B.gw[g] * dn(g);
+    o.fdn = f;
+    B.tout[tg] = o;
+}
