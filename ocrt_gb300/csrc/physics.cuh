@@ -176,8 +176,15 @@ __device__ inline double sancer_lambda(double mu, double slen)
 
 // Cox-Munk + Fresnel reflection Mueller R(mu_out, mu_in_dn, phi)
 // (shared/surface.c:514-619).  sig2 = slope variance, lam = lam_i + lam_v.
+// shalf2 = sin^2(phi/2).  The facet-incidence cosine and the facet tilt are
+// evaluated in the cancellation-free form
+//   4 cos^2(omega) = (mu_o + mu_i)^2 + B,  tan^2(beta) = B / (mu_o + mu_i)^2,
+//   B = (s_o - s_i)^2 + 4 s_o s_i sin^2(phi/2),
+// algebraically identical to cos(omega) = sqrt((1 - cosTheta)/2) and
+// tan^2(beta) = (1 - cos^2 beta)/cos^2 beta of the reference; near the specular
+// peak the reference form loses ~eps/sigma^2 in FP32.
 template <typename T>
-__device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T sig2, T lam,
+__device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T shalf2, T sig2, T lam,
                                  T nw, int qconv, T *R)
 {
 #pragma unroll
@@ -187,9 +194,12 @@ __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T sig2, T
     const T s2 = sqrt(fmax(T(0), T(1) - mi * mi));
     T cT = mu_out * mi + s1 * s2 * cphi;
     cT = cT > T(1) ? T(1) : (cT < T(-1) ? T(-1) : cT);
-    const T cw = sqrt(fmax(T(0), T(0.5) * (T(1) - cT)));
+    const T mu_sum = mu_out + mu_in_dn;
+    const T A2 = mu_sum * mu_sum;
+    const T Bt = (s1 - s2) * (s1 - s2) + T(4) * s1 * s2 * shalf2;
+    const T cw = T(0.5) * sqrt(A2 + Bt);
     if (cw <= T(1e-6)) return;
-    const T cb = (mu_out + mu_in_dn) / (T(2) * cw);
+    const T cb = mu_sum / (T(2) * cw);
     if (cb <= T(1e-6)) return;
     const T sT = sqrt(fmax(T(0), T(1) - cT * cT));
     const T den = fmax(T(1e-12), sT);
@@ -212,7 +222,7 @@ __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T sig2, T
     T MF[9];
     fresnel_R<T>(cw, nw, qconv, MF);
     const T cb2 = cb * cb;
-    const T tb2 = (T(1) - cb2) / fmax(cb2, T(1e-8));
+    const T tb2 = Bt / A2;
     const T Ps = (T(1) / (T(OCRT_PI) * sig2)) * exp(-tb2 / sig2);
     const T brdf = (Ps / (T(1) + lam)) / (T(4) * mu_in_dn * mu_out * cb2 * cb2);
     // R = L2 * MF * L1 * brdf with L(c,s) = [[1,0,0],[0,c2,-s2],[0,s2,c2]]

@@ -211,7 +211,8 @@ __device__ void sunglint(const PixDev &d, double mu_v, double phi_v, double tau,
     const double s2v = slope_variance(d.wind, d.sigma_type);
     const double lam = sancer_lambda(mu0, sqrt(s2v)) + sancer_lambda(mu_v, sqrt(s2v));
     double R[9];
-    coxmunk_R<double>(mu_v, mu0, cos(phi_v), sin(phi_v), s2v, lam, d.n_water, d.q_conv, R);
+    const double sh = sin(0.5 * phi_v);
+    coxmunk_R<double>(mu_v, mu0, cos(phi_v), sin(phi_v), sh * sh, s2v, lam, d.n_water, d.q_conv, R);
     g[0] = OCRT_PI * R[0] * trans; g[1] = OCRT_PI * R[3] * trans; g[2] = OCRT_PI * R[6] * trans;
 }
 

@@ -436,8 +436,9 @@ __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const 
     for (int q = threadIdx.x; q < half; q += blockDim.x) {
         const double phi = (q + 0.5) * dphi;
         float R[9];
-        coxmunk_R<float>((float)mo, (float)mi, (float)cos(phi), (float)sin(phi), (float)s2v, (float)lam,
-                         (float)d.n_water, d.q_conv, R);
+        const double sh = sin(0.5 * phi);
+        coxmunk_R<float>((float)mo, (float)mi, (float)cos(phi), (float)sin(phi), (float)(sh * sh), (float)s2v,
+                         (float)lam, (float)d.n_water, d.q_conv, R);
 #pragma unroll
         for (int e = 0; e < 9; ++e) sm_R[e * hs + q] = R[e];
     }

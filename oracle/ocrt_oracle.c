@@ -1409,3 +1409,13 @@ int ocrt_oracle_max_threads(void)
     return 1;
 #endif
 }
+
+/* sizeof of every ABI struct, so the ctypes mirror can be checked without a GPU. */
+void ocrt_oracle_abi_sizes(size_t *out)
+{
+    out[0] = sizeof(ocrt_case);
+    out[1] = sizeof(ocrt_opts);
+    out[2] = sizeof(ocrt_aerosol);
+    out[3] = sizeof(ocrt_result);
+    out[4] = sizeof(ocrt_diag);
+}

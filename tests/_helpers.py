@@ -1,0 +1,73 @@
+"""Shared helpers: oracle binding, fixture loading and the parity tolerance.
+
+Parity bar (spec accuracy statement): |rho_I - ref| <= 1e-5 * |ref|,
+|rho_Q - ref| <= 1e-4 and |rho_U - ref| <= 1e-4.
+"""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+from ocrt_gb300 import _abi as A
+from synthetic import hg_aerosol_moments
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "reference_cases.json")
+
+TOL_I_REL = 1e-5
+TOL_QU_ABS = 1e-4
+
+
+class Oracle:
+    def __init__(self, path):
+        self.lib = C.CDLL(path)
+        self.f = A.bind_solver(self.lib, "ocrt_oracle")
+        self.lib.ocrt_oracle_solve_batch.argtypes = [
+            C.c_int, C.POINTER(A.Case), C.POINTER(A.Opts), C.c_int, C.POINTER(A.Aerosol), C.c_int,
+            C.POINTER(A.Result), C.c_int]
+
+    def solve(self, case, opts, aer=None, diag=False):
+        n = opts.fourier_m_max + 1
+        arr = None
+        d = None
+        if diag:
+            arr = {"orders_per_m": (C.c_int * n)(), "residual_per_m": (C.c_double * n)(),
+                   "view_I_m": (C.c_double * n)(), "view_Q_m": (C.c_double * n)(),
+                   "view_U_m": (C.c_double * n)()}
+            d = A.Diag(**{k: C.cast(v, A.Diag._fields_[i][1]) for i, (k, v) in enumerate(arr.items())})
+        r = A.Result()
+        a = aer.struct if isinstance(aer, A.AerosolHolder) else aer
+        rc = self.f(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None, C.byref(r),
+                    C.byref(d) if d is not None else None)
+        if rc != 0:
+            raise RuntimeError(f"oracle rc {rc}")
+        out = A.result_dict(r)
+        if diag:
+            out.update({k: np.array(v[:]) for k, v in arr.items()})
+        return out
+
+
+def load_golden():
+    with open(GOLDEN) as fh:
+        return json.load(fh)
+
+
+def inputs_from_spec(spec):
+    c = A.default_case(**spec["case"])
+    o = A.default_opts(**spec["opts"])
+    aer = None
+    if spec.get("aerosol"):
+        a = spec["aerosol"]
+        aer = A.AerosolHolder(a["tau_a"], a["ssa_a"], *hg_aerosol_moments(a["g"], a["L"]))
+    return c, o, aer
+
+
+def assert_parity(got, ref, where="", i_rel=TOL_I_REL, qu_abs=TOL_QU_ABS):
+    relI = abs(got["rho_I"] - ref["rho_I"]) / abs(ref["rho_I"])
+    dQ = abs(got["rho_Q"] - ref["rho_Q"])
+    dU = abs(got["rho_U"] - ref["rho_U"])
+    assert relI <= i_rel, f"{where}: rho_I rel err {relI:.3e} > {i_rel}"
+    assert dQ <= qu_abs, f"{where}: rho_Q abs err {dQ:.3e} > {qu_abs}"
+    assert dU <= qu_abs, f"{where}: rho_U abs err {dU:.3e} > {qu_abs}"
+    return relI, dQ, dU
