@@ -1,0 +1,363 @@
+"""Benchmark: batched forward pixel-solves/s on one GB300 (configuration 3).
+
+Workload (seeded synthetic, config["workload"]): 4096 pixels in one call with
+uneven shapes -- sza U[0,80], vza U[0,70], raa U[0,180], AOD lognormal
+(median 0.1, sigma 0.6), layers uniform in {50,100,200,400}, 10 bands
+412-865 nm with tau_R ~ lambda^-4.08, wind U[1,12] m/s, Henyey-Greenstein
+aerosol g U[0.6,0.8], SSA U[0.85,0.99], moments to L=120, 32 Gauss streams,
+Fourier modes 0..32, rough Cox-Munk ocean, tolerance 1e-7.
+
+value : pixel-solves/s from a resident plan (inputs already in HBM), K steps
+        timed with CUDA events on the launching stream.
+e2e   : the same metric through the C ABI call ocrt_gb_solve_batch with host
+        buffers (uploads, solve, result download inside the timed region).
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference] [--pixels P]
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from ocrt_gb300 import _abi as A  # noqa: E402
+from synthetic import batched_forward_pixels, hg_aerosol_moments  # noqa: E402
+
+METRIC = "pixel-solves/s"
+N_MU, M_MAX, L_AER = 32, 32, 120
+
+
+def workload(n_pix, seed=20261203 + 3):
+    p = batched_forward_pixels(n_pix, seed=seed)
+    cases, opts, aers = [], [], []
+    for i in range(n_pix):
+        cases.append(A.default_case(surface="black_fresnel_ocean", sza_deg=p["sza"][i], vza_deg=p["vza"][i],
+                                    raa_deg=p["raa"][i], wavelength_nm=p["wavelength"][i],
+                                    wind_speed=p["wind"][i], tau_r_input=p["tau_r"][i]))
+        opts.append(A.default_opts(n_mu=N_MU, n_layers=int(p["n_layers"][i]), fourier_m_max=M_MAX,
+                                   tau_r_source=A.TAU_R_FROM_INPUT, max_orders=1000, tolerance=1e-7))
+        aers.append(A.AerosolHolder(p["aod"][i], p["ssa"][i], *hg_aerosol_moments(p["g"][i], L_AER)))
+    return cases, opts, aers
+
+
+def config_dict(n_pix, world):
+    return {"workload": f"configuration 3: batched forward, {n_pix} pixels/GPU, uneven layers 50-400, "
+                        f"N={N_MU} streams, m<=32, aerosol L={L_AER}, rough Cox-Munk ocean",
+            "pixels_per_gpu": n_pix, "n_mu": N_MU, "fourier_m_max": M_MAX, "aerosol_L": L_AER,
+            "tolerance": 1e-7, "parallelism": f"replicas x{world}",
+            "l2_policy": "working set (fields, totals, operators) >> 129 MB L2; no flush needed"}
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- helpers
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "src": "fallback"}
+
+
+def traffic_from_profiles(kernel):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    try:
+        d = json.load(open(path))
+        return d.get(kernel, {}).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def oracle_lib():
+    so = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+    if not os.path.exists(so):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
+    lib = C.CDLL(so)
+    lib.ocrt_oracle_solve_batch.argtypes = [C.c_int, C.POINTER(A.Case), C.POINTER(A.Opts), C.c_int,
+                                            C.POINTER(A.Aerosol), C.c_int, C.POINTER(A.Result), C.c_int]
+    lib.ocrt_oracle_max_threads.restype = C.c_int
+    return lib
+
+
+def cpu_run(cases, opts, aers, prefer_reference):
+    """Time the CPU implementation over the given pixels with every host thread."""
+    ref_so = os.path.join(ROOT, "oracle", "_ref", "libocrt_ref.so")
+    lib = oracle_lib()
+    threads = lib.ocrt_oracle_max_threads()
+    kind, fn = "port", lib.ocrt_oracle_solve_batch
+    if prefer_reference and os.path.exists(ref_so):
+        try:
+            rl = C.CDLL(ref_so)
+            rl.ocrt_ref_solve_batch.argtypes = lib.ocrt_oracle_solve_batch.argtypes
+            kind, fn = "reference", rl.ocrt_ref_solve_batch
+        except OSError:
+            pass
+    n = len(cases)
+    out = (A.Result * n)()
+    t0 = time.perf_counter()
+    rc = fn(n, (A.Case * n)(*cases), (A.Opts * n)(*opts), 1, (A.Aerosol * n)(*[a.struct for a in aers]), 1,
+            out, threads)
+    dt = time.perf_counter() - t0
+    if rc != 0:
+        raise RuntimeError(f"cpu baseline rc {rc}")
+    return dt, threads, kind, out
+
+
+def cpu_sample(cases, opts, aers, budget_s=20.0, prefer_reference=False):
+    """Bounded sample: grow the pixel count until about budget_s of CPU work."""
+    n = 16
+    dt, threads, kind, out = cpu_run(cases[:n], opts[:n], aers[:n], prefer_reference)
+    total_t, total_n = dt, n
+    outs = list(out)
+    while total_t < budget_s * 0.5 and total_n + n <= len(cases):
+        dt, _, _, out = cpu_run(cases[total_n:total_n + n], opts[total_n:total_n + n], aers[total_n:total_n + n],
+                                prefer_reference)
+        total_t += dt
+        total_n += n
+        outs += list(out)
+    return {"value": total_n / total_t, "unit": METRIC, "cores": threads, "kind": kind,
+            "sample": f"first {total_n} pixels of the workload, OpenMP over pixels, {total_t:.1f} s"}, outs
+
+
+# ---------------------------------------------------------------- arms
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cases, opts, aers = workload(max(args.pixels, 256))
+    for _ in range(args.warmup):
+        cpu_run(cases[:4], opts[:4], aers[:4], True)
+    vals = []
+    base = None
+    for k in range(args.steps):
+        base, _ = cpu_sample(cases[k * 16:], opts[k * 16:], aers[k * 16:], budget_s=args.cpu_budget,
+                             prefer_reference=True)
+        vals.append(base["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args.pixels, world),
+            "cpu_baseline": {**base, "value": v},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import torch
+    import ocrt_gb300 as og
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    og.lib().ocrt_gb_init(dev)
+    cases, opts, aers = workload(args.pixels)
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- value: resident plan ----
+    plan = og.Plan(cases, opts, aers)
+    for _ in range(args.warmup):
+        plan.execute(sp)
+    torch.cuda.synchronize()
+    og.set_timing(True)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    kstats = {}
+    launches = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        e0.record(stream)
+        plan.execute(sp)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        for k, v in plan.kernel_stats().items():
+            acc = kstats.setdefault(k, {"ms": 0.0, "launches": 0, "flops": 0.0, "bytes": 0.0})
+            for f in acc:
+                acc[f] += v[f]
+        launches += plan.stats()["kernel_launches"]
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    og.set_timing(False)
+    res = plan.results(sp)
+    om = float(np.sum(res["order_modes"]))
+    ms_step = total_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = args.pixels * world / (ms_step / 1e3)
+
+    # ---- roofline of the dominant kernel ----
+    pk = peaks()
+    dom = max(kstats, key=lambda k: kstats[k]["ms"])
+    d = kstats[dom]
+    per_launch_ms = d["ms"] / max(d["launches"], 1)
+    if d["flops"] > 0 and dom in ("source_gemm", "coxmunk_fourier", "phase_tables"):
+        achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
+        roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"],
+                "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops_sustained"],
+                "peak_source": f"{pk['src']} bf16 sustained",
+                "traffic": traffic_from_profiles(dom), "avg_launch_ms": per_launch_ms,
+                "alg_flops_per_launch": d["flops"] / max(d["launches"], 1)}
+    else:
+        achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "peak_source": f"{pk['src']} HBM copy",
+                "traffic": traffic_from_profiles(dom), "avg_launch_ms": per_launch_ms,
+                "alg_bytes_per_launch": d["bytes"] / max(d["launches"], 1)}
+    breakdown = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
+                     "share": v["ms"] / max(sum(x["ms"] for x in kstats.values()), 1e-9)}
+                 for k, v in sorted(kstats.items(), key=lambda kv: -kv[1]["ms"]) if v["launches"]}
+    plan.close()
+
+    # ---- e2e through the C ABI with host buffers ----
+    og.solve_batch(cases, opts, aers)          # warm the allocator cache
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r_e2e = og.solve_batch(cases, opts, aers)
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([t_e2e], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    h2d = args.pixels * (C.sizeof(A.Case) + C.sizeof(A.Opts) + C.sizeof(A.Aerosol) + 4 * 8 * (L_AER + 1))
+    d2h = args.pixels * C.sizeof(A.Result)
+    e2e = {"value": args.pixels * world / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        return
+    # ---- plain per-pixel GPU form (one solve call per pixel) ----
+    nplain = min(args.plain_pixels, args.pixels)
+    og.solve_case(cases[0], opts[0], aers[0])
+    t0 = time.perf_counter()
+    for i in range(nplain):
+        og.solve_case(cases[i], opts[i], aers[i])
+    plain = nplain / (time.perf_counter() - t0)
+
+    # ---- CPU baseline (oracle port, all host threads) + error vs FP64 ----
+    cpu, couts = (None, None)
+    err = None
+    if world == 1 and not args.no_cpu:
+        cpu, couts = cpu_sample(cases, opts, aers, budget_s=args.cpu_budget)
+        n = len(couts)
+        relI = max(abs(res["rho_I"][i] - couts[i].rho_I) / abs(couts[i].rho_I) for i in range(n))
+        dQ = max(abs(res["rho_Q"][i] - couts[i].rho_Q) for i in range(n))
+        dU = max(abs(res["rho_U"][i] - couts[i].rho_U) for i in range(n))
+        err = {"pixels": n, "max_rel_err_rho_I": relI, "max_abs_err_rho_Q": dQ, "max_abs_err_rho_U": dU,
+               "reference": "FP64 oracle on the same pixels"}
+
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args.pixels, world),
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof,
+            "cpu_baseline": cpu, "rel_err_vs_fp64": err,
+            "plain_per_pixel_gpu": {"value": plain, "unit": METRIC, "sample": f"{nplain} pixels, one "
+                                    f"ocrt_gb_solve_case call each", "batched_speedup": value / world / plain},
+            "order_modes_per_step": om, "kernel_breakdown": breakdown}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pixels", type=int, default=4096)
+    ap.add_argument("--plain-pixels", type=int, default=16)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,16 @@ int  ocrt_gb_plan_stats(const ocrt_plan *plan, double *order_modes_total,
                         long long *kernel_launches);
 void ocrt_gb_plan_destroy(ocrt_plan *plan);
 
+/* Per-kernel-class instrumentation (no reference counterpart).  With timing
+ * enabled every launch of a plan is bracketed by CUDA events on the launching
+ * stream.  ocrt_gb_plan_kernel_stats(plan, -1, ...) returns the number of
+ * classes; for a class index it returns the class name, summed device time of
+ * the last execute, launch count, and the algorithmic FLOPs and bytes that
+ * execute performed (derived from the orders each task ran). */
+void ocrt_gb_set_timing(int enable);
+int  ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, double *ms,
+                               long long *launches, double *alg_flops, double *alg_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,8 @@ _lib = None
 EXPORTS = [
     "ocrt_opts_default", "ocrt_case_default", "ocrt_gb_init", "ocrt_gb_shutdown", "ocrt_gb_last_error",
     "ocrt_gb_solve_case", "ocrt_gb_solve_batch", "ocrt_gb_plan_create", "ocrt_gb_plan_execute",
-    "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy",
+    "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy", "ocrt_gb_set_timing",
+    "ocrt_gb_plan_kernel_stats",
 ]
 
 
@@ -51,6 +52,10 @@ def lib():
     L.ocrt_gb_plan_results.argtypes = [C.c_void_p, C.POINTER(Result), C.c_void_p]
     L.ocrt_gb_plan_stats.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.ocrt_gb_plan_destroy.argtypes = [C.c_void_p]
+    L.ocrt_gb_set_timing.argtypes = [C.c_int]
+    L.ocrt_gb_plan_kernel_stats.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_longlong), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
     _lib = L
@@ -111,6 +116,10 @@ def solve_batch(cases, opts, aerosols=None):
     return results_to_numpy(out)
 
 
+def set_timing(enable):
+    lib().ocrt_gb_set_timing(1 if enable else 0)
+
+
 def results_to_numpy(out):
     dt = np.dtype([(f, np.float64 if t is C.c_double else np.int32) for f, t in Result._fields_],
                   align=True)
@@ -141,6 +150,20 @@ class Plan:
         om, nl = C.c_double(), C.c_longlong()
         _check(lib().ocrt_gb_plan_stats(self._h, C.byref(om), C.byref(nl)))
         return {"order_modes": om.value, "kernel_launches": nl.value}
+
+    def kernel_stats(self):
+        """Per kernel class: device ms of the last execute (timing must be on), launches,
+        algorithmic FLOPs and bytes."""
+        L = lib()
+        n = L.ocrt_gb_plan_kernel_stats(self._h, -1, None, None, None, None, None)
+        out = {}
+        for k in range(n):
+            nm, ms, nl, fl, by = C.c_char_p(), C.c_double(), C.c_longlong(), C.c_double(), C.c_double()
+            _check(L.ocrt_gb_plan_kernel_stats(self._h, k, C.byref(nm), C.byref(ms), C.byref(nl), C.byref(fl),
+                                               C.byref(by)))
+            out[nm.value.decode()] = {"ms": ms.value, "launches": nl.value, "flops": fl.value,
+                                      "bytes": by.value}
+        return out
 
     def close(self):
         if self._h:

@@ -28,6 +28,11 @@ cudaStream_t g_stream = nullptr;
 std::multimap<size_t, void *> g_free;      // caching allocator: size -> block
 std::map<void *, size_t> g_live;
 int *g_pinned = nullptr;
+int g_timing = 0;
+
+enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SCAN, KC_EXTRACT, KC_IPSS, KC_FINAL, KC_N };
+const char *kc_names[KC_N] = {"setup", "phase_tables", "coxmunk_fourier", "primary", "source_gemm",
+                              "transport_scan", "extract", "ipss", "finalize"};
 
 int fail(int rc, const std::string &msg)
 {
@@ -173,6 +178,12 @@ struct ocrt_plan {
     std::vector<Group> groups;
     long long launches = 0;
     double order_modes = 0;
+    // per-kernel-class timing (enabled by ocrt_gb_set_timing)
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+    double ms[KC_N] = {0};
+    long long cnt[KC_N] = {0};
+    double flops[KC_N] = {0}, bytes[KC_N] = {0};
+    bool work_done = false;
 };
 
 namespace {
@@ -319,10 +330,16 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     return OCRT_OK;
 }
 
-#define LAUNCH(plan, ...)                                                             \
+#define LAUNCH(plan, cls, ...)                                                        \
     do {                                                                              \
+        cudaEvent_t e0_ = nullptr, e1_ = nullptr;                                     \
+        if (g_timing) {                                                               \
+            cudaEventCreate(&e0_); cudaEventCreate(&e1_); cudaEventRecord(e0_, st);   \
+        }                                                                             \
         __VA_ARGS__;                                                                  \
         (plan)->launches++;                                                           \
+        (plan)->cnt[cls]++;                                                           \
+        if (g_timing) { cudaEventRecord(e1_, st); (plan)->ev.push_back({cls, {e0_, e1_}}); } \
         cudaError_t e_ = cudaGetLastError();                                          \
         if (e_ != cudaSuccess) return fail(OCRT_ERR_DEVICE, std::string("launch: ") + cudaGetErrorString(e_)); \
     } while (0)
@@ -332,14 +349,14 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     const Geom G = g.G;
     const int P = g.P;
     CK(cudaMemsetAsync(g.err, 0, sizeof(int), st));
-    LAUNCH(plan, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw));
-    LAUNCH(plan, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
-    LAUNCH(plan, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
-    LAUNCH(plan, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
-    LAUNCH(plan, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
-    LAUNCH(plan, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
-    if (g.any_rough) LAUNCH(plan, k_cs_table<<<g.Mmax + 1, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
-    if (g.any_flat) LAUNCH(plan, k_flat_fresnel<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.frs));
+    LAUNCH(plan, KC_SETUP, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw));
+    LAUNCH(plan, KC_SETUP, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
+    LAUNCH(plan, KC_SETUP, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
+    LAUNCH(plan, KC_SETUP, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
+    LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
+    LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
+    if (g.any_rough) LAUNCH(plan, KC_SETUP, k_cs_table<<<g.Mmax + 1, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
+    if (g.any_flat) LAUNCH(plan, KC_SETUP, k_flat_fresnel<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.frs));
 
     BatchBufs B;
     B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
@@ -356,34 +373,34 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         CK(cudaMemsetAsync(g.pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (g.any_flat) CK(cudaMemsetAsync(g.fvec, 0, sizeof(float) * (size_t)nw * 24 * G.NR, st));
         CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
-        LAUNCH(plan, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
-        LAUNCH(plan, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
+        LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
+        LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
         if (w.any_rough) {
             const size_t smem = sizeof(float) * 9 * (g.nphi / 2 + 1);
-            LAUNCH(plan, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
+            LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
                        g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.srf));
         }
-        LAUNCH(plan, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+        LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         const dim3 sgrid(nw, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= g.max_orders; ++it) {
-            LAUNCH(plan, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
-            LAUNCH(plan, k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0, it));
+            LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
+            LAUNCH(plan, KC_SCAN, k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0, it));
             if ((it - 1) % poll == 0 || it == g.max_orders) {
                 CK(cudaMemcpyAsync(g_pinned, g.active_cnt + it, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
                 if (*g_pinned == 0) break;
             }
         }
-        LAUNCH(plan, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
+        LAUNCH(plan, KC_EXTRACT, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
     }
     if (g.any_pssa) {
         int maxnt = 0;
         for (const PixDev &d : g.hpx) maxnt = std::max(maxnt, d.nt);
         const size_t smem = sizeof(double) * (6 * (size_t)maxnt + 6) + sizeof(int) * ((size_t)maxnt + 1);
-        LAUNCH(plan, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.kappa, g.taudir));
+        LAUNCH(plan, KC_IPSS, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.kappa, g.taudir));
     }
-    LAUNCH(plan, k_finalize<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.state, g.tout, g.gmu, g.gw, g.h,
+    LAUNCH(plan, KC_FINAL, k_finalize<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.state, g.tout, g.gmu, g.gw, g.h,
                                                               g.kappa, g.taudir, g.res));
     return OCRT_OK;
 }
@@ -482,6 +499,10 @@ int ocrt_gb_plan_execute(ocrt_plan *plan, void *stream)
     std::lock_guard<std::mutex> lk(g_mu);
     cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
     plan->launches = 0;
+    for (auto &e : plan->ev) { cudaEventDestroy(e.second.first); cudaEventDestroy(e.second.second); }
+    plan->ev.clear();
+    for (int c = 0; c < KC_N; ++c) { plan->ms[c] = 0; plan->cnt[c] = 0; }
+    plan->work_done = false;
     for (Group &g : plan->groups) {
         const int rc = run_group(plan, g, st);
         if (rc) return rc;
@@ -508,6 +529,63 @@ int ocrt_gb_plan_results(ocrt_plan *plan, ocrt_result *out, void *stream)
     return OCRT_OK;
 }
 
+void ocrt_gb_set_timing(int enable) { g_timing = enable ? 1 : 0; }
+
+int ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, double *ms, long long *launches,
+                              double *alg_flops, double *alg_bytes)
+{
+    if (!plan) return fail(OCRT_ERR_ARGS, "null plan");
+    if (cls == -1) return KC_N;
+    if (cls < 0 || cls >= KC_N) return fail(OCRT_ERR_ARGS, "kernel class out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!plan->ev.empty()) {
+        CK(cudaStreamSynchronize(g_stream));
+        for (auto &e : plan->ev) {
+            float t = 0.f;
+            if (cudaEventSynchronize(e.second.second) == cudaSuccess &&
+                cudaEventElapsedTime(&t, e.second.first, e.second.second) == cudaSuccess)
+                plan->ms[e.first] += t;
+            cudaEventDestroy(e.second.first);
+            cudaEventDestroy(e.second.second);
+        }
+        plan->ev.clear();
+    }
+    if (!plan->work_done) {
+        // algorithmic work from the orders each task actually executed
+        for (int c = 0; c < KC_N; ++c) { plan->flops[c] = 0; plan->bytes[c] = 0; }
+        for (Group &g : plan->groups) {
+            std::vector<TaskState> st(g.T);
+            CK(cudaMemcpy(st.data(), g.state, sizeof(TaskState) * g.T, cudaMemcpyDeviceToHost));
+            const double N = g.N, NR = g.G.NR;
+            for (int t = 0; t < g.T; ++t) {
+                const TaskDev &tk = g.htask[t];
+                const PixDev &d = g.hpx[tk.pix];
+                const double K = tk.K, nt = d.nt, ords = std::max(0, st[t].orders - 1);
+                plan->flops[KC_SOURCE] += ords * 72.0 * N * N * K;
+                plan->bytes[KC_SOURCE] += ords * (K * 6 * N + K * 6 * NR + 36.0 * N * NR * (tk.has_mol ? 2 : 1)) * 4.0;
+                plan->bytes[KC_SCAN] += ords * (2.0 * 6 * N * K + N * nt) * 4.0;
+                plan->flops[KC_SCAN] += ords * 6.0 * N * nt * 5.0;
+                plan->bytes[KC_PRIMARY] += K * 6 * NR * 12.0;
+                const double Lm = d.L - tk.m + 1;
+                plan->flops[KC_TABLES] += 2.0 * 26.0 * NR * N * Lm;
+                plan->bytes[KC_TABLES] += 36.0 * N * NR * 4.0 * (tk.has_mol ? 2 : 1);
+            }
+            for (const PixDev &d : g.hpx) {
+                if (!(d.surface == 2 && d.wind > 0.0)) continue;
+                plan->flops[KC_COXMUNK] += 18.0 * (N * N + N) * d.nphi * (d.M + 1);
+                plan->bytes[KC_COXMUNK] += (N * N + N) * 9.0 * (d.M + 1) * 4.0;
+            }
+        }
+        plan->work_done = true;
+    }
+    if (name) *name = kc_names[cls];
+    if (ms) *ms = plan->ms[cls];
+    if (launches) *launches = plan->cnt[cls];
+    if (alg_flops) *alg_flops = plan->flops[cls];
+    if (alg_bytes) *alg_bytes = plan->bytes[cls];
+    return OCRT_OK;
+}
+
 int ocrt_gb_plan_stats(const ocrt_plan *plan, double *order_modes_total, long long *kernel_launches)
 {
     if (!plan) return fail(OCRT_ERR_ARGS, "null plan");
@@ -522,6 +600,7 @@ void ocrt_gb_plan_destroy(ocrt_plan *plan)
     std::lock_guard<std::mutex> lk(g_mu);
     if (g_stream) cudaStreamSynchronize(g_stream);
     for (Group &g : plan->groups) free_group(g);
+    for (auto &e : plan->ev) { cudaEventDestroy(e.second.first); cudaEventDestroy(e.second.second); }
     delete plan;
 }
 

@@ -514,12 +514,14 @@ static void primary_source(const ctx_t *c, const mode_t_ *md, double *JI, double
 }
 
 /* Multiple-scattering source: the vector contraction of
- * rt_sos_operator.c:206-424 written directly on the phase tables. */
+ * rt_sos_operator.c:206-424.  The 18 aerosol and 18 molecular direction-pair
+ * coefficients are formed once per (outgoing, incoming) pair from the phase
+ * tables; the level loop is innermost over transposed field planes. */
 static int ms_source(const ctx_t *c, const mode_t_ *md,
                      const double *I, const double *Q, const double *U,
                      double *JI, double *JQ, double *JU)
 {
-    const int n = c->n, nt = c->md.nt, m = md->m;
+    const int n = c->n, nt = c->md.nt, m = md->m, K = nt + 1;
     const int mol = m <= 2;
     const double b0 = m == 0 ? c->beta0 : 0.0, b2 = c->beta2, g2 = c->gamma2, a2 = c->alpha2;
     const double *xp = md->xpl + n, *xr = md->xrl + n, *xt = md->xtl + n;
@@ -527,48 +529,70 @@ static int ms_source(const ctx_t *c, const mode_t_ *md,
         for (int j = -n; j <= n; ++j)
             if (j != 0 && (!isfinite(F(I, c, k, j)) || !isfinite(F(Q, c, k, j)) ||
                            !isfinite(F(U, c, k, j)))) return -2;
-    for (int k = 0; k <= nt; ++k) {
-        const double x = c->md.xdel[k], y = c->md.ydel[k];
-        for (int o = 1; o <= n; ++o) {
-            double Iu = 0, Id = 0, Qu = 0, Qd = 0, Uu = 0, Ud = 0;
-            for (int i = 1; i <= n; ++i) {
-                const double w = c->gb[RIDX(n, i)];
-                if (w == 0.0) continue;
-                /* aerosol tables + molecular l=2 (and l=0 at m=0) terms */
-                const double ii_s = x * TAB(md->pfm, n, i, o) + y * (mol ? b0 + b2 * xp[i] * xp[o] : 0.0);
-                const double ii_c = x * TAB(md->pfm, n, i, -o) + y * (mol ? b0 + b2 * xp[i] * xp[-o] : 0.0);
-                const double iu_s = x * TAB(md->gt, n, i, o) + y * (mol ? g2 * xp[i] * xt[o] : 0.0);
-                const double iu_c = x * TAB(md->gt, n, i, -o) + y * (mol ? g2 * xp[i] * xt[-o] : 0.0);
-                const double iuT_s = x * TAB(md->gt, n, o, i) + y * (mol ? g2 * xp[o] * xt[i] : 0.0);
-                const double iuT_c = x * TAB(md->gt, n, o, -i) + y * (mol ? g2 * xp[o] * xt[-i] : 0.0);
-                const double iq_s = x * TAB(md->gr, n, i, o) + y * (mol ? g2 * xp[i] * xr[o] : 0.0);
-                const double iq_c = x * TAB(md->gr, n, i, -o) + y * (mol ? g2 * xp[i] * xr[-o] : 0.0);
-                const double iqT_s = x * TAB(md->gr, n, o, i) + y * (mol ? g2 * xp[o] * xr[i] : 0.0);
-                const double iqT_c = x * TAB(md->gr, n, o, -i) + y * (mol ? g2 * xp[o] * xr[-i] : 0.0);
-                const double qq_s = x * TAB(md->arr, n, i, o) + y * (mol ? a2 * xr[i] * xr[o] : 0.0);
-                const double qq_c = x * TAB(md->arr, n, i, -o) + y * (mol ? a2 * xr[i] * xr[-o] : 0.0);
-                const double qu_s = x * TAB(md->art, n, i, o) + y * (mol ? a2 * xt[i] * xr[o] : 0.0);
-                const double qu_c = x * TAB(md->art, n, i, -o) + y * (mol ? a2 * xt[i] * xr[-o] : 0.0);
-                const double quT_s = x * TAB(md->art, n, o, i) + y * (mol ? a2 * xt[o] * xr[i] : 0.0);
-                const double quT_c = x * TAB(md->art, n, o, -i) + y * (mol ? a2 * xt[o] * xr[-i] : 0.0);
-                const double uu_s = x * TAB(md->att, n, i, o) + y * (mol ? a2 * xt[i] * xt[o] : 0.0);
-                const double uu_c = x * TAB(md->att, n, i, -o) + y * (mol ? a2 * xt[i] * xt[-o] : 0.0);
-                const double iu = F(I, c, k, i), id = F(I, c, k, -i);
-                const double qu = F(Q, c, k, i), qd = F(Q, c, k, -i);
-                const double uu = F(U, c, k, i), ud = F(U, c, k, -i);
-                Iu += w * (iu * ii_s + qu * iqT_s - uu * iuT_s + id * ii_c + qd * iqT_c - ud * iuT_c);
-                Id += w * (iu * ii_c + qu * iqT_c + uu * iuT_c + id * ii_s + qd * iqT_s + ud * iuT_s);
-                Qu += w * (iu * iq_s + qu * qq_s - uu * qu_s + id * iq_c + qd * qq_c + ud * qu_c);
-                Qd += w * (iu * iq_c + qu * qq_c - uu * qu_c + id * iq_s + qd * qq_s + ud * qu_s);
-                Uu -= w * (iu * iu_s + qu * quT_s - uu * uu_s - id * iu_c + qd * quT_c - ud * uu_c);
-                Ud -= w * (iu * iu_c - qu * quT_c - uu * uu_c - id * iu_s - qd * quT_s - ud * uu_s);
-            }
-            F(JI, c, k, o) = Iu; F(JI, c, k, -o) = Id;
-            F(JQ, c, k, o) = Qu; F(JQ, c, k, -o) = Qd;
-            F(JU, c, k, o) = Uu; F(JU, c, k, -o) = Ud;
+    double *pl = malloc(sizeof(double) * (size_t)K * (6 * n + 6));
+    if (!pl) return -3;
+    double *acc = pl + (size_t)6 * n * K;
+#define PLANE(comp, i) (pl + ((size_t)(comp) * n + (size_t)((i) - 1)) * K)
+    for (int i = 1; i <= n; ++i)
+        for (int k = 0; k <= nt; ++k) {
+            PLANE(0, i)[k] = F(I, c, k, i); PLANE(1, i)[k] = F(I, c, k, -i);
+            PLANE(2, i)[k] = F(Q, c, k, i); PLANE(3, i)[k] = F(Q, c, k, -i);
+            PLANE(4, i)[k] = F(U, c, k, i); PLANE(5, i)[k] = F(U, c, k, -i);
         }
-        F(JI, c, k, 0) = F(JQ, c, k, 0) = F(JU, c, k, 0) = NAN;
+    const double *xd = c->md.xdel, *yd = c->md.ydel;
+    for (int o = 1; o <= n; ++o) {
+        memset(acc, 0, sizeof(double) * 6 * (size_t)K);
+        double *Iu_ = acc, *Id_ = acc + K, *Qu_ = acc + 2 * K, *Qd_ = acc + 3 * K, *Uu_ = acc + 4 * K, *Ud_ = acc + 5 * K;
+        for (int i = 1; i <= n; ++i) {
+            const double w = c->gb[RIDX(n, i)];
+            if (w == 0.0) continue;
+            const double pa[18] = {
+                TAB(md->pfm, n, i, o), TAB(md->pfm, n, i, -o), TAB(md->gt, n, i, o), TAB(md->gt, n, i, -o),
+                TAB(md->gt, n, o, i), TAB(md->gt, n, o, -i), TAB(md->gr, n, i, o), TAB(md->gr, n, i, -o),
+                TAB(md->gr, n, o, i), TAB(md->gr, n, o, -i), TAB(md->arr, n, i, o), TAB(md->arr, n, i, -o),
+                TAB(md->art, n, i, o), TAB(md->art, n, i, -o), TAB(md->art, n, o, i), TAB(md->art, n, o, -i),
+                TAB(md->att, n, i, o), TAB(md->att, n, i, -o)};
+            double pm[18] = {0};
+            if (mol) {
+                const double v[18] = {
+                    b0 + b2 * xp[i] * xp[o], b0 + b2 * xp[i] * xp[-o], g2 * xp[i] * xt[o], g2 * xp[i] * xt[-o],
+                    g2 * xp[o] * xt[i], g2 * xp[o] * xt[-i], g2 * xp[i] * xr[o], g2 * xp[i] * xr[-o],
+                    g2 * xp[o] * xr[i], g2 * xp[o] * xr[-i], a2 * xr[i] * xr[o], a2 * xr[i] * xr[-o],
+                    a2 * xt[i] * xr[o], a2 * xt[i] * xr[-o], a2 * xt[o] * xr[i], a2 * xt[o] * xr[-i],
+                    a2 * xt[i] * xt[o], a2 * xt[i] * xt[-o]};
+                memcpy(pm, v, sizeof(v));
+            }
+            const double *iu_ = PLANE(0, i), *id_ = PLANE(1, i), *qu_ = PLANE(2, i), *qd_ = PLANE(3, i);
+            const double *uu_ = PLANE(4, i), *ud_ = PLANE(5, i);
+            for (int k = 0; k < K; ++k) {
+                const double x = xd[k], y = yd[k];
+                const double ii_s = x * pa[0] + y * pm[0], ii_c = x * pa[1] + y * pm[1];
+                const double iu_s = x * pa[2] + y * pm[2], iu_c = x * pa[3] + y * pm[3];
+                const double iuT_s = x * pa[4] + y * pm[4], iuT_c = x * pa[5] + y * pm[5];
+                const double iq_s = x * pa[6] + y * pm[6], iq_c = x * pa[7] + y * pm[7];
+                const double iqT_s = x * pa[8] + y * pm[8], iqT_c = x * pa[9] + y * pm[9];
+                const double qq_s = x * pa[10] + y * pm[10], qq_c = x * pa[11] + y * pm[11];
+                const double qu_s = x * pa[12] + y * pm[12], qu_c = x * pa[13] + y * pm[13];
+                const double quT_s = x * pa[14] + y * pm[14], quT_c = x * pa[15] + y * pm[15];
+                const double uu_s = x * pa[16] + y * pm[16], uu_c = x * pa[17] + y * pm[17];
+                const double iu = iu_[k], id = id_[k], qu = qu_[k], qd = qd_[k], uu = uu_[k], ud = ud_[k];
+                Iu_[k] += w * (iu * ii_s + qu * iqT_s - uu * iuT_s + id * ii_c + qd * iqT_c - ud * iuT_c);
+                Id_[k] += w * (iu * ii_c + qu * iqT_c + uu * iuT_c + id * ii_s + qd * iqT_s + ud * iuT_s);
+                Qu_[k] += w * (iu * iq_s + qu * qq_s - uu * qu_s + id * iq_c + qd * qq_c + ud * qu_c);
+                Qd_[k] += w * (iu * iq_c + qu * qq_c - uu * qu_c + id * iq_s + qd * qq_s + ud * qu_s);
+                Uu_[k] -= w * (iu * iu_s + qu * quT_s - uu * uu_s - id * iu_c + qd * quT_c - ud * uu_c);
+                Ud_[k] -= w * (iu * iu_c - qu * quT_c - uu * uu_c - id * iu_s - qd * quT_s - ud * uu_s);
+            }
+        }
+        for (int k = 0; k <= nt; ++k) {
+            F(JI, c, k, o) = Iu_[k]; F(JI, c, k, -o) = Id_[k];
+            F(JQ, c, k, o) = Qu_[k]; F(JQ, c, k, -o) = Qd_[k];
+            F(JU, c, k, o) = Uu_[k]; F(JU, c, k, -o) = Ud_[k];
+        }
     }
+    for (int k = 0; k <= nt; ++k) F(JI, c, k, 0) = F(JQ, c, k, 0) = F(JU, c, k, 0) = NAN;
+#undef PLANE
+    free(pl);
     return 0;
 }
 
