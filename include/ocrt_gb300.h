@@ -174,6 +174,26 @@ void ocrt_gb_set_timing(int enable);
 int  ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, double *ms,
                                long long *launches, double *alg_flops, double *alg_bytes);
 
+/* ---- single solve that allocates nothing --------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory: an application that owns the whole device budget through its own
+ * pool allocator and forbids any other cudaMalloc/cudaFree, or a latency-bound
+ * loop that cannot afford the implicit device synchronisation of cudaMalloc
+ * and cudaFree.  Same inputs, outputs and results as ocrt_gb_solve_case, but
+ * every device buffer lives in one fixed 32 MiB __device__ array that each GPU
+ * loading this library holds until exit; no cudaMalloc, cudaFree or pinned
+ * host allocation is made.  Limits: n_mu <= 32, n_layers <= 400,
+ * fourier_m_max <= 32, aerosol L_max <= 255, max_orders <= 4096; larger
+ * requests return OCRT_ERR_ARGS with a message.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) with that device
+ * current, so make it before any stream capture.  All calls share the array:
+ * each call clears what must start at zero, and calls whose GPU work overlaps
+ * race on it and must be serialised by the caller.  stream: a cudaStream_t as
+ * void* (NULL = the default stream). */
+int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *opts,
+                               const ocrt_aerosol *aer, ocrt_result *out,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif

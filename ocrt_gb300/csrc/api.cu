@@ -651,3 +651,15 @@ int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_ae
 }
 
 } // extern "C"
+
+// Internal helpers for other translation units of this library (C++ linkage,
+// not part of the C ABI).
+int ocrt_internal_validate(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer)
+{
+    return validate(cs, op, aer);
+}
+
+int ocrt_internal_fail(int rc, const char *msg)
+{
+    return fail(rc, msg);
+}
