@@ -266,7 +266,7 @@ def run_ours(args, rank, world):
     dom = max(kstats, key=lambda k: kstats[k]["ms"])
     d = kstats[dom]
     per_launch_ms = d["ms"] / max(d["launches"], 1)
-    if d["flops"] > 0 and dom in ("source_gemm", "coxmunk_fourier", "phase_tables"):
+    if d["flops"] > 0 and dom in ("source_gemm_simt", "source_gemm_tcgen05", "coxmunk_fourier", "phase_tables"):
         achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
         roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops_sustained"],
                 "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops_sustained"],

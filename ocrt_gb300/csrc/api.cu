@@ -30,9 +30,11 @@ std::map<void *, size_t> g_live;
 int *g_pinned = nullptr;
 int g_timing = 0;
 
-enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SCAN, KC_EXTRACT, KC_IPSS, KC_FINAL, KC_N };
-const char *kc_names[KC_N] = {"setup", "phase_tables", "coxmunk_fourier", "primary", "source_gemm",
-                              "transport_scan", "extract", "ipss", "finalize"};
+enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SOURCE_TC, KC_MOL, KC_SCAN, KC_EXTRACT,
+              KC_IPSS, KC_FINAL, KC_N };
+const char *kc_names[KC_N] = {"setup", "phase_tables", "coxmunk_fourier", "primary", "source_gemm_simt",
+                              "source_gemm_tcgen05", "source_molecular_lowrank", "transport_scan", "extract", "ipss",
+                              "finalize"};
 
 int fail(int rc, const std::string &msg)
 {
@@ -133,7 +135,50 @@ struct Wave {
     int Kmax;
     size_t fld, ops, srf;  // element counts of the wave buffers
     bool any_rough, any_flat;
+    int simt_off = 0, n_simt = 0, tc_off = 0, n_tc = 0, mol_off = 0, n_mol = 0;   // source-kernel task lists
 };
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// 2-D FP32 tensor map, rows x cols (row stride = cols), box {32, box_rows},
+// 128-byte swizzle, zero fill outside the tensor.
+bool make_map(CUtensorMap *map, void *base, size_t rows, int cols, int box_rows)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
+    const cuuint32_t box[2] = {32, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool force_simt()
+{
+    const char *e = getenv("OCRT_GB_SOURCE_KERNEL");
+    return e && strcmp(e, "simt") == 0;
+}
 
 struct Group {
     int N = 0, P = 0, T = 0;
@@ -155,11 +200,15 @@ struct Group {
     double *h = nullptr, *ch = nullptr, *xd = nullptr, *yd = nullptr, *z = nullptr;
     float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
+    double *Eatt = nullptr, *lam = nullptr;
     double *mb = nullptr, *mg = nullptr, *ma = nullptr, *mz = nullptr;
     double *kappa = nullptr, *taudir = nullptr;
     int *active_cnt = nullptr, *err = nullptr;
     float *F = nullptr, *J = nullptr, *ops = nullptr, *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     double *Tot = nullptr;
+    int *lists = nullptr;
+    bool use_tc = false;
+    CUtensorMap mapF, mapA;
 };
 
 size_t wave_budget_bytes()
@@ -205,8 +254,8 @@ template <class T> int alloc(T *&dst, size_t n)
 void free_group(Group &g)
 {
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.h, g.ch, g.xd, g.yd, g.z,
-                    g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
-                    g.active_cnt, g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot};
+                    g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
+                    g.active_cnt, g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.lists};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -267,7 +316,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     g.nlev = lev; g.ncoef = coef; g.nmom = mb.size();
     // ---- waves of whole pixels under the workspace budget ----
     const size_t budget = wave_budget_bytes();
-    const size_t op_elems = (size_t)G.CIN * G.LDO;
+    const size_t op_elems = (size_t)G.NP * G.CIN;
     Wave w{0, 0, 0, 0, 0, 0, 0, 0, false, false};
     size_t bytes = 0;
     auto close = [&](int pend) {
@@ -317,7 +366,9 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.Bp, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Br, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Bt, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
-        (rc = alloc(g.cs, (size_t)(g.Mmax + 1) * 2 * (g.nphi / 2))) ||
+        (rc = alloc(g.cs, (size_t)(g.Mmax + 1) * 2 * (g.nphi / 2) + 3 * (size_t)(g.nphi / 2))) ||
+        (rc = alloc(g.Eatt, g.any_rough ? g.nlev * G.NR : 1)) ||
+        (rc = alloc(g.lam, (size_t)g.P * (G.N + 2))) ||
         (rc = alloc(g.frs, (size_t)g.P * G.NR * 9)) ||
         (rc = alloc(g.kappa, g.P)) || (rc = alloc(g.taudir, g.P)) ||
         (rc = alloc(g.active_cnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.err, 1)) ||
@@ -327,6 +378,29 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.srf, g.wave_srf)) ||
         (rc = alloc(g.Bx, (size_t)g.wave_tasks * 6 * (g.Lmax + 1))))
         return rc;
+    // ---- source-kernel task lists: tcgen05 for modes without a molecular
+    // term when the geometry allows it, CUDA cores for the rest ----
+    g.use_tc = tc_supported(G) && !force_simt();
+    if (g.use_tc) {
+        g.use_tc = make_map(&g.mapF, g.F, g.wave_fld / G.LDC, G.LDC, 128) &&
+                   make_map(&g.mapA, g.ops, g.wave_ops / G.CIN, G.CIN, G.NP);
+    }
+    std::vector<int> lists;
+    for (Wave &w : g.waves) {
+        w.simt_off = (int)lists.size();
+        if (!g.use_tc)
+            for (int t = w.t0; t < w.t1; ++t) lists.push_back(t - w.t0);
+        w.n_simt = (int)lists.size() - w.simt_off;
+        w.tc_off = (int)lists.size();
+        if (g.use_tc)
+            for (int t = w.t0; t < w.t1; ++t) lists.push_back(t - w.t0);
+        w.n_tc = (int)lists.size() - w.tc_off;
+        w.mol_off = (int)lists.size();
+        for (int t = w.t0; t < w.t1; ++t)
+            if (g.htask[t].has_mol) lists.push_back(t - w.t0);
+        w.n_mol = (int)lists.size() - w.mol_off;
+    }
+    if ((rc = up(g.lists, lists))) return rc;
     return OCRT_OK;
 }
 
@@ -355,13 +429,17 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     LAUNCH(plan, KC_SETUP, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
     LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
     LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
-    if (g.any_rough) LAUNCH(plan, KC_SETUP, k_cs_table<<<g.Mmax + 1, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
+    if (g.any_rough) {
+        LAUNCH(plan, KC_SETUP, k_cs_table<<<g.Mmax + 2, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
+        LAUNCH(plan, KC_SETUP, k_seed_att<<<dim3(8, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Eatt));
+        LAUNCH(plan, KC_SETUP, k_sancer<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.lam));
+    }
     if (g.any_flat) LAUNCH(plan, KC_SETUP, k_flat_fresnel<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.frs));
 
     BatchBufs B;
     B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
     B.gmu = g.gmu; B.gw = g.gw; B.h = g.h; B.ch = g.ch; B.xd = g.xd; B.yd = g.yd; B.z = g.z;
-    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.active_cnt = g.active_cnt; B.err = g.err;
+    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.Eatt = g.Eatt; B.active_cnt = g.active_cnt; B.err = g.err;
     WaveBufs W;
     W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.pvec = g.pvec;
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
@@ -377,14 +455,23 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
         if (w.any_rough) {
-            const size_t smem = sizeof(float) * 9 * (g.nphi / 2 + 1);
+            const size_t smem = sizeof(float) * (9 * (g.nphi / 2 + 1) + (size_t)(256 / (2 * ((g.Mmax + 4) / 4))) * (g.Mmax + 1) * 9);
             LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
-                       g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.srf));
+                       g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.lam, g.srf));
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
-        const dim3 sgrid(nw, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
+        const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
+        const int mtiles = (w.Kmax + 127) / 128;
+        const size_t tc_smem = tc_smem_bytes(G);
         for (int it = 2; it <= g.max_orders; ++it) {
-            LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
+            if (w.n_simt)
+                LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it, g.lists + w.simt_off));
+            if (w.n_tc)
+                LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<w.n_tc * mtiles, 128, tc_smem, st>>>(
+                           g.mapF, g.mapA, B, W, G, w.t0, g.lists + w.tc_off, w.n_tc, mtiles));
+            if (w.n_mol)
+                LAUNCH(plan, KC_MOL, k_mol_lowrank<<<dim3(w.n_mol, (w.Kmax + 31) / 32), 256, mol_smem_bytes(G), st>>>(
+                           B, W, G, w.t0, g.lists + w.mol_off, g.Bp, g.Br, g.Bt, g.Lmax));
             LAUNCH(plan, KC_SCAN, k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0, it));
             if ((it - 1) % poll == 0 || it == g.max_orders) {
                 CK(cudaMemcpyAsync(g_pinned, g.active_cnt + it, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -435,6 +522,10 @@ int ocrt_gb_init(int device)
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
     CK(cudaMallocHost(&g_pinned, sizeof(int) * 16));
+    CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     g_device = device;
     return OCRT_OK;
 }
@@ -561,8 +652,13 @@ int ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, doubl
                 const TaskDev &tk = g.htask[t];
                 const PixDev &d = g.hpx[tk.pix];
                 const double K = tk.K, nt = d.nt, ords = std::max(0, st[t].orders - 1);
-                plan->flops[KC_SOURCE] += ords * 72.0 * N * N * K;
-                plan->bytes[KC_SOURCE] += ords * (K * 6 * N + K * 6 * NR + 36.0 * N * NR * (tk.has_mol ? 2 : 1)) * 4.0;
+                const int sc = g.use_tc ? KC_SOURCE_TC : KC_SOURCE;
+                plan->flops[sc] += ords * 72.0 * N * N * K;
+                plan->bytes[sc] += ords * (K * 6 * N + K * 6 * NR + 36.0 * N * NR) * 4.0;
+                if (tk.has_mol) {
+                    plan->flops[KC_MOL] += ords * 2.0 * K * 24.0 * (N + 6 * NR);
+                    plan->bytes[KC_MOL] += ords * (K * 6 * N + 2.0 * K * 6 * NR) * 4.0;
+                }
                 plan->bytes[KC_SCAN] += ords * (2.0 * 6 * N * K + N * nt) * 4.0;
                 plan->flops[KC_SCAN] += ords * 6.0 * N * nt * 5.0;
                 plan->bytes[KC_PRIMARY] += K * 6 * NR * 12.0;

@@ -9,9 +9,13 @@
 // order): slots 0..N-1 are the Gauss nodes in ascending mu, slot N is the
 // zero-weight view node when one is inserted (rt_angle_grid.c:37-73).
 // NR = N + 1 is the padded ring width.  Field columns:
-//     c = s * 2*NR + h * NR + g,   s in {I,Q,U}, h = 0 up / 1 down, g = slot
-// so the weighted (Gauss) inputs of the source contraction are six
-// contiguous blocks of N columns.  Field rows are levels k = 0 (TOA) .. nt.
+//     Gauss slot g < N:  c = s * 2N + h * N + g
+//     view slot  g = N:  c = 6N + 2s + h
+// (s in {I,Q,U}, h = 0 up / 1 down), so the weighted inputs of the source
+// contraction are exactly columns [0, 6N) -- six 16-byte aligned blocks of N --
+// and the view columns follow.  Field rows are levels k = 0 (TOA) .. nt.
+// Source operators are stored output-major, Aop[c_out][c_in] with c_in in
+// [0, 6N) contiguous and NP >= 6N + 6 output rows (multiple of 16).
 #pragma once
 #include <cstdint>
 
@@ -45,7 +49,7 @@ struct PixDev {
 struct TaskDev {
     int pix, m, K, has_mol;
     long long fld_off;      // wave-relative offset of F/J/Tot (K * LDC entries)
-    long long op_off;       // wave-relative offset of the aerosol operator (6N * LDO)
+    long long op_off;       // wave-relative offset of the aerosol operator (NP * CIN)
     long long mol_off;      // wave-relative offset of the molecular operator, -1 if none
     long long srf_off;      // wave-relative offset of the surface kernels (NR*N*9 + NR*9), -1 if none
 };
@@ -64,9 +68,10 @@ struct TaskOut {
 };
 
 struct Geom {
-    int N, NR, LDC, LDO;    // LDC: field row stride, LDO: operator row stride
-    int CIN;                // 6N weighted input columns
-    int COUT;               // 6NR output columns
+    int N, NR, LDC;         // LDC: field row stride (floats)
+    int CIN;                // 6N weighted input columns (operator row stride)
+    int COUT;               // 6N + 6 output columns
+    int NP;                 // operator rows, COUT rounded up to 16
 };
 
 __host__ __device__ inline Geom make_geom(int N)
@@ -74,21 +79,21 @@ __host__ __device__ inline Geom make_geom(int N)
     Geom g;
     g.N = N;
     g.NR = N + 1;
-    g.COUT = 6 * g.NR;
-    g.LDC = (g.COUT + 7) & ~7;
-    g.LDO = g.LDC;
     g.CIN = 6 * N;
+    g.COUT = 6 * N + 6;
+    g.LDC = (g.COUT + 7) & ~7;
+    g.NP = (g.COUT + 15) & ~15;
     return g;
 }
 
 __host__ __device__ inline int col_of(const Geom &g, int s, int h, int slot)
 {
-    return s * 2 * g.NR + h * g.NR + slot;
+    return slot < g.N ? s * 2 * g.N + h * g.N + slot : 6 * g.N + 2 * s + h;
 }
 
-// Input column (weighted Gauss direction) -> field column.
+// Input column (weighted Gauss direction) -> field column: the identity.
 __host__ __device__ inline int in_to_col(const Geom &g, int cin)
 {
-    const int blk = cin / g.N, gi = cin - blk * g.N;   // blk = s*2 + h
-    return blk * g.NR + gi;
+    (void)g;
+    return cin;
 }

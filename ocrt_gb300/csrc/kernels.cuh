@@ -1,5 +1,6 @@
 // kernels.cuh — kernel declarations shared by the host orchestration.
 #pragma once
+#include <cuda.h>
 #include "common.cuh"
 #include "../../include/ocrt_gb300.h"
 
@@ -18,9 +19,11 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const double *mb, const double *mg, const double *ma, const double *mz,
                          float *ops, float *pvec, float *fvec);
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
-                          Geom G, const double *gmu, const float *cs_tab, float *srf);
+                          Geom G, const double *gmu, const float *cs_tab, const double *lamv, float *srf);
+__global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam);
 __global__ void k_cs_table(int M, int nphi, float *cs);
 __global__ void k_flat_fresnel(const PixDev *px, int P, int N, const double *gmu, float *frs);
+__global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, double *E);
 
 // sos.cu
 #define ST_M_TILE 64
@@ -41,13 +44,23 @@ struct BatchBufs {
     const double *h, *ch, *xd, *yd, *z;
     const float *Tc, *Ca, *Cb;
     const float *frs;
+    const double *Eatt;    // rough direct-beam attenuation [lev_off*NR + k*NR + g]
     int *active_cnt;       // [max_orders + 2]
     int *err;              // device error word
 };
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
-__global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
+__global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it, const int *list);
+
+// tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
+__global__ void k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
+                            BatchBufs B, WaveBufs W, Geom G, int t0, const int *tc_list, int n_list, int mtiles);
+size_t tc_smem_bytes(const Geom &G);
+bool tc_supported(const Geom &G);
 __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
+__global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, const int *list,
+                              const float *Bp, const float *Br, const float *Bt, int L);
+inline size_t mol_smem_bytes(const Geom &G) { return sizeof(float) * (4 * G.N + G.COUT * 24 + 32 * G.CIN + 32 * 25); }
 __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks);
 
 // post.cu

@@ -92,6 +92,9 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         g_na_base[dev] = p;
     }
     cudaStream_t st = (cudaStream_t)stream;
+    NA_CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    NA_CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    NA_CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 
     // ---- host staging (stack only) ----
     const int N = opts->n_mu, M = opts->fourier_m_max, T = M + 1, nt = opts->n_layers, K = nt + 1;
@@ -117,7 +120,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     const bool flat = cs->surface == OCRT_SURFACE_FLAT ||
                       (cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && cs->wind_speed <= 0.0);
     const bool rough = surf && !flat;
-    const size_t op_elems = (size_t)G.CIN * G.LDO;
+    const size_t op_elems = (size_t)G.NP * G.CIN;
     const size_t srf_elems = (size_t)NR * N * 9 + (size_t)NR * 9;
 
     // ---- carve the static array: fixed part, then as many mode tasks per wave as fit ----
@@ -134,7 +137,9 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     float *Tc = cv.take<float>((size_t)nt * NR), *Ca = cv.take<float>((size_t)nt * NR), *Cb = cv.take<float>((size_t)nt * NR);
     const size_t nb = (size_t)T * (L + 1) * N;
     float *Bp = cv.take<float>(nb), *Br = cv.take<float>(nb), *Bt = cv.take<float>(nb);
-    float *cst = cv.take<float>(rough ? (size_t)T * 2 * (d.nphi / 2) : 1);
+    float *cst = cv.take<float>(rough ? (size_t)(T * 2 + 3) * (d.nphi / 2) : 1);
+    double *Eatt = cv.take<double>(rough ? (size_t)K * NR : 1);
+    double *lamv = cv.take<double>((size_t)N + 2);
     float *frs = cv.take<float>((size_t)NR * 9);
     const int La1 = aer ? aer->L_max + 1 : 1;
     double *mb = cv.take<double>(La1), *mg = cv.take<double>(La1), *ma = cv.take<double>(La1), *mz = cv.take<double>(La1);
@@ -155,6 +160,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     float *pvec = cv.take<float>((size_t)Wt * 2 * G.LDC);
     float *fvec = cv.take<float>((size_t)Wt * 24 * NR);
     float *Bx = cv.take<float>((size_t)Wt * 6 * (L + 1));
+    int *ident = cv.take<int>((size_t)Wt);
     if (!cv.ok) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
 
     TaskDev ht[NA_MAX_M + 1];
@@ -168,9 +174,12 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         ht[m].srf_off = rough ? (long long)m * (long long)srf_elems : -1;
     }
     const int zero = 0;
+    int hident[NA_MAX_M + 1];
+    for (int q = 0; q < Wt; ++q) hident[q] = q;
     NA_CK(cudaMemcpyAsync(px, &d, sizeof(PixDev), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(tasks, ht, sizeof(TaskDev) * T, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(ptask0, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    NA_CK(cudaMemcpyAsync(ident, hident, sizeof(int) * Wt, cudaMemcpyHostToDevice, st));
     if (aer) {
         NA_CK(cudaMemcpyAsync(mb, aer->beta, sizeof(double) * La1, cudaMemcpyHostToDevice, st));
         NA_CK(cudaMemcpyAsync(mg, aer->gamma, sizeof(double) * La1, cudaMemcpyHostToDevice, st));
@@ -188,21 +197,26 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_LAUNCH(k_coef<<<dim3(16, 1), 256, 0, st>>>(px, 1, N, gmu, h, Tc, Ca, Cb));
     NA_LAUNCH(k_basis_gauss<<<T, 64, 0, st>>>(N, M, L, gmu, Bp, Br, Bt));
     if (rough) {
-        NA_LAUNCH(k_cs_table<<<T, 256, 0, st>>>(M, d.nphi, cst));
-        NA_LAUNCH(k_coxmunk<<<dim3(N + 1, NR, 1), 256, sizeof(float) * 9 * (d.nphi / 2 + 1), st>>>(
-            tasks, px, 0, ptask0, G, gmu, cst, srf));
+        NA_LAUNCH(k_cs_table<<<T + 1, 256, 0, st>>>(M, d.nphi, cst));
+        NA_LAUNCH(k_seed_att<<<dim3(8, 1), 256, 0, st>>>(px, 1, N, gmu, h, Eatt));
+        NA_LAUNCH(k_sancer<<<1, 128, 0, st>>>(px, 1, N, gmu, lamv));
+        NA_LAUNCH(k_coxmunk<<<dim3(N + 1, NR, 1), 256, sizeof(float) * (9 * (d.nphi / 2 + 1) + (size_t)(256 / (2 * ((M + 4) / 4))) * (M + 1) * 9), st>>>(
+            tasks, px, 0, ptask0, G, gmu, cst, lamv, srf));
     }
     if (flat) NA_LAUNCH(k_flat_fresnel<<<1, 128, 0, st>>>(px, 1, N, gmu, frs));
 
     BatchBufs B;
     B.px = px; B.tasks = tasks; B.state = state; B.tout = tout; B.gmu = gmu; B.gw = gw;
-    B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs;
+    B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs; B.Eatt = Eatt;
     B.active_cnt = active; B.err = err;
     WaveBufs W;
     W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     for (int t0 = 0; t0 < T; t0 += Wt) {
         const int nw = (T - t0) < Wt ? (T - t0) : Wt;
+        // tasks are ordered by mode, so the molecular (m <= 2) tasks of this
+        // wave are its first nmol entries of the identity list
+        const int nmol = t0 <= 2 ? ((3 - t0) < nw ? (3 - t0) : nw) : 0;
         NA_CK(cudaMemsetAsync(ops, 0, sizeof(float) * 2 * (size_t)nw * op_elems, st));
         NA_CK(cudaMemsetAsync(pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (flat) NA_CK(cudaMemsetAsync(fvec, 0, sizeof(float) * (size_t)nw * 24 * NR, st));
@@ -213,7 +227,10 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= opts->max_orders; ++it) {
-            NA_LAUNCH(k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, t0, it));
+            NA_LAUNCH(k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, t0, it, ident));
+            if (nmol > 0)
+                NA_LAUNCH(k_mol_lowrank<<<dim3(nmol, (K + 31) / 32), 256, mol_smem_bytes(G), st>>>(
+                    B, W, G, t0, ident, Bp, Br, Bt, L));
             NA_LAUNCH(k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, t0, it));
             if ((it - 1) % 4 == 0 || it == opts->max_orders) {
                 int left_active = 0;

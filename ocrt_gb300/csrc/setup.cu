@@ -202,7 +202,7 @@ __device__ inline void put_pair(float *A, const Geom &G, int o, int i, float w, 
            QU_S, QU_C, QUT_S, QUT_C, UU_S, UU_C };
     auto at = [&](int so, int ho, int si, int hi) -> float & {
         const int cin = (si * 2 + hi) * G.N + i;
-        return A[(size_t)cin * G.LDO + col_of(G, so, ho, o)];
+        return A[(size_t)col_of(G, so, ho, o) * G.CIN + cin];
     };
     // I up / down
     at(0, 0, 0, 0) = w * c[II_S];   at(0, 0, 1, 0) = w * c[IQT_S];  at(0, 0, 2, 0) = -w * c[IUT_S];
@@ -302,23 +302,51 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
         c[16] = S[7] + S[8];     c[17] = -D[7] + D[8];      // att[i][+-o]
         const float w = (float)gw[i];
         put_pair(Aop, G, os, i, w, c);
-        if (Bop && mol) {
-            const float pi = basis(0, i, 2), ri = basis(1, i, 2), ti = basis(2, i, 2);
-            const float po = basis(0, os, 2), ro = basis(1, os, 2), to = basis(2, os, 2);
-            const float pmo = par * po, rmo = par * ro, tmo = -par * to;    // at -o
-            const float pmi = par * pi, rmi = par * ri, tmi = -par * ti;    // at -i
-            (void)pmi;
-            float cm[18];
-            cm[0] = b0 + b2 * pi * po;  cm[1] = b0 + b2 * pi * pmo;
-            cm[2] = g2 * pi * to;       cm[3] = g2 * pi * tmo;
-            cm[4] = g2 * po * ti;       cm[5] = g2 * po * tmi;
-            cm[6] = g2 * pi * ro;       cm[7] = g2 * pi * rmo;
-            cm[8] = g2 * po * ri;       cm[9] = g2 * po * rmi;
-            cm[10] = a2 * ri * ro;      cm[11] = a2 * ri * rmo;
-            cm[12] = a2 * ti * ro;      cm[13] = a2 * ti * rmo;
-            cm[14] = a2 * to * ri;      cm[15] = a2 * to * rmi;
-            cm[16] = a2 * ti * to;      cm[17] = a2 * ti * tmo;
-            put_pair(Bop, G, os, i, w, cm);
+    }
+    // ---- molecular operator (m <= 2) in factored form U[c_out][24] ----
+    // Every molecular entry is (function of the outgoing direction) x
+    // w_i f(mu_i), f in {1, P2m, R2m, T2m}; U holds the outgoing factors for
+    // input block b = 2s + h and functional f at column 4b + f.  The sign
+    // pattern is that of the pair contraction in rt_sos_operator.c:387-406.
+    if (Bop && mol) {
+        for (int e = threadIdx.x; e < n * 6; e += blockDim.x) {
+            const int o = e / 6, ob = e - o * 6;
+            const float po = basis(0, o, 2), ro = basis(1, o, 2), to = basis(2, o, 2);
+            const float sr = par, st = -par;                 // r(-x) = sr r(x), t(-x) = st t(x)
+            const float pm = par * po, rm = sr * ro, tm = st * to;
+            float u[24];
+#pragma unroll
+            for (int q = 0; q < 24; ++q) u[q] = 0.f;
+            // u[4*ib + f], ib = 2*s_in + h_in, f: 0 const, 1 P, 2 R, 3 T
+            switch (ob) {
+            case 0:   // I up
+                u[0] = b0; u[1] = b2 * po; u[8 + 2] = g2 * po; u[16 + 3] = -g2 * po;
+                u[4] = b0; u[4 + 1] = b2 * pm; u[12 + 2] = g2 * po * sr; u[20 + 3] = -g2 * po * st;
+                break;
+            case 1:   // I down
+                u[0] = b0; u[1] = b2 * pm; u[8 + 2] = g2 * po * sr; u[16 + 3] = g2 * po * st;
+                u[4] = b0; u[4 + 1] = b2 * po; u[12 + 2] = g2 * po; u[20 + 3] = g2 * po;
+                break;
+            case 2:   // Q up
+                u[1] = g2 * ro; u[8 + 2] = a2 * ro; u[16 + 3] = -a2 * ro;
+                u[4 + 1] = g2 * rm; u[12 + 2] = a2 * rm; u[20 + 3] = a2 * rm;
+                break;
+            case 3:   // Q down
+                u[1] = g2 * rm; u[8 + 2] = a2 * rm; u[16 + 3] = -a2 * rm;
+                u[4 + 1] = g2 * ro; u[12 + 2] = a2 * ro; u[20 + 3] = a2 * ro;
+                break;
+            case 4:   // U up
+                u[1] = -g2 * to; u[8 + 2] = -a2 * to; u[16 + 3] = a2 * to;
+                u[4 + 1] = g2 * tm; u[12 + 2] = -a2 * to * sr; u[20 + 3] = a2 * tm;
+                break;
+            default:  // U down
+                u[1] = -g2 * tm; u[8 + 2] = a2 * to * sr; u[16 + 3] = a2 * tm;
+                u[4 + 1] = g2 * to; u[12 + 2] = a2 * to; u[20 + 3] = a2 * to;
+                break;
+            }
+            const int c = col_of(G, ob >> 1, ob & 1, o);
+#pragma unroll
+            for (int q = 0; q < 24; ++q) Bop[(size_t)c * 24 + q] = u[q];
         }
     }
 
@@ -417,7 +445,7 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
 // mphi in FP32, normalisation dphi/(2pi or pi) and the m>0 IU/QU sign of
 // shared/surface.c:896-906 applied at the end.
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
-                          Geom G, const double *gmu, const float *cs_tab, float *srf)
+                          Geom G, const double *gmu, const float *cs_tab, const double *lamv, float *srf)
 {
     extern __shared__ float sm_R[];                 // [9][nphi/2 + 1]
     const int p = p0 + blockIdx.z;
@@ -430,36 +458,76 @@ __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const 
     const double mo = os < N ? gmu[os] : d.mu_view;
     const double mi = i < N ? gmu[i] : d.mu0;
     const double s2v = slope_variance(d.wind, d.sigma_type);
-    const double lam = sancer_lambda(mi, sqrt(s2v)) + sancer_lambda(mo, sqrt(s2v));
+    // Sancer shadowing terms, precomputed per (pixel, slot); slot N+1 is the sun
+    const double *lp = lamv + (size_t)p * (N + 2);
+    const double lam = lp[i < N ? i : N + 1] + lp[os];
     const int nphi = d.nphi, half = nphi / 2, hs = half + 1;
     const double dphi = 2.0 * OCRT_PI / (double)nphi;
+    const float *ptab = cs_tab + (size_t)(d.M + 1) * 2 * half;     // [cos, sin, sin^2(phi/2)][half]
+    const float fmo = (float)mo, fmi = (float)mi, fs2 = (float)s2v, flam = (float)lam, fnw = (float)d.n_water;
     for (int q = threadIdx.x; q < half; q += blockDim.x) {
-        const double phi = (q + 0.5) * dphi;
         float R[9];
-        const double sh = sin(0.5 * phi);
-        coxmunk_R<float>((float)mo, (float)mi, (float)cos(phi), (float)sin(phi), (float)(sh * sh), (float)s2v,
-                         (float)lam, (float)d.n_water, d.q_conv, R);
+        coxmunk_R<float>(fmo, fmi, ptab[q], ptab[half + q], ptab[2 * half + q], fs2, flam, fnw, d.q_conv, R);
 #pragma unroll
         for (int e = 0; e < 9; ++e) sm_R[e * hs + q] = R[e];
     }
     __syncthreads();
+    // Projection onto cos/sin(m phi): work item = (cos or sin entry group,
+    // group of 4 modes); threads beyond the item count split the azimuth
+    // range and are reduced through shared memory.  Each thread keeps a 5x4
+    // (cos) or 4x4 (sin) register tile, so every table value and every
+    // Mueller value it loads feeds 4-5 FMAs.
     const int M = d.M;
+    const int nmg = (M + 4) / 4;                    // mode groups of 4
+    const int items = 2 * nmg;
+    const int S = blockDim.x / items;               // azimuth slices (>= 1)
+    float *part = sm_R + 9 * hs;                    // [S][(M+1)*9]
     const int nout = (M + 1) * 9;
-    const int task_first = pix_task0[p];
-    for (int e2 = threadIdx.x; e2 < nout; e2 += blockDim.x) {
-        const int m = e2 / 9, e = e2 - m * 9;
-        const bool is_cos = (e == 0 || e == 1 || e == 3 || e == 4 || e == 8);
-        const float *tab = cs_tab + ((size_t)m * 2 + (is_cos ? 0 : 1)) * half;
-        const float *rv = sm_R + e * hs;
-        float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
-        int q = 0;
-        for (; q + 3 < half; q += 4) {
-            acc0 += rv[q] * tab[q]; acc1 += rv[q + 1] * tab[q + 1];
-            acc2 += rv[q + 2] * tab[q + 2]; acc3 += rv[q + 3] * tab[q + 3];
+    const int t = threadIdx.x;
+    const int item = t % items, slice = t / items;
+    if (slice < S) {
+        const int kind = item & 1, mg = item >> 1;  // kind 0: cos entries, 1: sin entries
+        const int ecos[5] = {0, 1, 3, 4, 8}, esin[4] = {2, 5, 6, 7};
+        const int ne = kind == 0 ? 5 : 4;
+        const int q0 = (int)((long long)half * slice / S), q1 = (int)((long long)half * (slice + 1) / S);
+        float acc[5][4];
+#pragma unroll
+        for (int a = 0; a < 5; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+        const float *tb[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int m = min(4 * mg + b, M);
+            tb[b] = cs_tab + ((size_t)m * 2 + kind) * half;
         }
-        for (; q < half; ++q) acc0 += rv[q] * tab[q];
-        double v = 2.0 * (((double)acc0 + (double)acc1) + ((double)acc2 + (double)acc3));
-        v *= dphi * (m == 0 ? 1.0 / (2.0 * OCRT_PI) : 1.0 / OCRT_PI);
+        for (int q = q0; q < q1; ++q) {
+            float tv[4], rv[5];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) tv[b] = __ldg(tb[b] + q);
+#pragma unroll
+            for (int a = 0; a < 5; ++a) rv[a] = a < ne ? sm_R[(kind == 0 ? ecos[a] : esin[a < 4 ? a : 3]) * hs + q] : 0.f;
+#pragma unroll
+            for (int a = 0; a < 5; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(rv[a], tv[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int m = 4 * mg + b;
+            if (m > M) continue;
+#pragma unroll
+            for (int a = 0; a < 5; ++a)
+                if (a < ne) part[(size_t)slice * nout + m * 9 + (kind == 0 ? ecos[a] : esin[a])] = acc[a][b];
+        }
+    }
+    __syncthreads();
+    const int task_first = pix_task0[p];
+    for (int e2 = t; e2 < nout; e2 += blockDim.x) {
+        const int m = e2 / 9, e = e2 - m * 9;
+        double v = 0.0;
+        for (int sl = 0; sl < S; ++sl) v += (double)part[(size_t)sl * nout + e2];
+        v *= 2.0 * dphi * (m == 0 ? 1.0 / (2.0 * OCRT_PI) : 1.0 / OCRT_PI);
         if (m > 0 && (e == 2 || e == 5)) v = -v;
         const TaskDev &tk = tasks[task_first + m];
         float *dst = srf + tk.srf_off;
@@ -468,7 +536,9 @@ __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const 
     }
 }
 
-// cos / sin(m phi_q) on the half azimuth grid, FP64 evaluated.
+// cos / sin(m phi_q) on the half azimuth grid for m = 0..M, followed by the
+// rows cos(phi), sin(phi), sin^2(phi/2) used by the Mueller evaluation; all
+// evaluated in FP64 (grid launch: M + 2 blocks).
 __global__ void k_cs_table(int M, int nphi, float *cs)
 {
     const int half = nphi / 2;
@@ -476,8 +546,46 @@ __global__ void k_cs_table(int M, int nphi, float *cs)
     const double dphi = 2.0 * OCRT_PI / (double)nphi;
     for (int q = threadIdx.x; q < half; q += blockDim.x) {
         const double phi = (q + 0.5) * dphi;
-        cs[((size_t)m * 2 + 0) * half + q] = (float)cos(m * phi);
-        cs[((size_t)m * 2 + 1) * half + q] = (float)sin(m * phi);
+        if (m <= M) {
+            cs[((size_t)m * 2 + 0) * half + q] = (float)cos(m * phi);
+            cs[((size_t)m * 2 + 1) * half + q] = (float)sin(m * phi);
+        } else {
+            float *pt = cs + (size_t)(M + 1) * 2 * half;
+            const double sh = sin(0.5 * phi);
+            pt[q] = (float)cos(phi);
+            pt[half + q] = (float)sin(phi);
+            pt[2 * half + q] = (float)(sh * sh);
+        }
+    }
+}
+
+// Sancer shadowing term lambda(mu) (shared/surface.c:578-598) of every ring
+// slot and of the sun, once per rough pixel: lam[p*(N+2) + slot], slot N+1 = sun.
+__global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam)
+{
+    const int p = blockIdx.x, s = threadIdx.x;
+    if (p >= P || s > N + 1) return;
+    const PixDev &d = px[p];
+    if (!d.rough) return;
+    const double mu = s < N ? gmu[s] : (s == N ? d.mu_view : d.mu0);
+    lam[(size_t)p * (N + 2) + s] = sancer_lambda(mu, sqrt(slope_variance(d.wind, d.sigma_type)));
+}
+
+// Direct-beam attenuation from the surface to level k along slot g,
+// exp(-(tau - h_k)/mu_g), FP64, once per pixel (shared by every mode):
+// E[lev_off*NR + k*NR + g].
+__global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, double *E)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    if (!d.rough) return;
+    const int NR = N + 1, total = (d.nt + 1) * NR;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int k = e / NR, g = e - k * NR;
+        double am = g < N ? gmu[g] : d.mu_view;
+        if (g >= d.n_ring) am = 1.0;
+        E[d.lev_off * NR + e] = exp(-(d.tau_total - h[d.lev_off + k]) / am);
     }
 }
 

@@ -4,8 +4,11 @@
 //                  reflected-beam source (rt_surface_boundary.c:210-428) and the
 //                  rough direct-beam seed (rt_surface_boundary.c:430-493), then
 //                  the formal solution of order 1 (rt_layer_transport.c:107-208).
-//   k_source_simt  multiple-scattering source J = x*(A F) + y*(B F) over all levels
-//                  (rt_sos_operator.c:206-424) as a tiled FP32 GEMM on CUDA cores.
+//   k_source_simt  aerosol part of the multiple-scattering source, J = x * (A F) over all
+//                  levels (rt_sos_operator.c:206-424), tiled FP32 GEMM on CUDA cores (used
+//                  where the tcgen05 kernel's shape rules do not hold).
+//   k_mol_lowrank  molecular part for m <= 2, J += y * U (V F) with the rank-24 factored
+//                  molecular operator.
 //   k_scan         surface boundary condition (rt_surface_boundary.c:137-208),
 //                  up/down formal solution, FP64 order totals, sup-norm residual and
 //                  the convergence test (rt_solver.c:2923-3150).
@@ -13,12 +16,22 @@
 #include "kernels.cuh"
 #include "physics.cuh"
 
+// Field column -> (Stokes s, hemisphere h, ring slot g); columns past the view
+// block decode to slot NR (never a valid ring slot).
 __device__ inline void decode_col(const Geom &G, int c, int &s, int &h, int &g)
 {
-    s = c / (2 * G.NR);
-    const int r = c - s * 2 * G.NR;
-    h = r / G.NR;
-    g = r - h * G.NR;
+    const int N = G.N;
+    if (c < 6 * N) {
+        s = c / (2 * N);
+        const int r = c - s * 2 * N;
+        h = r / N;
+        g = r - h * N;
+    } else if (c < 6 * N + 6) {
+        const int v = c - 6 * N;
+        s = v >> 1; h = v & 1; g = N;
+    } else {
+        s = 0; h = 0; g = G.NR;
+    }
 }
 
 __device__ inline double ring_mu(const PixDev &d, const double *gmu, int N, int g)
@@ -26,14 +39,15 @@ __device__ inline double ring_mu(const PixDev &d, const double *gmu, int N, int 
     return g < N ? gmu[g] : d.mu_view;
 }
 
-// Rough direct-beam seed at level k for upward slot g, Stokes s (FP64).
-__device__ inline double rough_seed(const PixDev &d, const TaskDev &tk, const WaveBufs &W, const Geom &G,
-                                    const double *gmu, double hk, int g, int s)
+// Rough direct-beam seed at level k for upward slot g, Stokes s (FP64):
+// (pi or pi/2) mu0 exp(-tau/mu0) exp(-(tau-h_k)/mu_g) R_m(mu_g, mu0)[s,I]
+// (rt_surface_boundary.c:430-493).
+__device__ inline double rough_seed(const PixDev &d, const TaskDev &tk, const WaveBufs &W, const BatchBufs &B,
+                                    const Geom &G, double tdn, int k, int g, int s)
 {
     const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * G.N * 9;
-    const double tdn = exp(-d.tau_total / d.mu0);
     const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
-    return fs * tdn * exp(-(d.tau_total - hk) / ring_mu(d, gmu, G.N, g)) * (double)Rs[g * 9 + s * 3];
+    return fs * tdn * B.Eatt[(d.lev_off + k) * G.NR + g] * (double)Rs[g * 9 + s * 3];
 }
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
@@ -80,19 +94,21 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
         fm1 = fm[s * NR + g]; fm2 = fm[(s + 3) * NR + g];
     }
     int bad = 0;
+    const float faP = (float)aP, fmP = (float)mP;
+    const double tdn = exp(-d.tau_total / d.mu0);
     auto Jat = [&](int k) -> float {
-        const double x = xd[k], y = yd[k];
-        double v = ch[k] * (x * aP + y * mP);
+        const float x = (float)xd[k], y = (float)yd[k];
+        float v = (float)ch[k] * (x * faP + y * fmP);
         if (d.flat && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
             const double beam = sb * exp(hh[k] / d.mu0);
-            v += beam * (RI * (x * fa1 + y * fm1) + RQ * (x * fa2 + y * fm2));
+            v += (float)(beam * (RI * (x * fa1 + y * fm1) + RQ * (x * fa2 + y * fm2)));
         }
         if (!isfinite(v)) bad = 1;
-        return (float)v;
+        return v;
     };
     auto store = [&](int k, float I) {
         double seed = 0.0;
-        if (d.rough && h == 0) seed = rough_seed(d, tk, W, G, B.gmu, hh[k], g, s);
+        if (d.rough && h == 0) seed = rough_seed(d, tk, W, B, G, tdn, k, g, s);
         F[(size_t)k * G.LDC + c] = (float)((double)I + seed);
         Tot[(size_t)k * G.LDC + c] = (double)I + seed;
     };
@@ -125,9 +141,10 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
 #define ST_K 16
 #define ST_M 64
 #define ST_N 64
-__global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
+__global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it,
+                                                     const int *list)
 {
-    const int tl = blockIdx.x, tg = t0 + tl;
+    const int tl = list[blockIdx.x], tg = t0 + tl;
     if (!B.state[tg].active) return;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
@@ -136,12 +153,10 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
     if (k0 > nt || c0 >= G.COUT) return;
     __shared__ float Fs[ST_K][ST_M + 4];
     __shared__ float As[ST_K][ST_N + 4];
-    __shared__ float Bs[ST_K][ST_N + 4];
     const float *F = W.F + tk.fld_off;
     const float *A = W.ops + tk.op_off;
-    const float *Bm = tk.has_mol ? W.ops + tk.mol_off : nullptr;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    float accA[4][4] = {{0}}, accB[4][4] = {{0}};
+    float accA[4][4] = {{0}};
     for (int kc = 0; kc < G.CIN; kc += ST_K) {
         for (int idx = threadIdx.x; idx < ST_M * ST_K; idx += 256) {
             const int lv = idx / ST_K, kk = idx - lv * ST_K;
@@ -149,11 +164,10 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
             Fs[kk][lv] = (k <= nt && ci < G.CIN) ? F[(size_t)k * G.LDC + in_to_col(G, ci)] : 0.f;
         }
         for (int idx = threadIdx.x; idx < ST_K * ST_N; idx += 256) {
-            const int kk = idx / ST_N, cc = idx - kk * ST_N;
+            const int cc = idx / ST_K, kk = idx - cc * ST_K;
             const int ci = kc + kk, co = c0 + cc;
-            const bool ok = ci < G.CIN && co < G.LDO;
-            As[kk][cc] = ok ? A[(size_t)ci * G.LDO + co] : 0.f;
-            if (Bm) Bs[kk][cc] = ok ? Bm[(size_t)ci * G.LDO + co] : 0.f;
+            const bool ok = ci < G.CIN && co < G.NP;
+            As[kk][cc] = ok ? A[(size_t)co * G.CIN + ci] : 0.f;
         }
         __syncthreads();
 #pragma unroll
@@ -167,30 +181,73 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
             for (int i = 0; i < 4; ++i)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) accA[i][j] = fmaf(fr[i], ar[j], accA[i][j]);
-            if (Bm) {
-                float br[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) br[j] = Bs[kk][tx + 16 * j];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) accB[i][j] = fmaf(fr[i], br[j], accB[i][j]);
-            }
         }
         __syncthreads();
     }
     float *J = W.J + tk.fld_off;
-    const double *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
+    const double *xd = B.xd + d.lev_off;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int k = k0 + ty + 16 * i;
         if (k > nt) continue;
-        const float x = (float)xd[k], y = (float)yd[k];
+        const float x = (float)xd[k];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int c = c0 + tx + 16 * j;
-            if (c < G.COUT) J[(size_t)k * G.LDC + c] = x * accA[i][j] + y * accB[i][j];
+            if (c < G.COUT) J[(size_t)k * G.LDC + c] = x * accA[i][j];
         }
+    }
+}
+
+// Molecular source for m <= 2 tasks: xi[k][4b+f] = sum_i w_i f(mu_i) F[k][bN+i]
+// (f in {1, P2m, R2m, T2m}), then J[k][c] += y_k sum_r U[c][r] xi[k][r].
+// Grid (task in list, tile of 32 levels), 256 threads.
+__global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, const int *list,
+                                                     const float *Bp, const float *Br, const float *Bt, int L)
+{
+    extern __shared__ float sm[];
+    const int tl = list[blockIdx.x], tg = t0 + tl;
+    if (!B.state[tg].active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt, N = G.N, k0 = blockIdx.y * 32;
+    if (k0 > nt) return;
+    const int nk = min(32, nt - k0 + 1);
+    float *fv = sm;                          // [4][N]
+    float *U = fv + 4 * N;                   // [COUT][24]
+    float *Fs = U + G.COUT * 24;             // [32][6N]
+    float *xi = Fs + 32 * G.CIN;             // [32][25]
+    const size_t gb = (size_t)tk.m * (L + 1) * N + (size_t)2 * N;    // degree-2 row of mode m
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float w = (float)B.gw[i];
+        fv[i] = w; fv[N + i] = w * Bp[gb + i]; fv[2 * N + i] = w * Br[gb + i]; fv[3 * N + i] = w * Bt[gb + i];
+    }
+    const float *Ug = W.ops + tk.mol_off;
+    for (int e = threadIdx.x; e < G.COUT * 24; e += blockDim.x) U[e] = Ug[e];
+    const float *F = W.F + tk.fld_off + (size_t)k0 * G.LDC;
+    for (int e = threadIdx.x; e < nk * G.CIN; e += blockDim.x) {
+        const int k = e / G.CIN, ci = e - k * G.CIN;
+        Fs[k * G.CIN + ci] = F[(size_t)k * G.LDC + ci];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nk * 24; e += blockDim.x) {
+        const int k = e / 24, r = e - k * 24, b = r >> 2, f = r & 3;
+        const float *fr = Fs + k * G.CIN + b * N;
+        const float *ff = fv + f * N;
+        float acc = 0.f;
+        for (int i = 0; i < N; ++i) acc = fmaf(ff[i], fr[i], acc);
+        xi[k * 25 + r] = acc;
+    }
+    __syncthreads();
+    float *J = W.J + tk.fld_off;
+    const double *yd = B.yd + d.lev_off;
+    for (int e = threadIdx.x; e < nk * G.COUT; e += blockDim.x) {
+        const int k = e / G.COUT, c = e - k * G.COUT;
+        const float *u = U + c * 24, *x = xi + k * 25;
+        float acc = 0.f;
+#pragma unroll
+        for (int r = 0; r < 24; ++r) acc = fmaf(u[r], x[r], acc);
+        J[(size_t)(k0 + k) * G.LDC + c] += (float)yd[k0 + k] * acc;
     }
 }
 
@@ -257,26 +314,74 @@ __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
             mi = fmax(mi, fabs((double)I));
             mt = fmax(mt, fabs(t));
         };
+        // Levels are processed in chunks of PF: every load of a chunk is issued
+        // before the dependent recurrence runs, so the scan is not bound by one
+        // memory round trip per level.
+        constexpr int PF = 8;
         if (h == 0) {
-            float I = bc, Jn = J[(size_t)nt * G.LDC + c];
+            float I = bc;
             put(nt, I);
-            for (int k = nt - 1; k >= 0; --k) {
-                const float Jk = J[(size_t)k * G.LDC + c];
-                const int e = k * NR + g;
-                I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jn;
-                put(k, I);
-                Jn = Jk;
+            float Jn = J[(size_t)nt * G.LDC + c];
+            for (int k1 = nt - 1; k1 >= 0; k1 -= PF) {
+                const int cnt = k1 + 1 < PF ? k1 + 1 : PF;
+                float jv[PF], tv[PF], av[PF], bv[PF];
+                double ov[PF];
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 - q, e = k * NR + g;
+                        jv[q] = J[(size_t)k * G.LDC + c];
+                        tv[q] = Tc[e]; av[q] = Ca[e]; bv[q] = Cb[e];
+                        ov[q] = Tot[(size_t)k * G.LDC + c];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 - q;
+                        I = tv[q] * I + av[q] * jv[q] + bv[q] * Jn;
+                        Jn = jv[q];
+                        const size_t o = (size_t)k * G.LDC + c;
+                        F[o] = I;
+                        const double t = ov[q] + (double)I;
+                        Tot[o] = t;
+                        mi = fmax(mi, fabs((double)I));
+                        mt = fmax(mt, fabs(t));
+                    }
+                }
             }
             bad = !isfinite(I);
         } else {
-            float I = 0.f, Jp = J[c];
+            float I = 0.f;
             put(0, I);
-            for (int k = 1; k <= nt; ++k) {
-                const float Jk = J[(size_t)k * G.LDC + c];
-                const int e = (k - 1) * NR + g;
-                I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jp;
-                put(k, I);
-                Jp = Jk;
+            float Jp = J[c];
+            for (int k1 = 1; k1 <= nt; k1 += PF) {
+                const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
+                float jv[PF], tv[PF], av[PF], bv[PF];
+                double ov[PF];
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 + q, e = (k - 1) * NR + g;
+                        jv[q] = J[(size_t)k * G.LDC + c];
+                        tv[q] = Tc[e]; av[q] = Ca[e]; bv[q] = Cb[e];
+                        ov[q] = Tot[(size_t)k * G.LDC + c];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 + q;
+                        I = tv[q] * I + av[q] * jv[q] + bv[q] * Jp;
+                        Jp = jv[q];
+                        const size_t o = (size_t)k * G.LDC + c;
+                        F[o] = I;
+                        const double t = ov[q] + (double)I;
+                        Tot[o] = t;
+                        mi = fmax(mi, fabs((double)I));
+                        mt = fmax(mt, fabs(t));
+                    }
+                }
             }
             bad = !isfinite(I);
         }
@@ -318,9 +423,10 @@ __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
     const double *Tot = W.Tot + tk.fld_off;
     const int nt = d.nt, N = G.N, vs = d.view_slot;
     const double *hh = B.h + d.lev_off;
+    const double tdn = exp(-d.tau_total / d.mu0);
     auto up0 = [&](int s, int g) -> double {
         double v = Tot[col_of(G, s, 0, g)];
-        if (d.rough) v -= rough_seed(d, tk, W, G, B.gmu, hh[0], g, s);
+        if (d.rough) v -= rough_seed(d, tk, W, B, G, tdn, 0, g, s);
         return v;
     };
     auto dn = [&](int g) -> double { return Tot[(size_t)nt * G.LDC + col_of(G, 0, 1, g)]; };

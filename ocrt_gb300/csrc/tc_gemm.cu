@@ -1,0 +1,300 @@
+// tc_gemm.cu — multiple-scattering source contraction on the tcgen05 tensor
+// cores (rt_sos_operator.c:206-424 for modes without a molecular term, m > 2).
+//
+// Per CTA: one (task, 128-level tile).  D[128 levels][NP outputs] (FP32 in
+// TMEM) = F[128 levels][6N inputs] x Aop^T, K = 6N swept in 32-element tiles
+// (one 128-byte swizzle row).  Each K tile is brought in by TMA into a
+// SWIZZLE_128B K-major layout, split in place into tf32 hi and lo parts, and
+// contracted with three tcgen05.mma.kind::tf32 passes (hi*hi + hi*lo + lo*hi),
+// which carries FP32-level accuracy on the TF32 tensor path.  The epilogue
+// reads TMEM with tcgen05.ld and writes J = x_k * D.
+//
+// Every wait is time-bounded: on timeout the CTA records an error word,
+// drains its own in-flight copies with a second bounded wait, frees TMEM and
+// returns.
+#include <cuda.h>
+#include <cstdint>
+#include "kernels.cuh"
+
+#define TC_M 128
+#define TC_KT 32
+#define TC_THREADS 128
+#define TC_TMEM_COLS 256
+#define TC_WAIT_NS 2000000000ull
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Wait for phase `parity` of a barrier; false after TC_WAIT_NS nanoseconds.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer() - t0 > TC_WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+                 ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major with 128-byte swizzle: rows of
+// 128 B, 8-row groups 1024 B apart (SBO), LBO unused, version 1 (sm_100 family).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Instruction descriptor: D F32, A/B TF32, both K-major, shape M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+} // namespace
+
+// Split a raw FP32 tile in place into a tf32 head (kept in place) and a tf32
+// tail (written to `lo`), each rounded to nearest, so x = hi + lo to ~2^-22
+// relative and the MMA's own tf32 reading of either part is exact.
+__device__ __forceinline__ uint32_t round_tf32(uint32_t u)
+{
+    return (u + 0x1000u) & 0xFFFFE000u;
+}
+
+__device__ __forceinline__ void split_tf32(uint32_t *hi, uint32_t *lo, int n)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t u = hi[i];
+        const uint32_t h = round_tf32(u);
+        hi[i] = h;
+        lo[i] = round_tf32(__float_as_uint(__uint_as_float(u) - __uint_as_float(h)));
+    }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
+            BatchBufs B, WaveBufs W, Geom G, int t0, const int *tc_list, int n_list, int mtiles)
+{
+    extern __shared__ unsigned char smem_raw[];
+    const int item = blockIdx.x;
+    const int li = item / mtiles, mt = item - li * mtiles;
+    if (li >= n_list) return;
+    const int tl = tc_list[li], tg = t0 + tl;
+    if (!B.state[tg].active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt, k0 = mt * TC_M;
+    if (k0 > nt) return;
+
+    const int NP = G.NP;
+    const uint32_t A_BYTES = TC_M * TC_KT * 4, B_BYTES = (uint32_t)NP * TC_KT * 4;
+    const uint32_t STAGE = 2 * A_BYTES + 2 * B_BYTES;
+    unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(base + 2 * STAGE);     // full[2], empty[2], done
+    uint32_t *tslot = (uint32_t *)(bars + 5);
+    int *abort_flag = (int *)(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 5; ++i) mbar_init(&bars[i], 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+
+    const int NKT = G.CIN / TC_KT;
+    const int rowF = (int)(tk.fld_off / G.LDC) + k0;
+    const int rowA = (int)(tk.op_off / G.CIN);
+    uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
+    auto stage_ptr = [&](int s) { return base + (size_t)s * STAGE; };
+    int inflight[2] = {0, 0};
+    if (tid == 0) {
+        for (int s = 0; s < 2 && s < NKT; ++s) {
+            unsigned char *sp = stage_ptr(s);
+            mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+            tma_load_2d(sp, &mapF, &full[s], s * TC_KT, rowF);
+            tma_load_2d(sp + 2 * A_BYTES, &mapA, &full[s], s * TC_KT, rowA);
+            inflight[s] = 1;
+        }
+    }
+    uint32_t ph_full[2] = {0, 0}, ph_empty[2] = {0, 0};
+    constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
+    const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(NP >> 3) << 17);
+    bool ok = true, done_committed = false;
+    for (int kt = 0; kt < NKT; ++kt) {
+        const int s = kt & 1;
+        if (mbar_wait(&full[s], ph_full[s])) ph_full[s] ^= 1;
+        else atomicExch(abort_flag, 1);
+        __syncthreads();
+        if (*abort_flag) { ok = false; break; }
+        if (tid == 0) inflight[s] = 0;
+        unsigned char *sp = stage_ptr(s);
+        uint32_t *ahi = (uint32_t *)sp, *alo = (uint32_t *)(sp + A_BYTES);
+        uint32_t *bhi = (uint32_t *)(sp + 2 * A_BYTES), *blo = (uint32_t *)(sp + 2 * A_BYTES + B_BYTES);
+        split_tf32(ahi, alo, TC_M * TC_KT);
+        split_tf32(bhi, blo, NP * TC_KT);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa_hi = smem_u32(ahi), sa_lo = smem_u32(alo);
+            const uint32_t sb_hi = smem_u32(bhi), sb_lo = smem_u32(blo);
+#pragma unroll
+            for (int kk = 0; kk < TC_KT / 8; ++kk) {
+                const uint32_t off = kk * 32;     // 8 tf32 = 32 bytes along the swizzled row
+                const uint64_t ah = sdesc_sw128(sa_hi + off), al = sdesc_sw128(sa_lo + off);
+                const uint64_t bh = sdesc_sw128(sb_hi + off), bl = sdesc_sw128(sb_lo + off);
+                umma_tf32(tmem, ah, bh, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+                umma_tf32(tmem, ah, bl, idesc, 1u);
+                umma_tf32(tmem, al, bh, idesc, 1u);
+            }
+            umma_commit(&empty[s]);
+            if (kt + 2 < NKT) {
+                if (!mbar_wait(&empty[s], ph_empty[s])) {
+                    atomicExch(abort_flag, 1);
+                } else {
+                    mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+                    tma_load_2d(sp, &mapF, &full[s], (kt + 2) * TC_KT, rowF);
+                    tma_load_2d(sp + 2 * A_BYTES, &mapA, &full[s], (kt + 2) * TC_KT, rowA);
+                    inflight[s] = 1;
+                }
+                ph_empty[s] ^= 1;
+            }
+        }
+    }
+    if (ok) {
+        if (tid == 0) umma_commit(done);
+        done_committed = true;
+        if (!mbar_wait(done, 0)) atomicExch(abort_flag, 1);
+        __syncthreads();
+        ok = *abort_flag == 0;
+    }
+    if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int lane = tid & 31;
+        const int k = k0 + warp * 32 + lane;
+        const float x = k <= nt ? (float)B.xd[d.lev_off + k] : 0.f;
+        float *Jrow = W.J + tk.fld_off + (size_t)k * G.LDC;
+        for (int cb = 0; cb < NP / 16; ++cb) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 16), v);
+            if (k <= nt) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int c = cb * 16 + j;
+                    if (c < G.COUT) Jrow[c] = x * v[j];
+                }
+            }
+        }
+    } else {
+        if (tid == 0) {
+            atomicExch(B.err, OCRT_ERR_DEVICE);
+            // drain this CTA's own copies and MMAs still in flight (bounded)
+            for (int s = 0; s < 2; ++s)
+                if (inflight[s]) mbar_wait(&full[s], ph_full[s]);
+            if (!done_committed) umma_commit(done);
+            mbar_wait(done, 0);
+        }
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+size_t tc_smem_bytes(const Geom &G)
+{
+    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)G.NP * TC_KT * 4) + 64;
+}
+
+bool tc_supported(const Geom &G)
+{
+    return (G.CIN % TC_KT) == 0 && G.NP <= 256 && tc_smem_bytes(G) <= 227 * 1024;
+}

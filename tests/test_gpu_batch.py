@@ -84,3 +84,35 @@ def test_plan_reexecute_is_deterministic(gpu):
     assert np.array_equal(r1, r2)
     assert plan.stats()["kernel_launches"] > 0
     plan.close()
+
+
+def test_tcgen05_and_cuda_core_source_agree(gpu, oracle):
+    """The tcgen05 3xTF32 contraction and the CUDA-core FP32 contraction give the
+    same solve within the parity bar, and both match the oracle."""
+    import os
+    cs, os_, aa = _batch(24, seed=33, n_mu=32, m_max=8, L=60)
+    try:
+        os.environ["OCRT_GB_SOURCE_KERNEL"] = "simt"
+        r_simt = gpu.solve_batch(cs, os_, aa)
+    finally:
+        os.environ.pop("OCRT_GB_SOURCE_KERNEL", None)
+    r_tc = gpu.solve_batch(cs, os_, aa)
+    for i in range(len(cs)):
+        ref = oracle.solve(cs[i], os_[i], aa[i])
+        assert_parity({k: r_tc[k][i] for k in ("rho_I", "rho_Q", "rho_U")}, ref, f"tcgen05 pixel {i}")
+        assert_parity({k: r_simt[k][i] for k in ("rho_I", "rho_Q", "rho_U")}, ref, f"simt pixel {i}")
+        assert abs(r_tc["rho_I"][i] - r_simt["rho_I"][i]) <= 2e-6 * abs(r_simt["rho_I"][i])
+
+
+def test_tcgen05_kernel_is_used(gpu):
+    cs, os_, aa = _batch(8, seed=34, n_mu=32, m_max=6, L=40)
+    gpu.set_timing(True)
+    try:
+        plan = gpu.Plan(cs, os_, aa)
+        plan.execute()
+        ks = plan.kernel_stats()
+        plan.close()
+    finally:
+        gpu.set_timing(False)
+    assert ks["source_gemm_tcgen05"]["launches"] > 0
+    assert ks["source_gemm_tcgen05"]["ms"] > 0
