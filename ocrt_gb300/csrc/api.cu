@@ -24,6 +24,7 @@ namespace {
 std::mutex g_mu;
 thread_local std::string g_err;
 int g_device = -1;
+int g_nsm = 152;           // SM count of the device, read at init
 cudaStream_t g_stream = nullptr;
 std::multimap<size_t, void *> g_free;      // caching allocator: size -> block
 std::map<void *, size_t> g_live;
@@ -135,7 +136,7 @@ struct Wave {
     int Kmax;
     size_t fld, ops, srf;  // element counts of the wave buffers
     bool any_rough, any_flat;
-    int simt_off = 0, n_simt = 0, tc_off = 0, n_tc = 0, mol_off = 0, n_mol = 0;   // source-kernel task lists
+    int n_simt = 0, n_tc = 0, n_mol = 0;   // tasks given to each source kernel
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -203,10 +204,10 @@ struct Group {
     double *Eatt = nullptr, *lam = nullptr;
     double *mb = nullptr, *mg = nullptr, *ma = nullptr, *mz = nullptr;
     double *kappa = nullptr, *taudir = nullptr;
-    int *active_cnt = nullptr, *err = nullptr;
+    int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
+    int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
     float *F = nullptr, *J = nullptr, *ops = nullptr, *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     double *Tot = nullptr;
-    int *lists = nullptr;
     bool use_tc = false;
     CUtensorMap mapF, mapA;
 };
@@ -255,7 +256,8 @@ void free_group(Group &g)
 {
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
-                    g.active_cnt, g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.lists};
+                    g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
+                    g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -371,36 +373,31 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.lam, (size_t)g.P * (G.N + 2))) ||
         (rc = alloc(g.frs, (size_t)g.P * G.NR * 9)) ||
         (rc = alloc(g.kappa, g.P)) || (rc = alloc(g.taudir, g.P)) ||
-        (rc = alloc(g.active_cnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.err, 1)) ||
+        (rc = alloc(g.active_cnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.mol_cnt, (size_t)g.max_orders + 2)) ||
+        (rc = alloc(g.work, 4 * ((size_t)g.max_orders + 2))) || (rc = alloc(g.err, 1)) ||
+        (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
+        (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
         (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) || (rc = alloc(g.Tot, g.wave_fld)) ||
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
         (rc = alloc(g.srf, g.wave_srf)) ||
         (rc = alloc(g.Bx, (size_t)g.wave_tasks * 6 * (g.Lmax + 1))))
         return rc;
-    // ---- source-kernel task lists: tcgen05 for modes without a molecular
-    // term when the geometry allows it, CUDA cores for the rest ----
+    // ---- source kernels: tcgen05 for the aerosol contraction when the
+    // geometry allows it, CUDA cores otherwise; the low-rank molecular kernel
+    // adds the m <= 2 Rayleigh term.  The per-order task lists themselves are
+    // built on the device (k_primary, k_scan). ----
     g.use_tc = tc_supported(G) && !force_simt();
     if (g.use_tc) {
         g.use_tc = make_map(&g.mapF, g.F, g.wave_fld / G.LDC, G.LDC, 128) &&
                    make_map(&g.mapA, g.ops, g.wave_ops / G.CIN, G.CIN, G.NP);
     }
-    std::vector<int> lists;
     for (Wave &w : g.waves) {
-        w.simt_off = (int)lists.size();
-        if (!g.use_tc)
-            for (int t = w.t0; t < w.t1; ++t) lists.push_back(t - w.t0);
-        w.n_simt = (int)lists.size() - w.simt_off;
-        w.tc_off = (int)lists.size();
-        if (g.use_tc)
-            for (int t = w.t0; t < w.t1; ++t) lists.push_back(t - w.t0);
-        w.n_tc = (int)lists.size() - w.tc_off;
-        w.mol_off = (int)lists.size();
-        for (int t = w.t0; t < w.t1; ++t)
-            if (g.htask[t].has_mol) lists.push_back(t - w.t0);
-        w.n_mol = (int)lists.size() - w.mol_off;
+        w.n_simt = g.use_tc ? 0 : w.t1 - w.t0;
+        w.n_tc = g.use_tc ? w.t1 - w.t0 : 0;
+        w.n_mol = 0;
+        for (int t = w.t0; t < w.t1; ++t) w.n_mol += g.htask[t].has_mol ? 1 : 0;
     }
-    if ((rc = up(g.lists, lists))) return rc;
     return OCRT_OK;
 }
 
@@ -440,6 +437,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
     B.gmu = g.gmu; B.gw = g.gw; B.h = g.h; B.ch = g.ch; B.xd = g.xd; B.yd = g.yd; B.z = g.z;
     B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.Eatt = g.Eatt; B.active_cnt = g.active_cnt; B.err = g.err;
+    B.mol_cnt = g.mol_cnt; B.work = g.work;
+    B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     WaveBufs W;
     W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.pvec = g.pvec;
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
@@ -451,6 +450,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         CK(cudaMemsetAsync(g.pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (g.any_flat) CK(cudaMemsetAsync(g.fvec, 0, sizeof(float) * (size_t)nw * 24 * G.NR, st));
         CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+        CK(cudaMemsetAsync(g.mol_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+        CK(cudaMemsetAsync(g.work, 0, sizeof(int) * 4 * ((size_t)g.max_orders + 2), st));
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
         LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
@@ -461,18 +462,23 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
-        const int mtiles = (w.Kmax + 127) / 128;
+        const int mtiles = (w.Kmax + 127) / 128, ltiles = (w.Kmax + 31) / 32;
         const size_t tc_smem = tc_smem_bytes(G);
+        // Persistent grids: CTAs pull (task, level tile) items from the order's
+        // active list, so tasks that have converged cost nothing.
+        const int tc_grid = std::min(w.n_tc * mtiles, g_nsm);
+        const int mol_grid = std::min(w.n_mol * ltiles, 4 * g_nsm);
+        const int scan_grid = std::min(nw, 8 * g_nsm);
         for (int it = 2; it <= g.max_orders; ++it) {
             if (w.n_simt)
-                LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it, g.lists + w.simt_off));
+                LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
             if (w.n_tc)
-                LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<w.n_tc * mtiles, 128, tc_smem, st>>>(
-                           g.mapF, g.mapA, B, W, G, w.t0, g.lists + w.tc_off, w.n_tc, mtiles));
+                LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(
+                           g.mapF, g.mapA, B, W, G, w.t0, it, mtiles));
             if (w.n_mol)
-                LAUNCH(plan, KC_MOL, k_mol_lowrank<<<dim3(w.n_mol, (w.Kmax + 31) / 32), 256, mol_smem_bytes(G), st>>>(
-                           B, W, G, w.t0, g.lists + w.mol_off, g.Bp, g.Br, g.Bt, g.Lmax));
-            LAUNCH(plan, KC_SCAN, k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0, it));
+                LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
+                           B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
+            LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, 0, st>>>(B, W, G, w.t0, it));
             if ((it - 1) % poll == 0 || it == g.max_orders) {
                 CK(cudaMemcpyAsync(g_pinned, g.active_cnt + it, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
@@ -522,6 +528,7 @@ int ocrt_gb_init(int device)
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
     CK(cudaMallocHost(&g_pinned, sizeof(int) * 16));
+    CK(cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, device));
     CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));

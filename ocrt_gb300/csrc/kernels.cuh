@@ -45,20 +45,24 @@ struct BatchBufs {
     const float *Tc, *Ca, *Cb;
     const float *frs;
     const double *Eatt;    // rough direct-beam attenuation [lev_off*NR + k*NR + g]
-    int *active_cnt;       // [max_orders + 2]
+    int *active_cnt;       // [max_orders + 2]: tasks still active after order it
+    int *mol_cnt;          // [max_orders + 2]: molecular (m <= 2) tasks still active after order it
+    int *alist[2];         // ping-pong active-task lists (wave-local ids); order it reads alist[it & 1]
+    int *mlist[2];         // same for the molecular tasks
+    int *work;             // [max_orders + 2][4] work counters of the persistent kernels
     int *err;              // device error word
 };
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
-__global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it, const int *list);
+__global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
 __global__ void k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
-                            BatchBufs B, WaveBufs W, Geom G, int t0, const int *tc_list, int n_list, int mtiles);
+                            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
 size_t tc_smem_bytes(const Geom &G);
 bool tc_supported(const Geom &G);
 __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
-__global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, const int *list,
+__global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int ltiles,
                               const float *Bp, const float *Br, const float *Bt, int L);
 inline size_t mol_smem_bytes(const Geom &G) { return sizeof(float) * (4 * G.N + G.COUT * 24 + 32 * G.CIN + 32 * 25); }
 __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks);

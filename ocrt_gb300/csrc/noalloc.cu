@@ -145,6 +145,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     double *mb = cv.take<double>(La1), *mg = cv.take<double>(La1), *ma = cv.take<double>(La1), *mz = cv.take<double>(La1);
     double *kappa = cv.take<double>(1), *taudir = cv.take<double>(1);
     int *active = cv.take<int>((size_t)opts->max_orders + 2);
+    int *molcnt = cv.take<int>((size_t)opts->max_orders + 2);
+    int *work = cv.take<int>(4 * ((size_t)opts->max_orders + 2));
     int *err = cv.take<int>(1);
     float *srf = cv.take<float>(rough ? (size_t)T * srf_elems : 1);
     if (!cv.ok) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
@@ -160,7 +162,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     float *pvec = cv.take<float>((size_t)Wt * 2 * G.LDC);
     float *fvec = cv.take<float>((size_t)Wt * 24 * NR);
     float *Bx = cv.take<float>((size_t)Wt * 6 * (L + 1));
-    int *ident = cv.take<int>((size_t)Wt);
+    int *alist0 = cv.take<int>((size_t)Wt), *alist1 = cv.take<int>((size_t)Wt);
+    int *mlist0 = cv.take<int>((size_t)Wt), *mlist1 = cv.take<int>((size_t)Wt);
     if (!cv.ok) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
 
     TaskDev ht[NA_MAX_M + 1];
@@ -174,12 +177,9 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         ht[m].srf_off = rough ? (long long)m * (long long)srf_elems : -1;
     }
     const int zero = 0;
-    int hident[NA_MAX_M + 1];
-    for (int q = 0; q < Wt; ++q) hident[q] = q;
     NA_CK(cudaMemcpyAsync(px, &d, sizeof(PixDev), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(tasks, ht, sizeof(TaskDev) * T, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(ptask0, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-    NA_CK(cudaMemcpyAsync(ident, hident, sizeof(int) * Wt, cudaMemcpyHostToDevice, st));
     if (aer) {
         NA_CK(cudaMemcpyAsync(mb, aer->beta, sizeof(double) * La1, cudaMemcpyHostToDevice, st));
         NA_CK(cudaMemcpyAsync(mg, aer->gamma, sizeof(double) * La1, cudaMemcpyHostToDevice, st));
@@ -208,29 +208,30 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     BatchBufs B;
     B.px = px; B.tasks = tasks; B.state = state; B.tout = tout; B.gmu = gmu; B.gw = gw;
     B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs; B.Eatt = Eatt;
-    B.active_cnt = active; B.err = err;
+    B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work;
+    B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
     W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     for (int t0 = 0; t0 < T; t0 += Wt) {
         const int nw = (T - t0) < Wt ? (T - t0) : Wt;
-        // tasks are ordered by mode, so the molecular (m <= 2) tasks of this
-        // wave are its first nmol entries of the identity list
-        const int nmol = t0 <= 2 ? ((3 - t0) < nw ? (3 - t0) : nw) : 0;
+        const int nmol = t0 <= 2 ? ((3 - t0) < nw ? (3 - t0) : nw) : 0;   // tasks are ordered by mode
         NA_CK(cudaMemsetAsync(ops, 0, sizeof(float) * 2 * (size_t)nw * op_elems, st));
         NA_CK(cudaMemsetAsync(pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (flat) NA_CK(cudaMemsetAsync(fvec, 0, sizeof(float) * (size_t)nw * 24 * NR, st));
         NA_CK(cudaMemsetAsync(active, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
+        NA_CK(cudaMemsetAsync(molcnt, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
+        NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
         NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, Bx));
         NA_LAUNCH(k_tables<<<nw, 256, 0, st>>>(tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz,
                                                ops, pvec, W.fvec));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= opts->max_orders; ++it) {
-            NA_LAUNCH(k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, t0, it, ident));
+            NA_LAUNCH(k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, t0, it));
             if (nmol > 0)
-                NA_LAUNCH(k_mol_lowrank<<<dim3(nmol, (K + 31) / 32), 256, mol_smem_bytes(G), st>>>(
-                    B, W, G, t0, ident, Bp, Br, Bt, L));
+                NA_LAUNCH(k_mol_lowrank<<<dim3(nmol * ((K + 31) / 32)), 256, mol_smem_bytes(G), st>>>(
+                    B, W, G, t0, it, (K + 31) / 32, Bp, Br, Bt, L));
             NA_LAUNCH(k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, t0, it));
             if ((it - 1) % 4 == 0 || it == opts->max_orders) {
                 int left_active = 0;

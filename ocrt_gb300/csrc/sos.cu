@@ -64,6 +64,10 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
         st.pad_ = 0;
         st.resid = 0.0;
         B.state[tg] = st;
+        if (st.active) {
+            B.alist[0][atomicAdd(&B.active_cnt[1], 1)] = tl;
+            if (tk.has_mol) B.mlist[0][atomicAdd(&B.mol_cnt[1], 1)] = tl;
+        }
     }
     if (c >= G.COUT) return;
     int s, h, g;
@@ -141,11 +145,10 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
 #define ST_K 16
 #define ST_M 64
 #define ST_N 64
-__global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it,
-                                                     const int *list)
+__global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
 {
-    const int tl = list[blockIdx.x], tg = t0 + tl;
-    if (!B.state[tg].active) return;
+    if ((int)blockIdx.x >= B.active_cnt[it - 1]) return;
+    const int tl = B.alist[it & 1][blockIdx.x], tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
     const int nt = d.nt;
@@ -202,16 +205,23 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
 // Molecular source for m <= 2 tasks: xi[k][4b+f] = sum_i w_i f(mu_i) F[k][bN+i]
 // (f in {1, P2m, R2m, T2m}), then J[k][c] += y_k sum_r U[c][r] xi[k][r].
 // Grid (task in list, tile of 32 levels), 256 threads.
-__global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, const int *list,
+__global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int ltiles,
                                                      const float *Bp, const float *Br, const float *Bt, int L)
 {
     extern __shared__ float sm[];
-    const int tl = list[blockIdx.x], tg = t0 + tl;
-    if (!B.state[tg].active) return;
+    __shared__ int item_s;
+    const int n_items = B.mol_cnt[it - 1] * ltiles;
+    for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) item_s = atomicAdd(&B.work[it * 4 + 1], 1);
+    __syncthreads();
+    const int item = item_s;
+    if (item >= n_items) return;
+    const int tl = B.mlist[it & 1][item / ltiles], tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
-    const int nt = d.nt, N = G.N, k0 = blockIdx.y * 32;
-    if (k0 > nt) return;
+    const int nt = d.nt, N = G.N, k0 = (item % ltiles) * 32;
+    if (k0 > nt) continue;
     const int nk = min(32, nt - k0 + 1);
     float *fv = sm;                          // [4][N]
     float *U = fv + 4 * N;                   // [COUT][24]
@@ -249,6 +259,7 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
         for (int r = 0; r < 24; ++r) acc = fmaf(u[r], x[r], acc);
         J[(size_t)(k0 + k) * G.LDC + c] += (float)yd[k0 + k] * acc;
     }
+    }
 }
 
 __device__ inline double block_max(double v, double *red)
@@ -266,12 +277,18 @@ __device__ inline double block_max(double v, double *red)
     return v;
 }
 
-__global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
+__global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
 {
     __shared__ double red[32];
-    const int tl = blockIdx.x, tg = t0 + tl;
+    __shared__ int item_s;
+    const int n_items = B.active_cnt[it - 1];
+    for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) item_s = atomicAdd(&B.work[it * 4 + 2], 1);
+    __syncthreads();
+    if (item_s >= n_items) return;
+    const int tl = B.alist[it & 1][item_s], tg = t0 + tl;
     const TaskState st = B.state[tg];
-    if (!st.active) return;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
     const int c = threadIdx.x, nt = d.nt, N = G.N, NR = G.NR;
@@ -317,7 +334,7 @@ __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
         // Levels are processed in chunks of PF: every load of a chunk is issued
         // before the dependent recurrence runs, so the scan is not bound by one
         // memory round trip per level.
-        constexpr int PF = 8;
+        constexpr int PF = 6;
         if (h == 0) {
             float I = bc;
             put(nt, I);
@@ -397,7 +414,11 @@ __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
         if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
         else if (it >= d.max_orders) ns.active = 0;
         B.state[tg] = ns;
-        if (ns.active) atomicAdd(&B.active_cnt[it], 1);
+        if (ns.active) {
+            B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
+            if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
+        }
+    }
     }
 }
 

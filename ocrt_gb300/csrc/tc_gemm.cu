@@ -1,7 +1,7 @@
 // tc_gemm.cu — multiple-scattering source contraction on the tcgen05 tensor
 // cores (rt_sos_operator.c:206-424 for modes without a molecular term, m > 2).
 //
-// Per CTA: one (task, 128-level tile).  D[128 levels][NP outputs] (FP32 in
+// Per item: one (task, 128-level tile).  D[128 levels][NP outputs] (FP32 in
 // TMEM) = F[128 levels][6N inputs] x Aop^T, K = 6N swept in 32-element tiles
 // (one 128-byte swizzle row).  Each K tile is brought in by TMA into a
 // SWIZZLE_128B K-major layout, split in place into tf32 hi and lo parts, and
@@ -18,7 +18,7 @@
 
 #define TC_M 128
 #define TC_KT 32
-#define TC_THREADS 128
+#define TC_THREADS 256
 #define TC_TMEM_COLS 256
 #define TC_WAIT_NS 2000000000ull
 
@@ -145,21 +145,16 @@ __device__ __forceinline__ void split_tf32(uint32_t *hi, uint32_t *lo, int n)
     }
 }
 
+// Persistent form: a grid of about one CTA per SM pulls (active task, 128-level
+// tile) items from a per-order counter.  TMEM and the barriers are set up once
+// per CTA; K tiles are numbered globally across the CTA's items (stage g & 1,
+// use g >> 1), so thread 0 streams the next item's first two tiles in while the
+// current item's epilogue drains TMEM.
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
-            BatchBufs B, WaveBufs W, Geom G, int t0, const int *tc_list, int n_list, int mtiles)
+            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles)
 {
     extern __shared__ unsigned char smem_raw[];
-    const int item = blockIdx.x;
-    const int li = item / mtiles, mt = item - li * mtiles;
-    if (li >= n_list) return;
-    const int tl = tc_list[li], tg = t0 + tl;
-    if (!B.state[tg].active) return;
-    const TaskDev tk = B.tasks[tg];
-    const PixDev &d = B.px[tk.pix];
-    const int nt = d.nt, k0 = mt * TC_M;
-    if (k0 > nt) return;
-
     const int NP = G.NP;
     const uint32_t A_BYTES = TC_M * TC_KT * 4, B_BYTES = (uint32_t)NP * TC_KT * 4;
     const uint32_t STAGE = 2 * A_BYTES + 2 * B_BYTES;
@@ -167,7 +162,11 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
     uint64_t *bars = (uint64_t *)(base + 2 * STAGE);     // full[2], empty[2], done
     uint32_t *tslot = (uint32_t *)(bars + 5);
     int *abort_flag = (int *)(tslot + 1);
+    int *slot = abort_flag + 1;                          // item ring [2]: task-list index * mtiles + tile, or -1
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int n_items = B.active_cnt[it - 1] * mtiles;
+    const int *alist = B.alist[it & 1];
+    int *counter = &B.work[it * 4 + 0];
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -175,111 +174,147 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
+    const int NKT = G.CIN / TC_KT;
+
+    // Thread 0 only: next valid item (k0 <= nt) from the shared counter, or -1.
+    auto fetch = [&]() -> int {
+        for (;;) {
+            const int item = atomicAdd(counter, 1);
+            if (item >= n_items) return -1;
+            const int li = item / mtiles, mt = item - li * mtiles;
+            const TaskDev tk = B.tasks[t0 + alist[li]];
+            if (mt * TC_M <= B.px[tk.pix].nt) return item;
+        }
+    };
+    // Thread 0 only: TMA loads of K tile kt of `item` into stage s.
+    auto issue = [&](int item, int kt, int s) {
+        const int li = item / mtiles, mt = item - li * mtiles;
+        const TaskDev tk = B.tasks[t0 + alist[li]];
+        const int rowF = (int)(tk.fld_off / G.LDC) + mt * TC_M;
+        const int rowA = (int)(tk.op_off / G.CIN);
+        unsigned char *sp = base + (size_t)s * STAGE;
+        mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+        tma_load_2d(sp, &mapF, &full[s], kt * TC_KT, rowF);
+        tma_load_2d(sp + 2 * A_BYTES, &mapA, &full[s], kt * TC_KT, rowA);
+    };
+
+    int inflight[2] = {0, 0};          // thread 0: stage holds an unconsumed load
     if (tid == 0) {
         for (int i = 0; i < 5; ++i) mbar_init(&bars[i], 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int first = fetch();
+        slot[0] = first;
+        slot[1] = -1;
+        if (first >= 0) {
+            issue(first, 0, 0); inflight[0] = 1;
+            issue(first, 1, 1); inflight[1] = 1;
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
 
-    const int NKT = G.CIN / TC_KT;
-    const int rowF = (int)(tk.fld_off / G.LDC) + k0;
-    const int rowA = (int)(tk.op_off / G.CIN);
-    uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
-    auto stage_ptr = [&](int s) { return base + (size_t)s * STAGE; };
-    int inflight[2] = {0, 0};
-    if (tid == 0) {
-        for (int s = 0; s < 2 && s < NKT; ++s) {
-            unsigned char *sp = stage_ptr(s);
-            mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-            tma_load_2d(sp, &mapF, &full[s], s * TC_KT, rowF);
-            tma_load_2d(sp + 2 * A_BYTES, &mapA, &full[s], s * TC_KT, rowA);
-            inflight[s] = 1;
-        }
-    }
-    uint32_t ph_full[2] = {0, 0}, ph_empty[2] = {0, 0};
     constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
     const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(NP >> 3) << 17);
-    bool ok = true, done_committed = false;
-    for (int kt = 0; kt < NKT; ++kt) {
-        const int s = kt & 1;
-        if (mbar_wait(&full[s], ph_full[s])) ph_full[s] ^= 1;
-        else atomicExch(abort_flag, 1);
+    uint32_t g = 0;                    // global K-tile sequence number of this CTA
+    uint32_t ph_done = 0;
+    bool ok = true, done_pending = false;
+    for (int j = 0;; ++j) {
+        __syncthreads();
+        const int item = slot[j & 1];
+        if (item < 0) break;
+        const int li = item / mtiles, mt = item - li * mtiles;
+        const TaskDev tk = B.tasks[t0 + alist[li]];
+        const PixDev &d = B.px[tk.pix];
+        const int nt = d.nt, k0 = mt * TC_M;
+        for (int kt = 0; kt < NKT; ++kt, ++g) {
+            const int s = g & 1;
+            const uint32_t use = g >> 1;
+            if (!mbar_wait(&full[s], use & 1)) atomicExch(abort_flag, 1);
+            __syncthreads();
+            if (*abort_flag) { ok = false; break; }
+            if (tid == 0) inflight[s] = 0;
+            unsigned char *sp = base + (size_t)s * STAGE;
+            uint32_t *ahi = (uint32_t *)sp, *alo = (uint32_t *)(sp + A_BYTES);
+            uint32_t *bhi = (uint32_t *)(sp + 2 * A_BYTES), *blo = (uint32_t *)(sp + 2 * A_BYTES + B_BYTES);
+            split_tf32(ahi, alo, TC_M * TC_KT);
+            split_tf32(bhi, blo, NP * TC_KT);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t sa_hi = smem_u32(ahi), sa_lo = smem_u32(alo);
+                const uint32_t sb_hi = smem_u32(bhi), sb_lo = smem_u32(blo);
+#pragma unroll
+                for (int kk = 0; kk < TC_KT / 8; ++kk) {
+                    const uint32_t off = kk * 32;     // 8 tf32 = 32 bytes along the swizzled row
+                    const uint64_t ah = sdesc_sw128(sa_hi + off), al = sdesc_sw128(sa_lo + off);
+                    const uint64_t bh = sdesc_sw128(sb_hi + off), bl = sdesc_sw128(sb_lo + off);
+                    umma_tf32(tmem, ah, bh, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+                    umma_tf32(tmem, ah, bl, idesc, 1u);
+                    umma_tf32(tmem, al, bh, idesc, 1u);
+                }
+                umma_commit(&empty[s]);
+                if (kt == NKT - 1) { umma_commit(done); done_pending = true; }
+                // Refill this stage with K tile g + 2 (this item's, or the next item's).
+                int nitem = item, nkt = kt + 2;
+                if (nkt >= NKT) {
+                    nkt -= NKT;
+                    if (nkt == 0) slot[(j + 1) & 1] = fetch();
+                    nitem = slot[(j + 1) & 1];
+                }
+                if (nitem >= 0) {
+                    if (!mbar_wait(&empty[s], use & 1)) {
+                        atomicExch(abort_flag, 1);
+                    } else {
+                        issue(nitem, nkt, s);
+                        inflight[s] = 1;
+                    }
+                }
+            }
+        }
+        if (!ok) break;
+        if (mbar_wait(done, ph_done)) {
+            ph_done ^= 1;
+            done_pending = false;
+        } else {
+            atomicExch(abort_flag, 1);
+        }
         __syncthreads();
         if (*abort_flag) { ok = false; break; }
-        if (tid == 0) inflight[s] = 0;
-        unsigned char *sp = stage_ptr(s);
-        uint32_t *ahi = (uint32_t *)sp, *alo = (uint32_t *)(sp + A_BYTES);
-        uint32_t *bhi = (uint32_t *)(sp + 2 * A_BYTES), *blo = (uint32_t *)(sp + 2 * A_BYTES + B_BYTES);
-        split_tf32(ahi, alo, TC_M * TC_KT);
-        split_tf32(bhi, blo, NP * TC_KT);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa_hi = smem_u32(ahi), sa_lo = smem_u32(alo);
-            const uint32_t sb_hi = smem_u32(bhi), sb_lo = smem_u32(blo);
-#pragma unroll
-            for (int kk = 0; kk < TC_KT / 8; ++kk) {
-                const uint32_t off = kk * 32;     // 8 tf32 = 32 bytes along the swizzled row
-                const uint64_t ah = sdesc_sw128(sa_hi + off), al = sdesc_sw128(sa_lo + off);
-                const uint64_t bh = sdesc_sw128(sb_hi + off), bl = sdesc_sw128(sb_lo + off);
-                umma_tf32(tmem, ah, bh, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
-                umma_tf32(tmem, ah, bl, idesc, 1u);
-                umma_tf32(tmem, al, bh, idesc, 1u);
-            }
-            umma_commit(&empty[s]);
-            if (kt + 2 < NKT) {
-                if (!mbar_wait(&empty[s], ph_empty[s])) {
-                    atomicExch(abort_flag, 1);
-                } else {
-                    mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-                    tma_load_2d(sp, &mapF, &full[s], (kt + 2) * TC_KT, rowF);
-                    tma_load_2d(sp + 2 * A_BYTES, &mapA, &full[s], (kt + 2) * TC_KT, rowA);
-                    inflight[s] = 1;
-                }
-                ph_empty[s] ^= 1;
-            }
-        }
-    }
-    if (ok) {
-        if (tid == 0) umma_commit(done);
-        done_committed = true;
-        if (!mbar_wait(done, 0)) atomicExch(abort_flag, 1);
-        __syncthreads();
-        ok = *abort_flag == 0;
-    }
-    if (ok) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int lane = tid & 31;
-        const int k = k0 + warp * 32 + lane;
+        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (one level each);
+        // warps 0-3 take the even 16-column chunks, warps 4-7 the odd ones.
+        const int lane = tid & 31, q = warp & 3, half = warp >> 2;
+        const int k = k0 + q * 32 + lane;
         const float x = k <= nt ? (float)B.xd[d.lev_off + k] : 0.f;
         float *Jrow = W.J + tk.fld_off + (size_t)k * G.LDC;
-        for (int cb = 0; cb < NP / 16; ++cb) {
+        for (int cb = half; cb < NP / 16; cb += 2) {
             float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(cb * 16), v);
+            tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 16), v);
             if (k <= nt) {
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int c = cb * 16 + j;
-                    if (c < G.COUT) Jrow[c] = x * v[j];
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int c = cb * 16 + jj;
+                    if (c < G.COUT) Jrow[c] = x * v[jj];
                 }
             }
         }
-    } else {
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    if (!ok) {
         if (tid == 0) {
             atomicExch(B.err, OCRT_ERR_DEVICE);
             // drain this CTA's own copies and MMAs still in flight (bounded)
             for (int s = 0; s < 2; ++s)
-                if (inflight[s]) mbar_wait(&full[s], ph_full[s]);
-            if (!done_committed) umma_commit(done);
-            mbar_wait(done, 0);
+                if (inflight[s]) mbar_wait(&full[s], ((g + (s != (int)(g & 1))) >> 1) & 1);
+            if (!done_pending) umma_commit(done);
+            mbar_wait(done, ph_done);
         }
-        __syncthreads();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -291,10 +326,11 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
 
 size_t tc_smem_bytes(const Geom &G)
 {
-    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)G.NP * TC_KT * 4) + 64;
+    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)G.NP * TC_KT * 4) + 128;
 }
 
 bool tc_supported(const Geom &G)
 {
-    return (G.CIN % TC_KT) == 0 && G.NP <= 256 && tc_smem_bytes(G) <= 227 * 1024;
+    return (G.CIN % TC_KT) == 0 && G.CIN / TC_KT >= 2 && G.NP <= 256 && G.NP % 16 == 0 &&
+           tc_smem_bytes(G) <= 227 * 1024;
 }
