@@ -194,6 +194,50 @@ int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *opts,
                                const ocrt_aerosol *aer, ocrt_result *out,
                                void *stream);
 
+/* ---- per-layer parameters and the adjoint ------------------------------
+ * No counterpart in the reference (its solve API takes no per-layer inputs
+ * and has no derivatives).  Layer l (0-based, l < n_layers) spans levels l
+ * and l+1 of the level grid (level 0 = TOA).
+ *   dtau[l] replaces the uniform optical-depth grid: h_k = sum_{l<k} dtau[l].
+ *   ssa[l]  is the single-scattering albedo of layer l: level l+1's aerosol
+ *           and molecular scattering fractions (rt_atm.c:313-383) are scaled
+ *           together so that they sum to ssa[l].
+ * The aerosol/molecular split of every layer, and the level altitudes, stay
+ * those of the profile's uniform grid.  NULL arrays keep the profile values.
+ * IPSS (opts.pssa) cannot be combined with overrides or gradients. */
+typedef struct {
+    int n_layers;            /* must equal opts.n_layers of the case */
+    const double *dtau;      /* [n_layers], each > 0, or NULL */
+    const double *ssa;       /* [n_layers], each in [0, 1], or NULL */
+} ocrt_layers;
+
+/* Gradient of  c_I rho_I + c_Q rho_Q + c_U rho_U  (one cotangent row) with
+ * respect to the layer optical depths, the layer single-scattering albedos
+ * and the wind speed.  The caller allocates d_dtau and d_ssa (n_layers). */
+typedef struct {
+    double *d_dtau;
+    double *d_ssa;
+    double  d_wind;
+} ocrt_grad;
+
+/* Batched forward solve with optional per-layer parameters and, for each
+ * pixel, n_cot cotangent rows cot[(i * n_cot + r) * 3 + {0,1,2}] for
+ * (rho_I, rho_Q, rho_U); grad[i * n_cot + r] receives row r's gradient.
+ * n_cot = 3 with the identity rows gives the full Jacobian.  n_cot = 0 is a
+ * plain forward solve with the overrides (cot and grad may be NULL).
+ * layers: NULL or n entries (one per case).  The gradient is the adjoint of
+ * the converged SOS system: the forward keeps two checkpoints per Fourier
+ * mode (the order total and the last order's field), and an adjoint
+ * successive-orders sweep with the transposed source, transport and surface
+ * operators gives every parameter derivative in one pass per cotangent row.
+ * Supported surfaces: BLACK and BLACK_FRESNEL_OCEAN with wind > 0; pssa = 0.
+ * Otherwise OCRT_ERR_UNSUPPORTED. */
+int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases,
+                                const ocrt_opts *opts, int opts_per_case,
+                                const ocrt_aerosol *aer, int aer_per_case,
+                                const ocrt_layers *layers, int n_cot, const double *cot,
+                                ocrt_result *out, ocrt_grad *grad, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,643 @@
+// adjoint.cu — gradients of the TOA reflectance with respect to the layer
+// optical depths, the layer single-scattering albedos and the wind speed.
+//
+// The reference has no derivatives; this is the adjoint of the discrete
+// system the forward solves.  For one Fourier mode the SOS computes the
+// Neumann series F = sum_n L^(n-1) F_1 of the linear order operator
+//     L F = Scan(S F, Rsurf F_dn(BOA)),
+// S the per-level source contraction (rt_sos_operator.c:206-424), Scan the
+// up/down linear-in-tau recurrences (rt_layer_transport.c:107-208) and Rsurf
+// the rough-surface boundary operator (rt_surface_boundary.c:137-208).  For an
+// output y = e^T F the adjoint field is a = sum_j (L^T)^j e, summed by its own
+// successive orders with the same convergence test, and for any parameter p
+//     dy/dp = a^T (dL/dp) F_tot + a^T dF_1/dp.
+// Because L is linear and the same at every order, the forward only needs two
+// checkpoints per mode: the order total F_tot and the last order's field
+// (their difference is the field that was scattered), not every order.
+//
+//   k_adj_prep      Xs = F_tot - F_last into the field buffer (the scattered field)
+//   k_fill_all      every task active, for one extra source pass J_tot = S Xs
+//   k_adj_init      a_1 = e: the output weights at the TOA view column(s)
+//   k_adj_scan      transposed transport of a_j (recurrences run the other way),
+//                   accumulation of the adjoint total and the residual test
+//   k_adj_source    a_{j+1} = x_k A^T muJ: the transposed aerosol contraction
+//   k_adj_mol       + y_k V^T (U^T muJ): the transposed rank-24 molecular term
+//   k_adj_surface   + Rsurf^T mu_bc at the BOA downward columns
+//   k_adj_grad      final transposed pass over the adjoint total: per-level and
+//                   per-layer sums of the parameter derivatives
+//   k_adj_pixel     sum over modes, chain rule to (dtau_l, ssa_l, wind), and
+//                   the direct terms (removed surface seed, sunglint)
+#include "kernels.cuh"
+#include "physics.cuh"
+
+namespace {
+
+__device__ inline void decode_col_a(const Geom &G, int c, int &s, int &h, int &g)
+{
+    const int N = G.N;
+    if (c < 6 * N) {
+        s = c / (2 * N);
+        const int r = c - s * 2 * N;
+        h = r / N;
+        g = r - h * N;
+    } else if (c < 6 * N + 6) {
+        const int v = c - 6 * N;
+        s = v >> 1; h = v & 1; g = N;
+    } else {
+        s = 0; h = 0; g = G.NR;
+    }
+}
+
+__device__ inline size_t adj_off(const TaskDev &tk, const Geom &G, int ncot, int r)
+{
+    return (size_t)tk.fld_off * ncot + (size_t)r * tk.K * G.LDC;
+}
+
+__device__ inline double block_max_a(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = l < nw ? red[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+__device__ inline double block_sum_a(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = l < nw ? red[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+__device__ inline float warp_sum(float v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Linear interpolation weights between the bracketing Gauss nodes
+// (rt_solver.c:386-403), as in the forward extraction.
+__device__ inline void bracket_a(const double *gmu, int n, double mu, int &lo, int &hi, double &t)
+{
+    int jh = 1;
+    while (jh < n && gmu[jh - 1] < mu) jh++;
+    int jl = jh - 1;
+    if (jl < 1) { jl = 1; jh = 2; }
+    if (jh > n) { jh = n; jl = n - 1; }
+    lo = jl - 1; hi = jh - 1;
+    t = (mu - gmu[lo]) / (gmu[hi] - gmu[lo]);
+}
+
+// Output weights of mode m for cotangent row (cI, cQ, cU):
+// rho = (1/mu0) [X_0 + 2 sum_m X_m cos m(phi+pi)] for I, Q and
+// (1/mu0) 2 sum_m U_m sin m(phi+pi) for U (rt_fourier.c:9-33).
+__device__ inline void mode_weights(const PixDev &d, int m, const double *cot, double *w)
+{
+    const double phi = d.raa_deg * OCRT_PI / 180.0 + OCRT_PI;
+    const double cm = m == 0 ? 1.0 : 2.0 * cos((double)m * phi);
+    const double sm = m == 0 ? 0.0 : 2.0 * sin((double)m * phi);
+    w[0] = cot[0] * cm / d.mu0;
+    w[1] = cot[1] * cm / d.mu0;
+    w[2] = cot[2] * sm / d.mu0;
+}
+
+} // namespace
+
+// Xs = F_tot - F_last for every valid column and level.
+__global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0)
+{
+    const int tl = blockIdx.x, tg = t0 + tl;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int c = threadIdx.x;
+    if (c >= G.COUT) return;
+    int s, h, g;
+    decode_col_a(G, c, s, h, g);
+    if (g >= d.n_ring) return;
+    float *F = W.F + tk.fld_off;
+    const double *Tot = W.Tot + tk.fld_off;
+    for (int k = 0; k <= d.nt; ++k) {
+        const size_t o = (size_t)k * G.LDC + c;
+        F[o] = (float)(Tot[o] - (double)F[o]);
+    }
+}
+
+// Mark every task of the wave active for order index `it` (one source pass).
+__global__ void k_fill_all(BatchBufs B, int t0, int nw, int it)
+{
+    __shared__ int nmol;
+    if (threadIdx.x == 0) nmol = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) {
+        B.alist[it & 1][i] = i;
+        if (B.tasks[t0 + i].has_mol) B.mlist[it & 1][atomicAdd(&nmol, 1)] = i;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        B.active_cnt[it - 1] = nw;
+        B.mol_cnt[it - 1] = nmol;
+        for (int q = 0; q < 4; ++q) B.work[it * 4 + q] = 0;
+    }
+}
+
+// a_1 = e.  One thread per adjoint task.
+__global__ void k_adj_init(BatchBufs B, AdjBufs A, Geom G, int t0, int nadj)
+{
+    const int ta = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ta >= nadj) return;
+    const int tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    TaskState st;
+    st.active = 1; st.orders = 0; st.converged = 0; st.pad_ = 0; st.resid = 0.0;
+    A.st[ta] = st;
+    double w[3];
+    mode_weights(d, tk.m, A.cot + ((size_t)tk.pix * A.ncot + r) * 3, w);
+    float *a = A.AF + adj_off(tk, G, A.ncot, r);
+    if (d.view_slot >= 0) {
+        for (int s = 0; s < 3; ++s) a[col_of(G, s, 0, d.view_slot)] = (float)w[s];
+    } else {
+        int lo, hi; double t;
+        bracket_a(B.gmu, G.N, d.mu_view, lo, hi, t);
+        for (int s = 0; s < 3; ++s) {
+            a[col_of(G, s, 0, lo)] += (float)((1.0 - t) * w[s]);
+            a[col_of(G, s, 0, hi)] += (float)(t * w[s]);
+        }
+    }
+}
+
+// Transposed transport of a_j.  Up column (forward I[nt] = bc,
+// I[k] = T_k I[k+1] + Ca_k J[k] + Cb_k J[k+1]):
+//   nu[0] = a[0], nu[k] = a[k] + T_{k-1} nu[k-1];
+//   muJ[k] = Ca_k nu[k] (k < nt) + Cb_{k-1} nu[k-1] (k > 0);  mu_bc = nu[nt].
+// Down column (forward I[0] = 0, I[k] = T_{k-1} I[k-1] + Ca_{k-1} J[k] + Cb_{k-1} J[k-1]):
+//   nu[nt] = a[nt], nu[k] = a[k] + T_k nu[k+1];
+//   muJ[k] = Ca_{k-1} nu[k] (k > 0) + Cb_k nu[k+1] (k < nt).
+__global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j)
+{
+    __shared__ double red[32];
+    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    const TaskState st = A.st[ta];
+    if (!st.active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int c = threadIdx.x, nt = d.nt, NR = G.NR;
+    int s = 0, h = 0, g = 0;
+    if (c < G.COUT) decode_col_a(G, c, s, h, g);
+    const bool valid = c < G.COUT && g < d.n_ring;
+    const size_t off = adj_off(tk, G, A.ncot, r);
+    const float *a = A.AF + off;
+    double *At = A.ATot + off;
+    float *mj = A.AJ + off;
+    double mi = 0.0, mt = 0.0;
+    if (valid) {
+        const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+        if (h == 0) {
+            float nup = 0.f;
+            for (int k = 0; k <= nt; ++k) {
+                const size_t o = (size_t)k * G.LDC + c;
+                const float av = a[o];
+                const double t = At[o] + (double)av;
+                At[o] = t;
+                mi = fmax(mi, fabs((double)av));
+                mt = fmax(mt, fabs(t));
+                const float nu = k > 0 ? av + Tc[(k - 1) * NR + g] * nup : av;
+                float mu = k < nt ? Ca[k * NR + g] * nu : 0.f;
+                if (k > 0) mu += Cb[(k - 1) * NR + g] * nup;
+                mj[o] = mu;
+                nup = nu;
+            }
+            if (d.surf_on) A.bc[(size_t)ta * NR * 3 + g * 3 + s] = nup;
+        } else {
+            float nun = 0.f;
+            for (int k = nt; k >= 0; --k) {
+                const size_t o = (size_t)k * G.LDC + c;
+                float av = 0.f;
+                if (k > 0) {          // the TOA downward radiance is fixed at zero
+                    av = a[o];
+                    const double t = At[o] + (double)av;
+                    At[o] = t;
+                    mi = fmax(mi, fabs((double)av));
+                    mt = fmax(mt, fabs(t));
+                }
+                const float nu = k < nt ? av + Tc[k * NR + g] * nun : av;
+                float mu = k > 0 ? Ca[(k - 1) * NR + g] * nu : 0.f;
+                if (k < nt) mu += Cb[k * NR + g] * nun;
+                mj[o] = mu;
+                nun = nu;
+            }
+        }
+    }
+    mi = block_max_a(mi, red);
+    __syncthreads();
+    mt = block_max_a(mt, red);
+    if (threadIdx.x == 0) {
+        TaskState ns = st;
+        ns.orders = j;
+        ns.resid = mt > 0.0 ? mi / mt : 0.0;
+        if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
+        else if (j >= d.max_orders) ns.active = 0;
+        A.st[ta] = ns;
+        if (ns.active) atomicAdd(&A.acnt[j], 1);
+    }
+}
+
+// a_{j+1}[k][cin] = x_k sum_row A[row][cin] muJ[k][row] (the transposed
+// aerosol contraction; rows are the COUT outputs).  Columns past the weighted
+// inputs are cleared.  Grid (adjoint task, 64-level tile, 64-column tile).
+__global__ void __launch_bounds__(256) k_adj_source(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
+{
+    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    if (!A.st[ta].active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt;
+    const int k0 = blockIdx.y * ST_M_TILE, c0 = blockIdx.z * ST_N_TILE;
+    if (k0 > nt || c0 >= G.LDC) return;
+    const size_t off = adj_off(tk, G, A.ncot, r);
+    float *out = A.AF + off;
+    if (c0 >= G.CIN) {
+        for (int e = threadIdx.x; e < ST_M_TILE * ST_N_TILE; e += 256) {
+            const int lv = e / ST_N_TILE, cc = e - lv * ST_N_TILE;
+            const int k = k0 + lv, c = c0 + cc;
+            if (k <= nt && c < G.LDC) out[(size_t)k * G.LDC + c] = 0.f;
+        }
+        return;
+    }
+    constexpr int KT = 16;
+    __shared__ float Ms[KT][ST_M_TILE + 4];
+    __shared__ float As[KT][ST_N_TILE + 4];
+    const float *mj = A.AJ + off;
+    const float *Aop = W.ops + tk.op_off;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[4][4] = {{0}};
+    for (int kc = 0; kc < G.COUT; kc += KT) {
+        for (int idx = threadIdx.x; idx < ST_M_TILE * KT; idx += 256) {
+            const int lv = idx / KT, kk = idx - lv * KT;
+            const int k = k0 + lv, row = kc + kk;
+            Ms[kk][lv] = (k <= nt && row < G.COUT) ? mj[(size_t)k * G.LDC + row] : 0.f;
+        }
+        for (int idx = threadIdx.x; idx < KT * ST_N_TILE; idx += 256) {
+            const int kk = idx / ST_N_TILE, cc = idx - kk * ST_N_TILE;
+            const int row = kc + kk, ci = c0 + cc;
+            As[kk][cc] = (row < G.COUT && ci < G.CIN) ? Aop[(size_t)row * G.CIN + ci] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < KT; ++kk) {
+            float fr[4], ar[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) fr[i] = Ms[kk][ty + 16 * i];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ar[q] = As[kk][tx + 16 * q];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[i][q] = fmaf(fr[i], ar[q], acc[i][q]);
+        }
+        __syncthreads();
+    }
+    const double *xd = B.xd + d.lev_off;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int k = k0 + ty + 16 * i;
+        if (k > nt) continue;
+        const float x = (float)xd[k];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int c = c0 + tx + 16 * q;
+            if (c < G.CIN) out[(size_t)k * G.LDC + c] = x * acc[i][q];
+            else if (c < G.LDC) out[(size_t)k * G.LDC + c] = 0.f;
+        }
+    }
+}
+
+// a_{j+1}[k][bN+i] += y_k sum_f fv[f][i] zeta[k][4b+f], zeta[k][r] = sum_c U[c][r] muJ[k][c]
+// (transpose of the rank-24 molecular operator of k_mol_lowrank).
+// Grid (adjoint task, tile of 32 levels), 256 threads.
+__global__ void __launch_bounds__(256) k_adj_mol(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0,
+                                                 const float *Bp, const float *Br, const float *Bt, int L)
+{
+    extern __shared__ float sm[];
+    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    if (!A.st[ta].active) return;
+    const TaskDev tk = B.tasks[tg];
+    if (!tk.has_mol) return;
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt, N = G.N, k0 = blockIdx.y * 32;
+    if (k0 > nt) return;
+    const int nk = min(32, nt - k0 + 1);
+    float *fv = sm;                          // [4][N]
+    float *U = fv + 4 * N;                   // [COUT][24]
+    float *Ms = U + G.COUT * 24;             // [32][COUT]
+    float *zt = Ms + 32 * G.COUT;            // [32][25]
+    const size_t gb = (size_t)tk.m * (L + 1) * N + (size_t)2 * N;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float w = (float)B.gw[i];
+        fv[i] = w; fv[N + i] = w * Bp[gb + i]; fv[2 * N + i] = w * Br[gb + i]; fv[3 * N + i] = w * Bt[gb + i];
+    }
+    const float *Ug = W.ops + tk.mol_off;
+    for (int e = threadIdx.x; e < G.COUT * 24; e += blockDim.x) U[e] = Ug[e];
+    const size_t off = adj_off(tk, G, A.ncot, r);
+    const float *mj = A.AJ + off + (size_t)k0 * G.LDC;
+    for (int e = threadIdx.x; e < nk * G.COUT; e += blockDim.x) {
+        const int k = e / G.COUT, c = e - k * G.COUT;
+        Ms[k * G.COUT + c] = mj[(size_t)k * G.LDC + c];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nk * 24; e += blockDim.x) {
+        const int k = e / 24, rr = e - k * 24;
+        const float *mr = Ms + k * G.COUT;
+        float acc = 0.f;
+        for (int c = 0; c < G.COUT; ++c) acc = fmaf(U[c * 24 + rr], mr[c], acc);
+        zt[k * 25 + rr] = acc;
+    }
+    __syncthreads();
+    float *out = A.AF + off;
+    const double *yd = B.yd + d.lev_off;
+    for (int e = threadIdx.x; e < nk * G.CIN; e += blockDim.x) {
+        const int k = e / G.CIN, ci = e - k * G.CIN, b = ci / N, i = ci - b * N;
+        const float *z = zt + k * 25 + 4 * b;
+        const float v = fv[i] * z[0] + fv[N + i] * z[1] + fv[2 * N + i] * z[2] + fv[3 * N + i] * z[3];
+        out[(size_t)(k0 + k) * G.LDC + ci] += (float)yd[k0 + k] * v;
+    }
+}
+
+size_t adj_mol_smem_bytes(const Geom &G)
+{
+    return sizeof(float) * (4 * (size_t)G.N + (size_t)G.COUT * 24 + 32 * (size_t)G.COUT + 32 * 25);
+}
+
+// a_{j+1}[nt][(s', down, i)] += pw_i sum_{g, s} R_m(g, i)[s][s'] mu_bc[g][s]
+// (transpose of the rough-surface boundary operator).  Threads over (s', i).
+__global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
+{
+    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    if (!A.st[ta].active) return;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    if (!d.rough) return;
+    const int N = G.N, NR = G.NR;
+    const int e = threadIdx.x;
+    if (e >= 3 * N) return;
+    const int sp = e / N, i = e - sp * N;
+    const float *mb = A.bc + (size_t)ta * NR * 3;
+    const float *R = W.srf + tk.srf_off;
+    const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
+    const float pw = (float)(fw * B.gmu[i] * B.gw[i]);
+    float acc = 0.f;
+    for (int g = 0; g < d.n_ring; ++g) {
+        const float *Rg = R + ((size_t)g * N + i) * 9 + sp;
+        acc += Rg[0] * mb[g * 3 + 0] + Rg[3] * mb[g * 3 + 1] + Rg[6] * mb[g * 3 + 2];
+    }
+    A.AF[adj_off(tk, G, A.ncot, r) + (size_t)d.nt * G.LDC + col_of(G, sp, 1, i)] += pw * acc;
+}
+
+// Final pass per adjoint task.  Pass 1 (thread per column) runs the
+// transposed transport over the adjoint total in FP64 and keeps nu in the
+// (now free) adjoint field buffer.  Pass 2 walks the levels in lock step and
+// forms, with the forward total field F_tot and total source
+// J_tot = S Xs + J_1:
+//   lev_ssa[k] = sum_c muJ[k][c] J_tot[k][c]            (x_k, y_k and J_1 scale with the albedo)
+//   lev_j1[k]  = sum_c muJ[k][c] J_1[k][c]              (J_1 ~ exp(-h_k/mu0))
+//   lay[l]     = sum_c nu . (F dT + J dCa + J dCb)_l    (layer-l transport coefficients)
+// plus, at the surface, mu_bc . dRsurf/dW . Xs_dn(BOA) and the seed terms.
+__global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
+{
+    extern __shared__ double gsm[];          // lev_ssa[K], lev_j1[K], lay[K]
+    __shared__ double red[32];
+    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int c = threadIdx.x, nt = d.nt, NR = G.NR, N = G.N, K = nt + 1;
+    double *lev_ssa = gsm, *lev_j1 = gsm + K, *lay = gsm + 2 * K;
+    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) gsm[e] = 0.0;
+    int s = 0, h = 0, g = 0;
+    if (c < G.COUT) decode_col_a(G, c, s, h, g);
+    const bool valid = c < G.COUT && g < d.n_ring;
+    const size_t off = adj_off(tk, G, A.ncot, r);
+    float *nuv = A.AF + off;
+    const double *At = A.ATot + off;
+    const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+    const float *dT = A.dTc + d.coef_off, *dA = A.dCa + d.coef_off, *dB = A.dCb + d.coef_off;
+    double nub = 0.0;                         // nu at the BOA of an up column (mu_bc)
+    if (valid) {
+        if (h == 0) {
+            double nu = 0.0;
+            for (int k = 0; k <= nt; ++k) {
+                const size_t o = (size_t)k * G.LDC + c;
+                nu = k > 0 ? At[o] + (double)Tc[(k - 1) * NR + g] * nu : At[o];
+                nuv[o] = (float)nu;
+            }
+            nub = nu;
+        } else {
+            double nu = 0.0;
+            for (int k = nt; k >= 1; --k) {
+                const size_t o = (size_t)k * G.LDC + c;
+                nu = k < nt ? At[o] + (double)Tc[k * NR + g] * nu : At[o];
+                nuv[o] = (float)nu;
+            }
+            nuv[c] = 0.f;
+        }
+    }
+    __syncthreads();
+    // pass 2: levels in lock step
+    const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
+    const float faP = valid ? pv[c] : 0.f, fmP = valid ? pv[G.LDC + c] : 0.f;
+    const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
+    const float *Jx = W.J + tk.fld_off;
+    const double *Tot = W.Tot + tk.fld_off;
+    float nu_p = 0.f, jt_p = 0.f;
+    double tot_p = 0.0;
+    const int lane = threadIdx.x & 31;
+    for (int k = 0; k <= nt; ++k) {
+        float ssa_c = 0.f, j1_c = 0.f, lay_c = 0.f;
+        float nu_k = 0.f, jt_k = 0.f;
+        double tot_k = 0.0;
+        if (valid) {
+            const size_t o = (size_t)k * G.LDC + c;
+            nu_k = nuv[o];
+            const float nu_n = k < nt ? nuv[o + G.LDC] : 0.f;
+            float mu;
+            if (h == 0) {
+                mu = k < nt ? Ca[k * NR + g] * nu_k : 0.f;
+                if (k > 0) mu += Cb[(k - 1) * NR + g] * nu_p;
+            } else {
+                mu = k > 0 ? Ca[(k - 1) * NR + g] * nu_k : 0.f;
+                if (k < nt) mu += Cb[k * NR + g] * nu_n;
+            }
+            const float x = (float)xd[k], y = (float)yd[k];
+            const float j1 = (float)ch[k] * (x * faP + y * fmP);
+            jt_k = Jx[o] + j1;
+            tot_k = Tot[o];
+            ssa_c = mu * jt_k;
+            j1_c = mu * j1;
+            if (k > 0) {
+                const int e = (k - 1) * NR + g;
+                if (h == 0)
+                    lay_c = nu_p * ((float)tot_k * dT[e] + jt_p * dA[e] + jt_k * dB[e]);
+                else
+                    lay_c = nu_k * ((float)tot_p * dT[e] + jt_k * dA[e] + jt_p * dB[e]);
+            }
+        }
+        ssa_c = warp_sum(ssa_c);
+        j1_c = warp_sum(j1_c);
+        lay_c = warp_sum(lay_c);
+        if (lane == 0) {
+            atomicAdd(&lev_ssa[k], (double)ssa_c);
+            atomicAdd(&lev_j1[k], (double)j1_c);
+            if (k > 0) atomicAdd(&lay[k - 1], (double)lay_c);
+        }
+        nu_p = nu_k; jt_p = jt_k; tot_p = tot_k;
+    }
+    // surface terms (up columns): wind derivative of the boundary operator and
+    // of the direct-beam seed, and the seed's optical-depth dependence
+    double gW = 0.0, gS = 0.0;
+    if (valid && h == 0 && d.rough) {
+        const float *Xs = W.F + tk.fld_off + (size_t)nt * G.LDC;
+        const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
+        const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
+        double acc = 0.0;
+        for (int i = 0; i < N; ++i) {
+            const double pw = (float)(fw * B.gmu[i] * B.gw[i]);
+            const float *Ri = RW + (size_t)i * 9;
+            acc += pw * ((double)Ri[0] * Xs[col_of(G, 0, 1, i)] + (double)Ri[1] * Xs[col_of(G, 1, 1, i)] +
+                         (double)Ri[2] * Xs[col_of(G, 2, 1, i)]);
+        }
+        const double tdn = exp(-d.tau_total / d.mu0);
+        const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
+        const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
+        const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
+        const double E = B.Eatt[(d.lev_off + nt) * NR + g];
+        gW = nub * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
+        gS = nub * fs * tdn * E * (double)Rs[g * 9 + s * 3];
+    }
+    gW = block_sum_a(gW, red);
+    __syncthreads();
+    gS = block_sum_a(gS, red);
+    __syncthreads();
+    double *go = A.gout + (size_t)ta * A.gstride;
+    for (int e = threadIdx.x; e < K; e += blockDim.x) {
+        go[e] = lev_ssa[e];
+        go[A.kstride + e] = lev_j1[e];
+        go[2 * A.kstride + e] = e < nt ? lay[e] : 0.0;
+    }
+    if (threadIdx.x == 0) {
+        go[3 * A.kstride + 0] = gW;
+        go[3 * A.kstride + 1] = gS;
+    }
+}
+
+// Per (pixel, cotangent row): sum the per-mode partials and apply the chain
+// rule to the layer parameters:
+//   d/ddtau_l = sum_m lay_m[l] - (1/mu0) sum_m sum_{k>l} lev_j1_m[k]
+//               - (1/mu0) sum_m seed_m + (removed view seed) + (sunglint)
+//   d/dssa_l  = sum_m lev_ssa_m[l+1] / ssa_l
+//   d/dW      = sum_m surface_m + (removed view seed) + (sunglint)
+__global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, int t0)
+{
+    extern __shared__ double psm[];          // suffix of lev_j1 [nt + 2]
+    __shared__ double dir[2];
+    const int q = p0 + blockIdx.x / A.ncot, r = blockIdx.x % A.ncot;
+    const PixDev &d = B.px[q];
+    const int nt = d.nt, M = d.M, N = G.N, NR = G.NR;
+    const double *cot = A.cot + ((size_t)q * A.ncot + r) * 3;
+    auto gout = [&](int m) -> const double * {
+        const int tl = d.task0 + m - t0;
+        return A.gout + ((size_t)tl * A.ncot + r) * A.gstride;
+    };
+    for (int k = threadIdx.x; k <= nt; k += blockDim.x) {
+        double v = 0.0;
+        for (int m = 0; m <= M; ++m) v += gout(m)[A.kstride + k];
+        psm[k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = 0.0;
+        psm[nt + 1] = 0.0;
+        for (int k = nt; k >= 0; --k) { acc += psm[k]; psm[k] = acc; }     // psm[k] = sum_{k' >= k}
+        // direct terms: the removed view seed and the sunglint
+        double dt = 0.0, dw = 0.0, seed_sum = 0.0, gw_sum = 0.0;
+        for (int m = 0; m <= M; ++m) {
+            seed_sum += gout(m)[3 * A.kstride + 1];
+            gw_sum += gout(m)[3 * A.kstride + 0];
+        }
+        dt -= seed_sum / d.mu0;
+        dw += gw_sum;
+        if (d.rough) {
+            const double tdn = exp(-d.tau_total / d.mu0);
+            int cols[2]; double cw[2]; int nc;
+            if (d.view_slot >= 0) { cols[0] = d.view_slot; cw[0] = 1.0; nc = 1; }
+            else {
+                int lo, hi; double t;
+                bracket_a(B.gmu, N, d.mu_view, lo, hi, t);
+                cols[0] = lo; cw[0] = 1.0 - t; cols[1] = hi; cw[1] = t; nc = 2;
+            }
+            for (int m = 0; m <= M; ++m) {
+                const TaskDev &tk = B.tasks[d.task0 + m];
+                double w[3];
+                mode_weights(d, m, cot, w);
+                const double fs = (m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
+                const float *Rs = W.srf + tk.srf_off + (size_t)NR * N * 9;
+                const float *RsW = A.srfW + tk.srf_off + (size_t)NR * N * 9;
+                for (int cc = 0; cc < nc; ++cc) {
+                    const int gg = cols[cc];
+                    const double mug = gg < N ? B.gmu[gg] : d.mu_view;
+                    const double E = B.Eatt[d.lev_off * NR + gg];
+                    for (int s = 0; s < 3; ++s) {
+                        const double sv = cw[cc] * fs * tdn * E * (double)Rs[gg * 9 + s * 3];
+                        const double svw = cw[cc] * fs * tdn * E * (double)RsW[gg * 9 + s * 3];
+                        dt += w[s] * sv * (1.0 / d.mu0 + 1.0 / mug);
+                        dw -= w[s] * svw;
+                    }
+                }
+            }
+            if (!d.decouple) {
+                const double phi_v = (d.raa_deg - 180.0) * OCRT_PI / 180.0;
+                const double mv = d.vza_deg > 0.0 ? d.mu_view : 1.0;
+                double gl[3];
+                sunglint(d, mv, phi_v, d.tau_total, gl);
+                const double yg = cot[0] * gl[0] + cot[1] * gl[1] - cot[2] * gl[2];
+                dt -= yg * (1.0 / d.mu0 + 1.0 / mv);
+                PixDev dp = d, dm = d;
+                const double hW = 1e-5 * d.wind;
+                dp.wind = d.wind + hW; dm.wind = d.wind - hW;
+                double gp[3], gm[3];
+                sunglint(dp, mv, phi_v, d.tau_total, gp);
+                sunglint(dm, mv, phi_v, d.tau_total, gm);
+                dw += (cot[0] * (gp[0] - gm[0]) + cot[1] * (gp[1] - gm[1]) - cot[2] * (gp[2] - gm[2])) / (2.0 * hW);
+            }
+        }
+        dir[0] = dt;
+        dir[1] = dw;
+    }
+    __syncthreads();
+    double *out = A.grad + ((size_t)q * A.ncot + r) * A.grad_stride;
+    const double *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
+    for (int l = threadIdx.x; l < nt; l += blockDim.x) {
+        double lay = 0.0, lss = 0.0;
+        for (int m = 0; m <= M; ++m) {
+            const double *go = gout(m);
+            lay += go[2 * A.kstride + l];
+            lss += go[l + 1];
+        }
+        out[l] = lay - psm[l + 1] / d.mu0 + dir[0];
+        const double w = xd[l + 1] + yd[l + 1];
+        out[nt + l] = w > 0.0 ? lss / w : 0.0;
+    }
+    if (threadIdx.x == 0) out[2 * nt] = dir[1];
+}

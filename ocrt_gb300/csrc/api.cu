@@ -32,10 +32,10 @@ int *g_pinned = nullptr;
 int g_timing = 0;
 
 enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SOURCE_TC, KC_MOL, KC_SCAN, KC_EXTRACT,
-              KC_IPSS, KC_FINAL, KC_N };
+              KC_IPSS, KC_FINAL, KC_ADJ_SCAN, KC_ADJ_SOURCE, KC_ADJ_OTHER, KC_N };
 const char *kc_names[KC_N] = {"setup", "phase_tables", "coxmunk_fourier", "primary", "source_gemm_simt",
                               "source_gemm_tcgen05", "source_molecular_lowrank", "transport_scan", "extract", "ipss",
-                              "finalize"};
+                              "finalize", "adjoint_scan", "adjoint_source", "adjoint_other"};
 
 int fail(int rc, const std::string &msg)
 {
@@ -210,6 +210,16 @@ struct Group {
     double *Tot = nullptr;
     bool use_tc = false;
     CUtensorMap mapF, mapA;
+    // per-layer overrides and the adjoint (ocrt_gb_solve_batch_adjoint)
+    bool any_layers = false;
+    int ncot = 0, ntmax = 0;
+    double *ldt = nullptr, *lss = nullptr, *cot = nullptr, *lamd = nullptr, *ATot = nullptr, *gout = nullptr,
+           *grad = nullptr;
+    float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJ = nullptr,
+          *Abc = nullptr;
+    TaskState *Ast = nullptr;
+    int *acnt = nullptr;
+    int gstride = 0, kstride = 0, grad_stride = 0;
 };
 
 size_t wave_budget_bytes()
@@ -257,12 +267,17 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot};
+                    g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
+                    g.Abc, g.Ast, g.acnt};
     for (void *p : ptrs) dfree(p);
 }
 
-int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app)
+int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app,
+                const ocrt_layers *layers = nullptr, int ncot = 0, const double *cot = nullptr)
 {
+    g.ncot = ncot;
+    std::vector<double> ldt, lss, hcot;
     const Geom G = make_geom(g.N);
     g.G = G;
     g.P = (int)g.idx.size();
@@ -285,6 +300,21 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         d.aer_h_km = o.aer_h_km; d.profile = o.rayleigh_profile; d.ray_h_km = o.rayleigh_h_km;
         d.nphi = o.n_phi_surface > 0 ? o.n_phi_surface : 1024;
         d.mom_off = -1; d.L_aer = -1;
+        d.lay_off = -1;
+        if (layers && (layers[i].dtau || layers[i].ssa)) {
+            d.lay_off = (long long)std::max(ldt.size(), lss.size());
+            ldt.resize(d.lay_off, 0.0); lss.resize(d.lay_off, 0.0);
+            for (int l = 0; l < o.n_layers; ++l) {
+                ldt.push_back(layers[i].dtau ? layers[i].dtau[l] : 0.0);
+                lss.push_back(layers[i].ssa ? layers[i].ssa[l] : 0.0);
+            }
+            d.has_dtau = layers[i].dtau != nullptr;
+            d.has_ssa = layers[i].ssa != nullptr;
+            g.any_layers = true;
+        }
+        for (int r = 0; r < ncot; ++r)
+            for (int x = 0; x < 3; ++x) hcot.push_back(cot[((size_t)i * ncot + r) * 3 + x]);
+        g.ntmax = std::max(g.ntmax, o.n_layers);
         if (a && a->tau_a > 0.0) {
             d.mom_off = (int)mb.size(); d.L_aer = a->L_max; d.tau_a = a->tau_a; d.ssa_a = a->ssa_a;
             for (int l = 0; l <= a->L_max; ++l) {
@@ -335,7 +365,9 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t pf = nm * K * G.LDC;
         const size_t po = (nm + std::min<size_t>(nm, 3)) * op_elems;
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
-        const size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
+            pb += (size_t)ncot * (pf * 16 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4;
         if (q > w.p0 && bytes + pb > budget) {
             close(q);
             w = Wave{q, 0, d.task0, 0, 0, 0, 0, 0, false, false};
@@ -383,6 +415,21 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.srf, g.wave_srf)) ||
         (rc = alloc(g.Bx, (size_t)g.wave_tasks * 6 * (g.Lmax + 1))))
         return rc;
+    if (g.any_layers && ((rc = up(g.ldt, ldt)) || (rc = up(g.lss, lss)))) return rc;
+    if (ncot > 0) {
+        g.kstride = g.ntmax + 1;
+        g.gstride = 3 * g.kstride + 2;
+        g.grad_stride = 2 * g.ntmax + 1;
+        const size_t na = (size_t)g.wave_tasks * ncot;
+        if ((rc = up(g.cot, hcot)) || (rc = alloc(g.lamd, (size_t)g.P * (G.N + 2))) ||
+            (rc = alloc(g.dTc, g.ncoef)) || (rc = alloc(g.dCa, g.ncoef)) || (rc = alloc(g.dCb, g.ncoef)) ||
+            (rc = alloc(g.srfW, g.wave_srf)) || (rc = alloc(g.AF, g.wave_fld * ncot)) ||
+            (rc = alloc(g.AJ, g.wave_fld * ncot)) || (rc = alloc(g.ATot, g.wave_fld * ncot)) ||
+            (rc = alloc(g.Abc, na * G.NR * 3)) || (rc = alloc(g.Ast, na)) ||
+            (rc = alloc(g.acnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.gout, na * g.gstride)) ||
+            (rc = alloc(g.grad, (size_t)g.P * ncot * g.grad_stride)))
+            return rc;
+    }
     // ---- source kernels: tcgen05 for the aerosol contraction when the
     // geometry allows it, CUDA cores otherwise; the low-rank molecular kernel
     // adds the m <= 2 Rayleigh term.  The per-order task lists themselves are
@@ -415,6 +462,64 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         if (e_ != cudaSuccess) return fail(OCRT_ERR_DEVICE, std::string("launch: ") + cudaGetErrorString(e_)); \
     } while (0)
 
+AdjBufs make_adj(Group &g)
+{
+    AdjBufs A;
+    A.ncot = g.ncot; A.AF = g.AF; A.AJ = g.AJ; A.ATot = g.ATot; A.bc = g.Abc; A.st = g.Ast; A.acnt = g.acnt;
+    A.cot = g.cot; A.gout = g.gout; A.gstride = g.gstride; A.kstride = g.kstride;
+    A.dTc = g.dTc; A.dCa = g.dCa; A.dCb = g.dCb; A.srfW = g.srfW; A.grad = g.grad; A.grad_stride = g.grad_stride;
+    return A;
+}
+
+// Adjoint of one wave, right after its forward orders (the forward fields of
+// the wave are still resident).
+int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &B, const WaveBufs &W, cudaStream_t st,
+                     int tc_grid, int mol_grid, int mtiles, int ltiles, dim3 sgrid, size_t tc_smem)
+{
+    const Geom G = g.G;
+    const int nw = w.t1 - w.t0, na = nw * g.ncot;
+    const int scan_threads = ((G.COUT + 31) / 32) * 32;
+    // the scattered field Xs = F_tot - F_last and its source S Xs = J_tot - J_1
+    LAUNCH(plan, KC_ADJ_OTHER, k_adj_prep<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+    const int it = g.max_orders + 1;
+    LAUNCH(plan, KC_ADJ_OTHER, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
+    if (w.n_simt) LAUNCH(plan, KC_ADJ_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
+    if (w.n_tc)
+        LAUNCH(plan, KC_ADJ_SOURCE, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(g.mapF, g.mapA, B, W, G, w.t0, it, mtiles));
+    if (w.n_mol)
+        LAUNCH(plan, KC_ADJ_SOURCE, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
+                   B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
+    // adjoint successive orders
+    CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.AJ, 0, sizeof(float) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.ATot, 0, sizeof(double) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
+    CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+    const AdjBufs A = make_adj(g);
+    LAUNCH(plan, KC_ADJ_OTHER, k_adj_init<<<(na + 127) / 128, 128, 0, st>>>(B, A, G, w.t0, na));
+    const dim3 agrid(na, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.LDC + ST_N_TILE - 1) / ST_N_TILE);
+    const int surf_threads = ((3 * G.N + 31) / 32) * 32;
+    for (int j = 1; j <= g.max_orders; ++j) {
+        LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<na, scan_threads, 0, st>>>(B, A, G, w.t0, j));
+        if ((j - 1) % 4 == 0 || j == g.max_orders) {
+            CK(cudaMemcpyAsync(g_pinned, g.acnt + j, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (*g_pinned == 0) break;
+        }
+        LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source<<<agrid, 256, 0, st>>>(B, W, A, G, w.t0));
+        if (w.n_mol)
+            LAUNCH(plan, KC_ADJ_SOURCE, k_adj_mol<<<dim3(na, ltiles), 256, adj_mol_smem_bytes(G), st>>>(
+                       B, W, A, G, w.t0, g.Bp, g.Br, g.Bt, g.Lmax));
+        if (w.any_rough)
+            LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<na, surf_threads, 0, st>>>(B, W, A, G, w.t0));
+    }
+    LAUNCH(plan, KC_ADJ_OTHER, k_adj_grad<<<na, scan_threads, sizeof(double) * 3 * (size_t)w.Kmax, st>>>(
+               B, W, A, G, w.t0));
+    LAUNCH(plan, KC_ADJ_OTHER, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
+               B, W, A, G, w.p0, w.t0));
+    return OCRT_OK;
+}
+
 int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
 {
     const Geom G = g.G;
@@ -424,14 +529,18 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     LAUNCH(plan, KC_SETUP, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
     LAUNCH(plan, KC_SETUP, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
     LAUNCH(plan, KC_SETUP, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
+    if (g.any_layers)
+        LAUNCH(plan, KC_SETUP, k_layers_apply<<<P, 256, 0, st>>>(g.px, P, g.ldt, g.lss, g.h, g.ch, g.xd, g.yd, g.err));
     LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
     LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
     if (g.any_rough) {
         LAUNCH(plan, KC_SETUP, k_cs_table<<<g.Mmax + 2, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
         LAUNCH(plan, KC_SETUP, k_seed_att<<<dim3(8, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Eatt));
-        LAUNCH(plan, KC_SETUP, k_sancer<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.lam));
+        LAUNCH(plan, KC_SETUP, k_sancer<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.lam, g.ncot ? g.lamd : nullptr));
     }
     if (g.any_flat) LAUNCH(plan, KC_SETUP, k_flat_fresnel<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.frs));
+    if (g.ncot)
+        LAUNCH(plan, KC_SETUP, k_coef_deriv<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.dTc, g.dCa, g.dCb));
 
     BatchBufs B;
     B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
@@ -456,9 +565,13 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
         if (w.any_rough) {
-            const size_t smem = sizeof(float) * (9 * (g.nphi / 2 + 1) + (size_t)(256 / (2 * ((g.Mmax + 4) / 4))) * (g.Mmax + 1) * 9);
-            LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
-                       g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.lam, g.srf));
+            const size_t smem = coxmunk_smem_bytes(g.nphi, g.ncot > 0);
+            if (g.ncot)
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk_dw<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
+                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.lam, g.lamd, g.srf, g.srfW));
+            else
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
+                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.lam, g.srf));
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
@@ -486,6 +599,10 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
             }
         }
         LAUNCH(plan, KC_EXTRACT, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
+        if (g.ncot) {
+            const int rc = run_adjoint_wave(plan, g, w, B, W, st, tc_grid, mol_grid, mtiles, ltiles, sgrid, tc_smem);
+            if (rc) return rc;
+        }
     }
     if (g.any_pssa) {
         int maxnt = 0;
@@ -530,9 +647,11 @@ int ocrt_gb_init(int device)
     CK(cudaMallocHost(&g_pinned, sizeof(int) * 16));
     CK(cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, device));
     CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_coxmunk_dw, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_adj_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     g_device = device;
     return OCRT_OK;
 }
@@ -552,14 +671,39 @@ void ocrt_gb_shutdown(void)
 
 const char *ocrt_gb_last_error(void) { return g_err.c_str(); }
 
-int ocrt_gb_plan_create(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
-                        const ocrt_aerosol *aer, int app, ocrt_plan **out)
+}   // extern "C"
+
+namespace {
+
+int validate_layers(const ocrt_case *cs, const ocrt_opts *op, const ocrt_layers *ly, int ncot)
+{
+    if ((ly || ncot > 0) && op->pssa)
+        return fail(OCRT_ERR_UNSUPPORTED, "IPSS cannot be combined with layer overrides or gradients");
+    if (ncot > 0) {
+        const bool rough = cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && cs->wind_speed > 0.0;
+        if (cs->surface != OCRT_SURFACE_BLACK && !rough)
+            return fail(OCRT_ERR_UNSUPPORTED, "gradients need a black or rough (wind > 0) Fresnel surface");
+    }
+    if (!ly) return OCRT_OK;
+    if (ly->n_layers != op->n_layers) return fail(OCRT_ERR_ARGS, "layers.n_layers differs from opts.n_layers");
+    for (int l = 0; l < ly->n_layers; ++l) {
+        if (ly->dtau && !(std::isfinite(ly->dtau[l]) && ly->dtau[l] > 0.0))
+            return fail(OCRT_ERR_ARGS, "layer optical depth not finite and positive");
+        if (ly->ssa && !(ly->ssa[l] >= 0.0 && ly->ssa[l] <= 1.0))
+            return fail(OCRT_ERR_ARGS, "layer single-scattering albedo outside [0, 1]");
+    }
+    return OCRT_OK;
+}
+
+int plan_create_impl(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app,
+                     const ocrt_layers *layers, int ncot, const double *cot, ocrt_plan **out)
 {
     if (!out) return fail(OCRT_ERR_ARGS, "null plan pointer");
     *out = nullptr;
     if (n < 0 || (n > 0 && (!cases || !opts))) return fail(OCRT_ERR_ARGS, "bad batch arguments");
     for (int i = 0; i < n; ++i) {
-        const int rc = validate(&cases[i], opp ? &opts[i] : &opts[0], aer ? (app ? &aer[i] : &aer[0]) : nullptr);
+        int rc = validate(&cases[i], opp ? &opts[i] : &opts[0], aer ? (app ? &aer[i] : &aer[0]) : nullptr);
+        if (!rc) rc = validate_layers(&cases[i], opp ? &opts[i] : &opts[0], layers ? &layers[i] : nullptr, ncot);
         if (rc) return rc;
     }
     int rc = ensure_init();
@@ -575,7 +719,7 @@ int ocrt_gb_plan_create(int n, const ocrt_case *cases, const ocrt_opts *opts, in
         plan->groups[it->second].idx.push_back(i);
     }
     for (Group &g : plan->groups) {
-        rc = build_group(g, cases, opts, opp, aer, app);
+        rc = build_group(g, cases, opts, opp, aer, app, layers, ncot, cot);
         if (rc) {
             for (Group &h : plan->groups) free_group(h);
             delete plan;
@@ -589,6 +733,16 @@ int ocrt_gb_plan_create(int n, const ocrt_case *cases, const ocrt_opts *opts, in
     }
     *out = plan;
     return OCRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int ocrt_gb_plan_create(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
+                        const ocrt_aerosol *aer, int app, ocrt_plan **out)
+{
+    return plan_create_impl(n, cases, opts, opp, aer, app, nullptr, 0, nullptr, out);
 }
 
 int ocrt_gb_plan_execute(ocrt_plan *plan, void *stream)
@@ -717,6 +871,44 @@ int ocrt_gb_solve_batch(int n, const ocrt_case *cases, const ocrt_opts *opts, in
     if (rc) return rc;
     rc = ocrt_gb_plan_execute(plan, stream);
     if (!rc) rc = ocrt_gb_plan_results(plan, out, stream);
+    ocrt_gb_plan_destroy(plan);
+    return rc;
+}
+
+int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
+                                const ocrt_aerosol *aer, int app, const ocrt_layers *layers, int n_cot,
+                                const double *cot, ocrt_result *out, ocrt_grad *grad, void *stream)
+{
+    if (n == 0) return OCRT_OK;
+    if (!out) return fail(OCRT_ERR_ARGS, "null output");
+    if (n_cot < 0 || n_cot > 3) return fail(OCRT_ERR_ARGS, "n_cot outside [0, 3]");
+    if (n_cot > 0 && (!cot || !grad)) return fail(OCRT_ERR_ARGS, "null cotangent or gradient array");
+    if (n_cot > 0)
+        for (int i = 0; i < n * n_cot; ++i)
+            if (!grad[i].d_dtau || !grad[i].d_ssa) return fail(OCRT_ERR_ARGS, "null gradient array");
+    ocrt_plan *plan = nullptr;
+    int rc = plan_create_impl(n, cases, opts, opp, aer, app, layers, n_cot, cot, &plan);
+    if (rc) return rc;
+    rc = ocrt_gb_plan_execute(plan, stream);
+    if (!rc) rc = ocrt_gb_plan_results(plan, out, stream);
+    if (!rc && n_cot > 0) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
+        for (Group &g : plan->groups) {
+            std::vector<double> h((size_t)g.P * n_cot * g.grad_stride);
+            if (cudaMemcpyAsync(h.data(), g.grad, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess) { rc = fail(OCRT_ERR_DEVICE, "gradient copy failed"); break; }
+            for (int q = 0; q < g.P; ++q) {
+                const int i = g.idx[q], nt = g.hpx[q].nt;
+                for (int r = 0; r < n_cot; ++r) {
+                    const double *src = h.data() + ((size_t)q * n_cot + r) * g.grad_stride;
+                    ocrt_grad &gr = grad[(size_t)i * n_cot + r];
+                    for (int l = 0; l < nt; ++l) { gr.d_dtau[l] = src[l]; gr.d_ssa[l] = src[nt + l]; }
+                    gr.d_wind = src[2 * nt];
+                }
+            }
+        }
+    }
     ocrt_gb_plan_destroy(plan);
     return rc;
 }

@@ -39,6 +39,8 @@ struct PixDev {
     int task0;              // first task of this pixel
     long long lev_off;      // offset of level arrays (nt+1 entries)
     long long coef_off;     // offset of transport coefficients (nt * NR entries)
+    long long lay_off;      // offset of the per-layer override arrays (nt entries), -1 = none
+    int has_dtau, has_ssa;  // which overrides are present
     // ---- derived on device (k_pixel_setup) ----
     double mu0, mu_view, tau_r, tau_total;
     int n_ring, view_slot;  // view_slot: ring slot holding mu_view, -1 = interpolate

@@ -18,9 +18,16 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
                          float *ops, float *pvec, float *fvec);
-__global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
-                          Geom G, const double *gmu, const float *cs_tab, const double *lamv, float *srf);
-__global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam);
+__global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
+                          const double *gmu, const float *cs_tab, const double *lamv, float *srf);
+__global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
+                             const double *gmu, const float *cs_tab, const double *lamv, const double *lamd,
+                             float *srf, float *srfW);
+__global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam, double *lamd);
+__global__ void k_layers_apply(PixDev *px, int P, const double *ldt, const double *lss, double *h, double *ch,
+                               double *xd, double *yd, int *err);
+__global__ void k_coef_deriv(const PixDev *px, int P, int N, const double *gmu, const double *h,
+                             float *dTc, float *dCa, float *dCb);
 __global__ void k_cs_table(int M, int nphi, float *cs);
 __global__ void k_flat_fresnel(const PixDev *px, int P, int N, const double *gmu, float *frs);
 __global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, double *E);
@@ -53,12 +60,41 @@ struct BatchBufs {
     int *err;              // device error word
 };
 
+// adjoint.cu
+struct AdjBufs {
+    int ncot;              // cotangent rows per pixel; adjoint task = wave task * ncot + row
+    float *AF, *AJ;        // adjoint field a_j and transposed-transport output muJ (wave-relative, x ncot)
+    double *ATot;          // adjoint total
+    float *bc;             // mu_bc per adjoint task [NR][3]
+    TaskState *st;         // per adjoint task
+    int *acnt;             // [max_orders + 2] adjoint tasks still active after order j
+    const double *cot;     // [P][ncot][3]
+    double *gout;          // per adjoint task partials, gstride doubles (3 arrays of kstride + 2 scalars)
+    int gstride, kstride;
+    const float *dTc, *dCa, *dCb;   // transport-coefficient derivatives (like Tc/Ca/Cb)
+    const float *srfW;     // dR_m/dW, laid out like WaveBufs::srf
+    double *grad;          // [P][ncot][grad_stride]: d_dtau[nt], d_ssa[nt], d_wind
+    int grad_stride;
+};
+__global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0);
+__global__ void k_fill_all(BatchBufs B, int t0, int nw, int it);
+__global__ void k_adj_init(BatchBufs B, AdjBufs A, Geom G, int t0, int nadj);
+__global__ void k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j);
+__global__ void k_adj_source(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
+__global__ void k_adj_mol(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0,
+                          const float *Bp, const float *Br, const float *Bt, int L);
+__global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
+__global__ void k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
+__global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, int t0);
+size_t adj_mol_smem_bytes(const Geom &G);
+
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
 __global__ void k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
                             BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
+size_t coxmunk_smem_bytes(int nphi, bool dw);
 size_t tc_smem_bytes(const Geom &G);
 bool tc_supported(const Geom &G);
 __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);

@@ -102,6 +102,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     const int NR = G.NR;
     PixDev d;
     memset(&d, 0, sizeof(d));
+    d.lay_off = -1;
     d.sza_deg = cs->sza_deg; d.vza_deg = cs->vza_deg; d.raa_deg = cs->raa_deg; d.wavelength_nm = cs->wavelength_nm;
     d.pressure_hpa = cs->pressure_hpa; d.tau_r_input = cs->tau_r_input;
     d.n_water = cs->n_water; d.wind = cs->wind_speed; d.surface = cs->surface;
@@ -199,8 +200,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     if (rough) {
         NA_LAUNCH(k_cs_table<<<T + 1, 256, 0, st>>>(M, d.nphi, cst));
         NA_LAUNCH(k_seed_att<<<dim3(8, 1), 256, 0, st>>>(px, 1, N, gmu, h, Eatt));
-        NA_LAUNCH(k_sancer<<<1, 128, 0, st>>>(px, 1, N, gmu, lamv));
-        NA_LAUNCH(k_coxmunk<<<dim3(N + 1, NR, 1), 256, sizeof(float) * (9 * (d.nphi / 2 + 1) + (size_t)(256 / (2 * ((M + 4) / 4))) * (M + 1) * 9), st>>>(
+        NA_LAUNCH(k_sancer<<<1, 128, 0, st>>>(px, 1, N, gmu, lamv, nullptr));
+        NA_LAUNCH(k_coxmunk<<<dim3(N + 1, NR, 1), 256, coxmunk_smem_bytes(d.nphi, false), st>>>(
             tasks, px, 0, ptask0, G, gmu, cst, lamv, srf));
     }
     if (flat) NA_LAUNCH(k_flat_fresnel<<<1, 128, 0, st>>>(px, 1, N, gmu, frs));

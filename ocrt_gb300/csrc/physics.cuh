@@ -164,6 +164,14 @@ __host__ __device__ inline double slope_variance(double ws, int sigma_type)
     return fmax(s * s, 1e-10);
 }
 
+// d(slope variance)/d(wind speed) of slope_variance (0 where a floor is active).
+__host__ __device__ inline double slope_variance_dw(double ws, int sigma_type)
+{
+    if (sigma_type == 1) return ws > 0.01 ? 0.00512 : 0.0;
+    const double s2 = 0.0731 * 0.0731 * fmax(0.0, ws);
+    return s2 > 1e-10 ? 0.0731 * 0.0731 : 0.0;
+}
+
 // Sancer shadowing term of one direction (shared/surface.c:578-598), FP64.
 __device__ inline double sancer_lambda(double mu, double slen)
 {
@@ -172,6 +180,18 @@ __device__ inline double sancer_lambda(double mu, double slen)
     const double nu = (mu / s) / slen;
     if (nu > 20.0) return 0.0;
     return 0.5 * (exp(-nu * nu) / (nu * sqrt(OCRT_PI)) - erfc(nu));
+}
+
+// d lambda / d s2 of sancer_lambda with slen = sqrt(s2): lambda depends on
+// nu = mu / (sqrt(1 - mu^2) slen) only, dlambda/dnu = -exp(-nu^2) / (2 sqrt(pi) nu^2)
+// and dnu/ds2 = -nu / (2 s2), so dlambda/ds2 = exp(-nu^2) / (4 sqrt(pi) nu s2).
+__device__ inline double sancer_lambda_ds2(double mu, double slen)
+{
+    if (!(mu < 1.0 - 1e-10)) return 0.0;
+    const double s = sqrt(fmax(1e-20, 1.0 - mu * mu));
+    const double nu = (mu / s) / slen;
+    if (nu > 20.0) return 0.0;
+    return exp(-nu * nu) / (4.0 * sqrt(OCRT_PI) * nu * slen * slen);
 }
 
 // Cox-Munk + Fresnel reflection Mueller R(mu_out, mu_in_dn, phi)
@@ -185,7 +205,7 @@ __device__ inline double sancer_lambda(double mu, double slen)
 // peak the reference form loses ~eps/sigma^2 in FP32.
 template <typename T>
 __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T shalf2, T sig2, T lam,
-                                 T nw, int qconv, T *R)
+                                 T nw, int qconv, T *R, T *tb2_out = nullptr)
 {
 #pragma unroll
     for (int i = 0; i < 9; ++i) R[i] = T(0);
@@ -223,6 +243,7 @@ __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T shalf2,
     fresnel_R<T>(cw, nw, qconv, MF);
     const T cb2 = cb * cb;
     const T tb2 = Bt / A2;
+    if (tb2_out) *tb2_out = tb2;
     const T Ps = (T(1) / (T(OCRT_PI) * sig2)) * exp(-tb2 / sig2);
     const T brdf = (Ps / (T(1) + lam)) / (T(4) * mu_in_dn * mu_out * cb2 * cb2);
     // R = L2 * MF * L1 * brdf with L(c,s) = [[1,0,0],[0,c2,-s2],[0,s2,c2]]
@@ -236,4 +257,34 @@ __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T shalf2,
     R[0] = A00 * brdf; R[1] = A01 * brdf; R[2] = A02 * brdf;
     R[3] = (a2 * A10 - b2 * A20) * brdf; R[4] = (a2 * A11 - b2 * A21) * brdf; R[5] = (a2 * A12 - b2 * A22) * brdf;
     R[6] = (b2 * A10 + a2 * A20) * brdf; R[7] = (b2 * A11 + a2 * A21) * brdf; R[8] = (b2 * A12 + a2 * A22) * brdf;
+}
+
+// Direct sunglint reflectance (shared/surface.c:1813-1907), FP64.
+__device__ inline void sunglint(const PixDev &d, double mu_v, double phi_v, double tau, double *g)
+{
+    const double mu0 = d.mu0;
+    const double trans = exp(-tau / mu0) * exp(-tau / mu_v);
+    if (d.wind < 1e-6) {
+        const double fov = 0.5 * OCRT_PI / 180.0;
+        const double s0 = sqrt(fmax(0.0, 1.0 - mu0 * mu0));
+        const double smu = fov * fmax(s0, 1e-3), sph = fov;
+        double de = phi_v;
+        while (de > OCRT_PI) de -= 2.0 * OCRT_PI;
+        while (de < -OCRT_PI) de += 2.0 * OCRT_PI;
+        const double dm = mu_v - mu0;
+        const double ex = -0.5 * (dm * dm / (smu * smu) + de * de / (sph * sph));
+        if (ex < -50.0) { g[0] = g[1] = g[2] = 0.0; return; }
+        double MF[9];
+        fresnel_R<double>(mu0, d.n_water, d.q_conv, MF);
+        const double den = fmax(2.0 * mu0 * s0 * mu0 * mu_v, 1e-12);
+        const double r = 4.0 * OCRT_PI * trans / den * exp(ex);
+        g[0] = MF[0] * r; g[1] = MF[3] * r; g[2] = MF[6] * r;
+        return;
+    }
+    const double s2v = slope_variance(d.wind, d.sigma_type);
+    const double lam = sancer_lambda(mu0, sqrt(s2v)) + sancer_lambda(mu_v, sqrt(s2v));
+    double R[9];
+    const double sh = sin(0.5 * phi_v);
+    coxmunk_R<double>(mu_v, mu0, cos(phi_v), sin(phi_v), sh * sh, s2v, lam, d.n_water, d.q_conv, R);
+    g[0] = OCRT_PI * R[0] * trans; g[1] = OCRT_PI * R[3] * trans; g[2] = OCRT_PI * R[6] * trans;
 }

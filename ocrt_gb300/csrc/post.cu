@@ -186,35 +186,6 @@ __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z
     }
 }
 
-// Direct sunglint reflectance (shared/surface.c:1813-1907), FP64.
-__device__ void sunglint(const PixDev &d, double mu_v, double phi_v, double tau, double *g)
-{
-    const double mu0 = d.mu0;
-    const double trans = exp(-tau / mu0) * exp(-tau / mu_v);
-    if (d.wind < 1e-6) {
-        const double fov = 0.5 * OCRT_PI / 180.0;
-        const double s0 = sqrt(fmax(0.0, 1.0 - mu0 * mu0));
-        const double smu = fov * fmax(s0, 1e-3), sph = fov;
-        double de = phi_v;
-        while (de > OCRT_PI) de -= 2.0 * OCRT_PI;
-        while (de < -OCRT_PI) de += 2.0 * OCRT_PI;
-        const double dm = mu_v - mu0;
-        const double ex = -0.5 * (dm * dm / (smu * smu) + de * de / (sph * sph));
-        if (ex < -50.0) { g[0] = g[1] = g[2] = 0.0; return; }
-        double MF[9];
-        fresnel_R<double>(mu0, d.n_water, d.q_conv, MF);
-        const double den = fmax(2.0 * mu0 * s0 * mu0 * mu_v, 1e-12);
-        const double r = 4.0 * OCRT_PI * trans / den * exp(ex);
-        g[0] = MF[0] * r; g[1] = MF[3] * r; g[2] = MF[6] * r;
-        return;
-    }
-    const double s2v = slope_variance(d.wind, d.sigma_type);
-    const double lam = sancer_lambda(mu0, sqrt(s2v)) + sancer_lambda(mu_v, sqrt(s2v));
-    double R[9];
-    const double sh = sin(0.5 * phi_v);
-    coxmunk_R<double>(mu_v, mu0, cos(phi_v), sin(phi_v), sh * sh, s2v, lam, d.n_water, d.q_conv, R);
-    g[0] = OCRT_PI * R[0] * trans; g[1] = OCRT_PI * R[3] * trans; g[2] = OCRT_PI * R[6] * trans;
-}
 
 __global__ void k_finalize(const PixDev *px, int P, const TaskState *state, const TaskOut *tout,
                            const double *gmu, const double *gw, const double *h,

@@ -162,6 +162,72 @@ __global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const 
 }
 
 // GSF basis at the Gauss nodes for every mode: B[(m*(L+1) + l)*N + g], 3 arrays.
+// Per-layer overrides (ocrt_layers): optical depths replace the uniform level
+// grid (prefix sum in FP64, one thread per pixel) and the layer albedos
+// rescale the scattering fractions of the layer's bottom level.  Runs after
+// k_level_mix, so the mixing fractions stay those of the uniform grid.
+__global__ void k_layers_apply(PixDev *px, int P, const double *ldt, const double *lss, double *h, double *ch,
+                               double *xd, double *yd, int *err)
+{
+    const int p = blockIdx.x;
+    if (p >= P) return;
+    PixDev &d = px[p];
+    if (d.lay_off < 0) return;
+    const int nt = d.nt;
+    double *hh = h + d.lev_off;
+    if (d.has_dtau) {
+        if (threadIdx.x == 0) {
+            double acc = 0.0;
+            hh[0] = 0.0;
+            for (int l = 0; l < nt; ++l) { acc += ldt[d.lay_off + l]; hh[l + 1] = acc; }
+            d.tau_total = acc;
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k <= nt; k += blockDim.x) ch[d.lev_off + k] = 0.5 * exp(-hh[k] / d.mu0);
+    }
+    if (d.has_ssa) {
+        for (int l = threadIdx.x; l < nt; l += blockDim.x) {
+            const long long o = d.lev_off + l + 1;
+            const double w = lss[d.lay_off + l], w0 = xd[o] + yd[o];
+            if (!(w0 > 0.0)) { atomicExch(err, OCRT_ERR_ARGS); continue; }
+            xd[o] *= w / w0;
+            yd[o] *= w / w0;
+        }
+    }
+}
+
+// Derivatives of the transport coefficients with respect to the layer optical
+// depth, for the adjoint.  With x = dtau/mu: T = e^-x, G = (1-T)/x - T,
+// Ca = (1 - T - G)/2, Cb = G/2; dT/dx = -T, dG/dx = T + T/x - (1-T)/x^2 (its
+// Taylor series below x = 1e-2, where the closed form cancels), and
+// d/ddtau = (1/mu) d/dx.
+__global__ void k_coef_deriv(const PixDev *px, int P, int N, const double *gmu, const double *h,
+                             float *dTc, float *dCa, float *dCb)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    const int NR = N + 1;
+    const int total = d.nt * NR;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int layer = e / NR, g = e - layer * NR;
+        const long long o = d.coef_off + e;
+        double am = g < N ? gmu[g] : d.mu_view;
+        if (g >= d.n_ring) am = 1.0;
+        const double dtau = h[d.lev_off + layer + 1] - h[d.lev_off + layer];
+        const double x = dtau / am;
+        const double T = exp(-x);
+        double Gp;
+        if (x < 1e-2)
+            Gp = 0.5 + x * (-2.0 / 3.0 + x * (3.0 / 8.0 + x * (-2.0 / 15.0 + x * (5.0 / 144.0 - x / 140.0))));
+        else
+            Gp = T + T / x + expm1(-x) / (x * x);
+        dTc[o] = (float)(-T / am);
+        dCa[o] = (float)(0.5 * (T - Gp) / am);
+        dCb[o] = (float)(0.5 * Gp / am);
+    }
+}
+
 __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt)
 {
     const int m = blockIdx.x, g = threadIdx.x;
@@ -444,10 +510,20 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
 // phi -> 2pi - phi flips exactly the sin entries), projection onto cos/sin
 // mphi in FP32, normalisation dphi/(2pi or pi) and the m>0 IU/QU sign of
 // shared/surface.c:896-906 applied at the end.
-__global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
-                          Geom G, const double *gmu, const float *cs_tab, const double *lamv, float *srf)
+#define CM_MG 5
+
+// DW = true additionally writes srfW = dR_m/dW.  Only the slope-distribution
+// factor of R depends on the wind: R = brdf * (Fresnel, rotations) with
+// brdf ~ exp(-tan^2(beta)/s2) / (pi s2 (1 + lam)), so
+//   dR/dW = ds2/dW * R * [ -1/s2 + tan^2(beta)/s2^2 - (dlam/ds2)/(1 + lam) ]
+// and dR_m/dW = a R_m + b P_m[R tan^2(beta)] with per-pair constants a, b and
+// P_m the same azimuth projection.
+template <bool DW>
+__device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
+                                             Geom G, const double *gmu, const float *cs_tab, const double *lamv,
+                                             const double *lamd, float *srf, float *srfW)
 {
-    extern __shared__ float sm_R[];                 // [9][nphi/2 + 1]
+    extern __shared__ float sm_R[];                 // [9][nphi/2 + 1] (and R tan^2(beta) when DW)
     const int p = p0 + blockIdx.z;
     const PixDev &d = px[p];
     if (!d.rough) return;
@@ -465,75 +541,121 @@ __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const 
     const double dphi = 2.0 * OCRT_PI / (double)nphi;
     const float *ptab = cs_tab + (size_t)(d.M + 1) * 2 * half;     // [cos, sin, sin^2(phi/2)][half]
     const float fmo = (float)mo, fmi = (float)mi, fs2 = (float)s2v, flam = (float)lam, fnw = (float)d.n_water;
+    float *sm_T = sm_R + 9 * hs;
     for (int q = threadIdx.x; q < half; q += blockDim.x) {
-        float R[9];
-        coxmunk_R<float>(fmo, fmi, ptab[q], ptab[half + q], ptab[2 * half + q], fs2, flam, fnw, d.q_conv, R);
+        float R[9], tb2 = 0.f;
+        coxmunk_R<float>(fmo, fmi, ptab[q], ptab[half + q], ptab[2 * half + q], fs2, flam, fnw, d.q_conv, R,
+                         DW ? &tb2 : nullptr);
 #pragma unroll
         for (int e = 0; e < 9; ++e) sm_R[e * hs + q] = R[e];
+        if (DW) {
+#pragma unroll
+            for (int e = 0; e < 9; ++e) sm_T[e * hs + q] = R[e] * tb2;
+        }
+    }
+    float ca = 0.f, cb = 0.f;
+    if (DW) {
+        const double ds2 = slope_variance_dw(d.wind, d.sigma_type);
+        const double *ld = lamd + (size_t)p * (N + 2);
+        const double dlam = ld[i < N ? i : N + 1] + ld[os];
+        ca = (float)(ds2 * (-1.0 / s2v - dlam / (1.0 + lam)));
+        cb = (float)(ds2 / (s2v * s2v));
     }
     __syncthreads();
-    // Projection onto cos/sin(m phi): work item = (cos or sin entry group,
-    // group of 4 modes); threads beyond the item count split the azimuth
-    // range and are reduced through shared memory.  Each thread keeps a 5x4
-    // (cos) or 4x4 (sin) register tile, so every table value and every
-    // Mueller value it loads feeds 4-5 FMAs.
+    // Projection onto cos/sin(m phi).  Work item = (cos or sin entry group,
+    // group of CM_MG modes), one warp per item; the 32 lanes stride the
+    // azimuth nodes, so every table and Mueller load of a warp is one
+    // contiguous run, and each lane keeps a 5 x CM_MG register tile.  The
+    // lane partials are summed with shuffles.
     const int M = d.M;
-    const int nmg = (M + 4) / 4;                    // mode groups of 4
+    const int nmg = (M + CM_MG) / CM_MG;
     const int items = 2 * nmg;
-    const int S = blockDim.x / items;               // azimuth slices (>= 1)
-    float *part = sm_R + 9 * hs;                    // [S][(M+1)*9]
-    const int nout = (M + 1) * 9;
-    const int t = threadIdx.x;
-    const int item = t % items, slice = t / items;
-    if (slice < S) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int task_first = pix_task0[p];
+    const float scale0 = (float)(2.0 * dphi / (2.0 * OCRT_PI)), scale1 = (float)(2.0 * dphi / OCRT_PI);
+    const int ecos[5] = {0, 1, 3, 4, 8}, esin[5] = {2, 5, 6, 7, 7};
+    constexpr int AT = DW ? 5 : 1;
+    for (int item = warp; item < items; item += nwarp) {
         const int kind = item & 1, mg = item >> 1;  // kind 0: cos entries, 1: sin entries
-        const int ecos[5] = {0, 1, 3, 4, 8}, esin[4] = {2, 5, 6, 7};
         const int ne = kind == 0 ? 5 : 4;
-        const int q0 = (int)((long long)half * slice / S), q1 = (int)((long long)half * (slice + 1) / S);
-        float acc[5][4];
+        float acc[5][CM_MG], acct[AT][CM_MG];
 #pragma unroll
         for (int a = 0; a < 5; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-        const float *tb[4];
+            for (int b = 0; b < CM_MG; ++b) acc[a][b] = 0.f;
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int m = min(4 * mg + b, M);
+        for (int a = 0; a < AT; ++a)
+#pragma unroll
+            for (int b = 0; b < CM_MG; ++b) acct[a][b] = 0.f;
+        const float *tb[CM_MG];
+#pragma unroll
+        for (int b = 0; b < CM_MG; ++b) {
+            const int m = min(CM_MG * mg + b, M);
             tb[b] = cs_tab + ((size_t)m * 2 + kind) * half;
         }
-        for (int q = q0; q < q1; ++q) {
-            float tv[4], rv[5];
+        int ro[5];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) tv[b] = __ldg(tb[b] + q);
+        for (int a = 0; a < 5; ++a) ro[a] = (kind == 0 ? ecos[a] : esin[a]) * hs;
+        for (int q = lane; q < half; q += 32) {
+            float tv[CM_MG], rv[5];
 #pragma unroll
-            for (int a = 0; a < 5; ++a) rv[a] = a < ne ? sm_R[(kind == 0 ? ecos[a] : esin[a < 4 ? a : 3]) * hs + q] : 0.f;
+            for (int b = 0; b < CM_MG; ++b) tv[b] = __ldg(tb[b] + q);
 #pragma unroll
-            for (int a = 0; a < 5; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(rv[a], tv[b], acc[a][b]);
-        }
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int m = 4 * mg + b;
-            if (m > M) continue;
+            for (int a = 0; a < 5; ++a) rv[a] = sm_R[ro[a] + q];
 #pragma unroll
             for (int a = 0; a < 5; ++a)
-                if (a < ne) part[(size_t)slice * nout + m * 9 + (kind == 0 ? ecos[a] : esin[a])] = acc[a][b];
+#pragma unroll
+                for (int b = 0; b < CM_MG; ++b) acc[a][b] = fmaf(rv[a], tv[b], acc[a][b]);
+            if (DW) {
+#pragma unroll
+                for (int a = 0; a < AT; ++a) rv[a] = sm_T[ro[a] + q];
+#pragma unroll
+                for (int a = 0; a < AT; ++a)
+#pragma unroll
+                    for (int b = 0; b < CM_MG; ++b) acct[a][b] = fmaf(rv[a], tv[b], acct[a][b]);
+            }
         }
+#pragma unroll
+        for (int a = 0; a < 5; ++a)
+#pragma unroll
+            for (int b = 0; b < CM_MG; ++b)
+#pragma unroll
+                for (int o2 = 16; o2 > 0; o2 >>= 1) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], o2);
+#pragma unroll
+        for (int a = 0; a < AT; ++a)
+#pragma unroll
+            for (int b = 0; b < CM_MG; ++b)
+#pragma unroll
+                for (int o2 = 16; o2 > 0; o2 >>= 1) acct[a][b] += __shfl_xor_sync(0xffffffffu, acct[a][b], o2);
+        // lane (a * CM_MG + b) stores entry a of mode CM_MG * mg + b
+#pragma unroll
+        for (int a = 0; a < 5; ++a)
+#pragma unroll
+            for (int b = 0; b < CM_MG; ++b) {
+                const int m = CM_MG * mg + b;
+                if (lane != a * CM_MG + b || a >= ne || m > M) continue;
+                const int e = kind == 0 ? ecos[a] : esin[a];
+                float sc = m == 0 ? scale0 : scale1;
+                if (m > 0 && (e == 2 || e == 5)) sc = -sc;
+                const TaskDev &tk = tasks[task_first + m];
+                const size_t off = i < N ? ((size_t)os * N + i) * 9 + e : (size_t)G.NR * N * 9 + (size_t)os * 9 + e;
+                srf[tk.srf_off + off] = acc[a][b] * sc;
+                if (DW) srfW[tk.srf_off + off] = (ca * acc[a][b] + cb * acct[AT == 5 ? a : 0][b]) * sc;
+            }
     }
-    __syncthreads();
-    const int task_first = pix_task0[p];
-    for (int e2 = t; e2 < nout; e2 += blockDim.x) {
-        const int m = e2 / 9, e = e2 - m * 9;
-        double v = 0.0;
-        for (int sl = 0; sl < S; ++sl) v += (double)part[(size_t)sl * nout + e2];
-        v *= 2.0 * dphi * (m == 0 ? 1.0 / (2.0 * OCRT_PI) : 1.0 / OCRT_PI);
-        if (m > 0 && (e == 2 || e == 5)) v = -v;
-        const TaskDev &tk = tasks[task_first + m];
-        float *dst = srf + tk.srf_off;
-        if (i < N) dst[((size_t)os * N + i) * 9 + e] = (float)v;
-        else dst[(size_t)G.NR * N * 9 + (size_t)os * 9 + e] = (float)v;
-    }
+}
+
+__global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
+                          const double *gmu, const float *cs_tab, const double *lamv, float *srf)
+{
+    coxmunk_body<false>(tasks, px, p0, pix_task0, G, gmu, cs_tab, lamv, nullptr, srf, nullptr);
+}
+
+__global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
+                             const double *gmu, const float *cs_tab, const double *lamv, const double *lamd,
+                             float *srf, float *srfW)
+{
+    coxmunk_body<true>(tasks, px, p0, pix_task0, G, gmu, cs_tab, lamv, lamd, srf, srfW);
 }
 
 // cos / sin(m phi_q) on the half azimuth grid for m = 0..M, followed by the
@@ -561,14 +683,16 @@ __global__ void k_cs_table(int M, int nphi, float *cs)
 
 // Sancer shadowing term lambda(mu) (shared/surface.c:578-598) of every ring
 // slot and of the sun, once per rough pixel: lam[p*(N+2) + slot], slot N+1 = sun.
-__global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam)
+__global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam, double *lamd)
 {
     const int p = blockIdx.x, s = threadIdx.x;
     if (p >= P || s > N + 1) return;
     const PixDev &d = px[p];
     if (!d.rough) return;
     const double mu = s < N ? gmu[s] : (s == N ? d.mu_view : d.mu0);
-    lam[(size_t)p * (N + 2) + s] = sancer_lambda(mu, sqrt(slope_variance(d.wind, d.sigma_type)));
+    const double slen = sqrt(slope_variance(d.wind, d.sigma_type));
+    lam[(size_t)p * (N + 2) + s] = sancer_lambda(mu, slen);
+    if (lamd) lamd[(size_t)p * (N + 2) + s] = sancer_lambda_ds2(mu, slen);
 }
 
 // Direct-beam attenuation from the surface to level k along slot g,
@@ -601,4 +725,9 @@ __global__ void k_flat_fresnel(const PixDev *px, int P, int N, const double *gmu
     double M[9];
     fresnel_R<double>(mu, d.n_water, d.q_conv, M);
     for (int e = 0; e < 9; ++e) frs[((size_t)p * (N + 1) + os) * 9 + e] = (float)M[e];
+}
+
+size_t coxmunk_smem_bytes(int nphi, bool dw)
+{
+    return sizeof(float) * 9 * (size_t)(nphi / 2 + 1) * (dw ? 2 : 1);
 }

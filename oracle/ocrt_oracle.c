@@ -23,6 +23,9 @@
 
 #include "../include/ocrt_gb300.h"
 
+int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                                  const ocrt_layers *layers, ocrt_result *out, ocrt_diag *diag);
+
 #define PI 3.14159265358979323846
 #define DEPOL 0.0279                  /* rt_solver.c:646 */
 #define Z_TOP_KM 100.0                /* rt_atm.c:219, 306 */
@@ -1122,12 +1125,52 @@ static int check_args(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
     return 0;
 }
 
+/* Per-layer overrides (no reference counterpart; the parameters of the
+ * adjoint).  Layer l (0-based) spans levels l..l+1.  dtau replaces the uniform
+ * optical-depth grid by h[k] = sum_{l<k} dtau[l]; ssa[l] rescales level l+1's
+ * scattering fractions (xdel, ydel) so that xdel + ydel = ssa[l], keeping the
+ * aerosol/molecular split of that layer.  The level altitudes, and with them
+ * the mixing fractions, stay those of the uniform grid; IPSS is not allowed
+ * with overrides (it would need the altitudes of the new grid). */
+static int apply_layers(medium_t *md, const ocrt_layers *ly, double mu0)
+{
+    const int nt = md->nt;
+    if (ly->n_layers != nt) return -1;
+    if (ly->dtau) {
+        double h = 0.0;
+        md->h[0] = 0.0;
+        for (int l = 0; l < nt; ++l) {
+            if (!(ly->dtau[l] > 0.0) || !isfinite(ly->dtau[l])) return -1;
+            h += ly->dtau[l];
+            md->h[l + 1] = h;
+        }
+        md->tau_total = h;
+        for (int k = 0; k <= nt; ++k) md->ch[k] = 0.5 * exp(-md->h[k] / mu0);
+    }
+    if (ly->ssa) {
+        for (int l = 0; l < nt; ++l) {
+            const double w = ly->ssa[l], w0 = md->xdel[l + 1] + md->ydel[l + 1];
+            if (!(w >= 0.0 && w <= 1.0) || !(w0 > 0.0)) return -1;
+            md->xdel[l + 1] *= w / w0;
+            md->ydel[l + 1] *= w / w0;
+        }
+    }
+    return 0;
+}
+
 int ocrt_oracle_solve_case(const ocrt_case *cs, const ocrt_opts *op,
                            const ocrt_aerosol *aer_in, ocrt_result *out, ocrt_diag *diag)
+{
+    return ocrt_oracle_solve_case_layers(cs, op, aer_in, NULL, out, diag);
+}
+
+int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                                  const ocrt_layers *layers, ocrt_result *out, ocrt_diag *diag)
 {
     int rc = check_args(cs, op, aer_in);
     if (rc) return rc;
     if (!out) return -1;
+    if (layers && op->pssa) return -5;
     memset(out, 0, sizeof(*out));
     const ocrt_aerosol *aer = (aer_in && aer_in->tau_a > 0.0) ? aer_in : NULL;
 
@@ -1171,7 +1214,8 @@ int ocrt_oracle_solve_case(const ocrt_case *cs, const ocrt_opts *op,
         rc = medium_build(&c->md, nt, tau_r, 0.0, 1.0, c->mu0, op->aer_h_km,
                           op->rayleigh_profile, op->rayleigh_h_km);
     }
-    if (rc) { free(c); return rc; }
+    if (!rc && layers) rc = apply_layers(&c->md, layers, c->mu0);
+    if (rc) { medium_free(&c->md); free(c); return rc; }
     if ((rc = transport_prepare(c))) goto done;
 
     int L = M > 2 ? M : 2;
