@@ -10,8 +10,8 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import (Aerosol, AerosolHolder, Case, Diag, Opts, Result, default_case, default_opts,
-                   result_dict, RESULT_FIELDS)
+from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Opts, Result, default_case,
+                   default_opts, result_dict, RESULT_FIELDS)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libocrt_gb300.so")
@@ -21,7 +21,7 @@ EXPORTS = [
     "ocrt_opts_default", "ocrt_case_default", "ocrt_gb_init", "ocrt_gb_shutdown", "ocrt_gb_last_error",
     "ocrt_gb_solve_case", "ocrt_gb_solve_batch", "ocrt_gb_plan_create", "ocrt_gb_plan_execute",
     "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy", "ocrt_gb_set_timing",
-    "ocrt_gb_plan_kernel_stats",
+    "ocrt_gb_plan_kernel_stats", "ocrt_gb_solve_case_noalloc", "ocrt_gb_solve_batch_adjoint",
 ]
 
 
@@ -56,6 +56,9 @@ def lib():
     L.ocrt_gb_plan_kernel_stats.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                             C.POINTER(C.c_longlong), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double)]
+    L.ocrt_gb_solve_batch_adjoint.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int,
+                                              C.POINTER(Aerosol), C.c_int, C.POINTER(Layers), C.c_int,
+                                              C.POINTER(C.c_double), C.POINTER(Result), C.POINTER(Grad), C.c_void_p]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
     _lib = L
@@ -114,6 +117,54 @@ def solve_batch(cases, opts, aerosols=None):
     out = (Result * n)()
     _check(L.ocrt_gb_solve_batch(n, ca, oa, opp, aa, app, out, None))
     return results_to_numpy(out)
+
+
+def solve_batch_adjoint(cases, opts, aerosols=None, layers=None, cot=None):
+    """Batched forward solve with per-layer parameters and gradients.
+
+    layers: None or a list (one per case) of LayersHolder / None.
+    cot: None (forward only) or an array [n, n_cot, 3] of cotangent rows for
+    (rho_I, rho_Q, rho_U); n_cot = 3 with identity rows gives the Jacobian.
+    Returns (results, grads) with grads a dict of arrays
+    d_dtau [n, n_cot, nt], d_ssa [n, n_cot, nt], d_wind [n, n_cot] (None if cot is None).
+    """
+    L = lib()
+    n, ca, oa, opp, aa, app = _arrays(cases, opts, aerosols)
+    la = None
+    if layers is not None:
+        structs = []
+        for i, ly in enumerate(layers):
+            nl = (opts[i] if isinstance(opts, (list, tuple)) else opts).n_layers
+            structs.append(ly.struct if ly is not None else Layers(n_layers=nl, dtau=None, ssa=None))
+        la = (Layers * n)(*structs)
+    out = (Result * n)()
+    if cot is None:
+        _check(L.ocrt_gb_solve_batch_adjoint(n, ca, oa, opp, aa, app, la, 0, None, out, None, None))
+        return results_to_numpy(out), None
+    cot = np.ascontiguousarray(np.asarray(cot, dtype=np.float64))
+    if cot.ndim != 3 or cot.shape[0] != n or cot.shape[2] != 3:
+        raise ValueError("cot must have shape [n, n_cot, 3]")
+    ncot = cot.shape[1]
+    nts = [(opts[i] if isinstance(opts, (list, tuple)) else opts).n_layers for i in range(n)]
+    ntm = max(nts)
+    d_dtau = np.zeros((n, ncot, ntm))
+    d_ssa = np.zeros((n, ncot, ntm))
+    bufs = []
+    ga = (Grad * (n * ncot))()
+    for i in range(n):
+        for r in range(ncot):
+            a, b = np.zeros(nts[i]), np.zeros(nts[i])
+            bufs.append((i, r, a, b))
+            ga[i * ncot + r].d_dtau = a.ctypes.data_as(C.POINTER(C.c_double))
+            ga[i * ncot + r].d_ssa = b.ctypes.data_as(C.POINTER(C.c_double))
+    _check(L.ocrt_gb_solve_batch_adjoint(n, ca, oa, opp, aa, app, la, ncot,
+                                         cot.ctypes.data_as(C.POINTER(C.c_double)), out, ga, None))
+    d_wind = np.zeros((n, ncot))
+    for i, r, a, b in bufs:
+        d_dtau[i, r, :nts[i]] = a
+        d_ssa[i, r, :nts[i]] = b
+        d_wind[i, r] = ga[i * ncot + r].d_wind
+    return results_to_numpy(out), {"d_dtau": d_dtau, "d_ssa": d_ssa, "d_wind": d_wind}
 
 
 def set_timing(enable):

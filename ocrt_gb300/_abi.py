@@ -84,6 +84,28 @@ class Diag(C.Structure):
     ]
 
 
+class Layers(C.Structure):
+    _fields_ = [("n_layers", C.c_int), ("dtau", C.POINTER(C.c_double)), ("ssa", C.POINTER(C.c_double))]
+
+
+class Grad(C.Structure):
+    _fields_ = [("d_dtau", C.POINTER(C.c_double)), ("d_ssa", C.POINTER(C.c_double)), ("d_wind", C.c_double)]
+
+
+class LayersHolder:
+    """Keeps per-layer override arrays alive while a Layers struct points into them."""
+
+    def __init__(self, n_layers, dtau=None, ssa=None):
+        import numpy as np
+        self.dtau = None if dtau is None else np.ascontiguousarray(np.asarray(dtau, dtype=np.float64))
+        self.ssa = None if ssa is None else np.ascontiguousarray(np.asarray(ssa, dtype=np.float64))
+        for a in (self.dtau, self.ssa):
+            if a is not None and a.shape != (n_layers,):
+                raise ValueError("per-layer array length differs from n_layers")
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+        self.struct = Layers(n_layers=int(n_layers), dtau=ptr(self.dtau), ssa=ptr(self.ssa))
+
+
 RESULT_FIELDS = [f for f, _ in Result._fields_]
 
 

@@ -1444,6 +1444,31 @@ done:
     return rc;
 }
 
+/* Profile values of the per-layer parameters (the defaults that ocrt_layers
+ * overrides): dtau[l] = h[l+1] - h[l], ssa[l] = xdel[l+1] + ydel[l+1]. */
+int ocrt_oracle_layer_defaults(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                               double *dtau, double *ssa)
+{
+    int rc = check_args(cs, op, aer_in);
+    if (rc) return rc;
+    const ocrt_aerosol *aer = (aer_in && aer_in->tau_a > 0.0) ? aer_in : NULL;
+    double tau_r;
+    if (!(cs->pressure_hpa > 0.0)) tau_r = 0.0;
+    else if (op->tau_r_source == OCRT_TAU_R_FROM_INPUT) tau_r = cs->tau_r_input;
+    else tau_r = ocrt_oracle_tau_rayleigh(cs->wavelength_nm, cs->pressure_hpa);
+    medium_t md;
+    const double mu0 = cos(cs->sza_deg * PI / 180.0);
+    rc = medium_build(&md, op->n_layers, tau_r, aer ? aer->tau_a : 0.0, aer ? aer->ssa_a : 1.0, mu0,
+                      op->aer_h_km, op->rayleigh_profile, op->rayleigh_h_km);
+    if (rc) return rc;
+    for (int l = 0; l < op->n_layers; ++l) {
+        if (dtau) dtau[l] = md.h[l + 1] - md.h[l];
+        if (ssa) ssa[l] = md.xdel[l + 1] + md.ydel[l + 1];
+    }
+    medium_free(&md);
+    return 0;
+}
+
 /* OpenMP pixel loop (the reference's batch pattern rt_io.c:197-199). */
 int ocrt_oracle_solve_batch(int n, const ocrt_case *cases, const ocrt_opts *opts, int opts_per_case,
                             const ocrt_aerosol *aer, int aer_per_case, ocrt_result *out,

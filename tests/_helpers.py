@@ -27,6 +27,35 @@ class Oracle:
             C.c_int, C.POINTER(A.Case), C.POINTER(A.Opts), C.c_int, C.POINTER(A.Aerosol), C.c_int,
             C.POINTER(A.Result), C.c_int]
 
+        self.lib.ocrt_oracle_solve_case_layers.argtypes = [
+            C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol), C.POINTER(A.Layers), C.POINTER(A.Result),
+            C.POINTER(A.Diag)]
+        self.lib.ocrt_oracle_layer_defaults.argtypes = [
+            C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol), C.POINTER(C.c_double),
+            C.POINTER(C.c_double)]
+
+    def layer_defaults(self, case, opts, aer=None):
+        n = opts.n_layers
+        dt, ss = np.zeros(n), np.zeros(n)
+        a = aer.struct if isinstance(aer, A.AerosolHolder) else aer
+        rc = self.lib.ocrt_oracle_layer_defaults(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
+                                                 dt.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 ss.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != 0:
+            raise RuntimeError(f"oracle rc {rc}")
+        return dt, ss
+
+    def solve_layers(self, case, opts, aer=None, dtau=None, ssa=None):
+        ly = A.LayersHolder(opts.n_layers, dtau, ssa)
+        r = A.Result()
+        a = aer.struct if isinstance(aer, A.AerosolHolder) else aer
+        rc = self.lib.ocrt_oracle_solve_case_layers(C.byref(case), C.byref(opts),
+                                                    C.byref(a) if a is not None else None,
+                                                    C.byref(ly.struct), C.byref(r), None)
+        if rc != 0:
+            raise RuntimeError(f"oracle rc {rc}")
+        return A.result_dict(r)
+
     def solve(self, case, opts, aer=None, diag=False):
         n = opts.fourier_m_max + 1
         arr = None
@@ -71,3 +100,35 @@ def assert_parity(got, ref, where="", i_rel=TOL_I_REL, qu_abs=TOL_QU_ABS):
     assert dQ <= qu_abs, f"{where}: rho_Q abs err {dQ:.3e} > {qu_abs}"
     assert dU <= qu_abs, f"{where}: rho_U abs err {dU:.3e} > {qu_abs}"
     return relI, dQ, dU
+
+
+def rho_vec(r):
+    return np.array([r["rho_I"], r["rho_Q"], r["rho_U"]])
+
+
+def fd_gradient(orc, case, opts, aer, dtau, ssa, cot, which, rel_step=1e-6):
+    """FP64 central finite differences of cot . (rho_I, rho_Q, rho_U) on the
+    oracle with a fixed order count.  which: list of ("dtau", l), ("ssa", l) or
+    ("wind", None); the step is rel_step times the parameter value."""
+    import copy
+    out = []
+
+    def f(kind, l, delta):
+        dt, ss, cs = dtau.copy(), ssa.copy(), copy.copy(case)
+        if kind == "dtau":
+            dt[l] += delta
+        elif kind == "ssa":
+            ss[l] += delta
+        else:
+            cs.wind_speed = case.wind_speed + delta
+        return float(np.dot(cot, rho_vec(orc.solve_layers(cs, opts, aer, dt, ss))))
+
+    for kind, l in which:
+        x = dtau[l] if kind == "dtau" else (ssa[l] if kind == "ssa" else case.wind_speed)
+        h = rel_step * x
+        if kind == "ssa" and x + h > 1.0:
+            # albedo at its upper bound: second-order one-sided difference
+            out.append((3.0 * f(kind, l, 0.0) - 4.0 * f(kind, l, -h) + f(kind, l, -2.0 * h)) / (2.0 * h))
+        else:
+            out.append((f(kind, l, h) - f(kind, l, -h)) / (2.0 * h))
+    return np.array(out)
