@@ -50,6 +50,30 @@ def workload(n_pix, seed=20261203 + 3):
     return cases, opts, aers
 
 
+ADJ_BANDS = (443.0, 555.0, 865.0)
+ADJ_LAYERS = 200
+
+
+def adjoint_workload(n_pix, seed=20261203 + 4):
+    """Configuration 4: n_pix geometries x 3 bands, 200 layers, the fixed
+    aerosol of configuration 2 (HG g=0.7 to L=120, SSA 0.95, AOD 0.1), rough
+    ocean at 5 m/s, plane-parallel (IPSS is not differentiated)."""
+    rng = np.random.default_rng(seed)
+    sza, vza, raa = rng.uniform(0, 70, n_pix), rng.uniform(0, 60, n_pix), rng.uniform(0, 180, n_pix)
+    mom = hg_aerosol_moments(0.7, L_AER)
+    aer = A.AerosolHolder(0.1, 0.95, *mom)
+    cases, aers = [], []
+    for i in range(n_pix):
+        for wl in ADJ_BANDS:
+            cases.append(A.default_case(surface="black_fresnel_ocean", sza_deg=sza[i], vza_deg=vza[i],
+                                        raa_deg=raa[i], wavelength_nm=wl, wind_speed=5.0,
+                                        tau_r_input=0.0945 * (wl / 555.0) ** -4.08))
+            aers.append(aer)
+    opts = A.default_opts(n_mu=N_MU, n_layers=ADJ_LAYERS, fourier_m_max=M_MAX, tau_r_source=A.TAU_R_FROM_INPUT,
+                          max_orders=1000, tolerance=1e-7)
+    return cases, opts, aers
+
+
 def config_dict(n_pix, world):
     return {"workload": f"configuration 3: batched forward, {n_pix} pixels/GPU, uneven layers 50-400, "
                         f"N={N_MU} streams, m<=32, aerosol L={L_AER}, rough Cox-Munk ocean",
@@ -300,6 +324,11 @@ def run_ours(args, rank, world):
     e2e = {"value": args.pixels * world / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
+    # ---- adjoint: full Jacobians (3 cotangent rows) per pixel-band ----
+    adj = None
+    if args.adj_pixels > 0:
+        adj = run_adjoint(args, og, torch, stream, sp, barrier, world)
+
     if rank != 0:
         return
     # ---- plain per-pixel GPU form (one solve call per pixel) ----
@@ -329,8 +358,59 @@ def run_ours(args, rank, world):
             "cpu_baseline": cpu, "rel_err_vs_fp64": err,
             "plain_per_pixel_gpu": {"value": plain, "unit": METRIC, "sample": f"{nplain} pixels, one "
                                     f"ocrt_gb_solve_case call each", "batched_speedup": value / world / plain},
-            "order_modes_per_step": om, "kernel_breakdown": breakdown}
+            "order_modes_per_step": om, "kernel_breakdown": breakdown, "adjoint": adj}
     print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args, og, torch, stream, sp, barrier, world):
+    """Configuration 4 on a resident plan: forward alone and forward + the
+    3-row Jacobian, K steps each timed with CUDA events on the launching
+    stream; Jacobians/s counts pixel-band Jacobians (3 outputs x 401 inputs)."""
+    cases, opts, aers = adjoint_workload(args.adj_pixels)
+    n = len(cases)
+    eye = np.broadcast_to(np.eye(3), (n, 3, 3)).copy()
+
+    def timed(plan):
+        for _ in range(args.warmup):
+            plan.execute(sp)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot, ks = 0.0, {}
+        for _ in range(args.steps):
+            e0.record(stream)
+            plan.execute(sp)
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+            for k, v in plan.kernel_stats().items():
+                ks[k] = ks.get(k, 0.0) + v["ms"]
+        ms = tot / args.steps
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, {k: v / args.steps for k, v in sorted(ks.items(), key=lambda kv: -kv[1]) if v > 0}
+
+    og.set_timing(True)
+    fwd = og.Plan(cases, opts, aers)
+    ms_fwd, _ = timed(fwd)
+    fwd.close()
+    jac = og.Plan(cases, opts, aers, cot=eye)
+    ms_jac, ks = timed(jac)
+    g = jac.gradients(sp)
+    jac.close()
+    og.set_timing(False)
+    finite = bool(np.isfinite(g["d_dtau"]).all() and np.isfinite(g["d_ssa"]).all() and np.isfinite(g["d_wind"]).all())
+    return {"metric": "adjoint Jacobians/s", "value": n * world / (ms_jac / 1e3), "unit": "Jacobians/s",
+            "ms_per_step": ms_jac, "forward_ms_per_step": ms_fwd,
+            "jacobian_cost_vs_forward": ms_jac / ms_fwd,
+            "workload": f"configuration 4: {args.adj_pixels} pixels x {len(ADJ_BANDS)} bands, {ADJ_LAYERS} layers, "
+                        f"N={N_MU}, m<=32, aerosol L={L_AER}, rough ocean 5 m/s, IPSS off; "
+                        f"Jacobian of TOA (I,Q,U) w.r.t. {ADJ_LAYERS} dtau + {ADJ_LAYERS} ssa + wind",
+            "pixel_bands": n, "gradients_finite": finite,
+            "fd_check": "tests/test_gpu_adjoint.py (FP64 central differences on the oracle)",
+            "kernel_ms_per_step": ks}
 
 
 def main():
@@ -343,6 +423,8 @@ def main():
     ap.add_argument("--plain-pixels", type=int, default=16)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--adj-pixels", type=int, default=1024,
+                    help="configuration-4 geometries (x3 bands) for the adjoint line; 0 skips it")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

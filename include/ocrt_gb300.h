@@ -232,11 +232,30 @@ typedef struct {
  * operators gives every parameter derivative in one pass per cotangent row.
  * Supported surfaces: BLACK and BLACK_FRESNEL_OCEAN with wind > 0; pssa = 0.
  * Otherwise OCRT_ERR_UNSUPPORTED. */
+/* Profile values of the per-layer parameters of one case, the values that a
+ * NULL ocrt_layers array stands for: dtau[l] = h_{l+1} - h_l and
+ * ssa[l] = the summed scattering fractions of level l+1 (rt_atm.c:177-400).
+ * Both arrays hold opts.n_layers entries (either may be NULL). */
+int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                           double *dtau, double *ssa);
+
 int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases,
                                 const ocrt_opts *opts, int opts_per_case,
                                 const ocrt_aerosol *aer, int aer_per_case,
                                 const ocrt_layers *layers, int n_cot, const double *cot,
                                 ocrt_result *out, ocrt_grad *grad, void *stream);
+
+/* Resident-plan form of the adjoint: a plan that carries layer parameters and
+ * n_cot cotangent rows per pixel.  ocrt_gb_plan_execute then runs the forward
+ * and the adjoint sweeps, ocrt_gb_plan_results gives the forward results and
+ * ocrt_gb_plan_gradients the gradients (layout as ocrt_gb_solve_batch_adjoint);
+ * ocrt_gb_plan_kernel_stats covers the adjoint kernels too. */
+int ocrt_gb_plan_create_adjoint(int n, const ocrt_case *cases,
+                                const ocrt_opts *opts, int opts_per_case,
+                                const ocrt_aerosol *aer, int aer_per_case,
+                                const ocrt_layers *layers, int n_cot, const double *cot,
+                                ocrt_plan **plan);
+int ocrt_gb_plan_gradients(ocrt_plan *plan, ocrt_grad *grad, void *stream);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,7 @@ EXPORTS = [
     "ocrt_gb_solve_case", "ocrt_gb_solve_batch", "ocrt_gb_plan_create", "ocrt_gb_plan_execute",
     "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy", "ocrt_gb_set_timing",
     "ocrt_gb_plan_kernel_stats", "ocrt_gb_solve_case_noalloc", "ocrt_gb_solve_batch_adjoint",
+    "ocrt_gb_layer_defaults", "ocrt_gb_plan_create_adjoint", "ocrt_gb_plan_gradients",
 ]
 
 
@@ -59,6 +60,12 @@ def lib():
     L.ocrt_gb_solve_batch_adjoint.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int,
                                               C.POINTER(Aerosol), C.c_int, C.POINTER(Layers), C.c_int,
                                               C.POINTER(C.c_double), C.POINTER(Result), C.POINTER(Grad), C.c_void_p]
+    L.ocrt_gb_plan_create_adjoint.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int,
+                                              C.POINTER(Aerosol), C.c_int, C.POINTER(Layers), C.c_int,
+                                              C.POINTER(C.c_double), C.POINTER(C.c_void_p)]
+    L.ocrt_gb_plan_gradients.argtypes = [C.c_void_p, C.POINTER(Grad), C.c_void_p]
+    L.ocrt_gb_layer_defaults.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
     _lib = L
@@ -119,6 +126,49 @@ def solve_batch(cases, opts, aerosols=None):
     return results_to_numpy(out)
 
 
+def layer_defaults(case, opts, aerosol=None):
+    """Profile values (dtau[nt], ssa[nt]) of the per-layer parameters of one case."""
+    L = lib()
+    n = opts.n_layers
+    dt, ss = np.zeros(n), np.zeros(n)
+    a = aerosol.struct if isinstance(aerosol, AerosolHolder) else aerosol
+    _check(L.ocrt_gb_layer_defaults(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
+                                    dt.ctypes.data_as(C.POINTER(C.c_double)),
+                                    ss.ctypes.data_as(C.POINTER(C.c_double))))
+    return dt, ss
+
+
+def _layers_array(n, opts, layers):
+    if layers is None:
+        return None
+    structs = []
+    for i, ly in enumerate(layers):
+        nl = (opts[i] if isinstance(opts, (list, tuple)) else opts).n_layers
+        structs.append(ly.struct if ly is not None else Layers(n_layers=nl, dtau=None, ssa=None))
+    return (Layers * n)(*structs)
+
+
+def _collect_grads(n, ncot, nts, call):
+    ntm = max(nts)
+    bufs = []
+    ga = (Grad * (n * ncot))()
+    for i in range(n):
+        for r in range(ncot):
+            a, b = np.zeros(nts[i]), np.zeros(nts[i])
+            bufs.append((i, r, a, b))
+            ga[i * ncot + r].d_dtau = a.ctypes.data_as(C.POINTER(C.c_double))
+            ga[i * ncot + r].d_ssa = b.ctypes.data_as(C.POINTER(C.c_double))
+    _check(call(ga))
+    d_dtau = np.zeros((n, ncot, ntm))
+    d_ssa = np.zeros((n, ncot, ntm))
+    d_wind = np.zeros((n, ncot))
+    for i, r, a, b in bufs:
+        d_dtau[i, r, :nts[i]] = a
+        d_ssa[i, r, :nts[i]] = b
+        d_wind[i, r] = ga[i * ncot + r].d_wind
+    return {"d_dtau": d_dtau, "d_ssa": d_ssa, "d_wind": d_wind}
+
+
 def solve_batch_adjoint(cases, opts, aerosols=None, layers=None, cot=None):
     """Batched forward solve with per-layer parameters and gradients.
 
@@ -130,13 +180,7 @@ def solve_batch_adjoint(cases, opts, aerosols=None, layers=None, cot=None):
     """
     L = lib()
     n, ca, oa, opp, aa, app = _arrays(cases, opts, aerosols)
-    la = None
-    if layers is not None:
-        structs = []
-        for i, ly in enumerate(layers):
-            nl = (opts[i] if isinstance(opts, (list, tuple)) else opts).n_layers
-            structs.append(ly.struct if ly is not None else Layers(n_layers=nl, dtau=None, ssa=None))
-        la = (Layers * n)(*structs)
+    la = _layers_array(n, opts, layers)
     out = (Result * n)()
     if cot is None:
         _check(L.ocrt_gb_solve_batch_adjoint(n, ca, oa, opp, aa, app, la, 0, None, out, None, None))
@@ -146,25 +190,11 @@ def solve_batch_adjoint(cases, opts, aerosols=None, layers=None, cot=None):
         raise ValueError("cot must have shape [n, n_cot, 3]")
     ncot = cot.shape[1]
     nts = [(opts[i] if isinstance(opts, (list, tuple)) else opts).n_layers for i in range(n)]
-    ntm = max(nts)
-    d_dtau = np.zeros((n, ncot, ntm))
-    d_ssa = np.zeros((n, ncot, ntm))
-    bufs = []
-    ga = (Grad * (n * ncot))()
-    for i in range(n):
-        for r in range(ncot):
-            a, b = np.zeros(nts[i]), np.zeros(nts[i])
-            bufs.append((i, r, a, b))
-            ga[i * ncot + r].d_dtau = a.ctypes.data_as(C.POINTER(C.c_double))
-            ga[i * ncot + r].d_ssa = b.ctypes.data_as(C.POINTER(C.c_double))
-    _check(L.ocrt_gb_solve_batch_adjoint(n, ca, oa, opp, aa, app, la, ncot,
-                                         cot.ctypes.data_as(C.POINTER(C.c_double)), out, ga, None))
-    d_wind = np.zeros((n, ncot))
-    for i, r, a, b in bufs:
-        d_dtau[i, r, :nts[i]] = a
-        d_ssa[i, r, :nts[i]] = b
-        d_wind[i, r] = ga[i * ncot + r].d_wind
-    return results_to_numpy(out), {"d_dtau": d_dtau, "d_ssa": d_ssa, "d_wind": d_wind}
+    cp = cot.ctypes.data_as(C.POINTER(C.c_double))
+    grads = _collect_grads(n, ncot, nts,
+                           lambda ga: L.ocrt_gb_solve_batch_adjoint(n, ca, oa, opp, aa, app, la, ncot, cp, out, ga,
+                                                                    None))
+    return results_to_numpy(out), grads
 
 
 def set_timing(enable):
@@ -181,13 +211,32 @@ def results_to_numpy(out):
 class Plan:
     """Device-resident batch: upload once, execute many times."""
 
-    def __init__(self, cases, opts, aerosols=None):
+    def __init__(self, cases, opts, aerosols=None, layers=None, cot=None):
         L = lib()
         self._keep = _arrays(cases, opts, aerosols)
         n, ca, oa, opp, aa, app = self._keep
         self.n = n
         self._h = C.c_void_p()
-        _check(L.ocrt_gb_plan_create(n, ca, oa, opp, aa, app, C.byref(self._h)))
+        self.ncot = 0
+        if layers is None and cot is None:
+            _check(L.ocrt_gb_plan_create(n, ca, oa, opp, aa, app, C.byref(self._h)))
+            return
+        la = _layers_array(n, opts, layers)
+        self._nts = [(opts[i] if isinstance(opts, (list, tuple)) else opts).n_layers for i in range(n)]
+        cp = None
+        if cot is not None:
+            self._cot = np.ascontiguousarray(np.asarray(cot, dtype=np.float64))
+            if self._cot.ndim != 3 or self._cot.shape[0] != n or self._cot.shape[2] != 3:
+                raise ValueError("cot must have shape [n, n_cot, 3]")
+            self.ncot = self._cot.shape[1]
+            cp = self._cot.ctypes.data_as(C.POINTER(C.c_double))
+        self._la = la
+        _check(L.ocrt_gb_plan_create_adjoint(n, ca, oa, opp, aa, app, la, self.ncot, cp, C.byref(self._h)))
+
+    def gradients(self, stream=None):
+        """d_dtau [n, n_cot, nt], d_ssa [n, n_cot, nt], d_wind [n, n_cot] of the last execute."""
+        return _collect_grads(self.n, self.ncot, self._nts,
+                              lambda ga: lib().ocrt_gb_plan_gradients(self._h, ga, stream))
 
     def execute(self, stream=None):
         _check(lib().ocrt_gb_plan_execute(self._h, stream))

@@ -154,6 +154,30 @@ __global__ void k_fill_all(BatchBufs B, int t0, int nw, int it)
     }
 }
 
+// Transposed operators for the tcgen05 adjoint source: opsT[tl][cin][kk] =
+// Aop[kk][cin] for kk < COUT, 0 up to KP = COUT rounded up to 32.  32 x 32
+// tiles through shared memory.  Grid (task, CIN/32 tiles, KP/32 tiles), 32 x 8.
+__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT)
+{
+    __shared__ float tile[32][33];
+    const int tl = blockIdx.x;
+    if (tl >= nw) return;
+    const TaskDev tk = tasks[t0 + tl];
+    const int KP = (G.COUT + 31) & ~31;
+    const int c0 = blockIdx.y * 32, r0 = blockIdx.z * 32;
+    const float *A = ops + tk.op_off;
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int row = r0 + yy, cin = c0 + threadIdx.x;
+        tile[yy][threadIdx.x] = (row < G.COUT && cin < G.CIN) ? A[(size_t)row * G.CIN + cin] : 0.f;
+    }
+    __syncthreads();
+    float *T = opsT + (size_t)tl * G.CIN * KP;
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        const int cin = c0 + yy, kk = r0 + threadIdx.x;
+        if (cin < G.CIN && kk < KP) T[(size_t)cin * KP + kk] = tile[threadIdx.x][yy];
+    }
+}
+
 // a_1 = e.  One thread per adjoint task.
 __global__ void k_adj_init(BatchBufs B, AdjBufs A, Geom G, int t0, int nadj)
 {
@@ -200,45 +224,87 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
     if (c < G.COUT) decode_col_a(G, c, s, h, g);
     const bool valid = c < G.COUT && g < d.n_ring;
     const size_t off = adj_off(tk, G, A.ncot, r);
-    const float *a = A.AF + off;
+    float *a = A.AF + off;
     double *At = A.ATot + off;
     float *mj = A.AJ + off;
     double mi = 0.0, mt = 0.0;
     if (valid) {
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+        // The view columns are outputs only (zero quadrature weight): the
+        // transposed source never writes them, so they are cleared here once read.
+        const bool clear = c >= G.CIN;
+        // Levels in chunks of PF: every load of a chunk is issued before the
+        // dependent recurrence runs.
+        constexpr int PF = 6;
         if (h == 0) {
             float nup = 0.f;
-            for (int k = 0; k <= nt; ++k) {
-                const size_t o = (size_t)k * G.LDC + c;
-                const float av = a[o];
-                const double t = At[o] + (double)av;
-                At[o] = t;
-                mi = fmax(mi, fabs((double)av));
-                mt = fmax(mt, fabs(t));
-                const float nu = k > 0 ? av + Tc[(k - 1) * NR + g] * nup : av;
-                float mu = k < nt ? Ca[k * NR + g] * nu : 0.f;
-                if (k > 0) mu += Cb[(k - 1) * NR + g] * nup;
-                mj[o] = mu;
-                nup = nu;
+            for (int k1 = 0; k1 <= nt; k1 += PF) {
+                const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
+                float av[PF], tv[PF], ca[PF], cb[PF];
+                double ov[PF];
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 + q;
+                        const size_t o = (size_t)k * G.LDC + c;
+                        av[q] = a[o]; ov[q] = At[o];
+                        tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
+                        ca[q] = k < nt ? Ca[k * NR + g] : 0.f;
+                        cb[q] = k > 0 ? Cb[(k - 1) * NR + g] : 0.f;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 + q;
+                        const size_t o = (size_t)k * G.LDC + c;
+                        const double t = ov[q] + (double)av[q];
+                        At[o] = t;
+                        if (clear) a[o] = 0.f;
+                        mi = fmax(mi, fabs((double)av[q]));
+                        mt = fmax(mt, fabs(t));
+                        const float nu = av[q] + tv[q] * nup;
+                        mj[o] = ca[q] * nu + cb[q] * nup;
+                        nup = nu;
+                    }
+                }
             }
             if (d.surf_on) A.bc[(size_t)ta * NR * 3 + g * 3 + s] = nup;
         } else {
             float nun = 0.f;
-            for (int k = nt; k >= 0; --k) {
-                const size_t o = (size_t)k * G.LDC + c;
-                float av = 0.f;
-                if (k > 0) {          // the TOA downward radiance is fixed at zero
-                    av = a[o];
-                    const double t = At[o] + (double)av;
-                    At[o] = t;
-                    mi = fmax(mi, fabs((double)av));
-                    mt = fmax(mt, fabs(t));
+            for (int k1 = nt; k1 >= 0; k1 -= PF) {
+                const int cnt = k1 + 1 < PF ? k1 + 1 : PF;
+                float av[PF], tv[PF], ca[PF], cb[PF];
+                double ov[PF];
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 - q;
+                        const size_t o = (size_t)k * G.LDC + c;
+                        av[q] = k > 0 ? a[o] : 0.f;          // the TOA downward radiance is fixed at zero
+                        ov[q] = k > 0 ? At[o] : 0.0;
+                        tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
+                        ca[q] = k > 0 ? Ca[(k - 1) * NR + g] : 0.f;
+                        cb[q] = k < nt ? Cb[k * NR + g] : 0.f;
+                    }
                 }
-                const float nu = k < nt ? av + Tc[k * NR + g] * nun : av;
-                float mu = k > 0 ? Ca[(k - 1) * NR + g] * nu : 0.f;
-                if (k < nt) mu += Cb[k * NR + g] * nun;
-                mj[o] = mu;
-                nun = nu;
+#pragma unroll
+                for (int q = 0; q < PF; ++q) {
+                    if (q < cnt) {
+                        const int k = k1 - q;
+                        const size_t o = (size_t)k * G.LDC + c;
+                        if (k > 0) {
+                            const double t = ov[q] + (double)av[q];
+                            At[o] = t;
+                            if (clear) a[o] = 0.f;
+                            mi = fmax(mi, fabs((double)av[q]));
+                            mt = fmax(mt, fabs(t));
+                        }
+                        const float nu = av[q] + tv[q] * nun;
+                        mj[o] = ca[q] * nu + cb[q] * nun;
+                        nun = nu;
+                    }
+                }
             }
         }
     }
@@ -409,68 +475,121 @@ __global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0
 
 // Final pass per adjoint task.  Pass 1 (thread per column) runs the
 // transposed transport over the adjoint total in FP64 and keeps nu in the
-// (now free) adjoint field buffer.  Pass 2 walks the levels in lock step and
-// forms, with the forward total field F_tot and total source
-// J_tot = S Xs + J_1:
+// (now free) adjoint field buffer.  Pass 2 gives each warp whole levels (lanes
+// over columns, coalesced rows) and forms, with the forward total field F_tot
+// and total source J_tot = S Xs + J_1:
 //   lev_ssa[k] = sum_c muJ[k][c] J_tot[k][c]            (x_k, y_k and J_1 scale with the albedo)
 //   lev_j1[k]  = sum_c muJ[k][c] J_1[k][c]              (J_1 ~ exp(-h_k/mu0))
 //   lay[l]     = sum_c nu . (F dT + J dCa + J dCb)_l    (layer-l transport coefficients)
 // plus, at the surface, mu_bc . dRsurf/dW . Xs_dn(BOA) and the seed terms.
 __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
 {
-    extern __shared__ double gsm[];          // lev_ssa[K], lev_j1[K], lay[K]
     __shared__ double red[32];
     const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
-    const int c = threadIdx.x, nt = d.nt, NR = G.NR, N = G.N, K = nt + 1;
-    double *lev_ssa = gsm, *lev_j1 = gsm + K, *lay = gsm + 2 * K;
-    for (int e = threadIdx.x; e < 3 * K; e += blockDim.x) gsm[e] = 0.0;
-    int s = 0, h = 0, g = 0;
-    if (c < G.COUT) decode_col_a(G, c, s, h, g);
-    const bool valid = c < G.COUT && g < d.n_ring;
+    const int nt = d.nt, NR = G.NR, N = G.N;
     const size_t off = adj_off(tk, G, A.ncot, r);
     float *nuv = A.AF + off;
     const double *At = A.ATot + off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const float *dT = A.dTc + d.coef_off, *dA = A.dCa + d.coef_off, *dB = A.dCb + d.coef_off;
-    double nub = 0.0;                         // nu at the BOA of an up column (mu_bc)
-    if (valid) {
-        if (h == 0) {
+    // ---- pass 1: nu = transposed transport of the adjoint total (FP64 recurrence)
+    double gW = 0.0, gS = 0.0;
+    {
+        const int c = threadIdx.x;
+        int s = 0, h = 0, g = 0;
+        if (c < G.COUT) decode_col_a(G, c, s, h, g);
+        const bool valid = c < G.COUT && g < d.n_ring;
+        constexpr int PF = 8;
+        if (valid && h == 0) {
             double nu = 0.0;
-            for (int k = 0; k <= nt; ++k) {
-                const size_t o = (size_t)k * G.LDC + c;
-                nu = k > 0 ? At[o] + (double)Tc[(k - 1) * NR + g] * nu : At[o];
-                nuv[o] = (float)nu;
+            for (int k1 = 0; k1 <= nt; k1 += PF) {
+                const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
+                double av[PF];
+                float tv[PF];
+#pragma unroll
+                for (int q = 0; q < PF; ++q)
+                    if (q < cnt) {
+                        const int k = k1 + q;
+                        av[q] = At[(size_t)k * G.LDC + c];
+                        tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
+                    }
+#pragma unroll
+                for (int q = 0; q < PF; ++q)
+                    if (q < cnt) {
+                        nu = av[q] + (double)tv[q] * nu;
+                        nuv[(size_t)(k1 + q) * G.LDC + c] = (float)nu;
+                    }
             }
-            nub = nu;
-        } else {
+            if (d.rough) {
+                // surface terms: wind derivative of the boundary operator and of
+                // the direct-beam seed, and the seed's optical-depth dependence
+                const float *Xs = W.F + tk.fld_off + (size_t)nt * G.LDC;
+                const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
+                const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
+                double acc = 0.0;
+                for (int i = 0; i < N; ++i) {
+                    const double pw = (float)(fw * B.gmu[i] * B.gw[i]);
+                    const float *Ri = RW + (size_t)i * 9;
+                    acc += pw * ((double)Ri[0] * Xs[col_of(G, 0, 1, i)] + (double)Ri[1] * Xs[col_of(G, 1, 1, i)] +
+                                 (double)Ri[2] * Xs[col_of(G, 2, 1, i)]);
+                }
+                const double tdn = exp(-d.tau_total / d.mu0);
+                const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
+                const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
+                const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
+                const double E = B.Eatt[(d.lev_off + nt) * NR + g];
+                gW = nu * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
+                gS = nu * fs * tdn * E * (double)Rs[g * 9 + s * 3];
+            }
+        } else if (valid) {
             double nu = 0.0;
-            for (int k = nt; k >= 1; --k) {
-                const size_t o = (size_t)k * G.LDC + c;
-                nu = k < nt ? At[o] + (double)Tc[k * NR + g] * nu : At[o];
-                nuv[o] = (float)nu;
+            for (int k1 = nt; k1 >= 1; k1 -= PF) {
+                const int cnt = k1 < PF ? k1 : PF;
+                double av[PF];
+                float tv[PF];
+#pragma unroll
+                for (int q = 0; q < PF; ++q)
+                    if (q < cnt) {
+                        const int k = k1 - q;
+                        av[q] = At[(size_t)k * G.LDC + c];
+                        tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
+                    }
+#pragma unroll
+                for (int q = 0; q < PF; ++q)
+                    if (q < cnt) {
+                        nu = av[q] + (double)tv[q] * nu;
+                        nuv[(size_t)(k1 - q) * G.LDC + c] = (float)nu;
+                    }
             }
             nuv[c] = 0.f;
         }
     }
+    gW = block_sum_a(gW, red);
     __syncthreads();
-    // pass 2: levels in lock step
+    gS = block_sum_a(gS, red);
+    __syncthreads();
+    // ---- pass 2: a warp per level, lanes over columns
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
-    const float faP = valid ? pv[c] : 0.f, fmP = valid ? pv[G.LDC + c] : 0.f;
     const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
     const float *Jx = W.J + tk.fld_off;
     const double *Tot = W.Tot + tk.fld_off;
-    float nu_p = 0.f, jt_p = 0.f;
-    double tot_p = 0.0;
-    const int lane = threadIdx.x & 31;
-    for (int k = 0; k <= nt; ++k) {
+    double *go = A.gout + (size_t)ta * A.gstride;
+    for (int k = warp; k <= nt; k += nwarp) {
+        const float xk = (float)xd[k], yk = (float)yd[k], chk = (float)ch[k];
+        const float xp = k > 0 ? (float)xd[k - 1] : 0.f, yp = k > 0 ? (float)yd[k - 1] : 0.f;
+        const float chp = k > 0 ? (float)ch[k - 1] : 0.f;
         float ssa_c = 0.f, j1_c = 0.f, lay_c = 0.f;
-        float nu_k = 0.f, jt_k = 0.f;
-        double tot_k = 0.0;
-        if (valid) {
+        for (int c = lane; c < G.COUT; c += 32) {
+            int s, h, g;
+            decode_col_a(G, c, s, h, g);
+            if (g >= d.n_ring) continue;
             const size_t o = (size_t)k * G.LDC + c;
-            nu_k = nuv[o];
+            const float faP = pv[c], fmP = pv[G.LDC + c];
+            const float nu_k = nuv[o];
+            const float nu_p = k > 0 ? nuv[o - G.LDC] : 0.f;
             const float nu_n = k < nt ? nuv[o + G.LDC] : 0.f;
             float mu;
             if (h == 0) {
@@ -480,63 +599,30 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
                 mu = k > 0 ? Ca[(k - 1) * NR + g] * nu_k : 0.f;
                 if (k < nt) mu += Cb[k * NR + g] * nu_n;
             }
-            const float x = (float)xd[k], y = (float)yd[k];
-            const float j1 = (float)ch[k] * (x * faP + y * fmP);
-            jt_k = Jx[o] + j1;
-            tot_k = Tot[o];
-            ssa_c = mu * jt_k;
-            j1_c = mu * j1;
+            const float j1 = chk * (xk * faP + yk * fmP);
+            const float jt = Jx[o] + j1;
+            ssa_c += mu * jt;
+            j1_c += mu * j1;
             if (k > 0) {
                 const int e = (k - 1) * NR + g;
+                const float jtp = Jx[o - G.LDC] + chp * (xp * faP + yp * fmP);
                 if (h == 0)
-                    lay_c = nu_p * ((float)tot_k * dT[e] + jt_p * dA[e] + jt_k * dB[e]);
+                    lay_c += nu_p * ((float)Tot[o] * dT[e] + jtp * dA[e] + jt * dB[e]);
                 else
-                    lay_c = nu_k * ((float)tot_p * dT[e] + jt_k * dA[e] + jt_p * dB[e]);
+                    lay_c += nu_k * ((float)Tot[o - G.LDC] * dT[e] + jt * dA[e] + jtp * dB[e]);
             }
         }
         ssa_c = warp_sum(ssa_c);
         j1_c = warp_sum(j1_c);
         lay_c = warp_sum(lay_c);
         if (lane == 0) {
-            atomicAdd(&lev_ssa[k], (double)ssa_c);
-            atomicAdd(&lev_j1[k], (double)j1_c);
-            if (k > 0) atomicAdd(&lay[k - 1], (double)lay_c);
+            go[k] = ssa_c;
+            go[A.kstride + k] = j1_c;
+            if (k > 0) go[2 * A.kstride + k - 1] = lay_c;
         }
-        nu_p = nu_k; jt_p = jt_k; tot_p = tot_k;
-    }
-    // surface terms (up columns): wind derivative of the boundary operator and
-    // of the direct-beam seed, and the seed's optical-depth dependence
-    double gW = 0.0, gS = 0.0;
-    if (valid && h == 0 && d.rough) {
-        const float *Xs = W.F + tk.fld_off + (size_t)nt * G.LDC;
-        const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
-        const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
-        double acc = 0.0;
-        for (int i = 0; i < N; ++i) {
-            const double pw = (float)(fw * B.gmu[i] * B.gw[i]);
-            const float *Ri = RW + (size_t)i * 9;
-            acc += pw * ((double)Ri[0] * Xs[col_of(G, 0, 1, i)] + (double)Ri[1] * Xs[col_of(G, 1, 1, i)] +
-                         (double)Ri[2] * Xs[col_of(G, 2, 1, i)]);
-        }
-        const double tdn = exp(-d.tau_total / d.mu0);
-        const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
-        const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
-        const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
-        const double E = B.Eatt[(d.lev_off + nt) * NR + g];
-        gW = nub * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
-        gS = nub * fs * tdn * E * (double)Rs[g * 9 + s * 3];
-    }
-    gW = block_sum_a(gW, red);
-    __syncthreads();
-    gS = block_sum_a(gS, red);
-    __syncthreads();
-    double *go = A.gout + (size_t)ta * A.gstride;
-    for (int e = threadIdx.x; e < K; e += blockDim.x) {
-        go[e] = lev_ssa[e];
-        go[A.kstride + e] = lev_j1[e];
-        go[2 * A.kstride + e] = e < nt ? lay[e] : 0.0;
     }
     if (threadIdx.x == 0) {
+        go[2 * A.kstride + nt] = 0.0;
         go[3 * A.kstride + 0] = gW;
         go[3 * A.kstride + 1] = gS;
     }

@@ -32,10 +32,11 @@ int *g_pinned = nullptr;
 int g_timing = 0;
 
 enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SOURCE_TC, KC_MOL, KC_SCAN, KC_EXTRACT,
-              KC_IPSS, KC_FINAL, KC_ADJ_SCAN, KC_ADJ_SOURCE, KC_ADJ_OTHER, KC_N };
+              KC_IPSS, KC_FINAL, KC_ADJ_SCAN, KC_ADJ_SOURCE, KC_ADJ_OTHER, KC_ADJ_TOTALS, KC_ADJ_GRAD, KC_N };
 const char *kc_names[KC_N] = {"setup", "phase_tables", "coxmunk_fourier", "primary", "source_gemm_simt",
                               "source_gemm_tcgen05", "source_molecular_lowrank", "transport_scan", "extract", "ipss",
-                              "finalize", "adjoint_scan", "adjoint_source", "adjoint_other"};
+                              "finalize", "adjoint_scan", "adjoint_source", "adjoint_other", "adjoint_forward_totals",
+                              "adjoint_gradients"};
 
 int fail(int rc, const std::string &msg)
 {
@@ -218,7 +219,10 @@ struct Group {
     float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJ = nullptr,
           *Abc = nullptr;
     TaskState *Ast = nullptr;
-    int *acnt = nullptr;
+    int *acnt = nullptr, *awork = nullptr;
+    float *opsT = nullptr;            // transposed operators for the tcgen05 adjoint source
+    bool use_tc_adj = false;
+    CUtensorMap mapAJ, mapOT;
     int gstride = 0, kstride = 0, grad_stride = 0;
 };
 
@@ -235,6 +239,7 @@ size_t wave_budget_bytes()
 
 struct ocrt_plan {
     int n = 0;
+    int ncot = 0;          // cotangent rows per pixel (adjoint plans)
     std::vector<Group> groups;
     long long launches = 0;
     double order_modes = 0;
@@ -269,7 +274,7 @@ void free_group(Group &g)
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
                     g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
-                    g.Abc, g.Ast, g.acnt};
+                    g.Abc, g.Ast, g.acnt, g.awork, g.opsT};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -367,7 +372,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
         size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
-            pb += (size_t)ncot * (pf * 16 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4;
+            pb += (size_t)ncot * (pf * 16 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
+                  nm * (size_t)G.CIN * ((G.COUT + 31) & ~31) * 4;
         if (q > w.p0 && bytes + pb > budget) {
             close(q);
             w = Wave{q, 0, d.task0, 0, 0, 0, 0, 0, false, false};
@@ -426,7 +432,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
             (rc = alloc(g.srfW, g.wave_srf)) || (rc = alloc(g.AF, g.wave_fld * ncot)) ||
             (rc = alloc(g.AJ, g.wave_fld * ncot)) || (rc = alloc(g.ATot, g.wave_fld * ncot)) ||
             (rc = alloc(g.Abc, na * G.NR * 3)) || (rc = alloc(g.Ast, na)) ||
-            (rc = alloc(g.acnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.gout, na * g.gstride)) ||
+            (rc = alloc(g.acnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.awork, (size_t)g.max_orders + 2)) ||
+            (rc = alloc(g.gout, na * g.gstride)) ||
             (rc = alloc(g.grad, (size_t)g.P * ncot * g.grad_stride)))
             return rc;
     }
@@ -438,6 +445,12 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     if (g.use_tc) {
         g.use_tc = make_map(&g.mapF, g.F, g.wave_fld / G.LDC, G.LDC, 128) &&
                    make_map(&g.mapA, g.ops, g.wave_ops / G.CIN, G.CIN, G.NP);
+    }
+    if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
+        const int KP = (G.COUT + 31) & ~31;
+        if ((rc = alloc(g.opsT, (size_t)g.wave_tasks * G.CIN * KP))) return rc;
+        g.use_tc_adj = make_map(&g.mapAJ, g.AJ, g.wave_fld * ncot / G.LDC, G.LDC, 128) &&
+                       make_map(&g.mapOT, g.opsT, (size_t)g.wave_tasks * G.CIN, KP, G.CIN);
     }
     for (Wave &w : g.waves) {
         w.n_simt = g.use_tc ? 0 : w.t1 - w.t0;
@@ -468,6 +481,7 @@ AdjBufs make_adj(Group &g)
     A.ncot = g.ncot; A.AF = g.AF; A.AJ = g.AJ; A.ATot = g.ATot; A.bc = g.Abc; A.st = g.Ast; A.acnt = g.acnt;
     A.cot = g.cot; A.gout = g.gout; A.gstride = g.gstride; A.kstride = g.kstride;
     A.dTc = g.dTc; A.dCa = g.dCa; A.dCb = g.dCb; A.srfW = g.srfW; A.grad = g.grad; A.grad_stride = g.grad_stride;
+    A.awork = g.awork;
     return A;
 }
 
@@ -480,14 +494,14 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     const int nw = w.t1 - w.t0, na = nw * g.ncot;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     // the scattered field Xs = F_tot - F_last and its source S Xs = J_tot - J_1
-    LAUNCH(plan, KC_ADJ_OTHER, k_adj_prep<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+    LAUNCH(plan, KC_ADJ_TOTALS, k_adj_prep<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
     const int it = g.max_orders + 1;
-    LAUNCH(plan, KC_ADJ_OTHER, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
-    if (w.n_simt) LAUNCH(plan, KC_ADJ_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
+    LAUNCH(plan, KC_ADJ_TOTALS, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
+    if (w.n_simt) LAUNCH(plan, KC_ADJ_TOTALS, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
     if (w.n_tc)
-        LAUNCH(plan, KC_ADJ_SOURCE, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(g.mapF, g.mapA, B, W, G, w.t0, it, mtiles));
+        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(g.mapF, g.mapA, B, W, G, w.t0, it, mtiles));
     if (w.n_mol)
-        LAUNCH(plan, KC_ADJ_SOURCE, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
+        LAUNCH(plan, KC_ADJ_TOTALS, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                    B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
     // adjoint successive orders
     CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
@@ -495,6 +509,12 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     CK(cudaMemsetAsync(g.ATot, 0, sizeof(double) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+    CK(cudaMemsetAsync(g.awork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+    const int KP = (G.COUT + 31) & ~31;
+    const int amt = (g.ncot * w.Kmax + 127) / 128;
+    if (g.use_tc_adj)
+        LAUNCH(plan, KC_ADJ_OTHER, k_op_transpose<<<dim3(nw, (G.CIN + 31) / 32, KP / 32), dim3(32, 8), 0, st>>>(
+                   g.tasks, w.t0, nw, G, g.ops, g.opsT));
     const AdjBufs A = make_adj(g);
     LAUNCH(plan, KC_ADJ_OTHER, k_adj_init<<<(na + 127) / 128, 128, 0, st>>>(B, A, G, w.t0, na));
     const dim3 agrid(na, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.LDC + ST_N_TILE - 1) / ST_N_TILE);
@@ -506,16 +526,20 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
             CK(cudaStreamSynchronize(st));
             if (*g_pinned == 0) break;
         }
-        LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source<<<agrid, 256, 0, st>>>(B, W, A, G, w.t0));
+        if (g.use_tc_adj)
+            LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source_tc<<<std::min(nw * amt, g_nsm), 256, tc_adj_smem_bytes(G), st>>>(
+                       g.mapAJ, g.mapOT, B, W, A, G, w.t0, j, amt, nw));
+        else
+            LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source<<<agrid, 256, 0, st>>>(B, W, A, G, w.t0));
         if (w.n_mol)
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_mol<<<dim3(na, ltiles), 256, adj_mol_smem_bytes(G), st>>>(
                        B, W, A, G, w.t0, g.Bp, g.Br, g.Bt, g.Lmax));
         if (w.any_rough)
             LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<na, surf_threads, 0, st>>>(B, W, A, G, w.t0));
     }
-    LAUNCH(plan, KC_ADJ_OTHER, k_adj_grad<<<na, scan_threads, sizeof(double) * 3 * (size_t)w.Kmax, st>>>(
+    LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<na, scan_threads, 0, st>>>(
                B, W, A, G, w.t0));
-    LAUNCH(plan, KC_ADJ_OTHER, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
+    LAUNCH(plan, KC_ADJ_GRAD, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
                B, W, A, G, w.p0, w.t0));
     return OCRT_OK;
 }
@@ -652,6 +676,7 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_adj_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     g_device = device;
     return OCRT_OK;
 }
@@ -875,40 +900,59 @@ int ocrt_gb_solve_batch(int n, const ocrt_case *cases, const ocrt_opts *opts, in
     return rc;
 }
 
+int ocrt_gb_plan_create_adjoint(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
+                                const ocrt_aerosol *aer, int app, const ocrt_layers *layers, int n_cot,
+                                const double *cot, ocrt_plan **out)
+{
+    if (!out) return fail(OCRT_ERR_ARGS, "null plan pointer");
+    *out = nullptr;
+    if (n_cot < 0 || n_cot > 3) return fail(OCRT_ERR_ARGS, "n_cot outside [0, 3]");
+    if (n_cot > 0 && !cot) return fail(OCRT_ERR_ARGS, "null cotangent array");
+    const int rc = plan_create_impl(n, cases, opts, opp, aer, app, layers, n_cot, cot, out);
+    if (!rc) (*out)->ncot = n_cot;
+    return rc;
+}
+
+int ocrt_gb_plan_gradients(ocrt_plan *plan, ocrt_grad *grad, void *stream)
+{
+    if (!plan) return fail(OCRT_ERR_ARGS, "null plan");
+    if (plan->ncot == 0) return fail(OCRT_ERR_ARGS, "plan has no cotangent rows");
+    if (!grad) return fail(OCRT_ERR_ARGS, "null gradient array");
+    const int n_cot = plan->ncot;
+    for (int i = 0; i < plan->n * n_cot; ++i)
+        if (!grad[i].d_dtau || !grad[i].d_ssa) return fail(OCRT_ERR_ARGS, "null gradient array");
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
+    for (Group &g : plan->groups) {
+        std::vector<double> h((size_t)g.P * n_cot * g.grad_stride);
+        CK(cudaMemcpyAsync(h.data(), g.grad, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int q = 0; q < g.P; ++q) {
+            const int i = g.idx[q], nt = g.hpx[q].nt;
+            for (int r = 0; r < n_cot; ++r) {
+                const double *src = h.data() + ((size_t)q * n_cot + r) * g.grad_stride;
+                ocrt_grad &gr = grad[(size_t)i * n_cot + r];
+                for (int l = 0; l < nt; ++l) { gr.d_dtau[l] = src[l]; gr.d_ssa[l] = src[nt + l]; }
+                gr.d_wind = src[2 * nt];
+            }
+        }
+    }
+    return OCRT_OK;
+}
+
 int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
                                 const ocrt_aerosol *aer, int app, const ocrt_layers *layers, int n_cot,
                                 const double *cot, ocrt_result *out, ocrt_grad *grad, void *stream)
 {
     if (n == 0) return OCRT_OK;
     if (!out) return fail(OCRT_ERR_ARGS, "null output");
-    if (n_cot < 0 || n_cot > 3) return fail(OCRT_ERR_ARGS, "n_cot outside [0, 3]");
-    if (n_cot > 0 && (!cot || !grad)) return fail(OCRT_ERR_ARGS, "null cotangent or gradient array");
-    if (n_cot > 0)
-        for (int i = 0; i < n * n_cot; ++i)
-            if (!grad[i].d_dtau || !grad[i].d_ssa) return fail(OCRT_ERR_ARGS, "null gradient array");
+    if (n_cot > 0 && !grad) return fail(OCRT_ERR_ARGS, "null gradient array");
     ocrt_plan *plan = nullptr;
-    int rc = plan_create_impl(n, cases, opts, opp, aer, app, layers, n_cot, cot, &plan);
+    int rc = ocrt_gb_plan_create_adjoint(n, cases, opts, opp, aer, app, layers, n_cot, cot, &plan);
     if (rc) return rc;
     rc = ocrt_gb_plan_execute(plan, stream);
     if (!rc) rc = ocrt_gb_plan_results(plan, out, stream);
-    if (!rc && n_cot > 0) {
-        std::lock_guard<std::mutex> lk(g_mu);
-        cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
-        for (Group &g : plan->groups) {
-            std::vector<double> h((size_t)g.P * n_cot * g.grad_stride);
-            if (cudaMemcpyAsync(h.data(), g.grad, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-                cudaStreamSynchronize(st) != cudaSuccess) { rc = fail(OCRT_ERR_DEVICE, "gradient copy failed"); break; }
-            for (int q = 0; q < g.P; ++q) {
-                const int i = g.idx[q], nt = g.hpx[q].nt;
-                for (int r = 0; r < n_cot; ++r) {
-                    const double *src = h.data() + ((size_t)q * n_cot + r) * g.grad_stride;
-                    ocrt_grad &gr = grad[(size_t)i * n_cot + r];
-                    for (int l = 0; l < nt; ++l) { gr.d_dtau[l] = src[l]; gr.d_ssa[l] = src[nt + l]; }
-                    gr.d_wind = src[2 * nt];
-                }
-            }
-        }
-    }
+    if (!rc && n_cot > 0) rc = ocrt_gb_plan_gradients(plan, grad, stream);
     ocrt_gb_plan_destroy(plan);
     return rc;
 }
@@ -940,6 +984,40 @@ int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_ae
                 if (diag->view_Q_m) diag->view_Q_m[m] = to[m].vQ;
                 if (diag->view_U_m) diag->view_U_m[m] = to[m].vU;
             }
+    }
+    ocrt_gb_plan_destroy(plan);
+    return rc;
+}
+
+int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                           double *dtau, double *ssa)
+{
+    if (!cs || !opts) return fail(OCRT_ERR_ARGS, "null case or options");
+    ocrt_plan *plan = nullptr;
+    int rc = ocrt_gb_plan_create(1, cs, opts, 0, aer, 0, &plan);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        Group &g = plan->groups[0];
+        cudaStream_t st = g_stream;
+        const int nt = g.hpx[0].nt;
+        std::vector<double> h(nt + 1), x(nt + 1), y(nt + 1);
+        k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw);
+        k_pixel_setup<<<1, 128, 0, st>>>(g.px, 1, g.N, g.gmu);
+        k_levels<<<dim3(2, 1), 256, 0, st>>>(g.px, 1, g.h, g.ch, g.xd, g.yd, g.z);
+        k_level_mix<<<dim3(2, 1), 256, 0, st>>>(g.px, 1, g.z, g.xd, g.yd);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(h.data(), g.h, sizeof(double) * (nt + 1), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(x.data(), g.xd, sizeof(double) * (nt + 1), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(y.data(), g.yd, sizeof(double) * (nt + 1), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            rc = fail(OCRT_ERR_DEVICE, "level setup failed");
+        } else {
+            for (int l = 0; l < nt; ++l) {
+                if (dtau) dtau[l] = h[l + 1] - h[l];
+                if (ssa) ssa[l] = x[l + 1] + y[l + 1];
+            }
+        }
     }
     ocrt_gb_plan_destroy(plan);
     return rc;

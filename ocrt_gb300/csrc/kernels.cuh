@@ -68,6 +68,7 @@ struct AdjBufs {
     float *bc;             // mu_bc per adjoint task [NR][3]
     TaskState *st;         // per adjoint task
     int *acnt;             // [max_orders + 2] adjoint tasks still active after order j
+    int *awork;            // [max_orders + 2] work counters of the persistent transposed source
     const double *cot;     // [P][ncot][3]
     double *gout;          // per adjoint task partials, gstride doubles (3 arrays of kstride + 2 scalars)
     int gstride, kstride;
@@ -94,9 +95,14 @@ __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
 __global__ void k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
                             BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
+__global__ void k_adj_source_tc(const __grid_constant__ CUtensorMap mapJ, const __grid_constant__ CUtensorMap mapAT,
+                                BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
+__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
 size_t coxmunk_smem_bytes(int nphi, bool dw);
 size_t tc_smem_bytes(const Geom &G);
 bool tc_supported(const Geom &G);
+size_t tc_adj_smem_bytes(const Geom &G);
+bool tc_adj_supported(const Geom &G);
 __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 __global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int ltiles,
                               const float *Bp, const float *Br, const float *Bt, int L);

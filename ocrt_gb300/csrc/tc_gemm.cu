@@ -145,28 +145,39 @@ __device__ __forceinline__ void split_tf32(uint32_t *hi, uint32_t *lo, int n)
     }
 }
 
-// Persistent form: a grid of about one CTA per SM pulls (active task, 128-level
-// tile) items from a per-order counter.  TMEM and the barriers are set up once
-// per CTA; K tiles are numbered globally across the CTA's items (stage g & 1,
-// use g >> 1), so thread 0 streams the next item's first two tiles in while the
+// Persistent form: a grid of about one CTA per SM pulls (task, 128-row tile)
+// items from a per-order counter.  TMEM and the barriers are set up once per
+// CTA; K tiles are numbered globally across the CTA's items (stage g & 1, use
+// g >> 1), so thread 0 streams the next item's first two tiles in while the
 // current item's epilogue drains TMEM.
-__global__ void __launch_bounds__(TC_THREADS, 1)
-k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
-            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles)
+//
+// ADJ = false: forward source.  Rows = levels of one task's field F (map over
+//   the wave's F), B operand = the task's operator Aop [NP][CIN], K = CIN,
+//   epilogue J[k][c] = x_k D[k][c] for c < COUT; items = active list x tiles.
+// ADJ = true: transposed source of the adjoint.  Rows = the ncot adjoint
+//   fields of one task stacked (ncot * K rows of muJ), B operand = the task's
+//   transposed operator AopT [CIN][KP] (KP = COUT rounded up to 32), K = KP,
+//   epilogue a[row][cin] = x_k D[row][cin] for cin < CIN; items = every task of
+//   the wave x tiles, skipped when none of the task's rows is still active.
+template <bool ADJ>
+__device__ __forceinline__ void source_tc_body(const CUtensorMap *mapF, const CUtensorMap *mapA, const BatchBufs &B,
+                                               const WaveBufs &W, const AdjBufs &AB, const Geom &G, int t0, int it,
+                                               int mtiles, int nw)
 {
     extern __shared__ unsigned char smem_raw[];
-    const int NP = G.NP;
-    const uint32_t A_BYTES = TC_M * TC_KT * 4, B_BYTES = (uint32_t)NP * TC_KT * 4;
+    const int NB = ADJ ? G.CIN : G.NP;                  // MMA N (B operand rows)
+    const int NKT = ADJ ? ((G.COUT + TC_KT - 1) / TC_KT) : G.CIN / TC_KT;
+    const uint32_t A_BYTES = TC_M * TC_KT * 4, B_BYTES = (uint32_t)NB * TC_KT * 4;
     const uint32_t STAGE = 2 * A_BYTES + 2 * B_BYTES;
     unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(base + 2 * STAGE);     // full[2], empty[2], done
     uint32_t *tslot = (uint32_t *)(bars + 5);
     int *abort_flag = (int *)(tslot + 1);
-    int *slot = abort_flag + 1;                          // item ring [2]: task-list index * mtiles + tile, or -1
+    int *slot = abort_flag + 1;                          // item ring [2]: task index * mtiles + tile, or -1
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int n_items = B.active_cnt[it - 1] * mtiles;
-    const int *alist = B.alist[it & 1];
-    int *counter = &B.work[it * 4 + 0];
+    const int n_items = (ADJ ? nw : B.active_cnt[it - 1]) * mtiles;
+    const int *alist = ADJ ? nullptr : B.alist[it & 1];
+    int *counter = ADJ ? &AB.awork[it] : &B.work[it * 4 + 0];
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
@@ -175,28 +186,37 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     uint64_t *full = bars, *empty = bars + 2, *done = bars + 4;
-    const int NKT = G.CIN / TC_KT;
 
-    // Thread 0 only: next valid item (k0 <= nt) from the shared counter, or -1.
+    auto task_of = [&](int li) -> int { return ADJ ? li : alist[li]; };
+    // Thread 0 only: next item with work, or -1.
     auto fetch = [&]() -> int {
         for (;;) {
             const int item = atomicAdd(counter, 1);
             if (item >= n_items) return -1;
             const int li = item / mtiles, mt = item - li * mtiles;
-            const TaskDev tk = B.tasks[t0 + alist[li]];
-            if (mt * TC_M <= B.px[tk.pix].nt) return item;
+            const int tl = task_of(li);
+            const TaskDev tk = B.tasks[t0 + tl];
+            if (ADJ) {
+                if (mt * TC_M >= AB.ncot * tk.K) continue;
+                bool any = false;
+                for (int r = 0; r < AB.ncot; ++r) any |= AB.st[tl * AB.ncot + r].active != 0;
+                if (any) return item;
+            } else if (mt * TC_M <= B.px[tk.pix].nt) {
+                return item;
+            }
         }
     };
     // Thread 0 only: TMA loads of K tile kt of `item` into stage s.
     auto issue = [&](int item, int kt, int s) {
         const int li = item / mtiles, mt = item - li * mtiles;
-        const TaskDev tk = B.tasks[t0 + alist[li]];
-        const int rowF = (int)(tk.fld_off / G.LDC) + mt * TC_M;
-        const int rowA = (int)(tk.op_off / G.CIN);
+        const int tl = task_of(li);
+        const TaskDev tk = B.tasks[t0 + tl];
+        const int rowF = ADJ ? (int)(tk.fld_off * AB.ncot / G.LDC) + mt * TC_M : (int)(tk.fld_off / G.LDC) + mt * TC_M;
+        const int rowA = ADJ ? tl * G.CIN : (int)(tk.op_off / G.CIN);
         unsigned char *sp = base + (size_t)s * STAGE;
         mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-        tma_load_2d(sp, &mapF, &full[s], kt * TC_KT, rowF);
-        tma_load_2d(sp + 2 * A_BYTES, &mapA, &full[s], kt * TC_KT, rowA);
+        tma_load_2d(sp, mapF, &full[s], kt * TC_KT, rowF);
+        tma_load_2d(sp + 2 * A_BYTES, mapA, &full[s], kt * TC_KT, rowA);
     };
 
     int inflight[2] = {0, 0};          // thread 0: stage holds an unconsumed load
@@ -219,7 +239,7 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
     const uint32_t tmem = *tslot;
 
     constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
-    const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(NP >> 3) << 17);
+    const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(NB >> 3) << 17);
     uint32_t g = 0;                    // global K-tile sequence number of this CTA
     uint32_t ph_done = 0;
     bool ok = true, done_pending = false;
@@ -228,7 +248,7 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
         const int item = slot[j & 1];
         if (item < 0) break;
         const int li = item / mtiles, mt = item - li * mtiles;
-        const TaskDev tk = B.tasks[t0 + alist[li]];
+        const TaskDev tk = B.tasks[t0 + task_of(li)];
         const PixDev &d = B.px[tk.pix];
         const int nt = d.nt, k0 = mt * TC_M;
         for (int kt = 0; kt < NKT; ++kt, ++g) {
@@ -242,7 +262,7 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
             uint32_t *ahi = (uint32_t *)sp, *alo = (uint32_t *)(sp + A_BYTES);
             uint32_t *bhi = (uint32_t *)(sp + 2 * A_BYTES), *blo = (uint32_t *)(sp + 2 * A_BYTES + B_BYTES);
             split_tf32(ahi, alo, TC_M * TC_KT);
-            split_tf32(bhi, blo, NP * TC_KT);
+            split_tf32(bhi, blo, NB * TC_KT);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
             if (tid == 0) {
@@ -287,20 +307,34 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
         __syncthreads();
         if (*abort_flag) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (one level each);
+        // Epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (one row each);
         // warps 0-3 take the even 16-column chunks, warps 4-7 the odd ones.
         const int lane = tid & 31, q = warp & 3, half = warp >> 2;
-        const int k = k0 + q * 32 + lane;
-        const float x = k <= nt ? (float)B.xd[d.lev_off + k] : 0.f;
-        float *Jrow = W.J + tk.fld_off + (size_t)k * G.LDC;
-        for (int cb = half; cb < NP / 16; cb += 2) {
+        const int row = k0 + q * 32 + lane;
+        int k;
+        bool live;
+        float *out;
+        int ncols;
+        if (ADJ) {
+            live = row < AB.ncot * tk.K;
+            k = live ? row % tk.K : 0;
+            out = AB.AF + (size_t)tk.fld_off * AB.ncot + (size_t)row * G.LDC;
+            ncols = G.CIN;
+        } else {
+            live = row <= nt;
+            k = row;
+            out = W.J + tk.fld_off + (size_t)row * G.LDC;
+            ncols = G.COUT;
+        }
+        const float x = live ? (float)B.xd[d.lev_off + k] : 0.f;
+        for (int cb = half; cb < NB / 16; cb += 2) {
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cb * 16), v);
-            if (k <= nt) {
+            if (live) {
 #pragma unroll
                 for (int jj = 0; jj < 16; ++jj) {
                     const int c = cb * 16 + jj;
-                    if (c < G.COUT) Jrow[c] = x * v[jj];
+                    if (c < ncols) out[c] = x * v[jj];
                 }
             }
         }
@@ -324,9 +358,36 @@ k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CU
     }
 }
 
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
+            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles)
+{
+    AdjBufs none{};
+    source_tc_body<false>(&mapF, &mapA, B, W, none, G, t0, it, mtiles, 0);
+}
+
+// Transposed contraction of the adjoint for adjoint order `it` (work counter
+// AB.awork[it]).
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_adj_source_tc(const __grid_constant__ CUtensorMap mapJ, const __grid_constant__ CUtensorMap mapAT,
+                BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw)
+{
+    source_tc_body<true>(&mapJ, &mapAT, B, W, AB, G, t0, it, mtiles, nw);
+}
+
 size_t tc_smem_bytes(const Geom &G)
 {
     return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)G.NP * TC_KT * 4) + 128;
+}
+
+size_t tc_adj_smem_bytes(const Geom &G)
+{
+    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)G.CIN * TC_KT * 4) + 128;
+}
+
+bool tc_adj_supported(const Geom &G)
+{
+    return (G.CIN % 16) == 0 && G.CIN <= 256 && tc_adj_smem_bytes(G) <= 227 * 1024;
 }
 
 bool tc_supported(const Geom &G)

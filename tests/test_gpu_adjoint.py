@@ -142,3 +142,35 @@ def test_adjoint_rejects_unsupported(gpu):
     with pytest.raises(gpu.OcrtError) as e:
         gpu.solve_batch_adjoint([c], o, None, None, np.ones((1, 1, 3)))
     assert e.value.rc == A.OCRT_ERR_UNSUPPORTED
+
+
+def test_torch_autograd_function(gpu, oracle):
+    """sos_reflectance under torch.autograd: backward equals the library's
+    adjoint for the same cotangent, and the oracle's FP64 finite differences."""
+    torch = pytest.importorskip("torch")
+    from ocrt_gb300 import _abi as A
+    from ocrt_gb300.autograd import layer_parameters, sos_reflectance
+    from synthetic import hg_aerosol_moments
+    cs = [_case(A, sza_deg=35.0, vza_deg=40.0, raa_deg=100.0, wind=6.0),
+          _case(A, sza_deg=55.0, vza_deg=20.0, raa_deg=10.0, wind=2.5)]
+    o = A.default_opts(n_mu=16, n_layers=8, fourier_m_max=4, max_orders=400, tolerance=1e-9)
+    aers = [A.AerosolHolder(0.12, 0.93, *hg_aerosol_moments(0.7, 24)) for _ in cs]
+    dt, ss, w = layer_parameters(cs, o, aers)
+    # the library's defaults equal the oracle's profile values
+    dto, sso = oracle.layer_defaults(cs[0], o, aers[0])
+    np.testing.assert_allclose(dt[0].numpy(), dto, rtol=1e-12)
+    np.testing.assert_allclose(ss[0].numpy(), sso, rtol=1e-12)
+    dt.requires_grad_(True); ss.requires_grad_(True); w.requires_grad_(True)
+    rho = sos_reflectance(dt, ss, w, cs, o, aers)
+    wts = torch.tensor([[1.0, 0.5, -0.25], [0.2, -1.0, 0.4]], dtype=torch.float64)
+    (rho * wts).sum().backward()
+    _, g = gpu.solve_batch_adjoint(cs, o, aers, None, wts.numpy()[:, None, :])
+    np.testing.assert_allclose(dt.grad.numpy(), g["d_dtau"][:, 0], rtol=1e-5, atol=1e-10)
+    np.testing.assert_allclose(ss.grad.numpy(), g["d_ssa"][:, 0], rtol=1e-5, atol=1e-10)
+    np.testing.assert_allclose(w.grad.numpy(), g["d_wind"][:, 0], rtol=1e-5, atol=1e-12)
+    o_fd = A.default_opts(n_mu=16, n_layers=8, fourier_m_max=4, max_orders=200, tolerance=1e-300)
+    fd_t, fd_s, fd_w = _fd_all(oracle, cs[1], o_fd, aers[1], dto * 0 + dt[1].detach().numpy(),
+                               ss[1].detach().numpy(), wts[1].numpy(), True)
+    _check_grad(dt.grad[1].numpy(), fd_t, "torch d/ddtau")
+    _check_grad(ss.grad[1].numpy(), fd_s, "torch d/dssa")
+    _check_grad(w.grad[1].item(), fd_w, "torch d/dwind")
