@@ -160,7 +160,9 @@ def traffic_from_profiles(kernel):
 
 
 def oracle_lib():
-    so = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+    """The CPU restatement compiled with the reference's floating-point flags
+    (liboracle_fast.so), the timed port baseline."""
+    so = os.path.join(ROOT, "oracle", "_build", "liboracle_fast.so")
     if not os.path.exists(so):
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
     lib = C.CDLL(so)

@@ -577,39 +577,59 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
     const float *Jx = W.J + tk.fld_off;
     const double *Tot = W.Tot + tk.fld_off;
     double *go = A.gout + (size_t)ta * A.gstride;
+    // Each lane takes CU columns per pass (32 * CU apart) and issues all their
+    // loads before the arithmetic, so a warp keeps many row loads in flight.
+    constexpr int CU = 4;
     for (int k = warp; k <= nt; k += nwarp) {
         const float xk = (float)xd[k], yk = (float)yd[k], chk = (float)ch[k];
         const float xp = k > 0 ? (float)xd[k - 1] : 0.f, yp = k > 0 ? (float)yd[k - 1] : 0.f;
         const float chp = k > 0 ? (float)ch[k - 1] : 0.f;
         float ssa_c = 0.f, j1_c = 0.f, lay_c = 0.f;
-        for (int c = lane; c < G.COUT; c += 32) {
-            int s, h, g;
-            decode_col_a(G, c, s, h, g);
-            if (g >= d.n_ring) continue;
-            const size_t o = (size_t)k * G.LDC + c;
-            const float faP = pv[c], fmP = pv[G.LDC + c];
-            const float nu_k = nuv[o];
-            const float nu_p = k > 0 ? nuv[o - G.LDC] : 0.f;
-            const float nu_n = k < nt ? nuv[o + G.LDC] : 0.f;
-            float mu;
-            if (h == 0) {
-                mu = k < nt ? Ca[k * NR + g] * nu_k : 0.f;
-                if (k > 0) mu += Cb[(k - 1) * NR + g] * nu_p;
-            } else {
-                mu = k > 0 ? Ca[(k - 1) * NR + g] * nu_k : 0.f;
-                if (k < nt) mu += Cb[k * NR + g] * nu_n;
+        for (int c0 = lane; c0 < G.COUT; c0 += 32 * CU) {
+            float nu_k[CU], nu_p[CU], nu_n[CU], jx[CU], jxp[CU], fa[CU], fm[CU], tt[CU], ttp[CU];
+            int hh[CU], gg[CU];
+#pragma unroll
+            for (int u = 0; u < CU; ++u) {
+                const int c = c0 + 32 * u;
+                int s_, h_, g_;
+                decode_col_a(G, c < G.COUT ? c : G.COUT, s_, h_, g_);
+                hh[u] = h_;
+                gg[u] = g_ < d.n_ring ? g_ : -1;
+                if (gg[u] < 0) continue;
+                const size_t o = (size_t)k * G.LDC + c;
+                fa[u] = pv[c]; fm[u] = pv[G.LDC + c];
+                nu_k[u] = nuv[o];
+                nu_p[u] = k > 0 ? nuv[o - G.LDC] : 0.f;
+                nu_n[u] = k < nt ? nuv[o + G.LDC] : 0.f;
+                jx[u] = Jx[o];
+                jxp[u] = k > 0 ? Jx[o - G.LDC] : 0.f;
+                tt[u] = (float)Tot[o];
+                ttp[u] = k > 0 ? (float)Tot[o - G.LDC] : 0.f;
             }
-            const float j1 = chk * (xk * faP + yk * fmP);
-            const float jt = Jx[o] + j1;
-            ssa_c += mu * jt;
-            j1_c += mu * j1;
-            if (k > 0) {
-                const int e = (k - 1) * NR + g;
-                const float jtp = Jx[o - G.LDC] + chp * (xp * faP + yp * fmP);
-                if (h == 0)
-                    lay_c += nu_p * ((float)Tot[o] * dT[e] + jtp * dA[e] + jt * dB[e]);
-                else
-                    lay_c += nu_k * ((float)Tot[o - G.LDC] * dT[e] + jt * dA[e] + jtp * dB[e]);
+#pragma unroll
+            for (int u = 0; u < CU; ++u) {
+                const int g = gg[u];
+                if (g < 0) continue;
+                float mu;
+                if (hh[u] == 0) {
+                    mu = k < nt ? Ca[k * NR + g] * nu_k[u] : 0.f;
+                    if (k > 0) mu += Cb[(k - 1) * NR + g] * nu_p[u];
+                } else {
+                    mu = k > 0 ? Ca[(k - 1) * NR + g] * nu_k[u] : 0.f;
+                    if (k < nt) mu += Cb[k * NR + g] * nu_n[u];
+                }
+                const float j1 = chk * (xk * fa[u] + yk * fm[u]);
+                const float jt = jx[u] + j1;
+                ssa_c += mu * jt;
+                j1_c += mu * j1;
+                if (k > 0) {
+                    const int e = (k - 1) * NR + g;
+                    const float jtp = jxp[u] + chp * (xp * fa[u] + yp * fm[u]);
+                    if (hh[u] == 0)
+                        lay_c += nu_p[u] * (tt[u] * dT[e] + jtp * dA[e] + jt * dB[e]);
+                    else
+                        lay_c += nu_k[u] * (ttp[u] * dT[e] + jt * dA[e] + jtp * dB[e]);
+                }
             }
         }
         ssa_c = warp_sum(ssa_c);

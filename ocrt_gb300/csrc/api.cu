@@ -589,13 +589,15 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
         if (w.any_rough) {
-            const size_t smem = coxmunk_smem_bytes(g.nphi, g.ncot > 0);
-            if (g.ncot)
-                LAUNCH(plan, KC_COXMUNK, k_coxmunk_dw<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
-                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.lam, g.lamd, g.srf, g.srfW));
+            const bool dw = g.ncot > 0;
+            const int np = w.p1 - w.p0;
+            const size_t smem = coxmunk_smem_bytes(g.nphi, dw);
+            if (dw)
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk_dw<<<dim3(G.N + 1, G.NR, np), 256, smem, st>>>(
+                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.Mmax, g.lam, g.lamd, g.srf, g.srfW));
             else
-                LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, w.p1 - w.p0), 256, smem, st>>>(
-                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.lam, g.srf));
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, np), 256, smem, st>>>(
+                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.Mmax, g.lam, g.srf));
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
@@ -736,11 +738,19 @@ int plan_create_impl(int n, const ocrt_case *cases, const ocrt_opts *opts, int o
     std::lock_guard<std::mutex> lk(g_mu);
     ocrt_plan *plan = new ocrt_plan();
     plan->n = n;
-    std::map<int, int> gid;
+    // groups share the Gauss order and the Cox-Munk azimuth grid
+    std::map<std::pair<int, int>, int> gid;
     for (int i = 0; i < n; ++i) {
-        const int N = (opp ? opts[i] : opts[0]).n_mu;
-        auto it = gid.find(N);
-        if (it == gid.end()) { gid[N] = (int)plan->groups.size(); plan->groups.emplace_back(); plan->groups.back().N = N; it = gid.find(N); }
+        const ocrt_opts &oi = opp ? opts[i] : opts[0];
+        const int N = oi.n_mu;
+        const std::pair<int, int> key(N, oi.n_phi_surface > 0 ? oi.n_phi_surface : 1024);
+        auto it = gid.find(key);
+        if (it == gid.end()) {
+            gid[key] = (int)plan->groups.size();
+            plan->groups.emplace_back();
+            plan->groups.back().N = N;
+            it = gid.find(key);
+        }
         plan->groups[it->second].idx.push_back(i);
     }
     for (Group &g : plan->groups) {

@@ -19,10 +19,10 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const double *mb, const double *mg, const double *ma, const double *mz,
                          float *ops, float *pvec, float *fvec);
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
-                          const double *gmu, const float *cs_tab, const double *lamv, float *srf);
+                          const double *gmu, const float *cs_tab, int Mtab, const double *lamv, float *srf);
 __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
-                             const double *gmu, const float *cs_tab, const double *lamv, const double *lamd,
-                             float *srf, float *srfW);
+                             const double *gmu, const float *cs_tab, int Mtab, const double *lamv,
+                             const double *lamd, float *srf, float *srfW);
 __global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, double *lam, double *lamd);
 __global__ void k_layers_apply(PixDev *px, int P, const double *ldt, const double *lss, double *h, double *ch,
                                double *xd, double *yd, int *err);

@@ -202,7 +202,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_LAUNCH(k_seed_att<<<dim3(8, 1), 256, 0, st>>>(px, 1, N, gmu, h, Eatt));
         NA_LAUNCH(k_sancer<<<1, 128, 0, st>>>(px, 1, N, gmu, lamv, nullptr));
         NA_LAUNCH(k_coxmunk<<<dim3(N + 1, NR, 1), 256, coxmunk_smem_bytes(d.nphi, false), st>>>(
-            tasks, px, 0, ptask0, G, gmu, cst, lamv, srf));
+            tasks, px, 0, ptask0, G, gmu, cst, M, lamv, srf));
     }
     if (flat) NA_LAUNCH(k_flat_fresnel<<<1, 128, 0, st>>>(px, 1, N, gmu, frs));
 

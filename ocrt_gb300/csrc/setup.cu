@@ -518,17 +518,18 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
 //   dR/dW = ds2/dW * R * [ -1/s2 + tan^2(beta)/s2^2 - (dlam/ds2)/(1 + lam) ]
 // and dR_m/dW = a R_m + b P_m[R tan^2(beta)] with per-pair constants a, b and
 // P_m the same azimuth projection.
-template <bool DW>
-__device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0,
-                                             Geom G, const double *gmu, const float *cs_tab, const double *lamv,
-                                             const double *lamd, float *srf, float *srfW)
+// One (pixel p, outgoing slot o, incoming slot i) pair, all modes, by the
+// whole block.  tab: cos/sin(m phi_q) rows [(m * 2 + kind) * half + q] of a
+// table built for Mtab modes, followed by the cos phi, sin phi, sin^2(phi/2)
+// rows; SMT = the table is in shared memory (else read through the read-only
+// cache).  sm_R holds R (and R tan^2(beta) when DW) on the half grid.  Ends with
+// a block barrier so the caller can reuse sm_R.
+template <bool DW, bool SMT>
+__device__ __forceinline__ void coxmunk_pair(int p, int o, int i, const TaskDev *tasks, const PixDev &d,
+                                             const int *pix_task0, const Geom &G, const double *gmu,
+                                             const float *tab, int Mtab, const double *lamv, const double *lamd,
+                                             float *srf, float *srfW, float *sm_R)
 {
-    extern __shared__ float sm_R[];                 // [9][nphi/2 + 1] (and R tan^2(beta) when DW)
-    const int p = p0 + blockIdx.z;
-    const PixDev &d = px[p];
-    if (!d.rough) return;
-    const int o = blockIdx.y, i = blockIdx.x;       // o: 0..NR-1, i: 0..N (N = sun)
-    if (o >= d.n_ring) return;
     const int N = G.N;
     const int os = o;
     const double mo = os < N ? gmu[os] : d.mu_view;
@@ -539,13 +540,14 @@ __device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev 
     const double lam = lp[i < N ? i : N + 1] + lp[os];
     const int nphi = d.nphi, half = nphi / 2, hs = half + 1;
     const double dphi = 2.0 * OCRT_PI / (double)nphi;
-    const float *ptab = cs_tab + (size_t)(d.M + 1) * 2 * half;     // [cos, sin, sin^2(phi/2)][half]
+    const float *ptab = tab + (size_t)(Mtab + 1) * 2 * half;       // [cos, sin, sin^2(phi/2)][half]
+    auto ld = [&](const float *a) -> float { return SMT ? *a : __ldg(a); };
     const float fmo = (float)mo, fmi = (float)mi, fs2 = (float)s2v, flam = (float)lam, fnw = (float)d.n_water;
     float *sm_T = sm_R + 9 * hs;
     for (int q = threadIdx.x; q < half; q += blockDim.x) {
         float R[9], tb2 = 0.f;
-        coxmunk_R<float>(fmo, fmi, ptab[q], ptab[half + q], ptab[2 * half + q], fs2, flam, fnw, d.q_conv, R,
-                         DW ? &tb2 : nullptr);
+        coxmunk_R<float>(fmo, fmi, ld(ptab + q), ld(ptab + half + q), ld(ptab + 2 * half + q), fs2, flam, fnw,
+                         d.q_conv, R, DW ? &tb2 : nullptr);
 #pragma unroll
         for (int e = 0; e < 9; ++e) sm_R[e * hs + q] = R[e];
         if (DW) {
@@ -556,8 +558,8 @@ __device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev 
     float ca = 0.f, cb = 0.f;
     if (DW) {
         const double ds2 = slope_variance_dw(d.wind, d.sigma_type);
-        const double *ld = lamd + (size_t)p * (N + 2);
-        const double dlam = ld[i < N ? i : N + 1] + ld[os];
+        const double *ldv = lamd + (size_t)p * (N + 2);
+        const double dlam = ldv[i < N ? i : N + 1] + ldv[os];
         ca = (float)(ds2 * (-1.0 / s2v - dlam / (1.0 + lam)));
         cb = (float)(ds2 / (s2v * s2v));
     }
@@ -591,7 +593,7 @@ __device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev 
 #pragma unroll
         for (int b = 0; b < CM_MG; ++b) {
             const int m = min(CM_MG * mg + b, M);
-            tb[b] = cs_tab + ((size_t)m * 2 + kind) * half;
+            tb[b] = tab + ((size_t)m * 2 + kind) * half;
         }
         int ro[5];
 #pragma unroll
@@ -599,7 +601,7 @@ __device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev 
         for (int q = lane; q < half; q += 32) {
             float tv[CM_MG], rv[5];
 #pragma unroll
-            for (int b = 0; b < CM_MG; ++b) tv[b] = __ldg(tb[b] + q);
+            for (int b = 0; b < CM_MG; ++b) tv[b] = ld(tb[b] + q);
 #pragma unroll
             for (int a = 0; a < 5; ++a) rv[a] = sm_R[ro[a] + q];
 #pragma unroll
@@ -643,19 +645,31 @@ __device__ __forceinline__ void coxmunk_body(const TaskDev *tasks, const PixDev 
                 if (DW) srfW[tk.srf_off + off] = (ca * acc[a][b] + cb * acct[AT == 5 ? a : 0][b]) * sc;
             }
     }
+    __syncthreads();
 }
 
+// Grid (N + 1 incoming, NR outgoing, pixels): one pair per block, table in global memory.
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
-                          const double *gmu, const float *cs_tab, const double *lamv, float *srf)
+                          const double *gmu, const float *cs_tab, int Mtab, const double *lamv, float *srf)
 {
-    coxmunk_body<false>(tasks, px, p0, pix_task0, G, gmu, cs_tab, lamv, nullptr, srf, nullptr);
+    extern __shared__ float sm_R[];
+    const int p = p0 + blockIdx.z;
+    const PixDev &d = px[p];
+    if (!d.rough || (int)blockIdx.y >= d.n_ring) return;
+    coxmunk_pair<false, false>(p, blockIdx.y, blockIdx.x, tasks, d, pix_task0, G, gmu, cs_tab, Mtab, lamv, nullptr,
+                               srf, nullptr, sm_R);
 }
 
 __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
-                             const double *gmu, const float *cs_tab, const double *lamv, const double *lamd,
-                             float *srf, float *srfW)
+                             const double *gmu, const float *cs_tab, int Mtab, const double *lamv,
+                             const double *lamd, float *srf, float *srfW)
 {
-    coxmunk_body<true>(tasks, px, p0, pix_task0, G, gmu, cs_tab, lamv, lamd, srf, srfW);
+    extern __shared__ float sm_R[];
+    const int p = p0 + blockIdx.z;
+    const PixDev &d = px[p];
+    if (!d.rough || (int)blockIdx.y >= d.n_ring) return;
+    coxmunk_pair<true, false>(p, blockIdx.y, blockIdx.x, tasks, d, pix_task0, G, gmu, cs_tab, Mtab, lamv, lamd, srf,
+                              srfW, sm_R);
 }
 
 // cos / sin(m phi_q) on the half azimuth grid for m = 0..M, followed by the
