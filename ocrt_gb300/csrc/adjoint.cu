@@ -129,10 +129,11 @@ __global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0)
     decode_col_a(G, c, s, h, g);
     if (g >= d.n_ring) return;
     float *F = W.F + tk.fld_off;
-    const double *Tot = W.Tot + tk.fld_off;
+    const float2 *Tot = W.Tot + tk.fld_off;
     for (int k = 0; k <= d.nt; ++k) {
         const size_t o = (size_t)k * G.LDC + c;
-        F[o] = (float)(Tot[o] - (double)F[o]);
+        const float2 t = Tot[o];
+        F[o] = (t.x - F[o]) + t.y;
     }
 }
 
@@ -225,9 +226,9 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
     const bool valid = c < G.COUT && g < d.n_ring;
     const size_t off = adj_off(tk, G, A.ncot, r);
     float *a = A.AF + off;
-    double *At = A.ATot + off;
+    float2 *At = A.ATot + off;
     float *mj = A.AJ + off;
-    double mi = 0.0, mt = 0.0;
+    float mi = 0.f, mt = 0.f;
     if (valid) {
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
         // The view columns are outputs only (zero quadrature weight): the
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
             for (int k1 = 0; k1 <= nt; k1 += PF) {
                 const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
                 float av[PF], tv[PF], ca[PF], cb[PF];
-                double ov[PF];
+                float2 ov[PF];
 #pragma unroll
                 for (int q = 0; q < PF; ++q) {
                     if (q < cnt) {
@@ -258,11 +259,11 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                     if (q < cnt) {
                         const int k = k1 + q;
                         const size_t o = (size_t)k * G.LDC + c;
-                        const double t = ov[q] + (double)av[q];
+                        const float2 t = df_add(ov[q], av[q]);
                         At[o] = t;
                         if (clear) a[o] = 0.f;
-                        mi = fmax(mi, fabs((double)av[q]));
-                        mt = fmax(mt, fabs(t));
+                        mi = fmaxf(mi, fabsf(av[q]));
+                        mt = fmaxf(mt, fabsf(t.x));
                         const float nu = av[q] + tv[q] * nup;
                         mj[o] = ca[q] * nu + cb[q] * nup;
                         nup = nu;
@@ -275,14 +276,14 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
             for (int k1 = nt; k1 >= 0; k1 -= PF) {
                 const int cnt = k1 + 1 < PF ? k1 + 1 : PF;
                 float av[PF], tv[PF], ca[PF], cb[PF];
-                double ov[PF];
+                float2 ov[PF];
 #pragma unroll
                 for (int q = 0; q < PF; ++q) {
                     if (q < cnt) {
                         const int k = k1 - q;
                         const size_t o = (size_t)k * G.LDC + c;
                         av[q] = k > 0 ? a[o] : 0.f;          // the TOA downward radiance is fixed at zero
-                        ov[q] = k > 0 ? At[o] : 0.0;
+                        ov[q] = k > 0 ? At[o] : make_float2(0.f, 0.f);
                         tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
                         ca[q] = k > 0 ? Ca[(k - 1) * NR + g] : 0.f;
                         cb[q] = k < nt ? Cb[k * NR + g] : 0.f;
@@ -294,11 +295,11 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                         const int k = k1 - q;
                         const size_t o = (size_t)k * G.LDC + c;
                         if (k > 0) {
-                            const double t = ov[q] + (double)av[q];
+                            const float2 t = df_add(ov[q], av[q]);
                             At[o] = t;
                             if (clear) a[o] = 0.f;
-                            mi = fmax(mi, fabs((double)av[q]));
-                            mt = fmax(mt, fabs(t));
+                            mi = fmaxf(mi, fabsf(av[q]));
+                            mt = fmaxf(mt, fabsf(t.x));
                         }
                         const float nu = av[q] + tv[q] * nun;
                         mj[o] = ca[q] * nu + cb[q] * nun;
@@ -308,13 +309,13 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
             }
         }
     }
-    mi = block_max_a(mi, red);
+    mi = (float)block_max_a(mi, red);
     __syncthreads();
-    mt = block_max_a(mt, red);
+    mt = (float)block_max_a(mt, red);
     if (threadIdx.x == 0) {
         TaskState ns = st;
         ns.orders = j;
-        ns.resid = mt > 0.0 ? mi / mt : 0.0;
+        ns.resid = mt > 0.f ? (double)(mi / mt) : 0.0;
         if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
         else if (j >= d.max_orders) ns.active = 0;
         A.st[ta] = ns;
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(256) k_adj_mol(BatchBufs B, WaveBufs W, AdjBuf
         const int k = e / G.CIN, ci = e - k * G.CIN, b = ci / N, i = ci - b * N;
         const float *z = zt + k * 25 + 4 * b;
         const float v = fv[i] * z[0] + fv[N + i] * z[1] + fv[2 * N + i] * z[2] + fv[3 * N + i] * z[3];
-        out[(size_t)(k0 + k) * G.LDC + ci] += (float)yd[k0 + k] * v;
+        out[(size_t)(k0 + k) * G.LDC + ci] += B.lvf[3 * (d.lev_off + k0 + k) + 1] * v;
     }
 }
 
@@ -463,8 +464,7 @@ __global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0
     const int sp = e / N, i = e - sp * N;
     const float *mb = A.bc + (size_t)ta * NR * 3;
     const float *R = W.srf + tk.srf_off;
-    const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
-    const float pw = (float)(fw * B.gmu[i] * B.gw[i]);
+    const float pw = B.pw[(tk.m == 0 ? 0 : N) + i];
     float acc = 0.f;
     for (int g = 0; g < d.n_ring; ++g) {
         const float *Rg = R + ((size_t)g * N + i) * 9 + sp;
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
     const int nt = d.nt, NR = G.NR, N = G.N;
     const size_t off = adj_off(tk, G, A.ncot, r);
     float *nuv = A.AF + off;
-    const double *At = A.ATot + off;
+    const float2 *At = A.ATot + off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const float *dT = A.dTc + d.coef_off, *dA = A.dCa + d.coef_off, *dB = A.dCb + d.coef_off;
     // ---- pass 1: nu = transposed transport of the adjoint total (FP64 recurrence)
@@ -503,23 +503,23 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
         const bool valid = c < G.COUT && g < d.n_ring;
         constexpr int PF = 8;
         if (valid && h == 0) {
-            double nu = 0.0;
+            float nu = 0.f;
             for (int k1 = 0; k1 <= nt; k1 += PF) {
                 const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
-                double av[PF];
-                float tv[PF];
+                float av[PF], tv[PF];
 #pragma unroll
                 for (int q = 0; q < PF; ++q)
                     if (q < cnt) {
                         const int k = k1 + q;
-                        av[q] = At[(size_t)k * G.LDC + c];
+                        const float2 t = At[(size_t)k * G.LDC + c];
+                        av[q] = t.x + t.y;
                         tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
                     }
 #pragma unroll
                 for (int q = 0; q < PF; ++q)
                     if (q < cnt) {
-                        nu = av[q] + (double)tv[q] * nu;
-                        nuv[(size_t)(k1 + q) * G.LDC + c] = (float)nu;
+                        nu = av[q] + tv[q] * nu;
+                        nuv[(size_t)(k1 + q) * G.LDC + c] = nu;
                     }
             }
             if (d.rough) {
@@ -527,10 +527,10 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
                 // the direct-beam seed, and the seed's optical-depth dependence
                 const float *Xs = W.F + tk.fld_off + (size_t)nt * G.LDC;
                 const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
-                const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
+                const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
                 double acc = 0.0;
                 for (int i = 0; i < N; ++i) {
-                    const double pw = (float)(fw * B.gmu[i] * B.gw[i]);
+                    const double pw = pwm[i];
                     const float *Ri = RW + (size_t)i * 9;
                     acc += pw * ((double)Ri[0] * Xs[col_of(G, 0, 1, i)] + (double)Ri[1] * Xs[col_of(G, 1, 1, i)] +
                                  (double)Ri[2] * Xs[col_of(G, 2, 1, i)]);
@@ -539,28 +539,28 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
                 const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
                 const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
                 const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
-                const double E = B.Eatt[(d.lev_off + nt) * NR + g];
+                const double E = (double)B.Eatt[(d.lev_off + nt) * NR + g];
                 gW = nu * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
                 gS = nu * fs * tdn * E * (double)Rs[g * 9 + s * 3];
             }
         } else if (valid) {
-            double nu = 0.0;
+            float nu = 0.f;
             for (int k1 = nt; k1 >= 1; k1 -= PF) {
                 const int cnt = k1 < PF ? k1 : PF;
-                double av[PF];
-                float tv[PF];
+                float av[PF], tv[PF];
 #pragma unroll
                 for (int q = 0; q < PF; ++q)
                     if (q < cnt) {
                         const int k = k1 - q;
-                        av[q] = At[(size_t)k * G.LDC + c];
+                        const float2 t = At[(size_t)k * G.LDC + c];
+                        av[q] = t.x + t.y;
                         tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
                     }
 #pragma unroll
                 for (int q = 0; q < PF; ++q)
                     if (q < cnt) {
-                        nu = av[q] + (double)tv[q] * nu;
-                        nuv[(size_t)(k1 - q) * G.LDC + c] = (float)nu;
+                        nu = av[q] + tv[q] * nu;
+                        nuv[(size_t)(k1 - q) * G.LDC + c] = nu;
                     }
             }
             nuv[c] = 0.f;
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
     const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
     const float *Jx = W.J + tk.fld_off;
-    const double *Tot = W.Tot + tk.fld_off;
+    const float2 *Tot = W.Tot + tk.fld_off;
     double *go = A.gout + (size_t)ta * A.gstride;
     // Each lane takes CU columns per pass (32 * CU apart) and issues all their
     // loads before the arithmetic, so a warp keeps many row loads in flight.
@@ -603,8 +603,8 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
                 nu_n[u] = k < nt ? nuv[o + G.LDC] : 0.f;
                 jx[u] = Jx[o];
                 jxp[u] = k > 0 ? Jx[o - G.LDC] : 0.f;
-                tt[u] = (float)Tot[o];
-                ttp[u] = k > 0 ? (float)Tot[o - G.LDC] : 0.f;
+                tt[u] = Tot[o].x;
+                ttp[u] = k > 0 ? Tot[o - G.LDC].x : 0.f;
             }
 #pragma unroll
             for (int u = 0; u < CU; ++u) {
@@ -703,7 +703,7 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
                 for (int cc = 0; cc < nc; ++cc) {
                     const int gg = cols[cc];
                     const double mug = gg < N ? B.gmu[gg] : d.mu_view;
-                    const double E = B.Eatt[d.lev_off * NR + gg];
+                    const double E = (double)B.Eatt[d.lev_off * NR + gg];
                     for (int s = 0; s < 3; ++s) {
                         const double sv = cw[cc] * fs * tdn * E * (double)Rs[gg * 9 + s * 3];
                         const double svw = cw[cc] * fs * tdn * E * (double)RsW[gg * 9 + s * 3];

@@ -199,25 +199,28 @@ struct Group {
     PixDev *px = nullptr; TaskDev *tasks = nullptr; TaskState *state = nullptr; TaskOut *tout = nullptr;
     ocrt_result *res = nullptr; int *pix_task0 = nullptr;
     double *gmu = nullptr, *gw = nullptr;
+    float *pw = nullptr;
     double *h = nullptr, *ch = nullptr, *xd = nullptr, *yd = nullptr, *z = nullptr;
     float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
-    double *Eatt = nullptr, *lam = nullptr;
+    double *lam = nullptr;
+    float *Eatt = nullptr, *lvf = nullptr;
     double *mb = nullptr, *mg = nullptr, *ma = nullptr, *mz = nullptr;
     double *kappa = nullptr, *taudir = nullptr;
     int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
     float *F = nullptr, *J = nullptr, *ops = nullptr, *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
-    double *Tot = nullptr;
+    float2 *Tot = nullptr;
     bool use_tc = false;
     CUtensorMap mapF, mapA;
     // per-layer overrides and the adjoint (ocrt_gb_solve_batch_adjoint)
     bool any_layers = false;
     int ncot = 0, ntmax = 0;
-    double *ldt = nullptr, *lss = nullptr, *cot = nullptr, *lamd = nullptr, *ATot = nullptr, *gout = nullptr,
+    double *ldt = nullptr, *lss = nullptr, *cot = nullptr, *lamd = nullptr, *gout = nullptr,
            *grad = nullptr;
     float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJ = nullptr,
           *Abc = nullptr;
+    float2 *ATot = nullptr;
     TaskState *Ast = nullptr;
     int *acnt = nullptr, *awork = nullptr;
     float *opsT = nullptr;            // transposed operators for the tcgen05 adjoint source
@@ -269,8 +272,8 @@ template <class T> int alloc(T *&dst, size_t n)
 
 void free_group(Group &g)
 {
-    void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.h, g.ch, g.xd, g.yd, g.z,
-                    g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
+    void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
+                    g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
                     g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
@@ -399,7 +402,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     if ((rc = up(g.px, g.hpx)) || (rc = up(g.tasks, g.htask)) || (rc = up(g.pix_task0, g.hpix_task0)) ||
         (rc = up(g.mb, mb)) || (rc = up(g.mg, mgv)) || (rc = up(g.ma, ma)) || (rc = up(g.mz, mz)) ||
         (rc = alloc(g.state, g.T)) || (rc = alloc(g.tout, g.T)) || (rc = alloc(g.res, g.P)) ||
-        (rc = alloc(g.gmu, g.N)) || (rc = alloc(g.gw, g.N)) ||
+        (rc = alloc(g.gmu, g.N)) || (rc = alloc(g.gw, g.N)) || (rc = alloc(g.pw, 2 * (size_t)g.N)) ||
         (rc = alloc(g.h, g.nlev)) || (rc = alloc(g.ch, g.nlev)) || (rc = alloc(g.xd, g.nlev)) ||
         (rc = alloc(g.yd, g.nlev)) || (rc = alloc(g.z, g.nlev)) ||
         (rc = alloc(g.Tc, g.ncoef)) || (rc = alloc(g.Ca, g.ncoef)) || (rc = alloc(g.Cb, g.ncoef)) ||
@@ -407,7 +410,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.Br, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Bt, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.cs, (size_t)(g.Mmax + 1) * 2 * (g.nphi / 2) + 3 * (size_t)(g.nphi / 2))) ||
-        (rc = alloc(g.Eatt, g.any_rough ? g.nlev * G.NR : 1)) ||
+        (rc = alloc(g.Eatt, g.any_rough ? g.nlev * G.NR : 1)) || (rc = alloc(g.lvf, 3 * g.nlev)) ||
         (rc = alloc(g.lam, (size_t)g.P * (G.N + 2))) ||
         (rc = alloc(g.frs, (size_t)g.P * G.NR * 9)) ||
         (rc = alloc(g.kappa, g.P)) || (rc = alloc(g.taudir, g.P)) ||
@@ -506,7 +509,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     // adjoint successive orders
     CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.AJ, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.ATot, 0, sizeof(double) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.ATot, 0, sizeof(float2) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
     CK(cudaMemsetAsync(g.awork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
@@ -549,7 +552,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     const Geom G = g.G;
     const int P = g.P;
     CK(cudaMemsetAsync(g.err, 0, sizeof(int), st));
-    LAUNCH(plan, KC_SETUP, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw));
+    LAUNCH(plan, KC_SETUP, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw, g.pw));
     LAUNCH(plan, KC_SETUP, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
     LAUNCH(plan, KC_SETUP, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
     LAUNCH(plan, KC_SETUP, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
@@ -562,14 +565,15 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         LAUNCH(plan, KC_SETUP, k_seed_att<<<dim3(8, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Eatt));
         LAUNCH(plan, KC_SETUP, k_sancer<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.lam, g.ncot ? g.lamd : nullptr));
     }
+    LAUNCH(plan, KC_SETUP, k_level_float<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.xd, g.yd, g.ch, g.lvf));
     if (g.any_flat) LAUNCH(plan, KC_SETUP, k_flat_fresnel<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.frs));
     if (g.ncot)
         LAUNCH(plan, KC_SETUP, k_coef_deriv<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.dTc, g.dCa, g.dCb));
 
     BatchBufs B;
     B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
-    B.gmu = g.gmu; B.gw = g.gw; B.h = g.h; B.ch = g.ch; B.xd = g.xd; B.yd = g.yd; B.z = g.z;
-    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.Eatt = g.Eatt; B.active_cnt = g.active_cnt; B.err = g.err;
+    B.gmu = g.gmu; B.gw = g.gw; B.pw = g.pw; B.h = g.h; B.ch = g.ch; B.xd = g.xd; B.yd = g.yd; B.z = g.z;
+    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.Eatt = g.Eatt; B.lvf = g.lvf; B.active_cnt = g.active_cnt; B.err = g.err;
     B.mol_cnt = g.mol_cnt; B.work = g.work;
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     WaveBufs W;
@@ -586,7 +590,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         CK(cudaMemsetAsync(g.mol_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.work, 0, sizeof(int) * 4 * ((size_t)g.max_orders + 2), st));
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
-        LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
+        LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, sizeof(float) * 4 * ((size_t)g.Lmax + 1), st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
         if (w.any_rough) {
             const bool dw = g.ncot > 0;
@@ -1012,7 +1016,7 @@ int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocr
         cudaStream_t st = g_stream;
         const int nt = g.hpx[0].nt;
         std::vector<double> h(nt + 1), x(nt + 1), y(nt + 1);
-        k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw);
+        k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw, g.pw);
         k_pixel_setup<<<1, 128, 0, st>>>(g.px, 1, g.N, g.gmu);
         k_levels<<<dim3(2, 1), 256, 0, st>>>(g.px, 1, g.h, g.ch, g.xd, g.yd, g.z);
         k_level_mix<<<dim3(2, 1), 256, 0, st>>>(g.px, 1, g.z, g.xd, g.yd);

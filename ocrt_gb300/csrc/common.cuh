@@ -99,3 +99,19 @@ __host__ __device__ inline int in_to_col(const Geom &g, int cin)
     (void)g;
     return cin;
 }
+
+// Order totals are kept as unevaluated FP32 pairs (hi + lo, ~48-bit
+// significand): FP64 issues at a small fraction of the FP32 rate on this part,
+// and the totals are touched at every order, level and column.
+// df_add(a, b) = a + b with TwoSum on the heads and the tails folded in.
+__host__ __device__ inline float2 df_add(float2 a, float b)
+{
+    const float s = a.x + b;
+    const float bp = s - a.x;
+    const float e = (a.x - (s - bp)) + (b - bp);
+    const float t = e + a.y;
+    const float hi = s + t;
+    return make_float2(hi, t - (hi - s));
+}
+
+__host__ __device__ inline double df_value(float2 a) { return (double)a.x + (double)a.y; }

@@ -5,7 +5,7 @@
 #include "../../include/ocrt_gb300.h"
 
 // setup.cu
-__global__ void k_gauss(int N, double *mu, double *w);
+__global__ void k_gauss(int N, double *mu, double *w, float *pw);
 __global__ void k_pixel_setup(PixDev *px, int P, int N, const double *gmu);
 __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double *xd, double *yd, double *z);
 __global__ void k_level_mix(const PixDev *px, int P, const double *z, double *xd, double *yd);
@@ -30,14 +30,15 @@ __global__ void k_coef_deriv(const PixDev *px, int P, int N, const double *gmu, 
                              float *dTc, float *dCa, float *dCb);
 __global__ void k_cs_table(int M, int nphi, float *cs);
 __global__ void k_flat_fresnel(const PixDev *px, int P, int N, const double *gmu, float *frs);
-__global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, double *E);
+__global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, float *E);
+__global__ void k_level_float(const PixDev *px, int P, const double *xd, const double *yd, const double *ch, float *lvf);
 
 // sos.cu
 #define ST_M_TILE 64
 #define ST_N_TILE 64
 struct WaveBufs {
     float *F, *J;          // fields, wave-relative by TaskDev::fld_off
-    double *Tot;
+    float2 *Tot;           // order totals (hi, lo) pairs
     float *ops;            // operators, wave-relative
     float *pvec, *fvec;    // per wave-task primary and flat-beam vectors
     float *srf;            // rough surface kernels, wave-relative
@@ -48,10 +49,12 @@ struct BatchBufs {
     TaskState *state;
     TaskOut *tout;
     const double *gmu, *gw;
+    const float *pw;       // [2N]: (float)(2 pi mu_i w_i) for m = 0, then (float)(pi mu_i w_i)
     const double *h, *ch, *xd, *yd, *z;
     const float *Tc, *Ca, *Cb;
     const float *frs;
-    const double *Eatt;    // rough direct-beam attenuation [lev_off*NR + k*NR + g]
+    const float *Eatt;     // rough direct-beam attenuation [lev_off*NR + k*NR + g]
+    const float *lvf;      // [lev_off + k][3]: x_k, y_k, direct beam ch_k rounded to FP32
     int *active_cnt;       // [max_orders + 2]: tasks still active after order it
     int *mol_cnt;          // [max_orders + 2]: molecular (m <= 2) tasks still active after order it
     int *alist[2];         // ping-pong active-task lists (wave-local ids); order it reads alist[it & 1]
@@ -64,7 +67,7 @@ struct BatchBufs {
 struct AdjBufs {
     int ncot;              // cotangent rows per pixel; adjoint task = wave task * ncot + row
     float *AF, *AJ;        // adjoint field a_j and transposed-transport output muJ (wave-relative, x ncot)
-    double *ATot;          // adjoint total
+    float2 *ATot;          // adjoint total (hi, lo) pairs
     float *bc;             // mu_bc per adjoint task [NR][3]
     TaskState *st;         // per adjoint task
     int *acnt;             // [max_orders + 2] adjoint tasks still active after order j

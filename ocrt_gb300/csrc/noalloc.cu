@@ -133,13 +133,15 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     ocrt_result *res = cv.take<ocrt_result>(1);
     int *ptask0 = cv.take<int>(1);
     double *gmu = cv.take<double>(N), *gw = cv.take<double>(N);
+    float *pwt = cv.take<float>(2 * (size_t)N);
     double *h = cv.take<double>(K), *ch = cv.take<double>(K), *xd = cv.take<double>(K);
     double *yd = cv.take<double>(K), *z = cv.take<double>(K);
     float *Tc = cv.take<float>((size_t)nt * NR), *Ca = cv.take<float>((size_t)nt * NR), *Cb = cv.take<float>((size_t)nt * NR);
     const size_t nb = (size_t)T * (L + 1) * N;
     float *Bp = cv.take<float>(nb), *Br = cv.take<float>(nb), *Bt = cv.take<float>(nb);
     float *cst = cv.take<float>(rough ? (size_t)(T * 2 + 3) * (d.nphi / 2) : 1);
-    double *Eatt = cv.take<double>(rough ? (size_t)K * NR : 1);
+    float *Eatt = cv.take<float>(rough ? (size_t)K * NR : 1);
+    float *lvf = cv.take<float>(3 * (size_t)K);
     double *lamv = cv.take<double>((size_t)N + 2);
     float *frs = cv.take<float>((size_t)NR * 9);
     const int La1 = aer ? aer->L_max + 1 : 1;
@@ -158,7 +160,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     if (Wt > T) Wt = T;
     if (Wt < 1) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
     float *F = cv.take<float>((size_t)Wt * K * G.LDC), *J = cv.take<float>((size_t)Wt * K * G.LDC);
-    double *Tot = cv.take<double>((size_t)Wt * K * G.LDC);
+    float2 *Tot = cv.take<float2>((size_t)Wt * K * G.LDC);
     float *ops = cv.take<float>(2 * (size_t)Wt * op_elems);
     float *pvec = cv.take<float>((size_t)Wt * 2 * G.LDC);
     float *fvec = cv.take<float>((size_t)Wt * 24 * NR);
@@ -191,7 +193,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_CK(cudaMemsetAsync(err, 0, sizeof(int), st));
 
     // ---- the same kernel sequence as the allocating path ----
-    NA_LAUNCH(k_gauss<<<1, 64, 0, st>>>(N, gmu, gw));
+    NA_LAUNCH(k_gauss<<<1, 64, 0, st>>>(N, gmu, gw, pwt));
     NA_LAUNCH(k_pixel_setup<<<1, 32, 0, st>>>(px, 1, N, gmu));
     NA_LAUNCH(k_levels<<<dim3(2, 1), 256, 0, st>>>(px, 1, h, ch, xd, yd, z));
     NA_LAUNCH(k_level_mix<<<dim3(2, 1), 256, 0, st>>>(px, 1, z, xd, yd));
@@ -204,11 +206,12 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_LAUNCH(k_coxmunk<<<dim3(N + 1, NR, 1), 256, coxmunk_smem_bytes(d.nphi, false), st>>>(
             tasks, px, 0, ptask0, G, gmu, cst, M, lamv, srf));
     }
+    NA_LAUNCH(k_level_float<<<dim3(2, 1), 256, 0, st>>>(px, 1, xd, yd, ch, lvf));
     if (flat) NA_LAUNCH(k_flat_fresnel<<<1, 128, 0, st>>>(px, 1, N, gmu, frs));
 
     BatchBufs B;
-    B.px = px; B.tasks = tasks; B.state = state; B.tout = tout; B.gmu = gmu; B.gw = gw;
-    B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs; B.Eatt = Eatt;
+    B.px = px; B.tasks = tasks; B.state = state; B.tout = tout; B.gmu = gmu; B.gw = gw; B.pw = pwt;
+    B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs; B.Eatt = Eatt; B.lvf = lvf;
     B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work;
     B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
@@ -224,7 +227,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_CK(cudaMemsetAsync(molcnt, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
         NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
         NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, Bx));
-        NA_LAUNCH(k_tables<<<nw, 256, 0, st>>>(tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz,
+        NA_LAUNCH(k_tables<<<nw, 256, sizeof(float) * 4 * ((size_t)L + 1), st>>>(tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz,
                                                ops, pvec, W.fvec));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);

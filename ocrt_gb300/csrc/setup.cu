@@ -13,7 +13,7 @@
 #include "kernels.cuh"
 #include "physics.cuh"
 
-__global__ void k_gauss(int N, double *mu, double *w)
+__global__ void k_gauss(int N, double *mu, double *w, float *pw)
 {
     const int k = threadIdx.x + 1;               // 1..N (largest root first)
     if (k > N) return;
@@ -34,6 +34,11 @@ __global__ void k_gauss(int N, double *mu, double *w)
     dp = (double)order * (t * b - a) / (t * t - 1.0);
     mu[N - k] = t;
     w[N - k] = 2.0 / ((1.0 - t * t) * dp * dp);
+    // surface-operator weights (2 pi or pi) mu w, rounded once (rt_surface_boundary.c:137-208)
+    if (pw) {
+        pw[N - k] = (float)(2.0 * OCRT_PI * t * w[N - k]);
+        pw[N + N - k] = (float)(OCRT_PI * t * w[N - k]);
+    }
 }
 
 __global__ void k_pixel_setup(PixDev *px, int P, int N, const double *gmu)
@@ -321,6 +326,16 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
     const int mol = m <= 2;
     float *Aop = ops + tk.op_off;
     float *Bop = tk.mol_off >= 0 ? ops + tk.mol_off : nullptr;
+    // aerosol moments in FP32 shared memory (read at every l of every pair)
+    extern __shared__ float smom[];                               // [4][Lp + 1]
+    for (int l = threadIdx.x; l <= Lp; l += blockDim.x) {
+        const bool in = l <= La;
+        smom[l] = in ? (float)mb[d.mom_off + l] : 0.f;
+        smom[(Lp + 1) + l] = in ? (float)mg[d.mom_off + l] : 0.f;
+        smom[2 * (Lp + 1) + l] = in ? (float)ma[d.mom_off + l] : 0.f;
+        smom[3 * (Lp + 1) + l] = in ? (float)mz[d.mom_off + l] : 0.f;
+    }
+    __syncthreads();
 
     // ---- operator pairs (o ring slot, i Gauss) ----
     for (int e = threadIdx.x; e < n * N; e += blockDim.x) {
@@ -329,10 +344,8 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
         // accumulators: [row i, col o] products, even (E) / odd (O) in l+m
         float E[9] = {0}, O[9] = {0}, Et[4] = {0}, Ot[4] = {0};
         for (int l = m; l <= Lp; ++l) {
-            const float be = l <= La ? (float)mb[d.mom_off + l] : 0.f;
-            const float ga = l <= La ? (float)mg[d.mom_off + l] : 0.f;
-            const float al = l <= La ? (float)ma[d.mom_off + l] : 0.f;
-            const float ze = l <= La ? (float)mz[d.mom_off + l] : 0.f;
+            const float be = smom[l], ga = smom[(Lp + 1) + l];
+            const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
             const float Pi = basis(0, i, l), Ri = basis(1, i, l), Ti = basis(2, i, l);
             const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
             float v[9] = {Pi * Po * be, Pi * Ro * ga, Pi * To * ga, Ti * To * ze, Ri * Ro * al,
@@ -426,10 +439,8 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
         float Ex[3] = {0}, Ox[3] = {0};    // RT z, TT a, RR z
         float Ey[2] = {0}, Oy[2] = {0};    // P_o R_0 g  (gr pair),  T_o R_0 a + R_o T_0 z (art pair)
         for (int l = m; l <= Lp; ++l) {
-            const float be = l <= La ? (float)mb[d.mom_off + l] : 0.f;
-            const float ga = l <= La ? (float)mg[d.mom_off + l] : 0.f;
-            const float al = l <= La ? (float)ma[d.mom_off + l] : 0.f;
-            const float ze = l <= La ? (float)mz[d.mom_off + l] : 0.f;
+            const float be = smom[l], ga = smom[(Lp + 1) + l];
+            const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
             const float P0 = basis(0, -1, l), R0 = basis(1, -1, l), T0 = basis(2, -1, l);
             const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
             const float v[6] = {P0 * Po * be, P0 * Ro * ga, P0 * To * ga, T0 * To * ze, R0 * Ro * al, T0 * Ro * al};
@@ -530,19 +541,21 @@ __device__ __forceinline__ void coxmunk_pair(int p, int o, int i, const TaskDev 
                                              const float *tab, int Mtab, const double *lamv, const double *lamd,
                                              float *srf, float *srfW, float *sm_R)
 {
+    // Per-pair scalars are formed in FP32 (FP64 issues at a small fraction of
+    // the FP32 rate on this part and every thread of the block needs them).
     const int N = G.N;
     const int os = o;
-    const double mo = os < N ? gmu[os] : d.mu_view;
-    const double mi = i < N ? gmu[i] : d.mu0;
-    const double s2v = slope_variance(d.wind, d.sigma_type);
+    const float fmo = (float)(os < N ? gmu[os] : d.mu_view);
+    const float fmi = (float)(i < N ? gmu[i] : d.mu0);
+    const float fs2 = d.sigma_type == 1 ? 0.003f + 0.00512f * fmaxf(0.01f, (float)d.wind)
+                                        : fmaxf(0.0731f * 0.0731f * fmaxf(0.f, (float)d.wind), 1e-10f);
     // Sancer shadowing terms, precomputed per (pixel, slot); slot N+1 is the sun
     const double *lp = lamv + (size_t)p * (N + 2);
-    const double lam = lp[i < N ? i : N + 1] + lp[os];
+    const float flam = (float)lp[i < N ? i : N + 1] + (float)lp[os];
     const int nphi = d.nphi, half = nphi / 2, hs = half + 1;
-    const double dphi = 2.0 * OCRT_PI / (double)nphi;
     const float *ptab = tab + (size_t)(Mtab + 1) * 2 * half;       // [cos, sin, sin^2(phi/2)][half]
     auto ld = [&](const float *a) -> float { return SMT ? *a : __ldg(a); };
-    const float fmo = (float)mo, fmi = (float)mi, fs2 = (float)s2v, flam = (float)lam, fnw = (float)d.n_water;
+    const float fnw = (float)d.n_water;
     float *sm_T = sm_R + 9 * hs;
     for (int q = threadIdx.x; q < half; q += blockDim.x) {
         float R[9], tb2 = 0.f;
@@ -557,11 +570,11 @@ __device__ __forceinline__ void coxmunk_pair(int p, int o, int i, const TaskDev 
     }
     float ca = 0.f, cb = 0.f;
     if (DW) {
-        const double ds2 = slope_variance_dw(d.wind, d.sigma_type);
+        const float ds2 = (float)slope_variance_dw(d.wind, d.sigma_type);
         const double *ldv = lamd + (size_t)p * (N + 2);
-        const double dlam = ldv[i < N ? i : N + 1] + ldv[os];
-        ca = (float)(ds2 * (-1.0 / s2v - dlam / (1.0 + lam)));
-        cb = (float)(ds2 / (s2v * s2v));
+        const float dlam = (float)ldv[i < N ? i : N + 1] + (float)ldv[os];
+        ca = ds2 * (-1.f / fs2 - dlam / (1.f + flam));
+        cb = ds2 / (fs2 * fs2);
     }
     __syncthreads();
     // Projection onto cos/sin(m phi).  Work item = (cos or sin entry group,
@@ -574,7 +587,8 @@ __device__ __forceinline__ void coxmunk_pair(int p, int o, int i, const TaskDev 
     const int items = 2 * nmg;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int task_first = pix_task0[p];
-    const float scale0 = (float)(2.0 * dphi / (2.0 * OCRT_PI)), scale1 = (float)(2.0 * dphi / OCRT_PI);
+    // normalisation x2 (half grid) x dphi / (2 pi) for m = 0 and dphi / pi for m > 0, dphi = 2 pi / nphi
+    const float scale0 = 2.f / (float)nphi, scale1 = 4.f / (float)nphi;
     const int ecos[5] = {0, 1, 3, 4, 8}, esin[5] = {2, 5, 6, 7, 7};
     constexpr int AT = DW ? 5 : 1;
     for (int item = warp; item < items; item += nwarp) {
@@ -712,7 +726,7 @@ __global__ void k_sancer(const PixDev *px, int P, int N, const double *gmu, doub
 // Direct-beam attenuation from the surface to level k along slot g,
 // exp(-(tau - h_k)/mu_g), FP64, once per pixel (shared by every mode):
 // E[lev_off*NR + k*NR + g].
-__global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, double *E)
+__global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, const double *h, float *E)
 {
     const int p = blockIdx.y;
     if (p >= P) return;
@@ -723,7 +737,22 @@ __global__ void k_seed_att(const PixDev *px, int P, int N, const double *gmu, co
         const int k = e / NR, g = e - k * NR;
         double am = g < N ? gmu[g] : d.mu_view;
         if (g >= d.n_ring) am = 1.0;
-        E[d.lev_off * NR + e] = exp(-(d.tau_total - h[d.lev_off + k]) / am);
+        E[d.lev_off * NR + e] = (float)exp(-(d.tau_total - h[d.lev_off + k]) / am);
+    }
+}
+
+// FP32 copies of the per-level scattering fractions and direct beam, read at
+// every (level, column) by the order-loop kernels.
+__global__ void k_level_float(const PixDev *px, int P, const double *xd, const double *yd, const double *ch, float *lvf)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= d.nt; k += gridDim.x * blockDim.x) {
+        const long long o = d.lev_off + k;
+        lvf[3 * o + 0] = (float)xd[o];
+        lvf[3 * o + 1] = (float)yd[o];
+        lvf[3 * o + 2] = (float)ch[o];
     }
 }
 

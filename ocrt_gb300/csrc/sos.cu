@@ -39,15 +39,20 @@ __device__ inline double ring_mu(const PixDev &d, const double *gmu, int N, int 
     return g < N ? gmu[g] : d.mu_view;
 }
 
-// Rough direct-beam seed at level k for upward slot g, Stokes s (FP64):
+// Rough direct-beam seed at level k for upward slot g, Stokes s:
 // (pi or pi/2) mu0 exp(-tau/mu0) exp(-(tau-h_k)/mu_g) R_m(mu_g, mu0)[s,I]
-// (rt_surface_boundary.c:430-493).
-__device__ inline double rough_seed(const PixDev &d, const TaskDev &tk, const WaveBufs &W, const BatchBufs &B,
-                                    const Geom &G, double tdn, int k, int g, int s)
+// (rt_surface_boundary.c:430-493).  fs_tdn = (pi or pi/2) mu0 exp(-tau/mu0),
+// formed once per task in FP64 and rounded; the product is FP32 like the field.
+__device__ inline float rough_seed(const TaskDev &tk, const WaveBufs &W, const BatchBufs &B, const PixDev &d,
+                                   const Geom &G, float fs_tdn, int k, int g, int s)
 {
     const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * G.N * 9;
-    const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
-    return fs * tdn * B.Eatt[(d.lev_off + k) * G.NR + g] * (double)Rs[g * 9 + s * 3];
+    return fs_tdn * B.Eatt[(d.lev_off + k) * G.NR + g] * Rs[g * 9 + s * 3];
+}
+
+__device__ inline float seed_scale(const PixDev &d, const TaskDev &tk)
+{
+    return (float)((tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0 * exp(-d.tau_total / d.mu0));
 }
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
@@ -77,7 +82,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
     const double aP = pv[c], mP = pv[G.LDC + c];
     float *F = W.F + tk.fld_off;
-    double *Tot = W.Tot + tk.fld_off;
+    float2 *Tot = W.Tot + tk.fld_off;
     const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off, *hh = B.h + d.lev_off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const int NR = G.NR;
@@ -99,10 +104,11 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     }
     int bad = 0;
     const float faP = (float)aP, fmP = (float)mP;
-    const double tdn = exp(-d.tau_total / d.mu0);
+    const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
     auto Jat = [&](int k) -> float {
-        const float x = (float)xd[k], y = (float)yd[k];
-        float v = (float)ch[k] * (x * faP + y * fmP);
+        const float *lv = B.lvf + 3 * (d.lev_off + k);
+        const float x = lv[0], y = lv[1];
+        float v = lv[2] * (x * faP + y * fmP);
         if (d.flat && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
             const double beam = sb * exp(hh[k] / d.mu0);
             v += (float)(beam * (RI * (x * fa1 + y * fm1) + RQ * (x * fa2 + y * fm2)));
@@ -111,10 +117,10 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
         return v;
     };
     auto store = [&](int k, float I) {
-        double seed = 0.0;
-        if (d.rough && h == 0) seed = rough_seed(d, tk, W, B, G, tdn, k, g, s);
-        F[(size_t)k * G.LDC + c] = (float)((double)I + seed);
-        Tot[(size_t)k * G.LDC + c] = (double)I + seed;
+        float2 t = make_float2(I, 0.f);
+        if (d.rough && h == 0) t = df_add(t, rough_seed(tk, W, B, d, G, fs_tdn, k, g, s));
+        F[(size_t)k * G.LDC + c] = t.x;
+        Tot[(size_t)k * G.LDC + c] = t;
     };
     if (h == 0) {
         float Jn = Jat(nt), I = 0.f;
@@ -257,9 +263,24 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
         float acc = 0.f;
 #pragma unroll
         for (int r = 0; r < 24; ++r) acc = fmaf(u[r], x[r], acc);
-        J[(size_t)(k0 + k) * G.LDC + c] += (float)yd[k0 + k] * acc;
+        J[(size_t)(k0 + k) * G.LDC + c] += B.lvf[3 * (d.lev_off + k0 + k) + 1] * acc;
     }
     }
+}
+
+__device__ inline float block_maxf(float v, float *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = l < nw ? red[l] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;
 }
 
 __device__ inline double block_max(double v, double *red)
@@ -279,7 +300,7 @@ __device__ inline double block_max(double v, double *red)
 
 __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
 {
-    __shared__ double red[32];
+    __shared__ float redf[32];
     __shared__ int item_s;
     const int n_items = B.active_cnt[it - 1];
     for (;;) {
@@ -297,17 +318,17 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
     const bool valid = c < G.COUT && g < d.n_ring;
     float *F = W.F + tk.fld_off;
     const float *J = W.J + tk.fld_off;
-    double *Tot = W.Tot + tk.fld_off;
+    float2 *Tot = W.Tot + tk.fld_off;
     // ---- surface boundary condition from the previous order's BOA downward field
     float bc = 0.f;
     if (valid && h == 0 && d.surf_on) {
         const float *Fb = F + (size_t)nt * G.LDC;
         if (d.rough) {
             const float *R = W.srf + tk.srf_off + (size_t)g * N * 9 + s * 3;
-            const double fw = tk.m == 0 ? 2.0 * OCRT_PI : OCRT_PI;
+            const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
             float acc = 0.f;
             for (int i = 0; i < N; ++i) {
-                const float pw = (float)(fw * B.gmu[i] * B.gw[i]);
+                const float pw = pwm[i];
                 const float *Ri = R + (size_t)i * 9;
                 acc += pw * (Ri[0] * Fb[col_of(G, 0, 1, i)] + Ri[1] * Fb[col_of(G, 1, 1, i)] +
                              Ri[2] * Fb[col_of(G, 2, 1, i)]);
@@ -319,17 +340,19 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
         }
     }
     __syncthreads();
-    double mi = 0.0, mt = 0.0;
+    // sup norms in FP32: the order field is FP32, and the total's head carries
+    // the total to 2^-24 relative
+    float mi = 0.f, mt = 0.f;
     int bad = 0;
     if (valid) {
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
         auto put = [&](int k, float I) {
             const size_t o = (size_t)k * G.LDC + c;
             F[o] = I;
-            const double t = Tot[o] + (double)I;
+            const float2 t = df_add(Tot[o], I);
             Tot[o] = t;
-            mi = fmax(mi, fabs((double)I));
-            mt = fmax(mt, fabs(t));
+            mi = fmaxf(mi, fabsf(I));
+            mt = fmaxf(mt, fabsf(t.x));
         };
         // Levels are processed in chunks of PF: every load of a chunk is issued
         // before the dependent recurrence runs, so the scan is not bound by one
@@ -342,7 +365,7 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
             for (int k1 = nt - 1; k1 >= 0; k1 -= PF) {
                 const int cnt = k1 + 1 < PF ? k1 + 1 : PF;
                 float jv[PF], tv[PF], av[PF], bv[PF];
-                double ov[PF];
+                float2 ov[PF];
 #pragma unroll
                 for (int q = 0; q < PF; ++q) {
                     if (q < cnt) {
@@ -360,10 +383,10 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
                         Jn = jv[q];
                         const size_t o = (size_t)k * G.LDC + c;
                         F[o] = I;
-                        const double t = ov[q] + (double)I;
+                        const float2 t = df_add(ov[q], I);
                         Tot[o] = t;
-                        mi = fmax(mi, fabs((double)I));
-                        mt = fmax(mt, fabs(t));
+                        mi = fmaxf(mi, fabsf(I));
+                        mt = fmaxf(mt, fabsf(t.x));
                     }
                 }
             }
@@ -375,7 +398,7 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
             for (int k1 = 1; k1 <= nt; k1 += PF) {
                 const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
                 float jv[PF], tv[PF], av[PF], bv[PF];
-                double ov[PF];
+                float2 ov[PF];
 #pragma unroll
                 for (int q = 0; q < PF; ++q) {
                     if (q < cnt) {
@@ -393,10 +416,10 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
                         Jp = jv[q];
                         const size_t o = (size_t)k * G.LDC + c;
                         F[o] = I;
-                        const double t = ov[q] + (double)I;
+                        const float2 t = df_add(ov[q], I);
                         Tot[o] = t;
-                        mi = fmax(mi, fabs((double)I));
-                        mt = fmax(mt, fabs(t));
+                        mi = fmaxf(mi, fabsf(I));
+                        mt = fmaxf(mt, fabsf(t.x));
                     }
                 }
             }
@@ -404,13 +427,13 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
         }
     }
     if (bad) atomicExch(B.err, -2);
-    mi = block_max(mi, red);
+    mi = block_maxf(mi, redf);
     __syncthreads();
-    mt = block_max(mt, red);
+    mt = block_maxf(mt, redf);
     if (threadIdx.x == 0) {
         TaskState ns = st;
         ns.orders = it;
-        ns.resid = mt > 0.0 ? mi / mt : 0.0;
+        ns.resid = mt > 0.f ? (double)(mi / mt) : 0.0;
         if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
         else if (it >= d.max_orders) ns.active = 0;
         B.state[tg] = ns;
@@ -441,16 +464,15 @@ __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
     const int tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
-    const double *Tot = W.Tot + tk.fld_off;
+    const float2 *Tot = W.Tot + tk.fld_off;
     const int nt = d.nt, N = G.N, vs = d.view_slot;
-    const double *hh = B.h + d.lev_off;
-    const double tdn = exp(-d.tau_total / d.mu0);
+    const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
     auto up0 = [&](int s, int g) -> double {
-        double v = Tot[col_of(G, s, 0, g)];
-        if (d.rough) v -= rough_seed(d, tk, W, B, G, tdn, 0, g, s);
+        double v = df_value(Tot[col_of(G, s, 0, g)]);
+        if (d.rough) v -= (double)rough_seed(tk, W, B, d, G, fs_tdn, 0, g, s);
         return v;
     };
-    auto dn = [&](int g) -> double { return Tot[(size_t)nt * G.LDC + col_of(G, 0, 1, g)]; };
+    auto dn = [&](int g) -> double { return df_value(Tot[(size_t)nt * G.LDC + col_of(G, 0, 1, g)]); };
     TaskOut o;
     if (vs >= 0) {
         o.vI = up0(0, vs); o.vQ = up0(1, vs); o.vU = up0(2, vs);
