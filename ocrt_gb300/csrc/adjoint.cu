@@ -128,12 +128,12 @@ __global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0)
     int s, h, g;
     decode_col_a(G, c, s, h, g);
     if (g >= d.n_ring) return;
-    float *F = W.F + tk.fld_off;
+    float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
     const float2 *Tot = W.Tot + tk.fld_off;
     for (int k = 0; k <= d.nt; ++k) {
         const size_t o = (size_t)k * G.LDC + c;
         const float2 t = Tot[o];
-        F[o] = (t.x - F[o]) + t.y;
+        split_store(FH, FL, o, ((t.x - FH[o]) - FL[o]) + t.y);
     }
 }
 
@@ -158,7 +158,8 @@ __global__ void k_fill_all(BatchBufs B, int t0, int nw, int it)
 // Transposed operators for the tcgen05 adjoint source: opsT[tl][cin][kk] =
 // Aop[kk][cin] for kk < COUT, 0 up to KP = COUT rounded up to 32.  32 x 32
 // tiles through shared memory.  Grid (task, CIN/32 tiles, KP/32 tiles), 32 x 8.
-__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT)
+__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsTH,
+                               float *opsTL)
 {
     __shared__ float tile[32][33];
     const int tl = blockIdx.x;
@@ -172,11 +173,18 @@ __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, con
         tile[yy][threadIdx.x] = (row < G.COUT && cin < G.CIN) ? A[(size_t)row * G.CIN + cin] : 0.f;
     }
     __syncthreads();
-    float *T = opsT + (size_t)tl * G.CIN * KP;
+    float *TH = opsTH + (size_t)tl * G.CIN * KP, *TL = opsTL + (size_t)tl * G.CIN * KP;
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
         const int cin = c0 + yy, kk = r0 + threadIdx.x;
-        if (cin < G.CIN && kk < KP) T[(size_t)cin * KP + kk] = tile[threadIdx.x][yy];
+        if (cin < G.CIN && kk < KP) split_store(TH, TL, (size_t)cin * KP + kk, tile[threadIdx.x][yy]);
     }
+}
+
+// tf32 (hi, lo) planes of the forward operators for the tensor-core contraction.
+__global__ void k_split_ops(const float *ops, float *hi, float *lo, size_t n)
+{
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+        split_store(hi, lo, e, ops[e]);
 }
 
 // a_1 = e.  One thread per adjoint task.
@@ -227,7 +235,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
     const size_t off = adj_off(tk, G, A.ncot, r);
     float *a = A.AF + off;
     float2 *At = A.ATot + off;
-    float *mj = A.AJ + off;
+    float *mjH = A.AJH + off, *mjL = A.AJL + off;
     float mi = 0.f, mt = 0.f;
     if (valid) {
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
@@ -265,7 +273,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                         mi = fmaxf(mi, fabsf(av[q]));
                         mt = fmaxf(mt, fabsf(t.x));
                         const float nu = av[q] + tv[q] * nup;
-                        mj[o] = ca[q] * nu + cb[q] * nup;
+                        split_store(mjH, mjL, o, ca[q] * nu + cb[q] * nup);
                         nup = nu;
                     }
                 }
@@ -302,7 +310,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                             mt = fmaxf(mt, fabsf(t.x));
                         }
                         const float nu = av[q] + tv[q] * nun;
-                        mj[o] = ca[q] * nu + cb[q] * nun;
+                        split_store(mjH, mjL, o, ca[q] * nu + cb[q] * nun);
                         nun = nu;
                     }
                 }
@@ -348,7 +356,7 @@ __global__ void __launch_bounds__(256) k_adj_source(BatchBufs B, WaveBufs W, Adj
     constexpr int KT = 16;
     __shared__ float Ms[KT][ST_M_TILE + 4];
     __shared__ float As[KT][ST_N_TILE + 4];
-    const float *mj = A.AJ + off;
+    const float *mjH = A.AJH + off, *mjL = A.AJL + off;
     const float *Aop = W.ops + tk.op_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     float acc[4][4] = {{0}};
@@ -356,7 +364,8 @@ __global__ void __launch_bounds__(256) k_adj_source(BatchBufs B, WaveBufs W, Adj
         for (int idx = threadIdx.x; idx < ST_M_TILE * KT; idx += 256) {
             const int lv = idx / KT, kk = idx - lv * KT;
             const int k = k0 + lv, row = kc + kk;
-            Ms[kk][lv] = (k <= nt && row < G.COUT) ? mj[(size_t)k * G.LDC + row] : 0.f;
+            const size_t o = (size_t)k * G.LDC + row;
+            Ms[kk][lv] = (k <= nt && row < G.COUT) ? mjH[o] + mjL[o] : 0.f;
         }
         for (int idx = threadIdx.x; idx < KT * ST_N_TILE; idx += 256) {
             const int kk = idx / ST_N_TILE, cc = idx - kk * ST_N_TILE;
@@ -420,10 +429,11 @@ __global__ void __launch_bounds__(256) k_adj_mol(BatchBufs B, WaveBufs W, AdjBuf
     const float *Ug = W.ops + tk.mol_off;
     for (int e = threadIdx.x; e < G.COUT * 24; e += blockDim.x) U[e] = Ug[e];
     const size_t off = adj_off(tk, G, A.ncot, r);
-    const float *mj = A.AJ + off + (size_t)k0 * G.LDC;
+    const float *mjH = A.AJH + off + (size_t)k0 * G.LDC, *mjL = A.AJL + off + (size_t)k0 * G.LDC;
     for (int e = threadIdx.x; e < nk * G.COUT; e += blockDim.x) {
         const int k = e / G.COUT, c = e - k * G.COUT;
-        Ms[k * G.COUT + c] = mj[(size_t)k * G.LDC + c];
+        const size_t o = (size_t)k * G.LDC + c;
+        Ms[k * G.COUT + c] = mjH[o] + mjL[o];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nk * 24; e += blockDim.x) {
@@ -525,15 +535,16 @@ __global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, Ad
             if (d.rough) {
                 // surface terms: wind derivative of the boundary operator and of
                 // the direct-beam seed, and the seed's optical-depth dependence
-                const float *Xs = W.F + tk.fld_off + (size_t)nt * G.LDC;
+                const float *XsH = W.FH + tk.fld_off + (size_t)nt * G.LDC, *XsL = W.FL + tk.fld_off + (size_t)nt * G.LDC;
+                auto Xs = [&](int col) -> double { return (double)XsH[col] + (double)XsL[col]; };
                 const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
                 const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
                 double acc = 0.0;
                 for (int i = 0; i < N; ++i) {
                     const double pw = pwm[i];
                     const float *Ri = RW + (size_t)i * 9;
-                    acc += pw * ((double)Ri[0] * Xs[col_of(G, 0, 1, i)] + (double)Ri[1] * Xs[col_of(G, 1, 1, i)] +
-                                 (double)Ri[2] * Xs[col_of(G, 2, 1, i)]);
+                    acc += pw * ((double)Ri[0] * Xs(col_of(G, 0, 1, i)) + (double)Ri[1] * Xs(col_of(G, 1, 1, i)) +
+                                 (double)Ri[2] * Xs(col_of(G, 2, 1, i)));
                 }
                 const double tdn = exp(-d.tau_total / d.mu0);
                 const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;

@@ -34,7 +34,7 @@ int g_timing = 0;
 enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SOURCE_TC, KC_MOL, KC_SCAN, KC_EXTRACT,
               KC_IPSS, KC_FINAL, KC_ADJ_SCAN, KC_ADJ_SOURCE, KC_ADJ_OTHER, KC_ADJ_TOTALS, KC_ADJ_GRAD, KC_N };
 const char *kc_names[KC_N] = {"setup", "phase_tables", "coxmunk_fourier", "primary", "source_gemm_simt",
-                              "source_gemm_tcgen05", "source_molecular_lowrank", "transport_scan", "extract", "ipss",
+                              "source_gemm_tcgen05", "source_molecular", "transport_scan", "extract", "ipss",
                               "finalize", "adjoint_scan", "adjoint_source", "adjoint_other", "adjoint_forward_totals",
                               "adjoint_gradients"};
 
@@ -209,23 +209,24 @@ struct Group {
     double *kappa = nullptr, *taudir = nullptr;
     int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
-    float *F = nullptr, *J = nullptr, *ops = nullptr, *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
+    float *FH = nullptr, *FL = nullptr, *J = nullptr, *ops = nullptr, *opsH = nullptr, *opsL = nullptr;
+    float *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     float2 *Tot = nullptr;
     bool use_tc = false;
-    CUtensorMap mapF, mapA;
+    CUtensorMap mapFH, mapFL, mapAH, mapAL;
     // per-layer overrides and the adjoint (ocrt_gb_solve_batch_adjoint)
     bool any_layers = false;
     int ncot = 0, ntmax = 0;
     double *ldt = nullptr, *lss = nullptr, *cot = nullptr, *lamd = nullptr, *gout = nullptr,
            *grad = nullptr;
-    float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJ = nullptr,
+    float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJH = nullptr, *AJL = nullptr,
           *Abc = nullptr;
     float2 *ATot = nullptr;
     TaskState *Ast = nullptr;
     int *acnt = nullptr, *awork = nullptr;
-    float *opsT = nullptr;            // transposed operators for the tcgen05 adjoint source
+    float *opsTH = nullptr, *opsTL = nullptr;   // transposed operator planes for the tcgen05 adjoint source
     bool use_tc_adj = false;
-    CUtensorMap mapAJ, mapOT;
+    CUtensorMap mapJH, mapJL, mapTH, mapTL;
     int gstride = 0, kstride = 0, grad_stride = 0;
 };
 
@@ -275,9 +276,9 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
-                    g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
-                    g.Abc, g.Ast, g.acnt, g.awork, g.opsT};
+                    g.err, g.FH, g.FL, g.J, g.ops, g.opsH, g.opsL, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJH,
+                    g.AJL, g.Abc, g.Ast, g.acnt, g.awork, g.opsTH, g.opsTL};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -371,9 +372,9 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t K = d.nt + 1, nm = d.M + 1;
         const bool rough = (d.surface == 2 && d.wind > 0.0);
         const size_t pf = nm * K * G.LDC;
-        const size_t po = (nm + std::min<size_t>(nm, 3)) * op_elems;
+        const size_t po = (nm + 2 * std::min<size_t>(nm, 3)) * op_elems;
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
-        size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        size_t pb = pf * 20 + po * 12 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 16 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)G.CIN * ((G.COUT + 31) & ~31) * 4;
@@ -386,7 +387,12 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         for (size_t m = 0; m < nm; ++m) {
             tk[m].fld_off = (long long)w.fld; w.fld += K * G.LDC;
             tk[m].op_off = (long long)w.ops; w.ops += op_elems;
-            if (m <= 2) { tk[m].mol_off = (long long)w.ops; w.ops += op_elems; } else tk[m].mol_off = -1;
+            if (m <= 2) {
+                tk[m].mol_off = (long long)w.ops; w.ops += op_elems;
+                tk[m].uv_off = (long long)w.ops; w.ops += op_elems;
+            } else {
+                tk[m].mol_off = tk[m].uv_off = -1;
+            }
             if (rough) { tk[m].srf_off = (long long)w.srf; w.srf += (size_t)G.NR * G.N * 9 + (size_t)G.NR * 9; }
             else tk[m].srf_off = -1;
             tk[m].has_mol = m <= 2;
@@ -418,7 +424,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.work, 4 * ((size_t)g.max_orders + 2))) || (rc = alloc(g.err, 1)) ||
         (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
         (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
-        (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) || (rc = alloc(g.Tot, g.wave_fld)) ||
+        (rc = alloc(g.FH, g.wave_fld)) || (rc = alloc(g.FL, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
+        (rc = alloc(g.Tot, g.wave_fld)) ||
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
         (rc = alloc(g.srf, g.wave_srf)) ||
@@ -433,7 +440,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         if ((rc = up(g.cot, hcot)) || (rc = alloc(g.lamd, (size_t)g.P * (G.N + 2))) ||
             (rc = alloc(g.dTc, g.ncoef)) || (rc = alloc(g.dCa, g.ncoef)) || (rc = alloc(g.dCb, g.ncoef)) ||
             (rc = alloc(g.srfW, g.wave_srf)) || (rc = alloc(g.AF, g.wave_fld * ncot)) ||
-            (rc = alloc(g.AJ, g.wave_fld * ncot)) || (rc = alloc(g.ATot, g.wave_fld * ncot)) ||
+            (rc = alloc(g.AJH, g.wave_fld * ncot)) || (rc = alloc(g.AJL, g.wave_fld * ncot)) ||
+            (rc = alloc(g.ATot, g.wave_fld * ncot)) ||
             (rc = alloc(g.Abc, na * G.NR * 3)) || (rc = alloc(g.Ast, na)) ||
             (rc = alloc(g.acnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.awork, (size_t)g.max_orders + 2)) ||
             (rc = alloc(g.gout, na * g.gstride)) ||
@@ -446,14 +454,20 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     // built on the device (k_primary, k_scan). ----
     g.use_tc = tc_supported(G) && !force_simt();
     if (g.use_tc) {
-        g.use_tc = make_map(&g.mapF, g.F, g.wave_fld / G.LDC, G.LDC, 128) &&
-                   make_map(&g.mapA, g.ops, g.wave_ops / G.CIN, G.CIN, G.NP);
+        if ((rc = alloc(g.opsH, g.wave_ops)) || (rc = alloc(g.opsL, g.wave_ops))) return rc;
+        g.use_tc = make_map(&g.mapFH, g.FH, g.wave_fld / G.LDC, G.LDC, 128) &&
+                   make_map(&g.mapFL, g.FL, g.wave_fld / G.LDC, G.LDC, 128) &&
+                   make_map(&g.mapAH, g.opsH, g.wave_ops / G.CIN, G.CIN, G.NP) &&
+                   make_map(&g.mapAL, g.opsL, g.wave_ops / G.CIN, G.CIN, G.NP);
     }
     if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
         const int KP = (G.COUT + 31) & ~31;
-        if ((rc = alloc(g.opsT, (size_t)g.wave_tasks * G.CIN * KP))) return rc;
-        g.use_tc_adj = make_map(&g.mapAJ, g.AJ, g.wave_fld * ncot / G.LDC, G.LDC, 128) &&
-                       make_map(&g.mapOT, g.opsT, (size_t)g.wave_tasks * G.CIN, KP, G.CIN);
+        if ((rc = alloc(g.opsTH, (size_t)g.wave_tasks * G.CIN * KP)) ||
+            (rc = alloc(g.opsTL, (size_t)g.wave_tasks * G.CIN * KP))) return rc;
+        g.use_tc_adj = make_map(&g.mapJH, g.AJH, g.wave_fld * ncot / G.LDC, G.LDC, 128) &&
+                       make_map(&g.mapJL, g.AJL, g.wave_fld * ncot / G.LDC, G.LDC, 128) &&
+                       make_map(&g.mapTH, g.opsTH, (size_t)g.wave_tasks * G.CIN, KP, G.CIN) &&
+                       make_map(&g.mapTL, g.opsTL, (size_t)g.wave_tasks * G.CIN, KP, G.CIN);
     }
     for (Wave &w : g.waves) {
         w.n_simt = g.use_tc ? 0 : w.t1 - w.t0;
@@ -481,7 +495,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
 AdjBufs make_adj(Group &g)
 {
     AdjBufs A;
-    A.ncot = g.ncot; A.AF = g.AF; A.AJ = g.AJ; A.ATot = g.ATot; A.bc = g.Abc; A.st = g.Ast; A.acnt = g.acnt;
+    A.ncot = g.ncot; A.AF = g.AF; A.AJH = g.AJH; A.AJL = g.AJL; A.ATot = g.ATot; A.bc = g.Abc; A.st = g.Ast; A.acnt = g.acnt;
     A.cot = g.cot; A.gout = g.gout; A.gstride = g.gstride; A.kstride = g.kstride;
     A.dTc = g.dTc; A.dCa = g.dCa; A.dCb = g.dCb; A.srfW = g.srfW; A.grad = g.grad; A.grad_stride = g.grad_stride;
     A.awork = g.awork;
@@ -502,13 +516,18 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     LAUNCH(plan, KC_ADJ_TOTALS, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
     if (w.n_simt) LAUNCH(plan, KC_ADJ_TOTALS, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
     if (w.n_tc)
-        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(g.mapF, g.mapA, B, W, G, w.t0, it, mtiles));
-    if (w.n_mol)
+        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it,
+                                                                              mtiles, 0));
+    if (w.n_mol && w.n_tc)
+        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), 256, tc_smem, st>>>(
+                   g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it, mtiles, 1));
+    else if (w.n_mol)
         LAUNCH(plan, KC_ADJ_TOTALS, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                    B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
     // adjoint successive orders
     CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.AJ, 0, sizeof(float) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.AJH, 0, sizeof(float) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.AJL, 0, sizeof(float) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.ATot, 0, sizeof(float2) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
@@ -517,7 +536,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     const int amt = (g.ncot * w.Kmax + 127) / 128;
     if (g.use_tc_adj)
         LAUNCH(plan, KC_ADJ_OTHER, k_op_transpose<<<dim3(nw, (G.CIN + 31) / 32, KP / 32), dim3(32, 8), 0, st>>>(
-                   g.tasks, w.t0, nw, G, g.ops, g.opsT));
+                   g.tasks, w.t0, nw, G, g.ops, g.opsTH, g.opsTL));
     const AdjBufs A = make_adj(g);
     LAUNCH(plan, KC_ADJ_OTHER, k_adj_init<<<(na + 127) / 128, 128, 0, st>>>(B, A, G, w.t0, na));
     const dim3 agrid(na, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.LDC + ST_N_TILE - 1) / ST_N_TILE);
@@ -531,7 +550,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
         }
         if (g.use_tc_adj)
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source_tc<<<std::min(nw * amt, g_nsm), 256, tc_adj_smem_bytes(G), st>>>(
-                       g.mapAJ, g.mapOT, B, W, A, G, w.t0, j, amt, nw));
+                       g.mapJH, g.mapJL, g.mapTH, g.mapTL, B, W, A, G, w.t0, j, amt, nw));
         else
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source<<<agrid, 256, 0, st>>>(B, W, A, G, w.t0));
         if (w.n_mol)
@@ -577,7 +596,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     B.mol_cnt = g.mol_cnt; B.work = g.work;
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     WaveBufs W;
-    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.pvec = g.pvec;
+    W.FH = g.FH; W.FL = g.FL; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.opsH = g.opsH; W.opsL = g.opsL;
+    W.pvec = g.pvec;
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     const int poll = 4;
@@ -592,6 +612,11 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
         LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, sizeof(float) * 4 * ((size_t)g.Lmax + 1), st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
                                                    g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
+        if (g.use_tc) {
+            LAUNCH(plan, KC_TABLES, k_mol_dense<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.Lmax, g.Bp, g.Br, g.Bt,
+                                                                     g.gw, g.ops));
+            LAUNCH(plan, KC_TABLES, k_split_ops<<<4 * g_nsm, 256, 0, st>>>(g.ops, g.opsH, g.opsL, w.ops));
+        }
         if (w.any_rough) {
             const bool dw = g.ncot > 0;
             const int np = w.p1 - w.p0;
@@ -617,8 +642,11 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
                 LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
             if (w.n_tc)
                 LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(
-                           g.mapF, g.mapA, B, W, G, w.t0, it, mtiles));
-            if (w.n_mol)
+                           g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it, mtiles, 0));
+            if (w.n_mol && w.n_tc)
+                LAUNCH(plan, KC_MOL, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), 256, tc_smem, st>>>(
+                           g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it, mtiles, 1));
+            else if (w.n_mol)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
             LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, 0, st>>>(B, W, G, w.t0, it));
@@ -855,7 +883,10 @@ int ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, doubl
                 const int sc = g.use_tc ? KC_SOURCE_TC : KC_SOURCE;
                 plan->flops[sc] += ords * 72.0 * N * N * K;
                 plan->bytes[sc] += ords * (K * 6 * N + K * 6 * NR + 36.0 * N * NR) * 4.0;
-                if (tk.has_mol) {
+                if (tk.has_mol && g.use_tc) {          // dense U V pass on the tensor cores
+                    plan->flops[KC_MOL] += ords * 72.0 * N * N * K;
+                    plan->bytes[KC_MOL] += ords * (K * 6 * N + 2.0 * K * 6 * NR + 36.0 * N * NR) * 4.0;
+                } else if (tk.has_mol) {               // rank-24 form on CUDA cores
                     plan->flops[KC_MOL] += ords * 2.0 * K * 24.0 * (N + 6 * NR);
                     plan->bytes[KC_MOL] += ords * (K * 6 * N + 2.0 * K * 6 * NR) * 4.0;
                 }

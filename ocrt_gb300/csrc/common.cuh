@@ -18,6 +18,7 @@
 // [0, 6N) contiguous and NP >= 6N + 6 output rows (multiple of 16).
 #pragma once
 #include <cstdint>
+#include <cstring>
 
 #define OCRT_PI 3.14159265358979323846
 #define OCRT_MAX_N 64
@@ -52,7 +53,8 @@ struct TaskDev {
     int pix, m, K, has_mol;
     long long fld_off;      // wave-relative offset of F/J/Tot (K * LDC entries)
     long long op_off;       // wave-relative offset of the aerosol operator (NP * CIN)
-    long long mol_off;      // wave-relative offset of the molecular operator, -1 if none
+    long long mol_off;      // wave-relative offset of the molecular operator factor U [COUT][24], -1 if none
+    long long uv_off;       // wave-relative offset of the dense molecular operator U V [NP][CIN], -1 if none
     long long srf_off;      // wave-relative offset of the surface kernels (NR*N*9 + NR*9), -1 if none
 };
 
@@ -115,3 +117,23 @@ __host__ __device__ inline float2 df_add(float2 a, float b)
 }
 
 __host__ __device__ inline double df_value(float2 a) { return (double)a.x + (double)a.y; }
+
+// Fields that feed the tensor-core contraction are stored as two planes of
+// tf32 values: hi = RN_tf32(v), lo = RN_tf32(v - hi), so each plane is exact
+// as an MMA operand and hi + lo carries v to ~2^-22 relative.  Readers that
+// need the value add the planes.
+__host__ __device__ inline float round_tf32f(float v)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
+#else
+    unsigned u; memcpy(&u, &v, 4); u = (u + 0x1000u) & 0xFFFFE000u; float r; memcpy(&r, &u, 4); return r;
+#endif
+}
+
+__host__ __device__ inline void split_store(float *hi, float *lo, size_t o, float v)
+{
+    const float h = round_tf32f(v);
+    hi[o] = h;
+    lo[o] = round_tf32f(v - h);
+}

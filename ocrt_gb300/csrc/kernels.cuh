@@ -37,9 +37,11 @@ __global__ void k_level_float(const PixDev *px, int P, const double *xd, const d
 #define ST_M_TILE 64
 #define ST_N_TILE 64
 struct WaveBufs {
-    float *F, *J;          // fields, wave-relative by TaskDev::fld_off
+    float *FH, *FL;        // field of the current order as tf32 (hi, lo) planes, wave-relative by TaskDev::fld_off
+    float *J;              // source of the current order
     float2 *Tot;           // order totals (hi, lo) pairs
-    float *ops;            // operators, wave-relative
+    float *ops;            // operators, wave-relative (FP32)
+    float *opsH, *opsL;    // the same operators as tf32 (hi, lo) planes, for the tensor-core contraction
     float *pvec, *fvec;    // per wave-task primary and flat-beam vectors
     float *srf;            // rough surface kernels, wave-relative
 };
@@ -66,7 +68,8 @@ struct BatchBufs {
 // adjoint.cu
 struct AdjBufs {
     int ncot;              // cotangent rows per pixel; adjoint task = wave task * ncot + row
-    float *AF, *AJ;        // adjoint field a_j and transposed-transport output muJ (wave-relative, x ncot)
+    float *AF;             // adjoint field a_j (wave-relative, x ncot)
+    float *AJH, *AJL;      // transposed-transport output muJ as tf32 (hi, lo) planes
     float2 *ATot;          // adjoint total (hi, lo) pairs
     float *bc;             // mu_bc per adjoint task [NR][3]
     TaskState *st;         // per adjoint task
@@ -93,14 +96,20 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
 size_t adj_mol_smem_bytes(const Geom &G);
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
+__global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
+                            const float *Bt, const double *gw, float *ops);
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
-__global__ void k_source_tc(const __grid_constant__ CUtensorMap mapF, const __grid_constant__ CUtensorMap mapA,
-                            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
-__global__ void k_adj_source_tc(const __grid_constant__ CUtensorMap mapJ, const __grid_constant__ CUtensorMap mapAT,
+__global__ void k_source_tc(const __grid_constant__ CUtensorMap mFH, const __grid_constant__ CUtensorMap mFL,
+                            const __grid_constant__ CUtensorMap mAH, const __grid_constant__ CUtensorMap mAL,
+                            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode);
+__global__ void k_adj_source_tc(const __grid_constant__ CUtensorMap mJH, const __grid_constant__ CUtensorMap mJL,
+                                const __grid_constant__ CUtensorMap mTH, const __grid_constant__ CUtensorMap mTL,
                                 BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
-__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
+__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsTH,
+                               float *opsTL);
+__global__ void k_split_ops(const float *ops, float *hi, float *lo, size_t n);
 size_t coxmunk_smem_bytes(int nphi, bool dw);
 size_t tc_smem_bytes(const Geom &G);
 bool tc_supported(const Geom &G);

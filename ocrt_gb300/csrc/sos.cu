@@ -81,7 +81,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     const int nt = d.nt;
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
     const double aP = pv[c], mP = pv[G.LDC + c];
-    float *F = W.F + tk.fld_off;
+    float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
     float2 *Tot = W.Tot + tk.fld_off;
     const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off, *hh = B.h + d.lev_off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
@@ -119,7 +119,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     auto store = [&](int k, float I) {
         float2 t = make_float2(I, 0.f);
         if (d.rough && h == 0) t = df_add(t, rough_seed(tk, W, B, d, G, fs_tdn, k, g, s));
-        F[(size_t)k * G.LDC + c] = t.x;
+        split_store(FH, FL, (size_t)k * G.LDC + c, t.x);
         Tot[(size_t)k * G.LDC + c] = t;
     };
     if (h == 0) {
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
     if (k0 > nt || c0 >= G.COUT) return;
     __shared__ float Fs[ST_K][ST_M + 4];
     __shared__ float As[ST_K][ST_N + 4];
-    const float *F = W.F + tk.fld_off;
+    const float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
     const float *A = W.ops + tk.op_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     float accA[4][4] = {{0}};
@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
         for (int idx = threadIdx.x; idx < ST_M * ST_K; idx += 256) {
             const int lv = idx / ST_K, kk = idx - lv * ST_K;
             const int k = k0 + lv, ci = kc + kk;
-            Fs[kk][lv] = (k <= nt && ci < G.CIN) ? F[(size_t)k * G.LDC + in_to_col(G, ci)] : 0.f;
+            const size_t o = (size_t)k * G.LDC + in_to_col(G, ci);
+            Fs[kk][lv] = (k <= nt && ci < G.CIN) ? FH[o] + FL[o] : 0.f;
         }
         for (int idx = threadIdx.x; idx < ST_K * ST_N; idx += 256) {
             const int cc = idx / ST_K, kk = idx - cc * ST_K;
@@ -240,10 +241,11 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
     }
     const float *Ug = W.ops + tk.mol_off;
     for (int e = threadIdx.x; e < G.COUT * 24; e += blockDim.x) U[e] = Ug[e];
-    const float *F = W.F + tk.fld_off + (size_t)k0 * G.LDC;
+    const float *FH = W.FH + tk.fld_off + (size_t)k0 * G.LDC, *FL = W.FL + tk.fld_off + (size_t)k0 * G.LDC;
     for (int e = threadIdx.x; e < nk * G.CIN; e += blockDim.x) {
         const int k = e / G.CIN, ci = e - k * G.CIN;
-        Fs[k * G.CIN + ci] = F[(size_t)k * G.LDC + ci];
+        const size_t o = (size_t)k * G.LDC + ci;
+        Fs[k * G.CIN + ci] = FH[o] + FL[o];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nk * 24; e += blockDim.x) {
@@ -265,6 +267,38 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
         for (int r = 0; r < 24; ++r) acc = fmaf(u[r], x[r], acc);
         J[(size_t)(k0 + k) * G.LDC + c] += B.lvf[3 * (d.lev_off + k0 + k) + 1] * acc;
     }
+    }
+}
+
+// Dense molecular operator for the tensor-core contraction:
+// UV[c][bN + i] = sum_f U[c][4b + f] fv[f][i], fv[f][i] = w_i {1, P2m, R2m, T2m}(mu_i),
+// so that UV F equals U (V F) of k_mol_lowrank.  Rows COUT..NP-1 are zero.
+// One block per molecular task of the wave.
+__global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
+                            const float *Bt, const double *gw, float *ops)
+{
+    const int tl = blockIdx.x;
+    if (tl >= nw) return;
+    const TaskDev tk = tasks[t0 + tl];
+    if (tk.uv_off < 0) return;
+    const int N = G.N;
+    __shared__ float fv[4 * OCRT_MAX_N];
+    const size_t gb = (size_t)tk.m * (L + 1) * N + (size_t)2 * N;    // degree-2 row of mode m
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float w = (float)gw[i];
+        fv[i] = w; fv[N + i] = w * Bp[gb + i]; fv[2 * N + i] = w * Br[gb + i]; fv[3 * N + i] = w * Bt[gb + i];
+    }
+    __syncthreads();
+    const float *U = ops + tk.mol_off;
+    float *UV = ops + tk.uv_off;
+    for (int e = threadIdx.x; e < G.NP * G.CIN; e += blockDim.x) {
+        const int c = e / G.CIN, ci = e - c * G.CIN, b = ci / N, i = ci - b * N;
+        float v = 0.f;
+        if (c < G.COUT) {
+            const float *u = U + (size_t)c * 24 + 4 * b;
+            v = u[0] * fv[i] + u[1] * fv[N + i] + u[2] * fv[2 * N + i] + u[3] * fv[3 * N + i];
+        }
+        UV[e] = v;
     }
 }
 
@@ -316,13 +350,14 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
     int s = 0, h = 0, g = 0;
     if (c < G.COUT) decode_col(G, c, s, h, g);
     const bool valid = c < G.COUT && g < d.n_ring;
-    float *F = W.F + tk.fld_off;
+    float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
     const float *J = W.J + tk.fld_off;
     float2 *Tot = W.Tot + tk.fld_off;
     // ---- surface boundary condition from the previous order's BOA downward field
     float bc = 0.f;
     if (valid && h == 0 && d.surf_on) {
-        const float *Fb = F + (size_t)nt * G.LDC;
+        const float *FbH = FH + (size_t)nt * G.LDC, *FbL = FL + (size_t)nt * G.LDC;
+        auto Fb = [&](int col) -> float { return FbH[col] + FbL[col]; };
         if (d.rough) {
             const float *R = W.srf + tk.srf_off + (size_t)g * N * 9 + s * 3;
             const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
@@ -330,13 +365,13 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
             for (int i = 0; i < N; ++i) {
                 const float pw = pwm[i];
                 const float *Ri = R + (size_t)i * 9;
-                acc += pw * (Ri[0] * Fb[col_of(G, 0, 1, i)] + Ri[1] * Fb[col_of(G, 1, 1, i)] +
-                             Ri[2] * Fb[col_of(G, 2, 1, i)]);
+                acc += pw * (Ri[0] * Fb(col_of(G, 0, 1, i)) + Ri[1] * Fb(col_of(G, 1, 1, i)) +
+                             Ri[2] * Fb(col_of(G, 2, 1, i)));
             }
             bc = acc;
         } else {
             const float *MF = B.frs + ((size_t)tk.pix * NR + g) * 9 + s * 3;
-            bc = MF[0] * Fb[col_of(G, 0, 1, g)] + MF[1] * Fb[col_of(G, 1, 1, g)] + MF[2] * Fb[col_of(G, 2, 1, g)];
+            bc = MF[0] * Fb(col_of(G, 0, 1, g)) + MF[1] * Fb(col_of(G, 1, 1, g)) + MF[2] * Fb(col_of(G, 2, 1, g));
         }
     }
     __syncthreads();
@@ -348,7 +383,7 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
         auto put = [&](int k, float I) {
             const size_t o = (size_t)k * G.LDC + c;
-            F[o] = I;
+            split_store(FH, FL, o, I);
             const float2 t = df_add(Tot[o], I);
             Tot[o] = t;
             mi = fmaxf(mi, fabsf(I));
@@ -382,7 +417,7 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
                         I = tv[q] * I + av[q] * jv[q] + bv[q] * Jn;
                         Jn = jv[q];
                         const size_t o = (size_t)k * G.LDC + c;
-                        F[o] = I;
+                        split_store(FH, FL, o, I);
                         const float2 t = df_add(ov[q], I);
                         Tot[o] = t;
                         mi = fmaxf(mi, fabsf(I));
@@ -415,7 +450,7 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
                         I = tv[q] * I + av[q] * jv[q] + bv[q] * Jp;
                         Jp = jv[q];
                         const size_t o = (size_t)k * G.LDC + c;
-                        F[o] = I;
+                        split_store(FH, FL, o, I);
                         const float2 t = df_add(ov[q], I);
                         Tot[o] = t;
                         mi = fmaxf(mi, fabsf(I));
