@@ -31,6 +31,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from ocrt_gb300 import _abi as A  # noqa: E402
+from ocrt_gb300.replicas import max_over_ranks  # noqa: E402
 from synthetic import batched_forward_pixels, hg_aerosol_moments  # noqa: E402
 
 METRIC = "pixel-solves/s"
@@ -285,11 +286,7 @@ def run_ours(args, rank, world):
     og.set_timing(False)
     res = plan.results(sp)
     om = float(np.sum(res["order_modes"]))
-    ms_step = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(total_ms / args.steps)
     value = args.pixels * world / (ms_step / 1e3)
 
     # ---- roofline of the dominant kernel ----
@@ -330,11 +327,7 @@ def run_ours(args, rank, world):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         r_e2e = og.solve_batch(cases, opts, aers)
-    t_e2e = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([t_e2e], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
     h2d = args.pixels * (C.sizeof(A.Case) + C.sizeof(A.Opts) + C.sizeof(A.Aerosol) + 4 * 8 * (L_AER + 1))
     d2h = args.pixels * C.sizeof(A.Result)
     e2e = {"value": args.pixels * world / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
@@ -401,11 +394,7 @@ def run_adjoint(args, og, torch, stream, sp, barrier, world):
             tot += e0.elapsed_time(e1)
             for k, v in plan.kernel_stats().items():
                 ks[k] = ks.get(k, 0.0) + v["ms"]
-        ms = tot / args.steps
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(tot / args.steps)
         return ms, {k: v / args.steps for k, v in sorted(ks.items(), key=lambda kv: -kv[1]) if v > 0}
 
     og.set_timing(True)
