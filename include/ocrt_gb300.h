@@ -194,6 +194,34 @@ int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *opts,
                                const ocrt_aerosol *aer, ocrt_result *out,
                                void *stream);
 
+/* ---- angle-grid LUT mode ------------------------------------------------
+ * Replaces rt_solve_case_pol_lut (rt_solver.h:207-210) and its
+ * rt_lut_grid_out_t (rt_types.h:805-846): one SOS per case, then the TOA
+ * reflectance at every (vza, raa) of a grid.  Per Fourier mode the upwelling
+ * TOA field is sampled at each grid vza by monotone cubic (PCHIP) interpolation
+ * over the ring nodes (linear outside them), the modes are summed at each raa,
+ * and IPSS kappa (when pssa) and the direct sunglint (rough ocean) are applied
+ * per grid direction.  Arrays are caller-allocated; outputs are row-major
+ * [iv * n_raa + ir].  The case's own vza/raa give the result in `out` as usual
+ * (the reference CLI passes vza = raa = 0 for a grid run). */
+typedef struct {
+    int n_vza;
+    const double *vza_deg;     /* [n_vza], each in [0, 90) */
+    int n_raa;
+    const double *raa_deg;     /* [n_raa], public relative azimuth */
+    double *rho_I, *rho_Q, *rho_U;                      /* [n_vza * n_raa] */
+    double *T_diff_dn_dir, *T_sg_up_dir, *T_total_up_dir; /* optional (NULL to skip) */
+    double T_dir_dn, T_diff_dn_hemi;                    /* filled: case-level scalars */
+} ocrt_lut;
+
+int ocrt_gb_solve_case_lut(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                           ocrt_result *out, ocrt_lut *lut);
+/* n cases, each with its own grid (luts[i]); one device pass. */
+int ocrt_gb_solve_batch_lut(int n, const ocrt_case *cases,
+                            const ocrt_opts *opts, int opts_per_case,
+                            const ocrt_aerosol *aer, int aer_per_case,
+                            ocrt_lut *luts, ocrt_result *out, void *stream);
+
 /* ---- per-layer parameters and the adjoint ------------------------------
  * No counterpart in the reference (its solve API takes no per-layer inputs
  * and has no derivatives).  Layer l (0-based, l < n_layers) spans levels l

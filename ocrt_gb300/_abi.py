@@ -106,6 +106,43 @@ class LayersHolder:
         self.struct = Layers(n_layers=int(n_layers), dtau=ptr(self.dtau), ssa=ptr(self.ssa))
 
 
+class Lut(C.Structure):
+    _fields_ = [("n_vza", C.c_int), ("vza_deg", C.POINTER(C.c_double)),
+                ("n_raa", C.c_int), ("raa_deg", C.POINTER(C.c_double)),
+                ("rho_I", C.POINTER(C.c_double)), ("rho_Q", C.POINTER(C.c_double)),
+                ("rho_U", C.POINTER(C.c_double)), ("T_diff_dn_dir", C.POINTER(C.c_double)),
+                ("T_sg_up_dir", C.POINTER(C.c_double)), ("T_total_up_dir", C.POINTER(C.c_double)),
+                ("T_dir_dn", C.c_double), ("T_diff_dn_hemi", C.c_double)]
+
+
+LUT_FIELDS = ("rho_I", "rho_Q", "rho_U", "T_diff_dn_dir", "T_sg_up_dir", "T_total_up_dir")
+
+
+class LutHolder:
+    """A (vza, raa) grid and its caller-owned output arrays (numpy), bound to a Lut struct."""
+
+    def __init__(self, vza_deg, raa_deg):
+        import numpy as np
+        self.vza = np.ascontiguousarray(np.asarray(vza_deg, dtype=np.float64))
+        self.raa = np.ascontiguousarray(np.asarray(raa_deg, dtype=np.float64))
+        n = self.vza.size * self.raa.size
+        self.out = {k: np.zeros(n) for k in LUT_FIELDS}
+        P = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self.struct = Lut(n_vza=self.vza.size, vza_deg=P(self.vza), n_raa=self.raa.size, raa_deg=P(self.raa),
+                          **{k: P(v) for k, v in self.out.items()}, T_dir_dn=0.0, T_diff_dn_hemi=0.0)
+
+    def grid(self, key):
+        return self.out[key].reshape(self.vza.size, self.raa.size)
+
+
+def lut_grid_reference_cli(vza_step=2.5, raa_step=2.5, vza_max=85.0):
+    """The grid of the reference CLI's LUT mode (main.c:3794-3804)."""
+    import numpy as np
+    n_vza = int(vza_max / vza_step) + 1
+    n_raa = int(360.0 / raa_step)
+    return np.arange(n_vza) * vza_step, np.arange(n_raa) * raa_step
+
+
 RESULT_FIELDS = [f for f, _ in Result._fields_]
 
 

@@ -25,11 +25,14 @@
 
 int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
                                   const ocrt_layers *layers, ocrt_result *out, ocrt_diag *diag);
+static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                      const ocrt_layers *layers, ocrt_lut *lut, ocrt_result *out, ocrt_diag *diag);
 
 #define PI 3.14159265358979323846
 #define DEPOL 0.0279                  /* rt_solver.c:646 */
 #define Z_TOP_KM 100.0                /* rt_atm.c:219, 306 */
 #define MAX_RING 130
+#define MAX_M1 256                    /* Fourier modes 0..255 */
 #define DEDUP_TOL 1.0e-12             /* rt_angle_grid.h:12 */
 
 /* ======================================================================
@@ -1010,6 +1013,57 @@ static double interp_pos(const double *mu_pos, const double *vals, int n, double
     return (1.0 - t) * vals[jl - 1] + t * vals[jh - 1];
 }
 
+/* Monotone cubic (PCHIP) sample of ring values at mu (rt_solver.c:435-481,
+ * the Fritsch-Carlson method with the weighted-harmonic interior slope and
+ * the three-point one-sided edge slope with its monotonicity clamp).  The
+ * bracket is that of interp_pos; outside the node range, or with fewer than
+ * four nodes, the linear sample is returned. */
+static double pchip_slope_interior(double h0, double h1, double s0, double s1)
+{
+    if (s0 == 0.0 || s1 == 0.0 || (s0 > 0.0) != (s1 > 0.0)) return 0.0;
+    const double w1 = 2.0 * h1 + h0, w2 = h1 + 2.0 * h0;
+    return (w1 + w2) / (w1 / s0 + w2 / s1);
+}
+
+static double pchip_slope_edge(double h0, double h1, double s0, double s1)
+{
+    double d = ((2.0 * h0 + h1) * s0 - h0 * s1) / (h0 + h1);
+    if (d == 0.0 || s0 == 0.0 || (d > 0.0) != (s0 > 0.0)) {
+        if (s0 == 0.0 || (d > 0.0) != (s0 > 0.0)) d = 0.0;
+    } else if (((s0 > 0.0) != (s1 > 0.0)) && fabs(d) > 3.0 * fabs(s0)) {
+        d = 3.0 * s0;
+    }
+    return d;
+}
+
+static double pchip_pos(const double *mu_pos, const double *vals, int n, double mu)
+{
+    int jh = 1;
+    while (jh < n && mu_pos[jh - 1] < mu) jh++;
+    const int jl = jh - 1;
+    if (jl < 1 || jh > n || n < 4) return interp_pos(mu_pos, vals, n, mu);
+    const double x1 = mu_pos[jl - 1], x2 = mu_pos[jh - 1], y1 = vals[jl - 1], y2 = vals[jh - 1];
+    const double h = x2 - x1, sl = (y2 - y1) / h;
+    double d1, d2;
+    if (jl == 1) {
+        const double x3 = mu_pos[jh], s2 = (vals[jh] - y2) / (x3 - x2);
+        d1 = pchip_slope_edge(h, x3 - x2, sl, s2);
+        d2 = pchip_slope_interior(h, x3 - x2, sl, s2);
+    } else if (jh == n) {
+        const double x0 = mu_pos[jl - 2], s0 = (y1 - vals[jl - 2]) / (x1 - x0);
+        d1 = pchip_slope_interior(x1 - x0, h, s0, sl);
+        d2 = pchip_slope_edge(h, x1 - x0, sl, s0);
+    } else {
+        const double x0 = mu_pos[jl - 2], x3 = mu_pos[jh];
+        const double s0 = (y1 - vals[jl - 2]) / (x1 - x0), s2 = (vals[jh] - y2) / (x3 - x2);
+        d1 = pchip_slope_interior(x1 - x0, h, s0, sl);
+        d2 = pchip_slope_interior(h, x3 - x2, sl, s2);
+    }
+    const double t = (mu - x1) / h, t2 = t * t, t3 = t2 * t;
+    return (2.0 * t3 - 3.0 * t2 + 1.0) * y1 + (t3 - 2.0 * t2 + t) * h * d1 + (-2.0 * t3 + 3.0 * t2) * y2 +
+           (t3 - t2) * h * d2;
+}
+
 static double recon_cos(const double *v, int M, double dphi)
 {
     const double phi = dphi + PI;
@@ -1167,6 +1221,24 @@ int ocrt_oracle_solve_case(const ocrt_case *cs, const ocrt_opts *op,
 int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
                                   const ocrt_layers *layers, ocrt_result *out, ocrt_diag *diag)
 {
+    return solve_impl(cs, op, aer_in, layers, NULL, out, diag);
+}
+
+/* Angle-grid LUT (rt_solve_case_pol_lut, rt_solver.c:870-900, 1025-1045,
+ * 1276-1424). */
+int ocrt_oracle_solve_case_lut(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                               ocrt_result *out, ocrt_lut *lut)
+{
+    if (!lut || lut->n_vza <= 0 || lut->n_raa <= 0 || !lut->vza_deg || !lut->raa_deg || !lut->rho_I ||
+        !lut->rho_Q || !lut->rho_U) return -1;
+    for (int i = 0; i < lut->n_vza; ++i)
+        if (!(lut->vza_deg[i] >= 0.0 && lut->vza_deg[i] < 90.0)) return -1;
+    return solve_impl(cs, op, aer_in, NULL, lut, out, NULL);
+}
+
+static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                      const ocrt_layers *layers, ocrt_lut *lut, ocrt_result *out, ocrt_diag *diag)
+{
     int rc = check_args(cs, op, aer_in);
     if (rc) return rc;
     if (!out) return -1;
@@ -1251,6 +1323,8 @@ int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, cons
                              cs->n_water, cs->q_convention, Ks);
     }
     double *I_dn_boa = calloc((size_t)(M + 1) * n, sizeof(double));
+    const int nvg = lut ? lut->n_vza : 0;
+    double *lut_samp = lut ? calloc((size_t)(M + 1) * nvg * 3, sizeof(double)) : NULL;   /* [m][iv][IQU] */
     double *vI = calloc((size_t)(M + 1) * 3, sizeof(double));
     double *vQ = vI + (M + 1), *vU = vQ + (M + 1);
     double *seed = rough ? calloc(cnt * 3, sizeof(double)) : NULL;
@@ -1376,6 +1450,15 @@ int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, cons
             vU[m] = interp_pos(mu_pos, tmp[2], n, c->mu_view);
         }
         for (int j = 1; j <= n; ++j) I_dn_boa[(size_t)m * n + j - 1] = F(Tt[0], c, nt, -j);
+        if (lut) {
+            double tmp[3][MAX_RING];
+            for (int st = 0; st < 3; ++st) for (int j = 1; j <= n; ++j) tmp[st][j - 1] = F(Tt[st], c, 0, j);
+            for (int iv = 0; iv < nvg; ++iv) {
+                const double mug = cos(lut->vza_deg[iv] * PI / 180.0);
+                for (int st = 0; st < 3; ++st)
+                    lut_samp[((size_t)m * nvg + iv) * 3 + st] = pchip_pos(mu_pos, tmp[st], n, mug);
+            }
+        }
         if (diag) {
             if (diag->view_I_m) diag->view_I_m[m] = vI[m];
             if (diag->view_Q_m) diag->view_Q_m[m] = vQ[m];
@@ -1388,9 +1471,12 @@ int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, cons
         out->rho_I = I / c->mu0; out->rho_Q = Q / c->mu0; out->rho_U = U / c->mu0;
         out->kappa_ipss = 1.0;
         double tau_dir = -1.0;
+        ipss_t g;
+        int ipss_ready = 0;
+        memset(&g, 0, sizeof(g));
         if (op->pssa) {
-            ipss_t g;
             if (ipss_init(&g, &c->md, c->mu0, aer) == 0) {
+                ipss_ready = 1;
                 const double rB[3] = {0.0, 0.0, g.Re};
                 const double ts = ipss_tau_sun(&g, rB);
                 tau_dir = isfinite(ts) ? ts : -1.0;
@@ -1399,7 +1485,6 @@ int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, cons
                 out->rho_I *= kap; out->rho_Q *= kap; out->rho_U *= kap;
                 out->I_TOA *= kap; out->Q_TOA *= kap; out->U_TOA *= kap;
             } else rc = -1;
-            ipss_free(&g);
         }
         const double tau_t = c->md.h[nt];
         if (!rc && cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN) {
@@ -1434,8 +1519,50 @@ int ocrt_oracle_solve_case_layers(const ocrt_case *cs, const ocrt_opts *op, cons
         free(vdn);
         out->T_total_up_dir = out->rho_I * c->mu0;
         out->T_dir_up_view = exp(-tau_t / (c->mu_view > 0.0 ? c->mu_view : 1.0));
+        if (!rc && lut) {
+            /* per grid direction: Fourier sums, rho, kappa, direct glint (rt_solver.c:1276-1424) */
+            lut->T_dir_dn = out->T_dir_dn;
+            lut->T_diff_dn_hemi = out->T_diff_dn_hemi;
+            const double cglint = (ipss_ready && tau_dir >= 0.0) ? exp(-(tau_dir - tau_t / c->mu0)) : 1.0;
+            double pm[3][MAX_M1], dnm[MAX_M1];
+            for (int iv = 0; iv < nvg; ++iv) {
+                const double mug = cos(lut->vza_deg[iv] * PI / 180.0);
+                for (int m = 0; m <= M; ++m) {
+                    for (int st = 0; st < 3; ++st) pm[st][m] = lut_samp[((size_t)m * nvg + iv) * 3 + st];
+                    dnm[m] = interp_pos(mu_pos, I_dn_boa + (size_t)m * n, n, mug);
+                }
+                for (int ir = 0; ir < lut->n_raa; ++ir) {
+                    const double raa = lut->raa_deg[ir], ph = raa * PI / 180.0;
+                    double rI = recon_cos(pm[0], M, ph) / c->mu0;
+                    double rQ = recon_cos(pm[1], M, ph) / c->mu0;
+                    double rU = recon_sin(pm[2], M, ph) / c->mu0;
+                    if (ipss_ready) {
+                        const double kg = ipss_kappa(&g, lut->vza_deg[iv], raa);
+                        rI *= kg; rQ *= kg; rU *= kg;
+                    }
+                    double sgI = 0.0;
+                    if (cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && cs->wind_speed > 0.0) {
+                        const double phv = (raa - 180.0) * PI / 180.0;
+                        const double mvu = lut->vza_deg[iv] > 0.0 ? mug : 1.0;
+                        double gl[3];
+                        sunglint_rho(mvu, phv, c->mu0, cs->wind_speed, cs->sigma_type, cs->n_water, tau_t,
+                                     cs->q_convention, gl);
+                        gl[0] *= cglint; gl[1] *= cglint; gl[2] *= cglint;
+                        if (cs->decouple_sunglint == 0) { rI += gl[0]; rQ += gl[1]; rU += -gl[2]; }
+                        sgI = gl[0];
+                    }
+                    const int idx = iv * lut->n_raa + ir;
+                    lut->rho_I[idx] = rI; lut->rho_Q[idx] = rQ; lut->rho_U[idx] = rU;
+                    if (lut->T_diff_dn_dir)
+                        lut->T_diff_dn_dir[idx] = 2.0 * PI * mug * recon_cos(dnm, M, ph) / (PI * c->mu0);
+                    if (lut->T_sg_up_dir) lut->T_sg_up_dir[idx] = sgI * c->mu0;
+                    if (lut->T_total_up_dir) lut->T_total_up_dir[idx] = rI * c->mu0;
+                }
+            }
+        }
+        ipss_free(&g);
     }
-    free(seed); free(vI); free(I_dn_boa); free(Kr); free(Ks); free(mu_pos); free(buf);
+    free(lut_samp); free(seed); free(vI); free(I_dn_boa); free(Kr); free(Ks); free(mu_pos); free(buf);
     mode_free(&md);
 done:
     free(c->Tr); free(c->Ca); free(c->Cb);

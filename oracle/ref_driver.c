@@ -189,3 +189,39 @@ int ocrt_ref_solve_batch(int n, const ocrt_case *cases, const ocrt_opts *opts, i
     }
     return rc_all;
 }
+
+/* Angle-grid LUT through the reference's own rt_solve_case_pol_lut
+ * (rt_solver.h:207-210); US62 profile only. */
+int ocrt_ref_solve_case_lut(const ocrt_case *c, const ocrt_opts *o, const ocrt_aerosol *a,
+                            ocrt_result *out, ocrt_lut *lut)
+{
+    if (o->rayleigh_profile == OCRT_PROFILE_EXPONENTIAL) return -5;
+    rt_case_t cs; rt_options_t op;
+    fill(c, o, &cs, &op);
+    rt_lut_grid_out_t L;
+    memset(&L, 0, sizeof(L));
+    L.n_vza = lut->n_vza; L.vza_deg = lut->vza_deg;
+    L.n_raa = lut->n_raa; L.raa_deg = lut->raa_deg;
+    L.rho_I = lut->rho_I; L.rho_Q = lut->rho_Q; L.rho_U = lut->rho_U;
+    L.T_diff_dn_dir = lut->T_diff_dn_dir; L.T_sg_up_dir = lut->T_sg_up_dir; L.T_total_up_dir = lut->T_total_up_dir;
+    L.view_m_max = -1;
+    rt_aerosol_input_t ai;
+    memset(&ai, 0, sizeof(ai));
+    rt_result_t r;
+    int rc;
+    if (a && a->tau_a > 0.0) {
+        ai.tau_a = a->tau_a; ai.ssa_a = a->ssa_a; ai.L_max = a->L_max;
+        ai.betal_aer = a->beta; ai.gammal_aer = a->gamma;
+        ai.alphal_aer = a->alpha; ai.zetal_aer = a->zeta;
+        ai.use_value_kernel = 0;
+        rc = rt_solve_case_pol_lut(&cs, &op, &ai, &r, &L);
+    } else {
+        rc = rt_solve_case_pol_lut(&cs, &op, NULL, &r, &L);
+    }
+    if (rc) return rc;
+    memset(out, 0, sizeof(*out));
+    out->rho_I = r.rho_I; out->rho_Q = r.rho_Q; out->rho_U = r.rho_U;
+    out->n_orders_used = r.n_orders_used; out->converged = r.converged;
+    lut->T_dir_dn = L.T_dir_dn; lut->T_diff_dn_hemi = L.T_diff_dn_hemi;
+    return 0;
+}

@@ -132,3 +132,24 @@ def fd_gradient(orc, case, opts, aer, dtau, ssa, cot, which, rel_step=1e-6):
         else:
             out.append((f(kind, l, h) - f(kind, l, -h)) / (2.0 * h))
     return np.array(out)
+
+
+GOLDEN_LUT = os.path.join(HERE, "golden", "reference_lut.json")
+
+
+def load_golden_lut():
+    with open(GOLDEN_LUT) as fh:
+        return json.load(fh)
+
+
+def oracle_lut(orc, case, opts, aer, vza, raa):
+    lut = A.LutHolder(vza, raa)
+    f = orc.lib.ocrt_oracle_solve_case_lut
+    f.argtypes = [C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol), C.POINTER(A.Result),
+                  C.POINTER(A.Lut)]
+    a = aer.struct if isinstance(aer, A.AerosolHolder) else aer
+    r = A.Result()
+    rc = f(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None, C.byref(r), C.byref(lut.struct))
+    if rc != 0:
+        raise RuntimeError(f"oracle lut rc {rc}")
+    return lut

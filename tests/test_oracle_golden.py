@@ -67,3 +67,25 @@ def test_oracle_vs_live_reference_random(oracle):
         got = oracle.solve(c, o, aer)
         for k in ("rho_I", "rho_Q", "rho_U", "T_diff_dn_hemi", "T_diff_dn_dir"):
             assert _close(got[k], getattr(r, k), rel=1e-9, absol=1e-14), (k, got[k], getattr(r, k))
+
+
+from _helpers import load_golden_lut, oracle_lut  # noqa: E402
+
+LUTDOC = load_golden_lut()
+
+
+@pytest.mark.parametrize("spec", LUTDOC["cases"], ids=[c["name"] for c in LUTDOC["cases"]])
+def test_oracle_lut_matches_reference_fixture(oracle, spec):
+    """Angle-grid LUT (rt_solve_case_pol_lut): PCHIP view sampling per mode,
+    per-direction Fourier sums, IPSS kappa and sunglint, against the reference."""
+    import numpy as np
+    from ocrt_gb300 import _abi as A
+    c, o, a = inputs_from_spec(spec)
+    lut = oracle_lut(oracle, c, o, a, LUTDOC["vza_deg"], LUTDOC["raa_deg"])
+    ref = spec["reference"]
+    for k in A.LUT_FIELDS:
+        got, want = lut.out[k], np.asarray(ref[k])
+        scale = max(np.max(np.abs(want)), 1e-300)
+        assert np.max(np.abs(got - want)) <= 1e-9 * scale + 1e-15, k
+    assert _close(lut.struct.T_dir_dn, ref["T_dir_dn"])
+    assert _close(lut.struct.T_diff_dn_hemi, ref["T_diff_dn_hemi"])
