@@ -10,8 +10,8 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Opts, Result, default_case,
-                   default_opts, result_dict, RESULT_FIELDS)
+from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Lut, LutHolder, Opts, Result,
+                   default_case, default_opts, lut_grid_reference_cli, result_dict, RESULT_FIELDS)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libocrt_gb300.so")
@@ -23,6 +23,7 @@ EXPORTS = [
     "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy", "ocrt_gb_set_timing",
     "ocrt_gb_plan_kernel_stats", "ocrt_gb_solve_case_noalloc", "ocrt_gb_solve_batch_adjoint",
     "ocrt_gb_layer_defaults", "ocrt_gb_plan_create_adjoint", "ocrt_gb_plan_gradients",
+    "ocrt_gb_solve_case_lut", "ocrt_gb_solve_batch_lut",
 ]
 
 
@@ -66,6 +67,10 @@ def lib():
     L.ocrt_gb_plan_gradients.argtypes = [C.c_void_p, C.POINTER(Grad), C.c_void_p]
     L.ocrt_gb_layer_defaults.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol),
                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.ocrt_gb_solve_case_lut.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol), C.POINTER(Result),
+                                         C.POINTER(Lut)]
+    L.ocrt_gb_solve_batch_lut.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int, C.POINTER(Aerosol),
+                                          C.c_int, C.POINTER(Lut), C.POINTER(Result), C.c_void_p]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
     _lib = L
@@ -195,6 +200,24 @@ def solve_batch_adjoint(cases, opts, aerosols=None, layers=None, cot=None):
                            lambda ga: L.ocrt_gb_solve_batch_adjoint(n, ca, oa, opp, aa, app, la, ncot, cp, out, ga,
                                                                     None))
     return results_to_numpy(out), grads
+
+
+def solve_batch_lut(cases, opts, aerosols, luts):
+    """Angle-grid LUT for n cases in one device pass; luts: one LutHolder per
+    case (its output arrays are filled).  Returns the per-case results."""
+    L = lib()
+    n, ca, oa, opp, aa, app = _arrays(cases, opts, aerosols)
+    la = (Lut * n)(*[x.struct for x in luts])
+    out = (Result * n)()
+    _check(L.ocrt_gb_solve_batch_lut(n, ca, oa, opp, aa, app, la, out, None))
+    for i, x in enumerate(luts):
+        x.struct.T_dir_dn, x.struct.T_diff_dn_hemi = la[i].T_dir_dn, la[i].T_diff_dn_hemi
+    return results_to_numpy(out)
+
+
+def solve_case_lut(case, opts, aerosol, lut):
+    """Angle-grid LUT of one case (rt_solve_case_pol_lut); fills `lut` (a LutHolder)."""
+    return solve_batch_lut([case], opts, [aerosol] if aerosol is not None else None, [lut])
 
 
 def set_timing(enable):

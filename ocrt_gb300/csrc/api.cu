@@ -223,6 +223,11 @@ struct Group {
           *Abc = nullptr;
     float2 *ATot = nullptr;
     TaskState *Ast = nullptr;
+    // angle-grid LUT mode
+    bool any_lut = false;
+    int lut_nvmax = 0, lut_ptmax = 0;
+    long long lut_ntot = 0;
+    double *lut_vza = nullptr, *lut_raa = nullptr, *lut_samp = nullptr, *lut_kappa = nullptr, *lut_out = nullptr;
     int *acnt = nullptr, *awork = nullptr;
     float *opsTH = nullptr, *opsTL = nullptr;   // transposed operator planes for the tcgen05 adjoint source
     bool use_tc_adj = false;
@@ -278,15 +283,17 @@ void free_group(Group &g)
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
                     g.err, g.FH, g.FL, g.J, g.ops, g.opsH, g.opsL, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJH,
-                    g.AJL, g.Abc, g.Ast, g.acnt, g.awork, g.opsTH, g.opsTL};
+                    g.AJL, g.Abc, g.Ast, g.acnt, g.awork, g.opsTH, g.opsTL,
+                    g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
     for (void *p : ptrs) dfree(p);
 }
 
 int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app,
-                const ocrt_layers *layers = nullptr, int ncot = 0, const double *cot = nullptr)
+                const ocrt_layers *layers = nullptr, int ncot = 0, const double *cot = nullptr,
+                const ocrt_lut *luts = nullptr)
 {
     g.ncot = ncot;
-    std::vector<double> ldt, lss, hcot;
+    std::vector<double> ldt, lss, hcot, hlv, hlr;
     const Geom G = make_geom(g.N);
     g.G = G;
     g.P = (int)g.idx.size();
@@ -324,6 +331,18 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         for (int r = 0; r < ncot; ++r)
             for (int x = 0; x < 3; ++x) hcot.push_back(cot[((size_t)i * ncot + r) * 3 + x]);
         g.ntmax = std::max(g.ntmax, o.n_layers);
+        d.lut_nv = d.lut_nr = 0;
+        if (luts) {
+            const ocrt_lut &L = luts[i];
+            d.lut_nv = L.n_vza; d.lut_nr = L.n_raa;
+            d.lut_vo = (long long)hlv.size(); d.lut_ro = (long long)hlr.size(); d.lut_oo = g.lut_ntot;
+            hlv.insert(hlv.end(), L.vza_deg, L.vza_deg + L.n_vza);
+            hlr.insert(hlr.end(), L.raa_deg, L.raa_deg + L.n_raa);
+            g.lut_ntot += (long long)L.n_vza * L.n_raa;
+            g.lut_nvmax = std::max(g.lut_nvmax, L.n_vza);
+            g.lut_ptmax = std::max(g.lut_ptmax, L.n_vza * L.n_raa);
+            g.any_lut = true;
+        }
         if (a && a->tau_a > 0.0) {
             d.mom_off = (int)mb.size(); d.L_aer = a->L_max; d.tau_a = a->tau_a; d.ssa_a = a->ssa_a;
             for (int l = 0; l <= a->L_max; ++l) {
@@ -432,6 +451,10 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.Bx, (size_t)g.wave_tasks * 6 * (g.Lmax + 1))))
         return rc;
     if (g.any_layers && ((rc = up(g.ldt, ldt)) || (rc = up(g.lss, lss)))) return rc;
+    if (g.any_lut && ((rc = up(g.lut_vza, hlv)) || (rc = up(g.lut_raa, hlr)) ||
+                      (rc = alloc(g.lut_samp, (size_t)g.T * g.lut_nvmax * 4)) ||
+                      (rc = alloc(g.lut_kappa, (size_t)g.lut_ntot)) || (rc = alloc(g.lut_out, 6 * (size_t)g.lut_ntot))))
+        return rc;
     if (ncot > 0) {
         g.kstride = g.ntmax + 1;
         g.gstride = 3 * g.kstride + 2;
@@ -491,6 +514,14 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         cudaError_t e_ = cudaGetLastError();                                          \
         if (e_ != cudaSuccess) return fail(OCRT_ERR_DEVICE, std::string("launch: ") + cudaGetErrorString(e_)); \
     } while (0)
+
+LutBufs make_lut(Group &g)
+{
+    LutBufs L;
+    L.vza = g.lut_vza; L.raa = g.lut_raa; L.samp = g.lut_samp; L.nvmax = g.lut_nvmax;
+    L.kappa = g.lut_kappa; L.tau_dir = g.taudir; L.out = g.lut_out; L.ntot = g.lut_ntot;
+    return L;
+}
 
 AdjBufs make_adj(Group &g)
 {
@@ -657,6 +688,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
             }
         }
         LAUNCH(plan, KC_EXTRACT, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
+        if (g.any_lut) LAUNCH(plan, KC_EXTRACT, k_lut_sample<<<nw, 128, 0, st>>>(B, W, make_lut(g), G, w.t0, nw));
         if (g.ncot) {
             const int rc = run_adjoint_wave(plan, g, w, B, W, st, tc_grid, mol_grid, mtiles, ltiles, sgrid, tc_smem);
             if (rc) return rc;
@@ -667,7 +699,13 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         for (const PixDev &d : g.hpx) maxnt = std::max(maxnt, d.nt);
         const size_t smem = sizeof(double) * (6 * (size_t)maxnt + 6) + sizeof(int) * ((size_t)maxnt + 1);
         LAUNCH(plan, KC_IPSS, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.kappa, g.taudir));
+        if (g.any_lut)
+            LAUNCH(plan, KC_IPSS, k_ipss_lut<<<dim3(std::min(g.lut_ptmax, 2048), P), 256, smem, st>>>(
+                       g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.lut_vza, g.lut_raa, g.lut_kappa));
     }
+    if (g.any_lut)
+        LAUNCH(plan, KC_FINAL, k_lut_final<<<dim3((g.lut_ptmax + 127) / 128, P), 128, 0, st>>>(g.px, P, make_lut(g),
+                                                                                              g.pix_task0));
     LAUNCH(plan, KC_FINAL, k_finalize<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.state, g.tout, g.gmu, g.gw, g.h,
                                                               g.kappa, g.taudir, g.res));
     return OCRT_OK;
@@ -754,8 +792,20 @@ int validate_layers(const ocrt_case *cs, const ocrt_opts *op, const ocrt_layers 
     return OCRT_OK;
 }
 
+int validate_lut(const ocrt_lut *L)
+{
+    if (L->n_vza <= 0 || L->n_raa <= 0 || !L->vza_deg || !L->raa_deg || !L->rho_I || !L->rho_Q || !L->rho_U)
+        return fail(OCRT_ERR_ARGS, "bad LUT grid or outputs");
+    for (int i = 0; i < L->n_vza; ++i)
+        if (!(L->vza_deg[i] >= 0.0 && L->vza_deg[i] < 90.0)) return fail(OCRT_ERR_ARGS, "LUT vza outside [0, 90)");
+    for (int i = 0; i < L->n_raa; ++i)
+        if (!std::isfinite(L->raa_deg[i])) return fail(OCRT_ERR_ARGS, "LUT raa not finite");
+    return OCRT_OK;
+}
+
 int plan_create_impl(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app,
-                     const ocrt_layers *layers, int ncot, const double *cot, ocrt_plan **out)
+                     const ocrt_layers *layers, int ncot, const double *cot, ocrt_plan **out,
+                     const ocrt_lut *luts = nullptr)
 {
     if (!out) return fail(OCRT_ERR_ARGS, "null plan pointer");
     *out = nullptr;
@@ -763,6 +813,7 @@ int plan_create_impl(int n, const ocrt_case *cases, const ocrt_opts *opts, int o
     for (int i = 0; i < n; ++i) {
         int rc = validate(&cases[i], opp ? &opts[i] : &opts[0], aer ? (app ? &aer[i] : &aer[0]) : nullptr);
         if (!rc) rc = validate_layers(&cases[i], opp ? &opts[i] : &opts[0], layers ? &layers[i] : nullptr, ncot);
+        if (!rc && luts) rc = validate_lut(&luts[i]);
         if (rc) return rc;
     }
     int rc = ensure_init();
@@ -786,7 +837,7 @@ int plan_create_impl(int n, const ocrt_case *cases, const ocrt_opts *opts, int o
         plan->groups[it->second].idx.push_back(i);
     }
     for (Group &g : plan->groups) {
-        rc = build_group(g, cases, opts, opp, aer, app, layers, ncot, cot);
+        rc = build_group(g, cases, opts, opp, aer, app, layers, ncot, cot, luts);
         if (rc) {
             for (Group &h : plan->groups) free_group(h);
             delete plan;
@@ -1000,6 +1051,52 @@ int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases, const ocrt_opts *
     if (!rc && n_cot > 0) rc = ocrt_gb_plan_gradients(plan, grad, stream);
     ocrt_gb_plan_destroy(plan);
     return rc;
+}
+
+int ocrt_gb_solve_batch_lut(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp,
+                            const ocrt_aerosol *aer, int app, ocrt_lut *luts, ocrt_result *out, void *stream)
+{
+    if (n == 0) return OCRT_OK;
+    if (!out || !luts) return fail(OCRT_ERR_ARGS, "null output or LUT array");
+    ocrt_plan *plan = nullptr;
+    int rc = plan_create_impl(n, cases, opts, opp, aer, app, nullptr, 0, nullptr, &plan, luts);
+    if (rc) return rc;
+    rc = ocrt_gb_plan_execute(plan, stream);
+    if (!rc) rc = ocrt_gb_plan_results(plan, out, stream);
+    if (!rc) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
+        for (Group &g : plan->groups) {
+            std::vector<double> h(6 * (size_t)g.lut_ntot);
+            if (cudaMemcpyAsync(h.data(), g.lut_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st) !=
+                    cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+                rc = fail(OCRT_ERR_DEVICE, "LUT copy failed");
+                break;
+            }
+            for (int q = 0; q < g.P; ++q) {
+                const int i = g.idx[q];
+                const PixDev &d = g.hpx[q];
+                ocrt_lut &L = luts[i];
+                double *dst[6] = {L.rho_I, L.rho_Q, L.rho_U, L.T_diff_dn_dir, L.T_sg_up_dir, L.T_total_up_dir};
+                const size_t np = (size_t)d.lut_nv * d.lut_nr;
+                for (int f = 0; f < 6; ++f)
+                    if (dst[f]) memcpy(dst[f], h.data() + (size_t)f * g.lut_ntot + d.lut_oo, sizeof(double) * np);
+                L.T_dir_dn = out[i].T_dir_dn;
+                L.T_diff_dn_hemi = out[i].T_diff_dn_hemi;
+            }
+        }
+    }
+    ocrt_gb_plan_destroy(plan);
+    return rc;
+}
+
+int ocrt_gb_solve_case_lut(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer, ocrt_result *out,
+                           ocrt_lut *lut)
+{
+    if (!cs || !out || !lut) return fail(OCRT_ERR_ARGS, "null case, output or LUT");
+    ocrt_opts def;
+    if (!opts) { ocrt_opts_default(&def); opts = &def; }
+    return ocrt_gb_solve_batch_lut(1, cs, opts, 0, aer, 0, lut, out, nullptr);
 }
 
 int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,

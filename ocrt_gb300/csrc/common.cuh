@@ -42,6 +42,8 @@ struct PixDev {
     long long coef_off;     // offset of transport coefficients (nt * NR entries)
     long long lay_off;      // offset of the per-layer override arrays (nt entries), -1 = none
     int has_dtau, has_ssa;  // which overrides are present
+    int lut_nv, lut_nr;     // angle-grid LUT size (0 = no LUT)
+    long long lut_vo, lut_ro, lut_oo;   // offsets of the grid vza, grid raa and the LUT outputs
     // ---- derived on device (k_pixel_setup) ----
     double mu0, mu_view, tau_r, tau_total;
     int n_ring, view_slot;  // view_slot: ring slot holding mu_view, -1 = interpolate

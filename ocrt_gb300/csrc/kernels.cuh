@@ -96,6 +96,22 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
 size_t adj_mol_smem_bytes(const Geom &G);
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
+
+// lut.cu (angle-grid LUT mode)
+struct LutBufs {
+    const double *vza, *raa;   // grid angles in degrees, by PixDev::lut_vo / lut_ro
+    double *samp;              // [task][nvmax][4]: TOA-up I, Q, U (PCHIP) and BOA-down I (linear) per grid vza
+    int nvmax;
+    const double *kappa;       // [lut_oo + point] IPSS kappa per grid direction
+    const double *tau_dir;     // [pixel] IPSS direct slant depth (or -1)
+    double *out;               // 6 planes of ntot: rho_I, rho_Q, rho_U, T_diff_dn_dir, T_sg_up_dir, T_total_up_dir
+    long long ntot;
+};
+__global__ void k_lut_sample(BatchBufs B, WaveBufs W, LutBufs Lb, Geom G, int t0, int nw);
+__global__ void k_lut_final(const PixDev *px, int P, LutBufs Lb, const int *pix_task0);
+__global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
+                           const double *yd, const double *mb, const double *lut_vza, const double *lut_raa,
+                           double *lut_kappa);
 __global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
                             const float *Bt, const double *gw, float *ops);
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);

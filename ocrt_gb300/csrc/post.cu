@@ -53,18 +53,13 @@ __device__ double ipss_tau_sun(const double *he, const double *beta, int nl, dou
     return tau;
 }
 
-__global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
-                       const double *xd, const double *yd,
-                       const double *mb, double *kappa, double *tau_dir)
+// IPSS for one view direction (vza_deg, raa_deg) of pixel d by the whole
+// block; thread 0 writes *kappa and, when tau_dir is non-null, the direct-beam
+// slant depth to the surface.
+__device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, const double *h, const double *z,
+                           const double *xd, const double *yd, const double *mb, double *kappa, double *tau_dir)
 {
     extern __shared__ double sm[];
-    const int p = blockIdx.x;
-    if (p >= P) return;
-    const PixDev &d = px[p];
-    if (!d.pssa) {
-        if (threadIdx.x == 0) { kappa[p] = 1.0; tau_dir[p] = -1.0; }
-        return;
-    }
     const int nl = d.nt;
     double *he = sm;                    // [nl+1] ascending edges
     double *beta = he + nl + 1;         // [nl]
@@ -88,7 +83,7 @@ __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z
         if (xd[lo + k + 1] > 0.0) have_aer = 1;
     }
     __syncthreads();
-    const double tv = d.vza_deg * OCRT_PI / 180.0, fp = (180.0 - d.raa_deg) * OCRT_PI / 180.0;
+    const double tv = vza_deg * OCRT_PI / 180.0, fp = (180.0 - raa_deg) * OCRT_PI / 180.0;
     const int use_w = have_aer && d.mom_off >= 0 && d.tau_a > 0.0;
     double PR = 1.0, PA = 1.0;
     if (use_w) {
@@ -179,10 +174,47 @@ __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z
                 Ipp += wsrc[jj] / (mv * C) * (exp(-C * above[jj + 1]) - exp(-C * above[jj]));
             }
         }
-        kappa[p] = (!(Ipp > 1.0e-300) || !isfinite(tot)) ? 1.0 : tot / Ipp;
-        const double r0[3] = {0.0, 0.0, IPSS_RE};
-        const double td = ipss_tau_sun(he, beta, nl, d.mu0, r0);
-        tau_dir[p] = isfinite(td) ? td : -1.0;
+        *kappa = (!(Ipp > 1.0e-300) || !isfinite(tot)) ? 1.0 : tot / Ipp;
+        if (tau_dir) {
+            const double r0[3] = {0.0, 0.0, IPSS_RE};
+            const double td = ipss_tau_sun(he, beta, nl, d.mu0, r0);
+            *tau_dir = isfinite(td) ? td : -1.0;
+        }
+    }
+}
+
+__global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
+                       const double *xd, const double *yd,
+                       const double *mb, double *kappa, double *tau_dir)
+{
+    const int p = blockIdx.x;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    if (!d.pssa) {
+        if (threadIdx.x == 0) { kappa[p] = 1.0; tau_dir[p] = -1.0; }
+        return;
+    }
+    ipss_block(d, d.vza_deg, d.raa_deg, h, z, xd, yd, mb, &kappa[p], &tau_dir[p]);
+}
+
+// IPSS kappa at every (vza, raa) of each pixel's LUT grid: block (point, pixel).
+__global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
+                           const double *yd, const double *mb, const double *lut_vza, const double *lut_raa,
+                           double *lut_kappa)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    const int npts = d.lut_nv * d.lut_nr;
+    for (int pt = blockIdx.x; pt < npts; pt += gridDim.x) {
+        double *kout = &lut_kappa[d.lut_oo + pt];
+        if (!d.pssa) {
+            if (threadIdx.x == 0) *kout = 1.0;
+            continue;
+        }
+        const int iv = pt / d.lut_nr, ir = pt - iv * d.lut_nr;
+        ipss_block(d, lut_vza[d.lut_vo + iv], lut_raa[d.lut_ro + ir], h, z, xd, yd, mb, kout, nullptr);
+        __syncthreads();
     }
 }
 
