@@ -56,7 +56,22 @@ def build(verbose=False, extra=()):
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
     if jobs or not os.path.exists(LIB):
         run([nvcc, *ARCH, "-shared", *objs, "-o", LIB, "-lcudart"])
+    build_cli(run)
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "cli", "ocrt_cli.c")
+CLI_BIN = os.path.join(HERE, "bin", "ocrt")
+
+
+def build_cli(run):
+    """The `ocrt` command-line front end: plain C over the C ABI."""
+    if os.path.exists(CLI_BIN) and os.path.getmtime(CLI_BIN) >= max(os.path.getmtime(CLI_SRC), os.path.getmtime(LIB)):
+        return CLI_BIN
+    os.makedirs(os.path.dirname(CLI_BIN), exist_ok=True)
+    run([os.environ.get("CC", "gcc"), "-std=c11", "-O2", "-Wall", "-Werror=implicit-function-declaration", CLI_SRC, "-I", os.path.join(HERE, "..", "include"),
+         "-L", HERE, "-locrt_gb300", "-Wl,-rpath,$ORIGIN/..", "-lm", "-o", CLI_BIN])
+    return CLI_BIN
 
 
 if __name__ == "__main__":

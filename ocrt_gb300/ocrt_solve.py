@@ -1,0 +1,157 @@
+"""Python entry point with the signatures of the reference's ocrt_solve.py
+(code/OCRT_Python/ocrt_solve.py:131-206 `solve_reflectances`, and the
+`single` / `grid` sub-commands at :279-410), running on the GB300 library.
+
+The reference computes three reflectances per row (ocrt_solve.py:5-10):
+  R1 rho_TOA      ocean + atmosphere + aerosol + water-leaving (coupled ocean)
+  R2 rho_R        Rayleigh atmosphere over a black Fresnel ocean surface, glint decoupled
+  R3 rho_RA_black Rayleigh + aerosol over a black Fresnel ocean surface, glint decoupled
+R2 and R3 are on this path.  R1 needs the coupled in-water solve, which is
+not, and raises.  Gas absorption layering (gas_on) is not on this path
+either: pass gas_on=False.  The reference's aerosol comes from FR631 `.mie`
+models named by aer_name; here aer_name is a synthetic expansion spec
+"HG:g,ssa[,L]" (Henyey-Greenstein beta_l = (2l+1) g^l with the Rayleigh-form
+gamma_2/alpha_2 x 0.3) and aod865 is the AOD at the row's wavelength.
+"""
+import argparse
+import csv
+import sys
+
+import numpy as np
+
+from . import _abi as A
+from . import solve_batch
+
+DEPOL = 0.0279
+
+
+def _hg(spec, aod):
+    if not isinstance(spec, str) or not spec.upper().startswith("HG:"):
+        raise NotImplementedError("aerosol models from FR631 .mie files are not on this path; "
+                                  "use aer_name='HG:g,ssa[,L]'")
+    parts = [float(x) for x in spec[3:].split(",")]
+    g, ssa = parts[0], parts[1]
+    L = int(parts[2]) if len(parts) > 2 else 80
+    l = np.arange(L + 1, dtype=np.float64)
+    beta = (2.0 * l + 1.0) * g ** l
+    gamma, alpha, zeta = np.zeros(L + 1), np.zeros(L + 1), np.zeros(L + 1)
+    Ar = 2.0 * (1.0 - DEPOL) / (2.0 + DEPOL)
+    gamma[2], alpha[2] = 0.3 * (-Ar * np.sqrt(1.5)), 0.3 * 3.0 * Ar
+    return A.AerosolHolder(aod, ssa, beta, gamma, alpha, zeta)
+
+
+def _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa, max_it=100):
+    """Cases of the R2 / R3 solves of every row (ocrt_solve.py:160-177)."""
+    out = []
+    for r in rows:
+        base = dict(sza_deg=r["sza"], vza_deg=r["vza"], raa_deg=r["raa"], wavelength_nm=r["wl_nm"],
+                    wind_speed=r["wind"], surface="black_fresnel_ocean", pressure_hpa=pressure_hpa,
+                    decouple_sunglint=1)
+        if "R2" in which:
+            out.append(("R2", r, A.default_case(**base),
+                        A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=2, max_orders=max_it), None))
+        if "R3" in which:
+            out.append(("R3", r, A.default_case(**base),
+                        A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=fourier_m_max, max_orders=max_it),
+                        _hg(r["aer_name"], r["aod865"])))
+    return out
+
+
+def _solve_rows(rows, which, fourier_m_max, nt_atm, pressure_hpa, gas_on):
+    which = tuple(which)
+    if "R1" in which:
+        raise NotImplementedError("R1 (coupled atmosphere-ocean, rho_TOA) is not on the GB300 solve path")
+    if gas_on:
+        raise NotImplementedError("gas absorption layering is not on the GB300 solve path; pass gas_on=False")
+    jobs = _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa)
+    outs = [dict(wavelength_nm=r["wl_nm"], sza=r["sza"], vza=r["vza"], raa=r["raa"], wind=r["wind"],
+                 aod865=r["aod865"], aer_model=r["aer_name"], aod_band=r["aod865"]) for r in rows]
+    index = {id(r): i for i, r in enumerate(rows)}
+    if jobs:
+        res = solve_batch([j[2] for j in jobs], [j[3] for j in jobs],
+                          [j[4] if j[4] is not None else A.AerosolHolder(0.0, 1.0, [1.0, 0, 0], [0] * 3, [0] * 3,
+                                                                         [0] * 3) for j in jobs])
+        for k, (tag, r, *_rest) in enumerate(jobs):
+            o = outs[index[id(r)]]
+            key = "rho_R" if tag == "R2" else "rho_RA_black"
+            o[key + "_I"], o[key + "_Q"], o[key + "_U"] = (float(res["rho_I"][k]), float(res["rho_Q"][k]),
+                                                           float(res["rho_U"][k]))
+    for o in outs:
+        if "R2" in which and "R3" in which:
+            o["rho_AplusRA_I"] = o["rho_RA_black_I"] - o["rho_R_I"]
+    return outs
+
+
+def solve_reflectances(wl_nm, sza, vza, raa, wind, chl, tsm, acdom440,
+                       aod865, aer_name, which=('R1', 'R2', 'R3'),
+                       phyto_group='micro', tsm_species='red_clay',
+                       n_mu_water=48, fourier_m_max=16, nt_atm=400,
+                       max_it_water=500, pressure_hpa=1013.25,
+                       gas_on=True, cdom_slope=0.014,
+                       det_a440=0.0, det_slope=0.0109):
+    """Same signature as the reference; see the module docstring for what is
+    on this path.  The water constituent arguments only feed R1."""
+    row = dict(wl_nm=wl_nm, sza=sza, vza=vza, raa=raa, wind=wind, aod865=aod865, aer_name=aer_name)
+    return _solve_rows([row], which, fourier_m_max, nt_atm, pressure_hpa, gas_on)[0]
+
+
+def cmd_single(a):
+    out = solve_reflectances(a.wl, a.sza, a.vza, a.raa, a.wind, a.chl, a.tsm, a.acdom440, a.aod865, a.aer,
+                             which=a.which, fourier_m_max=a.m_max, nt_atm=a.n_layers, pressure_hpa=a.pressure,
+                             gas_on=not a.no_gas)
+    for k, v in out.items():
+        print(f"{k}={v}")
+    return 0
+
+
+def cmd_grid(a):
+    """Rows of a CSV (columns sza, vza, raa, wind, aod865, aer, and wl or one
+    run per --bands) solved in one batched call, written to --out."""
+    with open(a.grid) as fh:
+        src = list(csv.DictReader(fh))
+    rows = []
+    for r in src:
+        bands = [float(r["wl"])] if "wl" in r and r["wl"] else a.bands
+        for wl in bands:
+            rows.append(dict(wl_nm=float(wl), sza=float(r["sza"]), vza=float(r["vza"]), raa=float(r["raa"]),
+                             wind=float(r["wind"]), aod865=float(r.get("aod865", 0.0) or 0.0),
+                             aer_name=r.get("aer", a.aer) or a.aer))
+    outs = _solve_rows(rows, a.which, a.m_max, a.n_layers, a.pressure, not a.no_gas)
+    keys = sorted({k for o in outs for k in o})
+    with open(a.out, "w", newline="") as fh:
+        w = csv.DictWriter(fh, fieldnames=keys)
+        w.writeheader()
+        w.writerows(outs)
+    print(f"wrote {len(outs)} rows to {a.out}")
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="GB300 OCRT reflectances (R2/R3)")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+
+    def common(p):
+        p.add_argument("--which", nargs="+", default=["R2", "R3"])
+        p.add_argument("--m-max", type=int, default=16)
+        p.add_argument("--n-layers", type=int, default=400)
+        p.add_argument("--pressure", type=float, default=1013.25)
+        p.add_argument("--no-gas", action="store_true")
+        p.add_argument("--aer", default="HG:0.7,0.95,80")
+
+    ps = sub.add_parser("single")
+    common(ps)
+    for k in ("wl", "sza", "vza", "raa", "wind"):
+        ps.add_argument("--" + k, type=float, required=True)
+    for k in ("chl", "tsm", "acdom440", "aod865"):
+        ps.add_argument("--" + k, type=float, default=0.0)
+    pg = sub.add_parser("grid")
+    common(pg)
+    pg.add_argument("--grid", required=True)
+    pg.add_argument("--out", required=True)
+    pg.add_argument("--bands", type=float, nargs="+", default=[443.0, 555.0, 865.0])
+    a = ap.parse_args(argv)
+    return cmd_single(a) if a.cmd == "single" else cmd_grid(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
