@@ -256,16 +256,18 @@ def run_ours(args, rank, world):
             torch.distributed.barrier()
 
     # ---- value: resident plan ----
+    # Warm-up: the first execute runs eagerly (host polls end the order loops
+    # and record their lengths, the autotuner picks block sizes), the second
+    # captures the launch sequence into a CUDA graph; timed steps replay it.
     plan = og.Plan(cases, opts, aers)
     for _ in range(args.warmup):
         plan.execute(sp)
     torch.cuda.synchronize()
-    og.set_timing(True)
+    graph = plan.graph_ready
     clocks = ClockSampler(dev)
     clocks.start()
     barrier()
     torch.cuda.synchronize()
-    kstats = {}
     launches = 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     total_ms = 0.0
@@ -275,16 +277,31 @@ def run_ours(args, rank, world):
         e1.record(stream)
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
-        for k, v in plan.kernel_stats().items():
-            acc = kstats.setdefault(k, {"ms": 0.0, "launches": 0, "flops": 0.0, "bytes": 0.0})
-            for f in acc:
-                acc[f] += v[f]
         launches += plan.stats()["kernel_launches"]
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    og.set_timing(False)
     res = plan.results(sp)
+
+    # ---- per-kernel breakdown: the same steps executed eagerly with every
+    # launch bracketed by CUDA events on the launching stream ----
+    og.set_timing(True)
+    kstats = {}
+    instr_ms = 0.0
+    for _ in range(args.steps):
+        e0.record(stream)
+        plan.execute(sp)
+        e1.record(stream)
+        e1.synchronize()
+        instr_ms += e0.elapsed_time(e1)
+        for k, v in plan.kernel_stats().items():
+            acc = kstats.setdefault(k, {"ms": 0.0, "launches": 0, "flops": 0.0, "bytes": 0.0})
+            for f in acc:
+                acc[f] += v[f]
+    og.set_timing(False)
+    res_instr = plan.results(sp)
+    if not np.array_equal(res, res_instr):
+        raise RuntimeError("graph replay and eager execute disagree")
     om = float(np.sum(res["order_modes"]))
     ms_step = max_over_ranks(total_ms / args.steps)
     value = args.pixels * world / (ms_step / 1e3)
@@ -317,7 +334,8 @@ def run_ours(args, rank, world):
                 "intensity_flop_per_byte": intensity if d["flops"] > 0 else None, "ridge_flop_per_byte": ridge,
                 "tensor_frac_of_bf16": tensor_frac}
     breakdown = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
-                     "share": v["ms"] / max(sum(x["ms"] for x in kstats.values()), 1e-9)}
+                     "share": v["ms"] / max(sum(x["ms"] for x in kstats.values()), 1e-9),
+                     "alg_bytes_per_step": v["bytes"] / args.steps, "alg_flops_per_step": v["flops"] / args.steps}
                  for k, v in sorted(kstats.items(), key=lambda kv: -kv[1]["ms"]) if v["launches"]}
     plan.close()
 
@@ -367,7 +385,9 @@ def run_ours(args, rank, world):
             "cpu_baseline": cpu, "rel_err_vs_fp64": err,
             "plain_per_pixel_gpu": {"value": plain, "unit": METRIC, "sample": f"{nplain} pixels, one "
                                     f"ocrt_gb_solve_case call each", "batched_speedup": value / world / plain},
-            "order_modes_per_step": om, "kernel_breakdown": breakdown, "adjoint": adj}
+            "order_modes_per_step": om, "kernel_breakdown": breakdown, "adjoint": adj,
+            "execute": {"graph_replay": graph, "eager_instrumented_ms_per_step": instr_ms / args.steps,
+                        "autotune": [{k: s[k] for k in ("kernel", "key", "best")} for s in og.autotune_summary()]}}
     print(json.dumps(line), flush=True)
 
 
@@ -385,19 +405,21 @@ def run_adjoint(args, og, torch, stream, sp, barrier, world):
         torch.cuda.synchronize()
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        tot, ks = 0.0, {}
+        tot = 0.0
         for _ in range(args.steps):
             e0.record(stream)
             plan.execute(sp)
             e1.record(stream)
             e1.synchronize()
             tot += e0.elapsed_time(e1)
-            for k, v in plan.kernel_stats().items():
-                ks[k] = ks.get(k, 0.0) + v["ms"]
         ms = max_over_ranks(tot / args.steps)
-        return ms, {k: v / args.steps for k, v in sorted(ks.items(), key=lambda kv: -kv[1]) if v > 0}
+        # one eager execute with per-launch events for the breakdown
+        og.set_timing(True)
+        plan.execute(sp)
+        ks = {k: v["ms"] for k, v in plan.kernel_stats().items()}
+        og.set_timing(False)
+        return ms, {k: v for k, v in sorted(ks.items(), key=lambda kv: -kv[1]) if v > 0}
 
-    og.set_timing(True)
     fwd = og.Plan(cases, opts, aers)
     ms_fwd, _ = timed(fwd)
     fwd.close()
@@ -405,7 +427,6 @@ def run_adjoint(args, og, torch, stream, sp, barrier, world):
     ms_jac, ks = timed(jac)
     g = jac.gradients(sp)
     jac.close()
-    og.set_timing(False)
     finite = bool(np.isfinite(g["d_dtau"]).all() and np.isfinite(g["d_ssa"]).all() and np.isfinite(g["d_wind"]).all())
     return {"metric": "adjoint Jacobians/s", "value": n * world / (ms_jac / 1e3), "unit": "Jacobians/s",
             "ms_per_step": ms_jac, "forward_ms_per_step": ms_fwd,

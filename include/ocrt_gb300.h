@@ -150,7 +150,15 @@ int ocrt_gb_solve_batch(int n, const ocrt_case *cases,
 /* ---- resident plans (inputs uploaded once, solved many times) -----------
  * A plan holds the device copy of a batch.  ocrt_gb_plan_execute runs the
  * full solve on device-resident inputs (no host traffic); results stay on the
- * device until ocrt_gb_plan_results copies them out. */
+ * device until ocrt_gb_plan_results copies them out.
+ * The first execute runs eagerly: host polls of the device active-task counts
+ * end each order loop, and the order count each wave needed is recorded.  The
+ * second execute captures the same launch sequence with those counts and no
+ * host polls into a CUDA graph; later executes replay the graph (one launch
+ * call, no host synchronisation).  A replay that ends with a task still
+ * iterating is reported by ocrt_gb_plan_results as an error and the plan goes
+ * back to eager executes.  OCRT_GB_GRAPH=0, or timing enabled, keeps every
+ * execute eager. */
 typedef struct ocrt_plan ocrt_plan;
 int  ocrt_gb_plan_create(int n, const ocrt_case *cases,
                          const ocrt_opts *opts, int opts_per_case,
@@ -163,6 +171,16 @@ int  ocrt_gb_plan_results(ocrt_plan *plan, ocrt_result *out, void *stream);
 int  ocrt_gb_plan_stats(const ocrt_plan *plan, double *order_modes_total,
                         long long *kernel_launches);
 void ocrt_gb_plan_destroy(ocrt_plan *plan);
+/* 1 when the next ocrt_gb_plan_execute replays a captured CUDA graph. */
+int  ocrt_gb_plan_graph_ready(const ocrt_plan *plan);
+
+/* Launch-shape autotuner (no reference counterpart).  The Cox-Munk Fourier
+ * projection and the phase-table kernels are timed at 128, 256 and 512
+ * threads per block the first time a shape (N, n_phi, M / N, L, M) is met,
+ * and the fastest is used from then on (OCRT_GB_AUTOTUNE=0: 256 always).
+ * Writes one line per tuned shape into buf (NUL-terminated, truncated to
+ * len) and returns the length of the full text. */
+int  ocrt_gb_autotune_summary(char *buf, int len);
 
 /* Per-kernel-class instrumentation (no reference counterpart).  With timing
  * enabled every launch of a plan is bracketed by CUDA events on the launching

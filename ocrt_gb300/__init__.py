@@ -23,7 +23,7 @@ EXPORTS = [
     "ocrt_gb_plan_results", "ocrt_gb_plan_stats", "ocrt_gb_plan_destroy", "ocrt_gb_set_timing",
     "ocrt_gb_plan_kernel_stats", "ocrt_gb_solve_case_noalloc", "ocrt_gb_solve_batch_adjoint",
     "ocrt_gb_layer_defaults", "ocrt_gb_plan_create_adjoint", "ocrt_gb_plan_gradients",
-    "ocrt_gb_solve_case_lut", "ocrt_gb_solve_batch_lut",
+    "ocrt_gb_solve_case_lut", "ocrt_gb_solve_batch_lut", "ocrt_gb_plan_graph_ready", "ocrt_gb_autotune_summary",
 ]
 
 
@@ -71,6 +71,8 @@ def lib():
                                          C.POINTER(Lut)]
     L.ocrt_gb_solve_batch_lut.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int, C.POINTER(Aerosol),
                                           C.c_int, C.POINTER(Lut), C.POINTER(Result), C.c_void_p]
+    L.ocrt_gb_plan_graph_ready.argtypes = [C.c_void_p]
+    L.ocrt_gb_autotune_summary.argtypes = [C.c_char_p, C.c_int]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
     _lib = L
@@ -224,6 +226,21 @@ def set_timing(enable):
     lib().ocrt_gb_set_timing(1 if enable else 0)
 
 
+def autotune_summary():
+    """Block sizes the launch-shape autotuner picked, one dict per shape."""
+    L = lib()
+    n = L.ocrt_gb_autotune_summary(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    L.ocrt_gb_autotune_summary(buf, n + 1)
+    out = []
+    for line in buf.value.decode().splitlines():
+        head, ms = line.split(" ms:")
+        kern, key, best = head.split(" ")
+        out.append({"kernel": kern, "key": [int(x) for x in key[4:].split(",")], "best": int(best[5:]),
+                    "ms": {int(a): float(b) for a, b in (t.split("=") for t in ms.split())}})
+    return out
+
+
 def results_to_numpy(out):
     dt = np.dtype([(f, np.float64 if t is C.c_double else np.int32) for f, t in Result._fields_],
                   align=True)
@@ -268,6 +285,11 @@ class Plan:
         out = (Result * self.n)()
         _check(lib().ocrt_gb_plan_results(self._h, out, stream))
         return results_to_numpy(out)
+
+    @property
+    def graph_ready(self):
+        """True when the next execute replays the captured CUDA graph."""
+        return bool(lib().ocrt_gb_plan_graph_ready(self._h))
 
     def stats(self):
         om, nl = C.c_double(), C.c_longlong()

@@ -445,7 +445,6 @@ __global__ void __launch_bounds__(256) k_adj_mol(BatchBufs B, WaveBufs W, AdjBuf
     }
     __syncthreads();
     float *out = A.AF + off;
-    const double *yd = B.yd + d.lev_off;
     for (int e = threadIdx.x; e < nk * G.CIN; e += blockDim.x) {
         const int k = e / G.CIN, ci = e - k * G.CIN, b = ci / N, i = ci - b * N;
         const float *z = zt + k * 25 + 4 * b;

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <climits>
+#include <utility>
 
 #include "kernels.cuh"
 #include "physics.cuh"
@@ -30,6 +32,29 @@ std::multimap<size_t, void *> g_free;      // caching allocator: size -> block
 std::map<void *, size_t> g_live;
 int *g_pinned = nullptr;
 int g_timing = 0;
+
+// ---- launch-shape autotuner ----
+// Kernels whose outputs are plain stores of values computed from their inputs
+// (k_coxmunk, k_tables) can be launched again without changing the result, so
+// on the first execute that meets a new shape key each candidate block size is
+// run twice on the launching stream and the second run timed with CUDA events;
+// the fastest size is kept for the rest of the process.  OCRT_GB_AUTOTUNE=0
+// keeps the default of 256 threads.
+struct TuneRec {
+    std::string kernel;
+    std::vector<int> key;
+    int best = 256;
+    std::vector<std::pair<int, float>> ms;
+};
+std::map<std::pair<std::string, std::vector<int>>, size_t> g_tune_idx;
+std::vector<TuneRec> g_tune;
+const int kTuneBlocks[3] = {128, 256, 512};
+
+bool autotune_enabled()
+{
+    const char *e = getenv("OCRT_GB_AUTOTUNE");
+    return !(e && strcmp(e, "0") == 0);
+}
 
 enum KClass { KC_SETUP, KC_TABLES, KC_COXMUNK, KC_PRIMARY, KC_SOURCE, KC_SOURCE_TC, KC_MOL, KC_SCAN, KC_EXTRACT,
               KC_IPSS, KC_FINAL, KC_ADJ_SCAN, KC_ADJ_SOURCE, KC_ADJ_OTHER, KC_ADJ_TOTALS, KC_ADJ_GRAD, KC_N };
@@ -138,6 +163,10 @@ struct Wave {
     size_t fld, ops, srf;  // element counts of the wave buffers
     bool any_rough, any_flat;
     int n_simt = 0, n_tc = 0, n_mol = 0;   // tasks given to each source kernel
+    // Last order run before every task was found converged (forward orders,
+    // adjoint orders); INT_MAX when the loop ran to max_orders.  Recorded by
+    // an eager execute, replayed without host polls by the captured graph.
+    int fwd_stop = INT_MAX, adj_stop = INT_MAX;
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -258,6 +287,12 @@ struct ocrt_plan {
     long long cnt[KC_N] = {0};
     double flops[KC_N] = {0}, bytes[KC_N] = {0};
     bool work_done = false;
+    // CUDA graph of a whole execute: captured on the second untimed execute
+    // from the order counts the first one recorded, replayed from then on.
+    cudaGraphExec_t gexec = nullptr;
+    int executes = 0;
+    bool graph_off = false;
+    long long graph_launches = 0;
 };
 
 namespace {
@@ -440,7 +475,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.frs, (size_t)g.P * G.NR * 9)) ||
         (rc = alloc(g.kappa, g.P)) || (rc = alloc(g.taudir, g.P)) ||
         (rc = alloc(g.active_cnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.mol_cnt, (size_t)g.max_orders + 2)) ||
-        (rc = alloc(g.work, 4 * ((size_t)g.max_orders + 2))) || (rc = alloc(g.err, 1)) ||
+        (rc = alloc(g.work, 4 * ((size_t)g.max_orders + 2))) || (rc = alloc(g.err, 2)) ||
         (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
         (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
         (rc = alloc(g.FH, g.wave_fld)) || (rc = alloc(g.FL, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
@@ -515,6 +550,55 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         if (e_ != cudaSuccess) return fail(OCRT_ERR_DEVICE, std::string("launch: ") + cudaGetErrorString(e_)); \
     } while (0)
 
+// Block size for `kernel` at shape `key`: the cached choice, else (when
+// tuning is allowed: never while a graph is being captured) a measurement of
+// every candidate the kernel's register and thread limits admit.
+template <class F>
+int tuned_block(const char *kernel, const void *fn, const std::vector<int> &key, bool may_tune, cudaStream_t st,
+                F &&launch, int *bs)
+{
+    *bs = 256;
+    if (!autotune_enabled()) return OCRT_OK;
+    const auto k = std::make_pair(std::string(kernel), key);
+    const auto it = g_tune_idx.find(k);
+    if (it != g_tune_idx.end()) { *bs = g_tune[it->second].best; return OCRT_OK; }
+    if (!may_tune) return OCRT_OK;
+    cudaFuncAttributes fa;
+    CK(cudaFuncGetAttributes(&fa, fn));
+    TuneRec r;
+    r.kernel = kernel;
+    r.key = key;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(OCRT_ERR_DEVICE, "autotune: event create failed");
+    }
+    float best = 0.f;
+    int rc = OCRT_OK;
+    for (int b : kTuneBlocks) {
+        if (b > fa.maxThreadsPerBlock) continue;
+        launch(b);                      // first run absorbs module loading and cold caches
+        cudaEventRecord(e0, st);
+        launch(b);
+        cudaEventRecord(e1, st);
+        float t = 0.f;
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (e != cudaSuccess) { rc = fail(OCRT_ERR_DEVICE, std::string("autotune: ") + cudaGetErrorString(e)); break; }
+        r.ms.push_back({b, t});
+        if (r.ms.size() == 1 || t < best) { best = t; r.best = b; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    g_tune_idx[k] = g_tune.size();
+    g_tune.push_back(r);
+    *bs = r.best;
+    return OCRT_OK;
+}
+
 LutBufs make_lut(Group &g)
 {
     LutBufs L;
@@ -535,8 +619,8 @@ AdjBufs make_adj(Group &g)
 
 // Adjoint of one wave, right after its forward orders (the forward fields of
 // the wave are still resident).
-int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &B, const WaveBufs &W, cudaStream_t st,
-                     int tc_grid, int mol_grid, int mtiles, int ltiles, dim3 sgrid, size_t tc_smem)
+int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, const WaveBufs &W, cudaStream_t st,
+                     int tc_grid, int mol_grid, int mtiles, int ltiles, dim3 sgrid, size_t tc_smem, bool capture)
 {
     const Geom G = g.G;
     const int nw = w.t1 - w.t0, na = nw * g.ncot;
@@ -572,12 +656,15 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     LAUNCH(plan, KC_ADJ_OTHER, k_adj_init<<<(na + 127) / 128, 128, 0, st>>>(B, A, G, w.t0, na));
     const dim3 agrid(na, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.LDC + ST_N_TILE - 1) / ST_N_TILE);
     const int surf_threads = ((3 * G.N + 31) / 32) * 32;
+    if (!capture) w.adj_stop = INT_MAX;
     for (int j = 1; j <= g.max_orders; ++j) {
         LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<na, scan_threads, 0, st>>>(B, A, G, w.t0, j));
-        if ((j - 1) % 4 == 0 || j == g.max_orders) {
+        if (capture) {
+            if (j == w.adj_stop) break;
+        } else if ((j - 1) % 4 == 0 || j == g.max_orders) {
             CK(cudaMemcpyAsync(g_pinned, g.acnt + j, sizeof(int), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
-            if (*g_pinned == 0) break;
+            if (*g_pinned == 0) { w.adj_stop = j; break; }
         }
         if (g.use_tc_adj)
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source_tc<<<std::min(nw * amt, g_nsm), 256, tc_adj_smem_bytes(G), st>>>(
@@ -590,6 +677,8 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
         if (w.any_rough)
             LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<na, surf_threads, 0, st>>>(B, W, A, G, w.t0));
     }
+    if (capture && w.adj_stop != INT_MAX)
+        LAUNCH(plan, KC_ADJ_OTHER, k_stop_check<<<1, 32, 0, st>>>(g.acnt + w.adj_stop, g.err + 1));
     LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<na, scan_threads, 0, st>>>(
                B, W, A, G, w.t0));
     LAUNCH(plan, KC_ADJ_GRAD, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
@@ -597,11 +686,15 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, const Wave &w, const BatchBufs &
     return OCRT_OK;
 }
 
-int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
+// One execute of a group.  Eager (capture == false): host polls of the active
+// counts end each wave's order loop and record where it ended.  Capture: the
+// same launch sequence with the recorded order counts and no host polls, for
+// a CUDA graph; a device check flags a replay that ends with tasks active.
+int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
 {
     const Geom G = g.G;
     const int P = g.P;
-    CK(cudaMemsetAsync(g.err, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(g.err, 0, 2 * sizeof(int), st));
     LAUNCH(plan, KC_SETUP, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw, g.pw));
     LAUNCH(plan, KC_SETUP, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
     LAUNCH(plan, KC_SETUP, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
@@ -632,8 +725,9 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     const int poll = 4;
-    for (const Wave &w : g.waves) {
+    for (Wave &w : g.waves) {
         const int nw = w.t1 - w.t0;
+        if (!capture) w.fwd_stop = INT_MAX;
         CK(cudaMemsetAsync(g.ops, 0, sizeof(float) * w.ops, st));
         CK(cudaMemsetAsync(g.pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (g.any_flat) CK(cudaMemsetAsync(g.fvec, 0, sizeof(float) * (size_t)nw * 24 * G.NR, st));
@@ -641,8 +735,15 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
         CK(cudaMemsetAsync(g.mol_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.work, 0, sizeof(int) * 4 * ((size_t)g.max_orders + 2), st));
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
-        LAUNCH(plan, KC_TABLES, k_tables<<<nw, 256, sizeof(float) * 4 * ((size_t)g.Lmax + 1), st>>>(g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw,
-                                                   g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec, W.fvec));
+        auto tables = [&](int b) {
+            k_tables<<<dim3(nw, tables_yblocks(b, G.NR, G.N)), b, tables_smem_bytes(b, G.N, g.Lmax), st>>>(
+                g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec,
+                W.fvec);
+        };
+        int tb = 256;
+        int rc = tuned_block("k_tables", (const void *)k_tables, {G.N, g.Lmax, g.Mmax}, !capture, st, tables, &tb);
+        if (rc) return rc;
+        LAUNCH(plan, KC_TABLES, tables(tb));
         if (g.use_tc) {
             LAUNCH(plan, KC_TABLES, k_mol_dense<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.Lmax, g.Bp, g.Br, g.Bt,
                                                                      g.gw, g.ops));
@@ -652,12 +753,19 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
             const bool dw = g.ncot > 0;
             const int np = w.p1 - w.p0;
             const size_t smem = coxmunk_smem_bytes(g.nphi, dw);
-            if (dw)
-                LAUNCH(plan, KC_COXMUNK, k_coxmunk_dw<<<dim3(G.N + 1, G.NR, np), 256, smem, st>>>(
-                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.Mmax, g.lam, g.lamd, g.srf, g.srfW));
-            else
-                LAUNCH(plan, KC_COXMUNK, k_coxmunk<<<dim3(G.N + 1, G.NR, np), 256, smem, st>>>(
-                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.Mmax, g.lam, g.srf));
+            auto coxmunk = [&](int b) {
+                if (dw)
+                    k_coxmunk_dw<<<dim3(G.N + 1, G.NR, np), b, smem, st>>>(g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu,
+                                                                         g.cs, g.Mmax, g.lam, g.lamd, g.srf, g.srfW);
+                else
+                    k_coxmunk<<<dim3(G.N + 1, G.NR, np), b, smem, st>>>(g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu,
+                                                                      g.cs, g.Mmax, g.lam, g.srf);
+            };
+            int cb = 256;
+            rc = tuned_block(dw ? "k_coxmunk_dw" : "k_coxmunk", dw ? (const void *)k_coxmunk_dw : (const void *)k_coxmunk,
+                             {G.N, g.nphi, g.Mmax}, !capture, st, coxmunk, &cb);
+            if (rc) return rc;
+            LAUNCH(plan, KC_COXMUNK, coxmunk(cb));
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
@@ -681,16 +789,21 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
             LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, 0, st>>>(B, W, G, w.t0, it));
-            if ((it - 1) % poll == 0 || it == g.max_orders) {
+            if (capture) {
+                if (it == w.fwd_stop) break;
+            } else if ((it - 1) % poll == 0 || it == g.max_orders) {
                 CK(cudaMemcpyAsync(g_pinned, g.active_cnt + it, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
-                if (*g_pinned == 0) break;
+                if (*g_pinned == 0) { w.fwd_stop = it; break; }
             }
         }
+        if (capture && w.fwd_stop != INT_MAX)
+            LAUNCH(plan, KC_EXTRACT, k_stop_check<<<1, 32, 0, st>>>(g.active_cnt + w.fwd_stop, g.err + 1));
         LAUNCH(plan, KC_EXTRACT, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
         if (g.any_lut) LAUNCH(plan, KC_EXTRACT, k_lut_sample<<<nw, 128, 0, st>>>(B, W, make_lut(g), G, w.t0, nw));
         if (g.ncot) {
-            const int rc = run_adjoint_wave(plan, g, w, B, W, st, tc_grid, mol_grid, mtiles, ltiles, sgrid, tc_smem);
+            const int rc = run_adjoint_wave(plan, g, w, B, W, st, tc_grid, mol_grid, mtiles, ltiles, sgrid, tc_smem,
+                                            capture);
             if (rc) return rc;
         }
     }
@@ -745,6 +858,7 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_coxmunk_dw, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -863,6 +977,61 @@ int ocrt_gb_plan_create(int n, const ocrt_case *cases, const ocrt_opts *opts, in
     return plan_create_impl(n, cases, opts, opp, aer, app, nullptr, 0, nullptr, out);
 }
 
+namespace {
+
+bool graphs_enabled()
+{
+    const char *e = getenv("OCRT_GB_GRAPH");
+    return !(e && strcmp(e, "0") == 0);
+}
+
+// Record every group's launch sequence (recorded order counts, no host polls)
+// into one graph on `st` and instantiate it.
+int capture_plan(ocrt_plan *plan, cudaStream_t st)
+{
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return OCRT_ERR_DEVICE;
+    }
+    plan->launches = 0;
+    int rc = OCRT_OK;
+    for (Group &g : plan->groups) {
+        rc = run_group(plan, g, st, true);
+        if (rc) break;
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc == OCRT_OK && (e != cudaSuccess || !graph)) rc = OCRT_ERR_DEVICE;
+    if (rc == OCRT_OK && cudaGraphInstantiate(&plan->gexec, graph, 0) != cudaSuccess) {
+        plan->gexec = nullptr;
+        rc = OCRT_ERR_DEVICE;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (rc) cudaGetLastError();
+    else plan->graph_launches = plan->launches;
+    return rc;
+}
+
+// Device error flags of a group after an execute: [0] a non-finite field,
+// [1] a graph replay whose recorded order counts ended with tasks still
+// iterating (later executes of the plan then run eagerly with host polls).
+int group_flags(ocrt_plan *plan, Group &g, cudaStream_t st)
+{
+    int f[2] = {0, 0};
+    CK(cudaMemcpyAsync(f, g.err, sizeof(f), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (f[0]) return fail(f[0], "non-finite field during the SOS iteration");
+    if (f[1]) {
+        if (plan->gexec) cudaGraphExecDestroy(plan->gexec);
+        plan->gexec = nullptr;
+        plan->graph_off = true;
+        return fail(OCRT_ERR_DEVICE, "graph replay ended with tasks still iterating; execute the plan again");
+    }
+    return OCRT_OK;
+}
+
+} // namespace
+
 int ocrt_gb_plan_execute(ocrt_plan *plan, void *stream)
 {
     if (!plan) return fail(OCRT_ERR_ARGS, "null plan");
@@ -873,10 +1042,29 @@ int ocrt_gb_plan_execute(ocrt_plan *plan, void *stream)
     plan->ev.clear();
     for (int c = 0; c < KC_N; ++c) { plan->ms[c] = 0; plan->cnt[c] = 0; }
     plan->work_done = false;
+    const bool want_graph = !g_timing && !plan->graph_off && graphs_enabled();
+    if (want_graph && plan->gexec) {
+        CK(cudaGraphLaunch(plan->gexec, st));
+        plan->launches = plan->graph_launches;
+        plan->executes++;
+        return OCRT_OK;
+    }
+    if (want_graph && plan->executes >= 1) {
+        if (capture_plan(plan, st) == OCRT_OK) {
+            CK(cudaGraphLaunch(plan->gexec, st));
+            plan->launches = plan->graph_launches;
+            plan->executes++;
+            return OCRT_OK;
+        }
+        plan->graph_off = true;    // capture not possible on this stream: stay eager
+        plan->launches = 0;
+        for (int c = 0; c < KC_N; ++c) plan->cnt[c] = 0;
+    }
     for (Group &g : plan->groups) {
-        const int rc = run_group(plan, g, st);
+        const int rc = run_group(plan, g, st, false);
         if (rc) return rc;
     }
+    plan->executes++;
     return OCRT_OK;
 }
 
@@ -888,11 +1076,9 @@ int ocrt_gb_plan_results(ocrt_plan *plan, ocrt_result *out, void *stream)
     double om = 0;
     for (Group &g : plan->groups) {
         std::vector<ocrt_result> r(g.P);
-        int err = 0;
         CK(cudaMemcpyAsync(r.data(), g.res, sizeof(ocrt_result) * g.P, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&err, g.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (err) return fail(err, "non-finite field during the SOS iteration");
+        const int rc = group_flags(plan, g, st);
+        if (rc) return rc;
         for (int q = 0; q < g.P; ++q) { out[g.idx[q]] = r[q]; om += r[q].order_modes; }
     }
     plan->order_modes = om;
@@ -950,7 +1136,10 @@ int ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, doubl
             }
             for (const PixDev &d : g.hpx) {
                 if (!(d.surface == 2 && d.wind > 0.0)) continue;
-                plan->flops[KC_COXMUNK] += 18.0 * (N * N + N) * d.nphi * (d.M + 1);
+                // pairs evaluated: Gauss-Gauss once per reciprocal couple, the
+                // view row and the sun column in full; all N^2 + N written
+                const double pairs = N * (N + 1) / 2 + (NR - N) * (N + 1) + N;
+                plan->flops[KC_COXMUNK] += 18.0 * pairs * d.nphi * (d.M + 1);
                 plan->bytes[KC_COXMUNK] += (N * N + N) * 9.0 * (d.M + 1) * 4.0;
             }
         }
@@ -972,6 +1161,32 @@ int ocrt_gb_plan_stats(const ocrt_plan *plan, double *order_modes_total, long lo
     return OCRT_OK;
 }
 
+int ocrt_gb_plan_graph_ready(const ocrt_plan *plan) { return plan && plan->gexec ? 1 : 0; }
+
+int ocrt_gb_autotune_summary(char *buf, int len)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    std::string t;
+    for (const TuneRec &r : g_tune) {
+        t += r.kernel;
+        t += " key=";
+        for (size_t i = 0; i < r.key.size(); ++i) t += (i ? "," : "") + std::to_string(r.key[i]);
+        t += " best=" + std::to_string(r.best) + " ms:";
+        for (const auto &m : r.ms) {
+            char b[48];
+            snprintf(b, sizeof(b), " %d=%.4f", m.first, m.second);
+            t += b;
+        }
+        t += "\n";
+    }
+    if (buf && len > 0) {
+        const size_t n = std::min(t.size(), (size_t)len - 1);
+        memcpy(buf, t.data(), n);
+        buf[n] = 0;
+    }
+    return (int)t.size();
+}
+
 void ocrt_gb_plan_destroy(ocrt_plan *plan)
 {
     if (!plan) return;
@@ -979,6 +1194,7 @@ void ocrt_gb_plan_destroy(ocrt_plan *plan)
     if (g_stream) cudaStreamSynchronize(g_stream);
     for (Group &g : plan->groups) free_group(g);
     for (auto &e : plan->ev) { cudaEventDestroy(e.second.first); cudaEventDestroy(e.second.second); }
+    if (plan->gexec) cudaGraphExecDestroy(plan->gexec);
     delete plan;
 }
 
@@ -1023,6 +1239,8 @@ int ocrt_gb_plan_gradients(ocrt_plan *plan, ocrt_grad *grad, void *stream)
         std::vector<double> h((size_t)g.P * n_cot * g.grad_stride);
         CK(cudaMemcpyAsync(h.data(), g.grad, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        const int rc = group_flags(plan, g, st);
+        if (rc) return rc;
         for (int q = 0; q < g.P; ++q) {
             const int i = g.idx[q], nt = g.hpx[q].nt;
             for (int r = 0; r < n_cot; ++r) {

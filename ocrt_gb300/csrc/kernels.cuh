@@ -13,6 +13,15 @@ __global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const 
                        float *Tc, float *Ca, float *Cb);
 __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt);
 __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx);
+// k_tables launch shape: grid (tasks, tables_yblocks), one (outgoing, incoming)
+// pair per thread; moments are staged TB_LC at a time (even).
+#define TB_LC 16
+__host__ __device__ inline int tables_orows(int threads, int N) { return threads / N + 2; }
+inline int tables_yblocks(int threads, int NR, int N) { return (NR * N + threads - 1) / threads; }
+inline size_t tables_smem_bytes(int threads, int N, int L)
+{
+    return sizeof(float) * (4 * ((size_t)L + 1) + 8 * (size_t)tables_orows(threads, N) * TB_LC + 3 * (size_t)TB_LC * N);
+}
 __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
@@ -136,6 +145,7 @@ __global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, i
                               const float *Bp, const float *Br, const float *Bt, int L);
 inline size_t mol_smem_bytes(const Geom &G) { return sizeof(float) * (4 * G.N + G.COUT * 24 + 32 * G.CIN + 32 * 25); }
 __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks);
+__global__ void k_stop_check(const int *active_after_last, int *flag);
 
 // post.cu
 __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,

@@ -94,6 +94,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     cudaStream_t st = (cudaStream_t)stream;
     NA_CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     NA_CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    NA_CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     NA_CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 
     // ---- host staging (stack only) ----
@@ -229,8 +230,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_CK(cudaMemsetAsync(molcnt, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
         NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
         NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, Bx));
-        NA_LAUNCH(k_tables<<<nw, 256, sizeof(float) * 4 * ((size_t)L + 1), st>>>(tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz,
-                                               ops, pvec, W.fvec));
+        NA_LAUNCH(k_tables<<<dim3(nw, tables_yblocks(256, G.NR, G.N)), 256, tables_smem_bytes(256, G.N, L), st>>>(
+            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= opts->max_orders; ++it) {

@@ -311,7 +311,6 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
     const int La = aer ? d.L_aer : -1;
     const float *bx = Bx + (size_t)tl * 2 * 3 * (L + 1);        // [which][comp][l]
     const size_t gb = (size_t)m * (L + 1) * N;
-    const int vs = d.view_slot;
     // basis accessor: slot s in 0..N-1 Gauss, s == N view, s == -1 solar
     auto basis = [&](int comp, int s, int l) -> float {
         if (s < 0) return bx[(size_t)(0 * 3 + comp) * (L + 1) + l];
@@ -338,36 +337,87 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
     __syncthreads();
 
     // ---- operator pairs (o ring slot, i Gauss) ----
-    for (int e = threadIdx.x; e < n * N; e += blockDim.x) {
-        const int o = e / N, i = e - o * N;
-        const int os = o;    // ring slot (the view node, when inserted, is slot N)
-        // accumulators: [row i, col o] products, even (E) / odd (O) in l+m
-        float E[9] = {0}, O[9] = {0}, Et[4] = {0}, Ot[4] = {0};
-        for (int l = m; l <= Lp; ++l) {
-            const float be = smom[l], ga = smom[(Lp + 1) + l];
-            const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
-            const float Pi = basis(0, i, l), Ri = basis(1, i, l), Ti = basis(2, i, l);
-            const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
-            float v[9] = {Pi * Po * be, Pi * Ro * ga, Pi * To * ga, Ti * To * ze, Ri * Ro * al,
-                          Ti * Ro * al, Ri * To * ze, Ti * To * al, Ri * Ro * ze};
-            float vt[4] = {Po * Ti * ga, Po * Ri * ga, To * Ri * al, Ro * Ti * ze};
-            if (((l + m) & 1) == 0) {
+    // Block y of the task takes pairs [y * blockDim, (y + 1) * blockDim) of the
+    // n * N pairs, one per thread.  Every pair product is (incoming basis) x
+    // (outgoing basis x moment); the eight outgoing factors Y_k(o, l) and the
+    // incoming bases X_c(i, l) are staged in shared memory TB_LC moments at a
+    // time, so a pair costs 13 FMAs per moment.  l starts at m and chunks are
+    // even, so the parity of l + m is the parity of the chunk offset.
+    float *Ys = smom + 4 * (L + 1);                               // [8][PO][TB_LC]
+    const int PO = tables_orows(blockDim.x, N);
+    float *Xs = Ys + 8 * PO * TB_LC;                              // [3][TB_LC][N]
+    const int npair = n * N, e0 = blockIdx.y * blockDim.x;
+    if (e0 < npair) {
+    const int e1 = min(e0 + (int)blockDim.x, npair);
+    const int o_lo = e0 / N, nor = (e1 - 1) / N - o_lo + 1;
+    const int e = e0 + threadIdx.x;
+    const bool mine = e < e1;
+    const int o = mine ? e / N : o_lo, i = mine ? e - o * N : 0;
+    const int os = o;    // ring slot (the view node, when inserted, is slot N)
+    // Y_k = basis(comp_k) x moment(mom_k), one nibble per k (k = 0 lowest):
+    // comp {P, R, T, T, R, T, R, P}, moment {beta, gamma, gamma, zeta, alpha, alpha, zeta, gamma}
+    // with moments 0 beta, 1 gamma, 2 alpha, 3 zeta
+    constexpr unsigned ycomp = 0x01212210u, ymom = 0x13223110u;
+    // accumulators 0..8: [row i, col o] products, 9..12: transposed pair; even (E) / odd (O) in l+m
+    float E[13], O[13];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) E[q] += v[q];
+    for (int q = 0; q < 13; ++q) { E[q] = 0.f; O[q] = 0.f; }
+    for (int l0 = m; l0 <= Lp; l0 += TB_LC) {
+        __syncthreads();
+        // Y: one (outgoing row, moment) per thread, all eight factors
+        for (int x = threadIdx.x; x < nor * TB_LC; x += blockDim.x) {
+            const int oo = x / TB_LC, lc = x % TB_LC, l = l0 + lc;
+            float bc[3] = {0.f, 0.f, 0.f}, mo[4] = {0.f, 0.f, 0.f, 0.f};
+            if (l <= Lp) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q) Et[q] += vt[q];
-            } else {
+                for (int c = 0; c < 3; ++c) bc[c] = basis(c, o_lo + oo, l);
 #pragma unroll
-                for (int q = 0; q < 9; ++q) O[q] += v[q];
+                for (int q = 0; q < 4; ++q) mo[q] = smom[q * (Lp + 1) + l];
+            }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) Ot[q] += vt[q];
+            for (int k = 0; k < 8; ++k)
+                Ys[(k * PO + oo) * TB_LC + lc] = bc[(ycomp >> (4 * k)) & 15] * mo[(ymom >> (4 * k)) & 15];
+        }
+        // X: the Gauss bases of moments l0 .. l0 + TB_LC - 1 are contiguous rows of Bp / Br / Bt
+        const int xe = min(TB_LC, Lp + 1 - l0) * N;
+        for (int x = threadIdx.x; x < TB_LC * N; x += blockDim.x) {
+            const size_t gsrc = gb + (size_t)l0 * N + x;
+            const bool in = x < xe;
+            Xs[x] = in ? Bp[gsrc] : 0.f;
+            Xs[TB_LC * N + x] = in ? Br[gsrc] : 0.f;
+            Xs[2 * TB_LC * N + x] = in ? Bt[gsrc] : 0.f;
+        }
+        __syncthreads();
+        if (mine) {
+            const float *yb = Ys + (o - o_lo) * TB_LC;
+#pragma unroll
+            for (int lc = 0; lc < TB_LC; lc += 4) {
+                float4 y[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) y[k] = *reinterpret_cast<const float4 *>(yb + k * PO * TB_LC + lc);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float Pi = Xs[(0 * TB_LC + lc + u) * N + i], Ri = Xs[(1 * TB_LC + lc + u) * N + i],
+                                Ti = Xs[(2 * TB_LC + lc + u) * N + i];
+                    float Y[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) Y[k] = u == 0 ? y[k].x : u == 1 ? y[k].y : u == 2 ? y[k].z : y[k].w;
+                    float *A = (u & 1) ? O : E;
+                    A[0] = fmaf(Pi, Y[0], A[0]);  A[1] = fmaf(Pi, Y[1], A[1]);  A[2] = fmaf(Pi, Y[2], A[2]);
+                    A[3] = fmaf(Ti, Y[3], A[3]);  A[4] = fmaf(Ri, Y[4], A[4]);  A[5] = fmaf(Ti, Y[4], A[5]);
+                    A[6] = fmaf(Ri, Y[3], A[6]);  A[7] = fmaf(Ti, Y[5], A[7]);  A[8] = fmaf(Ri, Y[6], A[8]);
+                    A[9] = fmaf(Ti, Y[7], A[9]);  A[10] = fmaf(Ri, Y[7], A[10]);
+                    A[11] = fmaf(Ri, Y[5], A[11]); A[12] = fmaf(Ti, Y[6], A[12]);
+                }
             }
         }
+    }
+    if (mine) {
         float S[9], D[9], St[4], Dt[4];
 #pragma unroll
         for (int q = 0; q < 9; ++q) { S[q] = E[q] + O[q]; D[q] = E[q] - O[q]; }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) { St[q] = Et[q] + Ot[q]; Dt[q] = Et[q] - Ot[q]; }
+        for (int q = 0; q < 4; ++q) { St[q] = E[9 + q] + O[9 + q]; Dt[q] = E[9 + q] - O[9 + q]; }
         // tables: value at +col = S, at -col = sigma * D with sigma from the column basis
         float c[18];
         c[0] = S[0];             c[1] = D[0];               // pfm[i][+-o]
@@ -382,6 +432,8 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
         const float w = (float)gw[i];
         put_pair(Aop, G, os, i, w, c);
     }
+    }
+    if (blockIdx.y != 0) return;
     // ---- molecular operator (m <= 2) in factored form U[c_out][24] ----
     // Every molecular entry is (function of the outgoing direction) x
     // w_i f(mu_i), f in {1, P2m, R2m, T2m}; U holds the outgoing factors for
@@ -535,11 +587,16 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
 // rows; SMT = the table is in shared memory (else read through the read-only
 // cache).  sm_R holds R (and R tan^2(beta) when DW) on the half grid.  Ends with
 // a block barrier so the caller can reuse sm_R.
+// mirror: o and i are both Gauss slots and the pair (i, o) is written here
+// too.  Swapping mu_out and mu_in leaves the facet geometry, Fresnel matrix,
+// slope density and shadowing unchanged and turns the two rotations into
+// each other's transposes, so R(i <- o) = R(o <- i)^T at every azimuth, and
+// so for every Fourier coefficient.
 template <bool DW, bool SMT>
 __device__ __forceinline__ void coxmunk_pair(int p, int o, int i, const TaskDev *tasks, const PixDev &d,
                                              const int *pix_task0, const Geom &G, const double *gmu,
                                              const float *tab, int Mtab, const double *lamv, const double *lamd,
-                                             float *srf, float *srfW, float *sm_R)
+                                             float *srf, float *srfW, float *sm_R, bool mirror)
 {
     // Per-pair scalars are formed in FP32 (FP64 issues at a small fraction of
     // the FP32 rate on this part and every thread of the block needs them).
@@ -657,6 +714,15 @@ __device__ __forceinline__ void coxmunk_pair(int p, int o, int i, const TaskDev 
                 const size_t off = i < N ? ((size_t)os * N + i) * 9 + e : (size_t)G.NR * N * 9 + (size_t)os * 9 + e;
                 srf[tk.srf_off + off] = acc[a][b] * sc;
                 if (DW) srfW[tk.srf_off + off] = (ca * acc[a][b] + cb * acct[AT == 5 ? a : 0][b]) * sc;
+                if (mirror) {
+                    // entry (r, c) of the pair is entry (c, r) of the reciprocal pair
+                    const int et = (e % 3) * 3 + e / 3;
+                    float st = m == 0 ? scale0 : scale1;
+                    if (m > 0 && (et == 2 || et == 5)) st = -st;
+                    const size_t offt = ((size_t)i * N + os) * 9 + et;
+                    srf[tk.srf_off + offt] = acc[a][b] * st;
+                    if (DW) srfW[tk.srf_off + offt] = (ca * acc[a][b] + cb * acct[AT == 5 ? a : 0][b]) * st;
+                }
             }
     }
     __syncthreads();
@@ -670,8 +736,10 @@ __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const 
     const int p = p0 + blockIdx.z;
     const PixDev &d = px[p];
     if (!d.rough || (int)blockIdx.y >= d.n_ring) return;
-    coxmunk_pair<false, false>(p, blockIdx.y, blockIdx.x, tasks, d, pix_task0, G, gmu, cs_tab, Mtab, lamv, nullptr,
-                               srf, nullptr, sm_R);
+    const int o = blockIdx.y, i = blockIdx.x;
+    if (o < G.N && i < G.N && o > i) return;      // written by the reciprocal block (i, o)
+    coxmunk_pair<false, false>(p, o, i, tasks, d, pix_task0, G, gmu, cs_tab, Mtab, lamv, nullptr, srf, nullptr, sm_R,
+                               o < G.N && i < G.N && o < i);
 }
 
 __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
@@ -682,8 +750,10 @@ __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, con
     const int p = p0 + blockIdx.z;
     const PixDev &d = px[p];
     if (!d.rough || (int)blockIdx.y >= d.n_ring) return;
-    coxmunk_pair<true, false>(p, blockIdx.y, blockIdx.x, tasks, d, pix_task0, G, gmu, cs_tab, Mtab, lamv, lamd, srf,
-                              srfW, sm_R);
+    const int o = blockIdx.y, i = blockIdx.x;
+    if (o < G.N && i < G.N && o > i) return;      // written by the reciprocal block (i, o)
+    coxmunk_pair<true, false>(p, o, i, tasks, d, pix_task0, G, gmu, cs_tab, Mtab, lamv, lamd, srf, srfW, sm_R,
+                              o < G.N && i < G.N && o < i);
 }
 
 // cos / sin(m phi_q) on the half azimuth grid for m = 0..M, followed by the

@@ -83,7 +83,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     const double aP = pv[c], mP = pv[G.LDC + c];
     float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
     float2 *Tot = W.Tot + tk.fld_off;
-    const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off, *hh = B.h + d.lev_off;
+    const double *hh = B.h + d.lev_off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const int NR = G.NR;
     // flat reflected beam: Stokes s uses kernel components (s, s+3)
@@ -258,7 +258,6 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
     }
     __syncthreads();
     float *J = W.J + tk.fld_off;
-    const double *yd = B.yd + d.lev_off;
     for (int e = threadIdx.x; e < nk * G.COUT; e += blockDim.x) {
         const int k = e / G.COUT, c = e - k * G.COUT;
         const float *u = U + c * 24, *x = xi + k * 25;
@@ -524,4 +523,11 @@ __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
     for (int g = 0; g < N; ++g) f += B.gmu[g] * B.gw[g] * dn(g);
     o.fdn = f;
     B.tout[tg] = o;
+}
+
+// A graph replay runs each wave for the order count an eager execute
+// recorded; this flags a replay that ends with a task still active.
+__global__ void k_stop_check(const int *active_after_last, int *flag)
+{
+    if (threadIdx.x == 0 && *active_after_last != 0) atomicExch(flag, 1);
 }
