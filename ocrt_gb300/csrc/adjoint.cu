@@ -220,7 +220,7 @@ __global__ void k_adj_init(BatchBufs B, AdjBufs A, Geom G, int t0, int nadj)
 // Down column (forward I[0] = 0, I[k] = T_{k-1} I[k-1] + Ca_{k-1} J[k] + Cb_{k-1} J[k-1]):
 //   nu[nt] = a[nt], nu[k] = a[k] + T_k nu[k+1];
 //   muJ[k] = Ca_{k-1} nu[k] (k > 0) + Cb_k nu[k+1] (k < nt).
-__global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j)
+__global__ void __launch_bounds__(512, 2) k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j)
 {
     __shared__ double red[32];
     const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
@@ -242,80 +242,62 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
         // The view columns are outputs only (zero quadrature weight): the
         // transposed source never writes them, so they are cleared here once read.
         const bool clear = c >= G.CIN;
-        // Levels in chunks of PF: every load of a chunk is issued before the
-        // dependent recurrence runs.
-        constexpr int PF = 6;
-        if (h == 0) {
-            float nup = 0.f;
-            for (int k1 = 0; k1 <= nt; k1 += PF) {
-                const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
-                float av[PF], tv[PF], ca[PF], cb[PF];
-                float2 ov[PF];
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 + q;
-                        const size_t o = (size_t)k * G.LDC + c;
-                        av[q] = a[o]; ov[q] = At[o];
-                        tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
-                        ca[q] = k < nt ? Ca[k * NR + g] : 0.f;
-                        cb[q] = k > 0 ? Cb[(k - 1) * NR + g] : 0.f;
-                    }
+        // Each column walks its levels in its (transposed) transport direction,
+        // step j at level j (upward columns) or nt - j (downward columns), with
+        // the adjoint order, its total and the coefficients of the next
+        // SCAN_DEPTH steps in flight as cp.async copies into this thread's own
+        // shared-memory slots (refilled only after the values read are used).
+        extern __shared__ float scan_smem[];
+        const int bs = blockDim.x;
+        float *As = scan_smem;                                             // [SCAN_DEPTH][bs]
+        float2 *Ts = reinterpret_cast<float2 *>(As + SCAN_DEPTH * bs);      // [SCAN_DEPTH][bs]
+        float *Cs = reinterpret_cast<float *>(Ts + SCAN_DEPTH * bs);        // [SCAN_DEPTH][3][bs]
+        // coefficient rows of step j: upward tv, cb at k - 1 and ca at k;
+        // downward tv, cb at k and ca at k - 1 (absent rows read as zero)
+        auto issue = [&](int j) {
+            if (j <= nt) {
+                const int k = h == 0 ? j : nt - j, sl = j & (SCAN_DEPTH - 1);
+                const size_t o = (size_t)k * G.LDC + c;
+                if (h == 0 || k > 0) {            // the TOA downward radiance is fixed at zero
+                    cp_async4(As + sl * bs + c, a + o);
+                    cp_async8(Ts + sl * bs + c, At + o);
                 }
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 + q;
-                        const size_t o = (size_t)k * G.LDC + c;
-                        const float2 t = df_add(ov[q], av[q]);
-                        At[o] = t;
-                        if (clear) a[o] = 0.f;
-                        mi = fmaxf(mi, fabsf(av[q]));
-                        mt = fmaxf(mt, fabsf(t.x));
-                        const float nu = av[q] + tv[q] * nup;
-                        split_store(mjH, mjL, o, ca[q] * nu + cb[q] * nup);
-                        nup = nu;
-                    }
+                const int kt = h == 0 ? k - 1 : k, ka = h == 0 ? k : k - 1;
+                if (kt >= 0 && kt < nt) {
+                    cp_async4(Cs + (sl * 3 + 0) * bs + c, Tc + kt * NR + g);
+                    cp_async4(Cs + (sl * 3 + 2) * bs + c, Cb + kt * NR + g);
                 }
+                if (ka >= 0 && ka < nt) cp_async4(Cs + (sl * 3 + 1) * bs + c, Ca + ka * NR + g);
             }
-            if (d.surf_on) A.bc[(size_t)ta * NR * 3 + g * 3 + s] = nup;
-        } else {
-            float nun = 0.f;
-            for (int k1 = nt; k1 >= 0; k1 -= PF) {
-                const int cnt = k1 + 1 < PF ? k1 + 1 : PF;
-                float av[PF], tv[PF], ca[PF], cb[PF];
-                float2 ov[PF];
+            cp_async_commit();
+        };
 #pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 - q;
-                        const size_t o = (size_t)k * G.LDC + c;
-                        av[q] = k > 0 ? a[o] : 0.f;          // the TOA downward radiance is fixed at zero
-                        ov[q] = k > 0 ? At[o] : make_float2(0.f, 0.f);
-                        tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
-                        ca[q] = k > 0 ? Ca[(k - 1) * NR + g] : 0.f;
-                        cb[q] = k < nt ? Cb[k * NR + g] : 0.f;
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 - q;
-                        const size_t o = (size_t)k * G.LDC + c;
-                        if (k > 0) {
-                            const float2 t = df_add(ov[q], av[q]);
-                            At[o] = t;
-                            if (clear) a[o] = 0.f;
-                            mi = fmaxf(mi, fabsf(av[q]));
-                            mt = fmaxf(mt, fabsf(t.x));
-                        }
-                        const float nu = av[q] + tv[q] * nun;
-                        split_store(mjH, mjL, o, ca[q] * nu + cb[q] * nun);
-                        nun = nu;
-                    }
-                }
+        for (int j = 0; j < SCAN_DEPTH; ++j) issue(j);
+        float nup = 0.f;
+        for (int j = 0; j <= nt; ++j) {
+            cp_async_wait<SCAN_DEPTH - 1>();
+            const int k = h == 0 ? j : nt - j, sl = j & (SCAN_DEPTH - 1);
+            const int kt = h == 0 ? k - 1 : k, ka = h == 0 ? k : k - 1;
+            const bool has_a = h == 0 || k > 0;
+            const float av = has_a ? As[sl * bs + c] : 0.f;
+            const float tv = kt >= 0 && kt < nt ? Cs[(sl * 3 + 0) * bs + c] : 0.f;
+            const float cb = kt >= 0 && kt < nt ? Cs[(sl * 3 + 2) * bs + c] : 0.f;
+            const float ca = ka >= 0 && ka < nt ? Cs[(sl * 3 + 1) * bs + c] : 0.f;
+            const size_t o = (size_t)k * G.LDC + c;
+            if (has_a) {
+                const float2 t = df_add(Ts[sl * bs + c], av);
+                At[o] = t;
+                if (clear) a[o] = 0.f;
+                mi = fmaxf(mi, fabsf(av));
+                mt = fmaxf(mt, fabsf(t.x));
             }
+            const float nu = av + tv * nup;
+            split_store(mjH, mjL, o, ca * nu + cb * nup);
+            nup = nu;
+            issue(j + SCAN_DEPTH);
         }
+        cp_async_wait<0>();
+        if (h == 0 && d.surf_on) A.bc[(size_t)ta * NR * 3 + g * 3 + s] = nup;
     }
     mi = (float)block_max_a(mi, red);
     __syncthreads();
@@ -482,177 +464,162 @@ __global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0
     A.AF[adj_off(tk, G, A.ncot, r) + (size_t)d.nt * G.LDC + col_of(G, sp, 1, i)] += pw * acc;
 }
 
-// Final pass per adjoint task.  Pass 1 (thread per column) runs the
-// transposed transport over the adjoint total in FP64 and keeps nu in the
-// (now free) adjoint field buffer.  Pass 2 gives each warp whole levels (lanes
-// over columns, coalesced rows) and forms, with the forward total field F_tot
-// and total source J_tot = S Xs + J_1:
+// Final pass per adjoint task: the transposed transport of the adjoint total
+// (the nu recurrence) fused with the per-level contractions.  With the forward
+// total field F_tot and total source J_tot = S Xs + J_1:
 //   lev_ssa[k] = sum_c muJ[k][c] J_tot[k][c]            (x_k, y_k and J_1 scale with the albedo)
 //   lev_j1[k]  = sum_c muJ[k][c] J_1[k][c]              (J_1 ~ exp(-h_k/mu0))
 //   lay[l]     = sum_c nu . (F dT + J dCa + J dCb)_l    (layer-l transport coefficients)
 // plus, at the surface, mu_bc . dRsurf/dW . Xs_dn(BOA) and the seed terms.
-__global__ void __launch_bounds__(512, 1) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
+// Each thread owns one column and walks its levels in the column's transport
+// direction, so nu, muJ and the neighbouring level's J_tot are in registers
+// when a level's terms are formed; each warp sums its lanes per level with
+// shuffles.  The block's first half of threads takes the upward columns and
+// the second half the downward ones (launch with 2 round32(3N + 3) threads),
+// so every warp runs one direction.  Per-warp level sums sit in shared memory
+// [warp][3][nt + 1] and are added in warp order, so the result does not
+// depend on scheduling.
+__global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
 {
+    extern __shared__ float wsum[];
     __shared__ double red[32];
     const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
-    const int nt = d.nt, NR = G.NR, N = G.N;
+    const int nt = d.nt, NR = G.NR, N = G.N, L1 = nt + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float *ws = wsum + (size_t)warp * 3 * L1;
+    for (int x = lane; x < 3 * L1; x += 32) ws[x] = 0.f;
+    __syncwarp();
     const size_t off = adj_off(tk, G, A.ncot, r);
-    float *nuv = A.AF + off;
     const float2 *At = A.ATot + off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const float *dT = A.dTc + d.coef_off, *dA = A.dCa + d.coef_off, *dB = A.dCb + d.coef_off;
-    // ---- pass 1: nu = transposed transport of the adjoint total (FP64 recurrence)
+    const float *lv = B.lvf + 3 * (size_t)d.lev_off;                 // x, y, ch per level
+    const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
+    const float *Jx = W.J + tk.fld_off;
+    const float2 *Tot = W.Tot + tk.fld_off;
+    // Threads [0, half) take the upward columns (h = 0), [half, 2 half) the
+    // downward ones, so every warp runs one direction; half = round32(3N + 3).
+    const int half = blockDim.x >> 1;
+    const int h = threadIdx.x >= half ? 1 : 0, u = threadIdx.x - h * half;
+    int s = 0, g = G.NR;
+    if (u < 3 * N) { s = u / N; g = u - s * N; }
+    else if (u < 3 * N + 3) { s = u - 3 * N; g = N; }
+    const int c = g < N ? col_of(G, s, h, g) : 6 * N + 2 * s + h;
+    const bool valid = g < d.n_ring;
+    const float fa = valid ? pv[c] : 0.f, fm = valid ? pv[G.LDC + c] : 0.f;
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    const unsigned dmask = __ballot_sync(0xffffffffu, valid && h == 1);
     double gW = 0.0, gS = 0.0;
-    {
-        const int c = threadIdx.x;
-        int s = 0, h = 0, g = 0;
-        if (c < G.COUT) decode_col_a(G, c, s, h, g);
-        const bool valid = c < G.COUT && g < d.n_ring;
-        constexpr int PF = 8;
-        if (valid && h == 0) {
-            float nu = 0.f;
-            for (int k1 = 0; k1 <= nt; k1 += PF) {
-                const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
-                float av[PF], tv[PF];
+    float nu_boa = 0.f;
+    constexpr int PF = 6;
+    for (int dir = 0; dir < 2; ++dir) {
+        if ((dir == 0 ? (vmask & ~dmask) : dmask) == 0) continue;        // warp-uniform
+        const bool on = valid && h == dir;
+        float nu_prev = 0.f, jt_prev = 0.f;
+        // step j visits level k = j (upward columns: nu from the TOA down) or
+        // k = nt - j (downward columns: nu from the BOA up, nu_0 = 0)
+        for (int j1 = 0; j1 <= nt; j1 += PF) {
+            const int cnt = nt - j1 + 1 < PF ? nt - j1 + 1 : PF;
+            float av[PF], tv[PF], ca[PF], cb[PF], jx[PF], tt[PF], xk[PF], yk[PF], chk[PF], lt[PF], la[PF], lb[PF];
 #pragma unroll
-                for (int q = 0; q < PF; ++q)
-                    if (q < cnt) {
-                        const int k = k1 + q;
-                        const float2 t = At[(size_t)k * G.LDC + c];
-                        av[q] = t.x + t.y;
+            for (int q = 0; q < PF; ++q) {
+                av[q] = tv[q] = ca[q] = cb[q] = jx[q] = tt[q] = xk[q] = yk[q] = chk[q] = lt[q] = la[q] = lb[q] = 0.f;
+                if (on && q < cnt) {
+                    const int k = dir == 0 ? j1 + q : nt - j1 - q;
+                    const size_t o = (size_t)k * G.LDC + c;
+                    const float2 t = At[o];
+                    av[q] = t.x + t.y;
+                    jx[q] = Jx[o];
+                    tt[q] = Tot[o].x;
+                    xk[q] = lv[3 * k]; yk[q] = lv[3 * k + 1]; chk[q] = lv[3 * k + 2];
+                    if (dir == 0) {
                         tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
-                    }
-#pragma unroll
-                for (int q = 0; q < PF; ++q)
-                    if (q < cnt) {
-                        nu = av[q] + tv[q] * nu;
-                        nuv[(size_t)(k1 + q) * G.LDC + c] = nu;
-                    }
-            }
-            if (d.rough) {
-                // surface terms: wind derivative of the boundary operator and of
-                // the direct-beam seed, and the seed's optical-depth dependence
-                const float *XsH = W.FH + tk.fld_off + (size_t)nt * G.LDC, *XsL = W.FL + tk.fld_off + (size_t)nt * G.LDC;
-                auto Xs = [&](int col) -> double { return (double)XsH[col] + (double)XsL[col]; };
-                const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
-                const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
-                double acc = 0.0;
-                for (int i = 0; i < N; ++i) {
-                    const double pw = pwm[i];
-                    const float *Ri = RW + (size_t)i * 9;
-                    acc += pw * ((double)Ri[0] * Xs(col_of(G, 0, 1, i)) + (double)Ri[1] * Xs(col_of(G, 1, 1, i)) +
-                                 (double)Ri[2] * Xs(col_of(G, 2, 1, i)));
-                }
-                const double tdn = exp(-d.tau_total / d.mu0);
-                const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
-                const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
-                const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
-                const double E = (double)B.Eatt[(d.lev_off + nt) * NR + g];
-                gW = nu * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
-                gS = nu * fs * tdn * E * (double)Rs[g * 9 + s * 3];
-            }
-        } else if (valid) {
-            float nu = 0.f;
-            for (int k1 = nt; k1 >= 1; k1 -= PF) {
-                const int cnt = k1 < PF ? k1 : PF;
-                float av[PF], tv[PF];
-#pragma unroll
-                for (int q = 0; q < PF; ++q)
-                    if (q < cnt) {
-                        const int k = k1 - q;
-                        const float2 t = At[(size_t)k * G.LDC + c];
-                        av[q] = t.x + t.y;
+                        ca[q] = k < nt ? Ca[k * NR + g] : 0.f;
+                        cb[q] = k > 0 ? Cb[(k - 1) * NR + g] : 0.f;
+                        if (k > 0) {
+                            const int e = (k - 1) * NR + g;
+                            lt[q] = dT[e]; la[q] = dA[e]; lb[q] = dB[e];
+                        }
+                    } else {
                         tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
+                        ca[q] = k > 0 ? Ca[(k - 1) * NR + g] : 0.f;
+                        cb[q] = k < nt ? Cb[k * NR + g] : 0.f;
+                        if (k < nt) {
+                            const int e = k * NR + g;
+                            lt[q] = dT[e]; la[q] = dA[e]; lb[q] = dB[e];
+                        }
                     }
-#pragma unroll
-                for (int q = 0; q < PF; ++q)
-                    if (q < cnt) {
-                        nu = av[q] + tv[q] * nu;
-                        nuv[(size_t)(k1 - q) * G.LDC + c] = nu;
-                    }
+                }
             }
-            nuv[c] = 0.f;
+#pragma unroll
+            for (int q = 0; q < PF; ++q) {
+                if (q >= cnt) break;                                        // warp-uniform
+                const int k = dir == 0 ? j1 + q : nt - j1 - q;
+                float vs = 0.f, vj = 0.f, vl = 0.f;
+                if (on) {
+                    const float nu = (dir == 1 && k == 0) ? 0.f : av[q] + tv[q] * nu_prev;
+                    // dir 0: mu = Ca_k nu_k + Cb_{k-1} nu_{k-1};  dir 1: mu = Ca_{k-1} nu_k + Cb_k nu_{k+1}
+                    const float mu = ca[q] * nu + cb[q] * nu_prev;
+                    const float j1v = chk[q] * (xk[q] * fa + yk[q] * fm);
+                    const float jt = jx[q] + j1v;
+                    vs = mu * jt;
+                    vj = mu * j1v;
+                    // layer term of the layer between this level and the previous step's:
+                    // dir 0 (layer k-1): nu_{k-1} (F_k dT + J_{k-1} dCa + J_k dCb)
+                    // dir 1 (layer k):   nu_{k+1} (F_k dT + J_{k+1} dCa + J_k dCb)
+                    vl = nu_prev * (tt[q] * lt[q] + jt_prev * la[q] + jt * lb[q]);
+                    nu_prev = nu;
+                    jt_prev = jt;
+                }
+                vs = warp_sum(vs);
+                vj = warp_sum(vj);
+                vl = warp_sum(vl);
+                if (lane == 0) {
+                    ws[k] += vs;
+                    ws[L1 + k] += vj;
+                    const int kl = dir == 0 ? k - 1 : k;
+                    if (kl >= 0 && kl < nt) ws[2 * L1 + kl] += vl;
+                }
+            }
         }
+        if (dir == 0) nu_boa = nu_prev;
+    }
+    if (valid && h == 0 && d.rough) {
+        // surface terms: wind derivative of the boundary operator and of
+        // the direct-beam seed, and the seed's optical-depth dependence
+        const float *XsH = W.FH + tk.fld_off + (size_t)nt * G.LDC, *XsL = W.FL + tk.fld_off + (size_t)nt * G.LDC;
+        auto Xs = [&](int col) -> double { return (double)XsH[col] + (double)XsL[col]; };
+        const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
+        const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
+        double acc = 0.0;
+        for (int i = 0; i < N; ++i) {
+            const double pw = pwm[i];
+            const float *Ri = RW + (size_t)i * 9;
+            acc += pw * ((double)Ri[0] * Xs(col_of(G, 0, 1, i)) + (double)Ri[1] * Xs(col_of(G, 1, 1, i)) +
+                         (double)Ri[2] * Xs(col_of(G, 2, 1, i)));
+        }
+        const double tdn = exp(-d.tau_total / d.mu0);
+        const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
+        const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
+        const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
+        const double E = (double)B.Eatt[(d.lev_off + nt) * NR + g];
+        gW = nu_boa * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
+        gS = nu_boa * fs * tdn * E * (double)Rs[g * 9 + s * 3];
     }
     gW = block_sum_a(gW, red);
     __syncthreads();
     gS = block_sum_a(gS, red);
     __syncthreads();
-    // ---- pass 2: a warp per level, lanes over columns
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
-    const double *ch = B.ch + d.lev_off, *xd = B.xd + d.lev_off, *yd = B.yd + d.lev_off;
-    const float *Jx = W.J + tk.fld_off;
-    const float2 *Tot = W.Tot + tk.fld_off;
     double *go = A.gout + (size_t)ta * A.gstride;
-    // Each lane takes CU columns per pass (32 * CU apart) and issues all their
-    // loads before the arithmetic, so a warp keeps many row loads in flight.
-    constexpr int CU = 4;
-    for (int k = warp; k <= nt; k += nwarp) {
-        const float xk = (float)xd[k], yk = (float)yd[k], chk = (float)ch[k];
-        const float xp = k > 0 ? (float)xd[k - 1] : 0.f, yp = k > 0 ? (float)yd[k - 1] : 0.f;
-        const float chp = k > 0 ? (float)ch[k - 1] : 0.f;
-        float ssa_c = 0.f, j1_c = 0.f, lay_c = 0.f;
-        for (int c0 = lane; c0 < G.COUT; c0 += 32 * CU) {
-            float nu_k[CU], nu_p[CU], nu_n[CU], jx[CU], jxp[CU], fa[CU], fm[CU], tt[CU], ttp[CU];
-            int hh[CU], gg[CU];
-#pragma unroll
-            for (int u = 0; u < CU; ++u) {
-                const int c = c0 + 32 * u;
-                int s_, h_, g_;
-                decode_col_a(G, c < G.COUT ? c : G.COUT, s_, h_, g_);
-                hh[u] = h_;
-                gg[u] = g_ < d.n_ring ? g_ : -1;
-                if (gg[u] < 0) continue;
-                const size_t o = (size_t)k * G.LDC + c;
-                fa[u] = pv[c]; fm[u] = pv[G.LDC + c];
-                nu_k[u] = nuv[o];
-                nu_p[u] = k > 0 ? nuv[o - G.LDC] : 0.f;
-                nu_n[u] = k < nt ? nuv[o + G.LDC] : 0.f;
-                jx[u] = Jx[o];
-                jxp[u] = k > 0 ? Jx[o - G.LDC] : 0.f;
-                tt[u] = Tot[o].x;
-                ttp[u] = k > 0 ? Tot[o - G.LDC].x : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < CU; ++u) {
-                const int g = gg[u];
-                if (g < 0) continue;
-                float mu;
-                if (hh[u] == 0) {
-                    mu = k < nt ? Ca[k * NR + g] * nu_k[u] : 0.f;
-                    if (k > 0) mu += Cb[(k - 1) * NR + g] * nu_p[u];
-                } else {
-                    mu = k > 0 ? Ca[(k - 1) * NR + g] * nu_k[u] : 0.f;
-                    if (k < nt) mu += Cb[k * NR + g] * nu_n[u];
-                }
-                const float j1 = chk * (xk * fa[u] + yk * fm[u]);
-                const float jt = jx[u] + j1;
-                ssa_c += mu * jt;
-                j1_c += mu * j1;
-                if (k > 0) {
-                    const int e = (k - 1) * NR + g;
-                    const float jtp = jxp[u] + chp * (xp * fa[u] + yp * fm[u]);
-                    if (hh[u] == 0)
-                        lay_c += nu_p[u] * (tt[u] * dT[e] + jtp * dA[e] + jt * dB[e]);
-                    else
-                        lay_c += nu_k[u] * (ttp[u] * dT[e] + jt * dA[e] + jtp * dB[e]);
-                }
-            }
-        }
-        ssa_c = warp_sum(ssa_c);
-        j1_c = warp_sum(j1_c);
-        lay_c = warp_sum(lay_c);
-        if (lane == 0) {
-            go[k] = ssa_c;
-            go[A.kstride + k] = j1_c;
-            if (k > 0) go[2 * A.kstride + k - 1] = lay_c;
-        }
+    for (int x = threadIdx.x; x < 3 * L1; x += blockDim.x) {
+        const int q = x / L1, k = x - q * L1;
+        float v = 0.f;
+        for (int w = 0; w < nwarp; ++w) v += wsum[(size_t)w * 3 * L1 + x];
+        go[(size_t)q * A.kstride + k] = v;
     }
     if (threadIdx.x == 0) {
-        go[2 * A.kstride + nt] = 0.0;
         go[3 * A.kstride + 0] = gW;
         go[3 * A.kstride + 1] = gS;
     }

@@ -658,7 +658,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     const int surf_threads = ((3 * G.N + 31) / 32) * 32;
     if (!capture) w.adj_stop = INT_MAX;
     for (int j = 1; j <= g.max_orders; ++j) {
-        LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<na, scan_threads, 0, st>>>(B, A, G, w.t0, j));
+        LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<na, scan_threads, scan_smem_bytes(scan_threads), st>>>(B, A, G, w.t0, j));
         if (capture) {
             if (j == w.adj_stop) break;
         } else if ((j - 1) % 4 == 0 || j == g.max_orders) {
@@ -679,7 +679,8 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     }
     if (capture && w.adj_stop != INT_MAX)
         LAUNCH(plan, KC_ADJ_OTHER, k_stop_check<<<1, 32, 0, st>>>(g.acnt + w.adj_stop, g.err + 1));
-    LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<na, scan_threads, 0, st>>>(
+    const int grad_threads = 2 * ((3 * G.N + 3 + 31) / 32) * 32;
+    LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<na, grad_threads, sizeof(float) * 3 * ((size_t)g.ntmax + 1) * (grad_threads / 32), st>>>(
                B, W, A, G, w.t0));
     LAUNCH(plan, KC_ADJ_GRAD, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
                B, W, A, G, w.p0, w.t0));
@@ -788,7 +789,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             else if (w.n_mol)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
-            LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, 0, st>>>(B, W, G, w.t0, it));
+            LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, scan_smem_bytes(scan_threads), st>>>(B, W, G, w.t0, it));
             if (capture) {
                 if (it == w.fwd_stop) break;
             } else if ((it - 1) % poll == 0 || it == g.max_orders) {
@@ -859,9 +860,12 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_coxmunk_dw, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_adj_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_adj_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     g_device = device;
     return OCRT_OK;

@@ -133,6 +133,22 @@ __host__ __device__ inline float round_tf32f(float v)
 #endif
 }
 
+#ifdef __CUDACC__
+// Per-thread asynchronous global -> shared copies (cp.async, cached in L1).
+__device__ inline void cp_async4(float *dst_smem, const float *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ inline void cp_async8(float2 *dst_smem, const float2 *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+#endif
+
 __host__ __device__ inline void split_store(float *hi, float *lo, size_t o, float v)
 {
     const float h = round_tf32f(v);

@@ -13,6 +13,10 @@ __global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const 
                        float *Tc, float *Ca, float *Cb);
 __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt);
 __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx);
+// k_scan: levels in flight per column (cp.async ring depth, a power of two)
+// and its dynamic shared memory: J, the float2 total and 3 coefficients per slot.
+#define SCAN_DEPTH 8
+inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (4 + 8 + 12); }
 // k_tables launch shape: grid (tasks, tables_yblocks), one (outgoing, incoming)
 // pair per thread; moments are staged TB_LC at a time (even).
 #define TB_LC 16

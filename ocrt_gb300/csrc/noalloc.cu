@@ -95,6 +95,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     NA_CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     NA_CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    NA_CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     NA_CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 
     // ---- host staging (stack only) ----
@@ -239,7 +240,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
             if (nmol > 0)
                 NA_LAUNCH(k_mol_lowrank<<<dim3(nmol * ((K + 31) / 32)), 256, mol_smem_bytes(G), st>>>(
                     B, W, G, t0, it, (K + 31) / 32, Bp, Br, Bt, L));
-            NA_LAUNCH(k_scan<<<nw, scan_threads, 0, st>>>(B, W, G, t0, it));
+            NA_LAUNCH(k_scan<<<nw, scan_threads, scan_smem_bytes(scan_threads), st>>>(B, W, G, t0, it));
             if ((it - 1) % 4 == 0 || it == opts->max_orders) {
                 int left_active = 0;
                 NA_CK(cudaMemcpyAsync(&left_active, active + it, sizeof(int), cudaMemcpyDeviceToHost, st));

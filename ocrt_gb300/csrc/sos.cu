@@ -331,9 +331,10 @@ __device__ inline double block_max(double v, double *red)
     return v;
 }
 
-__global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
+__global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
 {
     __shared__ float redf[32];
+    extern __shared__ float scan_smem[];
     __shared__ int item_s;
     const int n_items = B.active_cnt[it - 1];
     for (;;) {
@@ -379,86 +380,53 @@ __global__ void __launch_bounds__(512, 1) k_scan(BatchBufs B, WaveBufs W, Geom G
     float mi = 0.f, mt = 0.f;
     int bad = 0;
     if (valid) {
+        // Each column walks its nt + 1 levels in its transport direction (step
+        // j: level nt - j upward, j downward).  The J, total and coefficient
+        // values of the next SCAN_DEPTH steps are in flight as cp.async copies
+        // into this thread's own shared-memory slots, so the recurrence never
+        // waits on a memory round trip; a slot is refilled only after the
+        // values read from it have been used.
+        const int bs = blockDim.x;
+        float *Js = scan_smem;                                             // [SCAN_DEPTH][bs]
+        float2 *Ts = reinterpret_cast<float2 *>(Js + SCAN_DEPTH * bs);      // [SCAN_DEPTH][bs]
+        float *Cs = reinterpret_cast<float *>(Ts + SCAN_DEPTH * bs);        // [SCAN_DEPTH][3][bs]
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
-        auto put = [&](int k, float I) {
+        auto issue = [&](int j) {
+            if (j <= nt) {
+                const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
+                const size_t o = (size_t)k * G.LDC + c;
+                cp_async4(Js + sl * bs + c, J + o);
+                cp_async8(Ts + sl * bs + c, Tot + o);
+                if (j > 0) {
+                    const int e = (h == 0 ? k : k - 1) * NR + g;
+                    cp_async4(Cs + (sl * 3 + 0) * bs + c, Tc + e);
+                    cp_async4(Cs + (sl * 3 + 1) * bs + c, Ca + e);
+                    cp_async4(Cs + (sl * 3 + 2) * bs + c, Cb + e);
+                }
+            }
+            cp_async_commit();
+        };
+#pragma unroll
+        for (int j = 0; j < SCAN_DEPTH; ++j) issue(j);
+        float I = h == 0 ? bc : 0.f, Jp = 0.f;
+        for (int j = 0; j <= nt; ++j) {
+            cp_async_wait<SCAN_DEPTH - 1>();
+            const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
+            const float jv = Js[sl * bs + c];
+            const float2 ov = Ts[sl * bs + c];
+            if (j > 0)
+                I = Cs[(sl * 3 + 0) * bs + c] * I + Cs[(sl * 3 + 1) * bs + c] * jv + Cs[(sl * 3 + 2) * bs + c] * Jp;
+            Jp = jv;
             const size_t o = (size_t)k * G.LDC + c;
             split_store(FH, FL, o, I);
-            const float2 t = df_add(Tot[o], I);
+            const float2 t = df_add(ov, I);
             Tot[o] = t;
             mi = fmaxf(mi, fabsf(I));
             mt = fmaxf(mt, fabsf(t.x));
-        };
-        // Levels are processed in chunks of PF: every load of a chunk is issued
-        // before the dependent recurrence runs, so the scan is not bound by one
-        // memory round trip per level.
-        constexpr int PF = 6;
-        if (h == 0) {
-            float I = bc;
-            put(nt, I);
-            float Jn = J[(size_t)nt * G.LDC + c];
-            for (int k1 = nt - 1; k1 >= 0; k1 -= PF) {
-                const int cnt = k1 + 1 < PF ? k1 + 1 : PF;
-                float jv[PF], tv[PF], av[PF], bv[PF];
-                float2 ov[PF];
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 - q, e = k * NR + g;
-                        jv[q] = J[(size_t)k * G.LDC + c];
-                        tv[q] = Tc[e]; av[q] = Ca[e]; bv[q] = Cb[e];
-                        ov[q] = Tot[(size_t)k * G.LDC + c];
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 - q;
-                        I = tv[q] * I + av[q] * jv[q] + bv[q] * Jn;
-                        Jn = jv[q];
-                        const size_t o = (size_t)k * G.LDC + c;
-                        split_store(FH, FL, o, I);
-                        const float2 t = df_add(ov[q], I);
-                        Tot[o] = t;
-                        mi = fmaxf(mi, fabsf(I));
-                        mt = fmaxf(mt, fabsf(t.x));
-                    }
-                }
-            }
-            bad = !isfinite(I);
-        } else {
-            float I = 0.f;
-            put(0, I);
-            float Jp = J[c];
-            for (int k1 = 1; k1 <= nt; k1 += PF) {
-                const int cnt = nt - k1 + 1 < PF ? nt - k1 + 1 : PF;
-                float jv[PF], tv[PF], av[PF], bv[PF];
-                float2 ov[PF];
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 + q, e = (k - 1) * NR + g;
-                        jv[q] = J[(size_t)k * G.LDC + c];
-                        tv[q] = Tc[e]; av[q] = Ca[e]; bv[q] = Cb[e];
-                        ov[q] = Tot[(size_t)k * G.LDC + c];
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < PF; ++q) {
-                    if (q < cnt) {
-                        const int k = k1 + q;
-                        I = tv[q] * I + av[q] * jv[q] + bv[q] * Jp;
-                        Jp = jv[q];
-                        const size_t o = (size_t)k * G.LDC + c;
-                        split_store(FH, FL, o, I);
-                        const float2 t = df_add(ov[q], I);
-                        Tot[o] = t;
-                        mi = fmaxf(mi, fabsf(I));
-                        mt = fmaxf(mt, fabsf(t.x));
-                    }
-                }
-            }
-            bad = !isfinite(I);
+            issue(j + SCAN_DEPTH);
         }
+        cp_async_wait<0>();
+        bad = !isfinite(I);
     }
     if (bad) atomicExch(B.err, -2);
     mi = block_maxf(mi, redf);
