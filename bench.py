@@ -150,19 +150,18 @@ def peaks():
 
 
 def traffic_from_profiles(kernel, alg_bytes_per_launch):
-    """DRAM bytes per launch for `kernel`: the measured ratio of ncu DRAM
-    traffic to algorithmic bytes (profiles/traffic.json, captured on a smaller
-    case of the same kernel) times this run's algorithmic bytes per launch."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes per launch for kernel class `kernel`: the ratio of ncu DRAM
+    traffic to algorithmic bytes measured on a smaller case of the same
+    kernel (profiles/dram_traffic.txt: `class ratio kernel` lines) times this
+    run's algorithmic bytes per launch."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     if not os.path.exists(path):
         return None
-    try:
-        d = json.load(open(path)).get(kernel)
-        if not d:
-            return None
-        return d["dram_bytes_over_alg_bytes"] * alg_bytes_per_launch
-    except Exception:
-        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and not line.startswith("#") and parts[0] == kernel:
+            return float(parts[1]) * alg_bytes_per_launch
+    return None
 
 
 def oracle_lib():
@@ -333,6 +332,10 @@ def run_ours(args, rank, world):
                 "avg_launch_ms": per_launch_ms, "alg_bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                 "intensity_flop_per_byte": intensity if d["flops"] > 0 else None, "ridge_flop_per_byte": ridge,
                 "tensor_frac_of_bf16": tensor_frac}
+    if roof.get("traffic"):
+        # DRAM bytes actually moved per launch (measured ratio x algorithmic) over the launch time
+        roof["traffic_gbs"] = roof["traffic"] / (per_launch_ms / 1e3) / 1e9
+        roof["traffic_frac_of_hbm"] = roof["traffic_gbs"] / pk["hbm_gbs"]
     breakdown = {k: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps,
                      "share": v["ms"] / max(sum(x["ms"] for x in kstats.values()), 1e-9),
                      "alg_bytes_per_step": v["bytes"] / args.steps, "alg_flops_per_step": v["flops"] / args.steps}
