@@ -128,12 +128,12 @@ __global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0)
     int s, h, g;
     decode_col_a(G, c, s, h, g);
     if (g >= d.n_ring) return;
-    float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
+    float *F = W.F + tk.fld_off;
     const float2 *Tot = W.Tot + tk.fld_off;
     for (int k = 0; k <= d.nt; ++k) {
         const size_t o = (size_t)k * G.LDC + c;
         const float2 t = Tot[o];
-        split_store(FH, FL, o, ((t.x - FH[o]) - FL[o]) + t.y);
+        F[o] = (t.x - F[o]) + t.y;
     }
 }
 
@@ -589,8 +589,8 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
     if (valid && h == 0 && d.rough) {
         // surface terms: wind derivative of the boundary operator and of
         // the direct-beam seed, and the seed's optical-depth dependence
-        const float *XsH = W.FH + tk.fld_off + (size_t)nt * G.LDC, *XsL = W.FL + tk.fld_off + (size_t)nt * G.LDC;
-        auto Xs = [&](int col) -> double { return (double)XsH[col] + (double)XsL[col]; };
+        const float *Xb = W.F + tk.fld_off + (size_t)nt * G.LDC;
+        auto Xs = [&](int col) -> double { return (double)Xb[col]; };
         const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
         const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
         double acc = 0.0;

@@ -238,11 +238,10 @@ struct Group {
     double *kappa = nullptr, *taudir = nullptr;
     int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
-    float *FH = nullptr, *FL = nullptr, *J = nullptr, *ops = nullptr, *opsH = nullptr, *opsL = nullptr;
+    float *F = nullptr, *J = nullptr, *ops = nullptr;
     float *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     float2 *Tot = nullptr;
     bool use_tc = false;
-    CUtensorMap mapFH, mapFL, mapAH, mapAL;
     // per-layer overrides and the adjoint (ocrt_gb_solve_batch_adjoint)
     bool any_layers = false;
     int ncot = 0, ntmax = 0;
@@ -316,7 +315,7 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.FH, g.FL, g.J, g.ops, g.opsH, g.opsL, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJH,
                     g.AJL, g.Abc, g.Ast, g.acnt, g.awork, g.opsTH, g.opsTL,
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
@@ -428,7 +427,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t pf = nm * K * G.LDC;
         const size_t po = (nm + 2 * std::min<size_t>(nm, 3)) * op_elems;
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
-        size_t pb = pf * 20 + po * 12 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 16 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)G.CIN * ((G.COUT + 31) & ~31) * 4;
@@ -478,7 +477,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.work, 4 * ((size_t)g.max_orders + 2))) || (rc = alloc(g.err, 2)) ||
         (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
         (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
-        (rc = alloc(g.FH, g.wave_fld)) || (rc = alloc(g.FL, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
+        (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
         (rc = alloc(g.Tot, g.wave_fld)) ||
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
@@ -506,18 +505,11 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
             (rc = alloc(g.grad, (size_t)g.P * ncot * g.grad_stride)))
             return rc;
     }
-    // ---- source kernels: tcgen05 for the aerosol contraction when the
-    // geometry allows it, CUDA cores otherwise; the low-rank molecular kernel
-    // adds the m <= 2 Rayleigh term.  The per-order task lists themselves are
-    // built on the device (k_primary, k_scan). ----
+    // ---- source kernels: tcgen05 for the aerosol contraction and the dense
+    // m <= 2 molecular operator when the geometry allows it, CUDA cores
+    // otherwise.  The per-order task lists themselves are built on the device
+    // (k_primary, k_scan). ----
     g.use_tc = tc_supported(G) && !force_simt();
-    if (g.use_tc) {
-        if ((rc = alloc(g.opsH, g.wave_ops)) || (rc = alloc(g.opsL, g.wave_ops))) return rc;
-        g.use_tc = make_map(&g.mapFH, g.FH, g.wave_fld / G.LDC, G.LDC, 128) &&
-                   make_map(&g.mapFL, g.FL, g.wave_fld / G.LDC, G.LDC, 128) &&
-                   make_map(&g.mapAH, g.opsH, g.wave_ops / G.CIN, G.CIN, G.NP) &&
-                   make_map(&g.mapAL, g.opsL, g.wave_ops / G.CIN, G.CIN, G.NP);
-    }
     if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
         const int KP = (G.COUT + 31) & ~31;
         if ((rc = alloc(g.opsTH, (size_t)g.wave_tasks * G.CIN * KP)) ||
@@ -631,11 +623,10 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     LAUNCH(plan, KC_ADJ_TOTALS, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
     if (w.n_simt) LAUNCH(plan, KC_ADJ_TOTALS, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
     if (w.n_tc)
-        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it,
-                                                                              mtiles, 0));
+        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(B, W, G, w.t0, it, mtiles, 0));
     if (w.n_mol && w.n_tc)
-        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), 256, tc_smem, st>>>(
-                   g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it, mtiles, 1));
+        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), tc_fwd_threads(), tc_smem, st>>>(
+                   B, W, G, w.t0, it, mtiles, 1));
     else if (w.n_mol)
         LAUNCH(plan, KC_ADJ_TOTALS, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                    B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
@@ -721,7 +712,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     B.mol_cnt = g.mol_cnt; B.work = g.work;
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     WaveBufs W;
-    W.FH = g.FH; W.FL = g.FL; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.opsH = g.opsH; W.opsL = g.opsL;
+    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops;
     W.pvec = g.pvec;
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
@@ -748,7 +739,6 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         if (g.use_tc) {
             LAUNCH(plan, KC_TABLES, k_mol_dense<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.Lmax, g.Bp, g.Br, g.Bt,
                                                                      g.gw, g.ops));
-            LAUNCH(plan, KC_TABLES, k_split_ops<<<4 * g_nsm, 256, 0, st>>>(g.ops, g.opsH, g.opsL, w.ops));
         }
         if (w.any_rough) {
             const bool dw = g.ncot > 0;
@@ -781,11 +771,11 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             if (w.n_simt)
                 LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
             if (w.n_tc)
-                LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<tc_grid, 256, tc_smem, st>>>(
-                           g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it, mtiles, 0));
+                LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(
+                           B, W, G, w.t0, it, mtiles, 0));
             if (w.n_mol && w.n_tc)
-                LAUNCH(plan, KC_MOL, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), 256, tc_smem, st>>>(
-                           g.mapFH, g.mapFL, g.mapAH, g.mapAL, B, W, G, w.t0, it, mtiles, 1));
+                LAUNCH(plan, KC_MOL, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), tc_fwd_threads(), tc_smem, st>>>(
+                           B, W, G, w.t0, it, mtiles, 1));
             else if (w.n_mol)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));

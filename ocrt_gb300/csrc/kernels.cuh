@@ -50,11 +50,10 @@ __global__ void k_level_float(const PixDev *px, int P, const double *xd, const d
 #define ST_M_TILE 64
 #define ST_N_TILE 64
 struct WaveBufs {
-    float *FH, *FL;        // field of the current order as tf32 (hi, lo) planes, wave-relative by TaskDev::fld_off
+    float *F;              // field of the current order (FP32), wave-relative by TaskDev::fld_off
     float *J;              // source of the current order
     float2 *Tot;           // order totals (hi, lo) pairs
     float *ops;            // operators, wave-relative (FP32)
-    float *opsH, *opsL;    // the same operators as tf32 (hi, lo) planes, for the tensor-core contraction
     float *pvec, *fvec;    // per wave-task primary and flat-beam vectors
     float *srf;            // rough surface kernels, wave-relative
 };
@@ -130,9 +129,7 @@ __global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L,
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
-__global__ void k_source_tc(const __grid_constant__ CUtensorMap mFH, const __grid_constant__ CUtensorMap mFL,
-                            const __grid_constant__ CUtensorMap mAH, const __grid_constant__ CUtensorMap mAL,
-                            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode);
+__global__ void k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode);
 __global__ void k_adj_source_tc(const __grid_constant__ CUtensorMap mJH, const __grid_constant__ CUtensorMap mJL,
                                 const __grid_constant__ CUtensorMap mTH, const __grid_constant__ CUtensorMap mTL,
                                 BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
@@ -141,6 +138,7 @@ __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, con
 __global__ void k_split_ops(const float *ops, float *hi, float *lo, size_t n);
 size_t coxmunk_smem_bytes(int nphi, bool dw);
 size_t tc_smem_bytes(const Geom &G);
+int tc_fwd_threads();          // block size of k_source_tc
 bool tc_supported(const Geom &G);
 size_t tc_adj_smem_bytes(const Geom &G);
 bool tc_adj_supported(const Geom &G);

@@ -155,13 +155,13 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     int *err = cv.take<int>(1);
     float *srf = cv.take<float>(rough ? (size_t)T * srf_elems : 1);
     if (!cv.ok) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
-    const size_t per_task = (size_t)K * G.LDC * 20 + 2 * op_elems * 4 + (size_t)2 * G.LDC * 4 +
+    const size_t per_task = (size_t)K * G.LDC * 16 + 2 * op_elems * 4 + (size_t)2 * G.LDC * 4 +
                             (size_t)24 * NR * 4 + (size_t)6 * (L + 1) * 4 + 8 * 256;
     const size_t left = cv.cap - ((cv.off + 255) & ~size_t(255));
     int Wt = (int)(left / per_task);
     if (Wt > T) Wt = T;
     if (Wt < 1) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
-    float *FH = cv.take<float>((size_t)Wt * K * G.LDC), *FL = cv.take<float>((size_t)Wt * K * G.LDC);
+    float *F = cv.take<float>((size_t)Wt * K * G.LDC);
     float *J = cv.take<float>((size_t)Wt * K * G.LDC);
     float2 *Tot = cv.take<float2>((size_t)Wt * K * G.LDC);
     float *ops = cv.take<float>(2 * (size_t)Wt * op_elems);
@@ -219,7 +219,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work;
     B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
-    W.FH = FH; W.FL = FL; W.J = J; W.Tot = Tot; W.ops = ops; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
+    W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     for (int t0 = 0; t0 < T; t0 += Wt) {
         const int nw = (T - t0) < Wt ? (T - t0) : Wt;

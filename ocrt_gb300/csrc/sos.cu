@@ -81,7 +81,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     const int nt = d.nt;
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
     const double aP = pv[c], mP = pv[G.LDC + c];
-    float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
+    float *F = W.F + tk.fld_off;
     float2 *Tot = W.Tot + tk.fld_off;
     const double *hh = B.h + d.lev_off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
@@ -119,7 +119,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     auto store = [&](int k, float I) {
         float2 t = make_float2(I, 0.f);
         if (d.rough && h == 0) t = df_add(t, rough_seed(tk, W, B, d, G, fs_tdn, k, g, s));
-        split_store(FH, FL, (size_t)k * G.LDC + c, t.x);
+        F[(size_t)k * G.LDC + c] = t.x;
         Tot[(size_t)k * G.LDC + c] = t;
     };
     if (h == 0) {
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
     if (k0 > nt || c0 >= G.COUT) return;
     __shared__ float Fs[ST_K][ST_M + 4];
     __shared__ float As[ST_K][ST_N + 4];
-    const float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
+    const float *F = W.F + tk.fld_off;
     const float *A = W.ops + tk.op_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     float accA[4][4] = {{0}};
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_source_simt(BatchBufs B, WaveBufs W, Ge
             const int lv = idx / ST_K, kk = idx - lv * ST_K;
             const int k = k0 + lv, ci = kc + kk;
             const size_t o = (size_t)k * G.LDC + in_to_col(G, ci);
-            Fs[kk][lv] = (k <= nt && ci < G.CIN) ? FH[o] + FL[o] : 0.f;
+            Fs[kk][lv] = (k <= nt && ci < G.CIN) ? F[o] : 0.f;
         }
         for (int idx = threadIdx.x; idx < ST_K * ST_N; idx += 256) {
             const int cc = idx / ST_K, kk = idx - cc * ST_K;
@@ -241,11 +241,11 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
     }
     const float *Ug = W.ops + tk.mol_off;
     for (int e = threadIdx.x; e < G.COUT * 24; e += blockDim.x) U[e] = Ug[e];
-    const float *FH = W.FH + tk.fld_off + (size_t)k0 * G.LDC, *FL = W.FL + tk.fld_off + (size_t)k0 * G.LDC;
+    const float *F = W.F + tk.fld_off + (size_t)k0 * G.LDC;
     for (int e = threadIdx.x; e < nk * G.CIN; e += blockDim.x) {
         const int k = e / G.CIN, ci = e - k * G.CIN;
         const size_t o = (size_t)k * G.LDC + ci;
-        Fs[k * G.CIN + ci] = FH[o] + FL[o];
+        Fs[k * G.CIN + ci] = F[o];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nk * 24; e += blockDim.x) {
@@ -350,14 +350,14 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
     int s = 0, h = 0, g = 0;
     if (c < G.COUT) decode_col(G, c, s, h, g);
     const bool valid = c < G.COUT && g < d.n_ring;
-    float *FH = W.FH + tk.fld_off, *FL = W.FL + tk.fld_off;
+    float *F = W.F + tk.fld_off;
     const float *J = W.J + tk.fld_off;
     float2 *Tot = W.Tot + tk.fld_off;
     // ---- surface boundary condition from the previous order's BOA downward field
     float bc = 0.f;
     if (valid && h == 0 && d.surf_on) {
-        const float *FbH = FH + (size_t)nt * G.LDC, *FbL = FL + (size_t)nt * G.LDC;
-        auto Fb = [&](int col) -> float { return FbH[col] + FbL[col]; };
+        const float *Fbot = F + (size_t)nt * G.LDC;
+        auto Fb = [&](int col) -> float { return Fbot[col]; };
         if (d.rough) {
             const float *R = W.srf + tk.srf_off + (size_t)g * N * 9 + s * 3;
             const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
                 I = Cs[(sl * 3 + 0) * bs + c] * I + Cs[(sl * 3 + 1) * bs + c] * jv + Cs[(sl * 3 + 2) * bs + c] * Jp;
             Jp = jv;
             const size_t o = (size_t)k * G.LDC + c;
-            split_store(FH, FL, o, I);
+            F[o] = I;
             const float2 t = df_add(ov, I);
             Tot[o] = t;
             mi = fmaxf(mi, fabsf(I));

@@ -3,19 +3,26 @@
 //
 // Per item: one (task, 128-level tile).  D[128 levels][NP outputs] (FP32 in
 // TMEM) = F[128 levels][6N inputs] x Aop^T, K = 6N swept in 32-element tiles
-// (one 128-byte swizzle row).  Both operands arrive already split into tf32
-// (hi, lo) planes (the transport scan and the operator build write them), so
-// every K tile is four TMA loads into a SWIZZLE_128B K-major layout followed
-// by three tcgen05.mma.kind::tf32 passes (hi*hi + hi*lo + lo*hi), which carry
-// FP32-level accuracy on the TF32 tensor path.
+// (one 128-byte swizzle row), each tile as three tcgen05.mma.kind::tf32 passes
+// (hi*hi + hi*lo + lo*hi) over tf32 (hi, lo) splits of both operands, which
+// carry FP32-level accuracy on the TF32 tensor path.
 //
-// Warp roles (256 threads, one CTA per SM, persistent over items):
-//   warp 0  TMA producer: fetches items, fills a 2-stage ring;
+// Forward source (k_source_tc, 512 threads, one CTA per SM, persistent):
+//   warps 8-15 producers: read the FP32 field rows and operator rows of a K
+//           tile straight from global memory, split each value into tf32
+//           (hi, lo) in registers and store both into the SWIZZLE_128B
+//           K-major layout of a 2-stage shared-memory ring (warps 8-11 fill
+//           stage 0, warps 12-15 stage 1, so each group has two tile periods
+//           to cover its load latency); field rows past the task are zero
+//           and never read.  Warp 8 lane 0 also fetches the items.
 //   warp 1  MMA issuer: one thread issues the MMAs into one of two TMEM
 //           accumulators (2 x 256 columns), so the next item's MMAs run while
 //           the epilogue drains the previous one;
 //   warp 2  TMEM allocation owner;
 //   warps 4-7 epilogue: tcgen05.ld of their 32-lane quadrant, J = x_k * D.
+// Adjoint source (k_adj_source_tc, 256 threads): the operands are stored as
+// tf32 planes already, and warp 0 lane 0 fetches items and fills the ring
+// with four TMA loads per K tile instead.
 //
 // Every wait is time-bounded: on timeout the CTA records an error word,
 // drains its own in-flight copies with a second bounded wait, frees TMEM and
@@ -27,10 +34,16 @@
 #define TC_M 128
 #define TC_KT 32
 #define TC_THREADS 256
+#define TC_FWD_THREADS 512
+#define TC_PW0 8            // first producer warp of the forward kernel
+#define TC_PGW 4            // producer warps per stage group
+#define TC_AQ 8             // float4 chunks of a field tile per producer thread (128 rows x 8 / 128)
+#define TC_BQ 14            // operator-tile rows per producer thread, upper bound (NP <= 224)
 #define TC_TMEM_COLS 512
 #define TC_ACC_COLS 256
 #define TC_Q 8
 #define TC_WAIT_NS 2000000000ull
+#define TC_TP 20             // row stride (floats) of an epilogue transpose tile: 16 columns + pad
 
 namespace {
 
@@ -171,6 +184,8 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
     int *qitem = (int *)(qbar + TC_Q);                   // [TC_Q]
     uint32_t *tslot = (uint32_t *)(qitem + TC_Q);
     volatile int *abort_flag = (volatile int *)(tslot + 1);
+    // epilogue transpose tiles: [4 warps][32 rows][TC_TP floats]
+    float *tpose = (float *)(base + 2 * STAGE + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int n_items = (ADJ ? nw : (mode ? B.mol_cnt[it - 1] : B.active_cnt[it - 1])) * mtiles;
     const int *alist = ADJ ? nullptr : (mode ? B.mlist[it & 1] : B.alist[it & 1]);
@@ -185,7 +200,7 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
     }
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
-            mbar_init(&full[i], 1);
+            mbar_init(&full[i], ADJ ? 1 : TC_PGW);
             mbar_init(&empty[i], 1);
             mbar_init(&tfull[i], 1);
             mbar_init(&tempty[i], 4);
@@ -205,8 +220,8 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
     int inflight[2] = {0, 0};
     uint32_t inflight_par[2] = {0, 0};
 
-    if (warp == 0 && lane == 0) {
-        // ---------------- TMA producer ----------------
+    if (ADJ && warp == 0 && lane == 0) {
+        // ---------------- TMA producer (adjoint) ----------------
         uint32_t g = 0;
         for (int j = 0;; ++j) {
             int item = -1;
@@ -260,6 +275,91 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
                 break;
             }
         }
+    } else if (!ADJ && warp >= TC_PW0) {
+        // ---------------- producer warps (forward) ----------------
+        const int pt = tid - TC_PW0 * 32;                 // 0 .. 255
+        const int grp = pt >> 7, gt = pt & 127;           // stage group, thread within the group
+        // Thread gt owns 16-byte chunk ch = gt % 8 of rows r = gt / 8 + 16 i of a
+        // tile; all its rows share r % 8, so their swizzled chunk position
+        // (ch ^ r % 8) is one constant and row i sits 2048 i bytes further.
+        const int r8 = gt >> 3, ch = gt & 7;
+        const uint32_t soff = (uint32_t)r8 * 128u + ((uint32_t)(ch ^ (r8 & 7)) << 4);
+        float4 ra[TC_AQ], rb[TC_BQ];
+        // K tile kt of the item into registers: field rows 0 .. nra - 1 of the
+        // item (zero past the task), operator rows 0 .. NB - 1
+        auto load = [&](const float *Ab, int nra, const float *Bb, int kt) {
+            const float4 *pa = reinterpret_cast<const float4 *>(Ab + (size_t)r8 * G.LDC + kt * TC_KT + ch * 4);
+            const float4 *pb = reinterpret_cast<const float4 *>(Bb + (size_t)r8 * G.CIN + kt * TC_KT + ch * 4);
+#pragma unroll
+            for (int i = 0; i < TC_AQ; ++i)
+                ra[i] = r8 + 16 * i < nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < TC_BQ; ++i)
+                if (r8 + 16 * i < NB) rb[i] = __ldg(pb + (size_t)i * 4 * G.CIN);
+        };
+        // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
+        auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
+            float4 h, l;
+            h.x = round_tf32f(v.x); l.x = round_tf32f(v.x - h.x);
+            h.y = round_tf32f(v.y); l.y = round_tf32f(v.y - h.y);
+            h.z = round_tf32f(v.z); l.z = round_tf32f(v.z - h.z);
+            h.w = round_tf32f(v.w); l.w = round_tf32f(v.w - h.w);
+            *reinterpret_cast<float4 *>(hi + off) = h;
+            *reinterpret_cast<float4 *>(lo + off) = l;
+        };
+        uint32_t g = 0;
+        for (int j = 0;; ++j) {
+            const int slot = j & (TC_Q - 1);
+            if (pt == 0) {
+                int item = -1;
+                while (!*abort_flag) {
+                    const int cand = atomicAdd(counter, 1);
+                    if (cand >= n_items) break;
+                    const int li = cand / mtiles, mt = cand - li * mtiles;
+                    const TaskDev tk = B.tasks[t0 + task_of(li)];
+                    if (mt * TC_M > B.px[tk.pix].nt) continue;
+                    item = cand;
+                    break;
+                }
+                qitem[slot] = item;
+                mbar_arrive(&qbar[slot]);
+            }
+            // one lane per warp waits; the warp leaves every loop together
+            int ok = lane == 0 ? (int)mbar_wait(&qbar[slot], (j / TC_Q) & 1) : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            __syncwarp();                 // orders lane 0's acquire before the other lanes' reads
+            if (!ok) { *abort_flag = 1; break; }
+            const int item = qitem[slot];
+            if (item < 0) break;
+            const int li = item / mtiles, mt = item - li * mtiles;
+            const TaskDev tk = B.tasks[t0 + task_of(li)];
+            const int r0 = mt * TC_M, nra = min(TC_M, tk.K - r0);
+            const float *Ab = W.F + tk.fld_off + (size_t)r0 * G.LDC;
+            const float *Bb = W.ops + (mode ? tk.uv_off : tk.op_off);
+            // this group's K tiles of the item: global tile index g + kt with (g + kt) & 1 == grp
+            const int kt0 = (int)((grp - (int)(g & 1)) & 1);
+            if (kt0 < NKT && !*abort_flag) load(Ab, nra, Bb, kt0);
+            for (int kt = kt0; kt < NKT; kt += 2) {
+                const uint32_t gg = g + (uint32_t)kt, u = gg >> 1;
+                const int s = (int)(gg & 1);
+                int free_ok = (u == 0 || lane != 0) ? 1 : (int)mbar_wait(&empty[s], (u - 1) & 1);
+                free_ok = __shfl_sync(0xffffffffu, free_ok, 0);
+                __syncwarp();
+                if (!free_ok) { *abort_flag = 1; break; }
+                unsigned char *sp = base + (size_t)s * STAGE;
+#pragma unroll
+                for (int i = 0; i < TC_AQ; ++i) put(sp, sp + A_BYTES, soff + 2048u * i, ra[i]);
+#pragma unroll
+                for (int i = 0; i < TC_BQ; ++i)
+                    if (r8 + 16 * i < NB) put(sp + 2 * A_BYTES, sp + 2 * A_BYTES + B_BYTES, soff + 2048u * i, rb[i]);
+                // generic-proxy stores made visible to the tensor cores before the stage is marked full
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
+                if (kt + 2 < NKT) load(Ab, nra, Bb, kt + 2);
+            }
+            g += (uint32_t)NKT;
+        }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
@@ -299,7 +399,7 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
         // every MMA this thread issued has completed before TMEM is released
         umma_commit(done);
         if (!mbar_wait(done, 0)) *abort_flag = 1;
-    } else if (warp >= 4) {
+    } else if (warp >= 4 && warp < 8) {
         // ---------------- epilogue ----------------
         const int q4 = warp - 4;
         for (int j = 0;; ++j) {
@@ -315,36 +415,52 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
             const int row = mt * TC_M + q4 * 32 + lane;
             int k, ncols;
             bool live;
-            float *out;
+            float *outbase;                                  // row 0 of the item's output rows
             if (ADJ) {
                 live = row < AB.ncot * tk.K;
                 k = live ? row % tk.K : 0;
-                out = AB.AF + (size_t)tk.fld_off * AB.ncot + (size_t)row * G.LDC;
+                outbase = AB.AF + (size_t)tk.fld_off * AB.ncot;
                 ncols = G.CIN;
             } else {
                 live = row <= d.nt;
                 k = row;
-                out = W.J + tk.fld_off + (size_t)row * G.LDC;
+                outbase = W.J + tk.fld_off;
                 ncols = G.COUT;
             }
             const float x = live ? B.lvf[3 * (d.lev_off + k) + (mode ? 1 : 0)] : 0.f;
             const uint32_t tb = tmem + (uint32_t)(b * TC_ACC_COLS) + ((uint32_t)(q4 * 32) << 16);
+            // Each 32-row x 16-column chunk goes through a shared-memory
+            // transpose so the stores are row-contiguous: lane l then writes
+            // 16 bytes (columns 4 (l % 4) .. +3) of rows l / 4 + 8 i, i < 4.
+            float *tp = tpose + (size_t)q4 * 32 * TC_TP;
+            const int row0 = mt * TC_M + q4 * 32;            // first row of this warp's quadrant
             for (int cb = 0; cb < NB / 16; ++cb) {
                 float v[16];
                 tmem_ld16(tb + (uint32_t)(cb * 16), v);
-                if (live && mode) {
 #pragma unroll
-                    for (int jj = 0; jj < 16; ++jj) {
-                        const int c = cb * 16 + jj;
-                        if (c < ncols) out[c] += x * v[jj];
-                    }
-                } else if (live) {
+                for (int jj = 0; jj < 16; jj += 4)
+                    *reinterpret_cast<float4 *>(tp + lane * TC_TP + jj) =
+                        make_float4(x * v[jj], x * v[jj + 1], x * v[jj + 2], x * v[jj + 3]);
+                __syncwarp();
+                const int c = cb * 16 + (lane & 3) * 4;
+                if (c + 4 <= G.LDC && c < ncols) {
 #pragma unroll
-                    for (int jj = 0; jj < 16; ++jj) {
-                        const int c = cb * 16 + jj;
-                        if (c < ncols) out[c] = x * v[jj];
+                    for (int i = 0; i < 4; ++i) {
+                        const int rl = (lane >> 2) + 8 * i, rg = row0 + rl;
+                        const bool rlive = ADJ ? rg < AB.ncot * tk.K : rg <= d.nt;
+                        if (!rlive) continue;
+                        float *dst = outbase + (size_t)rg * G.LDC + c;
+                        const float4 t = *reinterpret_cast<const float4 *>(tp + rl * TC_TP + (lane & 3) * 4);
+                        if (!ADJ && mode) {
+                            float4 o = *reinterpret_cast<float4 *>(dst);
+                            o.x += t.x; o.y += t.y; o.z += t.z; o.w += t.w;
+                            *reinterpret_cast<float4 *>(dst) = o;
+                        } else {
+                            *reinterpret_cast<float4 *>(dst) = t;
+                        }
                     }
                 }
+                __syncwarp();
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -366,13 +482,11 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
     }
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
-k_source_tc(const __grid_constant__ CUtensorMap mFH, const __grid_constant__ CUtensorMap mFL,
-            const __grid_constant__ CUtensorMap mAH, const __grid_constant__ CUtensorMap mAL,
-            BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode)
+__global__ void __launch_bounds__(TC_FWD_THREADS, 1)
+k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode)
 {
     AdjBufs none{};
-    source_tc_body<false>(&mFH, &mFL, &mAH, &mAL, B, W, none, G, t0, it, mtiles, 0, mode);
+    source_tc_body<false>(nullptr, nullptr, nullptr, nullptr, B, W, none, G, t0, it, mtiles, 0, mode);
 }
 
 // Transposed contraction of the adjoint for adjoint order `it` (work counter
@@ -387,8 +501,10 @@ k_adj_source_tc(const __grid_constant__ CUtensorMap mJH, const __grid_constant__
 
 static size_t tc_smem_for(int NB)
 {
-    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)NB * TC_KT * 4) + 256;
+    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)NB * TC_KT * 4) + 256 + 4 * 32 * TC_TP * 4;
 }
+
+int tc_fwd_threads() { return TC_FWD_THREADS; }
 
 size_t tc_smem_bytes(const Geom &G)
 {
@@ -407,6 +523,6 @@ bool tc_adj_supported(const Geom &G)
 
 bool tc_supported(const Geom &G)
 {
-    return (G.CIN % TC_KT) == 0 && G.CIN / TC_KT >= 2 && G.NP <= TC_ACC_COLS && G.NP % 16 == 0 &&
-           tc_smem_bytes(G) <= 227 * 1024;
+    return (G.CIN % TC_KT) == 0 && G.CIN / TC_KT >= 2 && G.NP <= TC_ACC_COLS && G.NP <= 16 * TC_BQ &&
+           G.NP % 16 == 0 && (G.LDC % 4) == 0 && tc_smem_bytes(G) <= 227 * 1024;
 }
