@@ -137,6 +137,24 @@ __global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0)
     }
 }
 
+// Rows CIN .. CIN + 31 of a molecular task's transposed operator block:
+// U^T[q][kk] = U[kk][q] for q < 24, kk < COUT (zero elsewhere), the second
+// factor of the transposed rank-24 molecular term in the tcgen05 adjoint pass.
+__global__ void k_mol_utrans(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT)
+{
+    const int tl = blockIdx.x;
+    if (tl >= nw) return;
+    const TaskDev tk = tasks[t0 + tl];
+    if (!tk.has_mol) return;
+    const int KP = (G.COUT + 31) & ~31;
+    const float *U = ops + tk.mol_off;
+    float *T = opsT + (size_t)tl * (G.CIN + 32) * KP + (size_t)G.CIN * KP;
+    for (int e = threadIdx.x; e < 32 * KP; e += blockDim.x) {
+        const int q = e / KP, kk = e - q * KP;
+        T[e] = (q < 24 && kk < G.COUT) ? U[(size_t)kk * 24 + q] : 0.f;
+    }
+}
+
 // Mark every task of the wave active for order index `it` (one source pass).
 __global__ void k_fill_all(BatchBufs B, int t0, int nw, int it)
 {
@@ -156,10 +174,10 @@ __global__ void k_fill_all(BatchBufs B, int t0, int nw, int it)
 }
 
 // Transposed operators for the tcgen05 adjoint source: opsT[tl][cin][kk] =
-// Aop[kk][cin] for kk < COUT, 0 up to KP = COUT rounded up to 32.  32 x 32
+// Aop[kk][cin] for kk < COUT, 0 up to KP = COUT rounded up to 32 (per task
+// CIN + 32 rows of KP; k_mol_utrans fills the last 32 for m <= 2).  32 x 32
 // tiles through shared memory.  Grid (task, CIN/32 tiles, KP/32 tiles), 32 x 8.
-__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsTH,
-                               float *opsTL)
+__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT)
 {
     __shared__ float tile[32][33];
     const int tl = blockIdx.x;
@@ -173,18 +191,11 @@ __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, con
         tile[yy][threadIdx.x] = (row < G.COUT && cin < G.CIN) ? A[(size_t)row * G.CIN + cin] : 0.f;
     }
     __syncthreads();
-    float *TH = opsTH + (size_t)tl * G.CIN * KP, *TL = opsTL + (size_t)tl * G.CIN * KP;
+    float *T = opsT + (size_t)tl * (G.CIN + 32) * KP;
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
         const int cin = c0 + yy, kk = r0 + threadIdx.x;
-        if (cin < G.CIN && kk < KP) split_store(TH, TL, (size_t)cin * KP + kk, tile[threadIdx.x][yy]);
+        if (cin < G.CIN && kk < KP) T[(size_t)cin * KP + kk] = tile[threadIdx.x][yy];
     }
-}
-
-// tf32 (hi, lo) planes of the forward operators for the tensor-core contraction.
-__global__ void k_split_ops(const float *ops, float *hi, float *lo, size_t n)
-{
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-        split_store(hi, lo, e, ops[e]);
 }
 
 // a_1 = e.  One thread per adjoint task.
@@ -235,7 +246,7 @@ __global__ void __launch_bounds__(512, 2) k_adj_scan(BatchBufs B, AdjBufs A, Geo
     const size_t off = adj_off(tk, G, A.ncot, r);
     float *a = A.AF + off;
     float2 *At = A.ATot + off;
-    float *mjH = A.AJH + off, *mjL = A.AJL + off;
+    float *mj = A.AJ + off;
     float mi = 0.f, mt = 0.f;
     if (valid) {
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
@@ -292,7 +303,7 @@ __global__ void __launch_bounds__(512, 2) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                 mt = fmaxf(mt, fabsf(t.x));
             }
             const float nu = av + tv * nup;
-            split_store(mjH, mjL, o, ca * nu + cb * nup);
+            mj[o] = ca * nu + cb * nup;
             nup = nu;
             issue(j + SCAN_DEPTH);
         }
@@ -338,7 +349,7 @@ __global__ void __launch_bounds__(256) k_adj_source(BatchBufs B, WaveBufs W, Adj
     constexpr int KT = 16;
     __shared__ float Ms[KT][ST_M_TILE + 4];
     __shared__ float As[KT][ST_N_TILE + 4];
-    const float *mjH = A.AJH + off, *mjL = A.AJL + off;
+    const float *mj = A.AJ + off;
     const float *Aop = W.ops + tk.op_off;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     float acc[4][4] = {{0}};
@@ -347,7 +358,7 @@ __global__ void __launch_bounds__(256) k_adj_source(BatchBufs B, WaveBufs W, Adj
             const int lv = idx / KT, kk = idx - lv * KT;
             const int k = k0 + lv, row = kc + kk;
             const size_t o = (size_t)k * G.LDC + row;
-            Ms[kk][lv] = (k <= nt && row < G.COUT) ? mjH[o] + mjL[o] : 0.f;
+            Ms[kk][lv] = (k <= nt && row < G.COUT) ? mj[o] : 0.f;
         }
         for (int idx = threadIdx.x; idx < KT * ST_N_TILE; idx += 256) {
             const int kk = idx / ST_N_TILE, cc = idx - kk * ST_N_TILE;
@@ -411,11 +422,11 @@ __global__ void __launch_bounds__(256) k_adj_mol(BatchBufs B, WaveBufs W, AdjBuf
     const float *Ug = W.ops + tk.mol_off;
     for (int e = threadIdx.x; e < G.COUT * 24; e += blockDim.x) U[e] = Ug[e];
     const size_t off = adj_off(tk, G, A.ncot, r);
-    const float *mjH = A.AJH + off + (size_t)k0 * G.LDC, *mjL = A.AJL + off + (size_t)k0 * G.LDC;
+    const float *mj = A.AJ + off + (size_t)k0 * G.LDC;
     for (int e = threadIdx.x; e < nk * G.COUT; e += blockDim.x) {
         const int k = e / G.COUT, c = e - k * G.COUT;
         const size_t o = (size_t)k * G.LDC + c;
-        Ms[k * G.COUT + c] = mjH[o] + mjL[o];
+        Ms[k * G.COUT + c] = mj[o];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < nk * 24; e += blockDim.x) {

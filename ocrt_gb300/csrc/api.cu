@@ -169,42 +169,6 @@ struct Wave {
     int fwd_stop = INT_MAX, adj_stop = INT_MAX;
 };
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn()
-{
-    static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess && q == cudaDriverEntryPointSuccess)
-            fn = (EncodeTiledFn)p;
-        else
-            cudaGetLastError();
-    }
-    return fn;
-}
-
-// 2-D FP32 tensor map, rows x cols (row stride = cols), box {32, box_rows},
-// 128-byte swizzle, zero fill outside the tensor.
-bool make_map(CUtensorMap *map, void *base, size_t rows, int cols, int box_rows)
-{
-    EncodeTiledFn fn = encode_fn();
-    if (!fn) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)cols * 4};
-    const cuuint32_t box[2] = {32, (cuuint32_t)box_rows};
-    const cuuint32_t estr[2] = {1, 1};
-    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
 bool force_simt()
 {
     const char *e = getenv("OCRT_GB_SOURCE_KERNEL");
@@ -239,6 +203,7 @@ struct Group {
     int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
     float *F = nullptr, *J = nullptr, *ops = nullptr;
+    float *molV = nullptr;   // [3][32][CIN] molecular input factors V_m of the tensor-core pass
     float *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     float2 *Tot = nullptr;
     bool use_tc = false;
@@ -247,7 +212,7 @@ struct Group {
     int ncot = 0, ntmax = 0;
     double *ldt = nullptr, *lss = nullptr, *cot = nullptr, *lamd = nullptr, *gout = nullptr,
            *grad = nullptr;
-    float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJH = nullptr, *AJL = nullptr,
+    float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJ = nullptr,
           *Abc = nullptr;
     float2 *ATot = nullptr;
     TaskState *Ast = nullptr;
@@ -257,9 +222,8 @@ struct Group {
     long long lut_ntot = 0;
     double *lut_vza = nullptr, *lut_raa = nullptr, *lut_samp = nullptr, *lut_kappa = nullptr, *lut_out = nullptr;
     int *acnt = nullptr, *awork = nullptr;
-    float *opsTH = nullptr, *opsTL = nullptr;   // transposed operator planes for the tcgen05 adjoint source
+    float *opsT = nullptr;   // transposed aerosol operators for the tcgen05 adjoint source
     bool use_tc_adj = false;
-    CUtensorMap mapJH, mapJL, mapTH, mapTL;
     int gstride = 0, kstride = 0, grad_stride = 0;
 };
 
@@ -315,9 +279,9 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
-                    g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJH,
-                    g.AJL, g.Abc, g.Ast, g.acnt, g.awork, g.opsTH, g.opsTL,
+                    g.err, g.F, g.J, g.ops, g.molV, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
+                    g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
     for (void *p : ptrs) dfree(p);
 }
@@ -497,7 +461,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         if ((rc = up(g.cot, hcot)) || (rc = alloc(g.lamd, (size_t)g.P * (G.N + 2))) ||
             (rc = alloc(g.dTc, g.ncoef)) || (rc = alloc(g.dCa, g.ncoef)) || (rc = alloc(g.dCb, g.ncoef)) ||
             (rc = alloc(g.srfW, g.wave_srf)) || (rc = alloc(g.AF, g.wave_fld * ncot)) ||
-            (rc = alloc(g.AJH, g.wave_fld * ncot)) || (rc = alloc(g.AJL, g.wave_fld * ncot)) ||
+            (rc = alloc(g.AJ, g.wave_fld * ncot)) ||
             (rc = alloc(g.ATot, g.wave_fld * ncot)) ||
             (rc = alloc(g.Abc, na * G.NR * 3)) || (rc = alloc(g.Ast, na)) ||
             (rc = alloc(g.acnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.awork, (size_t)g.max_orders + 2)) ||
@@ -510,14 +474,11 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     // otherwise.  The per-order task lists themselves are built on the device
     // (k_primary, k_scan). ----
     g.use_tc = tc_supported(G) && !force_simt();
+    if (g.use_tc && (rc = alloc(g.molV, (size_t)3 * 32 * G.CIN))) return rc;
     if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
         const int KP = (G.COUT + 31) & ~31;
-        if ((rc = alloc(g.opsTH, (size_t)g.wave_tasks * G.CIN * KP)) ||
-            (rc = alloc(g.opsTL, (size_t)g.wave_tasks * G.CIN * KP))) return rc;
-        g.use_tc_adj = make_map(&g.mapJH, g.AJH, g.wave_fld * ncot / G.LDC, G.LDC, 128) &&
-                       make_map(&g.mapJL, g.AJL, g.wave_fld * ncot / G.LDC, G.LDC, 128) &&
-                       make_map(&g.mapTH, g.opsTH, (size_t)g.wave_tasks * G.CIN, KP, G.CIN) &&
-                       make_map(&g.mapTL, g.opsTL, (size_t)g.wave_tasks * G.CIN, KP, G.CIN);
+        if ((rc = alloc(g.opsT, (size_t)g.wave_tasks * (G.CIN + 32) * KP))) return rc;
+        g.use_tc_adj = true;
     }
     for (Wave &w : g.waves) {
         w.n_simt = g.use_tc ? 0 : w.t1 - w.t0;
@@ -602,7 +563,7 @@ LutBufs make_lut(Group &g)
 AdjBufs make_adj(Group &g)
 {
     AdjBufs A;
-    A.ncot = g.ncot; A.AF = g.AF; A.AJH = g.AJH; A.AJL = g.AJL; A.ATot = g.ATot; A.bc = g.Abc; A.st = g.Ast; A.acnt = g.acnt;
+    A.ncot = g.ncot; A.AF = g.AF; A.AJ = g.AJ; A.opsT = g.opsT; A.ATot = g.ATot; A.bc = g.Abc; A.st = g.Ast; A.acnt = g.acnt;
     A.cot = g.cot; A.gout = g.gout; A.gstride = g.gstride; A.kstride = g.kstride;
     A.dTc = g.dTc; A.dCa = g.dCa; A.dCb = g.dCb; A.srfW = g.srfW; A.grad = g.grad; A.grad_stride = g.grad_stride;
     A.awork = g.awork;
@@ -632,17 +593,18 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
                    B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
     // adjoint successive orders
     CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.AJH, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.AJL, 0, sizeof(float) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.AJ, 0, sizeof(float) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.ATot, 0, sizeof(float2) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
     CK(cudaMemsetAsync(g.awork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
     const int KP = (G.COUT + 31) & ~31;
     const int amt = (g.ncot * w.Kmax + 127) / 128;
-    if (g.use_tc_adj)
+    if (g.use_tc_adj) {
         LAUNCH(plan, KC_ADJ_OTHER, k_op_transpose<<<dim3(nw, (G.CIN + 31) / 32, KP / 32), dim3(32, 8), 0, st>>>(
-                   g.tasks, w.t0, nw, G, g.ops, g.opsTH, g.opsTL));
+                   g.tasks, w.t0, nw, G, g.ops, g.opsT));
+        if (w.n_mol) LAUNCH(plan, KC_ADJ_OTHER, k_mol_utrans<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.ops, g.opsT));
+    }
     const AdjBufs A = make_adj(g);
     LAUNCH(plan, KC_ADJ_OTHER, k_adj_init<<<(na + 127) / 128, 128, 0, st>>>(B, A, G, w.t0, na));
     const dim3 agrid(na, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.LDC + ST_N_TILE - 1) / ST_N_TILE);
@@ -658,11 +620,11 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
             if (*g_pinned == 0) { w.adj_stop = j; break; }
         }
         if (g.use_tc_adj)
-            LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source_tc<<<std::min(nw * amt, g_nsm), 256, tc_adj_smem_bytes(G), st>>>(
-                       g.mapJH, g.mapJL, g.mapTH, g.mapTL, B, W, A, G, w.t0, j, amt, nw));
+            LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source_tc<<<std::min(nw * amt, g_nsm), tc_fwd_threads(), tc_adj_smem_bytes(G),
+                                                         st>>>(B, W, A, G, w.t0, j, amt, nw));
         else
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_source<<<agrid, 256, 0, st>>>(B, W, A, G, w.t0));
-        if (w.n_mol)
+        if (w.n_mol && !g.use_tc_adj)
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_mol<<<dim3(na, ltiles), 256, adj_mol_smem_bytes(G), st>>>(
                        B, W, A, G, w.t0, g.Bp, g.Br, g.Bt, g.Lmax));
         if (w.any_rough)
@@ -695,6 +657,9 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         LAUNCH(plan, KC_SETUP, k_layers_apply<<<P, 256, 0, st>>>(g.px, P, g.ldt, g.lss, g.h, g.ch, g.xd, g.yd, g.err));
     LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
     LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
+    if (g.use_tc)
+        LAUNCH(plan, KC_SETUP, k_mol_vtab<<<std::min(g.Mmax, 2) + 1, 256, 0, st>>>(G, g.Lmax, g.Bp, g.Br, g.Bt, g.gw,
+                                                                                  g.molV));
     if (g.any_rough) {
         LAUNCH(plan, KC_SETUP, k_cs_table<<<g.Mmax + 2, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
         LAUNCH(plan, KC_SETUP, k_seed_att<<<dim3(8, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Eatt));
@@ -711,6 +676,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.Eatt = g.Eatt; B.lvf = g.lvf; B.active_cnt = g.active_cnt; B.err = g.err;
     B.mol_cnt = g.mol_cnt; B.work = g.work;
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
+    B.molV = g.molV;
     WaveBufs W;
     W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops;
     W.pvec = g.pvec;
@@ -736,10 +702,9 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         int rc = tuned_block("k_tables", (const void *)k_tables, {G.N, g.Lmax, g.Mmax}, !capture, st, tables, &tb);
         if (rc) return rc;
         LAUNCH(plan, KC_TABLES, tables(tb));
-        if (g.use_tc) {
+        if (g.use_tc)
             LAUNCH(plan, KC_TABLES, k_mol_dense<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.Lmax, g.Bp, g.Br, g.Bt,
                                                                      g.gw, g.ops));
-        }
         if (w.any_rough) {
             const bool dw = g.ncot > 0;
             const int np = w.p1 - w.p0;

@@ -120,10 +120,10 @@ __host__ __device__ inline float2 df_add(float2 a, float b)
 
 __host__ __device__ inline double df_value(float2 a) { return (double)a.x + (double)a.y; }
 
-// Fields that feed the tensor-core contraction are stored as two planes of
-// tf32 values: hi = RN_tf32(v), lo = RN_tf32(v - hi), so each plane is exact
-// as an MMA operand and hi + lo carries v to ~2^-22 relative.  Readers that
-// need the value add the planes.
+// tf32 rounding (to nearest, ties away from zero) of an FP32 value: the
+// tensor-core contraction splits each operand into hi = RN_tf32(v) and
+// lo = RN_tf32(v - hi), so each part is exact as an MMA operand and hi + lo
+// carries v to ~2^-22 relative.
 __host__ __device__ inline float round_tf32f(float v)
 {
 #ifdef __CUDA_ARCH__
@@ -149,9 +149,3 @@ __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\
 template <int N> __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 #endif
 
-__host__ __device__ inline void split_store(float *hi, float *lo, size_t o, float v)
-{
-    const float h = round_tf32f(v);
-    hi[o] = h;
-    lo[o] = round_tf32f(v - h);
-}

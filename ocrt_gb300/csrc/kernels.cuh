@@ -75,13 +75,17 @@ struct BatchBufs {
     int *mlist[2];         // same for the molecular tasks
     int *work;             // [max_orders + 2][4] work counters of the persistent kernels
     int *err;              // device error word
+    const float *molV;     // [3][32][CIN]: V_m[4b + f][bN + i] = w_i {1, P2m, R2m, T2m}(mu_i), rows 24..31 zero
+                           // (the adjoint's tensor-core pass contracts the transposed molecular term with it)
 };
 
 // adjoint.cu
 struct AdjBufs {
     int ncot;              // cotangent rows per pixel; adjoint task = wave task * ncot + row
     float *AF;             // adjoint field a_j (wave-relative, x ncot)
-    float *AJH, *AJL;      // transposed-transport output muJ as tf32 (hi, lo) planes
+    float *AJ;             // transposed-transport output muJ (FP32, like AF)
+    const float *opsT;     // per wave task [CIN + 32][KP] (FP32, KP = COUT rounded up to 32): the transposed
+                           // aerosol operator, then for m <= 2 the transposed molecular factor U^T (24 rows, 8 zero)
     float2 *ATot;          // adjoint total (hi, lo) pairs
     float *bc;             // mu_bc per adjoint task [NR][3]
     TaskState *st;         // per adjoint task
@@ -124,18 +128,17 @@ __global__ void k_lut_final(const PixDev *px, int P, LutBufs Lb, const int *pix_
 __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
                            const double *yd, const double *mb, const double *lut_vza, const double *lut_raa,
                            double *lut_kappa);
-__global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
-                            const float *Bt, const double *gw, float *ops);
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
 __global__ void k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode);
-__global__ void k_adj_source_tc(const __grid_constant__ CUtensorMap mJH, const __grid_constant__ CUtensorMap mJL,
-                                const __grid_constant__ CUtensorMap mTH, const __grid_constant__ CUtensorMap mTL,
-                                BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
-__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsTH,
-                               float *opsTL);
-__global__ void k_split_ops(const float *ops, float *hi, float *lo, size_t n);
+__global__ void k_adj_source_tc(BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
+__global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
+__global__ void k_mol_utrans(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
+__global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
+                            const float *Bt, const double *gw, float *ops);
+__global__ void k_mol_vtab(Geom G, int L, const float *Bp, const float *Br, const float *Bt, const double *gw,
+                           float *V);
 size_t coxmunk_smem_bytes(int nphi, bool dw);
 size_t tc_smem_bytes(const Geom &G);
 int tc_fwd_threads();          // block size of k_source_tc

@@ -216,7 +216,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     BatchBufs B;
     B.px = px; B.tasks = tasks; B.state = state; B.tout = tout; B.gmu = gmu; B.gw = gw; B.pw = pwt;
     B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs; B.Eatt = Eatt; B.lvf = lvf;
-    B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work;
+    B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work; B.molV = nullptr;
     B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
     W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;

@@ -269,38 +269,6 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
     }
 }
 
-// Dense molecular operator for the tensor-core contraction:
-// UV[c][bN + i] = sum_f U[c][4b + f] fv[f][i], fv[f][i] = w_i {1, P2m, R2m, T2m}(mu_i),
-// so that UV F equals U (V F) of k_mol_lowrank.  Rows COUT..NP-1 are zero.
-// One block per molecular task of the wave.
-__global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
-                            const float *Bt, const double *gw, float *ops)
-{
-    const int tl = blockIdx.x;
-    if (tl >= nw) return;
-    const TaskDev tk = tasks[t0 + tl];
-    if (tk.uv_off < 0) return;
-    const int N = G.N;
-    __shared__ float fv[4 * OCRT_MAX_N];
-    const size_t gb = (size_t)tk.m * (L + 1) * N + (size_t)2 * N;    // degree-2 row of mode m
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const float w = (float)gw[i];
-        fv[i] = w; fv[N + i] = w * Bp[gb + i]; fv[2 * N + i] = w * Br[gb + i]; fv[3 * N + i] = w * Bt[gb + i];
-    }
-    __syncthreads();
-    const float *U = ops + tk.mol_off;
-    float *UV = ops + tk.uv_off;
-    for (int e = threadIdx.x; e < G.NP * G.CIN; e += blockDim.x) {
-        const int c = e / G.CIN, ci = e - c * G.CIN, b = ci / N, i = ci - b * N;
-        float v = 0.f;
-        if (c < G.COUT) {
-            const float *u = U + (size_t)c * 24 + 4 * b;
-            v = u[0] * fv[i] + u[1] * fv[N + i] + u[2] * fv[2 * N + i] + u[3] * fv[3 * N + i];
-        }
-        UV[e] = v;
-    }
-}
-
 __device__ inline float block_maxf(float v, float *red)
 {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -498,4 +466,58 @@ __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
 __global__ void k_stop_check(const int *active_after_last, int *flag)
 {
     if (threadIdx.x == 0 && *active_after_last != 0) atomicExch(flag, 1);
+}
+
+// Dense molecular operator for the tensor-core contraction:
+// UV[c][bN + i] = sum_f U[c][4b + f] fv[f][i], fv[f][i] = w_i {1, P2m, R2m, T2m}(mu_i),
+// so that UV F equals U (V F) of k_mol_lowrank.  Rows COUT..NP-1 are zero.
+// One block per molecular task of the wave.
+__global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
+                            const float *Bt, const double *gw, float *ops)
+{
+    const int tl = blockIdx.x;
+    if (tl >= nw) return;
+    const TaskDev tk = tasks[t0 + tl];
+    if (tk.uv_off < 0) return;
+    const int N = G.N;
+    __shared__ float fv[4 * OCRT_MAX_N];
+    const size_t gb = (size_t)tk.m * (L + 1) * N + (size_t)2 * N;    // degree-2 row of mode m
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float w = (float)gw[i];
+        fv[i] = w; fv[N + i] = w * Bp[gb + i]; fv[2 * N + i] = w * Br[gb + i]; fv[3 * N + i] = w * Bt[gb + i];
+    }
+    __syncthreads();
+    const float *U = ops + tk.mol_off;
+    float *UV = ops + tk.uv_off;
+    for (int e = threadIdx.x; e < G.NP * G.CIN; e += blockDim.x) {
+        const int c = e / G.CIN, ci = e - c * G.CIN, b = ci / N, i = ci - b * N;
+        float v = 0.f;
+        if (c < G.COUT) {
+            const float *u = U + (size_t)c * 24 + 4 * b;
+            v = u[0] * fv[i] + u[1] * fv[N + i] + u[2] * fv[2 * N + i] + u[3] * fv[3 * N + i];
+        }
+        UV[e] = v;
+    }
+}
+
+// Molecular input factors of the tensor-core pass, one block per mode m <= 2:
+// V_m[4b + f][bN + i] = w_i f(mu_i), f in {1, P2m, R2m, T2m} at the Gauss
+// nodes (the xi = V F factor of k_mol_lowrank); rows 24..31 and the entries
+// outside block b are zero.  V[(m * 32 + q) * CIN + cin].
+__global__ void k_mol_vtab(Geom G, int L, const float *Bp, const float *Br, const float *Bt, const double *gw,
+                           float *V)
+{
+    const int m = blockIdx.x, N = G.N;
+    const size_t gb = (size_t)m * (L + 1) * N + (size_t)2 * N;        // degree-2 row of mode m
+    float *Vm = V + (size_t)m * 32 * G.CIN;
+    for (int e = threadIdx.x; e < 32 * G.CIN; e += blockDim.x) {
+        const int q = e / G.CIN, cin = e - q * G.CIN, b = cin / N, i = cin - b * N;
+        float v = 0.f;
+        if (q < 24 && (q >> 2) == b) {
+            const float w = (float)gw[i];
+            const int f = q & 3;
+            v = f == 0 ? w : w * (f == 1 ? Bp[gb + i] : (f == 2 ? Br[gb + i] : Bt[gb + i]));
+        }
+        Vm[e] = v;
+    }
 }

@@ -1,5 +1,5 @@
 // tc_gemm.cu — multiple-scattering source contraction on the tcgen05 tensor
-// cores (rt_sos_operator.c:206-424 for modes without a molecular term, m > 2).
+// cores (rt_sos_operator.c:206-424), aerosol operator and molecular term.
 //
 // Per item: one (task, 128-level tile).  D[128 levels][NP outputs] (FP32 in
 // TMEM) = F[128 levels][6N inputs] x Aop^T, K = 6N swept in 32-element tiles
@@ -7,7 +7,8 @@
 // (hi*hi + hi*lo + lo*hi) over tf32 (hi, lo) splits of both operands, which
 // carry FP32-level accuracy on the TF32 tensor path.
 //
-// Forward source (k_source_tc, 512 threads, one CTA per SM, persistent):
+// Both kernels (k_source_tc, k_adj_source_tc: 512 threads, one CTA per SM,
+// persistent over items):
 //   warps 8-15 producers: read the FP32 field rows and operator rows of a K
 //           tile straight from global memory, split each value into tf32
 //           (hi, lo) in registers and store both into the SWIZZLE_128B
@@ -19,26 +20,22 @@
 //           accumulators (2 x 256 columns), so the next item's MMAs run while
 //           the epilogue drains the previous one;
 //   warp 2  TMEM allocation owner;
-//   warps 4-7 epilogue: tcgen05.ld of their 32-lane quadrant, J = x_k * D.
-// Adjoint source (k_adj_source_tc, 256 threads): the operands are stored as
-// tf32 planes already, and warp 0 lane 0 fetches items and fills the ring
-// with four TMA loads per K tile instead.
+//   warps 4-7 epilogue: tcgen05.ld of their 32-lane quadrant, J = x_k * D,
+//           stored row-contiguous through a shared-memory transpose.
 //
-// Every wait is time-bounded: on timeout the CTA records an error word,
-// drains its own in-flight copies with a second bounded wait, frees TMEM and
-// returns.
+// Every wait is time-bounded: on timeout the CTA records an error word, waits
+// (bounded) for its own MMAs to complete, frees TMEM and returns.
 #include <cuda.h>
 #include <cstdint>
 #include "kernels.cuh"
 
 #define TC_M 128
 #define TC_KT 32
-#define TC_THREADS 256
 #define TC_FWD_THREADS 512
 #define TC_PW0 8            // first producer warp of the forward kernel
 #define TC_PGW 4            // producer warps per stage group
 #define TC_AQ 8             // float4 chunks of a field tile per producer thread (128 rows x 8 / 128)
-#define TC_BQ 14            // operator-tile rows per producer thread, upper bound (NP <= 224)
+#define TC_BQ 14            // B-tile rows per producer thread, upper bound (224 rows)
 #define TC_TMEM_COLS 512
 #define TC_ACC_COLS 256
 #define TC_Q 8
@@ -64,12 +61,6 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;
@@ -91,13 +82,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
         if (mbar_try_wait(bar, parity)) return true;
         if (globaltimer() - t0 > TC_WAIT_NS) return false;
     }
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y)
-{
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-                 ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-                 : "memory");
 }
 
 // Shared-memory matrix descriptor, K-major with 128-byte swizzle: rows of
@@ -155,27 +139,31 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 
 } // namespace
 
-// ADJ = false: forward source.  A rows = levels of one task's field (F planes),
-//   B = the task's operator planes [NP][CIN], K = CIN.  mode 0: the aerosol
-//   operator, J[k][c] = x_k D[k][c] for c < COUT, items = active list x level
-//   tiles; mode 1: the dense molecular operator U V of the m <= 2 tasks,
-//   J[k][c] += y_k D[k][c], items = active molecular list x level tiles (run
-//   after mode 0 on the same order).
+// ADJ = false: forward source.  A rows = levels of one task's field F,
+//   B = [NP][CIN], K = CIN.  mode 0: the aerosol operator, J[k][c] =
+//   x_k D[k][c] for c < COUT, items = active list x level tiles; mode 1: the
+//   dense molecular operator U V of the m <= 2 tasks (rt_sos_operator.c:
+//   387-406), J[k][c] += y_k D[k][c], items = active molecular list x level
+//   tiles (run after mode 0 on the same order).
 // ADJ = true: transposed source of the adjoint.  A rows = the ncot adjoint
-//   fields of one task stacked (ncot * K rows of muJ planes), B = the task's
-//   transposed operator AopT [CIN][KP] planes (KP = COUT rounded up to 32),
-//   K = KP; epilogue a[row][cin] = x_k D[row][cin] for cin < CIN; items =
-//   every task of the wave x tiles, skipped when none of its rows is active.
+//   fields of one task stacked (ncot * K rows of muJ, row stride LDC, columns
+//   past LDC read as zero), B = the task's transposed operator AopT [CIN][KP]
+//   and, for m <= 2, U^T [24][KP] (KP = COUT rounded up to 32), K = KP;
+//   epilogue a[row][cin] = x_k D[row][cin] + y_k sum_f V[4b+f][cin]
+//   D[row][CIN + 4b + f] (cin = bN + i) for cin < CIN; items = every task of
+//   the wave x tiles, skipped when none of its rows is active.
 template <bool ADJ>
-__device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUtensorMap *mAL,
-                                               const CUtensorMap *mBH, const CUtensorMap *mBL,
-                                               const BatchBufs &B, const WaveBufs &W, const AdjBufs &AB,
+__device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBufs &W, const AdjBufs &AB,
                                                const Geom &G, int t0, int it, int mtiles, int nw, int mode)
 {
     extern __shared__ unsigned char smem_raw[];
-    const int NB = ADJ ? G.CIN : G.NP;                  // MMA N (B operand rows)
+    // MMA N: the operator rows (NB); in the adjoint, m <= 2 tasks add 32 rows of
+    // the transposed molecular factor U^T, whose product lands in TMEM columns
+    // NB .. NB + 23 and is contracted with V^T in the epilogue.
+    const int NB = ADJ ? G.CIN : G.NP;
+    const int NBM = ADJ ? NB + 32 : NB;
     const int NKT = ADJ ? ((G.COUT + TC_KT - 1) / TC_KT) : G.CIN / TC_KT;
-    const uint32_t A_BYTES = TC_M * TC_KT * 4, B_BYTES = (uint32_t)NB * TC_KT * 4;
+    const uint32_t A_BYTES = TC_M * TC_KT * 4, B_BYTES = (uint32_t)NBM * TC_KT * 4;
     const uint32_t STAGE = 2 * A_BYTES + 2 * B_BYTES;
     unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = (uint64_t *)(base + 2 * STAGE);
@@ -200,7 +188,7 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
     }
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
-            mbar_init(&full[i], ADJ ? 1 : TC_PGW);
+            mbar_init(&full[i], TC_PGW);
             mbar_init(&empty[i], 1);
             mbar_init(&tfull[i], 1);
             mbar_init(&tempty[i], 4);
@@ -216,14 +204,47 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
 
-    // stage loads still in flight, for the drain after an abort (producer thread only)
-    int inflight[2] = {0, 0};
-    uint32_t inflight_par[2] = {0, 0};
-
-    if (ADJ && warp == 0 && lane == 0) {
-        // ---------------- TMA producer (adjoint) ----------------
-        uint32_t g = 0;
-        for (int j = 0;; ++j) {
+    if (warp >= TC_PW0) {
+        // ---------------- producer warps ----------------
+        const int pt = tid - TC_PW0 * 32;                 // 0 .. 255
+        const int grp = pt >> 7, gt = pt & 127;           // stage group, thread within the group
+        // Thread gt owns 16-byte chunk ch = gt % 8 of rows r = gt / 8 + 16 i of a
+        // tile; all its rows share r % 8, so their swizzled chunk position
+        // (ch ^ r % 8) is one constant and row i sits 2048 i bytes further.
+        const int r8 = gt >> 3, ch = gt & 7;
+        const uint32_t soff = (uint32_t)r8 * 128u + ((uint32_t)(ch ^ (r8 & 7)) << 4);
+        // A rows: field (forward) or stacked muJ rows (adjoint), stride LDC,
+        // K columns < a_cols real; B rows: operator rows of length b_ld.
+        const int a_cols = ADJ ? G.LDC : G.CIN, b_ld = ADJ ? ((G.COUT + 31) & ~31) : G.CIN;
+        float4 ra[TC_AQ], rb[TC_BQ];
+        // K tile kt of the item into registers: A rows 0 .. nra - 1 of the item
+        // (zero past the task and past a_cols), B rows 0 .. nbi - 1
+        auto load = [&](const float *Ab, int nra, const float *Bb, int nbi, int kt) {
+            const int col = kt * TC_KT + ch * 4;
+            const bool acol = col + 4 <= a_cols;
+            const float4 *pa = reinterpret_cast<const float4 *>(Ab + (size_t)r8 * G.LDC + col);
+            const float4 *pb = reinterpret_cast<const float4 *>(Bb + (size_t)r8 * b_ld + col);
+#pragma unroll
+            for (int i = 0; i < TC_AQ; ++i)
+                ra[i] = acol && r8 + 16 * i < nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < TC_BQ; ++i)
+                if (r8 + 16 * i < nbi) rb[i] = __ldg(pb + (size_t)i * 4 * b_ld);
+        };
+        // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
+        auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
+            float4 h, l;
+            h.x = round_tf32f(v.x); l.x = round_tf32f(v.x - h.x);
+            h.y = round_tf32f(v.y); l.y = round_tf32f(v.y - h.y);
+            h.z = round_tf32f(v.z); l.z = round_tf32f(v.z - h.z);
+            h.w = round_tf32f(v.w); l.w = round_tf32f(v.w - h.w);
+            *reinterpret_cast<float4 *>(hi + off) = h;
+            *reinterpret_cast<float4 *>(lo + off) = l;
+        };
+        // Item j + 1 is published as soon as item j is known, so each group
+        // loads its first tile of the next item while the current item's last
+        // tiles are still in the MMA pipeline.
+        auto fetch_publish = [&](int jj) {                // warp 8 lane 0 only
             int item = -1;
             while (!*abort_flag) {
                 const int cand = atomicAdd(counter, 1);
@@ -242,133 +263,87 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
                 item = cand;
                 break;
             }
-            qitem[j & (TC_Q - 1)] = item;
-            mbar_arrive(&qbar[j & (TC_Q - 1)]);
-            if (item < 0) break;
+            qitem[jj & (TC_Q - 1)] = item;
+            mbar_arrive(&qbar[jj & (TC_Q - 1)]);
+        };
+        // item of queue position jj; one lane waits and the warp stays converged
+        auto item_at = [&](int jj, int &item) -> bool {
+            int ok = lane == 0 ? (int)mbar_wait(&qbar[jj & (TC_Q - 1)], (jj / TC_Q) & 1) : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            __syncwarp();                 // orders lane 0's acquire before the other lanes' reads
+            if (ok) item = qitem[jj & (TC_Q - 1)];
+            return ok != 0;
+        };
+        struct Opnd { const float *Ab, *Bb; int nra, nbi; };
+        auto operands = [&](int item) -> Opnd {
             const int li = item / mtiles, mt = item - li * mtiles;
             const int tl = task_of(li);
             const TaskDev tk = B.tasks[t0 + tl];
-            const int rowA = ADJ ? (int)(tk.fld_off * AB.ncot / G.LDC) + mt * TC_M
-                                 : (int)(tk.fld_off / G.LDC) + mt * TC_M;
-            const int rowB = ADJ ? tl * G.CIN : (int)((mode ? tk.uv_off : tk.op_off) / G.CIN);
-            bool ok = true;
-            for (int kt = 0; kt < NKT; ++kt, ++g) {
-                const int s = g & 1;
-                const uint32_t u = g >> 1;
-                if (u >= 1) {
-                    if (!mbar_wait(&empty[s], (u - 1) & 1)) { *abort_flag = 1; ok = false; break; }
-                    inflight[s] = 0;
-                }
-                unsigned char *sp = base + (size_t)s * STAGE;
-                mbar_expect_tx(&full[s], 2 * A_BYTES + 2 * B_BYTES);
-                tma_load_2d(sp, mAH, &full[s], kt * TC_KT, rowA);
-                tma_load_2d(sp + A_BYTES, mAL, &full[s], kt * TC_KT, rowA);
-                tma_load_2d(sp + 2 * A_BYTES, mBH, &full[s], kt * TC_KT, rowB);
-                tma_load_2d(sp + 2 * A_BYTES + B_BYTES, mBL, &full[s], kt * TC_KT, rowB);
-                inflight[s] = 1;
-                inflight_par[s] = u & 1;
-            }
-            if (!ok) {
-                // wake the consumers of this item's queue slot chain with an end marker
-                qitem[(j + 1) & (TC_Q - 1)] = -1;
-                mbar_arrive(&qbar[(j + 1) & (TC_Q - 1)]);
-                break;
-            }
-        }
-    } else if (!ADJ && warp >= TC_PW0) {
-        // ---------------- producer warps (forward) ----------------
-        const int pt = tid - TC_PW0 * 32;                 // 0 .. 255
-        const int grp = pt >> 7, gt = pt & 127;           // stage group, thread within the group
-        // Thread gt owns 16-byte chunk ch = gt % 8 of rows r = gt / 8 + 16 i of a
-        // tile; all its rows share r % 8, so their swizzled chunk position
-        // (ch ^ r % 8) is one constant and row i sits 2048 i bytes further.
-        const int r8 = gt >> 3, ch = gt & 7;
-        const uint32_t soff = (uint32_t)r8 * 128u + ((uint32_t)(ch ^ (r8 & 7)) << 4);
-        float4 ra[TC_AQ], rb[TC_BQ];
-        // K tile kt of the item into registers: field rows 0 .. nra - 1 of the
-        // item (zero past the task), operator rows 0 .. NB - 1
-        auto load = [&](const float *Ab, int nra, const float *Bb, int kt) {
-            const float4 *pa = reinterpret_cast<const float4 *>(Ab + (size_t)r8 * G.LDC + kt * TC_KT + ch * 4);
-            const float4 *pb = reinterpret_cast<const float4 *>(Bb + (size_t)r8 * G.CIN + kt * TC_KT + ch * 4);
-#pragma unroll
-            for (int i = 0; i < TC_AQ; ++i)
-                ra[i] = r8 + 16 * i < nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < TC_BQ; ++i)
-                if (r8 + 16 * i < NB) rb[i] = __ldg(pb + (size_t)i * 4 * G.CIN);
+            const int r0 = mt * TC_M;
+            Opnd o;
+            o.nra = min(TC_M, (ADJ ? AB.ncot * tk.K : tk.K) - r0);
+            o.nbi = ADJ && tk.has_mol ? NBM : NB;
+            o.Ab = ADJ ? AB.AJ + (size_t)tk.fld_off * AB.ncot + (size_t)r0 * G.LDC : W.F + tk.fld_off + (size_t)r0 * G.LDC;
+            o.Bb = ADJ ? AB.opsT + (size_t)tl * (NB + 32) * b_ld : W.ops + (mode ? tk.uv_off : tk.op_off);
+            return o;
         };
-        // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
-        auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
-            float4 h, l;
-            h.x = round_tf32f(v.x); l.x = round_tf32f(v.x - h.x);
-            h.y = round_tf32f(v.y); l.y = round_tf32f(v.y - h.y);
-            h.z = round_tf32f(v.z); l.z = round_tf32f(v.z - h.z);
-            h.w = round_tf32f(v.w); l.w = round_tf32f(v.w - h.w);
-            *reinterpret_cast<float4 *>(hi + off) = h;
-            *reinterpret_cast<float4 *>(lo + off) = l;
-        };
+        if (pt == 0) fetch_publish(0);
         uint32_t g = 0;
+        bool have = false;           // the registers already hold this group's first tile of the item
         for (int j = 0;; ++j) {
-            const int slot = j & (TC_Q - 1);
-            if (pt == 0) {
-                int item = -1;
-                while (!*abort_flag) {
-                    const int cand = atomicAdd(counter, 1);
-                    if (cand >= n_items) break;
-                    const int li = cand / mtiles, mt = cand - li * mtiles;
-                    const TaskDev tk = B.tasks[t0 + task_of(li)];
-                    if (mt * TC_M > B.px[tk.pix].nt) continue;
-                    item = cand;
-                    break;
-                }
-                qitem[slot] = item;
-                mbar_arrive(&qbar[slot]);
-            }
-            // one lane per warp waits; the warp leaves every loop together
-            int ok = lane == 0 ? (int)mbar_wait(&qbar[slot], (j / TC_Q) & 1) : 0;
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            __syncwarp();                 // orders lane 0's acquire before the other lanes' reads
-            if (!ok) { *abort_flag = 1; break; }
-            const int item = qitem[slot];
+            int item = -1;
+            if (!item_at(j, item)) { *abort_flag = 1; break; }
             if (item < 0) break;
-            const int li = item / mtiles, mt = item - li * mtiles;
-            const TaskDev tk = B.tasks[t0 + task_of(li)];
-            const int r0 = mt * TC_M, nra = min(TC_M, tk.K - r0);
-            const float *Ab = W.F + tk.fld_off + (size_t)r0 * G.LDC;
-            const float *Bb = W.ops + (mode ? tk.uv_off : tk.op_off);
+            if (pt == 0) fetch_publish(j + 1);
+            const Opnd op = operands(item);
             // this group's K tiles of the item: global tile index g + kt with (g + kt) & 1 == grp
             const int kt0 = (int)((grp - (int)(g & 1)) & 1);
-            if (kt0 < NKT && !*abort_flag) load(Ab, nra, Bb, kt0);
+            if (!have && kt0 < NKT) load(op.Ab, op.nra, op.Bb, op.nbi, kt0);
+            have = false;
+            bool stop = false;
             for (int kt = kt0; kt < NKT; kt += 2) {
                 const uint32_t gg = g + (uint32_t)kt, u = gg >> 1;
                 const int s = (int)(gg & 1);
                 int free_ok = (u == 0 || lane != 0) ? 1 : (int)mbar_wait(&empty[s], (u - 1) & 1);
                 free_ok = __shfl_sync(0xffffffffu, free_ok, 0);
                 __syncwarp();
-                if (!free_ok) { *abort_flag = 1; break; }
+                if (!free_ok) { *abort_flag = 1; stop = true; break; }
                 unsigned char *sp = base + (size_t)s * STAGE;
 #pragma unroll
                 for (int i = 0; i < TC_AQ; ++i) put(sp, sp + A_BYTES, soff + 2048u * i, ra[i]);
 #pragma unroll
                 for (int i = 0; i < TC_BQ; ++i)
-                    if (r8 + 16 * i < NB) put(sp + 2 * A_BYTES, sp + 2 * A_BYTES + B_BYTES, soff + 2048u * i, rb[i]);
+                    if (r8 + 16 * i < op.nbi) put(sp + 2 * A_BYTES, sp + 2 * A_BYTES + B_BYTES, soff + 2048u * i, rb[i]);
                 // generic-proxy stores made visible to the tensor cores before the stage is marked full
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[s]);
-                if (kt + 2 < NKT) load(Ab, nra, Bb, kt + 2);
+                if (kt + 2 < NKT) {
+                    load(op.Ab, op.nra, op.Bb, op.nbi, kt + 2);
+                } else {
+                    int nxt = -1;
+                    if (!item_at(j + 1, nxt)) { *abort_flag = 1; stop = true; break; }
+                    const int kt0n = (int)((grp - (int)((g + (uint32_t)NKT) & 1)) & 1);
+                    if (nxt >= 0 && kt0n < NKT) {
+                        const Opnd on = operands(nxt);
+                        load(on.Ab, on.nra, on.Bb, on.nbi, kt0n);
+                        have = true;
+                    }
+                }
             }
+            if (stop) break;
             g += (uint32_t)NKT;
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
-        const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(NB >> 3) << 17);
         uint32_t g = 0;
         for (int j = 0;; ++j) {
             if (!mbar_wait(&qbar[j & (TC_Q - 1)], (j / TC_Q) & 1)) { *abort_flag = 1; break; }
             const int item = qitem[j & (TC_Q - 1)];
             if (item < 0 || *abort_flag) break;
+            const int nbi = ADJ && B.tasks[t0 + task_of(item / mtiles)].has_mol ? NBM : NB;
+            const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(nbi >> 3) << 17);
             const int b = j & 1;
             const uint32_t ub = j >> 1;
             if (ub >= 1 && !mbar_wait(&tempty[b], (ub - 1) & 1)) { *abort_flag = 1; break; }
@@ -429,6 +404,20 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
             }
             const float x = live ? B.lvf[3 * (d.lev_off + k) + (mode ? 1 : 0)] : 0.f;
             const uint32_t tb = tmem + (uint32_t)(b * TC_ACC_COLS) + ((uint32_t)(q4 * 32) << 16);
+            // adjoint, m <= 2: the rank-24 product U^T muJ of this row sits in
+            // columns NB .. NB + 23
+            const bool mol = ADJ && tk.has_mol;
+            float t24[24];
+            float y = 0.f;
+            const float *Vm = B.molV + (size_t)(mol ? tk.m : 0) * 32 * G.CIN;
+            if (mol) {
+                float th[16];
+                tmem_ld16(tb + (uint32_t)NB, t24);
+                tmem_ld16(tb + (uint32_t)(NB + 16), th);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) t24[16 + q] = th[q];
+                y = live ? B.lvf[3 * (d.lev_off + k) + 1] : 0.f;
+            }
             // Each 32-row x 16-column chunk goes through a shared-memory
             // transpose so the stores are row-contiguous: lane l then writes
             // 16 bytes (columns 4 (l % 4) .. +3) of rows l / 4 + 8 i, i < 4.
@@ -438,9 +427,26 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
                 float v[16];
                 tmem_ld16(tb + (uint32_t)(cb * 16), v);
 #pragma unroll
+                for (int jj = 0; jj < 16; ++jj) v[jj] *= x;
+                if (mol) {
+                    // the chunk lies in input block b = 16 cb / N (N % 16 == 0);
+                    // V^T: input column c = bN + i takes sum_f V[4b + f][c] t[4b + f]
+                    float w4[4] = {0.f, 0.f, 0.f, 0.f};
+                    const int b4 = 4 * ((cb * 16) / G.N);
+#pragma unroll
+                    for (int q = 0; q < 24; ++q)
+                        if ((q & ~3) == b4) w4[q & 3] = t24[q];
+                    for (int jj = 0; jj < 16; ++jj) {
+                        const int c = cb * 16 + jj;
+                        float acc = 0.f;
+#pragma unroll
+                        for (int f = 0; f < 4; ++f) acc = fmaf(__ldg(Vm + (size_t)(b4 + f) * G.CIN + c), w4[f], acc);
+                        v[jj] = fmaf(y, acc, v[jj]);
+                    }
+                }
+#pragma unroll
                 for (int jj = 0; jj < 16; jj += 4)
-                    *reinterpret_cast<float4 *>(tp + lane * TC_TP + jj) =
-                        make_float4(x * v[jj], x * v[jj + 1], x * v[jj + 2], x * v[jj + 3]);
+                    *reinterpret_cast<float4 *>(tp + lane * TC_TP + jj) = make_float4(v[jj], v[jj + 1], v[jj + 2], v[jj + 3]);
                 __syncwarp();
                 const int c = cb * 16 + (lane & 3) * 4;
                 if (c + 4 <= G.LDC && c < ncols) {
@@ -468,12 +474,7 @@ __device__ __forceinline__ void source_tc_body(const CUtensorMap *mAH, const CUt
         }
     }
     __syncthreads();
-    if (tid == 0 && *abort_flag) {
-        atomicExch(B.err, OCRT_ERR_DEVICE);
-        // drain this CTA's own copies still in flight (bounded)
-        for (int s = 0; s < 2; ++s)
-            if (inflight[s]) mbar_wait(&full[s], inflight_par[s]);
-    }
+    if (tid == 0 && *abort_flag) atomicExch(B.err, OCRT_ERR_DEVICE);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 2) {
@@ -486,22 +487,20 @@ __global__ void __launch_bounds__(TC_FWD_THREADS, 1)
 k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode)
 {
     AdjBufs none{};
-    source_tc_body<false>(nullptr, nullptr, nullptr, nullptr, B, W, none, G, t0, it, mtiles, 0, mode);
+    source_tc_body<false>(B, W, none, G, t0, it, mtiles, 0, mode);
 }
 
 // Transposed contraction of the adjoint for adjoint order `it` (work counter
 // AB.awork[it]).
-__global__ void __launch_bounds__(TC_THREADS, 1)
-k_adj_source_tc(const __grid_constant__ CUtensorMap mJH, const __grid_constant__ CUtensorMap mJL,
-                const __grid_constant__ CUtensorMap mTH, const __grid_constant__ CUtensorMap mTL,
-                BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw)
+__global__ void __launch_bounds__(TC_FWD_THREADS, 1)
+k_adj_source_tc(BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw)
 {
-    source_tc_body<true>(&mJH, &mJL, &mTH, &mTL, B, W, AB, G, t0, it, mtiles, nw, 0);
+    source_tc_body<true>(B, W, AB, G, t0, it, mtiles, nw, 0);
 }
 
-static size_t tc_smem_for(int NB)
+static size_t tc_smem_for(int NBM)
 {
-    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)NB * TC_KT * 4) + 256 + 4 * 32 * TC_TP * 4;
+    return 1024 + 2 * (2 * (size_t)TC_M * TC_KT * 4 + 2 * (size_t)NBM * TC_KT * 4) + 256 + 4 * 32 * TC_TP * 4;
 }
 
 int tc_fwd_threads() { return TC_FWD_THREADS; }
@@ -513,12 +512,13 @@ size_t tc_smem_bytes(const Geom &G)
 
 size_t tc_adj_smem_bytes(const Geom &G)
 {
-    return tc_smem_for(G.CIN);
+    return tc_smem_for(G.CIN + 32);
 }
 
 bool tc_adj_supported(const Geom &G)
 {
-    return (G.CIN % 16) == 0 && G.CIN <= TC_ACC_COLS && tc_adj_smem_bytes(G) <= 227 * 1024;
+    return (G.CIN % 16) == 0 && G.CIN + 32 <= TC_ACC_COLS && G.CIN + 32 <= 16 * TC_BQ && G.N % 16 == 0 &&
+           tc_adj_smem_bytes(G) <= 227 * 1024;
 }
 
 bool tc_supported(const Geom &G)
