@@ -105,42 +105,47 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     int bad = 0;
     const float faP = (float)aP, fmP = (float)mP;
     const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
-    auto Jat = [&](int k) -> float {
-        const float *lv = B.lvf + 3 * (d.lev_off + k);
-        const float x = lv[0], y = lv[1];
-        float v = lv[2] * (x * faP + y * fmP);
-        if (d.flat && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
-            const double beam = sb * exp(hh[k] / d.mu0);
-            v += (float)(beam * (RI * (x * fa1 + y * fm1) + RQ * (x * fa2 + y * fm2)));
+    // rough direct-beam seed (rt_surface_boundary.c:430-493) on upward columns:
+    // fs_tdn exp(-(tau-h_k)/mu_g) R_m(mu_g, mu0)[s, I], the attenuation per level from Eatt
+    const bool seeded = d.rough && h == 0;
+    const float rs = seeded ? W.srf[tk.srf_off + (size_t)G.NR * G.N * 9 + g * 9 + s * 3] : 0.f;
+    // Step j visits level nt - j (upward) or j (downward); the per-level inputs
+    // of PF steps are loaded before the dependent recurrence runs.
+    constexpr int PF = 8;
+    float I = 0.f, Jp = 0.f;
+    for (int j0 = 0; j0 <= nt; j0 += PF) {
+        const int cnt = nt - j0 + 1 < PF ? nt - j0 + 1 : PF;
+        float lx[PF], ly[PF], lc[PF], tv[PF], av[PF], bv[PF], ea[PF];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            if (q < cnt) {
+                const int j = j0 + q, k = h == 0 ? nt - j : j;
+                const float *lv = B.lvf + 3 * (d.lev_off + k);
+                lx[q] = lv[0]; ly[q] = lv[1]; lc[q] = lv[2];
+                if (j > 0) {
+                    const int e = (h == 0 ? k : k - 1) * NR + g;
+                    tv[q] = Tc[e]; av[q] = Ca[e]; bv[q] = Cb[e];
+                }
+                ea[q] = seeded ? B.Eatt[(d.lev_off + k) * NR + g] : 0.f;
+            }
         }
-        if (!isfinite(v)) bad = 1;
-        return v;
-    };
-    auto store = [&](int k, float I) {
-        float2 t = make_float2(I, 0.f);
-        if (d.rough && h == 0) t = df_add(t, rough_seed(tk, W, B, d, G, fs_tdn, k, g, s));
-        F[(size_t)k * G.LDC + c] = t.x;
-        Tot[(size_t)k * G.LDC + c] = t;
-    };
-    if (h == 0) {
-        float Jn = Jat(nt), I = 0.f;
-        store(nt, I);
-        for (int k = nt - 1; k >= 0; --k) {
-            const float Jk = Jat(k);
-            const int e = k * NR + g;
-            I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jn;
-            store(k, I);
-            Jn = Jk;
-        }
-    } else {
-        float Jp = Jat(0), I = 0.f;
-        store(0, I);
-        for (int k = 1; k <= nt; ++k) {
-            const float Jk = Jat(k);
-            const int e = (k - 1) * NR + g;
-            I = Tc[e] * I + Ca[e] * Jk + Cb[e] * Jp;
-            store(k, I);
-            Jp = Jk;
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            if (q < cnt) {
+                const int j = j0 + q, k = h == 0 ? nt - j : j;
+                float Jk = lc[q] * (lx[q] * faP + ly[q] * fmP);
+                if (d.flat && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
+                    const double beam = sb * exp(hh[k] / d.mu0);
+                    Jk += (float)(beam * (RI * (lx[q] * fa1 + ly[q] * fm1) + RQ * (lx[q] * fa2 + ly[q] * fm2)));
+                }
+                if (!isfinite(Jk)) bad = 1;
+                if (j > 0) I = tv[q] * I + av[q] * Jk + bv[q] * Jp;
+                Jp = Jk;
+                float2 t = make_float2(I, 0.f);
+                if (seeded) t = df_add(t, fs_tdn * ea[q] * rs);
+                F[(size_t)k * G.LDC + c] = t.x;
+                Tot[(size_t)k * G.LDC + c] = t;
+            }
         }
     }
     if (bad) atomicExch(B.err, -2);
