@@ -231,23 +231,39 @@ __global__ void k_adj_init(BatchBufs B, AdjBufs A, Geom G, int t0, int nadj)
 // Down column (forward I[0] = 0, I[k] = T_{k-1} I[k-1] + Ca_{k-1} J[k] + Cb_{k-1} J[k-1]):
 //   nu[nt] = a[nt], nu[k] = a[k] + T_k nu[k+1];
 //   muJ[k] = Ca_{k-1} nu[k] (k > 0) + Cb_k nu[k+1] (k < nt).
-__global__ void __launch_bounds__(512, 2) k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j)
+__global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j)
 {
+    // One block per (task, group of up to ADJ_RB cotangent rows): the rows
+    // share the transport coefficients and each thread runs its column's
+    // recurrence for every active row of the group.
     __shared__ double red[32];
-    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
-    const TaskState st = A.st[ta];
-    if (!st.active) return;
+    const int nrg = (A.ncot + ADJ_RB - 1) / ADJ_RB;
+    const int tl = blockIdx.x / nrg, r0 = (blockIdx.x - tl * nrg) * ADJ_RB, tg = t0 + tl;
+    const int nr = min(ADJ_RB, A.ncot - r0);
+    bool act[ADJ_RB];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) {
+        act[q] = q < nr && A.st[tl * A.ncot + r0 + q].active;
+        any |= act[q];
+    }
+    if (!any) return;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
     const int c = threadIdx.x, nt = d.nt, NR = G.NR;
     int s = 0, h = 0, g = 0;
     if (c < G.COUT) decode_col_a(G, c, s, h, g);
     const bool valid = c < G.COUT && g < d.n_ring;
-    const size_t off = adj_off(tk, G, A.ncot, r);
-    float *a = A.AF + off;
-    float2 *At = A.ATot + off;
-    float *mj = A.AJ + off;
-    float mi = 0.f, mt = 0.f;
+    float *a[ADJ_RB], *mj[ADJ_RB];
+    float2 *At[ADJ_RB];
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) {
+        const size_t off = adj_off(tk, G, A.ncot, r0 + (q < nr ? q : 0));
+        a[q] = A.AF + off; At[q] = A.ATot + off; mj[q] = A.AJ + off;
+    }
+    float mi[ADJ_RB], mt[ADJ_RB], nup[ADJ_RB];
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) { mi[q] = 0.f; mt[q] = 0.f; nup[q] = 0.f; }
     if (valid) {
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
         // The view columns are outputs only (zero quadrature weight): the
@@ -255,23 +271,27 @@ __global__ void __launch_bounds__(512, 2) k_adj_scan(BatchBufs B, AdjBufs A, Geo
         const bool clear = c >= G.CIN;
         // Each column walks its levels in its (transposed) transport direction,
         // step j at level j (upward columns) or nt - j (downward columns), with
-        // the adjoint order, its total and the coefficients of the next
+        // the adjoint orders, their totals and the coefficients of the next
         // SCAN_DEPTH steps in flight as cp.async copies into this thread's own
         // shared-memory slots (refilled only after the values read are used).
         extern __shared__ float scan_smem[];
         const int bs = blockDim.x;
-        float *As = scan_smem;                                             // [SCAN_DEPTH][bs]
-        float2 *Ts = reinterpret_cast<float2 *>(As + SCAN_DEPTH * bs);      // [SCAN_DEPTH][bs]
-        float *Cs = reinterpret_cast<float *>(Ts + SCAN_DEPTH * bs);        // [SCAN_DEPTH][3][bs]
+        float *As = scan_smem;                                                   // [SCAN_DEPTH][RB][bs]
+        float2 *Ts = reinterpret_cast<float2 *>(As + SCAN_DEPTH * ADJ_RB * bs);   // [SCAN_DEPTH][RB][bs]
+        float *Cs = reinterpret_cast<float *>(Ts + SCAN_DEPTH * ADJ_RB * bs);     // [SCAN_DEPTH][3][bs]
         // coefficient rows of step j: upward tv, cb at k - 1 and ca at k;
         // downward tv, cb at k and ca at k - 1 (absent rows read as zero)
-        auto issue = [&](int j) {
-            if (j <= nt) {
-                const int k = h == 0 ? j : nt - j, sl = j & (SCAN_DEPTH - 1);
+        auto issue = [&](int jj) {
+            if (jj <= nt) {
+                const int k = h == 0 ? jj : nt - jj, sl = jj & (SCAN_DEPTH - 1);
                 const size_t o = (size_t)k * G.LDC + c;
                 if (h == 0 || k > 0) {            // the TOA downward radiance is fixed at zero
-                    cp_async4(As + sl * bs + c, a + o);
-                    cp_async8(Ts + sl * bs + c, At + o);
+#pragma unroll
+                    for (int q = 0; q < ADJ_RB; ++q)
+                        if (act[q]) {
+                            cp_async4(As + (sl * ADJ_RB + q) * bs + c, a[q] + o);
+                            cp_async8(Ts + (sl * ADJ_RB + q) * bs + c, At[q] + o);
+                        }
                 }
                 const int kt = h == 0 ? k - 1 : k, ka = h == 0 ? k : k - 1;
                 if (kt >= 0 && kt < nt) {
@@ -283,44 +303,56 @@ __global__ void __launch_bounds__(512, 2) k_adj_scan(BatchBufs B, AdjBufs A, Geo
             cp_async_commit();
         };
 #pragma unroll
-        for (int j = 0; j < SCAN_DEPTH; ++j) issue(j);
-        float nup = 0.f;
-        for (int j = 0; j <= nt; ++j) {
+        for (int jj = 0; jj < SCAN_DEPTH; ++jj) issue(jj);
+        for (int jj = 0; jj <= nt; ++jj) {
             cp_async_wait<SCAN_DEPTH - 1>();
-            const int k = h == 0 ? j : nt - j, sl = j & (SCAN_DEPTH - 1);
+            const int k = h == 0 ? jj : nt - jj, sl = jj & (SCAN_DEPTH - 1);
             const int kt = h == 0 ? k - 1 : k, ka = h == 0 ? k : k - 1;
             const bool has_a = h == 0 || k > 0;
-            const float av = has_a ? As[sl * bs + c] : 0.f;
             const float tv = kt >= 0 && kt < nt ? Cs[(sl * 3 + 0) * bs + c] : 0.f;
             const float cb = kt >= 0 && kt < nt ? Cs[(sl * 3 + 2) * bs + c] : 0.f;
             const float ca = ka >= 0 && ka < nt ? Cs[(sl * 3 + 1) * bs + c] : 0.f;
             const size_t o = (size_t)k * G.LDC + c;
-            if (has_a) {
-                const float2 t = df_add(Ts[sl * bs + c], av);
-                At[o] = t;
-                if (clear) a[o] = 0.f;
-                mi = fmaxf(mi, fabsf(av));
-                mt = fmaxf(mt, fabsf(t.x));
+#pragma unroll
+            for (int q = 0; q < ADJ_RB; ++q) {
+                if (!act[q]) continue;
+                const float av = has_a ? As[(sl * ADJ_RB + q) * bs + c] : 0.f;
+                if (has_a) {
+                    const float2 t = df_add(Ts[(sl * ADJ_RB + q) * bs + c], av);
+                    At[q][o] = t;
+                    if (clear) a[q][o] = 0.f;
+                    mi[q] = fmaxf(mi[q], fabsf(av));
+                    mt[q] = fmaxf(mt[q], fabsf(t.x));
+                }
+                const float nu = av + tv * nup[q];
+                mj[q][o] = ca * nu + cb * nup[q];
+                nup[q] = nu;
             }
-            const float nu = av + tv * nup;
-            mj[o] = ca * nu + cb * nup;
-            nup = nu;
-            issue(j + SCAN_DEPTH);
+            issue(jj + SCAN_DEPTH);
         }
         cp_async_wait<0>();
-        if (h == 0 && d.surf_on) A.bc[(size_t)ta * NR * 3 + g * 3 + s] = nup;
+        if (h == 0 && d.surf_on)
+#pragma unroll
+            for (int q = 0; q < ADJ_RB; ++q)
+                if (act[q]) A.bc[(size_t)(tl * A.ncot + r0 + q) * NR * 3 + g * 3 + s] = nup[q];
     }
-    mi = (float)block_max_a(mi, red);
-    __syncthreads();
-    mt = (float)block_max_a(mt, red);
-    if (threadIdx.x == 0) {
-        TaskState ns = st;
-        ns.orders = j;
-        ns.resid = mt > 0.f ? (double)(mi / mt) : 0.0;
-        if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
-        else if (j >= d.max_orders) ns.active = 0;
-        A.st[ta] = ns;
-        if (ns.active) atomicAdd(&A.acnt[j], 1);
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) {
+        if (!act[q]) continue;                    // block-uniform
+        const float bmi = (float)block_max_a(mi[q], red);
+        __syncthreads();
+        const float bmt = (float)block_max_a(mt[q], red);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int ta = tl * A.ncot + r0 + q;
+            TaskState ns = A.st[ta];
+            ns.orders = j;
+            ns.resid = bmt > 0.f ? (double)(bmi / bmt) : 0.0;
+            if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
+            else if (j >= d.max_orders) ns.active = 0;
+            A.st[ta] = ns;
+            if (ns.active) atomicAdd(&A.acnt[j], 1);
+        }
     }
 }
 
@@ -490,20 +522,26 @@ __global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0
 // so every warp runs one direction.  Per-warp level sums sit in shared memory
 // [warp][3][nt + 1] and are added in warp order, so the result does not
 // depend on scheduling.
-__global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
+__global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb)
 {
-    extern __shared__ float wsum[];
+    // One block per (task, group of rb <= ADJ_RB cotangent rows): the forward
+    // totals, sources and coefficients a level's terms need are loaded once
+    // for all rows of the group.
+    extern __shared__ float wsum[];               // [warp][row][3][nt + 1]
     __shared__ double red[32];
-    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
+    const int nrg = (A.ncot + rb - 1) / rb;
+    const int tl = blockIdx.x / nrg, r0 = (blockIdx.x - tl * nrg) * rb, tg = t0 + tl;
+    const int nr = min(rb, A.ncot - r0);
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
     const int nt = d.nt, NR = G.NR, N = G.N, L1 = nt + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    float *ws = wsum + (size_t)warp * 3 * L1;
-    for (int x = lane; x < 3 * L1; x += 32) ws[x] = 0.f;
+    float *ws = wsum + (size_t)warp * rb * 3 * L1;
+    for (int x = lane; x < rb * 3 * L1; x += 32) ws[x] = 0.f;
     __syncwarp();
-    const size_t off = adj_off(tk, G, A.ncot, r);
-    const float2 *At = A.ATot + off;
+    const float2 *At[ADJ_RB];
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) At[q] = A.ATot + adj_off(tk, G, A.ncot, r0 + (q < nr ? q : 0));
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const float *dT = A.dTc + d.coef_off, *dA = A.dCa + d.coef_off, *dB = A.dCb + d.coef_off;
     const float *lv = B.lvf + 3 * (size_t)d.lev_off;                 // x, y, ch per level
@@ -520,119 +558,131 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
     const int c = g < N ? col_of(G, s, h, g) : 6 * N + 2 * s + h;
     const bool valid = g < d.n_ring;
     const float fa = valid ? pv[c] : 0.f, fm = valid ? pv[G.LDC + c] : 0.f;
-    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    const unsigned dmask = __ballot_sync(0xffffffffu, valid && h == 1);
-    double gW = 0.0, gS = 0.0;
-    float nu_boa = 0.f;
-    constexpr int PF = 6;
-    for (int dir = 0; dir < 2; ++dir) {
-        if ((dir == 0 ? (vmask & ~dmask) : dmask) == 0) continue;        // warp-uniform
-        const bool on = valid && h == dir;
-        float nu_prev = 0.f, jt_prev = 0.f;
-        // step j visits level k = j (upward columns: nu from the TOA down) or
-        // k = nt - j (downward columns: nu from the BOA up, nu_0 = 0)
-        for (int j1 = 0; j1 <= nt; j1 += PF) {
-            const int cnt = nt - j1 + 1 < PF ? nt - j1 + 1 : PF;
-            float av[PF], tv[PF], ca[PF], cb[PF], jx[PF], tt[PF], xk[PF], yk[PF], chk[PF], lt[PF], la[PF], lb[PF];
+    const bool wact = __any_sync(0xffffffffu, valid);                // warp-uniform
+    float nu_prev[ADJ_RB];
 #pragma unroll
-            for (int q = 0; q < PF; ++q) {
-                av[q] = tv[q] = ca[q] = cb[q] = jx[q] = tt[q] = xk[q] = yk[q] = chk[q] = lt[q] = la[q] = lb[q] = 0.f;
-                if (on && q < cnt) {
-                    const int k = dir == 0 ? j1 + q : nt - j1 - q;
-                    const size_t o = (size_t)k * G.LDC + c;
-                    const float2 t = At[o];
-                    av[q] = t.x + t.y;
-                    jx[q] = Jx[o];
-                    tt[q] = Tot[o].x;
-                    xk[q] = lv[3 * k]; yk[q] = lv[3 * k + 1]; chk[q] = lv[3 * k + 2];
-                    if (dir == 0) {
-                        tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
-                        ca[q] = k < nt ? Ca[k * NR + g] : 0.f;
-                        cb[q] = k > 0 ? Cb[(k - 1) * NR + g] : 0.f;
-                        if (k > 0) {
-                            const int e = (k - 1) * NR + g;
-                            lt[q] = dT[e]; la[q] = dA[e]; lb[q] = dB[e];
-                        }
-                    } else {
-                        tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
-                        ca[q] = k > 0 ? Ca[(k - 1) * NR + g] : 0.f;
-                        cb[q] = k < nt ? Cb[k * NR + g] : 0.f;
-                        if (k < nt) {
-                            const int e = k * NR + g;
-                            lt[q] = dT[e]; la[q] = dA[e]; lb[q] = dB[e];
-                        }
+    for (int q = 0; q < ADJ_RB; ++q) nu_prev[q] = 0.f;
+    float jt_prev = 0.f;
+    constexpr int PF = 4;
+    // step j visits level k = j (upward columns: nu from the TOA down) or
+    // k = nt - j (downward columns: nu from the BOA up, nu_0 = 0)
+    for (int j1 = 0; wact && j1 <= nt; j1 += PF) {
+        const int cnt = nt - j1 + 1 < PF ? nt - j1 + 1 : PF;
+        float av[ADJ_RB][PF], tv[PF], ca[PF], cb[PF], jx[PF], tt[PF], xk[PF], yk[PF], chk[PF], lt[PF], la[PF], lb[PF];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            tv[q] = ca[q] = cb[q] = jx[q] = tt[q] = xk[q] = yk[q] = chk[q] = lt[q] = la[q] = lb[q] = 0.f;
+#pragma unroll
+            for (int r = 0; r < ADJ_RB; ++r) av[r][q] = 0.f;
+            if (valid && q < cnt) {
+                const int k = h == 0 ? j1 + q : nt - j1 - q;
+                const size_t o = (size_t)k * G.LDC + c;
+#pragma unroll
+                for (int r = 0; r < ADJ_RB; ++r)
+                    if (r < nr) { const float2 t = At[r][o]; av[r][q] = t.x + t.y; }
+                jx[q] = Jx[o];
+                tt[q] = Tot[o].x;
+                xk[q] = lv[3 * k]; yk[q] = lv[3 * k + 1]; chk[q] = lv[3 * k + 2];
+                if (h == 0) {
+                    tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;
+                    ca[q] = k < nt ? Ca[k * NR + g] : 0.f;
+                    cb[q] = k > 0 ? Cb[(k - 1) * NR + g] : 0.f;
+                    if (k > 0) {
+                        const int e = (k - 1) * NR + g;
+                        lt[q] = dT[e]; la[q] = dA[e]; lb[q] = dB[e];
+                    }
+                } else {
+                    tv[q] = k < nt ? Tc[k * NR + g] : 0.f;
+                    ca[q] = k > 0 ? Ca[(k - 1) * NR + g] : 0.f;
+                    cb[q] = k < nt ? Cb[k * NR + g] : 0.f;
+                    if (k < nt) {
+                        const int e = k * NR + g;
+                        lt[q] = dT[e]; la[q] = dA[e]; lb[q] = dB[e];
                     }
                 }
             }
+        }
 #pragma unroll
-            for (int q = 0; q < PF; ++q) {
-                if (q >= cnt) break;                                        // warp-uniform
-                const int k = dir == 0 ? j1 + q : nt - j1 - q;
+        for (int q = 0; q < PF; ++q) {
+            if (q >= cnt) break;                                            // warp-uniform
+            const int k = h == 0 ? j1 + q : nt - j1 - q;
+            // row-independent parts: J_tot at this level and the layer bracket
+            // h 0 (layer k-1): F_k dT + J_{k-1} dCa + J_k dCb
+            // h 1 (layer k):   F_k dT + J_{k+1} dCa + J_k dCb
+            const float j1v = chk[q] * (xk[q] * fa + yk[q] * fm);
+            const float jt = jx[q] + j1v;
+            const float lay = tt[q] * lt[q] + jt_prev * la[q] + jt * lb[q];
+            jt_prev = valid ? jt : 0.f;
+            const int kl = h == 0 ? k - 1 : k;
+#pragma unroll
+            for (int r = 0; r < ADJ_RB; ++r) {
+                if (r >= nr) break;                                         // block-uniform
                 float vs = 0.f, vj = 0.f, vl = 0.f;
-                if (on) {
-                    const float nu = (dir == 1 && k == 0) ? 0.f : av[q] + tv[q] * nu_prev;
-                    // dir 0: mu = Ca_k nu_k + Cb_{k-1} nu_{k-1};  dir 1: mu = Ca_{k-1} nu_k + Cb_k nu_{k+1}
-                    const float mu = ca[q] * nu + cb[q] * nu_prev;
-                    const float j1v = chk[q] * (xk[q] * fa + yk[q] * fm);
-                    const float jt = jx[q] + j1v;
+                if (valid) {
+                    const float nu = (h == 1 && k == 0) ? 0.f : av[r][q] + tv[q] * nu_prev[r];
+                    // h 0: mu = Ca_k nu_k + Cb_{k-1} nu_{k-1};  h 1: mu = Ca_{k-1} nu_k + Cb_k nu_{k+1}
+                    const float mu = ca[q] * nu + cb[q] * nu_prev[r];
                     vs = mu * jt;
                     vj = mu * j1v;
-                    // layer term of the layer between this level and the previous step's:
-                    // dir 0 (layer k-1): nu_{k-1} (F_k dT + J_{k-1} dCa + J_k dCb)
-                    // dir 1 (layer k):   nu_{k+1} (F_k dT + J_{k+1} dCa + J_k dCb)
-                    vl = nu_prev * (tt[q] * lt[q] + jt_prev * la[q] + jt * lb[q]);
-                    nu_prev = nu;
-                    jt_prev = jt;
+                    vl = nu_prev[r] * lay;
+                    nu_prev[r] = nu;
                 }
                 vs = warp_sum(vs);
                 vj = warp_sum(vj);
                 vl = warp_sum(vl);
                 if (lane == 0) {
-                    ws[k] += vs;
-                    ws[L1 + k] += vj;
-                    const int kl = dir == 0 ? k - 1 : k;
-                    if (kl >= 0 && kl < nt) ws[2 * L1 + kl] += vl;
+                    float *wr = ws + (size_t)r * 3 * L1;
+                    wr[k] += vs;
+                    wr[L1 + k] += vj;
+                    if (kl >= 0 && kl < nt) wr[2 * L1 + kl] += vl;
                 }
             }
         }
-        if (dir == 0) nu_boa = nu_prev;
     }
+    // surface terms: wind derivative of the boundary operator and of the
+    // direct-beam seed, and the seed's optical-depth dependence
+    double gW[ADJ_RB], gS[ADJ_RB];
+#pragma unroll
+    for (int r = 0; r < ADJ_RB; ++r) { gW[r] = 0.0; gS[r] = 0.0; }
     if (valid && h == 0 && d.rough) {
-        // surface terms: wind derivative of the boundary operator and of
-        // the direct-beam seed, and the seed's optical-depth dependence
         const float *Xb = W.F + tk.fld_off + (size_t)nt * G.LDC;
-        auto Xs = [&](int col) -> double { return (double)Xb[col]; };
         const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
         const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
         double acc = 0.0;
         for (int i = 0; i < N; ++i) {
             const double pw = pwm[i];
             const float *Ri = RW + (size_t)i * 9;
-            acc += pw * ((double)Ri[0] * Xs(col_of(G, 0, 1, i)) + (double)Ri[1] * Xs(col_of(G, 1, 1, i)) +
-                         (double)Ri[2] * Xs(col_of(G, 2, 1, i)));
+            acc += pw * ((double)Ri[0] * Xb[col_of(G, 0, 1, i)] + (double)Ri[1] * Xb[col_of(G, 1, 1, i)] +
+                         (double)Ri[2] * Xb[col_of(G, 2, 1, i)]);
         }
         const double tdn = exp(-d.tau_total / d.mu0);
         const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
         const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
         const float *Rs = W.srf + tk.srf_off + (size_t)G.NR * N * 9;
         const double E = (double)B.Eatt[(d.lev_off + nt) * NR + g];
-        gW = nu_boa * (acc + fs * tdn * E * (double)RsW[g * 9 + s * 3]);
-        gS = nu_boa * fs * tdn * E * (double)Rs[g * 9 + s * 3];
+        const double sw = acc + fs * tdn * E * (double)RsW[g * 9 + s * 3];
+        const double ss = fs * tdn * E * (double)Rs[g * 9 + s * 3];
+#pragma unroll
+        for (int r = 0; r < ADJ_RB; ++r) { gW[r] = nu_prev[r] * sw; gS[r] = nu_prev[r] * ss; }
     }
-    gW = block_sum_a(gW, red);
-    __syncthreads();
-    gS = block_sum_a(gS, red);
-    __syncthreads();
-    double *go = A.gout + (size_t)ta * A.gstride;
-    for (int x = threadIdx.x; x < 3 * L1; x += blockDim.x) {
-        const int q = x / L1, k = x - q * L1;
-        float v = 0.f;
-        for (int w = 0; w < nwarp; ++w) v += wsum[(size_t)w * 3 * L1 + x];
-        go[(size_t)q * A.kstride + k] = v;
-    }
-    if (threadIdx.x == 0) {
-        go[3 * A.kstride + 0] = gW;
-        go[3 * A.kstride + 1] = gS;
+#pragma unroll
+    for (int r = 0; r < ADJ_RB; ++r) {
+        if (r >= nr) break;                       // block-uniform
+        const double bW = block_sum_a(gW[r], red);
+        __syncthreads();
+        const double bS = block_sum_a(gS[r], red);
+        __syncthreads();
+        double *go = A.gout + (size_t)(tl * A.ncot + r0 + r) * A.gstride;
+        for (int x = threadIdx.x; x < 3 * L1; x += blockDim.x) {
+            const int q = x / L1, k = x - q * L1;
+            float v = 0.f;
+            for (int w = 0; w < nwarp; ++w) v += wsum[((size_t)w * rb + r) * 3 * L1 + x];
+            go[(size_t)q * A.kstride + k] = v;
+        }
+        if (threadIdx.x == 0) {
+            go[3 * A.kstride + 0] = bW;
+            go[3 * A.kstride + 1] = bS;
+        }
     }
 }
 

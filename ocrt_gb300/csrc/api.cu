@@ -611,7 +611,8 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     const int surf_threads = ((3 * G.N + 31) / 32) * 32;
     if (!capture) w.adj_stop = INT_MAX;
     for (int j = 1; j <= g.max_orders; ++j) {
-        LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<na, scan_threads, scan_smem_bytes(scan_threads), st>>>(B, A, G, w.t0, j));
+        LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB), scan_threads,
+                                              adj_scan_smem_bytes(scan_threads), st>>>(B, A, G, w.t0, j));
         if (capture) {
             if (j == w.adj_stop) break;
         } else if ((j - 1) % 4 == 0 || j == g.max_orders) {
@@ -633,8 +634,11 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     if (capture && w.adj_stop != INT_MAX)
         LAUNCH(plan, KC_ADJ_OTHER, k_stop_check<<<1, 32, 0, st>>>(g.acnt + w.adj_stop, g.err + 1));
     const int grad_threads = 2 * ((3 * G.N + 3 + 31) / 32) * 32;
-    LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<na, grad_threads, sizeof(float) * 3 * ((size_t)g.ntmax + 1) * (grad_threads / 32), st>>>(
-               B, W, A, G, w.t0));
+    // cotangent rows per block: up to ADJ_RB while the per-warp level sums fit
+    const size_t row_smem = sizeof(float) * 3 * ((size_t)g.ntmax + 1) * (grad_threads / 32);
+    const int grad_rb = std::max(1, std::min({ADJ_RB, g.ncot, (int)((200 * 1024) / row_smem)}));
+    LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<nw * ((g.ncot + grad_rb - 1) / grad_rb), grad_threads, row_smem * grad_rb, st>>>(
+               B, W, A, G, w.t0, grad_rb));
     LAUNCH(plan, KC_ADJ_GRAD, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
                B, W, A, G, w.p0, w.t0));
     return OCRT_OK;

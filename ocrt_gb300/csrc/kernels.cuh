@@ -17,6 +17,9 @@ __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const Pi
 // and its dynamic shared memory: J, the float2 total and 3 coefficients per slot.
 #define SCAN_DEPTH 8
 inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (4 + 8 + 12); }
+// k_adj_scan: cotangent rows per block (they share the transport coefficients)
+#define ADJ_RB 3
+inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 8) + 12); }
 // k_tables launch shape: grid (tasks, tables_yblocks), one (outgoing, incoming)
 // pair per thread; moments are staged TB_LC at a time (even).
 #define TB_LC 16
@@ -107,7 +110,7 @@ __global__ void k_adj_source(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
 __global__ void k_adj_mol(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0,
                           const float *Bp, const float *Br, const float *Bt, int L);
 __global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
-__global__ void k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
+__global__ void k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb);
 __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, int t0);
 size_t adj_mol_smem_bytes(const Geom &G);
 
