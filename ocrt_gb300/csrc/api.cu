@@ -169,6 +169,12 @@ struct Wave {
     int fwd_stop = INT_MAX, adj_stop = INT_MAX;
 };
 
+bool force_simt_coxmunk()
+{
+    const char *e = getenv("OCRT_GB_COXMUNK");
+    return e && strcmp(e, "simt") == 0;
+}
+
 bool force_simt()
 {
     const char *e = getenv("OCRT_GB_SOURCE_KERNEL");
@@ -204,6 +210,8 @@ struct Group {
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
     float *F = nullptr, *J = nullptr, *ops = nullptr;
     float *molV = nullptr;   // [3][32][CIN] molecular input factors V_m of the tensor-core pass
+    short2 *cmpairs = nullptr;   // (outgoing, incoming) slot pairs of the tensor-core Cox-Munk kernel
+    int ncmpairs = 0;
     float *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     float2 *Tot = nullptr;
     bool use_tc = false;
@@ -279,7 +287,7 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.molV, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.err, g.F, g.J, g.ops, g.molV, g.cmpairs, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
@@ -475,6 +483,17 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     // (k_primary, k_scan). ----
     g.use_tc = tc_supported(G) && !force_simt();
     if (g.use_tc && (rc = alloc(g.molV, (size_t)3 * 32 * G.CIN))) return rc;
+    // Cox-Munk pairs for the tensor-core projection: ring slots o < NR, incoming
+    // Gauss slots and the sun (i = N); Gauss pairs with o > i are written by
+    // their reciprocal pair
+    if (g.any_rough && coxmunk_tc_supported(g.Mmax, g.nphi, ncot > 0) && !force_simt_coxmunk()) {
+        std::vector<short2> pl;
+        for (int o = 0; o < G.NR; ++o)
+            for (int i = 0; i <= G.N; ++i)
+                if (!(o < G.N && i < G.N && o > i)) pl.push_back(make_short2((short)o, (short)i));
+        g.ncmpairs = (int)pl.size();
+        if ((rc = up(g.cmpairs, pl))) return rc;
+    }
     if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
         const int KP = (G.COUT + 31) & ~31;
         if ((rc = alloc(g.opsT, (size_t)g.wave_tasks * (G.CIN + 32) * KP))) return rc;
@@ -721,11 +740,20 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
                     k_coxmunk<<<dim3(G.N + 1, G.NR, np), b, smem, st>>>(g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu,
                                                                       g.cs, g.Mmax, g.lam, g.srf);
             };
-            int cb = 256;
-            rc = tuned_block(dw ? "k_coxmunk_dw" : "k_coxmunk", dw ? (const void *)k_coxmunk_dw : (const void *)k_coxmunk,
-                             {G.N, g.nphi, g.Mmax}, !capture, st, coxmunk, &cb);
-            if (rc) return rc;
-            LAUNCH(plan, KC_COXMUNK, coxmunk(cb));
+            if (g.cmpairs) {
+                const int per = coxmunk_tc_pairs_per_cta();
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk_tc<<<dim3((g.ncmpairs + per - 1) / per, np), 256,
+                                                         coxmunk_tc_smem_bytes(g.Mmax, dw), st>>>(
+                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.Mmax, g.lam, dw ? g.lamd : nullptr, g.srf,
+                           dw ? g.srfW : nullptr, g.cmpairs, g.ncmpairs, dw ? 1 : 0, g.err));
+            } else {
+                int cb = 256;
+                rc = tuned_block(dw ? "k_coxmunk_dw" : "k_coxmunk",
+                                 dw ? (const void *)k_coxmunk_dw : (const void *)k_coxmunk, {G.N, g.nphi, g.Mmax},
+                                 !capture, st, coxmunk, &cb);
+                if (rc) return rc;
+                LAUNCH(plan, KC_COXMUNK, coxmunk(cb));
+            }
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
@@ -817,6 +845,7 @@ int ocrt_gb_init(int device)
     CK(cudaDeviceGetAttribute(&g_nsm, cudaDevAttrMultiProcessorCount, device));
     CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_coxmunk_dw, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_coxmunk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

@@ -34,6 +34,15 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
                          float *ops, float *pvec, float *fvec);
+// coxmunk_tc.cu: Cox-Munk Fourier kernels with the azimuth projection on tcgen05.
+// pairs: (outgoing slot, incoming slot) list of the ring (Gauss pairs with
+// outgoing > incoming left out: the reciprocal pair writes them).
+__global__ void k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
+                             const double *gmu, const float *cs_tab, int Mtab, const double *lamv, const double *lamd,
+                             float *srf, float *srfW, const short2 *pairs, int npairs, int dw, int *err);
+size_t coxmunk_tc_smem_bytes(int Mtab, bool dw);
+bool coxmunk_tc_supported(int Mtab, int nphi, bool dw);
+int coxmunk_tc_pairs_per_cta();
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
                           const double *gmu, const float *cs_tab, int Mtab, const double *lamv, float *srf);
 __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
