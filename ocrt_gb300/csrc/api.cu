@@ -211,6 +211,7 @@ struct Group {
     float *F = nullptr, *J = nullptr, *ops = nullptr;
     float *molV = nullptr;   // [3][32][CIN] molecular input factors V_m of the tensor-core pass
     short2 *cmpairs = nullptr;   // (outgoing, incoming) slot pairs of the tensor-core Cox-Munk kernel
+    float *cstiles = nullptr;    // its cos/sin B tiles, split and swizzled
     int ncmpairs = 0;
     float *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
     float2 *Tot = nullptr;
@@ -287,7 +288,7 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.molV, g.cmpairs, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.err, g.F, g.J, g.ops, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
@@ -492,7 +493,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
             for (int i = 0; i <= G.N; ++i)
                 if (!(o < G.N && i < G.N && o > i)) pl.push_back(make_short2((short)o, (short)i));
         g.ncmpairs = (int)pl.size();
-        if ((rc = up(g.cmpairs, pl))) return rc;
+        if ((rc = up(g.cmpairs, pl)) || (rc = alloc(g.cstiles, coxmunk_tc_tiles_floats(g.Mmax, g.nphi)))) return rc;
     }
     if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
         const int KP = (G.COUT + 31) & ~31;
@@ -685,6 +686,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
                                                                                   g.molV));
     if (g.any_rough) {
         LAUNCH(plan, KC_SETUP, k_cs_table<<<g.Mmax + 2, 256, 0, st>>>(g.Mmax, g.nphi, g.cs));
+        if (g.cstiles) LAUNCH(plan, KC_SETUP, k_cs_tiles<<<g.nphi / 64, 256, 0, st>>>(g.Mmax, g.nphi, g.cs, g.cstiles));
         LAUNCH(plan, KC_SETUP, k_seed_att<<<dim3(8, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Eatt));
         LAUNCH(plan, KC_SETUP, k_sancer<<<P, 128, 0, st>>>(g.px, P, g.N, g.gmu, g.lam, g.ncot ? g.lamd : nullptr));
     }
@@ -742,10 +744,11 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             };
             if (g.cmpairs) {
                 const int per = coxmunk_tc_pairs_per_cta();
-                LAUNCH(plan, KC_COXMUNK, k_coxmunk_tc<<<dim3((g.ncmpairs + per - 1) / per, np), 256,
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk_tc<<<dim3((g.ncmpairs + per - 1) / per, np), coxmunk_tc_threads(),
                                                          coxmunk_tc_smem_bytes(g.Mmax, dw), st>>>(
-                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.Mmax, g.lam, dw ? g.lamd : nullptr, g.srf,
-                           dw ? g.srfW : nullptr, g.cmpairs, g.ncmpairs, dw ? 1 : 0, g.err));
+                           g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.cstiles, g.Mmax, g.lam,
+                           dw ? g.lamd : nullptr, g.srf, dw ? g.srfW : nullptr, g.cmpairs, g.ncmpairs, dw ? 1 : 0,
+                           g.err));
             } else {
                 int cb = 256;
                 rc = tuned_block(dw ? "k_coxmunk_dw" : "k_coxmunk",

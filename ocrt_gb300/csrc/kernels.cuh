@@ -38,11 +38,15 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
 // pairs: (outgoing slot, incoming slot) list of the ring (Gauss pairs with
 // outgoing > incoming left out: the reciprocal pair writes them).
 __global__ void k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
-                             const double *gmu, const float *cs_tab, int Mtab, const double *lamv, const double *lamd,
-                             float *srf, float *srfW, const short2 *pairs, int npairs, int dw, int *err);
+                             const double *gmu, const float *cs_tab, const float *cs_tiles, int Mtab,
+                             const double *lamv, const double *lamd, float *srf, float *srfW, const short2 *pairs,
+                             int npairs, int dw, int *err);
+__global__ void k_cs_tiles(int Mtab, int nphi, const float *cs_tab, float *tiles);
 size_t coxmunk_tc_smem_bytes(int Mtab, bool dw);
+size_t coxmunk_tc_tiles_floats(int Mtab, int nphi);
 bool coxmunk_tc_supported(int Mtab, int nphi, bool dw);
 int coxmunk_tc_pairs_per_cta();
+int coxmunk_tc_threads();
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
                           const double *gmu, const float *cs_tab, int Mtab, const double *lamv, float *srf);
 __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
