@@ -604,11 +604,8 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     LAUNCH(plan, KC_ADJ_TOTALS, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
     if (w.n_simt) LAUNCH(plan, KC_ADJ_TOTALS, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
     if (w.n_tc)
-        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(B, W, G, w.t0, it, mtiles, 0));
-    if (w.n_mol && w.n_tc)
-        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), tc_fwd_threads(), tc_smem, st>>>(
-                   B, W, G, w.t0, it, mtiles, 1));
-    else if (w.n_mol)
+        LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(B, W, G, w.t0, it, mtiles));
+    if (w.n_mol && !w.n_tc)
         LAUNCH(plan, KC_ADJ_TOTALS, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                    B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
     // adjoint successive orders
@@ -772,11 +769,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
                 LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
             if (w.n_tc)
                 LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(
-                           B, W, G, w.t0, it, mtiles, 0));
-            if (w.n_mol && w.n_tc)
-                LAUNCH(plan, KC_MOL, k_source_tc<<<std::min(w.n_mol * mtiles, g_nsm), tc_fwd_threads(), tc_smem, st>>>(
-                           B, W, G, w.t0, it, mtiles, 1));
-            else if (w.n_mol)
+                           B, W, G, w.t0, it, mtiles));
+            if (w.n_mol && !w.n_tc)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
             LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, scan_smem_bytes(scan_threads), st>>>(B, W, G, w.t0, it));
@@ -1115,9 +1109,9 @@ int ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, doubl
                 const int sc = g.use_tc ? KC_SOURCE_TC : KC_SOURCE;
                 plan->flops[sc] += ords * 72.0 * N * N * K;
                 plan->bytes[sc] += ords * (K * 6 * N + K * 6 * NR + 36.0 * N * NR) * 4.0;
-                if (tk.has_mol && g.use_tc) {          // dense U V pass on the tensor cores
-                    plan->flops[KC_MOL] += ords * 72.0 * N * N * K;
-                    plan->bytes[KC_MOL] += ords * (K * 6 * N + 2.0 * K * 6 * NR + 36.0 * N * NR) * 4.0;
+                if (tk.has_mol && g.use_tc) {          // dense U V inside the tensor-core pass
+                    plan->flops[KC_SOURCE_TC] += ords * 72.0 * N * N * K;
+                    plan->bytes[KC_SOURCE_TC] += ords * (36.0 * N * NR) * 4.0;
                 } else if (tk.has_mol) {               // rank-24 form on CUDA cores
                     plan->flops[KC_MOL] += ords * 2.0 * K * 24.0 * (N + 6 * NR);
                     plan->bytes[KC_MOL] += ords * (K * 6 * N + 2.0 * K * 6 * NR) * 4.0;

@@ -147,7 +147,7 @@ __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const doubl
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
-__global__ void k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode);
+__global__ void k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
 __global__ void k_adj_source_tc(BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
 __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
 __global__ void k_mol_utrans(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);

@@ -44,12 +44,13 @@
 
 using namespace tcg;
 
-// ADJ = false: forward source.  A rows = levels of one task's field F,
-//   B = [NP][CIN], K = CIN.  mode 0: the aerosol operator, J[k][c] =
-//   x_k D[k][c] for c < COUT, items = active list x level tiles; mode 1: the
-//   dense molecular operator U V of the m <= 2 tasks (rt_sos_operator.c:
-//   387-406), J[k][c] += y_k D[k][c], items = active molecular list x level
-//   tiles (run after mode 0 on the same order).
+// ADJ = false: forward source.  A rows = levels of one task's field F, K = CIN,
+//   B = the aerosol operator [NP][CIN] into one TMEM accumulator; for m <= 2
+//   tasks the item runs NKT more K tiles over the same field rows with B = the
+//   dense molecular operator U V (rt_sos_operator.c:387-406) into the second
+//   accumulator.  Epilogue J[k][c] = x_k D_aer[k][c] + y_k D_mol[k][c] for
+//   c < COUT, one write.  Items = active list x level tiles; an item takes one
+//   accumulator slot, or two for m <= 2.
 // ADJ = true: transposed source of the adjoint.  A rows = the ncot adjoint
 //   fields of one task stacked (ncot * K rows of muJ, row stride LDC, columns
 //   past LDC read as zero), B = the task's transposed operator AopT [CIN][KP]
@@ -59,7 +60,7 @@ using namespace tcg;
 //   the wave x tiles, skipped when none of its rows is active.
 template <bool ADJ>
 __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBufs &W, const AdjBufs &AB,
-                                               const Geom &G, int t0, int it, int mtiles, int nw, int mode)
+                                               const Geom &G, int t0, int it, int mtiles, int nw)
 {
     extern __shared__ unsigned char smem_raw[];
     // MMA N: the operator rows (NB); in the adjoint, m <= 2 tasks add 32 rows of
@@ -80,9 +81,9 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
     // epilogue transpose tiles: [4 warps][32 rows][TC_TP floats]
     float *tpose = (float *)(base + 2 * STAGE + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n_items = (ADJ ? nw : (mode ? B.mol_cnt[it - 1] : B.active_cnt[it - 1])) * mtiles;
-    const int *alist = ADJ ? nullptr : (mode ? B.mlist[it & 1] : B.alist[it & 1]);
-    int *counter = ADJ ? &AB.awork[it] : &B.work[it * 4 + (mode ? 3 : 0)];
+    const int n_items = (ADJ ? nw : B.active_cnt[it - 1]) * mtiles;
+    const int *alist = ADJ ? nullptr : B.alist[it & 1];
+    int *counter = ADJ ? &AB.awork[it] : &B.work[it * 4];
     auto task_of = [&](int li) -> int { return ADJ ? li : alist[li]; };
 
     if (warp == 2) {
@@ -122,19 +123,23 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
         // K columns < a_cols real; B rows: operator rows of length b_ld.
         const int a_cols = ADJ ? G.LDC : G.CIN, b_ld = ADJ ? ((G.COUT + 31) & ~31) : G.CIN;
         float4 ra[TC_AQ], rb[TC_BQ];
+        // item operands: A rows (nra of them real), B = Bb for K tiles below
+        // NKT and Bm (dense molecular operator) for NKT .. nkt - 1
+        struct Opnd { const float *Ab, *Bb, *Bm; int nra, nbi, nkt; };
         // K tile kt of the item into registers: A rows 0 .. nra - 1 of the item
         // (zero past the task and past a_cols), B rows 0 .. nbi - 1
-        auto load = [&](const float *Ab, int nra, const float *Bb, int nbi, int kt) {
-            const int col = kt * TC_KT + ch * 4;
+        auto load = [&](const Opnd &o, int kt) {
+            const int kk = kt < NKT ? kt : kt - NKT;
+            const int col = kk * TC_KT + ch * 4;
             const bool acol = col + 4 <= a_cols;
-            const float4 *pa = reinterpret_cast<const float4 *>(Ab + (size_t)r8 * G.LDC + col);
-            const float4 *pb = reinterpret_cast<const float4 *>(Bb + (size_t)r8 * b_ld + col);
+            const float4 *pa = reinterpret_cast<const float4 *>(o.Ab + (size_t)r8 * G.LDC + col);
+            const float4 *pb = reinterpret_cast<const float4 *>((kt < NKT ? o.Bb : o.Bm) + (size_t)r8 * b_ld + col);
 #pragma unroll
             for (int i = 0; i < TC_AQ; ++i)
-                ra[i] = acol && r8 + 16 * i < nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
+                ra[i] = acol && r8 + 16 * i < o.nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
             for (int i = 0; i < TC_BQ; ++i)
-                if (r8 + 16 * i < nbi) rb[i] = __ldg(pb + (size_t)i * 4 * b_ld);
+                if (r8 + 16 * i < o.nbi) rb[i] = __ldg(pb + (size_t)i * 4 * b_ld);
         };
         // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
         auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
@@ -179,7 +184,6 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             if (ok) item = qitem[jj & (TC_Q - 1)];
             return ok != 0;
         };
-        struct Opnd { const float *Ab, *Bb; int nra, nbi; };
         auto operands = [&](int item) -> Opnd {
             const int li = item / mtiles, mt = item - li * mtiles;
             const int tl = task_of(li);
@@ -189,7 +193,10 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             o.nra = min(TC_M, (ADJ ? AB.ncot * tk.K : tk.K) - r0);
             o.nbi = ADJ && tk.has_mol ? NBM : NB;
             o.Ab = ADJ ? AB.AJ + (size_t)tk.fld_off * AB.ncot + (size_t)r0 * G.LDC : W.F + tk.fld_off + (size_t)r0 * G.LDC;
-            o.Bb = ADJ ? AB.opsT + (size_t)tl * (NB + 32) * b_ld : W.ops + (mode ? tk.uv_off : tk.op_off);
+            o.Bb = ADJ ? AB.opsT + (size_t)tl * (NB + 32) * b_ld : W.ops + tk.op_off;
+            const bool dbl = !ADJ && tk.has_mol;
+            o.Bm = dbl ? W.ops + tk.uv_off : o.Bb;
+            o.nkt = dbl ? 2 * NKT : NKT;
             return o;
         };
         if (pt == 0) fetch_publish(0);
@@ -203,10 +210,10 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             const Opnd op = operands(item);
             // this group's K tiles of the item: global tile index g + kt with (g + kt) & 1 == grp
             const int kt0 = (int)((grp - (int)(g & 1)) & 1);
-            if (!have && kt0 < NKT) load(op.Ab, op.nra, op.Bb, op.nbi, kt0);
+            if (!have && kt0 < op.nkt) load(op, kt0);
             have = false;
             bool stop = false;
-            for (int kt = kt0; kt < NKT; kt += 2) {
+            for (int kt = kt0; kt < op.nkt; kt += 2) {
                 const uint32_t gg = g + (uint32_t)kt, u = gg >> 1;
                 const int s = (int)(gg & 1);
                 int free_ok = (u == 0 || lane != 0) ? 1 : (int)mbar_wait(&empty[s], (u - 1) & 1);
@@ -223,39 +230,46 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[s]);
-                if (kt + 2 < NKT) {
-                    load(op.Ab, op.nra, op.Bb, op.nbi, kt + 2);
+                if (kt + 2 < op.nkt) {
+                    load(op, kt + 2);
                 } else {
                     int nxt = -1;
                     if (!item_at(j + 1, nxt)) { *abort_flag = 1; stop = true; break; }
-                    const int kt0n = (int)((grp - (int)((g + (uint32_t)NKT) & 1)) & 1);
-                    if (nxt >= 0 && kt0n < NKT) {
+                    const int kt0n = (int)((grp - (int)((g + (uint32_t)op.nkt) & 1)) & 1);
+                    if (nxt >= 0) {
                         const Opnd on = operands(nxt);
-                        load(on.Ab, on.nra, on.Bb, on.nbi, kt0n);
-                        have = true;
+                        if (kt0n < on.nkt) { load(on, kt0n); have = true; }
                     }
                 }
             }
             if (stop) break;
-            g += (uint32_t)NKT;
+            g += (uint32_t)op.nkt;
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
-        uint32_t g = 0;
+        uint32_t g = 0, u = 0, sc0 = 0, sc1 = 0;                 // tiles, accumulator slots, uses per slot
         for (int j = 0;; ++j) {
             if (!mbar_wait(&qbar[j & (TC_Q - 1)], (j / TC_Q) & 1)) { *abort_flag = 1; break; }
             const int item = qitem[j & (TC_Q - 1)];
             if (item < 0 || *abort_flag) break;
-            const int nbi = ADJ && B.tasks[t0 + task_of(item / mtiles)].has_mol ? NBM : NB;
+            const bool hm = B.tasks[t0 + task_of(item / mtiles)].has_mol;
+            const int nbi = ADJ && hm ? NBM : NB;
+            const bool dbl = !ADJ && hm;
+            const int nkt = dbl ? 2 * NKT : NKT;
             const uint32_t idesc = (IDESC_BASE & ~(0x3Fu << 17)) | ((uint32_t)(nbi >> 3) << 17);
-            const int b = j & 1;
-            const uint32_t ub = j >> 1;
-            if (ub >= 1 && !mbar_wait(&tempty[b], (ub - 1) & 1)) { *abort_flag = 1; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t acc = tmem + (uint32_t)(b * TC_ACC_COLS);
+            const int b0 = (int)(u & 1), b1 = (int)((u + 1) & 1);
             bool ok = true;
-            for (int kt = 0; kt < NKT; ++kt, ++g) {
+            for (int q = 0; q < (dbl ? 2 : 1); ++q) {
+                const int bq = q ? b1 : b0;
+                const uint32_t n = bq ? sc1 : sc0;
+                if (n >= 1 && !mbar_wait(&tempty[bq], (n - 1) & 1)) { ok = false; break; }
+            }
+            if (!ok) { *abort_flag = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int kt = 0; kt < nkt; ++kt, ++g) {
+                const uint32_t acc = tmem + (uint32_t)((kt < NKT ? b0 : b1) * TC_ACC_COLS);
+                const int kf = kt < NKT ? kt : kt - NKT;
                 const int s = g & 1;
                 if (!mbar_wait(&full[s], (g >> 1) & 1)) { *abort_flag = 1; ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -267,14 +281,17 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                     const uint32_t off = kk * 32;     // 8 tf32 = 32 bytes along the swizzled row
                     const uint64_t ah = sdesc_sw128(sa_hi + off), al = sdesc_sw128(sa_lo + off);
                     const uint64_t bh = sdesc_sw128(sb_hi + off), bl = sdesc_sw128(sb_lo + off);
-                    umma_tf32(acc, ah, bh, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+                    umma_tf32(acc, ah, bh, idesc, (kf > 0 || kk > 0) ? 1u : 0u);
                     umma_tf32(acc, ah, bl, idesc, 1u);
                     umma_tf32(acc, al, bh, idesc, 1u);
                 }
                 umma_commit(&empty[s]);
             }
             if (!ok) break;
-            umma_commit(&tfull[b]);
+            umma_commit(&tfull[b0]);
+            if (dbl) umma_commit(&tfull[b1]);
+            if (dbl) { ++sc0; ++sc1; } else if (b0) { ++sc1; } else { ++sc0; }
+            u += dbl ? 2 : 1;
         }
         // every MMA this thread issued has completed before TMEM is released
         umma_commit(done);
@@ -282,15 +299,20 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
     } else if (warp >= 4 && warp < 8) {
         // ---------------- epilogue ----------------
         const int q4 = warp - 4;
+        uint32_t u = 0, sc0 = 0, sc1 = 0;                        // accumulator slots, uses per slot
         for (int j = 0;; ++j) {
             if (!mbar_wait(&qbar[j & (TC_Q - 1)], (j / TC_Q) & 1)) { *abort_flag = 1; break; }
             const int item = qitem[j & (TC_Q - 1)];
             if (item < 0 || *abort_flag) break;
-            const int b = j & 1;
-            if (!mbar_wait(&tfull[b], (j >> 1) & 1)) { *abort_flag = 1; break; }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int li = item / mtiles, mt = item - li * mtiles;
             const TaskDev tk = B.tasks[t0 + task_of(li)];
+            const bool dbl = !ADJ && tk.has_mol;
+            const int b = (int)(u & 1), b1 = (int)((u + 1) & 1);
+            if (!mbar_wait(&tfull[b], (b ? sc1 : sc0) & 1) || (dbl && !mbar_wait(&tfull[b1], (b1 ? sc1 : sc0) & 1))) {
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const PixDev &d = B.px[tk.pix];
             const int row = mt * TC_M + q4 * 32 + lane;
             int k, ncols;
@@ -307,8 +329,10 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                 outbase = W.J + tk.fld_off;
                 ncols = G.COUT;
             }
-            const float x = live ? B.lvf[3 * (d.lev_off + k) + (mode ? 1 : 0)] : 0.f;
+            const float x = live ? B.lvf[3 * (d.lev_off + k)] : 0.f;
+            const float ym = dbl && live ? B.lvf[3 * (d.lev_off + k) + 1] : 0.f;
             const uint32_t tb = tmem + (uint32_t)(b * TC_ACC_COLS) + ((uint32_t)(q4 * 32) << 16);
+            const uint32_t tbm = tmem + (uint32_t)(b1 * TC_ACC_COLS) + ((uint32_t)(q4 * 32) << 16);
             // adjoint, m <= 2: the rank-24 product U^T muJ of this row sits in
             // columns NB .. NB + 23
             const bool mol = ADJ && tk.has_mol;
@@ -333,6 +357,12 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                 tmem_ld16(tb + (uint32_t)(cb * 16), v);
 #pragma unroll
                 for (int jj = 0; jj < 16; ++jj) v[jj] *= x;
+                if (dbl) {
+                    float vm[16];
+                    tmem_ld16(tbm + (uint32_t)(cb * 16), vm);
+#pragma unroll
+                    for (int jj = 0; jj < 16; ++jj) v[jj] = fmaf(ym, vm[jj], v[jj]);
+                }
                 if (mol) {
                     // the chunk lies in input block b = 16 cb / N (N % 16 == 0);
                     // V^T: input column c = bN + i takes sum_f V[4b + f][c] t[4b + f]
@@ -361,21 +391,19 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                         const bool rlive = ADJ ? rg < AB.ncot * tk.K : rg <= d.nt;
                         if (!rlive) continue;
                         float *dst = outbase + (size_t)rg * G.LDC + c;
-                        const float4 t = *reinterpret_cast<const float4 *>(tp + rl * TC_TP + (lane & 3) * 4);
-                        if (!ADJ && mode) {
-                            float4 o = *reinterpret_cast<float4 *>(dst);
-                            o.x += t.x; o.y += t.y; o.z += t.z; o.w += t.w;
-                            *reinterpret_cast<float4 *>(dst) = o;
-                        } else {
-                            *reinterpret_cast<float4 *>(dst) = t;
-                        }
+                        *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(tp + rl * TC_TP + (lane & 3) * 4);
                     }
                 }
                 __syncwarp();
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[b]);
+            if (lane == 0) {
+                mbar_arrive(&tempty[b]);
+                if (dbl) mbar_arrive(&tempty[b1]);
+            }
+            if (dbl) { ++sc0; ++sc1; } else if (b) { ++sc1; } else { ++sc0; }
+            u += dbl ? 2 : 1;
         }
     }
     __syncthreads();
@@ -389,10 +417,10 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
 }
 
 __global__ void __launch_bounds__(TC_FWD_THREADS, 1)
-k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mode)
+k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles)
 {
     AdjBufs none{};
-    source_tc_body<false>(B, W, none, G, t0, it, mtiles, 0, mode);
+    source_tc_body<false>(B, W, none, G, t0, it, mtiles, 0);
 }
 
 // Transposed contraction of the adjoint for adjoint order `it` (work counter
@@ -400,7 +428,7 @@ k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles, int mod
 __global__ void __launch_bounds__(TC_FWD_THREADS, 1)
 k_adj_source_tc(BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw)
 {
-    source_tc_body<true>(B, W, AB, G, t0, it, mtiles, nw, 0);
+    source_tc_body<true>(B, W, AB, G, t0, it, mtiles, nw);
 }
 
 static size_t tc_smem_for(int NBM)
