@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
     if (c < G.COUT) decode_col_a(G, c, s, h, g);
     const bool valid = c < G.COUT && g < d.n_ring;
     float *a[ADJ_RB], *mj[ADJ_RB];
-    float2 *At[ADJ_RB];
+    float *At[ADJ_RB];
 #pragma unroll
     for (int q = 0; q < ADJ_RB; ++q) {
         const size_t off = adj_off(tk, G, A.ncot, r0 + (q < nr ? q : 0));
@@ -277,8 +277,8 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
         extern __shared__ float scan_smem[];
         const int bs = blockDim.x;
         float *As = scan_smem;                                                   // [SCAN_DEPTH][RB][bs]
-        float2 *Ts = reinterpret_cast<float2 *>(As + SCAN_DEPTH * ADJ_RB * bs);   // [SCAN_DEPTH][RB][bs]
-        float *Cs = reinterpret_cast<float *>(Ts + SCAN_DEPTH * ADJ_RB * bs);     // [SCAN_DEPTH][3][bs]
+        float *Ts = As + SCAN_DEPTH * ADJ_RB * bs;                                // [SCAN_DEPTH][RB][bs]
+        float *Cs = Ts + SCAN_DEPTH * ADJ_RB * bs;                                // [SCAN_DEPTH][3][bs]
         // coefficient rows of step j: upward tv, cb at k - 1 and ca at k;
         // downward tv, cb at k and ca at k - 1 (absent rows read as zero)
         auto issue = [&](int jj) {
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                     for (int q = 0; q < ADJ_RB; ++q)
                         if (act[q]) {
                             cp_async4(As + (sl * ADJ_RB + q) * bs + c, a[q] + o);
-                            cp_async8(Ts + (sl * ADJ_RB + q) * bs + c, At[q] + o);
+                            cp_async4(Ts + (sl * ADJ_RB + q) * bs + c, At[q] + o);
                         }
                 }
                 const int kt = h == 0 ? k - 1 : k, ka = h == 0 ? k : k - 1;
@@ -318,11 +318,11 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
                 if (!act[q]) continue;
                 const float av = has_a ? As[(sl * ADJ_RB + q) * bs + c] : 0.f;
                 if (has_a) {
-                    const float2 t = df_add(Ts[(sl * ADJ_RB + q) * bs + c], av);
+                    const float t = Ts[(sl * ADJ_RB + q) * bs + c] + av;
                     At[q][o] = t;
                     if (clear) a[q][o] = 0.f;
                     mi[q] = fmaxf(mi[q], fabsf(av));
-                    mt[q] = fmaxf(mt[q], fabsf(t.x));
+                    mt[q] = fmaxf(mt[q], fabsf(t));
                 }
                 const float nu = av + tv * nup[q];
                 mj[q][o] = ca * nu + cb * nup[q];
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
     float *ws = wsum + (size_t)warp * rb * 3 * L1;
     for (int x = lane; x < rb * 3 * L1; x += 32) ws[x] = 0.f;
     __syncwarp();
-    const float2 *At[ADJ_RB];
+    const float *At[ADJ_RB];
 #pragma unroll
     for (int q = 0; q < ADJ_RB; ++q) At[q] = A.ATot + adj_off(tk, G, A.ncot, r0 + (q < nr ? q : 0));
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
                 const size_t o = (size_t)k * G.LDC + c;
 #pragma unroll
                 for (int r = 0; r < ADJ_RB; ++r)
-                    if (r < nr) { const float2 t = At[r][o]; av[r][q] = t.x + t.y; }
+                    if (r < nr) av[r][q] = At[r][o];
                 jx[q] = Jx[o];
                 tt[q] = Tot[o].x;
                 xk[q] = lv[3 * k]; yk[q] = lv[3 * k + 1]; chk[q] = lv[3 * k + 2];

@@ -223,7 +223,7 @@ struct Group {
            *grad = nullptr;
     float *dTc = nullptr, *dCa = nullptr, *dCb = nullptr, *srfW = nullptr, *AF = nullptr, *AJ = nullptr,
           *Abc = nullptr;
-    float2 *ATot = nullptr;
+    float *ATot = nullptr;
     TaskState *Ast = nullptr;
     // angle-grid LUT mode
     bool any_lut = false;
@@ -402,7 +402,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
         size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
-            pb += (size_t)ncot * (pf * 16 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
+            pb += (size_t)ncot * (pf * 12 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)G.CIN * ((G.COUT + 31) & ~31) * 4;
         if (q > w.p0 && bytes + pb > budget) {
             close(q);
@@ -611,7 +611,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     // adjoint successive orders
     CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.AJ, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.ATot, 0, sizeof(float2) * w.fld * g.ncot, st));
+    CK(cudaMemsetAsync(g.ATot, 0, sizeof(float) * w.fld * g.ncot, st));
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
     CK(cudaMemsetAsync(g.awork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));

@@ -19,7 +19,7 @@ __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const Pi
 inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (4 + 8 + 12); }
 // k_adj_scan: cotangent rows per block (they share the transport coefficients)
 #define ADJ_RB 3
-inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 8) + 12); }
+inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 4) + 12); }
 // k_tables launch shape: grid (tasks, tables_yblocks), one (outgoing, incoming)
 // pair per thread; moments are staged TB_LC at a time (even).
 #define TB_LC 16
@@ -102,7 +102,7 @@ struct AdjBufs {
     float *AJ;             // transposed-transport output muJ (FP32, like AF)
     const float *opsT;     // per wave task [CIN + 32][KP] (FP32, KP = COUT rounded up to 32): the transposed
                            // aerosol operator, then for m <= 2 the transposed molecular factor U^T (24 rows, 8 zero)
-    float2 *ATot;          // adjoint total (hi, lo) pairs
+    float *ATot;           // adjoint total (FP32: it only feeds the gradients)
     float *bc;             // mu_bc per adjoint task [NR][3]
     TaskState *st;         // per adjoint task
     int *acnt;             // [max_orders + 2] adjoint tasks still active after order j
