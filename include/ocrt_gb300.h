@@ -61,6 +61,12 @@ typedef struct {
     int    decouple_sunglint;/* 1 => direct sunglint not added to rho */
 } ocrt_case;
 
+/* ---- trace-gas absorption state (rt_absorption_t, rt_absorption.h:66-76) --
+ * Opaque; made by ocrt_gb_gas_create and named in ocrt_opts.gas the way the
+ * reference's rt_options_t.abs_state names an rt_absorption_t
+ * (rt_solver.c:753-759).  It must outlive every solve or plan that uses it. */
+typedef struct ocrt_gas ocrt_gas;
+
 /* ---- solver options (solve-relevant fields of rt_options_t, rt_types.h:654-795) */
 typedef struct {
     int    n_mu;             /* Gauss nodes per hemisphere, default 24, max 64 */
@@ -75,6 +81,7 @@ typedef struct {
     int    rayleigh_profile; /* OCRT_PROFILE_* (default US62, the reference's mapping) */
     double rayleigh_h_km;    /* scale height for OCRT_PROFILE_EXPONENTIAL */
     int    n_phi_surface;    /* Cox-Munk azimuth quadrature, default 1024 */
+    const ocrt_gas *gas;     /* NULL => no gas absorption (abs_state, rt_atm.c:437) */
 } ocrt_opts;
 
 /* ---- aerosol expansion (rt_aerosol_input_t moment path, rt_solver.h:94-114) */
@@ -280,10 +287,45 @@ typedef struct {
  * Otherwise OCRT_ERR_UNSUPPORTED. */
 /* Profile values of the per-layer parameters of one case, the values that a
  * NULL ocrt_layers array stands for: dtau[l] = h_{l+1} - h_l and
- * ssa[l] = the summed scattering fractions of level l+1 (rt_atm.c:177-400).
+ * ssa[l] = the summed scattering fractions of level l+1 (rt_atm.c:177-400),
+ * after the gas absorption step when opts.gas is set.
  * Both arrays hold opts.n_layers entries (either may be NULL). */
 int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
                            double *dtau, double *ssa);
+
+/* ---- trace-gas absorption (rt_absorption.c, rt_atm.c:437-548) -----------
+ * Six gases in the reference's order (rt_absorption.h:35-37) and the seven
+ * AFGL atmospheres (rt_absorption.h:24-32).  ocrt_gb_gas_create reads
+ * <afgl_dir>/afgl_<profile>.dat and <xsec_dir>/xsec_<gas>.dat (the files of
+ * the reference's inputs/afgl_atm and inputs/xsec), integrates the default
+ * columns and uploads the profile and the cross-section tables to the device
+ * once.  column_override: NULL, or six entries, each < 0 (AFGL default) or
+ * the total column in molecules/cm^2 (the profile shape is kept).  A missing
+ * or unusable cross-section file leaves that gas out, as in the reference
+ * (rt_absorption.c:486-520); a missing AFGL file is OCRT_ERR_ARGS.
+ * With opts.gas set, every solve adds the per-layer absorption depths of
+ * the case's level altitudes to the optical-depth grid and scales the
+ * scattering fractions by dtau_old / dtau_new (rt_atm.c:449-546); IPSS uses
+ * the layer absorption for its single-scattering albedo (rt_ipss.c:64-70).
+ * Layer overrides (ocrt_layers) apply on top of the gas-loaded profile. */
+enum { OCRT_GAS_H2O = 0, OCRT_GAS_O3, OCRT_GAS_O2, OCRT_GAS_CO2, OCRT_GAS_NO2, OCRT_GAS_CH4, OCRT_N_GAS };
+enum { OCRT_AFGL_USSTD76 = 0, OCRT_AFGL_TROPICAL, OCRT_AFGL_MLSUMM, OCRT_AFGL_MLWINT,
+       OCRT_AFGL_SASUMM, OCRT_AFGL_SAWINT, OCRT_AFGL_USERDEF };
+int  ocrt_gb_gas_create(const char *afgl_dir, const char *xsec_dir, int profile,
+                        const double *column_override, ocrt_gas **out);
+void ocrt_gb_gas_destroy(ocrt_gas *gas);
+/* Column absorption depth at one wavelength, per gas and total
+ * (rt_absorption_tau_per_gas / rt_absorption_tau_total, rt_absorption.c:556-600).
+ * tau_per_gas: NULL or OCRT_N_GAS entries. */
+int  ocrt_gb_gas_tau(const ocrt_gas *gas, double wavelength_nm, double *tau_per_gas, double *tau_total);
+/* Effective and default total columns (molecules/cm^2), OCRT_N_GAS entries
+ * each (either may be NULL); overridden[g] = 1 where the caller set it. */
+int  ocrt_gb_gas_columns(const ocrt_gas *gas, double *column_eff, double *column_default, int *overridden);
+/* Per-layer absorption depths of one case as the solve applies them
+ * (tau_abs, opts.n_layers entries, zero without opts.gas) and the level
+ * altitudes in km (z_km, opts.n_layers + 1 entries, level 0 = TOA). */
+int  ocrt_gb_layer_gas(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                       double *tau_abs, double *z_km);
 
 int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases,
                                 const ocrt_opts *opts, int opts_per_case,

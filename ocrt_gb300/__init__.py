@@ -24,6 +24,7 @@ EXPORTS = [
     "ocrt_gb_plan_kernel_stats", "ocrt_gb_solve_case_noalloc", "ocrt_gb_solve_batch_adjoint",
     "ocrt_gb_layer_defaults", "ocrt_gb_plan_create_adjoint", "ocrt_gb_plan_gradients",
     "ocrt_gb_solve_case_lut", "ocrt_gb_solve_batch_lut", "ocrt_gb_plan_graph_ready", "ocrt_gb_autotune_summary",
+    "ocrt_gb_gas_create", "ocrt_gb_gas_destroy", "ocrt_gb_gas_tau", "ocrt_gb_gas_columns", "ocrt_gb_layer_gas",
 ]
 
 
@@ -73,6 +74,15 @@ def lib():
                                           C.c_int, C.POINTER(Lut), C.POINTER(Result), C.c_void_p]
     L.ocrt_gb_plan_graph_ready.argtypes = [C.c_void_p]
     L.ocrt_gb_autotune_summary.argtypes = [C.c_char_p, C.c_int]
+    L.ocrt_gb_gas_create.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_void_p)]
+    L.ocrt_gb_gas_destroy.argtypes = [C.c_void_p]
+    L.ocrt_gb_gas_destroy.restype = None
+    L.ocrt_gb_gas_tau.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.ocrt_gb_gas_columns.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int)]
+    L.ocrt_gb_layer_gas.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
     _lib = L
@@ -143,6 +153,68 @@ def layer_defaults(case, opts, aerosol=None):
                                     dt.ctypes.data_as(C.POINTER(C.c_double)),
                                     ss.ctypes.data_as(C.POINTER(C.c_double))))
     return dt, ss
+
+
+AFGL_PROFILES = ("usstd76", "tropical", "mlsumm", "mlwint", "sasumm", "sawint", "userdef")
+GASES = ("h2o", "o3", "o2", "co2", "no2", "ch4")
+
+
+class GasState:
+    """Trace-gas absorption state (rt_absorption_t): an AFGL atmosphere and
+    the six cross-section tables, resident on the device.  Set
+    ``opts.gas = state.handle`` to make a solve gas-loaded; keep the object
+    alive while any solve or plan uses it."""
+
+    def __init__(self, afgl_dir, xsec_dir, profile="usstd76", column_override=None):
+        L = lib()
+        prof = AFGL_PROFILES.index(profile) if isinstance(profile, str) else int(profile)
+        ov = None
+        if column_override is not None:
+            vals = [-1.0] * 6
+            if isinstance(column_override, dict):
+                for k, v in column_override.items():
+                    vals[GASES.index(k)] = float(v)
+            else:
+                vals = [float(v) for v in column_override]
+            ov = (C.c_double * 6)(*vals)
+        h = C.c_void_p()
+        _check(L.ocrt_gb_gas_create(os.fsencode(afgl_dir), os.fsencode(xsec_dir), prof, ov, C.byref(h)))
+        self.handle = h.value
+
+    def tau(self, wavelength_nm):
+        """(per-gas column absorption depths [6], total) at one wavelength."""
+        per, tot = (C.c_double * 6)(), C.c_double()
+        _check(lib().ocrt_gb_gas_tau(self.handle, wavelength_nm, per, C.byref(tot)))
+        return np.array(per[:]), tot.value
+
+    def columns(self):
+        """(effective columns [6], AFGL default columns [6], overridden [6])."""
+        e, d, o = (C.c_double * 6)(), (C.c_double * 6)(), (C.c_int * 6)()
+        _check(lib().ocrt_gb_gas_columns(self.handle, e, d, o))
+        return np.array(e[:]), np.array(d[:]), np.array(o[:], dtype=bool)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().ocrt_gb_gas_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def layer_gas(case, opts, aerosol=None):
+    """(tau_abs[nt], z_km[nt+1]): the per-layer gas absorption depths a solve
+    of this case applies and its level altitudes (level 0 = TOA)."""
+    L = lib()
+    n = opts.n_layers
+    ta, z = np.zeros(n), np.zeros(n + 1)
+    a = aerosol.struct if isinstance(aerosol, AerosolHolder) else aerosol
+    _check(L.ocrt_gb_layer_gas(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
+                               ta.ctypes.data_as(C.POINTER(C.c_double)), z.ctypes.data_as(C.POINTER(C.c_double))))
+    return ta, z
 
 
 def _layers_array(n, opts, layers):

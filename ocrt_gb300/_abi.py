@@ -49,7 +49,7 @@ class Opts(C.Structure):
         ("max_orders", C.c_int), ("tolerance", C.c_double), ("tau_r_source", C.c_int),
         ("pssa", C.c_int), ("view_as_node", C.c_int), ("aer_h_km", C.c_double),
         ("rayleigh_profile", C.c_int), ("rayleigh_h_km", C.c_double),
-        ("n_phi_surface", C.c_int),
+        ("n_phi_surface", C.c_int), ("gas", C.c_void_p),
     ]
 
 

@@ -24,6 +24,15 @@
  * --aer-l-max L, with gamma_2 and alpha_2 at 0.3 x the Rayleigh-form values.
  * When an aerosol is on and --n-layers is not given, 400 layers are used
  * (main.c:3342-3345).
+ *
+ * Gas absorption is on by default, as in the reference (main.c:1950-1960):
+ * the AFGL atmosphere (--atm-profile, default usstd76) and the six
+ * cross-section tables are read from inputs/afgl_atm and inputs/xsec under
+ * the working directory (the reference's fixed paths), or under
+ * $OCRT_GB_INPUTS when that is set.  --gas-column-h2o G (g/cm^2, alias
+ * --pwv-g-cm), --gas-column-o3 DU, --gas-column-no2 DU, --gas-column-o2 N,
+ * --gas-column-co2 N, --gas-column-ch4 N (molecules/cm^2) rescale a gas's
+ * column (main.c:2720-2745); all six at 0 give the gas-free result.
  */
 #include <math.h>
 #include <stdio.h>
@@ -48,7 +57,9 @@ static int usage(void)
             "            [--aod TAU --aer-hg-g G --aer-ssa W --aer-l-max L --aer-h-km H] [--pssa]\n"
             "            [--decouple-sunglint] [--n-layers K] [--m-max M] [--n-mu N] [--sos-max-orders K]\n"
             "            [--sos-tolerance T] [--lut-vza-step D --lut-raa-step D --lut-vza-max D --lut-output F]\n"
-            "            [--batch FILE.csv]\n");
+            "            [--batch FILE.csv] [--atm-profile usstd76|tropical|mlsumm|mlwint|sasumm|sawint|userdef]\n"
+            "            [--gas-column-h2o G | --pwv-g-cm G] [--gas-column-o3 DU] [--gas-column-no2 DU]\n"
+            "            [--gas-column-o2 N] [--gas-column-co2 N] [--gas-column-ch4 N]\n");
     return 2;
 }
 
@@ -163,6 +174,10 @@ int main(int argc, char **argv)
     int L = 120;
     double vstep = 2.5, rstep = 2.5, vmax = 85.0;
     const char *lut_out = NULL, *batch = NULL;
+    static const char *const profiles[7] = {"usstd76", "tropical", "mlsumm", "mlwint", "sasumm", "sawint", "userdef"};
+    static const char *const gas_names[OCRT_N_GAS] = {"h2o", "o3", "o2", "co2", "no2", "ch4"};
+    int atm_profile = OCRT_AFGL_USSTD76;
+    double gas_col[OCRT_N_GAS] = {-1.0, -1.0, -1.0, -1.0, -1.0, -1.0};
     for (int i = 1; i < argc; ++i) {
         const char *a = argv[i];
         if (!strcmp(a, "--help") || !strcmp(a, "-h")) return usage();
@@ -259,6 +274,23 @@ int main(int argc, char **argv)
         else if (!strcmp(a, "--lut-output")) lut_out = need_s(argc, argv, &i);
         else if (!strcmp(a, "--output-full-grid")) have_lut = 1;
         else if (!strcmp(a, "--batch")) batch = need_s(argc, argv, &i);
+        else if (!strcmp(a, "--atm-profile") || !strcmp(a, "--gas-profile")) {
+            const char *v = need_s(argc, argv, &i);
+            atm_profile = -1;
+            for (int k = 0; k < 7; ++k) if (!strcmp(v, profiles[k])) atm_profile = k;
+            if (atm_profile < 0) {
+                fprintf(stderr, "error: --atm-profile must be one of "
+                                "usstd76|tropical|mlsumm|mlwint|sasumm|sawint|userdef\n");
+                return 2;
+            }
+        }
+        else if (!strcmp(a, "--gas-column-h2o") || !strcmp(a, "--pwv-g-cm"))
+            gas_col[OCRT_GAS_H2O] = need_d(argc, argv, &i) * 6.02214076e23 / 18.01528;
+        else if (!strcmp(a, "--gas-column-o3")) gas_col[OCRT_GAS_O3] = need_d(argc, argv, &i) * 2.6868e16;
+        else if (!strcmp(a, "--gas-column-no2")) gas_col[OCRT_GAS_NO2] = need_d(argc, argv, &i) * 2.6868e16;
+        else if (!strcmp(a, "--gas-column-o2")) gas_col[OCRT_GAS_O2] = need_d(argc, argv, &i);
+        else if (!strcmp(a, "--gas-column-co2")) gas_col[OCRT_GAS_CO2] = need_d(argc, argv, &i);
+        else if (!strcmp(a, "--gas-column-ch4")) gas_col[OCRT_GAS_CH4] = need_d(argc, argv, &i);
         else { fprintf(stderr, "error: unknown option '%s'\n", a); return usage(); }
     }
     if (!have_surface) {
@@ -283,6 +315,27 @@ int main(int argc, char **argv)
         return 2;
     }
     if (ocrt_gb_init(0) != OCRT_OK) { fprintf(stderr, "error: %s\n", ocrt_gb_last_error()); return 1; }
+    {   /* gas absorption state (main.c:3592-3613) */
+        const char *root = getenv("OCRT_GB_INPUTS");
+        char afgl_dir[1024], xsec_dir[1024];
+        snprintf(afgl_dir, sizeof afgl_dir, "%s/afgl_atm", root && *root ? root : "inputs");
+        snprintf(xsec_dir, sizeof xsec_dir, "%s/xsec", root && *root ? root : "inputs");
+        ocrt_gas *gas = NULL;
+        const int grc = ocrt_gb_gas_create(afgl_dir, xsec_dir, atm_profile, gas_col, &gas);
+        if (grc) {
+            fprintf(stderr, "error: gas absorption setup failed rc=%d: %s\n", grc, ocrt_gb_last_error());
+            return 1;
+        }
+        o.gas = gas;
+        double per[OCRT_N_GAS], tot = 0.0, eff[OCRT_N_GAS];
+        int ovr[OCRT_N_GAS];
+        ocrt_gb_gas_tau(gas, c.wavelength_nm, per, &tot);
+        ocrt_gb_gas_columns(gas, eff, NULL, ovr);
+        fprintf(stderr, "rt_absorption (SOS-integrated): \u03bb=%.1fnm \u03c4_abs_col=%.4e\n", c.wavelength_nm, tot);
+        for (int g = 0; g < OCRT_N_GAS; ++g)
+            fprintf(stderr, "  %s: column=%.3e mol/cm\u00b2%s  \u03c4_abs_col=%.4e\n", gas_names[g], eff[g],
+                    ovr[g] ? " (overridden)" : "", per[g]);
+    }
     moments_t mom = {0};
     ocrt_aerosol aer;
     memset(&aer, 0, sizeof aer);

@@ -190,7 +190,7 @@ struct Group {
     std::vector<int> hpix_task0;
     std::vector<Wave> waves;
     int Lmax = 2, Mmax = 0, max_orders = 1, nphi = 1024;
-    bool any_pssa = false, any_rough = false, any_flat = false;
+    bool any_pssa = false, any_rough = false, any_flat = false, any_gas = false;
     size_t nlev = 0, ncoef = 0, nmom = 0;
     size_t wave_fld = 0, wave_ops = 0, wave_srf = 0;
     int wave_tasks = 0;
@@ -200,6 +200,7 @@ struct Group {
     double *gmu = nullptr, *gw = nullptr;
     float *pw = nullptr;
     double *h = nullptr, *ch = nullptr, *xd = nullptr, *yd = nullptr, *z = nullptr;
+    double *tabs = nullptr;   // per-layer gas absorption depths (level-array layout), any_gas only
     float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
     double *lam = nullptr;
@@ -286,7 +287,7 @@ template <class T> int alloc(T *&dst, size_t n)
 void free_group(Group &g)
 {
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
-                    g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
+                    g.tabs, g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
                     g.err, g.F, g.J, g.ops, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
@@ -324,6 +325,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         d.nphi = o.n_phi_surface > 0 ? o.n_phi_surface : 1024;
         d.mom_off = -1; d.L_aer = -1;
         d.lay_off = -1;
+        d.gas = o.gas ? o.gas->dev : nullptr;
+        g.any_gas |= o.gas != nullptr;
         if (layers && (layers[i].dtau || layers[i].ssa)) {
             d.lay_off = (long long)std::max(ldt.size(), lss.size());
             ldt.resize(d.lay_off, 0.0); lss.resize(d.lay_off, 0.0);
@@ -436,7 +439,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.state, g.T)) || (rc = alloc(g.tout, g.T)) || (rc = alloc(g.res, g.P)) ||
         (rc = alloc(g.gmu, g.N)) || (rc = alloc(g.gw, g.N)) || (rc = alloc(g.pw, 2 * (size_t)g.N)) ||
         (rc = alloc(g.h, g.nlev)) || (rc = alloc(g.ch, g.nlev)) || (rc = alloc(g.xd, g.nlev)) ||
-        (rc = alloc(g.yd, g.nlev)) || (rc = alloc(g.z, g.nlev)) ||
+        (rc = alloc(g.yd, g.nlev)) || (rc = alloc(g.z, g.nlev)) || (rc = alloc(g.tabs, g.any_gas ? g.nlev : 1)) ||
         (rc = alloc(g.Tc, g.ncoef)) || (rc = alloc(g.Ca, g.ncoef)) || (rc = alloc(g.Cb, g.ncoef)) ||
         (rc = alloc(g.Bp, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Br, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
@@ -674,6 +677,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     LAUNCH(plan, KC_SETUP, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
     LAUNCH(plan, KC_SETUP, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
     LAUNCH(plan, KC_SETUP, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
+    if (g.any_gas)
+        LAUNCH(plan, KC_SETUP, k_gas_apply<<<P, 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z, g.tabs));
     if (g.any_layers)
         LAUNCH(plan, KC_SETUP, k_layers_apply<<<P, 256, 0, st>>>(g.px, P, g.ldt, g.lss, g.h, g.ch, g.xd, g.yd, g.err));
     LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
@@ -796,10 +801,12 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         int maxnt = 0;
         for (const PixDev &d : g.hpx) maxnt = std::max(maxnt, d.nt);
         const size_t smem = sizeof(double) * (6 * (size_t)maxnt + 6) + sizeof(int) * ((size_t)maxnt + 1);
-        LAUNCH(plan, KC_IPSS, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.kappa, g.taudir));
+        LAUNCH(plan, KC_IPSS, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd,
+                                                           g.any_gas ? g.tabs : nullptr, g.mb, g.kappa, g.taudir));
         if (g.any_lut)
             LAUNCH(plan, KC_IPSS, k_ipss_lut<<<dim3(std::min(g.lut_ptmax, 2048), P), 256, smem, st>>>(
-                       g.px, P, g.h, g.z, g.xd, g.yd, g.mb, g.lut_vza, g.lut_raa, g.lut_kappa));
+                       g.px, P, g.h, g.z, g.xd, g.yd, g.any_gas ? g.tabs : nullptr, g.mb, g.lut_vza, g.lut_raa,
+                       g.lut_kappa));
     }
     if (g.any_lut)
         LAUNCH(plan, KC_FINAL, k_lut_final<<<dim3((g.lut_ptmax + 127) / 128, P), 128, 0, st>>>(g.px, P, make_lut(g),
@@ -819,6 +826,7 @@ void ocrt_opts_default(ocrt_opts *o)
     o->n_mu = 24; o->n_layers = 40; o->fourier_m_max = 2; o->max_orders = 20; o->tolerance = 1e-7;
     o->tau_r_source = OCRT_TAU_R_AUTO; o->pssa = 0; o->view_as_node = 1; o->aer_h_km = 2.0;
     o->rayleigh_profile = OCRT_PROFILE_US62; o->rayleigh_h_km = 8.0; o->n_phi_surface = 1024;
+    o->gas = nullptr;
 }
 
 void ocrt_case_default(ocrt_case *c)
@@ -1338,8 +1346,12 @@ int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_ae
     return rc;
 }
 
-int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
-                           double *dtau, double *ssa)
+namespace {
+
+// Level grid of one case as the solve builds it, copied back: optical depths,
+// summed scattering fractions, altitudes and gas absorption depths.
+int level_profile(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer, std::vector<double> &h,
+                  std::vector<double> &w, std::vector<double> &zk, std::vector<double> &ta)
 {
     if (!cs || !opts) return fail(OCRT_ERR_ARGS, "null case or options");
     ocrt_plan *plan = nullptr;
@@ -1350,26 +1362,56 @@ int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocr
         Group &g = plan->groups[0];
         cudaStream_t st = g_stream;
         const int nt = g.hpx[0].nt;
-        std::vector<double> h(nt + 1), x(nt + 1), y(nt + 1);
+        std::vector<double> x(nt + 1), y(nt + 1);
+        h.assign(nt + 1, 0.0); zk.assign(nt + 1, 0.0); ta.assign(nt + 1, 0.0); w.assign(nt, 0.0);
         k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw, g.pw);
         k_pixel_setup<<<1, 128, 0, st>>>(g.px, 1, g.N, g.gmu);
         k_levels<<<dim3(2, 1), 256, 0, st>>>(g.px, 1, g.h, g.ch, g.xd, g.yd, g.z);
         k_level_mix<<<dim3(2, 1), 256, 0, st>>>(g.px, 1, g.z, g.xd, g.yd);
+        if (g.any_gas) k_gas_apply<<<1, 256, 0, st>>>(g.px, 1, g.h, g.ch, g.xd, g.yd, g.z, g.tabs);
+        const size_t lb = sizeof(double) * (nt + 1);
         if (cudaGetLastError() != cudaSuccess ||
-            cudaMemcpyAsync(h.data(), g.h, sizeof(double) * (nt + 1), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaMemcpyAsync(x.data(), g.xd, sizeof(double) * (nt + 1), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaMemcpyAsync(y.data(), g.yd, sizeof(double) * (nt + 1), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(h.data(), g.h, lb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(x.data(), g.xd, lb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(y.data(), g.yd, lb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(zk.data(), g.z, lb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            (g.any_gas && cudaMemcpyAsync(ta.data(), g.tabs, lb, cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
             cudaStreamSynchronize(st) != cudaSuccess) {
             rc = fail(OCRT_ERR_DEVICE, "level setup failed");
         } else {
-            for (int l = 0; l < nt; ++l) {
-                if (dtau) dtau[l] = h[l + 1] - h[l];
-                if (ssa) ssa[l] = x[l + 1] + y[l + 1];
-            }
+            for (int l = 0; l < nt; ++l) w[l] = x[l + 1] + y[l + 1];
         }
     }
     ocrt_gb_plan_destroy(plan);
     return rc;
+}
+
+}  // namespace
+
+int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                           double *dtau, double *ssa)
+{
+    std::vector<double> h, w, zk, ta;
+    const int rc = level_profile(cs, opts, aer, h, w, zk, ta);
+    if (rc) return rc;
+    for (size_t l = 0; l < w.size(); ++l) {
+        if (dtau) dtau[l] = h[l + 1] - h[l];
+        if (ssa) ssa[l] = w[l];
+    }
+    return OCRT_OK;
+}
+
+int ocrt_gb_layer_gas(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer, double *tau_abs,
+                      double *z_km)
+{
+    std::vector<double> h, w, zk, ta;
+    const int rc = level_profile(cs, opts, aer, h, w, zk, ta);
+    if (rc) return rc;
+    for (size_t l = 0; l < w.size(); ++l)
+        if (tau_abs) tau_abs[l] = ta[l];
+    for (size_t k = 0; k < zk.size(); ++k)
+        if (z_km) z_km[k] = zk[k];
+    return OCRT_OK;
 }
 
 } // extern "C"

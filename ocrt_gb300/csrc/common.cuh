@@ -26,6 +26,8 @@
 #define OCRT_DEPOL 0.0279
 #define OCRT_ZTOP_KM 100.0
 
+struct GasDev;
+
 struct PixDev {
     // ---- inputs (host) ----
     double sza_deg, vza_deg, raa_deg, wavelength_nm;
@@ -44,6 +46,7 @@ struct PixDev {
     int has_dtau, has_ssa;  // which overrides are present
     int lut_nv, lut_nr;     // angle-grid LUT size (0 = no LUT)
     long long lut_vo, lut_ro, lut_oo;   // offsets of the grid vza, grid raa and the LUT outputs
+    const GasDev *gas;      // device gas tables, nullptr = no gas absorption
     // ---- derived on device (k_pixel_setup) ----
     double mu0, mu_view, tau_r, tau_total;
     int n_ring, view_slot;  // view_slot: ring slot holding mu_view, -1 = interpolate

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda.h>
 #include "common.cuh"
+#include "gas.cuh"
 #include "../../include/ocrt_gb300.h"
 
 // setup.cu
@@ -142,8 +143,8 @@ struct LutBufs {
 __global__ void k_lut_sample(BatchBufs B, WaveBufs W, LutBufs Lb, Geom G, int t0, int nw);
 __global__ void k_lut_final(const PixDev *px, int P, LutBufs Lb, const int *pix_task0);
 __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
-                           const double *yd, const double *mb, const double *lut_vza, const double *lut_raa,
-                           double *lut_kappa);
+                           const double *yd, const double *tabs, const double *mb, const double *lut_vza,
+                           const double *lut_raa, double *lut_kappa);
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
@@ -170,7 +171,7 @@ __global__ void k_stop_check(const int *active_after_last, int *flag);
 
 // post.cu
 __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
-                       const double *xd, const double *yd,
+                       const double *xd, const double *yd, const double *tabs,
                        const double *mb, double *kappa, double *tau_dir);
 __global__ void k_finalize(const PixDev *px, int P, const TaskState *state, const TaskOut *tout,
                            const double *gmu, const double *gw, const double *h,

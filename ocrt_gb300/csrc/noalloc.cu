@@ -114,6 +114,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     d.aer_h_km = opts->aer_h_km; d.profile = opts->rayleigh_profile; d.ray_h_km = opts->rayleigh_h_km;
     d.nphi = opts->n_phi_surface > 0 ? opts->n_phi_surface : 1024;
     d.mom_off = -1; d.L_aer = -1;
+    d.gas = opts->gas ? opts->gas->dev : nullptr;
     if (aer) { d.mom_off = 0; d.L_aer = aer->L_max; d.tau_a = aer->tau_a; d.ssa_a = aer->ssa_a; }
     d.L = M > 2 ? M : 2;
     if (d.L_aer > d.L) d.L = d.L_aer;
@@ -138,6 +139,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     float *pwt = cv.take<float>(2 * (size_t)N);
     double *h = cv.take<double>(K), *ch = cv.take<double>(K), *xd = cv.take<double>(K);
     double *yd = cv.take<double>(K), *z = cv.take<double>(K);
+    double *tabs = cv.take<double>(opts->gas ? K : 1);
     float *Tc = cv.take<float>((size_t)nt * NR), *Ca = cv.take<float>((size_t)nt * NR), *Cb = cv.take<float>((size_t)nt * NR);
     const size_t nb = (size_t)T * (L + 1) * N;
     float *Bp = cv.take<float>(nb), *Br = cv.take<float>(nb), *Bt = cv.take<float>(nb);
@@ -201,6 +203,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_LAUNCH(k_pixel_setup<<<1, 32, 0, st>>>(px, 1, N, gmu));
     NA_LAUNCH(k_levels<<<dim3(2, 1), 256, 0, st>>>(px, 1, h, ch, xd, yd, z));
     NA_LAUNCH(k_level_mix<<<dim3(2, 1), 256, 0, st>>>(px, 1, z, xd, yd));
+    if (opts->gas) NA_LAUNCH(k_gas_apply<<<1, 256, 0, st>>>(px, 1, h, ch, xd, yd, z, tabs));
     NA_LAUNCH(k_coef<<<dim3(16, 1), 256, 0, st>>>(px, 1, N, gmu, h, Tc, Ca, Cb));
     NA_LAUNCH(k_basis_gauss<<<T, 64, 0, st>>>(N, M, L, gmu, Bp, Br, Bt));
     if (rough) {
@@ -252,7 +255,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     }
     if (opts->pssa) {
         const size_t smem = sizeof(double) * (6 * (size_t)nt + 6) + sizeof(int) * ((size_t)nt + 1);
-        NA_LAUNCH(k_ipss<<<1, 256, smem, st>>>(px, 1, h, z, xd, yd, mb, kappa, taudir));
+        NA_LAUNCH(k_ipss<<<1, 256, smem, st>>>(px, 1, h, z, xd, yd, opts->gas ? tabs : nullptr, mb, kappa,
+                                               taudir));
     }
     NA_LAUNCH(k_finalize<<<1, 32, 0, st>>>(px, 1, state, tout, gmu, gw, h, kappa, taudir, res));
     int dev_err = 0;

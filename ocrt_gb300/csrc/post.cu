@@ -57,7 +57,8 @@ __device__ double ipss_tau_sun(const double *he, const double *beta, int nl, dou
 // block; thread 0 writes *kappa and, when tau_dir is non-null, the direct-beam
 // slant depth to the surface.
 __device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, const double *h, const double *z,
-                           const double *xd, const double *yd, const double *mb, double *kappa, double *tau_dir)
+                           const double *xd, const double *yd, const double *tabs, const double *mb, double *kappa,
+                           double *tau_dir)
 {
     extern __shared__ double sm[];
     const int nl = d.nt;
@@ -104,6 +105,11 @@ __device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, cons
             const double wr = yd[lo + k + 1] > 0.0 ? yd[lo + k + 1] : 0.0;
             const double wa = xd[lo + k + 1] > 0.0 ? xd[lo + k + 1] : 0.0;
             wsrc[j] = wr * PR + wa * PA;
+        } else if (tabs && d.gas) {
+            // the layer's scattering fraction of its extinction (rt_ipss.c:64-70)
+            const double dtau = h[lo + k + 1] - h[lo + k];
+            const double ta = fmin(fmax(tabs[lo + k], 0.0), dtau);
+            wsrc[j] = dtau > 0.0 ? (dtau - ta) / dtau : 0.0;
         } else {
             wsrc[j] = beta[j] > 0.0 ? 1.0 : 0.0;
         }
@@ -184,7 +190,7 @@ __device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, cons
 }
 
 __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
-                       const double *xd, const double *yd,
+                       const double *xd, const double *yd, const double *tabs,
                        const double *mb, double *kappa, double *tau_dir)
 {
     const int p = blockIdx.x;
@@ -194,13 +200,13 @@ __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z
         if (threadIdx.x == 0) { kappa[p] = 1.0; tau_dir[p] = -1.0; }
         return;
     }
-    ipss_block(d, d.vza_deg, d.raa_deg, h, z, xd, yd, mb, &kappa[p], &tau_dir[p]);
+    ipss_block(d, d.vza_deg, d.raa_deg, h, z, xd, yd, tabs, mb, &kappa[p], &tau_dir[p]);
 }
 
 // IPSS kappa at every (vza, raa) of each pixel's LUT grid: block (point, pixel).
 __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
-                           const double *yd, const double *mb, const double *lut_vza, const double *lut_raa,
-                           double *lut_kappa)
+                           const double *yd, const double *tabs, const double *mb, const double *lut_vza,
+                           const double *lut_raa, double *lut_kappa)
 {
     const int p = blockIdx.y;
     if (p >= P) return;
@@ -213,7 +219,7 @@ __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const doubl
             continue;
         }
         const int iv = pt / d.lut_nr, ir = pt - iv * d.lut_nr;
-        ipss_block(d, lut_vza[d.lut_vo + iv], lut_raa[d.lut_ro + ir], h, z, xd, yd, mb, kout, nullptr);
+        ipss_block(d, lut_vza[d.lut_vo + iv], lut_raa[d.lut_ro + ir], h, z, xd, yd, tabs, mb, kout, nullptr);
         __syncthreads();
     }
 }

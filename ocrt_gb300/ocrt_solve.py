@@ -7,22 +7,35 @@ The reference computes three reflectances per row (ocrt_solve.py:5-10):
   R2 rho_R        Rayleigh atmosphere over a black Fresnel ocean surface, glint decoupled
   R3 rho_RA_black Rayleigh + aerosol over a black Fresnel ocean surface, glint decoupled
 R2 and R3 are on this path.  R1 needs the coupled in-water solve, which is
-not, and raises.  Gas absorption layering (gas_on) is not on this path
-either: pass gas_on=False.  The reference's aerosol comes from FR631 `.mie`
+not, and raises.  gas_on (default True, as in the reference) loads the AFGL
+US76 atmosphere and the six cross-section tables once (ocrt_solve.py:41-45)
+from $OCRT_GB_INPUTS/afgl_atm and $OCRT_GB_INPUTS/xsec, or inputs/afgl_atm and
+inputs/xsec under the working directory, and folds the per-layer absorption
+into every solve.  The reference's aerosol comes from FR631 `.mie`
 models named by aer_name; here aer_name is a synthetic expansion spec
 "HG:g,ssa[,L]" (Henyey-Greenstein beta_l = (2l+1) g^l with the Rayleigh-form
 gamma_2/alpha_2 x 0.3) and aod865 is the AOD at the row's wavelength.
 """
 import argparse
 import csv
+import os
 import sys
 
 import numpy as np
 
 from . import _abi as A
-from . import solve_batch
+from . import GasState, solve_batch
 
 DEPOL = 0.0279
+_STATE = {}
+
+
+def _absorption():
+    """The gas state, made once per process (the reference's lazy singleton)."""
+    if "ab" not in _STATE:
+        root = os.environ.get("OCRT_GB_INPUTS") or "inputs"
+        _STATE["ab"] = GasState(os.path.join(root, "afgl_atm"), os.path.join(root, "xsec"), "usstd76")
+    return _STATE["ab"]
 
 
 def _hg(spec, aod):
@@ -40,19 +53,21 @@ def _hg(spec, aod):
     return A.AerosolHolder(aod, ssa, beta, gamma, alpha, zeta)
 
 
-def _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa, max_it=100):
+def _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa, max_it=100, gas=None):
     """Cases of the R2 / R3 solves of every row (ocrt_solve.py:160-177)."""
     out = []
+    g = gas.handle if gas is not None else None
     for r in rows:
         base = dict(sza_deg=r["sza"], vza_deg=r["vza"], raa_deg=r["raa"], wavelength_nm=r["wl_nm"],
                     wind_speed=r["wind"], surface="black_fresnel_ocean", pressure_hpa=pressure_hpa,
                     decouple_sunglint=1)
         if "R2" in which:
             out.append(("R2", r, A.default_case(**base),
-                        A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=2, max_orders=max_it), None))
+                        A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=2, max_orders=max_it, gas=g), None))
         if "R3" in which:
             out.append(("R3", r, A.default_case(**base),
-                        A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=fourier_m_max, max_orders=max_it),
+                        A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=fourier_m_max, max_orders=max_it,
+                                       gas=g),
                         _hg(r["aer_name"], r["aod865"])))
     return out
 
@@ -61,9 +76,7 @@ def _solve_rows(rows, which, fourier_m_max, nt_atm, pressure_hpa, gas_on):
     which = tuple(which)
     if "R1" in which:
         raise NotImplementedError("R1 (coupled atmosphere-ocean, rho_TOA) is not on the GB300 solve path")
-    if gas_on:
-        raise NotImplementedError("gas absorption layering is not on the GB300 solve path; pass gas_on=False")
-    jobs = _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa)
+    jobs = _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa, gas=_absorption() if gas_on else None)
     outs = [dict(wavelength_nm=r["wl_nm"], sza=r["sza"], vza=r["vza"], raa=r["raa"], wind=r["wind"],
                  aod865=r["aod865"], aer_model=r["aer_name"], aod_band=r["aod865"]) for r in rows]
     index = {id(r): i for i, r in enumerate(rows)}

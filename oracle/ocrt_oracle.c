@@ -211,11 +211,12 @@ typedef struct {
     int nt;
     double tau_total;
     double *h, *ch, *xdel, *ydel, *z;
+    double *tabs;                     /* [nt] gas absorption per layer, NULL without gas */
 } medium_t;
 
 static void medium_free(medium_t *md)
 {
-    free(md->h); free(md->ch); free(md->xdel); free(md->ydel); free(md->z);
+    free(md->h); free(md->ch); free(md->xdel); free(md->ydel); free(md->z); free(md->tabs);
     memset(md, 0, sizeof(*md));
 }
 
@@ -270,6 +271,361 @@ static int medium_build(medium_t *md, int nt, double tau_r, double tau_a,
         else { md->xdel[j] = 0.0; md->ydel[j] = tau_r > 0.0 ? 1.0 : 0.0; }
         z_prev = zj; ray_prev = ray_j; aer_prev = aer_j;
     }
+    return 0;
+}
+
+/* ======================================================================
+ * Trace-gas absorption (rt_absorption.c, rt_atm.c:437-548).  AFGL level
+ * profiles give per-gas number densities; layered cross-section tables
+ * sigma(AFGL level, wavelength) are interpolated linearly in altitude and
+ * wavelength; columns are trapezoids on the AFGL grid.  The per-layer
+ * absorption depth of every solver layer is added to h[] and the scattering
+ * fractions are rescaled by dtau_old / dtau_new.
+ * ==================================================================== */
+#define NGAS 6
+static const char *const GAS_NAMES[NGAS] = {"h2o", "o3", "o2", "co2", "no2", "ch4"};   /* rt_absorption.c:38 */
+static const char *const AFGL_NAMES[7] = {"usstd76", "tropical", "mlsumm", "mlwint",
+                                          "sasumm", "sawint", "userdef"};             /* :40-42 */
+
+typedef struct {
+    int avail, nwl, nlay;
+    double *wl, *sig;                 /* sig[layer * nwl + i] */
+} xsec_t;
+
+struct ocrt_gas {
+    int nlev;
+    double *z, *ntot, *mr[NGAS];
+    double col_default[NGAS], col_eff[NGAS];
+    int overridden[NGAS];
+    xsec_t xs[NGAS];
+};
+
+/* Whole file as a NUL-terminated buffer; NULL if it cannot be read. */
+static char *slurp(const char *path)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f) return NULL;
+    size_t cap = 1 << 16, len = 0;
+    char *b = malloc(cap);
+    while (b) {
+        if (len + 4096 + 1 > cap) { char *nb = realloc(b, cap *= 2); if (!nb) { free(b); b = NULL; break; } b = nb; }
+        const size_t r = fread(b + len, 1, 4096, f);
+        len += r;
+        if (r == 0) break;
+    }
+    fclose(f);
+    if (b) b[len] = 0;
+    return b;
+}
+
+/* Next line of a buffer, NUL-terminated in place; NULL at the end. */
+static char *next_line(char **cur)
+{
+    char *s = *cur;
+    if (!s || !*s) return NULL;
+    char *e = strchr(s, '\n');
+    if (e) { *e = 0; *cur = e + 1; } else *cur = s + strlen(s);
+    return s;
+}
+
+/* Data lines skip '#' comments and empty lines (rt_absorption.c:68-72). */
+static int is_skip(const char *l) { return l[0] == '#' || l[0] == 0 || l[0] == '\r'; }
+
+/* AFGL loader (rt_afgl_load, rt_absorption.c:48-175): z P T n_total and six
+ * mixing ratios (ppmv) per level, default columns by trapezoids (:160-172). */
+static int afgl_load(struct ocrt_gas *g, const char *dir, int profile)
+{
+    char path[1024];
+    snprintf(path, sizeof(path), "%s/afgl_%s.dat", dir, AFGL_NAMES[profile]);
+    char *buf = slurp(path);
+    if (!buf) return -2;
+    int cap = 64, n = 0;
+    double *rows = malloc(sizeof(double) * 10 * cap);
+    char *cur = buf, *l;
+    int bad = 0;
+    while (rows && (l = next_line(&cur))) {
+        if (is_skip(l)) continue;
+        double v[10];
+        if (sscanf(l, "%lf %lf %lf %lf %lf %lf %lf %lf %lf %lf", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5],
+                   &v[6], &v[7], &v[8], &v[9]) != 10) {
+            /* blank-looking lines are skipped; any other malformed row is an error */
+            const char *q = l;
+            while (*q == ' ' || *q == '\t' || *q == '\r') ++q;
+            if (*q) bad = 1;
+            continue;
+        }
+        if (n == cap) { double *nr = realloc(rows, sizeof(double) * 10 * (cap *= 2)); if (!nr) { free(rows); rows = NULL; break; } rows = nr; }
+        memcpy(rows + 10 * n, v, sizeof(v));
+        ++n;
+    }
+    free(buf);
+    if (!rows) return -3;
+    if (bad || n < 2) { free(rows); return -1; }
+    g->nlev = n;
+    g->z = malloc(sizeof(double) * n);
+    g->ntot = malloc(sizeof(double) * n);
+    for (int k = 0; k < NGAS; ++k) g->mr[k] = malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) {
+        g->z[i] = rows[10 * i];
+        g->ntot[i] = rows[10 * i + 3];
+        for (int k = 0; k < NGAS; ++k) g->mr[k][i] = rows[10 * i + 4 + k];
+    }
+    free(rows);
+    for (int k = 0; k < NGAS; ++k) {
+        double col = 0.0;
+        for (int i = 0; i + 1 < n; ++i) {
+            const double n1 = g->mr[k][i] * 1e-6 * g->ntot[i];
+            const double n2 = g->mr[k][i + 1] * 1e-6 * g->ntot[i + 1];
+            col += 0.5 * (n1 + n2) * ((g->z[i + 1] - g->z[i]) * 1.0e5);
+        }
+        g->col_default[k] = col;
+    }
+    return 0;
+}
+
+/* Cross-section table (rt_xsec_load, rt_absorption.c:192-333).  Header tag
+ * "n_layers" selects the layered form: a wavelength row, then one sigma row
+ * per AFGL level; otherwise rows of (wavelength, sigma).  The grid must be
+ * increasing and cover 330-1100 nm (rt_spectral_contract.h); a table that
+ * fails to load leaves the gas out. */
+static void xsec_load(xsec_t *x, const char *dir, int gas)
+{
+    memset(x, 0, sizeof(*x));
+    char path[1024];
+    snprintf(path, sizeof(path), "%s/xsec_%s.dat", dir, GAS_NAMES[gas]);
+    char *buf = slurp(path);
+    if (!buf) return;
+    int nlay = 1;
+    char *cur = buf, *l;
+    while ((l = next_line(&cur))) {
+        if (l[0] != '#') continue;
+        const char *p = strstr(l, "n_layers");
+        if (p) { sscanf(p, "n_layers = %d", &nlay); if (nlay < 1) nlay = 1; }
+    }
+    for (char *q = buf; q < cur; ++q) if (*q == 0) *q = '\n';   /* restore the lines */
+    cur = buf;
+    int ok = 1;
+    if (nlay == 1) {
+        int cap = 1024, n = 0;
+        x->wl = malloc(sizeof(double) * cap);
+        x->sig = malloc(sizeof(double) * cap);
+        while ((l = next_line(&cur))) {
+            if (is_skip(l)) continue;
+            double a, b;
+            if (sscanf(l, "%lf %lf", &a, &b) != 2) continue;
+            if (n == cap) { cap *= 2; x->wl = realloc(x->wl, sizeof(double) * cap); x->sig = realloc(x->sig, sizeof(double) * cap); }
+            x->wl[n] = a; x->sig[n] = b; ++n;
+        }
+        x->nwl = n; x->nlay = 1;
+    } else {
+        int row = -1;
+        while ((l = next_line(&cur))) {
+            if (is_skip(l)) continue;
+            if (row < 0) {
+                int cnt = 0;
+                for (char *p = l, *e; ; p = e) { strtod(p, &e); if (e == p) break; ++cnt; }
+                if (cnt < 2) { ok = 0; break; }
+                x->nwl = cnt; x->nlay = nlay;
+                x->wl = malloc(sizeof(double) * cnt);
+                x->sig = calloc((size_t)cnt * nlay, sizeof(double));
+                char *p = l, *e;
+                for (int i = 0; i < cnt; ++i, p = e) x->wl[i] = strtod(p, &e);
+                row = 0;
+            } else if (row < nlay) {
+                char *p = l, *e;
+                for (int i = 0; i < x->nwl; ++i, p = e) {
+                    const double v = strtod(p, &e);
+                    if (e == p) break;
+                    x->sig[(size_t)row * x->nwl + i] = v;
+                }
+                ++row;
+            }
+        }
+        if (row < 0) ok = 0;
+    }
+    free(buf);
+    if (ok && x->nwl >= 2) {
+        for (int i = 0; i < x->nwl; ++i)
+            if (!isfinite(x->wl[i]) || (i > 0 && !(x->wl[i] > x->wl[i - 1]))) ok = 0;
+        if (ok && !(x->wl[0] <= 330.0 + 1e-9 && x->wl[x->nwl - 1] >= 1100.0 - 1e-9)) ok = 0;
+    } else ok = 0;
+    if (!ok) { free(x->wl); free(x->sig); memset(x, 0, sizeof(*x)); return; }
+    x->avail = 1;
+}
+
+static void gas_free(struct ocrt_gas *g)
+{
+    if (!g) return;
+    free(g->z); free(g->ntot);
+    for (int k = 0; k < NGAS; ++k) { free(g->mr[k]); free(g->xs[k].wl); free(g->xs[k].sig); }
+    free(g);
+}
+
+/* rt_absorption_init (rt_absorption.c:486-533). */
+int ocrt_oracle_gas_create(const char *afgl_dir, const char *xsec_dir, int profile,
+                           const double *override, ocrt_gas **out)
+{
+    if (!afgl_dir || !xsec_dir || !out || profile < 0 || profile > 6) return -1;
+    *out = NULL;
+    struct ocrt_gas *g = calloc(1, sizeof(*g));
+    if (!g) return -3;
+    int rc = afgl_load(g, afgl_dir, profile);
+    if (rc) { gas_free(g); return rc == -3 ? -3 : -1; }
+    for (int k = 0; k < NGAS; ++k) {
+        xsec_load(&g->xs[k], xsec_dir, k);
+        /* the reference reads the altitude of table level i from AFGL level i */
+        if (g->xs[k].avail && g->xs[k].nlay > g->nlev) { gas_free(g); return -1; }
+        if (override && override[k] >= 0.0) { g->col_eff[k] = override[k]; g->overridden[k] = 1; }
+        else g->col_eff[k] = g->col_default[k];
+    }
+    *out = g;
+    return 0;
+}
+
+void ocrt_oracle_gas_destroy(ocrt_gas *g) { gas_free(g); }
+
+/* sigma at (table level, wavelength) (rt_xsec_interp_layer, rt_absorption.c:347-371). */
+static double xsec_at(const xsec_t *x, int layer, double wl)
+{
+    if (!x->avail || x->nwl < 2) return 0.0;
+    if (layer < 0) layer = 0;
+    if (layer >= x->nlay) layer = x->nlay - 1;
+    const double *s = x->sig + (size_t)layer * x->nwl;
+    const int n = x->nwl;
+    if (wl < x->wl[0] || wl > x->wl[n - 1]) return NAN;
+    if (wl == x->wl[0]) return s[0];
+    if (wl == x->wl[n - 1]) return s[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) { const int mid = (lo + hi) / 2; if (x->wl[mid] <= wl) lo = mid; else hi = mid; }
+    const double t = (wl - x->wl[lo]) / (x->wl[hi] - x->wl[lo]);
+    return (1.0 - t) * s[lo] + t * s[hi];
+}
+
+/* sigma at (altitude, wavelength), linear between bracketing AFGL levels
+ * (rt_xsec_interp_layer_z, rt_absorption.c:378-412). */
+static double xsec_at_z(const xsec_t *x, const double *zg, double z, double wl)
+{
+    if (!x->avail) return 0.0;
+    const int nl = x->nlay;
+    if (nl == 1) return xsec_at(x, 0, wl);
+    if (z <= zg[0]) return xsec_at(x, 0, wl);
+    if (z >= zg[nl - 1]) return xsec_at(x, nl - 1, wl);
+    int lo = 0, hi = nl - 1;
+    while (hi - lo > 1) { const int mid = (lo + hi) / 2; if (zg[mid] <= z) lo = mid; else hi = mid; }
+    const double dz = zg[hi] - zg[lo];
+    if (dz <= 0.0) return xsec_at(x, lo, wl);
+    const double t = (z - zg[lo]) / dz;
+    return (1.0 - t) * xsec_at(x, lo, wl) + t * xsec_at(x, hi, wl);
+}
+
+/* Column above z (molecules/cm^2), trapezoids with the cut layer
+ * interpolated (rt_afgl_cumulative_column, rt_absorption.c:425-453). */
+static double col_above(const struct ocrt_gas *g, int k, double z)
+{
+    double cum = 0.0;
+    for (int i = 0; i + 1 < g->nlev; ++i) {
+        const double z1 = g->z[i], z2 = g->z[i + 1];
+        if (z2 <= z) continue;
+        const double a = z1 < z ? z : z1, b = z2;
+        if (b <= a) continue;
+        const double f1 = (a - z1) / (z2 - z1), f2 = (b - z1) / (z2 - z1);
+        const double n1 = g->mr[k][i] * 1e-6 * g->ntot[i];
+        const double n2 = g->mr[k][i + 1] * 1e-6 * g->ntot[i + 1];
+        const double nlo = (1.0 - f1) * n1 + f1 * n2, nhi = (1.0 - f2) * n1 + f2 * n2;
+        cum += 0.5 * (nlo + nhi) * ((b - a) * 1.0e5);
+    }
+    return cum;
+}
+
+/* Column in [z_lo, z_hi] (rt_afgl_layer_column, rt_absorption.c:455-461). */
+static double col_layer(const struct ocrt_gas *g, int k, double zlo, double zhi)
+{
+    if (zhi <= zlo) return 0.0;
+    return col_above(g, k, zlo) - col_above(g, k, zhi);
+}
+
+/* Column absorption depth of one gas (rt_absorption_tau_per_gas, :556-590). */
+static double gas_tau_one(const struct ocrt_gas *g, int k, double wl)
+{
+    const xsec_t *x = &g->xs[k];
+    if (!x->avail || g->nlev < 2) return 0.0;
+    const double ndef = g->col_default[k];
+    const int ov = g->overridden[k] && ndef > 0.0;
+    const double scale = ov ? g->col_eff[k] / ndef : 1.0;
+    double tau = 0.0;
+    for (int i = 0; i + 1 < g->nlev; ++i) {
+        const double zlo = g->z[i], zhi = g->z[i + 1];
+        const double sig = xsec_at_z(x, g->z, 0.5 * (zlo + zhi), wl);
+        double nl = col_layer(g, k, zlo, zhi);
+        if (ov) nl *= scale;
+        tau += sig * nl;
+    }
+    return tau;
+}
+
+int ocrt_oracle_gas_tau(const ocrt_gas *g, double wl, double *per_gas, double *total)
+{
+    if (!g) return -1;
+    double t = 0.0;
+    for (int k = 0; k < NGAS; ++k) {
+        const double v = gas_tau_one(g, k, wl);
+        if (per_gas) per_gas[k] = v;
+        t += v;
+    }
+    if (total) *total = t;
+    return 0;
+}
+
+int ocrt_oracle_gas_columns(const ocrt_gas *g, double *eff, double *def, int *ov)
+{
+    if (!g) return -1;
+    for (int k = 0; k < NGAS; ++k) {
+        if (eff) eff[k] = g->col_eff[k];
+        if (def) def[k] = g->col_default[k];
+        if (ov) ov[k] = g->overridden[k];
+    }
+    return 0;
+}
+
+/* Fold the gas into the medium (rt_atm_apply_gas_absorption, rt_atm.c:437-548). */
+static int medium_apply_gas(medium_t *md, const struct ocrt_gas *g, double wl, double mu0)
+{
+    const int nt = md->nt;
+    if (!(mu0 > 0.0)) return -1;
+    md->tabs = calloc(nt, sizeof(double));
+    double *hold = malloc(sizeof(double) * (nt + 1));
+    if (!md->tabs || !hold) { free(hold); return -3; }
+    for (int k = 0; k < nt; ++k) {
+        double zhi = md->z[k], zlo = md->z[k + 1];
+        if (zlo > zhi) { const double t = zlo; zlo = zhi; zhi = t; }
+        const double zmid = 0.5 * (zlo + zhi);
+        double dt = 0.0;
+        for (int q = 0; q < NGAS; ++q) {
+            double N;
+            if (g->overridden[q]) {
+                const double ndef = g->col_default[q];
+                N = ndef > 0.0 ? g->col_eff[q] * (col_layer(g, q, zlo, zhi) / ndef) : 0.0;
+            } else N = col_layer(g, q, zlo, zhi);
+            dt += xsec_at_z(&g->xs[q], g->z, zmid, wl) * N;
+        }
+        md->tabs[k] = dt;
+    }
+    for (int k = 0; k <= nt; ++k) hold[k] = md->h[k];
+    double cum = 0.0;
+    for (int k = 0; k <= nt; ++k) {
+        md->h[k] = hold[k] + cum;
+        md->ch[k] = 0.5 * exp(-md->h[k] / mu0);
+        if (k < nt) cum += md->tabs[k];
+    }
+    for (int k = 1; k <= nt; ++k) {
+        const double dold = hold[k] - hold[k - 1], dnew = dold + md->tabs[k - 1];
+        if (dnew > 0.0 && dold > 0.0) {
+            md->xdel[k] = md->xdel[k] * dold / dnew;
+            md->ydel[k] = md->ydel[k] * dold / dnew;
+        }
+    }
+    md->tau_total = md->h[nt];
+    free(hold);
     return 0;
 }
 
@@ -820,7 +1176,12 @@ static int ipss_init(ipss_t *g, const medium_t *md, double mu0, const ocrt_aeros
         g->wray[j] = md->ydel[k + 1] > 0.0 ? md->ydel[k + 1] : 0.0;
         g->waer[j] = md->xdel[k + 1] > 0.0 ? md->xdel[k + 1] : 0.0;
         if (md->xdel[k + 1] > 0.0) have_aer = 1;
-        g->wsrc[j] = 1.0;                  /* phase-free omega (no gas absorption) */
+        /* phase-free source weight: the layer's scattering fraction of its
+         * extinction, 1 without gas (rt_ipss.c:64-70) */
+        double ta = md->tabs ? md->tabs[k] : 0.0;
+        if (ta < 0.0) ta = 0.0;
+        if (ta > dtau) ta = dtau;
+        g->wsrc[j] = dtau > 0.0 ? (dtau - ta) / dtau : 0.0;
     }
     g->aer = (have_aer && aer) ? aer : NULL;
     g->above[nt] = 0.0;
@@ -1286,6 +1647,7 @@ static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
         rc = medium_build(&c->md, nt, tau_r, 0.0, 1.0, c->mu0, op->aer_h_km,
                           op->rayleigh_profile, op->rayleigh_h_km);
     }
+    if (!rc && op->gas) rc = medium_apply_gas(&c->md, op->gas, cs->wavelength_nm, c->mu0);
     if (!rc && layers) rc = apply_layers(&c->md, layers, c->mu0);
     if (rc) { medium_free(&c->md); free(c); return rc; }
     if ((rc = transport_prepare(c))) goto done;
@@ -1587,11 +1949,39 @@ int ocrt_oracle_layer_defaults(const ocrt_case *cs, const ocrt_opts *op, const o
     const double mu0 = cos(cs->sza_deg * PI / 180.0);
     rc = medium_build(&md, op->n_layers, tau_r, aer ? aer->tau_a : 0.0, aer ? aer->ssa_a : 1.0, mu0,
                       op->aer_h_km, op->rayleigh_profile, op->rayleigh_h_km);
-    if (rc) return rc;
+    if (!rc && op->gas) rc = medium_apply_gas(&md, op->gas, cs->wavelength_nm, mu0);
+    if (rc) { medium_free(&md); return rc; }
     for (int l = 0; l < op->n_layers; ++l) {
         if (dtau) dtau[l] = md.h[l + 1] - md.h[l];
         if (ssa) ssa[l] = md.xdel[l + 1] + md.ydel[l + 1];
     }
+    medium_free(&md);
+    return 0;
+}
+
+/* Per-layer gas absorption depths and level altitudes of one case
+ * (atm->tau_abs_layer and atm->z_km_level after rt_atm_apply_gas_absorption). */
+int ocrt_oracle_layer_gas(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,
+                          double *tau_abs, double *z_km)
+{
+    int rc = check_args(cs, op, aer_in);
+    if (rc) return rc;
+    const ocrt_aerosol *aer = (aer_in && aer_in->tau_a > 0.0) ? aer_in : NULL;
+    double tau_r;
+    if (!(cs->pressure_hpa > 0.0)) tau_r = 0.0;
+    else if (op->tau_r_source == OCRT_TAU_R_FROM_INPUT) tau_r = cs->tau_r_input;
+    else tau_r = ocrt_oracle_tau_rayleigh(cs->wavelength_nm, cs->pressure_hpa);
+    if (!aer && !(tau_r > 0.0)) return -1;
+    medium_t md;
+    const double mu0 = cos(cs->sza_deg * PI / 180.0);
+    rc = medium_build(&md, op->n_layers, tau_r, aer ? aer->tau_a : 0.0, aer ? aer->ssa_a : 1.0, mu0,
+                      op->aer_h_km, op->rayleigh_profile, op->rayleigh_h_km);
+    if (!rc && op->gas) rc = medium_apply_gas(&md, op->gas, cs->wavelength_nm, mu0);
+    if (rc) { medium_free(&md); return rc; }
+    for (int l = 0; l < op->n_layers; ++l)
+        if (tau_abs) tau_abs[l] = md.tabs ? md.tabs[l] : 0.0;
+    for (int k = 0; k <= op->n_layers; ++k)
+        if (z_km) z_km[k] = md.z[k];
     medium_free(&md);
     return 0;
 }

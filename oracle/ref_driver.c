@@ -25,6 +25,7 @@
 #include "rt_ipss.h"
 #include "rt_raa_convention.h"
 #include "shared/surface.h"
+#include "rt_absorption.h"
 #include "../include/ocrt_gb300.h"
 
 #define OCRT_PI_ 3.14159265358979323846
@@ -55,6 +56,54 @@ static void fill(const ocrt_case *c, const ocrt_opts *o, rt_case_t *cs, rt_optio
     op->sos.max_iterations = o->max_orders; op->sos.tolerance = o->tolerance;
     op->tau_r_source = (rt_tau_r_source_t)o->tau_r_source;
     op->pssa = o->pssa; op->view_as_node = o->view_as_node; op->aer_h_km = o->aer_h_km;
+    /* for this driver ocrt_opts.gas holds the reference's own rt_absorption_t */
+    op->abs_state = (const void *)o->gas;
+}
+
+/* Gas absorption state made by the reference's rt_absorption_init
+ * (rt_absorption.c:486); the handle is an rt_absorption_t. */
+int ocrt_ref_gas_create(const char *afgl_dir, const char *xsec_dir, int profile,
+                        const double *override, ocrt_gas **out)
+{
+    if (!out) return -1;
+    *out = NULL;
+    rt_absorption_t *st = calloc(1, sizeof(*st));
+    if (!st) return -3;
+    double ov[RT_N_GAS];
+    for (int g = 0; g < RT_N_GAS; ++g) ov[g] = override ? override[g] : -1.0;
+    const int rc = rt_absorption_init(afgl_dir, xsec_dir, (rt_afgl_profile_t)profile, ov, st);
+    if (rc < 0 || rc > 0) { rt_absorption_free(st); free(st); return rc ? rc : -1; }
+    *out = (ocrt_gas *)st;
+    return 0;
+}
+
+void ocrt_ref_gas_destroy(ocrt_gas *g)
+{
+    if (!g) return;
+    rt_absorption_free((rt_absorption_t *)g);
+    free(g);
+}
+
+int ocrt_ref_gas_tau(const ocrt_gas *g, double wl, double *per_gas, double *total)
+{
+    if (!g) return -1;
+    const rt_absorption_t *st = (const rt_absorption_t *)g;
+    for (int k = 0; k < RT_N_GAS; ++k)
+        if (per_gas) per_gas[k] = rt_absorption_tau_per_gas(st, k, wl);
+    if (total) *total = rt_absorption_tau_total(st, wl);
+    return 0;
+}
+
+int ocrt_ref_gas_columns(const ocrt_gas *g, double *eff, double *def, int *ov)
+{
+    if (!g) return -1;
+    const rt_absorption_t *st = (const rt_absorption_t *)g;
+    for (int k = 0; k < RT_N_GAS; ++k) {
+        if (eff) eff[k] = st->column_eff[k];
+        if (def) def[k] = st->atm.column_default[k];
+        if (ov) ov[k] = st->column_overridden[k];
+    }
+    return 0;
 }
 
 int ocrt_ref_solve_case(const ocrt_case *c, const ocrt_opts *o, const ocrt_aerosol *a,

@@ -34,6 +34,51 @@ class Oracle:
             C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol), C.POINTER(C.c_double),
             C.POINTER(C.c_double)]
 
+        L = self.lib
+        L.ocrt_oracle_gas_create.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_double),
+                                             C.POINTER(C.c_void_p)]
+        L.ocrt_oracle_gas_destroy.argtypes = [C.c_void_p]
+        L.ocrt_oracle_gas_destroy.restype = None
+        L.ocrt_oracle_gas_tau.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.ocrt_oracle_gas_columns.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.POINTER(C.c_int)]
+        L.ocrt_oracle_layer_gas.argtypes = [C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double)]
+
+    def gas_create(self, root, profile, override=None):
+        """Oracle gas state on <root>/afgl_atm and <root>/xsec; returns the handle."""
+        h = C.c_void_p()
+        ov = (C.c_double * 6)(*override) if override is not None else None
+        rc = self.lib.ocrt_oracle_gas_create(os.path.join(root, "afgl_atm").encode(),
+                                             os.path.join(root, "xsec").encode(), profile, ov, C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"oracle gas rc {rc}")
+        return h.value
+
+    def gas_destroy(self, h):
+        self.lib.ocrt_oracle_gas_destroy(h)
+
+    def gas_tau(self, h, wl):
+        per, tot = (C.c_double * 6)(), C.c_double()
+        self.lib.ocrt_oracle_gas_tau(h, wl, per, C.byref(tot))
+        return np.array(per[:]), tot.value
+
+    def gas_columns(self, h):
+        e, d, o = (C.c_double * 6)(), (C.c_double * 6)(), (C.c_int * 6)()
+        self.lib.ocrt_oracle_gas_columns(h, e, d, o)
+        return np.array(e[:]), np.array(d[:]), np.array(o[:])
+
+    def layer_gas(self, case, opts, aer=None):
+        n = opts.n_layers
+        ta, z = np.zeros(n), np.zeros(n + 1)
+        a = aer.struct if isinstance(aer, A.AerosolHolder) else aer
+        rc = self.lib.ocrt_oracle_layer_gas(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
+                                            ta.ctypes.data_as(C.POINTER(C.c_double)),
+                                            z.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != 0:
+            raise RuntimeError(f"oracle rc {rc}")
+        return ta, z
+
     def layer_defaults(self, case, opts, aer=None):
         n = opts.n_layers
         dt, ss = np.zeros(n), np.zeros(n)
@@ -75,6 +120,24 @@ class Oracle:
         if diag:
             out.update({k: np.array(v[:]) for k, v in arr.items()})
         return out
+
+
+GAS_DATA = os.path.join(HERE, "golden", "gas_data")
+GAS_PROFILES = {"usstd76": 0, "tropical": 1, "mlwint": 3}
+
+
+def load_gas_golden():
+    with open(os.path.join(HERE, "golden", "reference_gas.json")) as fh:
+        return json.load(fh)
+
+
+def gas_solve_inputs(spec):
+    """(case, opts, aerosol holder or None) of one gas fixture solve; opts.gas unset."""
+    c = A.default_case(**spec["case"])
+    o = A.default_opts(**spec["opts"])
+    af = spec["aerosol"]
+    aer = A.AerosolHolder(af["tau_a"], af["ssa_a"], *hg_aerosol_moments(af["g"], af["L"])) if af else None
+    return c, o, aer
 
 
 def load_golden():
