@@ -210,6 +210,7 @@ struct Group {
     int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
     float *F = nullptr, *J = nullptr, *ops = nullptr;
+    float *opt = nullptr;    // pre-split operator tiles of the tensor-core pass (2 x wave_ops floats)
     float *molV = nullptr;   // [3][32][CIN] molecular input factors V_m of the tensor-core pass
     short2 *cmpairs = nullptr;   // (outgoing, incoming) slot pairs of the tensor-core Cox-Munk kernel
     float *cstiles = nullptr;    // its cos/sin B tiles, split and swizzled
@@ -289,7 +290,7 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.tabs, g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
@@ -387,6 +388,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     // ---- waves of whole pixels under the workspace budget ----
     const size_t budget = wave_budget_bytes();
     const size_t op_elems = (size_t)G.NP * G.CIN;
+    const bool tiles = tc_supported(G) && !force_simt();
     Wave w{0, 0, 0, 0, 0, 0, 0, 0, false, false};
     size_t bytes = 0;
     auto close = [&](int pend) {
@@ -403,7 +405,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t pf = nm * K * G.LDC;
         const size_t po = (nm + 2 * std::min<size_t>(nm, 3)) * op_elems;
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
-        size_t pb = pf * 16 + po * 4 + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        size_t pb = pf * 16 + po * (tiles ? 12 : 4) + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 12 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)G.CIN * ((G.COUT + 31) & ~31) * 4;
@@ -486,6 +488,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     // otherwise.  The per-order task lists themselves are built on the device
     // (k_primary, k_scan). ----
     g.use_tc = tc_supported(G) && !force_simt();
+    if (g.use_tc && (rc = alloc(g.opt, 2 * g.wave_ops))) return rc;
     if (g.use_tc && (rc = alloc(g.molV, (size_t)3 * 32 * G.CIN))) return rc;
     // Cox-Munk pairs for the tensor-core projection: ring slots o < NR, incoming
     // Gauss slots and the sun (i = N); Gauss pairs with o > i are written by
@@ -705,7 +708,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     B.molV = g.molV;
     WaveBufs W;
-    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops;
+    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.opt = g.use_tc ? g.opt : nullptr;
     W.pvec = g.pvec;
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
@@ -723,7 +726,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         auto tables = [&](int b) {
             k_tables<<<dim3(nw, tables_yblocks(b, G.NR, G.N)), b, tables_smem_bytes(b, G.N, g.Lmax), st>>>(
                 g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec,
-                W.fvec);
+                W.fvec, W.opt, (!g.use_tc || g.ncot > 0) ? 1 : 0);
         };
         int tb = 256;
         int rc = tuned_block("k_tables", (const void *)k_tables, {G.N, g.Lmax, g.Mmax}, !capture, st, tables, &tb);
@@ -731,7 +734,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         LAUNCH(plan, KC_TABLES, tables(tb));
         if (g.use_tc)
             LAUNCH(plan, KC_TABLES, k_mol_dense<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.Lmax, g.Bp, g.Br, g.Bt,
-                                                                     g.gw, g.ops));
+                                                                     g.gw, g.ops, g.opt));
         if (w.any_rough) {
             const bool dw = g.ncot > 0;
             const int np = w.p1 - w.p0;

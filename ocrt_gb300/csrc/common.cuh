@@ -136,6 +136,20 @@ __host__ __device__ inline float round_tf32f(float v)
 #endif
 }
 
+// Operator entry (row, cin) into the pre-split tensor-core tiles of one
+// operator: per 32-column K tile kt, a tf32 hi tile then a lo tile of NP rows
+// x 128 bytes in the SWIZZLE_128B K-major layout the MMA reads (16-byte chunk
+// j of row r at chunk position j ^ (r % 8)), so a tile is one bulk copy.
+__device__ inline void tile_put(float *T, const Geom &G, int row, int cin, float v)
+{
+    const int kt = cin >> 5, kc = cin & 31;
+    float *hi = T + (size_t)kt * 2 * G.NP * 32;
+    const int off = row * 32 + (((kc >> 2) ^ (row & 7)) << 2) + (kc & 3);
+    const float h = round_tf32f(v);
+    hi[off] = h;
+    hi[(size_t)G.NP * 32 + off] = round_tf32f(v - h);
+}
+
 #ifdef __CUDACC__
 // Per-thread asynchronous global -> shared copies (cp.async, cached in L1).
 __device__ inline void cp_async4(float *dst_smem, const float *src)

@@ -34,7 +34,7 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
-                         float *ops, float *pvec, float *fvec);
+                         float *ops, float *pvec, float *fvec, float *opt, int plain);
 // coxmunk_tc.cu: Cox-Munk Fourier kernels with the azimuth projection on tcgen05.
 // pairs: (outgoing slot, incoming slot) list of the ring (Gauss pairs with
 // outgoing > incoming left out: the reciprocal pair writes them).
@@ -71,6 +71,8 @@ struct WaveBufs {
     float *J;              // source of the current order
     float2 *Tot;           // order totals (hi, lo) pairs
     float *ops;            // operators, wave-relative (FP32)
+    float *opt;            // tensor-core path: the aerosol and dense molecular operators pre-split into
+                           // tf32 (hi, lo) SWIZZLE_128B tiles at 2 x op_off / 2 x uv_off (tile_put)
     float *pvec, *fvec;    // per wave-task primary and flat-beam vectors
     float *srf;            // rough surface kernels, wave-relative
 };
@@ -153,7 +155,7 @@ __global__ void k_adj_source_tc(BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int
 __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
 __global__ void k_mol_utrans(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
 __global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
-                            const float *Bt, const double *gw, float *ops);
+                            const float *Bt, const double *gw, const float *ops, float *opt);
 __global__ void k_mol_vtab(Geom G, int L, const float *Bp, const float *Br, const float *Bt, const double *gw,
                            float *V);
 size_t coxmunk_smem_bytes(int nphi, bool dw);

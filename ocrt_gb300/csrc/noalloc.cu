@@ -222,7 +222,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work; B.molV = nullptr;
     B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
-    W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
+    W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.opt = nullptr; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     for (int t0 = 0; t0 < T; t0 += Wt) {
         const int nw = (T - t0) < Wt ? (T - t0) : Wt;
@@ -235,7 +235,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
         NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, Bx));
         NA_LAUNCH(k_tables<<<dim3(nw, tables_yblocks(256, G.NR, G.N)), 256, tables_smem_bytes(256, G.N, L), st>>>(
-            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec));
+            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec, nullptr, 1));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= opts->max_orders; ++it) {

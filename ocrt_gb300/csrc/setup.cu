@@ -267,29 +267,27 @@ __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const Pi
 // (order: ii_s ii_c iu_s iu_c iuT_s iuT_c iq_s iq_c iqT_s iqT_c qq_s qq_c
 //  qu_s qu_c quT_s quT_c uu_s uu_c), with the quadrature weight folded in.
 // The signs are those of the contraction in rt_sos_operator.c:387-406.
-__device__ inline void put_pair(float *A, const Geom &G, int o, int i, float w, const float *c)
+template <class Store>
+__device__ inline void put_pair(Store st, const Geom &G, int o, int i, float w, const float *c)
 {
     enum { II_S, II_C, IU_S, IU_C, IUT_S, IUT_C, IQ_S, IQ_C, IQT_S, IQT_C, QQ_S, QQ_C,
            QU_S, QU_C, QUT_S, QUT_C, UU_S, UU_C };
-    auto at = [&](int so, int ho, int si, int hi) -> float & {
-        const int cin = (si * 2 + hi) * G.N + i;
-        return A[(size_t)col_of(G, so, ho, o) * G.CIN + cin];
-    };
+    auto at = [&](int so, int ho, int si, int hi, float v) { st(col_of(G, so, ho, o), (si * 2 + hi) * G.N + i, v); };
     // I up / down
-    at(0, 0, 0, 0) = w * c[II_S];   at(0, 0, 1, 0) = w * c[IQT_S];  at(0, 0, 2, 0) = -w * c[IUT_S];
-    at(0, 0, 0, 1) = w * c[II_C];   at(0, 0, 1, 1) = w * c[IQT_C];  at(0, 0, 2, 1) = -w * c[IUT_C];
-    at(0, 1, 0, 0) = w * c[II_C];   at(0, 1, 1, 0) = w * c[IQT_C];  at(0, 1, 2, 0) = w * c[IUT_C];
-    at(0, 1, 0, 1) = w * c[II_S];   at(0, 1, 1, 1) = w * c[IQT_S];  at(0, 1, 2, 1) = w * c[IUT_S];
+    at(0, 0, 0, 0, w * c[II_S]);   at(0, 0, 1, 0, w * c[IQT_S]);  at(0, 0, 2, 0, -w * c[IUT_S]);
+    at(0, 0, 0, 1, w * c[II_C]);   at(0, 0, 1, 1, w * c[IQT_C]);  at(0, 0, 2, 1, -w * c[IUT_C]);
+    at(0, 1, 0, 0, w * c[II_C]);   at(0, 1, 1, 0, w * c[IQT_C]);  at(0, 1, 2, 0, w * c[IUT_C]);
+    at(0, 1, 0, 1, w * c[II_S]);   at(0, 1, 1, 1, w * c[IQT_S]);  at(0, 1, 2, 1, w * c[IUT_S]);
     // Q up / down
-    at(1, 0, 0, 0) = w * c[IQ_S];   at(1, 0, 1, 0) = w * c[QQ_S];   at(1, 0, 2, 0) = -w * c[QU_S];
-    at(1, 0, 0, 1) = w * c[IQ_C];   at(1, 0, 1, 1) = w * c[QQ_C];   at(1, 0, 2, 1) = w * c[QU_C];
-    at(1, 1, 0, 0) = w * c[IQ_C];   at(1, 1, 1, 0) = w * c[QQ_C];   at(1, 1, 2, 0) = -w * c[QU_C];
-    at(1, 1, 0, 1) = w * c[IQ_S];   at(1, 1, 1, 1) = w * c[QQ_S];   at(1, 1, 2, 1) = w * c[QU_S];
+    at(1, 0, 0, 0, w * c[IQ_S]);   at(1, 0, 1, 0, w * c[QQ_S]);   at(1, 0, 2, 0, -w * c[QU_S]);
+    at(1, 0, 0, 1, w * c[IQ_C]);   at(1, 0, 1, 1, w * c[QQ_C]);   at(1, 0, 2, 1, w * c[QU_C]);
+    at(1, 1, 0, 0, w * c[IQ_C]);   at(1, 1, 1, 0, w * c[QQ_C]);   at(1, 1, 2, 0, -w * c[QU_C]);
+    at(1, 1, 0, 1, w * c[IQ_S]);   at(1, 1, 1, 1, w * c[QQ_S]);   at(1, 1, 2, 1, w * c[QU_S]);
     // U up / down (leading minus of rt_sos_operator.c:399-406 folded in)
-    at(2, 0, 0, 0) = -w * c[IU_S];  at(2, 0, 1, 0) = -w * c[QUT_S]; at(2, 0, 2, 0) = w * c[UU_S];
-    at(2, 0, 0, 1) = w * c[IU_C];   at(2, 0, 1, 1) = -w * c[QUT_C]; at(2, 0, 2, 1) = w * c[UU_C];
-    at(2, 1, 0, 0) = -w * c[IU_C];  at(2, 1, 1, 0) = w * c[QUT_C];  at(2, 1, 2, 0) = w * c[UU_C];
-    at(2, 1, 0, 1) = w * c[IU_S];   at(2, 1, 1, 1) = w * c[QUT_S];  at(2, 1, 2, 1) = w * c[UU_S];
+    at(2, 0, 0, 0, -w * c[IU_S]);  at(2, 0, 1, 0, -w * c[QUT_S]); at(2, 0, 2, 0, w * c[UU_S]);
+    at(2, 0, 0, 1, w * c[IU_C]);   at(2, 0, 1, 1, -w * c[QUT_C]); at(2, 0, 2, 1, w * c[UU_C]);
+    at(2, 1, 0, 0, -w * c[IU_C]);  at(2, 1, 1, 0, w * c[QUT_C]);  at(2, 1, 2, 0, w * c[UU_C]);
+    at(2, 1, 0, 1, w * c[IU_S]);   at(2, 1, 1, 1, w * c[QUT_S]);  at(2, 1, 2, 1, w * c[UU_S]);
 }
 
 // One block per task.  Phase tables by contraction over l in FP32 with the
@@ -300,7 +298,7 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
-                         float *ops, float *pvec, float *fvec)
+                         float *ops, float *pvec, float *fvec, float *opt, int plain)
 {
     const int tl = blockIdx.x;
     if (tl >= nt_tasks) return;
@@ -324,6 +322,7 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
     const float b0 = m == 0 ? 1.f : 0.f, b2 = (float)(0.5 * A), g2 = (float)(-A * sqrt(1.5)), a2 = (float)(3.0 * A);
     const int mol = m <= 2;
     float *Aop = ops + tk.op_off;
+    float *Atile = opt ? opt + 2 * tk.op_off : nullptr;     // tensor-core tiles of the aerosol operator
     float *Bop = tk.mol_off >= 0 ? ops + tk.mol_off : nullptr;
     // aerosol moments in FP32 shared memory (read at every l of every pair)
     extern __shared__ float smom[];                               // [4][Lp + 1]
@@ -430,10 +429,20 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
         c[14] = St[2] + St[3];   c[15] = Dt[2] - Dt[3];     // art[o][+-i]
         c[16] = S[7] + S[8];     c[17] = -D[7] + D[8];      // att[i][+-o]
         const float w = (float)gw[i];
-        put_pair(Aop, G, os, i, w, c);
+        if (plain) put_pair([&](int r, int ci, float v) { Aop[(size_t)r * G.CIN + ci] = v; }, G, os, i, w, c);
+        if (Atile) put_pair([&](int r, int ci, float v) { tile_put(Atile, G, r, ci, v); }, G, os, i, w, c);
     }
     }
     if (blockIdx.y != 0) return;
+    // tile rows no pair writes: the view rows when the view is a Gauss node,
+    // and the padding rows COUT .. NP - 1
+    if (Atile) {
+        const int nz0 = n == N ? 6 : 0, nz = nz0 + (G.NP - G.COUT);
+        for (int e = threadIdx.x; e < nz * G.CIN; e += blockDim.x) {
+            const int q = e / G.CIN, ci = e - q * G.CIN;
+            tile_put(Atile, G, q < nz0 ? 6 * N + q : G.COUT + (q - nz0), ci, 0.f);
+        }
+    }
     // ---- molecular operator (m <= 2) in factored form U[c_out][24] ----
     // Every molecular entry is (function of the outgoing direction) x
     // w_i f(mu_i), f in {1, P2m, R2m, T2m}; U holds the outgoing factors for

@@ -478,7 +478,7 @@ __global__ void k_stop_check(const int *active_after_last, int *flag)
 // so that UV F equals U (V F) of k_mol_lowrank.  Rows COUT..NP-1 are zero.
 // One block per molecular task of the wave.
 __global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L, const float *Bp, const float *Br,
-                            const float *Bt, const double *gw, float *ops)
+                            const float *Bt, const double *gw, const float *ops, float *opt)
 {
     const int tl = blockIdx.x;
     if (tl >= nw) return;
@@ -493,7 +493,7 @@ __global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L,
     }
     __syncthreads();
     const float *U = ops + tk.mol_off;
-    float *UV = ops + tk.uv_off;
+    float *UVt = opt + 2 * tk.uv_off;          // pre-split tensor-core tiles, padding rows included
     for (int e = threadIdx.x; e < G.NP * G.CIN; e += blockDim.x) {
         const int c = e / G.CIN, ci = e - c * G.CIN, b = ci / N, i = ci - b * N;
         float v = 0.f;
@@ -501,7 +501,7 @@ __global__ void k_mol_dense(const TaskDev *tasks, int t0, int nw, Geom G, int L,
             const float *u = U + (size_t)c * 24 + 4 * b;
             v = u[0] * fv[i] + u[1] * fv[N + i] + u[2] * fv[2 * N + i] + u[3] * fv[3 * N + i];
         }
-        UV[e] = v;
+        tile_put(UVt, G, c, ci, v);
     }
 }
 

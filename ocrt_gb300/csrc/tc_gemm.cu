@@ -94,7 +94,8 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
     }
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
-            mbar_init(&full[i], TC_PGW);
+            // forward: one more arrival, the bulk-copy thread's arrive.expect_tx for the B tiles
+            mbar_init(&full[i], TC_PGW + (ADJ ? 0 : 1));
             mbar_init(&empty[i], 1);
             mbar_init(&tfull[i], 1);
             mbar_init(&tempty[i], 4);
@@ -125,7 +126,8 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
         float4 ra[TC_AQ], rb[TC_BQ];
         // item operands: A rows (nra of them real), B = Bb for K tiles below
         // NKT and Bm (dense molecular operator) for NKT .. nkt - 1
-        struct Opnd { const float *Ab, *Bb, *Bm; int nra, nbi, nkt; };
+        // forward: Bt / Btm = the pre-split operator tiles (aerosol, dense molecular)
+        struct Opnd { const float *Ab, *Bb, *Bm, *Bt, *Btm; int nra, nbi, nkt; };
         // K tile kt of the item into registers: A rows 0 .. nra - 1 of the item
         // (zero past the task and past a_cols), B rows 0 .. nbi - 1
         auto load = [&](const Opnd &o, int kt) {
@@ -137,9 +139,11 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
 #pragma unroll
             for (int i = 0; i < TC_AQ; ++i)
                 ra[i] = acol && r8 + 16 * i < o.nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (ADJ) {
 #pragma unroll
-            for (int i = 0; i < TC_BQ; ++i)
-                if (r8 + 16 * i < o.nbi) rb[i] = __ldg(pb + (size_t)i * 4 * b_ld);
+                for (int i = 0; i < TC_BQ; ++i)
+                    if (r8 + 16 * i < o.nbi) rb[i] = __ldg(pb + (size_t)i * 4 * b_ld);
+            }
         };
         // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
         auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
@@ -196,12 +200,16 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             o.Bb = ADJ ? AB.opsT + (size_t)tl * (NB + 32) * b_ld : W.ops + tk.op_off;
             const bool dbl = !ADJ && tk.has_mol;
             o.Bm = dbl ? W.ops + tk.uv_off : o.Bb;
+            o.Bt = ADJ ? nullptr : W.opt + 2 * tk.op_off;
+            o.Btm = dbl ? W.opt + 2 * tk.uv_off : o.Bt;
             o.nkt = dbl ? 2 * NKT : NKT;
             return o;
         };
         if (pt == 0) fetch_publish(0);
         uint32_t g = 0;
-        bool have = false;           // the registers already hold this group's first tile of the item
+        bool have = false;
+        int armed = 0;               // bulk copies issued into this group's stage; parity of the last
+        uint32_t armed_par = 0;           // the registers already hold this group's first tile of the item
         for (int j = 0;; ++j) {
             int item = -1;
             if (!item_at(j, item)) { *abort_flag = 1; break; }
@@ -221,11 +229,24 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                 __syncwarp();
                 if (!free_ok) { *abort_flag = 1; stop = true; break; }
                 unsigned char *sp = base + (size_t)s * STAGE;
+                if (!ADJ && gt == 0) {
+                    // the B tiles of this K tile: two bulk copies completing on full[s]
+                    const int kf = kt < NKT ? kt : kt - NKT;
+                    const float *src = (kt < NKT ? op.Bt : op.Btm) + (size_t)kf * 2 * NB * TC_KT;
+                    mbar_expect_tx(&full[s], 2 * B_BYTES);
+                    armed = 1;
+                    armed_par = u & 1;
+                    bulk_g2s(sp + 2 * A_BYTES, src, B_BYTES, &full[s]);
+                    bulk_g2s(sp + 2 * A_BYTES + B_BYTES, src + (size_t)NB * TC_KT, B_BYTES, &full[s]);
+                }
 #pragma unroll
                 for (int i = 0; i < TC_AQ; ++i) put(sp, sp + A_BYTES, soff + 2048u * i, ra[i]);
+                if (ADJ) {
 #pragma unroll
-                for (int i = 0; i < TC_BQ; ++i)
-                    if (r8 + 16 * i < op.nbi) put(sp + 2 * A_BYTES, sp + 2 * A_BYTES + B_BYTES, soff + 2048u * i, rb[i]);
+                    for (int i = 0; i < TC_BQ; ++i)
+                        if (r8 + 16 * i < op.nbi)
+                            put(sp + 2 * A_BYTES, sp + 2 * A_BYTES + B_BYTES, soff + 2048u * i, rb[i]);
+                }
                 // generic-proxy stores made visible to the tensor cores before the stage is marked full
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
@@ -245,6 +266,9 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             if (stop) break;
             g += (uint32_t)op.nkt;
         }
+        // the last B copies into this group's stage have landed before the CTA
+        // can leave (every armed stage also gets the group's four arrivals)
+        if (!ADJ && gt == 0 && armed) mbar_wait(&full[grp], armed_par);
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
