@@ -148,10 +148,10 @@ __global__ void k_mol_utrans(const TaskDev *tasks, int t0, int nw, Geom G, const
     if (!tk.has_mol) return;
     const int KP = (G.COUT + 31) & ~31;
     const float *U = ops + tk.mol_off;
-    float *T = opsT + (size_t)tl * (G.CIN + 32) * KP + (size_t)G.CIN * KP;
+    float *T = opsT + (size_t)tl * 2 * (G.CIN + 32) * KP;
     for (int e = threadIdx.x; e < 32 * KP; e += blockDim.x) {
         const int q = e / KP, kk = e - q * KP;
-        T[e] = (q < 24 && kk < G.COUT) ? U[(size_t)kk * 24 + q] : 0.f;
+        tile_put_rows(T, G.CIN + 32, G.CIN + q, kk, (q < 24 && kk < G.COUT) ? U[(size_t)kk * 24 + q] : 0.f);
     }
 }
 
@@ -173,10 +173,12 @@ __global__ void k_fill_all(BatchBufs B, int t0, int nw, int it)
     }
 }
 
-// Transposed operators for the tcgen05 adjoint source: opsT[tl][cin][kk] =
-// Aop[kk][cin] for kk < COUT, 0 up to KP = COUT rounded up to 32 (per task
-// CIN + 32 rows of KP; k_mol_utrans fills the last 32 for m <= 2).  32 x 32
-// tiles through shared memory.  Grid (task, CIN/32 tiles, KP/32 tiles), 32 x 8.
+// Transposed operators for the tcgen05 adjoint source: entry (cin, kk) =
+// Aop[kk][cin] for kk < COUT, 0 up to KP = COUT rounded up to 32, per task
+// CIN + 32 rows (k_mol_utrans fills the last 32 for m <= 2), written as the
+// pre-split tf32 hi/lo SWIZZLE_128B tiles the tensor-core pass copies in
+// (tile_put_rows; 2 (CIN + 32) KP floats per task).  32 x 32 blocks through
+// shared memory.  Grid (task, CIN/32 blocks, KP/32 blocks), 32 x 8.
 __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT)
 {
     __shared__ float tile[32][33];
@@ -191,10 +193,10 @@ __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, con
         tile[yy][threadIdx.x] = (row < G.COUT && cin < G.CIN) ? A[(size_t)row * G.CIN + cin] : 0.f;
     }
     __syncthreads();
-    float *T = opsT + (size_t)tl * (G.CIN + 32) * KP;
+    float *T = opsT + (size_t)tl * 2 * (G.CIN + 32) * KP;
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
         const int cin = c0 + yy, kk = r0 + threadIdx.x;
-        if (cin < G.CIN && kk < KP) T[(size_t)cin * KP + kk] = tile[threadIdx.x][yy];
+        if (cin < G.CIN && kk < KP) tile_put_rows(T, G.CIN + 32, cin, kk, tile[threadIdx.x][yy]);
     }
 }
 

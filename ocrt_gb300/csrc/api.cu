@@ -408,7 +408,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         size_t pb = pf * 16 + po * (tiles ? 12 : 4) + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 12 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
-                  nm * (size_t)G.CIN * ((G.COUT + 31) & ~31) * 4;
+                  nm * (size_t)2 * (G.CIN + 32) * ((G.COUT + 31) & ~31) * 4;
         if (q > w.p0 && bytes + pb > budget) {
             close(q);
             w = Wave{q, 0, d.task0, 0, 0, 0, 0, 0, false, false};
@@ -503,7 +503,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     }
     if (g.use_tc && ncot > 0 && tc_adj_supported(G)) {
         const int KP = (G.COUT + 31) & ~31;
-        if ((rc = alloc(g.opsT, (size_t)g.wave_tasks * (G.CIN + 32) * KP))) return rc;
+        if ((rc = alloc(g.opsT, (size_t)g.wave_tasks * 2 * (G.CIN + 32) * KP))) return rc;
         g.use_tc_adj = true;
     }
     for (Wave &w : g.waves) {

@@ -140,14 +140,19 @@ __host__ __device__ inline float round_tf32f(float v)
 // operator: per 32-column K tile kt, a tf32 hi tile then a lo tile of NP rows
 // x 128 bytes in the SWIZZLE_128B K-major layout the MMA reads (16-byte chunk
 // j of row r at chunk position j ^ (r % 8)), so a tile is one bulk copy.
-__device__ inline void tile_put(float *T, const Geom &G, int row, int cin, float v)
+__device__ inline void tile_put_rows(float *T, int nrows, int row, int col, float v)
 {
-    const int kt = cin >> 5, kc = cin & 31;
-    float *hi = T + (size_t)kt * 2 * G.NP * 32;
+    const int kt = col >> 5, kc = col & 31;
+    float *hi = T + (size_t)kt * 2 * nrows * 32;
     const int off = row * 32 + (((kc >> 2) ^ (row & 7)) << 2) + (kc & 3);
     const float h = round_tf32f(v);
     hi[off] = h;
-    hi[(size_t)G.NP * 32 + off] = round_tf32f(v - h);
+    hi[(size_t)nrows * 32 + off] = round_tf32f(v - h);
+}
+// forward operators: NP rows (outputs), K = CIN
+__device__ inline void tile_put(float *T, const Geom &G, int row, int cin, float v)
+{
+    tile_put_rows(T, G.NP, row, cin, v);
 }
 
 #ifdef __CUDACC__

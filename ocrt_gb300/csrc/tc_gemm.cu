@@ -9,13 +9,17 @@
 //
 // Both kernels (k_source_tc, k_adj_source_tc: 512 threads, one CTA per SM,
 // persistent over items):
-//   warps 8-15 producers: read the FP32 field rows and operator rows of a K
-//           tile straight from global memory, split each value into tf32
-//           (hi, lo) in registers and store both into the SWIZZLE_128B
-//           K-major layout of a 2-stage shared-memory ring (warps 8-11 fill
-//           stage 0, warps 12-15 stage 1, so each group has two tile periods
-//           to cover its load latency); field rows past the task are zero
-//           and never read.  Warp 8 lane 0 also fetches the items.
+//   warps 8-15 producers: read the FP32 field rows of a K tile straight from
+//           global memory, split each value into tf32 (hi, lo) in registers
+//           and store both into the SWIZZLE_128B K-major layout of a 2-stage
+//           shared-memory ring (warps 8-11 fill stage 0, warps 12-15 stage 1,
+//           so each group has two tile periods to cover its load latency);
+//           field rows past the task are zero and never read.  The operator
+//           side arrives pre-split: the first thread of the group issues two
+//           bulk copies of the operator's hi and lo tiles for that K tile
+//           (written once per wave by k_tables / k_mol_dense, or by
+//           k_op_transpose / k_mol_utrans for the adjoint), completing on the
+//           stage's full barrier.  Warp 8 lane 0 also fetches the items.
 //   warp 1  MMA issuer: one thread issues the MMAs into one of two TMEM
 //           accumulators (2 x 256 columns), so the next item's MMAs run while
 //           the epilogue drains the previous one;
@@ -94,8 +98,8 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
     }
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
-            // forward: one more arrival, the bulk-copy thread's arrive.expect_tx for the B tiles
-            mbar_init(&full[i], TC_PGW + (ADJ ? 0 : 1));
+            // one more arrival: the bulk-copy thread's arrive.expect_tx for the B tiles
+            mbar_init(&full[i], TC_PGW + 1);
             mbar_init(&empty[i], 1);
             mbar_init(&tfull[i], 1);
             mbar_init(&tempty[i], 4);
@@ -123,11 +127,13 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
         // A rows: field (forward) or stacked muJ rows (adjoint), stride LDC,
         // K columns < a_cols real; B rows: operator rows of length b_ld.
         const int a_cols = ADJ ? G.LDC : G.CIN, b_ld = ADJ ? ((G.COUT + 31) & ~31) : G.CIN;
-        float4 ra[TC_AQ], rb[TC_BQ];
+        float4 ra[TC_AQ];
         // item operands: A rows (nra of them real), B = Bb for K tiles below
         // NKT and Bm (dense molecular operator) for NKT .. nkt - 1
-        // forward: Bt / Btm = the pre-split operator tiles (aerosol, dense molecular)
-        struct Opnd { const float *Ab, *Bb, *Bm, *Bt, *Btm; int nra, nbi, nkt; };
+        // Bt / Btm: the pre-split operator tiles (forward: aerosol, dense
+        // molecular; adjoint: transposed operator with U^T rows), tile row count tr
+        struct Opnd { const float *Ab, *Bt, *Btm; int nra, nbi, nkt; };
+        const int tr = ADJ ? NB + 32 : NB;
         // K tile kt of the item into registers: A rows 0 .. nra - 1 of the item
         // (zero past the task and past a_cols), B rows 0 .. nbi - 1
         auto load = [&](const Opnd &o, int kt) {
@@ -135,15 +141,9 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             const int col = kk * TC_KT + ch * 4;
             const bool acol = col + 4 <= a_cols;
             const float4 *pa = reinterpret_cast<const float4 *>(o.Ab + (size_t)r8 * G.LDC + col);
-            const float4 *pb = reinterpret_cast<const float4 *>((kt < NKT ? o.Bb : o.Bm) + (size_t)r8 * b_ld + col);
 #pragma unroll
             for (int i = 0; i < TC_AQ; ++i)
                 ra[i] = acol && r8 + 16 * i < o.nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
-            if (ADJ) {
-#pragma unroll
-                for (int i = 0; i < TC_BQ; ++i)
-                    if (r8 + 16 * i < o.nbi) rb[i] = __ldg(pb + (size_t)i * 4 * b_ld);
-            }
         };
         // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
         auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
@@ -197,10 +197,8 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             o.nra = min(TC_M, (ADJ ? AB.ncot * tk.K : tk.K) - r0);
             o.nbi = ADJ && tk.has_mol ? NBM : NB;
             o.Ab = ADJ ? AB.AJ + (size_t)tk.fld_off * AB.ncot + (size_t)r0 * G.LDC : W.F + tk.fld_off + (size_t)r0 * G.LDC;
-            o.Bb = ADJ ? AB.opsT + (size_t)tl * (NB + 32) * b_ld : W.ops + tk.op_off;
             const bool dbl = !ADJ && tk.has_mol;
-            o.Bm = dbl ? W.ops + tk.uv_off : o.Bb;
-            o.Bt = ADJ ? nullptr : W.opt + 2 * tk.op_off;
+            o.Bt = ADJ ? AB.opsT + (size_t)tl * 2 * tr * b_ld : W.opt + 2 * tk.op_off;
             o.Btm = dbl ? W.opt + 2 * tk.uv_off : o.Bt;
             o.nkt = dbl ? 2 * NKT : NKT;
             return o;
@@ -229,24 +227,21 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
                 __syncwarp();
                 if (!free_ok) { *abort_flag = 1; stop = true; break; }
                 unsigned char *sp = base + (size_t)s * STAGE;
-                if (!ADJ && gt == 0) {
-                    // the B tiles of this K tile: two bulk copies completing on full[s]
+                if (gt == 0) {
+                    // the B tiles of this K tile (its first nbi rows): two bulk
+                    // copies completing on full[s]
                     const int kf = kt < NKT ? kt : kt - NKT;
-                    const float *src = (kt < NKT ? op.Bt : op.Btm) + (size_t)kf * 2 * NB * TC_KT;
-                    mbar_expect_tx(&full[s], 2 * B_BYTES);
+                    const float *src = (kt < NKT ? op.Bt : op.Btm) + (size_t)kf * 2 * tr * TC_KT;
+                    const uint32_t nb = (uint32_t)op.nbi * TC_KT * 4;
+                    mbar_expect_tx(&full[s], 2 * nb);
                     armed = 1;
                     armed_par = u & 1;
-                    bulk_g2s(sp + 2 * A_BYTES, src, B_BYTES, &full[s]);
-                    bulk_g2s(sp + 2 * A_BYTES + B_BYTES, src + (size_t)NB * TC_KT, B_BYTES, &full[s]);
+                    bulk_g2s(sp + 2 * A_BYTES, src, nb, &full[s]);
+                    bulk_g2s(sp + 2 * A_BYTES + B_BYTES, src + (size_t)tr * TC_KT, nb, &full[s]);
                 }
 #pragma unroll
                 for (int i = 0; i < TC_AQ; ++i) put(sp, sp + A_BYTES, soff + 2048u * i, ra[i]);
-                if (ADJ) {
-#pragma unroll
-                    for (int i = 0; i < TC_BQ; ++i)
-                        if (r8 + 16 * i < op.nbi)
-                            put(sp + 2 * A_BYTES, sp + 2 * A_BYTES + B_BYTES, soff + 2048u * i, rb[i]);
-                }
+
                 // generic-proxy stores made visible to the tensor cores before the stage is marked full
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
@@ -268,7 +263,7 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
         }
         // the last B copies into this group's stage have landed before the CTA
         // can leave (every armed stage also gets the group's four arrivals)
-        if (!ADJ && gt == 0 && armed) mbar_wait(&full[grp], armed_par);
+        if (gt == 0 && armed) mbar_wait(&full[grp], armed_par);
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
         constexpr uint32_t IDESC_BASE = idesc_tf32(TC_M, 16);    // N filled in below
