@@ -21,11 +21,12 @@ inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads
 // k_adj_scan: cotangent rows per block (they share the transport coefficients)
 #define ADJ_RB 3
 inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 4) + 12); }
-// k_tables launch shape: grid (tasks, tables_yblocks), one (outgoing, incoming)
-// pair per thread; moments are staged TB_LC at a time (even).
+// k_tables launch shape: grid (tasks, tables_yblocks), two (outgoing, incoming)
+// pairs per thread, (o, i) and (o, i + ceil(N/2)); moments are staged TB_LC at a
+// time (even).
 #define TB_LC 16
-__host__ __device__ inline int tables_orows(int threads, int N) { return threads / N + 2; }
-inline int tables_yblocks(int threads, int NR, int N) { return (NR * N + threads - 1) / threads; }
+__host__ __device__ inline int tables_orows(int threads, int N) { return threads / ((N + 1) / 2) + 2; }
+inline int tables_yblocks(int threads, int NR, int N) { return (NR * ((N + 1) / 2) + threads - 1) / threads; }
 inline size_t tables_smem_bytes(int threads, int N, int L)
 {
     return sizeof(float) * (4 * ((size_t)L + 1) + 8 * (size_t)tables_orows(threads, N) * TB_LC + 3 * (size_t)TB_LC * N);

@@ -294,7 +294,7 @@ __device__ inline void put_pair(Store st, const Geom &G, int o, int i, float w, 
 // even/odd parity split giving the mirrored columns; then the packed aerosol
 // operator (and molecular operator for m <= 2), the primary-source vectors and
 // the flat-surface reflected-beam vectors.
-__global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
+__global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
@@ -336,31 +336,37 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
     __syncthreads();
 
     // ---- operator pairs (o ring slot, i Gauss) ----
-    // Block y of the task takes pairs [y * blockDim, (y + 1) * blockDim) of the
-    // n * N pairs, one per thread.  Every pair product is (incoming basis) x
-    // (outgoing basis x moment); the eight outgoing factors Y_k(o, l) and the
-    // incoming bases X_c(i, l) are staged in shared memory TB_LC moments at a
-    // time, so a pair costs 13 FMAs per moment.  l starts at m and chunks are
-    // even, so the parity of l + m is the parity of the chunk offset.
+    // A thread takes the two pairs (o, i) and (o, i + hN), hN = ceil(N / 2), so
+    // both share the outgoing factors; block y of the task takes the (o, i)
+    // slots [y * blockDim, (y + 1) * blockDim) of n * hN.  Every pair product
+    // is (incoming basis) x (outgoing basis x moment); the eight outgoing
+    // factors Y_k(o, l) and the incoming bases X_c(i, l) are staged in shared
+    // memory TB_LC moments at a time, so a pair costs 13 FMAs per moment.  l
+    // starts at m and chunks are even, so the parity of l + m is the parity of
+    // the chunk offset.
     float *Ys = smom + 4 * (L + 1);                               // [8][PO][TB_LC]
     const int PO = tables_orows(blockDim.x, N);
     float *Xs = Ys + 8 * PO * TB_LC;                              // [3][TB_LC][N]
-    const int npair = n * N, e0 = blockIdx.y * blockDim.x;
-    if (e0 < npair) {
-    const int e1 = min(e0 + (int)blockDim.x, npair);
-    const int o_lo = e0 / N, nor = (e1 - 1) / N - o_lo + 1;
+    const int hN = (N + 1) / 2;
+    const int nslot = n * hN, e0 = blockIdx.y * blockDim.x;
+    if (e0 < nslot) {
+    const int e1 = min(e0 + (int)blockDim.x, nslot);
+    const int o_lo = e0 / hN, nor = (e1 - 1) / hN - o_lo + 1;
     const int e = e0 + threadIdx.x;
     const bool mine = e < e1;
-    const int o = mine ? e / N : o_lo, i = mine ? e - o * N : 0;
+    const int o = mine ? e / hN : o_lo, i0 = mine ? e - o * hN : 0, i1 = i0 + hN;
+    const bool mine1 = mine && i1 < N;
     const int os = o;    // ring slot (the view node, when inserted, is slot N)
     // Y_k = basis(comp_k) x moment(mom_k), one nibble per k (k = 0 lowest):
     // comp {P, R, T, T, R, T, R, P}, moment {beta, gamma, gamma, zeta, alpha, alpha, zeta, gamma}
     // with moments 0 beta, 1 gamma, 2 alpha, 3 zeta
     constexpr unsigned ycomp = 0x01212210u, ymom = 0x13223110u;
-    // accumulators 0..8: [row i, col o] products, 9..12: transposed pair; even (E) / odd (O) in l+m
-    float E[13], O[13];
+    // accumulators 0..8: [row i, col o] products, 9..12: transposed pair; even
+    // (E) / odd (O) in l+m; the second pair's in E1 / O1
+    float E[13], O[13], E1[13], O1[13];
 #pragma unroll
-    for (int q = 0; q < 13; ++q) { E[q] = 0.f; O[q] = 0.f; }
+    for (int q = 0; q < 13; ++q) { E[q] = 0.f; O[q] = 0.f; E1[q] = 0.f; O1[q] = 0.f; }
+    const int ia = i0, ib = mine1 ? i1 : i0;
     for (int l0 = m; l0 <= Lp; l0 += TB_LC) {
         __syncthreads();
         // Y: one (outgoing row, moment) per thread, all eight factors
@@ -396,28 +402,39 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                 for (int k = 0; k < 8; ++k) y[k] = *reinterpret_cast<const float4 *>(yb + k * PO * TB_LC + lc);
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const float Pi = Xs[(0 * TB_LC + lc + u) * N + i], Ri = Xs[(1 * TB_LC + lc + u) * N + i],
-                                Ti = Xs[(2 * TB_LC + lc + u) * N + i];
                     float Y[8];
 #pragma unroll
                     for (int k = 0; k < 8; ++k) Y[k] = u == 0 ? y[k].x : u == 1 ? y[k].y : u == 2 ? y[k].z : y[k].w;
-                    float *A = (u & 1) ? O : E;
-                    A[0] = fmaf(Pi, Y[0], A[0]);  A[1] = fmaf(Pi, Y[1], A[1]);  A[2] = fmaf(Pi, Y[2], A[2]);
-                    A[3] = fmaf(Ti, Y[3], A[3]);  A[4] = fmaf(Ri, Y[4], A[4]);  A[5] = fmaf(Ti, Y[4], A[5]);
-                    A[6] = fmaf(Ri, Y[3], A[6]);  A[7] = fmaf(Ti, Y[5], A[7]);  A[8] = fmaf(Ri, Y[6], A[8]);
-                    A[9] = fmaf(Ti, Y[7], A[9]);  A[10] = fmaf(Ri, Y[7], A[10]);
-                    A[11] = fmaf(Ri, Y[5], A[11]); A[12] = fmaf(Ti, Y[6], A[12]);
+                    const float *xr = Xs + (lc + u) * N;
+                    {
+                        const float Pi = xr[ia], Ri = xr[TB_LC * N + ia], Ti = xr[2 * TB_LC * N + ia];
+                        float *A = (u & 1) ? O : E;
+                        A[0] = fmaf(Pi, Y[0], A[0]);  A[1] = fmaf(Pi, Y[1], A[1]);  A[2] = fmaf(Pi, Y[2], A[2]);
+                        A[3] = fmaf(Ti, Y[3], A[3]);  A[4] = fmaf(Ri, Y[4], A[4]);  A[5] = fmaf(Ti, Y[4], A[5]);
+                        A[6] = fmaf(Ri, Y[3], A[6]);  A[7] = fmaf(Ti, Y[5], A[7]);  A[8] = fmaf(Ri, Y[6], A[8]);
+                        A[9] = fmaf(Ti, Y[7], A[9]);  A[10] = fmaf(Ri, Y[7], A[10]);
+                        A[11] = fmaf(Ri, Y[5], A[11]); A[12] = fmaf(Ti, Y[6], A[12]);
+                    }
+                    {
+                        const float Pi = xr[ib], Ri = xr[TB_LC * N + ib], Ti = xr[2 * TB_LC * N + ib];
+                        float *A = (u & 1) ? O1 : E1;
+                        A[0] = fmaf(Pi, Y[0], A[0]);  A[1] = fmaf(Pi, Y[1], A[1]);  A[2] = fmaf(Pi, Y[2], A[2]);
+                        A[3] = fmaf(Ti, Y[3], A[3]);  A[4] = fmaf(Ri, Y[4], A[4]);  A[5] = fmaf(Ti, Y[4], A[5]);
+                        A[6] = fmaf(Ri, Y[3], A[6]);  A[7] = fmaf(Ti, Y[5], A[7]);  A[8] = fmaf(Ri, Y[6], A[8]);
+                        A[9] = fmaf(Ti, Y[7], A[9]);  A[10] = fmaf(Ri, Y[7], A[10]);
+                        A[11] = fmaf(Ri, Y[5], A[11]); A[12] = fmaf(Ti, Y[6], A[12]);
+                    }
                 }
             }
         }
     }
-    if (mine) {
+    // tables: value at +col = S, at -col = sigma * D with sigma from the column basis
+    auto emit = [&](const float *Ea, const float *Oa, int i) {
         float S[9], D[9], St[4], Dt[4];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) { S[q] = E[q] + O[q]; D[q] = E[q] - O[q]; }
+        for (int q = 0; q < 9; ++q) { S[q] = Ea[q] + Oa[q]; D[q] = Ea[q] - Oa[q]; }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) { St[q] = E[9 + q] + O[9 + q]; Dt[q] = E[9 + q] - O[9 + q]; }
-        // tables: value at +col = S, at -col = sigma * D with sigma from the column basis
+        for (int q = 0; q < 4; ++q) { St[q] = Ea[9 + q] + Oa[9 + q]; Dt[q] = Ea[9 + q] - Oa[9 + q]; }
         float c[18];
         c[0] = S[0];             c[1] = D[0];               // pfm[i][+-o]
         c[2] = S[2];             c[3] = -D[2];              // gt[i][+-o]
@@ -431,7 +448,9 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
         const float w = (float)gw[i];
         if (plain) put_pair([&](int r, int ci, float v) { Aop[(size_t)r * G.CIN + ci] = v; }, G, os, i, w, c);
         if (Atile) put_pair([&](int r, int ci, float v) { tile_put(Atile, G, r, ci, v); }, G, os, i, w, c);
-    }
+    };
+    if (mine) emit(E, O, i0);
+    if (mine1) emit(E1, O1, i1);
     }
     if (blockIdx.y != 0) return;
     // tile rows no pair writes: the view rows when the view is a Gauss node,
