@@ -83,6 +83,55 @@ __device__ inline double ray_above(double z, int profile, double h)
     return profile == 1 ? exp_above(z, OCRT_ZTOP_KM, h) : us62_grid_above(z);
 }
 
+// The same column fractions with their altitude-independent parts evaluated
+// once per thread (the table logarithms, the 45-degree gravity term, the US62
+// fraction at 84.852 km, exp(-ztop / h)), for the 64-step level bisection.
+struct AboveEval {
+    int prof;
+    double rh, ah, et_r, et_a;
+    double lp[8], a45, q0, ft;
+};
+
+__device__ inline double above_g45(const AboveEval &E, double z_m) { return E.a45 - 3.086e-6 * z_m; }
+
+__device__ inline void above_init(AboveEval &E, int prof, double ray_h, double aer_h)
+{
+    const double P[8] = {101325.0, 22632.1, 5474.89, 868.019, 110.906, 66.9389, 3.95642, 0.3734};
+    E.prof = prof; E.rh = ray_h; E.ah = aer_h;
+    E.et_r = exp(-OCRT_ZTOP_KM / ray_h);
+    E.et_a = exp(-OCRT_ZTOP_KM / aer_h);
+    for (int i = 0; i < 8; ++i) E.lp[i] = log(P[i]);
+    const double lat = 45.0 * OCRT_PI / 180.0;
+    const double s1 = sin(lat) * sin(lat), s2 = sin(2.0 * lat) * sin(2.0 * lat);
+    E.a45 = 9.780327 * (1.0 + 0.0053024 * s1 - 0.0000058 * s2);
+    E.q0 = 101325.0 / above_g45(E, 0.0);
+    E.ft = clamp01d((0.3734 / above_g45(E, 84852.0)) / E.q0);     // us62_raw(84.852)
+}
+
+__device__ inline double above_exp(double z, double h, double et)
+{
+    if (z <= 0.0) return 1.0;
+    if (z >= OCRT_ZTOP_KM) return 0.0;
+    return (exp(-z / h) - et) / (1.0 - et);
+}
+
+__device__ inline double above_ray(const AboveEval &E, double z)
+{
+    if (E.prof == 1) return above_exp(z, E.rh, E.et_r);
+    if (z <= 0.0) return 1.0;
+    if (z >= 84.852) return 0.0;
+    const double Z[8] = {0.0, 11.0, 20.0, 32.0, 47.0, 51.0, 71.0, 84.852};
+    int lo = 0, hi = 7;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (z < Z[mid]) hi = mid; else lo = mid;
+    }
+    const double t = (z - Z[lo]) / (Z[hi] - Z[lo]);
+    const double a = E.lp[lo], b = E.lp[hi];
+    const double raw = clamp01d((exp(a + t * (b - a)) / above_g45(E, z * 1000.0)) / E.q0);
+    return clamp01d((raw - E.ft) / (1.0 - E.ft));
+}
+
 // ---- generalized spherical functions (rt_angular_basis.c:19-124) ----
 __host__ __device__ inline double gsf_diag_norm(int m)
 {

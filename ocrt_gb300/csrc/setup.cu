@@ -83,6 +83,8 @@ __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double 
     const int aer = d.mom_off >= 0 && d.tau_a > 0.0;
     const double ta = aer ? d.tau_a : 0.0;
     const double ah = d.aer_h_km > 0.0 ? d.aer_h_km : 2.0;
+    AboveEval E;
+    above_init(E, d.profile, d.ray_h_km, ah);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= nt; k += gridDim.x * blockDim.x) {
         const long long o = d.lev_off + k;
         const double hk = (double)k * tau / (double)nt;
@@ -96,16 +98,20 @@ __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double 
             const double f = hk / tau;
             if (!aer && f >= 1.0) zk = 0.0;
             else {
+                // Once the midpoint equals an end, every later step leaves
+                // 0.5 (lo + hi) at that midpoint, so the loop can stop there.
                 double lo = 0.0, hi = aer ? OCRT_ZTOP_KM : ztop;
+                const double target = aer ? hk : f;
+                zk = 0.5 * (lo + hi);
                 for (int it = 0; it < 64; ++it) {
                     const double mid = 0.5 * (lo + hi);
-                    const double above = aer ? tr * ray_above(mid, d.profile, d.ray_h_km) +
-                                                   ta * exp_above(mid, OCRT_ZTOP_KM, ah)
-                                             : ray_above(mid, d.profile, d.ray_h_km);
-                    const double target = aer ? hk : f;
+                    zk = mid;
+                    if (mid == lo || mid == hi) break;
+                    const double above = aer ? tr * above_ray(E, mid) + ta * above_exp(mid, ah, E.et_a)
+                                             : above_ray(E, mid);
                     if (above > target) lo = mid; else hi = mid;
+                    zk = 0.5 * (lo + hi);
                 }
-                zk = 0.5 * (lo + hi);
             }
         }
         z[o] = zk;
