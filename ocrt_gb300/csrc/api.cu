@@ -716,7 +716,9 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     for (Wave &w : g.waves) {
         const int nw = w.t1 - w.t0;
         if (!capture) w.fwd_stop = INT_MAX;
-        CK(cudaMemsetAsync(g.ops, 0, sizeof(float) * w.ops, st));
+        // the plain operators are read only off the forward tensor-core path; the
+        // molecular factors it reads are written in full by k_tables
+        if (!g.use_tc || g.ncot > 0) CK(cudaMemsetAsync(g.ops, 0, sizeof(float) * w.ops, st));
         CK(cudaMemsetAsync(g.pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (g.any_flat) CK(cudaMemsetAsync(g.fvec, 0, sizeof(float) * (size_t)nw * 24 * G.NR, st));
         CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));

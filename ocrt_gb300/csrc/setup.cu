@@ -513,6 +513,10 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
 #pragma unroll
             for (int q = 0; q < 24; ++q) Bop[(size_t)c * 24 + q] = u[q];
         }
+        // the view rows when the view is a Gauss node (the buffer is not cleared
+        // between waves on the tensor-core path)
+        if (n == N)
+            for (int e = threadIdx.x; e < 6 * 24; e += blockDim.x) Bop[(size_t)(6 * N) * 24 + e] = 0.f;
     }
 
     // ---- solar row: primary-source vectors and flat reflected-beam vectors ----
