@@ -55,7 +55,7 @@ __device__ inline float seed_scale(const PixDev &d, const TaskDev &tk)
     return (float)((tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0 * exp(-d.tau_total / d.mu0));
 }
 
-__global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
+__global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
 {
     const int tl = blockIdx.x, tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
@@ -111,7 +111,7 @@ __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
     const float rs = seeded ? W.srf[tk.srf_off + (size_t)G.NR * G.N * 9 + g * 9 + s * 3] : 0.f;
     // Step j visits level nt - j (upward) or j (downward); the per-level inputs
     // of PF steps are loaded before the dependent recurrence runs.
-    constexpr int PF = 8;
+    constexpr int PF = 4;
     float I = 0.f, Jp = 0.f;
     for (int j0 = 0; j0 <= nt; j0 += PF) {
         const int cnt = nt - j0 + 1 < PF ? nt - j0 + 1 : PF;
