@@ -136,3 +136,26 @@ def test_coxmunk_tensor_core_and_cuda_core_agree(gpu, oracle):
         assert abs(r_tc["rho_I"][i] - r_simt["rho_I"][i]) <= 2e-6 * abs(r_simt["rho_I"][i])
         assert abs(r_tc["rho_Q"][i] - r_simt["rho_Q"][i]) <= 1e-6
         assert abs(r_tc["rho_U"][i] - r_simt["rho_U"][i]) <= 1e-6
+
+
+def test_source_tensor_core_and_cuda_core_agree(gpu):
+    """The tcgen05 source pass (operators as pre-split tf32 tiles, 3xTF32) and
+    the CUDA-core source (FP32) give the same solve: m <= 2 tasks take the
+    dense molecular tiles; half the pixels interpolate the view (no view slot:
+    its operator tile rows are zero) and half carry it as a ring node."""
+    import os
+    from ocrt_gb300 import _abi as A
+    cs, os_, aa = _batch(24, seed=36, n_mu=32, m_max=8, L=60)
+    for i in range(len(cs)):
+        os_[i].view_as_node = i % 2
+    try:
+        os.environ["OCRT_GB_SOURCE_KERNEL"] = "simt"
+        r_simt = gpu.solve_batch(cs, os_, aa)
+    finally:
+        os.environ.pop("OCRT_GB_SOURCE_KERNEL", None)
+    r_tc = gpu.solve_batch(cs, os_, aa)
+    for i in range(len(cs)):
+        assert abs(r_tc["rho_I"][i] - r_simt["rho_I"][i]) <= 2e-6 * abs(r_simt["rho_I"][i]), i
+        assert abs(r_tc["rho_Q"][i] - r_simt["rho_Q"][i]) <= 1e-6, i
+        assert abs(r_tc["rho_U"][i] - r_simt["rho_U"][i]) <= 1e-6, i
+        assert abs(r_tc["order_modes"][i] - r_simt["order_modes"][i]) <= 2, i
