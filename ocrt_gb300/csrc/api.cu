@@ -1351,6 +1351,8 @@ int ocrt_gb_solve_case(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_ae
     return rc;
 }
 
+} // extern "C"
+
 namespace {
 
 // Level grid of one case as the solve builds it, copied back: optical depths,
@@ -1392,6 +1394,8 @@ int level_profile(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol
 }
 
 }  // namespace
+
+extern "C" {
 
 int ocrt_gb_layer_defaults(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
                            double *dtau, double *ssa)
