@@ -604,6 +604,14 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
                 }
             }
         }
+        // per-lane contributions of the PF levels of this batch: [row][quantity][level]
+        float v3[ADJ_RB][3][PF];
+#pragma unroll
+        for (int r = 0; r < ADJ_RB; ++r)
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+                for (int q = 0; q < PF; ++q) v3[r][x][q] = 0.f;
 #pragma unroll
         for (int q = 0; q < PF; ++q) {
             if (q >= cnt) break;                                            // warp-uniform
@@ -615,28 +623,47 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
             const float jt = jx[q] + j1v;
             const float lay = tt[q] * lt[q] + jt_prev * la[q] + jt * lb[q];
             jt_prev = valid ? jt : 0.f;
-            const int kl = h == 0 ? k - 1 : k;
 #pragma unroll
             for (int r = 0; r < ADJ_RB; ++r) {
                 if (r >= nr) break;                                         // block-uniform
-                float vs = 0.f, vj = 0.f, vl = 0.f;
                 if (valid) {
                     const float nu = (h == 1 && k == 0) ? 0.f : av[r][q] + tv[q] * nu_prev[r];
                     // h 0: mu = Ca_k nu_k + Cb_{k-1} nu_{k-1};  h 1: mu = Ca_{k-1} nu_k + Cb_k nu_{k+1}
                     const float mu = ca[q] * nu + cb[q] * nu_prev[r];
-                    vs = mu * jt;
-                    vj = mu * j1v;
-                    vl = nu_prev[r] * lay;
+                    v3[r][0][q] = mu * jt;
+                    v3[r][1][q] = mu * j1v;
+                    v3[r][2][q] = nu_prev[r] * lay;
                     nu_prev[r] = nu;
                 }
-                vs = warp_sum(vs);
-                vj = warp_sum(vj);
-                vl = warp_sum(vl);
-                if (lane == 0) {
+            }
+        }
+        // Sums over the warp's 32 columns for the four levels at once: halve
+        // the level set across lanes 16 and 8 apart (reduce-scatter), then
+        // finish with three butterfly steps; lane 8 (2 b16 + b8) ends with
+        // the total of level 2 b16 + b8, and lanes 0, 8, 16, 24 store them.
+        const int b16 = (lane >> 4) & 1, b8 = (lane >> 3) & 1;
+        const int qmine = 2 * b16 + b8;
+        const int kmine = h == 0 ? j1 + qmine : nt - j1 - qmine;
+        const int klmine = h == 0 ? kmine - 1 : kmine;
+#pragma unroll
+        for (int r = 0; r < ADJ_RB; ++r) {
+            if (r >= nr) break;                                             // block-uniform
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                const float *v = v3[r][x];
+                const float s0 = b16 ? v[0] : v[2], s1 = b16 ? v[1] : v[3];
+                const float r0 = __shfl_xor_sync(0xffffffffu, s0, 16), r1 = __shfl_xor_sync(0xffffffffu, s1, 16);
+                const float k0 = (b16 ? v[2] : v[0]) + r0, k1 = (b16 ? v[3] : v[1]) + r1;
+                const float se = b8 ? k0 : k1;
+                float tot = (b8 ? k1 : k0) + __shfl_xor_sync(0xffffffffu, se, 8);
+                tot += __shfl_xor_sync(0xffffffffu, tot, 4);
+                tot += __shfl_xor_sync(0xffffffffu, tot, 2);
+                tot += __shfl_xor_sync(0xffffffffu, tot, 1);
+                if ((lane & 7) == 0 && qmine < cnt) {
                     float *wr = ws + (size_t)r * 3 * L1;
-                    wr[k] += vs;
-                    wr[L1 + k] += vj;
-                    if (kl >= 0 && kl < nt) wr[2 * L1 + kl] += vl;
+                    if (x == 0) wr[kmine] += tot;
+                    else if (x == 1) wr[L1 + kmine] += tot;
+                    else if (klmine >= 0 && klmine < nt) wr[2 * L1 + klmine] += tot;
                 }
             }
         }
