@@ -677,13 +677,13 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
         const float *Xb = W.F + tk.fld_off + (size_t)nt * G.LDC;
         const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
         const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
-        double acc = 0.0;
+        float accf = 0.f;          // FP32 like the boundary condition it differentiates
         for (int i = 0; i < N; ++i) {
-            const double pw = pwm[i];
             const float *Ri = RW + (size_t)i * 9;
-            acc += pw * ((double)Ri[0] * Xb[col_of(G, 0, 1, i)] + (double)Ri[1] * Xb[col_of(G, 1, 1, i)] +
-                         (double)Ri[2] * Xb[col_of(G, 2, 1, i)]);
+            accf += pwm[i] * (Ri[0] * Xb[col_of(G, 0, 1, i)] + Ri[1] * Xb[col_of(G, 1, 1, i)] +
+                              Ri[2] * Xb[col_of(G, 2, 1, i)]);
         }
+        const double acc = accf;
         const double tdn = exp(-d.tau_total / d.mu0);
         const double fs = (tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0;
         const float *RsW = A.srfW + tk.srf_off + (size_t)G.NR * N * 9;
