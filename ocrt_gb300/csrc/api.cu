@@ -243,7 +243,7 @@ size_t wave_budget_bytes()
     const char *e = getenv("OCRT_GB_WAVE_BYTES");
     if (e && *e) return (size_t)strtoull(e, nullptr, 10);
     size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 0) return (size_t)(fr * 0.45);
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 0) return (size_t)(fr * 0.7);
     return (size_t)8 << 30;
 }
 
