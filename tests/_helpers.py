@@ -1,6 +1,6 @@
 """Shared helpers: oracle binding, fixture loading and the parity tolerance.
 
-Parity bar (spec accuracy statement): |rho_I - ref| <= 1e-5 * |ref|,
+Parity bar (the accuracy requirement of this path): |rho_I - ref| <= 1e-5 * |ref|,
 |rho_Q - ref| <= 1e-4 and |rho_U - ref| <= 1e-4.
 """
 import ctypes as C
