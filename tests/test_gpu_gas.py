@@ -188,3 +188,29 @@ def test_gas_adjoint_matches_finite_differences(gpu, oracle, states):
     for got, ref, what in ((g["d_dtau"][0, 0], fd[:n], "dtau"), (g["d_ssa"][0, 0], fd[n:], "ssa")):
         scale = np.max(np.abs(ref))
         assert np.max(np.abs(got - ref)) <= 1e-4 * scale + 1e-8, what
+
+
+def test_gas_loader_edge_cases_match_oracle(gpu, oracle, tmp_path):
+    """Missing cross-section table (gas left out), a caller's column, and a
+    malformed AFGL row, as in the oracle's loader."""
+    import shutil
+    root = tmp_path / "data"
+    shutil.copytree(GAS_DATA, root)
+    (root / "xsec" / "xsec_no2.dat").unlink()
+    ov = [-1.0, 300.0 * 2.6868e16, -1.0, -1.0, -1.0, -1.0]
+    g = gpu.GasState(str(root / "afgl_atm"), str(root / "xsec"), "tropical", ov)
+    h = oracle.gas_create(str(root), GAS_PROFILES["tropical"], ov)
+    try:
+        for wl in DOC["wavelengths"]:
+            pg, tg = g.tau(wl)
+            po, to = oracle.gas_tau(h, wl)
+            assert pg[4] == 0.0
+            np.testing.assert_allclose(pg, po, rtol=1e-12, atol=1e-300)
+            assert tg == pytest.approx(to, rel=1e-12)
+    finally:
+        g.close()
+        oracle.gas_destroy(h)
+    f = root / "afgl_atm" / "afgl_usstd76.dat"
+    f.write_text(f.read_text() + "  1.0 2.0 three\n")
+    with pytest.raises(gpu.OcrtError):
+        gpu.GasState(str(root / "afgl_atm"), str(root / "xsec"), "usstd76")

@@ -104,3 +104,55 @@ def test_gas_defaults_feed_the_layer_parameters(oracle):
 def test_missing_afgl_profile_is_an_error(oracle, tmp_path):
     with pytest.raises(RuntimeError):
         oracle.gas_create(str(tmp_path), 0)
+
+
+def test_missing_cross_section_table_leaves_the_gas_out(oracle, tmp_path):
+    """rt_absorption.c:500-515: a missing xsec file contributes zero absorption
+    for that gas; the other gases are unchanged."""
+    import shutil
+    root = tmp_path / "data"
+    shutil.copytree(GAS_DATA, root)
+    (root / "xsec" / "xsec_o3.dat").unlink()
+    full = oracle.gas_create(GAS_DATA, 0)
+    part = oracle.gas_create(str(root), 0)
+    try:
+        for wl in (443.0, 600.3):
+            pf, _ = oracle.gas_tau(full, wl)
+            pp, tp = oracle.gas_tau(part, wl)
+            assert pp[1] == 0.0
+            np.testing.assert_array_equal(np.delete(pp, 1), np.delete(pf, 1))
+            assert tp == pytest.approx(pf.sum() - pf[1], rel=1e-14)
+    finally:
+        oracle.gas_destroy(full)
+        oracle.gas_destroy(part)
+
+
+def test_column_override_scales_the_profile(oracle):
+    """A caller's column rescales that gas's layers in proportion
+    (rt_absorption.c:566-583): the depth scales by column / default."""
+    h0 = oracle.gas_create(GAS_DATA, 0)
+    try:
+        _, dflt, _ = oracle.gas_columns(h0)
+        ov = [-1.0] * 6
+        ov[1] = 2.0 * dflt[1]
+        h1 = oracle.gas_create(GAS_DATA, 0, ov)
+        try:
+            for wl in (330.0, 555.0, 600.3):
+                p0, _ = oracle.gas_tau(h0, wl)
+                p1, _ = oracle.gas_tau(h1, wl)
+                assert p1[1] == pytest.approx(2.0 * p0[1], rel=1e-12)
+                np.testing.assert_array_equal(np.delete(p1, 1), np.delete(p0, 1))
+        finally:
+            oracle.gas_destroy(h1)
+    finally:
+        oracle.gas_destroy(h0)
+
+
+def test_malformed_afgl_row_is_an_error(oracle, tmp_path):
+    import shutil
+    root = tmp_path / "data"
+    shutil.copytree(GAS_DATA, root)
+    f = root / "afgl_atm" / "afgl_usstd76.dat"
+    f.write_text(f.read_text() + "  1.0 2.0 three\n")
+    with pytest.raises(RuntimeError):
+        oracle.gas_create(str(root), 0)
