@@ -129,11 +129,11 @@ __global__ void k_adj_prep(BatchBufs B, WaveBufs W, Geom G, int t0)
     decode_col_a(G, c, s, h, g);
     if (g >= d.n_ring) return;
     float *F = W.F + tk.fld_off;
-    const float2 *Tot = W.Tot + tk.fld_off;
+    const float *Tot = W.Tot + tk.fld_off;
     for (int k = 0; k <= d.nt; ++k) {
         const size_t o = (size_t)k * G.LDC + c;
-        const float2 t = Tot[o];
-        F[o] = (t.x - F[o]) + t.y;
+        const float lo = (k == 0 || k == d.nt) ? W.Ttl[tot_tail_off(tk, G, k, c)] : 0.f;
+        F[o] = (Tot[o] - F[o]) + lo;
     }
 }
 
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
     const float *lv = B.lvf + 3 * (size_t)d.lev_off;                 // x, y, ch per level
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
     const float *Jx = W.J + tk.fld_off;
-    const float2 *Tot = W.Tot + tk.fld_off;
+    const float *Tot = W.Tot + tk.fld_off;
     // Threads [0, half) take the upward columns (h = 0), [half, 2 half) the
     // downward ones, so every warp runs one direction; half = round32(3N + 3).
     const int half = blockDim.x >> 1;
@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
                 for (int r = 0; r < ADJ_RB; ++r)
                     if (r < nr) av[r][q] = At[r][o];
                 jx[q] = Jx[o];
-                tt[q] = Tot[o].x;
+                tt[q] = Tot[o];
                 xk[q] = lv[3 * k]; yk[q] = lv[3 * k + 1]; chk[q] = lv[3 * k + 2];
                 if (h == 0) {
                     tv[q] = k > 0 ? Tc[(k - 1) * NR + g] : 0.f;

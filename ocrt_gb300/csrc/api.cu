@@ -216,7 +216,7 @@ struct Group {
     float *cstiles = nullptr;    // its cos/sin B tiles, split and swizzled
     int ncmpairs = 0;
     float *pvec = nullptr, *fvec = nullptr, *srf = nullptr, *Bx = nullptr;
-    float2 *Tot = nullptr;
+    float *Tot = nullptr, *Ttl = nullptr;
     bool use_tc = false;
     // per-layer overrides and the adjoint (ocrt_gb_solve_batch_adjoint)
     bool any_layers = false;
@@ -290,7 +290,7 @@ void free_group(Group &g)
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.tabs, g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
-                    g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot,
+                    g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.Ttl,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
@@ -456,7 +456,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
         (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
         (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
-        (rc = alloc(g.Tot, g.wave_fld)) ||
+        (rc = alloc(g.Tot, g.wave_fld)) || (rc = alloc(g.Ttl, g.wave_fld)) ||
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
         (rc = alloc(g.srf, g.wave_srf)) ||
@@ -708,7 +708,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     B.molV = g.molV;
     WaveBufs W;
-    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.ops = g.ops; W.opt = g.use_tc ? g.opt : nullptr;
+    W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.Ttl = g.Ttl; W.ops = g.ops; W.opt = g.use_tc ? g.opt : nullptr;
     W.pvec = g.pvec;
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;

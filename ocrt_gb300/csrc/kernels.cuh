@@ -15,9 +15,9 @@ __global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const 
 __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt);
 __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx);
 // k_scan: levels in flight per column (cp.async ring depth, a power of two)
-// and its dynamic shared memory: J, the float2 total and 3 coefficients per slot.
+// and its dynamic shared memory: J, the total's FP32 head and 3 coefficients per slot.
 #define SCAN_DEPTH 8
-inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (4 + 8 + 12); }
+inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (4 + 4 + 12); }
 // k_adj_scan: cotangent rows per block (they share the transport coefficients)
 #define ADJ_RB 3
 inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 4) + 12); }
@@ -70,13 +70,29 @@ __global__ void k_level_float(const PixDev *px, int P, const double *xd, const d
 struct WaveBufs {
     float *F;              // field of the current order (FP32), wave-relative by TaskDev::fld_off
     float *J;              // source of the current order
-    float2 *Tot;           // order totals (hi, lo) pairs
+    float *Tot;            // order totals, FP32 head at every level (convergence norm, adjoint)
+    float *Ttl;            // tails of the totals at the output levels: row 0 (k = 0) and row 1
+                           // (k = nt) of each task's block, so (Tot, Ttl) is a double-float there
     float *ops;            // operators, wave-relative (FP32)
     float *opt;            // tensor-core path: the aerosol and dense molecular operators pre-split into
                            // tf32 (hi, lo) SWIZZLE_128B tiles at 2 x op_off / 2 x uv_off (tile_put)
     float *pvec, *fvec;    // per wave-task primary and flat-beam vectors
     float *srf;            // rough surface kernels, wave-relative
 };
+// The outputs read the totals only at the TOA (k = 0) and the BOA (k = nt);
+// there they are double-floats (head in Tot, tail in Ttl).  Interior levels
+// feed only the FP32 convergence norm and the adjoint, so they keep the FP32
+// head alone, which saves the scan 8 B per element and order.
+__device__ inline size_t tot_tail_off(const TaskDev &tk, const Geom &G, int k, int c)
+{
+    return (size_t)tk.fld_off + (k == 0 ? 0 : (size_t)G.LDC) + c;
+}
+__device__ inline double tot_value(const WaveBufs &W, const TaskDev &tk, const Geom &G, int k, int nt, int c)
+{
+    const float hi = W.Tot[(size_t)tk.fld_off + (size_t)k * G.LDC + c];
+    const float lo = (k == 0 || k == nt) ? W.Ttl[tot_tail_off(tk, G, k, c)] : 0.f;
+    return (double)hi + (double)lo;
+}
 struct BatchBufs {
     const PixDev *px;
     const TaskDev *tasks;

@@ -91,7 +91,6 @@ __global__ void k_lut_sample(BatchBufs B, WaveBufs W, LutBufs Lb, Geom G, int t0
         vpos = 0;
         while (vpos < N && B.gmu[vpos] < d.mu_view) ++vpos;
     }
-    const float2 *Tot = W.Tot + tk.fld_off;
     const float fs_tdn = d.rough ? (float)((tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0 *
                                            exp(-d.tau_total / d.mu0)) : 0.f;
     const float *Rs = d.rough ? W.srf + tk.srf_off + (size_t)G.NR * G.N * 9 : nullptr;
@@ -101,11 +100,11 @@ __global__ void k_lut_sample(BatchBufs B, WaveBufs W, LutBufs Lb, Geom G, int t0
         else slot = j < vpos ? j : (j == vpos ? N : j - 1);
         xr[j] = slot < N ? B.gmu[slot] : d.mu_view;
         for (int s = 0; s < 3; ++s) {
-            double v = df_value(Tot[col_of(G, s, 0, slot)]);
+            double v = tot_value(W, tk, G, 0, d.nt, col_of(G, s, 0, slot));
             if (d.rough) v -= (double)(fs_tdn * B.Eatt[d.lev_off * G.NR + slot] * Rs[slot * 9 + s * 3]);
             yr[s][j] = v;
         }
-        yr[3][j] = df_value(Tot[(size_t)d.nt * G.LDC + col_of(G, 0, 1, slot)]);
+        yr[3][j] = tot_value(W, tk, G, d.nt, d.nt, col_of(G, 0, 1, slot));
     }
     __syncthreads();
     for (int iv = threadIdx.x; iv < d.lut_nv; iv += blockDim.x) {

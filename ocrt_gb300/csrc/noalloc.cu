@@ -165,7 +165,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     if (Wt < 1) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
     float *F = cv.take<float>((size_t)Wt * K * G.LDC);
     float *J = cv.take<float>((size_t)Wt * K * G.LDC);
-    float2 *Tot = cv.take<float2>((size_t)Wt * K * G.LDC);
+    float *Tot = cv.take<float>((size_t)Wt * K * G.LDC);
+    float *Ttl = cv.take<float>((size_t)Wt * K * G.LDC);
     float *ops = cv.take<float>(2 * (size_t)Wt * op_elems);
     float *pvec = cv.take<float>((size_t)Wt * 2 * G.LDC);
     float *fvec = cv.take<float>((size_t)Wt * 24 * NR);
@@ -222,7 +223,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work; B.molV = nullptr;
     B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
-    W.F = F; W.J = J; W.Tot = Tot; W.ops = ops; W.opt = nullptr; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
+    W.F = F; W.J = J; W.Tot = Tot; W.Ttl = Ttl; W.ops = ops; W.opt = nullptr; W.pvec = pvec; W.fvec = flat ? fvec : nullptr; W.srf = srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     for (int t0 = 0; t0 < T; t0 += Wt) {
         const int nw = (T - t0) < Wt ? (T - t0) : Wt;

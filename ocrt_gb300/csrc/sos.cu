@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geo
     const float *pv = W.pvec + (size_t)tl * 2 * G.LDC;
     const double aP = pv[c], mP = pv[G.LDC + c];
     float *F = W.F + tk.fld_off;
-    float2 *Tot = W.Tot + tk.fld_off;
+    float *Tot = W.Tot + tk.fld_off;
     const double *hh = B.h + d.lev_off;
     const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
     const int NR = G.NR;
@@ -144,7 +144,8 @@ __global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geo
                 float2 t = make_float2(I, 0.f);
                 if (seeded) t = df_add(t, fs_tdn * ea[q] * rs);
                 F[(size_t)k * G.LDC + c] = t.x;
-                Tot[(size_t)k * G.LDC + c] = t;
+                Tot[(size_t)k * G.LDC + c] = t.x;
+                if (k == 0 || k == nt) W.Ttl[tot_tail_off(tk, G, k, c)] = t.y;
             }
         }
     }
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
     const bool valid = c < G.COUT && g < d.n_ring;
     float *F = W.F + tk.fld_off;
     const float *J = W.J + tk.fld_off;
-    float2 *Tot = W.Tot + tk.fld_off;
+    float *Tot = W.Tot + tk.fld_off;
     // ---- surface boundary condition from the previous order's BOA downward field
     float bc = 0.f;
     if (valid && h == 0 && d.surf_on) {
@@ -361,15 +362,15 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         // values read from it have been used.
         const int bs = blockDim.x;
         float *Js = scan_smem;                                             // [SCAN_DEPTH][bs]
-        float2 *Ts = reinterpret_cast<float2 *>(Js + SCAN_DEPTH * bs);      // [SCAN_DEPTH][bs]
-        float *Cs = reinterpret_cast<float *>(Ts + SCAN_DEPTH * bs);        // [SCAN_DEPTH][3][bs]
+        float *Ts = Js + SCAN_DEPTH * bs;                                  // [SCAN_DEPTH][bs]
+        float *Cs = Ts + SCAN_DEPTH * bs;                                  // [SCAN_DEPTH][3][bs]
         const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
         auto issue = [&](int j) {
             if (j <= nt) {
                 const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
                 const size_t o = (size_t)k * G.LDC + c;
                 cp_async4(Js + sl * bs + c, J + o);
-                cp_async8(Ts + sl * bs + c, Tot + o);
+                cp_async4(Ts + sl * bs + c, Tot + o);
                 if (j > 0) {
                     const int e = (h == 0 ? k : k - 1) * NR + g;
                     cp_async4(Cs + (sl * 3 + 0) * bs + c, Tc + e);
@@ -381,21 +382,31 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         };
 #pragma unroll
         for (int j = 0; j < SCAN_DEPTH; ++j) issue(j);
+        // tails of the TOA and BOA totals (double-float output levels)
+        float *tl0 = W.Ttl + tot_tail_off(tk, G, 0, c), *tlN = W.Ttl + tot_tail_off(tk, G, nt, c);
+        const float lo0 = *tl0, loN = *tlN;
         float I = h == 0 ? bc : 0.f, Jp = 0.f;
         for (int j = 0; j <= nt; ++j) {
             cp_async_wait<SCAN_DEPTH - 1>();
             const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
             const float jv = Js[sl * bs + c];
-            const float2 ov = Ts[sl * bs + c];
+            const float ov = Ts[sl * bs + c];
             if (j > 0)
                 I = Cs[(sl * 3 + 0) * bs + c] * I + Cs[(sl * 3 + 1) * bs + c] * jv + Cs[(sl * 3 + 2) * bs + c] * Jp;
             Jp = jv;
             const size_t o = (size_t)k * G.LDC + c;
             F[o] = I;
-            const float2 t = df_add(ov, I);
+            float t;
+            if (k == 0 || k == nt) {
+                const float2 td = df_add(make_float2(ov, k == 0 ? lo0 : loN), I);
+                t = td.x;
+                *(k == 0 ? tl0 : tlN) = td.y;
+            } else {
+                t = ov + I;
+            }
             Tot[o] = t;
             mi = fmaxf(mi, fabsf(I));
-            mt = fmaxf(mt, fabsf(t.x));
+            mt = fmaxf(mt, fabsf(t));
             issue(j + SCAN_DEPTH);
         }
         cp_async_wait<0>();
@@ -439,15 +450,14 @@ __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
     const int tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
-    const float2 *Tot = W.Tot + tk.fld_off;
     const int nt = d.nt, N = G.N, vs = d.view_slot;
     const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
     auto up0 = [&](int s, int g) -> double {
-        double v = df_value(Tot[col_of(G, s, 0, g)]);
+        double v = tot_value(W, tk, G, 0, nt, col_of(G, s, 0, g));
         if (d.rough) v -= (double)rough_seed(tk, W, B, d, G, fs_tdn, 0, g, s);
         return v;
     };
-    auto dn = [&](int g) -> double { return df_value(Tot[(size_t)nt * G.LDC + col_of(G, 0, 1, g)]); };
+    auto dn = [&](int g) -> double { return tot_value(W, tk, G, nt, nt, col_of(G, 0, 1, g)); };
     TaskOut o;
     if (vs >= 0) {
         o.vI = up0(0, vs); o.vQ = up0(1, vs); o.vU = up0(2, vs);
