@@ -327,6 +327,42 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
     float *F = W.F + tk.fld_off;
     const float *J = W.J + tk.fld_off;
     float *Tot = W.Tot + tk.fld_off;
+    // Each column walks its nt + 1 levels in its transport direction (step
+    // j: level nt - j upward, j downward).  The J, total and coefficient
+    // values of the next SCAN_DEPTH steps are in flight as cp.async copies
+    // into this thread's own shared-memory slots, so the recurrence never
+    // waits on a memory round trip; a slot is refilled only after the
+    // values read from it have been used.
+    const int bs = blockDim.x;
+    float *Js = scan_smem;                                             // [SCAN_DEPTH][bs]
+    float *Ts = Js + SCAN_DEPTH * bs;                                  // [SCAN_DEPTH][bs]
+    float *Cs = Ts + SCAN_DEPTH * bs;                                  // [SCAN_DEPTH][3][bs]
+    const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+    auto issue = [&](int j) {
+        if (j <= nt) {
+            const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
+            const size_t o = (size_t)k * G.LDC + c;
+            cp_async4(Js + sl * bs + c, J + o);
+            cp_async4(Ts + sl * bs + c, Tot + o);
+            if (j > 0) {
+                const int e = (h == 0 ? k : k - 1) * NR + g;
+                cp_async4(Cs + (sl * 3 + 0) * bs + c, Tc + e);
+                cp_async4(Cs + (sl * 3 + 1) * bs + c, Ca + e);
+                cp_async4(Cs + (sl * 3 + 2) * bs + c, Cb + e);
+            }
+        }
+        cp_async_commit();
+    };
+    // tails of the TOA and BOA totals (double-float output levels)
+    float *tl0 = W.Ttl + tot_tail_off(tk, G, 0, c), *tlN = W.Ttl + tot_tail_off(tk, G, nt, c);
+    float lo0 = 0.f, loN = 0.f;
+    // the first ring copies and the tails are in flight while the boundary
+    // condition below is summed (they read J and the totals, not F)
+    if (valid) {
+#pragma unroll
+        for (int j = 0; j < SCAN_DEPTH; ++j) issue(j);
+        lo0 = *tl0; loN = *tlN;
+    }
     // ---- surface boundary condition from the previous order's BOA downward field
     float bc = 0.f;
     if (valid && h == 0 && d.surf_on) {
@@ -354,37 +390,6 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
     float mi = 0.f, mt = 0.f;
     int bad = 0;
     if (valid) {
-        // Each column walks its nt + 1 levels in its transport direction (step
-        // j: level nt - j upward, j downward).  The J, total and coefficient
-        // values of the next SCAN_DEPTH steps are in flight as cp.async copies
-        // into this thread's own shared-memory slots, so the recurrence never
-        // waits on a memory round trip; a slot is refilled only after the
-        // values read from it have been used.
-        const int bs = blockDim.x;
-        float *Js = scan_smem;                                             // [SCAN_DEPTH][bs]
-        float *Ts = Js + SCAN_DEPTH * bs;                                  // [SCAN_DEPTH][bs]
-        float *Cs = Ts + SCAN_DEPTH * bs;                                  // [SCAN_DEPTH][3][bs]
-        const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
-        auto issue = [&](int j) {
-            if (j <= nt) {
-                const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
-                const size_t o = (size_t)k * G.LDC + c;
-                cp_async4(Js + sl * bs + c, J + o);
-                cp_async4(Ts + sl * bs + c, Tot + o);
-                if (j > 0) {
-                    const int e = (h == 0 ? k : k - 1) * NR + g;
-                    cp_async4(Cs + (sl * 3 + 0) * bs + c, Tc + e);
-                    cp_async4(Cs + (sl * 3 + 1) * bs + c, Ca + e);
-                    cp_async4(Cs + (sl * 3 + 2) * bs + c, Cb + e);
-                }
-            }
-            cp_async_commit();
-        };
-#pragma unroll
-        for (int j = 0; j < SCAN_DEPTH; ++j) issue(j);
-        // tails of the TOA and BOA totals (double-float output levels)
-        float *tl0 = W.Ttl + tot_tail_off(tk, G, 0, c), *tlN = W.Ttl + tot_tail_off(tk, G, nt, c);
-        const float lo0 = *tl0, loN = *tlN;
         float I = h == 0 ? bc : 0.f, Jp = 0.f;
         for (int j = 0; j <= nt; ++j) {
             cp_async_wait<SCAN_DEPTH - 1>();
