@@ -275,19 +275,27 @@ __global__ void __launch_bounds__(256) k_mol_lowrank(BatchBufs B, WaveBufs W, Ge
     }
 }
 
-__device__ inline float block_maxf(float v, float *red)
+// Block-wide maxima of two values at once (thread 0 holds the result).
+__device__ inline float2 block_maxf2(float a, float b, float2 *red)
 {
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
-    if (l == 0) red[w] = v;
+    if (l == 0) red[w] = make_float2(a, b);
     __syncthreads();
     if (w == 0) {
         const int nw = (blockDim.x + 31) >> 5;
-        v = l < nw ? red[l] : 0.f;
-        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        const float2 v = l < nw ? red[l] : make_float2(0.f, 0.f);
+        a = v.x; b = v.y;
+        for (int o = 16; o > 0; o >>= 1) {
+            a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
     }
-    return v;
+    return make_float2(a, b);
 }
 
 __device__ inline double block_max(double v, double *red)
@@ -307,7 +315,7 @@ __device__ inline double block_max(double v, double *red)
 
 __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
 {
-    __shared__ float redf[32];
+    __shared__ float2 redf2[32];
     extern __shared__ float scan_smem[];
     __shared__ int item_s;
     const int n_items = B.active_cnt[it - 1];
@@ -418,9 +426,8 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         bad = !isfinite(I);
     }
     if (bad) atomicExch(B.err, -2);
-    mi = block_maxf(mi, redf);
-    __syncthreads();
-    mt = block_maxf(mt, redf);
+    const float2 mm = block_maxf2(mi, mt, redf2);
+    mi = mm.x; mt = mm.y;
     if (threadIdx.x == 0) {
         TaskState ns = st;
         ns.orders = it;
