@@ -204,17 +204,23 @@ int  ocrt_gb_plan_kernel_stats(ocrt_plan *plan, int cls, const char **name, doub
  * memory: an application that owns the whole device budget through its own
  * pool allocator and forbids any other cudaMalloc/cudaFree, or a latency-bound
  * loop that cannot afford the implicit device synchronisation of cudaMalloc
- * and cudaFree.  Same inputs, outputs and results as ocrt_gb_solve_case, but
- * every device buffer lives in one fixed 32 MiB __device__ array that each GPU
+ * and cudaFree.  Same inputs and outputs as ocrt_gb_solve_case; it runs the
+ * CUDA-core source and Cox-Munk kernels of the allocating path (which takes
+ * the tensor-core ones where it can), so results agree with
+ * ocrt_gb_solve_case to the parity tolerance rather than bit for bit.  Every
+ * device buffer lives in one fixed 32 MiB __device__ array that each GPU
  * loading this library holds until exit; no cudaMalloc, cudaFree or pinned
  * host allocation is made.  Limits: n_mu <= 32, n_layers <= 400,
  * fourier_m_max <= 32, aerosol L_max <= 255, max_orders <= 4096; larger
  * requests return OCRT_ERR_ARGS with a message.  The first call on a device
  * looks up the array's address (cudaGetSymbolAddress) with that device
- * current, so make it before any stream capture.  All calls share the array:
- * each call clears what must start at zero, and calls whose GPU work overlaps
- * race on it and must be serialised by the caller.  stream: a cudaStream_t as
- * void* (NULL = the default stream). */
+ * current.  Every call synchronises its stream and polls device counters, so
+ * it must never be called while a stream is being captured.  All calls share
+ * the array: each call clears what must start at zero, and calls whose GPU
+ * work overlaps race on it and must be serialised by the caller (calls in
+ * one process are serialised by a lock; a call that fails after queuing work
+ * waits for that work before returning).  stream: a cudaStream_t as void*
+ * (NULL = the default stream). */
 int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *opts,
                                const ocrt_aerosol *aer, ocrt_result *out,
                                void *stream);

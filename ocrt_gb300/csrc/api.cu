@@ -162,6 +162,7 @@ struct Wave {
     int Kmax;
     size_t fld, ops, srf;  // element counts of the wave buffers
     bool any_rough, any_flat;
+    size_t tail = 0;       // element count of the total-tail rows (2 * LDC per task)
     int n_simt = 0, n_tc = 0, n_mol = 0;   // tasks given to each source kernel
     // Last order run before every task was found converged (forward orders,
     // adjoint orders); INT_MAX when the loop ran to max_orders.  Recorded by
@@ -192,7 +193,7 @@ struct Group {
     int Lmax = 2, Mmax = 0, max_orders = 1, nphi = 1024;
     bool any_pssa = false, any_rough = false, any_flat = false, any_gas = false;
     size_t nlev = 0, ncoef = 0, nmom = 0;
-    size_t wave_fld = 0, wave_ops = 0, wave_srf = 0;
+    size_t wave_fld = 0, wave_ops = 0, wave_srf = 0, wave_tail = 0;
     int wave_tasks = 0;
     // device
     PixDev *px = nullptr; TaskDev *tasks = nullptr; TaskState *state = nullptr; TaskOut *tout = nullptr;
@@ -396,6 +397,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         w.t1 = pend < g.P ? g.hpx[pend].task0 : g.T;
         g.waves.push_back(w);
         g.wave_fld = std::max(g.wave_fld, w.fld); g.wave_ops = std::max(g.wave_ops, w.ops);
+        g.wave_tail = std::max(g.wave_tail, w.tail);
         g.wave_srf = std::max(g.wave_srf, w.srf); g.wave_tasks = std::max(g.wave_tasks, w.t1 - w.t0);
     };
     for (int q = 0; q < g.P; ++q) {
@@ -405,7 +407,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         const size_t pf = nm * K * G.LDC;
         const size_t po = (nm + 2 * std::min<size_t>(nm, 3)) * op_elems;
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
-        size_t pb = pf * 16 + po * (tiles ? 12 : 4) + ps * 4 + nm * (2 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        size_t pb = pf * 12 + po * (tiles ? 12 : 4) + ps * 4 + nm * (4 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 12 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)2 * (G.CIN + 32) * ((G.COUT + 31) & ~31) * 4;
@@ -417,6 +419,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         TaskDev *tk = &g.htask[d.task0];
         for (size_t m = 0; m < nm; ++m) {
             tk[m].fld_off = (long long)w.fld; w.fld += K * G.LDC;
+            tk[m].tail_off = (long long)w.tail; w.tail += 2 * (size_t)G.LDC;
             tk[m].op_off = (long long)w.ops; w.ops += op_elems;
             if (m <= 2) {
                 tk[m].mol_off = (long long)w.ops; w.ops += op_elems;
@@ -456,7 +459,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
         (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
         (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
-        (rc = alloc(g.Tot, g.wave_fld)) || (rc = alloc(g.Ttl, g.wave_fld)) ||
+        (rc = alloc(g.Tot, g.wave_fld)) || (rc = alloc(g.Ttl, g.wave_tail)) ||
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
         (rc = alloc(g.srf, g.wave_srf)) ||

@@ -61,6 +61,7 @@ struct TaskDev {
     long long mol_off;      // wave-relative offset of the molecular operator factor U [COUT][24], -1 if none
     long long uv_off;       // wave-relative offset of the dense molecular operator U V [NP][CIN], -1 if none
     long long srf_off;      // wave-relative offset of the surface kernels (NR*N*9 + NR*9), -1 if none
+    long long tail_off;     // wave-relative offset of the total's tails at the TOA and BOA (2 * LDC entries)
 };
 
 // Per-task mutable SOS state.

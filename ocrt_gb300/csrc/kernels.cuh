@@ -71,8 +71,9 @@ struct WaveBufs {
     float *F;              // field of the current order (FP32), wave-relative by TaskDev::fld_off
     float *J;              // source of the current order
     float *Tot;            // order totals, FP32 head at every level (convergence norm, adjoint)
-    float *Ttl;            // tails of the totals at the output levels: row 0 (k = 0) and row 1
-                           // (k = nt) of each task's block, so (Tot, Ttl) is a double-float there
+    float *Ttl;            // tails of the totals at the output levels: two rows per task at
+                           // TaskDev::tail_off, row 0 for k = 0 and row 1 for k = nt, so
+                           // (Tot, Ttl) is a double-float there
     float *ops;            // operators, wave-relative (FP32)
     float *opt;            // tensor-core path: the aerosol and dense molecular operators pre-split into
                            // tf32 (hi, lo) SWIZZLE_128B tiles at 2 x op_off / 2 x uv_off (tile_put)
@@ -85,7 +86,7 @@ struct WaveBufs {
 // head alone, which saves the scan 8 B per element and order.
 __device__ inline size_t tot_tail_off(const TaskDev &tk, const Geom &G, int k, int c)
 {
-    return (size_t)tk.fld_off + (k == 0 ? 0 : (size_t)G.LDC) + c;
+    return (size_t)tk.tail_off + (k == 0 ? 0 : (size_t)G.LDC) + c;
 }
 __device__ inline double tot_value(const WaveBufs &W, const TaskDev &tk, const Geom &G, int k, int nt, int c)
 {

@@ -4,22 +4,30 @@
 // the whole device budget through its own pool allocator and forbids any
 // other cudaMalloc/cudaFree, or a latency-bound loop that cannot afford the
 // implicit device synchronisation cudaMalloc/cudaFree imply.  For them,
-// ocrt_gb_solve_case_noalloc runs the same kernels as ocrt_gb_solve_case with
-// every device buffer carved from g_noalloc_scratch, a fixed file-scope
-// __device__ array of OCRT_NOALLOC_BYTES that each GPU loading this library
-// holds until process exit.  Host staging uses the stack only.
+// ocrt_gb_solve_case_noalloc solves one pixel with the CUDA-core kernels of
+// the allocating path (k_source_simt and k_mol_lowrank for the source,
+// k_coxmunk for the rough surface; ocrt_gb_solve_case takes the tensor-core
+// kernels k_source_tc and k_coxmunk_tc where it can, so the two agree to the
+// parity tolerance, not bit for bit), with every device buffer carved from
+// g_noalloc_scratch, a fixed file-scope __device__ array of OCRT_NOALLOC_BYTES
+// that each GPU loading this library holds until process exit.  Host staging
+// uses the stack only.
 //
 // Contract:
 //  * limits: n_mu <= 32, n_layers <= 400, fourier_m_max <= 32, aerosol
 //    L_max <= 255, max_orders <= 4096, and the case's working set must fit
 //    the array; larger requests are rejected with OCRT_ERR_ARGS and a message.
 //  * the first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress while that device is current; make that first call
-//    before any stream capture.
+//    cudaGetSymbolAddress (and sets the kernels' shared-memory limits) while
+//    that device is current.
+//  * every call synchronises its stream and polls device counters from the
+//    host, so no call may be made while a stream is being captured.
 //  * every call shares the one array and leaves its contents behind; each
 //    call clears what must start at zero.  Calls whose GPU work overlaps
 //    (different host threads, or streams that run concurrently) race on the
-//    array and must be serialised by the caller.
+//    array and must be serialised by the caller.  In-process calls are
+//    serialised by a mutex, and a call that fails after it has queued work
+//    waits for that work before it returns.
 #include <cuda_runtime.h>
 #include <cstring>
 #include <mutex>
@@ -58,14 +66,22 @@ struct Carver {
     }
 };
 
+// Failure exits: once work is queued on the stream (enq), wait for it before
+// returning, so that the next call does not reuse the array under it.
 #define NA_CK(call)                                                                  \
     do {                                                                             \
-        if ((call) != cudaSuccess) return ocrt_internal_fail(OCRT_ERR_DEVICE, "noalloc: " #call " failed"); \
+        if ((call) != cudaSuccess) {                                                 \
+            if (enq) (void)cudaStreamSynchronize(st);                                \
+            return ocrt_internal_fail(OCRT_ERR_DEVICE, "noalloc: " #call " failed"); \
+        }                                                                            \
     } while (0)
 #define NA_LAUNCH(...)                                                               \
     do {                                                                             \
         __VA_ARGS__;                                                                 \
-        if (cudaGetLastError() != cudaSuccess) return ocrt_internal_fail(OCRT_ERR_DEVICE, "noalloc: kernel launch failed"); \
+        if (cudaGetLastError() != cudaSuccess) {                                     \
+            if (enq) (void)cudaStreamSynchronize(st);                                \
+            return ocrt_internal_fail(OCRT_ERR_DEVICE, "noalloc: kernel launch failed"); \
+        }                                                                            \
     } while (0)
 
 } // namespace
@@ -81,6 +97,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         (aer && aer->L_max > NA_MAX_L) || opts->max_orders > NA_MAX_ORDERS)
         return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static-scratch limits "
                                                  "(n_mu<=32, n_layers<=400, m_max<=32, L_max<=255, max_orders<=4096)");
+    cudaStream_t st = (cudaStream_t)stream;
+    bool enq = false;
     int dev = 0;
     NA_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= NA_MAX_DEVICES) return ocrt_internal_fail(OCRT_ERR_DEVICE, "noalloc: device index too large");
@@ -89,14 +107,13 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) return ocrt_internal_fail(OCRT_ERR_DEVICE, "noalloc: cudaGetSymbolAddress failed");
+        NA_CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NA_CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NA_CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NA_CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        NA_CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         g_na_base[dev] = p;
     }
-    cudaStream_t st = (cudaStream_t)stream;
-    NA_CK(cudaFuncSetAttribute(k_coxmunk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    NA_CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    NA_CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    NA_CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    NA_CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
 
     // ---- host staging (stack only) ----
     const int N = opts->n_mu, M = opts->fourier_m_max, T = M + 1, nt = opts->n_layers, K = nt + 1;
@@ -157,7 +174,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     int *err = cv.take<int>(1);
     float *srf = cv.take<float>(rough ? (size_t)T * srf_elems : 1);
     if (!cv.ok) return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static scratch size");
-    const size_t per_task = (size_t)K * G.LDC * 16 + 2 * op_elems * 4 + (size_t)2 * G.LDC * 4 +
+    const size_t per_task = (size_t)K * G.LDC * 12 + 2 * op_elems * 4 + (size_t)4 * G.LDC * 4 +
                             (size_t)24 * NR * 4 + (size_t)6 * (L + 1) * 4 + 8 * 256;
     const size_t left = cv.cap - ((cv.off + 255) & ~size_t(255));
     int Wt = (int)(left / per_task);
@@ -166,7 +183,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     float *F = cv.take<float>((size_t)Wt * K * G.LDC);
     float *J = cv.take<float>((size_t)Wt * K * G.LDC);
     float *Tot = cv.take<float>((size_t)Wt * K * G.LDC);
-    float *Ttl = cv.take<float>((size_t)Wt * K * G.LDC);
+    float *Ttl = cv.take<float>((size_t)Wt * 2 * G.LDC);
     float *ops = cv.take<float>(2 * (size_t)Wt * op_elems);
     float *pvec = cv.take<float>((size_t)Wt * 2 * G.LDC);
     float *fvec = cv.take<float>((size_t)Wt * 24 * NR);
@@ -181,12 +198,14 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         memset(&ht[m], 0, sizeof(TaskDev));
         ht[m].pix = 0; ht[m].m = m; ht[m].K = K; ht[m].has_mol = m <= 2;
         ht[m].fld_off = (long long)q * K * G.LDC;
+        ht[m].tail_off = (long long)q * 2 * G.LDC;
         ht[m].op_off = (long long)(2 * q) * (long long)op_elems;
         ht[m].mol_off = m <= 2 ? (long long)(2 * q + 1) * (long long)op_elems : -1;
         ht[m].uv_off = -1;
         ht[m].srf_off = rough ? (long long)m * (long long)srf_elems : -1;
     }
     const int zero = 0;
+    enq = true;
     NA_CK(cudaMemcpyAsync(px, &d, sizeof(PixDev), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(tasks, ht, sizeof(TaskDev) * T, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(ptask0, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
@@ -199,7 +218,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_CK(cudaStreamSynchronize(st));      // host staging lives on this stack frame
     NA_CK(cudaMemsetAsync(err, 0, sizeof(int), st));
 
-    // ---- the same kernel sequence as the allocating path ----
+    // ---- the kernel sequence of the allocating path, CUDA-core source and Cox-Munk kernels ----
     NA_LAUNCH(k_gauss<<<1, 64, 0, st>>>(N, gmu, gw, pwt));
     NA_LAUNCH(k_pixel_setup<<<1, 32, 0, st>>>(px, 1, N, gmu));
     NA_LAUNCH(k_levels<<<dim3(2, 1), 256, 0, st>>>(px, 1, h, ch, xd, yd, z));

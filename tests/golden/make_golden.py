@@ -5,7 +5,7 @@ Runs the reference C solver compiled from its own sources by oracle/Makefile
 inputs and records its outputs.  Only runnable where the reference sources
 exist; the JSON it writes is committed and travels with the tests.
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    OCRT_REF_ROOT=<reference checkout> make -C oracle ref && python tests/golden/make_golden.py
 """
 import ctypes as C
 import json
@@ -67,6 +67,19 @@ def case_list():
              "max_orders": 500},
             {"g": float(p["g"][i]), "L": 60, "tau_a": float(p["aod"][i]), "ssa_a": float(p["ssa"][i])},
             note="configuration-3 distribution, reduced layers and modes")
+    # configuration 3 at its full shape: the first three 400-layer and the
+    # first three 200-layer pixels of the batched-forward workload's own draw
+    q = batched_forward_pixels(4096)
+    picked = [i for i in range(4096) if q["n_layers"][i] == 400][:3] + \
+             [i for i in range(4096) if q["n_layers"][i] == 200][:3]
+    for i in picked:
+        add(f"config3_full_{i}", {"surface": 2, "wind_speed": float(q["wind"][i]), "sza_deg": float(q["sza"][i]),
+                                  "vza_deg": float(q["vza"][i]), "raa_deg": float(q["raa"][i]),
+                                  "wavelength_nm": float(q["wavelength"][i]), "tau_r_input": float(q["tau_r"][i])},
+            {"n_mu": 32, "n_layers": int(q["n_layers"][i]), "fourier_m_max": 32, "tau_r_source": 1,
+             "max_orders": 1000},
+            {"g": float(q["g"][i]), "L": 120, "tau_a": float(q["aod"][i]), "ssa_a": float(q["ssa"][i])},
+            note="configuration 3 at full shape (N 32, m <= 32, L 120), pixel i of the 4096-pixel draw")
     return cases
 
 

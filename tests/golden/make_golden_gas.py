@@ -18,7 +18,8 @@ tests/golden/reference_gas.json.
 
 Only runnable where the reference sources exist; the outputs are committed.
 
-    make -C oracle ref && python tests/golden/make_golden_gas.py
+    OCRT_REF_ROOT=<reference checkout> make -C oracle ref && \
+        OCRT_REF_ROOT=<reference checkout> python tests/golden/make_golden_gas.py
 """
 import ctypes as C
 import json
@@ -36,7 +37,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from ocrt_gb300 import _abi as A  # noqa: E402
 from synthetic import hg_aerosol_moments  # noqa: E402
 
-REF_INPUTS = "/root/reference/code/OCRT_C/inputs"
+REF_INPUTS = os.path.join(os.environ.get("OCRT_REF_ROOT", ""), "code", "OCRT_C", "inputs")
 DATA = os.path.join(HERE, "gas_data")
 OUT = os.path.join(HERE, "reference_gas.json")
 GASES = ("h2o", "o3", "o2", "co2", "no2", "ch4")

@@ -3,7 +3,7 @@ reference solver (rt_solve_case_pol_lut through oracle/ref_driver.c, compiled
 from the reference's own sources by oracle/Makefile).  Only runnable where the
 reference sources exist; the JSON it writes is committed.
 
-    make -C oracle ref && python tests/golden/make_golden_lut.py
+    OCRT_REF_ROOT=<reference checkout> make -C oracle ref && python tests/golden/make_golden_lut.py
 """
 import ctypes as C
 import json
