@@ -38,7 +38,7 @@ enum {
     OCRT_SURFACE_LAMBERT = 1,               /* not on the solve path: -5 */
     OCRT_SURFACE_BLACK_FRESNEL_OCEAN = 2,   /* rough (wind>0) or flat (wind<=0) Fresnel over a black ocean */
     OCRT_SURFACE_FLAT = 3,                  /* exact flat Fresnel */
-    OCRT_SURFACE_OCEAN = 4                  /* coupled in-water solve: -5 (not built) */
+    OCRT_SURFACE_OCEAN = 4                  /* coupled in-water solve: ocrt_gb_solve_ocean */
 };
 enum { OCRT_TAU_R_AUTO = 0, OCRT_TAU_R_FROM_INPUT = 1 };
 /* Altitude mapping of the uniform-optical-depth level grid.  The plane-parallel
@@ -332,6 +332,70 @@ int  ocrt_gb_gas_columns(const ocrt_gas *gas, double *column_eff, double *column
  * altitudes in km (z_km, opts.n_layers + 1 entries, level 0 = TOA). */
 int  ocrt_gb_layer_gas(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
                        double *tau_abs, double *z_km);
+
+/* ---- coupled atmosphere-ocean (rt_solve_case_ocean, rt_solver.h:145-149) -
+ * Three successive-orders solves joined at a rough (Cox-Munk) air-water
+ * interface, as rt_solve_case_ocean runs them (rt_solver.c:3468-6660):
+ *   1. the atmosphere over the rough Fresnel surface, with the diffuse
+ *      downward field at the bottom of the atmosphere exported per mode;
+ *   2. the water column: the refracted direct beam (polarised by the
+ *      Fresnel transmission) and the transmitted skylight as sources, the
+ *      internal reflection of the upward field at the surface as the top
+ *      boundary, a black bottom (rt_water_rt.c:3549-7578);
+ *   3. the atmosphere again, driven only by the water-leaving radiance
+ *      transmitted up through the surface as a bottom source.
+ * TOA reflectance = pass 1 + pass 3; the water-leaving and in-water
+ * quantities of rt_result_t go to ocrt_ocean_result.  The case's surface
+ * must be OCRT_SURFACE_OCEAN with wind_speed > 0; opts.n_mu is ignored (the
+ * atmosphere solves use n_mu_water nodes, as the reference does), pssa must
+ * be 0 (the reference refuses IPSS on this path).
+ * Water optical properties are given directly (the reference derives them
+ * from its pure-water tables and constituent models, rt_water_iop.c):
+ * pure-seawater scattering uses the Rayleigh-like matrix with depolarisation
+ * 0.039 (rt_water_rt.c:2104-2236), hydrosol scattering a moment expansion
+ * like the aerosol's. */
+typedef struct {
+    double a_total;          /* absorption of the water [1/m] */
+    double b_water;          /* pure-seawater scattering [1/m] */
+    double b_particle;       /* hydrosol scattering [1/m]; 0 = none */
+    int    L_particle;       /* hydrosol expansion order (>= 1 when b_particle > 0) */
+    const double *beta, *gamma, *alpha, *zeta;   /* [L_particle+1] hydrosol moments, beta_0 = 1 */
+    int    n_mu_water;       /* Gauss nodes per hemisphere in the water (default 48) */
+    int    m_max_water;      /* Fourier modes of the in-water solve (default 2) */
+    int    max_orders_water; /* in-water SOS orders (default 20) */
+    double tolerance_water;  /* in-water SOS tolerance (default 1e-7) */
+    int    n_layers_water;   /* 0 (default) = optical depth / 0.05, as the depth policy */
+    double depth_m;          /* > 0: black bottom at this depth; 0 (default) = depth policy
+                                (optical depth >= 20 and 1e-8 transport attenuation) */
+    int    view_as_node;     /* 1 (default): the refracted view is a zero-weight water node */
+} ocrt_ocean;
+
+typedef struct {
+    double rho_atm_I, rho_atm_Q, rho_atm_U;          /* TOA reflectance of pass 1 (atmosphere and surface) */
+    double rho_water_I, rho_water_Q, rho_water_U;    /* TOA reflectance of the water-leaving light (pass 3) */
+    double Lu_0minus_I, Lu_0minus_Q, Lu_0minus_U;    /* upwelling just below the surface, view direction */
+    double Lu_0plus_I, Lu_0plus_Q, Lu_0plus_U;       /* water-leaving radiance just above the surface */
+    double Ed_0minus, Eu_0minus, Ed_0plus;           /* irradiances (F_sun = pi units) */
+    double Ed_0minus_direct, Ed_0plus_direct;
+    double Rrs_0plus_I, Rrs_0plus_Q, Rrs_0plus_U;    /* Lu(0+) / Ed(0+) */
+    double rrs_0minus_I, rrs_0minus_Q, rrs_0minus_U; /* Lu(0-) / Ed(0-) */
+    double Kd_0minus, Ku_0minus;                     /* diffuse attenuation of the first water layer [1/m] */
+    double tau_water, depth_water_m;                 /* optical and physical depth of the water column */
+    int    n_layers_water, n_ring_water;             /* water layers; water directions (Gauss + zero-weight) */
+    int    orders_water, converged_water;            /* max orders over modes; AND over modes */
+} ocrt_ocean_result;
+
+/* Defaults of rt_water_rt_options_default (rt_water_rt.c:1340-1410) and of a
+ * pure-seawater column with no hydrosol (a_total and b_water left 0). */
+void ocrt_ocean_default(ocrt_ocean *oc);
+int  ocrt_gb_solve_ocean(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
+                         const ocrt_ocean *oc, ocrt_result *out, ocrt_ocean_result *wout);
+/* n coupled pixels in one device pass; opts / aer / oc shared or per case. */
+int  ocrt_gb_solve_batch_ocean(int n, const ocrt_case *cases,
+                               const ocrt_opts *opts, int opts_per_case,
+                               const ocrt_aerosol *aer, int aer_per_case,
+                               const ocrt_ocean *oc, int oc_per_case,
+                               ocrt_result *out, ocrt_ocean_result *wout, void *stream);
 
 int ocrt_gb_solve_batch_adjoint(int n, const ocrt_case *cases,
                                 const ocrt_opts *opts, int opts_per_case,

@@ -196,3 +196,55 @@ def bind_solver(lib, prefix):
                   C.POINTER(Diag)]
     f.restype = C.c_int
     return f
+
+
+class Ocean(C.Structure):
+    _fields_ = [
+        ("a_total", C.c_double), ("b_water", C.c_double), ("b_particle", C.c_double),
+        ("L_particle", C.c_int),
+        ("beta", C.POINTER(C.c_double)), ("gamma", C.POINTER(C.c_double)),
+        ("alpha", C.POINTER(C.c_double)), ("zeta", C.POINTER(C.c_double)),
+        ("n_mu_water", C.c_int), ("m_max_water", C.c_int), ("max_orders_water", C.c_int),
+        ("tolerance_water", C.c_double), ("n_layers_water", C.c_int), ("depth_m", C.c_double),
+        ("view_as_node", C.c_int),
+    ]
+
+
+class OceanResult(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "rho_atm_I", "rho_atm_Q", "rho_atm_U", "rho_water_I", "rho_water_Q", "rho_water_U",
+        "Lu_0minus_I", "Lu_0minus_Q", "Lu_0minus_U", "Lu_0plus_I", "Lu_0plus_Q", "Lu_0plus_U",
+        "Ed_0minus", "Eu_0minus", "Ed_0plus", "Ed_0minus_direct", "Ed_0plus_direct",
+        "Rrs_0plus_I", "Rrs_0plus_Q", "Rrs_0plus_U", "rrs_0minus_I", "rrs_0minus_Q", "rrs_0minus_U",
+        "Kd_0minus", "Ku_0minus", "tau_water", "depth_water_m")] + [
+        (k, C.c_int) for k in ("n_layers_water", "n_ring_water", "orders_water", "converged_water")]
+
+
+OCEAN_RESULT_FIELDS = [f for f, _ in OceanResult._fields_]
+
+
+class OceanHolder:
+    """A water column (ocrt_ocean) with its hydrosol moment arrays kept alive.
+
+    a_total, b_water and b_particle in 1/m; moments (beta, gamma, alpha,
+    zeta) of the hydrosol as for the aerosol, or None without a hydrosol.
+    Remaining keywords set ocrt_ocean fields (n_mu_water, m_max_water, ...)."""
+
+    def __init__(self, a_total, b_water, b_particle=0.0, moments=None, **kw):
+        import numpy as np
+        o = Ocean(a_total=float(a_total), b_water=float(b_water), b_particle=float(b_particle), L_particle=0,
+                  n_mu_water=48, m_max_water=2, max_orders_water=20, tolerance_water=1e-7,
+                  n_layers_water=0, depth_m=0.0, view_as_node=1)
+        self.arrays = []
+        if moments is not None:
+            self.arrays = [np.ascontiguousarray(np.asarray(a, dtype=np.float64)) for a in moments]
+            ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self.arrays]
+            o.L_particle = len(self.arrays[0]) - 1
+            o.beta, o.gamma, o.alpha, o.zeta = ptrs
+        for k, v in kw.items():
+            setattr(o, k, v)
+        self.struct = o
+
+
+def ocean_result_dict(r):
+    return {f: getattr(r, f) for f in OCEAN_RESULT_FIELDS}

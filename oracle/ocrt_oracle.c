@@ -29,6 +29,27 @@ static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
                       const ocrt_layers *layers, ocrt_lut *lut, ocrt_result *out, ocrt_diag *diag);
 
 #define PI 3.14159265358979323846
+
+/* Hooks of the coupled atmosphere-ocean driver (ocean.c) into the atmosphere
+ * solve, thread-local so that batched oracle solves stay independent:
+ *   bottom_only: the solar primary and the surface seeds are dropped, only
+ *     the bottom source drives the field (rt_solver.c:949-954,
+ *     rt_surface_boundary.c:553-569);
+ *   ext_*: upward radiance per mode and ring node emitted at the bottom of
+ *     the atmosphere, attenuated upward and added to order 1 and the total
+ *     (rt_surface_boundary.c:495-527);
+ *   boa_*: the converged downward total at the bottom per mode and ring node
+ *     (rt_solver.c:1050-1076);
+ *   mu / w / n: the ring of the solve. */
+typedef struct {
+    int bottom_only;
+    const double *ext_I, *ext_Q, *ext_U;
+    int ext_mmax;
+    double *boa_I, *boa_Q, *boa_U;
+    double mu[260], w[260];
+    int n;
+} atm_hooks_t;
+static _Thread_local atm_hooks_t *g_atm_hooks;
 #define DEPOL 0.0279                  /* rt_solver.c:646 */
 #define Z_TOP_KM 100.0                /* rt_atm.c:219, 306 */
 #define MAX_RING 130
@@ -1629,6 +1650,10 @@ static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
     if (op->view_as_node) c->view_idx = ring_insert(mu_r, w_r, &nr, c->mu_view) + 1;
     const int n = nr, nt = op->n_layers, nd = 2 * n + 1, M = op->fourier_m_max;
     c->n = n;
+    if (g_atm_hooks) {
+        g_atm_hooks->n = n;
+        for (int j = 0; j < n; ++j) { g_atm_hooks->mu[j] = mu_r[j]; g_atm_hooks->w[j] = w_r[j]; }
+    }
     c->rm[RIDX(n, 0)] = -c->mu0; c->gb[RIDX(n, 0)] = 0.0;
     for (int j = 1; j <= n; ++j) {
         c->rm[RIDX(n, j)] = mu_r[j - 1]; c->rm[RIDX(n, -j)] = -mu_r[j - 1];
@@ -1697,11 +1722,16 @@ static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
         primary_source(c, &md, Js[0], Js[1], Js[2]);
         for (int s = 0; s < 3 && !rc; ++s) if (transport(c, Js[s], NULL, Pr[s])) rc = -2;
         if (rc) break;
+        const int bottom_only = g_atm_hooks && g_atm_hooks->bottom_only;
+        if (bottom_only)
+            for (int s = 0; s < 3; ++s)
+                for (int k = 0; k <= nt; ++k)
+                    for (int j = -n; j <= n; ++j) if (j) F(Pr[s], c, k, j) = 0.0;
         for (int s = 0; s < 3; ++s) { memcpy(Tt[s], Pr[s], cnt * sizeof(double)); memset(O1[s], 0, cnt * sizeof(double)); }
         int orders = 1, conv = 0;
         double resid = 0.0;
         const double *Krm = rough ? Kr + (size_t)m * n * n * 9 : NULL;
-        if (surf_on) {
+        if (surf_on && !bottom_only) {
             if (flat) {
                 if ((rc = flat_reflected_beam(c, &md, aer, cs->n_water, cs->q_convention, Tt, O1))) break;
             } else {
@@ -1720,6 +1750,20 @@ static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
                             F(O1[s], c, k, o) += v[s];
                             seed[(size_t)s * cnt + (size_t)k * nd + RIDX(n, o)] = v[s];
                         }
+                    }
+                }
+            }
+        }
+        if (g_atm_hooks && g_atm_hooks->ext_I && m <= g_atm_hooks->ext_mmax) {
+            const double *ex[3] = {g_atm_hooks->ext_I, g_atm_hooks->ext_Q, g_atm_hooks->ext_U};
+            for (int k = 0; k <= nt; ++k) {
+                const double up = c->md.h[nt] - c->md.h[k];
+                for (int o = 1; o <= n; ++o) {
+                    const double att = exp(-up / mu_pos[o - 1]);
+                    for (int s = 0; s < 3; ++s) {
+                        const double v = ex[s][(size_t)m * n + o - 1] * att;
+                        F(Tt[s], c, k, o) += v;
+                        F(O1[s], c, k, o) += v;
                     }
                 }
             }
@@ -1793,6 +1837,12 @@ static int solve_impl(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aeros
                 for (int k = 0; k <= nt; ++k)
                     for (int o = 1; o <= n; ++o)
                         F(Tt[s], c, k, o) -= seed[(size_t)s * cnt + (size_t)k * nd + RIDX(n, o)];
+        if (g_atm_hooks && g_atm_hooks->boa_I)
+            for (int j = 1; j <= n; ++j) {
+                g_atm_hooks->boa_I[(size_t)m * n + j - 1] = F(Tt[0], c, nt, -j);
+                g_atm_hooks->boa_Q[(size_t)m * n + j - 1] = F(Tt[1], c, nt, -j);
+                g_atm_hooks->boa_U[(size_t)m * n + j - 1] = F(Tt[2], c, nt, -j);
+            }
         if (orders > max_orders_seen) max_orders_seen = orders;
         if (!conv) all_conv = 0;
         order_modes += orders;
@@ -2029,3 +2079,4 @@ void ocrt_oracle_abi_sizes(size_t *out)
     out[3] = sizeof(ocrt_result);
     out[4] = sizeof(ocrt_diag);
 }
+#include "ocean.c"
