@@ -364,9 +364,13 @@ typedef struct {
     int    m_max_water;      /* Fourier modes of the in-water solve (default 2) */
     int    max_orders_water; /* in-water SOS orders (default 20) */
     double tolerance_water;  /* in-water SOS tolerance (default 1e-7) */
-    int    n_layers_water;   /* 0 (default) = optical depth / 0.05, as the depth policy */
-    double depth_m;          /* > 0: black bottom at this depth; 0 (default) = depth policy
-                                (optical depth >= 20 and 1e-8 transport attenuation) */
+    int    n_layers_water;   /* depth policy: at least this many layers, and at least
+                                optical depth / 0.05; fixed depth: exactly this many
+                                (0 = optical depth / 0.05) */
+    double depth_m;          /* > 0: black bottom at this depth; 0 (default) = depth policy:
+                                optical depth >= tau_base and 1e-8 transport attenuation */
+    double tau_base;         /* base optical depth of the depth policy (default 20; the
+                                reference's constituent-model path uses 15) */
     int    view_as_node;     /* 1 (default): the refracted view is a zero-weight water node */
 } ocrt_ocean;
 

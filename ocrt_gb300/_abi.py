@@ -206,7 +206,7 @@ class Ocean(C.Structure):
         ("alpha", C.POINTER(C.c_double)), ("zeta", C.POINTER(C.c_double)),
         ("n_mu_water", C.c_int), ("m_max_water", C.c_int), ("max_orders_water", C.c_int),
         ("tolerance_water", C.c_double), ("n_layers_water", C.c_int), ("depth_m", C.c_double),
-        ("view_as_node", C.c_int),
+        ("tau_base", C.c_double), ("view_as_node", C.c_int),
     ]
 
 
@@ -234,7 +234,7 @@ class OceanHolder:
         import numpy as np
         o = Ocean(a_total=float(a_total), b_water=float(b_water), b_particle=float(b_particle), L_particle=0,
                   n_mu_water=48, m_max_water=2, max_orders_water=20, tolerance_water=1e-7,
-                  n_layers_water=0, depth_m=0.0, view_as_node=1)
+                  n_layers_water=0, depth_m=0.0, tau_base=20.0, view_as_node=1)
         self.arrays = []
         if moments is not None:
             self.arrays = [np.ascontiguousarray(np.asarray(a, dtype=np.float64)) for a in moments]

@@ -560,12 +560,15 @@ static int water_solve(water_t *W)
         const double sb = bp + oc->b_water;
         double ge = sb > 0.0 ? bp * gp / sb : 0.0;
         ge = ge > 0.999 ? 0.999 : (ge < -0.999 ? -0.999 : ge);
-        double z_req = 20.0 / ext;
+        double z_req = (oc->tau_base > 0.0 ? oc->tau_base : 20.0) / ext;
         const double te = oc->a_total + b_rt * fmax(0.0, 1.0 - ge);
         if (te > 0.0) { const double ztr = -log(1.0e-8) / te; if (ztr > z_req) z_req = ztr; }
         tau_max = ext * z_req;
     }
-    nt = oc->n_layers_water > 0 ? oc->n_layers_water : (int)ceil(tau_max / 0.05);
+    /* layers: Delta tau <= 0.05 (layer_dtau_target), the caller's count a floor
+     * under the depth policy and exact for a fixed depth (rt_water_rt.c:5174-5179) */
+    nt = (int)ceil(tau_max / 0.05);
+    if (oc->n_layers_water > 0 && (oc->depth_m > 0.0 || oc->n_layers_water > nt)) nt = oc->n_layers_water;
     if (nt < 1) nt = 1;
     W->tau_max = tau_max; W->z_max = tau_max / ext; W->nt = nt;
 
@@ -775,7 +778,7 @@ void ocrt_oracle_ocean_default(ocrt_ocean *oc)
 {
     memset(oc, 0, sizeof(*oc));
     oc->n_mu_water = 48; oc->m_max_water = 2; oc->max_orders_water = 20; oc->tolerance_water = 1e-7;
-    oc->view_as_node = 1;
+    oc->tau_base = 20.0; oc->view_as_node = 1;
 }
 
 int ocrt_oracle_solve_ocean(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer_in,

@@ -216,3 +216,66 @@ def oracle_lut(orc, case, opts, aer, vza, raa):
     if rc != 0:
         raise RuntimeError(f"oracle lut rc {rc}")
     return lut
+
+
+GOLDEN_OCEAN = os.path.join(HERE, "golden", "reference_ocean.json")
+
+# reference CLI key -> (ocrt_result / ocrt_ocean_result key, relative tolerance of the
+# oracle's reproduction, set by the printed precision); Kd / Ku are printed to 1e-6 absolute
+OCEAN_RADIOMETRIC = ("Lu0plus", "Qu0plus", "Uu0plus", "Ed0plus", "Lu0minus", "Qu0minus", "Uu0minus", "Ed0minus",
+                     "Eu0minus")
+REF_OCEAN_KEYS = {
+    "TOA_rho_I": ("rho_I", 1e-9), "TOA_rho_Q": ("rho_Q", 1e-9), "TOA_rho_U": ("rho_U", 1e-9),
+    "TOA_rho_atm_I": ("rho_atm_I", 1e-9), "TOA_rho_atm_Q": ("rho_atm_Q", 1e-9), "TOA_rho_atm_U": ("rho_atm_U", 1e-9),
+    "TOA_rho_water_direct_I": ("rho_water_I", 1e-9), "TOA_rho_water_direct_Q": ("rho_water_Q", 1e-9),
+    "TOA_rho_water_direct_U": ("rho_water_U", 1e-9),
+    "TOA_rho_glint_direct_I": ("rho_glint_direct_I", 1e-9),
+    "T_dir_dn": ("T_dir_dn", 1e-9), "T_diff_dn_hemi": ("T_diff_dn_hemi", 1e-9), "T_diff_dn_dir": ("T_diff_dn_dir", 1e-9),
+    "Lu0plus": ("Lu_0plus_I", 1e-6), "Qu0plus": ("Lu_0plus_Q", 1e-6), "Uu0plus": ("Lu_0plus_U", 1e-6),
+    "Ed0plus": ("Ed_0plus", 1e-6), "Rrs0plus_I": ("Rrs_0plus_I", 1e-6), "Rrs0plus_Q": ("Rrs_0plus_Q", 1e-6),
+    "Rrs0plus_U": ("Rrs_0plus_U", 1e-6),
+    "Lu0minus": ("Lu_0minus_I", 1e-6), "Qu0minus": ("Lu_0minus_Q", 1e-6), "Uu0minus": ("Lu_0minus_U", 1e-6),
+    "Ed0minus": ("Ed_0minus", 1e-6), "Eu0minus": ("Eu_0minus", 1e-6), "rrs0minus_I": ("rrs_0minus_I", 1e-6),
+    "Kd0minus": ("Kd_0minus", 1e-5), "Ku0minus": ("Ku_0minus", 1e-5),
+}
+
+
+def ocean_ref_value(spec, key):
+    """Reference value of a key in this library's units (F_sun = pi): the
+    reference's constituent-model path reports radiances and irradiances for
+    F_sun = 1."""
+    v = spec["reference"][key]
+    return v * (3.141592653589793 / spec["F_sun"]) if key in OCEAN_RADIOMETRIC else v
+
+
+def load_golden_ocean():
+    with open(GOLDEN_OCEAN) as fh:
+        return json.load(fh)
+
+
+def ocean_inputs_from_spec(spec, **ocean_kw):
+    """(case, opts, OceanHolder) of one reference_ocean.json case: the water's
+    absorption and scattering are the values the reference printed."""
+    ref = spec["reference"]
+    c = A.default_case(surface="ocean", sza_deg=spec["sza_deg"], vza_deg=spec["vza_deg"], raa_deg=spec["raa_deg"],
+                       wavelength_nm=spec["wavelength_nm"], wind_speed=spec["wind_speed"])
+    m = spec["m_max"] if spec["m_max"] is not None else 2
+    o = A.default_opts(fourier_m_max=m, n_layers=spec["n_layers"] or 40)
+    kw = dict(n_mu_water=spec["n_mu_water"] or 48, m_max_water=m)
+    kw.update(spec.get("water_policy", {}))
+    kw.update(ocean_kw)
+    oc = A.OceanHolder(ref["a_total"], ref["b_total"], **kw)
+    return c, o, oc
+
+
+def oracle_ocean(orc, case, opts, oc, aer=None):
+    f = orc.lib.ocrt_oracle_solve_ocean
+    f.argtypes = [C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol), C.POINTER(A.Ocean),
+                  C.POINTER(A.Result), C.POINTER(A.OceanResult)]
+    r, w = A.Result(), A.OceanResult()
+    a = aer.struct if isinstance(aer, A.AerosolHolder) else aer
+    rc = f(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None, C.byref(oc.struct), C.byref(r),
+           C.byref(w))
+    if rc != 0:
+        raise RuntimeError(f"oracle ocean rc {rc}")
+    return {**A.result_dict(r), **A.ocean_result_dict(w)}
