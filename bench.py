@@ -32,7 +32,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from ocrt_gb300 import _abi as A  # noqa: E402
 from ocrt_gb300.replicas import max_over_ranks  # noqa: E402
-from synthetic import batched_forward_pixels, hg_aerosol_moments  # noqa: E402
+from synthetic import batched_forward_pixels, coupled_ocean_pixels, hg_aerosol_moments  # noqa: E402
 
 METRIC = "pixel-solves/s"
 N_MU, M_MAX, L_AER = 32, 32, 120
@@ -73,6 +73,83 @@ def adjoint_workload(n_pix, seed=20261203 + 4):
     opts = A.default_opts(n_mu=N_MU, n_layers=ADJ_LAYERS, fourier_m_max=M_MAX, tau_r_source=A.TAU_R_FROM_INPUT,
                           max_orders=1000, tolerance=1e-7)
     return cases, opts, aers
+
+
+OCEAN_N, OCEAN_M, OCEAN_LAYERS_ATM, OCEAN_LAYERS_W, L_HYD = 32, 16, 400, 100, 200
+
+
+def ocean_workload(n_geom):
+    """Configuration 5: n_geom geometries x 8 bands; the configuration-2
+    atmosphere (400 layers, HG g=0.7 aerosol to L=120, SSA 0.95, AOD 0.1) over
+    a 50 m, 100-layer ocean with a forward-peaked hydrosol (HG g=0.92 to
+    L=200) and pure-water scattering, Cox-Munk interface, n_water 1.34."""
+    rows = coupled_ocean_pixels(n_geom)
+    aer = A.AerosolHolder(0.1, 0.95, *hg_aerosol_moments(0.7, L_AER))
+    hyd = hg_aerosol_moments(0.92, L_HYD)
+    cases, oceans = [], []
+    for r in rows:
+        cases.append(A.default_case(surface="ocean", sza_deg=r["sza"], vza_deg=r["vza"], raa_deg=r["raa"],
+                                    wavelength_nm=r["wavelength"], wind_speed=r["wind"], tau_r_input=r["tau_r"],
+                                    n_water=1.34))
+        oceans.append(A.OceanHolder(r["a"], r["b_water"], r["b_particle"], hyd, n_mu_water=OCEAN_N,
+                                    m_max_water=OCEAN_M, depth_m=50.0, n_layers_water=OCEAN_LAYERS_W,
+                                    max_orders_water=1000, tolerance_water=1e-7))
+    opts = A.default_opts(n_mu=OCEAN_N, n_layers=OCEAN_LAYERS_ATM, fourier_m_max=OCEAN_M,
+                          tau_r_source=A.TAU_R_FROM_INPUT, max_orders=1000, tolerance=1e-7)
+    return cases, opts, [aer] * len(cases), oceans
+
+
+def run_ocean(args, og, world):
+    """Configuration-5 sub-line: coupled atmosphere-ocean pixel-bands per
+    second through ocrt_gb_solve_batch_ocean with host buffers (uploads,
+    the three SOS passes, the interface kernels and the result download
+    inside the timed region), and the error against the FP64 oracle."""
+    cases, opts, aers, oceans = ocean_workload(args.ocean_geoms)
+    n = len(cases)
+    og.solve_batch_ocean(cases[:8], opts, oceans[:8], aers[:8])      # warm the allocator cache
+    for _ in range(max(0, min(args.warmup, 1))):
+        og.solve_batch_ocean(cases, opts, oceans, aers)
+    steps = max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        res = og.solve_batch_ocean(cases, opts, oceans, aers)
+    dt = max_over_ranks((time.perf_counter() - t0) / steps)
+    out = {"metric": "coupled pixel-solves/s", "value": n * world / dt, "unit": "pixel-solves/s",
+           "ms_per_step": dt * 1e3, "steps": steps, "pixel_bands": n,
+           "workload": f"configuration 5: {args.ocean_geoms} geometries x 8 bands, atmosphere {OCEAN_LAYERS_ATM} "
+                       f"layers (aerosol HG g=0.7 to L={L_AER}), ocean {OCEAN_LAYERS_W} layers, 50 m, hydrosol "
+                       f"HG g=0.92 to L={L_HYD}, a U[0.02,0.5] b U[0.01,1.0] per m, wind U[1,12]; "
+                       f"N={OCEAN_N} shared streams, Fourier modes 0..{OCEAN_M} in both media; "
+                       f"IPSS off (the coupled path is plane-parallel); forward only",
+           "timing": "wall clock around ocrt_gb_solve_batch_ocean with host buffers (host<->device copies, "
+                     "allocation and the three SOS passes inside)",
+           "water_orders_max": max(r["orders_water"] for r in res)}
+    if world == 1 and not args.no_cpu and args.ocean_cpu > 0:
+        lib = oracle_lib()
+        f = lib.ocrt_oracle_solve_ocean
+        f.argtypes = [C.POINTER(A.Case), C.POINTER(A.Opts), C.POINTER(A.Aerosol), C.POINTER(A.Ocean),
+                      C.POINTER(A.Result), C.POINTER(A.OceanResult)]
+        k = min(args.ocean_cpu, n)
+        errs = {"rho_I": 0.0, "rho_Q": 0.0, "rho_U": 0.0, "Rrs": 0.0}
+        t0 = time.perf_counter()
+        for i in range(k):
+            r, w = A.Result(), A.OceanResult()
+            rc = f(C.byref(cases[i]), C.byref(opts), C.byref(aers[i].struct), C.byref(oceans[i].struct),
+                   C.byref(r), C.byref(w))
+            if rc != 0:
+                raise RuntimeError(f"oracle ocean rc {rc}")
+            g = res[i]
+            errs["rho_I"] = max(errs["rho_I"], abs(g["rho_I"] - r.rho_I) / abs(r.rho_I))
+            errs["rho_Q"] = max(errs["rho_Q"], abs(g["rho_Q"] - r.rho_Q))
+            errs["rho_U"] = max(errs["rho_U"], abs(g["rho_U"] - r.rho_U))
+            errs["Rrs"] = max(errs["Rrs"], abs(g["Rrs_0plus_I"] - w.Rrs_0plus_I) / abs(w.Rrs_0plus_I))
+        tc = time.perf_counter() - t0
+        out["rel_err_vs_fp64"] = {"pixels": k, "max_rel_err_rho_I": errs["rho_I"], "max_abs_err_rho_Q": errs["rho_Q"],
+                                  "max_abs_err_rho_U": errs["rho_U"], "max_rel_err_Rrs_0plus": errs["Rrs"],
+                                  "reference": "FP64 oracle on the same pixel-bands"}
+        out["cpu_baseline"] = {"value": k / tc, "unit": "pixel-solves/s", "cores": 1, "kind": "port",
+                               "sample": f"first {k} pixel-bands, one oracle call each, {tc:.1f} s"}
+    return out
 
 
 def config_dict(n_pix, world):
@@ -231,7 +308,15 @@ def run_reference(args, rank, world):
                              prefer_reference=True)
         vals.append(base["value"])
     v = statistics.median(vals)
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+    extra = {}
+    if args.compare_port and base["kind"] == "reference":
+        # the port on the same pixels and threads: its speed relative to the
+        # reference library on this host
+        n = int(base["sample"].split()[1])
+        dt_r, _, _, _ = cpu_run(cases[:n], opts[:n], aers[:n], True)
+        dt_p, _, _, _ = cpu_run(cases[:n], opts[:n], aers[:n], False)
+        extra = {"port_time_over_reference": dt_p / dt_r, "compare_pixels": n}
+    line = {"impl": "reference", **extra, "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(args.pixels, world),
@@ -359,6 +444,9 @@ def run_ours(args, rank, world):
     if args.adj_pixels > 0:
         adj = run_adjoint(args, og, torch, stream, sp, barrier, world)
 
+    # ---- configuration 5: the coupled atmosphere-ocean solve ----
+    ocean = run_ocean(args, og, world) if args.ocean_geoms > 0 else None
+
     if rank != 0:
         return
     # ---- plain per-pixel GPU form (one solve call per pixel) ----
@@ -388,7 +476,7 @@ def run_ours(args, rank, world):
             "cpu_baseline": cpu, "rel_err_vs_fp64": err,
             "plain_per_pixel_gpu": {"value": plain, "unit": METRIC, "sample": f"{nplain} pixels, one "
                                     f"ocrt_gb_solve_case call each", "batched_speedup": value / world / plain},
-            "order_modes_per_step": om, "kernel_breakdown": breakdown, "adjoint": adj,
+            "order_modes_per_step": om, "kernel_breakdown": breakdown, "adjoint": adj, "coupled_ocean": ocean,
             "execute": {"graph_replay": graph, "eager_instrumented_ms_per_step": instr_ms / args.steps,
                         "autotune": [{k: s[k] for k in ("kernel", "key", "best")} for s in og.autotune_summary()]}}
     print(json.dumps(line), flush=True)
@@ -452,8 +540,14 @@ def main():
     ap.add_argument("--plain-pixels", type=int, default=16)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--compare-port", action="store_true",
+                    help="reference arm: also time the port on the same pixels (where the reference library exists)")
     ap.add_argument("--adj-pixels", type=int, default=1024,
                     help="configuration-4 geometries (x3 bands) for the adjoint line; 0 skips it")
+    ap.add_argument("--ocean-geoms", type=int, default=128,
+                    help="configuration-5 geometries (x8 bands) for the coupled-ocean line; 0 skips it")
+    ap.add_argument("--ocean-cpu", type=int, default=2,
+                    help="pixel-bands of the coupled line checked against (and timed on) the FP64 oracle")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

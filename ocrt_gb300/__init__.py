@@ -10,8 +10,9 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Lut, LutHolder, Opts, Result,
-                   default_case, default_opts, lut_grid_reference_cli, result_dict, RESULT_FIELDS)
+from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Lut, LutHolder, Ocean, OceanHolder,
+                   OceanResult, Opts, Result, default_case, default_opts, lut_grid_reference_cli, ocean_result_dict,
+                   result_dict, RESULT_FIELDS)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libocrt_gb300.so")
@@ -25,6 +26,7 @@ EXPORTS = [
     "ocrt_gb_layer_defaults", "ocrt_gb_plan_create_adjoint", "ocrt_gb_plan_gradients",
     "ocrt_gb_solve_case_lut", "ocrt_gb_solve_batch_lut", "ocrt_gb_plan_graph_ready", "ocrt_gb_autotune_summary",
     "ocrt_gb_gas_create", "ocrt_gb_gas_destroy", "ocrt_gb_gas_tau", "ocrt_gb_gas_columns", "ocrt_gb_layer_gas",
+    "ocrt_ocean_default", "ocrt_gb_solve_ocean", "ocrt_gb_solve_batch_ocean",
 ]
 
 
@@ -85,6 +87,12 @@ def lib():
                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ocrt_opts_default.argtypes = [C.POINTER(Opts)]
     L.ocrt_case_default.argtypes = [C.POINTER(Case)]
+    L.ocrt_ocean_default.argtypes = [C.POINTER(Ocean)]
+    L.ocrt_gb_solve_ocean.argtypes = [C.POINTER(Case), C.POINTER(Opts), C.POINTER(Aerosol), C.POINTER(Ocean),
+                                      C.POINTER(Result), C.POINTER(OceanResult)]
+    L.ocrt_gb_solve_batch_ocean.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int, C.POINTER(Aerosol),
+                                            C.c_int, C.POINTER(Ocean), C.c_int, C.POINTER(Result),
+                                            C.POINTER(OceanResult), C.c_void_p]
     _lib = L
     return L
 
@@ -114,6 +122,27 @@ def solve_case(case, opts=None, aerosol=None, diag=False):
     if diag:
         out.update({k: np.array(v[:]) for k, v in arrs.items()})
     return out
+
+
+def solve_ocean(case, opts=None, ocean=None, aerosol=None):
+    """One coupled atmosphere-ocean pixel (ocrt_gb_solve_ocean): a dict of
+    the ocrt_result and ocrt_ocean_result fields.  ocean: an OceanHolder."""
+    res = solve_batch_ocean([case], opts, [ocean], None if aerosol is None else [aerosol])
+    return res[0]
+
+
+def solve_batch_ocean(cases, opts, oceans, aerosols=None):
+    """n coupled pixels in one device pass (ocrt_gb_solve_batch_ocean); a list
+    of dicts of the ocrt_result and ocrt_ocean_result fields."""
+    L = lib()
+    opts = opts or default_opts()
+    n, ca, oa, opp, aa, app = _arrays(cases, opts, aerosols)
+    structs = [o.struct if isinstance(o, OceanHolder) else o for o in oceans]
+    ocs = (Ocean * len(structs))(*structs)
+    r = (Result * n)()
+    w = (OceanResult * n)()
+    _check(L.ocrt_gb_solve_batch_ocean(n, ca, oa, opp, aa, app, ocs, 1 if len(structs) > 1 else 0, r, w, None))
+    return [{**result_dict(r[i]), **ocean_result_dict(w[i])} for i in range(n)]
 
 
 def _arrays(cases, opts, aerosols):

@@ -32,21 +32,7 @@
 
 namespace {
 
-__device__ inline void decode_col_a(const Geom &G, int c, int &s, int &h, int &g)
-{
-    const int N = G.N;
-    if (c < 6 * N) {
-        s = c / (2 * N);
-        const int r = c - s * 2 * N;
-        h = r / N;
-        g = r - h * N;
-    } else if (c < 6 * N + 6) {
-        const int v = c - 6 * N;
-        s = v >> 1; h = v & 1; g = N;
-    } else {
-        s = 0; h = 0; g = G.NR;
-    }
-}
+__device__ inline void decode_col_a(const Geom &G, int c, int &s, int &h, int &g) { decode_col(G, c, s, h, g); }
 
 __device__ inline size_t adj_off(const TaskDev &tk, const Geom &G, int ncot, int r)
 {

@@ -16,6 +16,7 @@
 #include <vector>
 #include <algorithm>
 #include <climits>
+#include <functional>
 #include <utility>
 
 #include "kernels.cuh"
@@ -163,6 +164,7 @@ struct Wave {
     size_t fld, ops, srf;  // element counts of the wave buffers
     bool any_rough, any_flat;
     size_t tail = 0;       // element count of the total-tail rows (2 * LDC per task)
+    bool any_water = false, any_top = false;   // water-column pixels; with a skylight top source
     int n_simt = 0, n_tc = 0, n_mol = 0;   // tasks given to each source kernel
     // Last order run before every task was found converged (forward orders,
     // adjoint orders); INT_MAX when the loop ran to max_orders.  Recorded by
@@ -182,8 +184,16 @@ bool force_simt()
     return e && strcmp(e, "simt") == 0;
 }
 
+// OCRT_GB_SCAN=column keeps the one-column-per-thread scan where the
+// four-column one applies (N a multiple of 4).
+bool scan4_allowed(int N)
+{
+    const char *e = getenv("OCRT_GB_SCAN");
+    return N % 4 == 0 && !(e && strcmp(e, "column") == 0);
+}
+
 struct Group {
-    int N = 0, P = 0, T = 0;
+    int N = 0, E = 1, P = 0, T = 0;   // E zero-weight ring slots (1 atmosphere, 4 water column)
     Geom G{};
     std::vector<int> idx;                 // case index of each pixel
     std::vector<PixDev> hpx;
@@ -191,7 +201,12 @@ struct Group {
     std::vector<int> hpix_task0;
     std::vector<Wave> waves;
     int Lmax = 2, Mmax = 0, max_orders = 1, nphi = 1024;
-    bool any_pssa = false, any_rough = false, any_flat = false, any_gas = false;
+    bool any_pssa = false, any_rough = false, any_flat = false, any_gas = false, any_water = false;
+    // coupled atmosphere-ocean: boundary sources read by the solve (owned by the
+    // ocean plan), the edge export written after each wave's orders (k_edges)
+    const double *ext = nullptr;
+    double *edge = nullptr;
+    int nphi_ww = 176;
     size_t nlev = 0, ncoef = 0, nmom = 0;
     size_t wave_fld = 0, wave_ops = 0, wave_srf = 0, wave_tail = 0;
     int wave_tasks = 0;
@@ -203,6 +218,7 @@ struct Group {
     double *h = nullptr, *ch = nullptr, *xd = nullptr, *yd = nullptr, *z = nullptr;
     double *tabs = nullptr;   // per-layer gas absorption depths (level-array layout), any_gas only
     float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
+    float *Cq = nullptr;                  // Gauss-slot weights in quads (k_scan4), nullptr when the column scan runs
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
     double *lam = nullptr;
     float *Eatt = nullptr, *lvf = nullptr;
@@ -289,7 +305,7 @@ template <class T> int alloc(T *&dst, size_t n)
 void free_group(Group &g)
 {
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
-                    g.tabs, g.Tc, g.Ca, g.Cb, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
+                    g.tabs, g.Tc, g.Ca, g.Cb, g.Cq, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
                     g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.Ttl,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
@@ -298,13 +314,16 @@ void free_group(Group &g)
     for (void *p : ptrs) dfree(p);
 }
 
+// patch: optional per-pixel adjustment of the device record (the coupled
+// ocean's pass flags, water-column geometry and source offsets), applied once
+// the record is built from the case, options and aerosol.
 int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app,
                 const ocrt_layers *layers = nullptr, int ncot = 0, const double *cot = nullptr,
-                const ocrt_lut *luts = nullptr)
+                const ocrt_lut *luts = nullptr, const std::function<void(int, PixDev &)> &patch = {})
 {
     g.ncot = ncot;
     std::vector<double> ldt, lss, hcot, hlv, hlr;
-    const Geom G = make_geom(g.N);
+    const Geom G = make_geom(g.N, g.E);
     g.G = G;
     g.P = (int)g.idx.size();
     std::vector<double> mb, mgv, ma, mz;
@@ -328,6 +347,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         d.mom_off = -1; d.L_aer = -1;
         d.lay_off = -1;
         d.gas = o.gas ? o.gas->dev : nullptr;
+        d.depol = OCRT_DEPOL; d.ext_off = -1;
         g.any_gas |= o.gas != nullptr;
         if (layers && (layers[i].dtau || layers[i].ssa)) {
             d.lay_off = (long long)std::max(ldt.size(), lss.size());
@@ -379,8 +399,10 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         g.nphi = std::max(g.nphi, d.nphi);
         const bool surf = c.surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN || c.surface == OCRT_SURFACE_FLAT;
         const bool flat = c.surface == OCRT_SURFACE_FLAT || (c.surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && c.wind_speed <= 0.0);
-        g.any_rough |= surf && !flat;
-        g.any_flat |= flat;
+        if (patch) patch(q, d);
+        g.any_rough |= surf && !flat && d.medium == 0;
+        g.any_flat |= flat && d.medium == 0;
+        g.any_water |= d.medium == 1;
         g.any_pssa |= o.pssa != 0;
         g.hpx.push_back(d);
     }
@@ -403,11 +425,11 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     for (int q = 0; q < g.P; ++q) {
         const PixDev &d = g.hpx[q];
         const size_t K = d.nt + 1, nm = d.M + 1;
-        const bool rough = (d.surface == 2 && d.wind > 0.0);
+        const bool rough = (d.surface == 2 && d.wind > 0.0) || d.medium == 1;   // water: R_ww kernels
         const size_t pf = nm * K * G.LDC;
         const size_t po = (nm + 2 * std::min<size_t>(nm, 3)) * op_elems;
         const size_t ps = rough ? nm * ((size_t)G.NR * G.N * 9 + (size_t)G.NR * 9) : 0;
-        size_t pb = pf * 12 + po * (tiles ? 12 : 4) + ps * 4 + nm * (4 * G.LDC + 24 * G.NR + 6 * (g.Lmax + 1)) * 4;
+        size_t pb = pf * 12 + po * (tiles ? 12 : 4) + ps * 4 + nm * (4 * G.LDC + 24 * G.NR + 3 * (1 + G.E) * (g.Lmax + 1)) * 4;
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 12 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)2 * (G.CIN + 32) * ((G.COUT + 31) & ~31) * 4;
@@ -432,7 +454,9 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
             tk[m].has_mol = m <= 2;
         }
         w.Kmax = std::max(w.Kmax, (int)K);
-        w.any_rough |= rough;
+        w.any_rough |= rough && d.medium == 0;
+        w.any_water |= d.medium == 1;
+        w.any_top |= d.medium == 1 && d.ext_off >= 0;
         w.any_flat |= (d.surface == 3 || (d.surface == 2 && d.wind <= 0.0));
         bytes += pb;
     }
@@ -446,6 +470,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.h, g.nlev)) || (rc = alloc(g.ch, g.nlev)) || (rc = alloc(g.xd, g.nlev)) ||
         (rc = alloc(g.yd, g.nlev)) || (rc = alloc(g.z, g.nlev)) || (rc = alloc(g.tabs, g.any_gas ? g.nlev : 1)) ||
         (rc = alloc(g.Tc, g.ncoef)) || (rc = alloc(g.Ca, g.ncoef)) || (rc = alloc(g.Cb, g.ncoef)) ||
+        (scan4_allowed(g.N) && (rc = alloc(g.Cq, g.ncoef / G.NR * 3 * (size_t)g.N))) ||
         (rc = alloc(g.Bp, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Br, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Bt, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
@@ -463,7 +488,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
         (rc = alloc(g.srf, g.wave_srf)) ||
-        (rc = alloc(g.Bx, (size_t)g.wave_tasks * 6 * (g.Lmax + 1))))
+        (rc = alloc(g.Bx, (size_t)g.wave_tasks * 3 * (1 + G.E) * (g.Lmax + 1))))
         return rc;
     if (g.any_layers && ((rc = up(g.ldt, ldt)) || (rc = up(g.lss, lss)))) return rc;
     if (g.any_lut && ((rc = up(g.lut_vza, hlv)) || (rc = up(g.lut_raa, hlr)) ||
@@ -682,12 +707,16 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     LAUNCH(plan, KC_SETUP, k_gauss<<<1, 64, 0, st>>>(g.N, g.gmu, g.gw, g.pw));
     LAUNCH(plan, KC_SETUP, k_pixel_setup<<<(P + 127) / 128, 128, 0, st>>>(g.px, P, g.N, g.gmu));
     LAUNCH(plan, KC_SETUP, k_levels<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
+    if (g.any_water)
+        LAUNCH(plan, KC_SETUP, k_levels_water<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z));
     LAUNCH(plan, KC_SETUP, k_level_mix<<<dim3(2, P), 256, 0, st>>>(g.px, P, g.z, g.xd, g.yd));
     if (g.any_gas)
         LAUNCH(plan, KC_SETUP, k_gas_apply<<<P, 256, 0, st>>>(g.px, P, g.h, g.ch, g.xd, g.yd, g.z, g.tabs));
     if (g.any_layers)
         LAUNCH(plan, KC_SETUP, k_layers_apply<<<P, 256, 0, st>>>(g.px, P, g.ldt, g.lss, g.h, g.ch, g.xd, g.yd, g.err));
-    LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
+    LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, G.NR, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
+    if (g.Cq)
+        LAUNCH(plan, KC_SETUP, k_coef_quads<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, G.NR, g.Tc, g.Ca, g.Cb, g.Cq));
     LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
     if (g.use_tc)
         LAUNCH(plan, KC_SETUP, k_mol_vtab<<<std::min(g.Mmax, 2) + 1, 256, 0, st>>>(G, g.Lmax, g.Bp, g.Br, g.Bt, g.gw,
@@ -706,10 +735,11 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     BatchBufs B;
     B.px = g.px; B.tasks = g.tasks; B.state = g.state; B.tout = g.tout;
     B.gmu = g.gmu; B.gw = g.gw; B.pw = g.pw; B.h = g.h; B.ch = g.ch; B.xd = g.xd; B.yd = g.yd; B.z = g.z;
-    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.frs = g.frs; B.Eatt = g.Eatt; B.lvf = g.lvf; B.active_cnt = g.active_cnt; B.err = g.err;
+    B.Tc = g.Tc; B.Ca = g.Ca; B.Cb = g.Cb; B.Cq = g.Cq; B.frs = g.frs; B.Eatt = g.Eatt; B.lvf = g.lvf; B.active_cnt = g.active_cnt; B.err = g.err;
     B.mol_cnt = g.mol_cnt; B.work = g.work;
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     B.molV = g.molV;
+    B.ext = g.ext;
     WaveBufs W;
     W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.Ttl = g.Ttl; W.ops = g.ops; W.opt = g.use_tc ? g.opt : nullptr;
     W.pvec = g.pvec;
@@ -727,7 +757,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.mol_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.work, 0, sizeof(int) * 4 * ((size_t)g.max_orders + 2), st));
-        LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(g.tasks, w.t0, nw, g.px, g.Lmax, g.Bx));
+        LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 128 / (1 + G.E) - 1) / (128 / (1 + G.E)), 128, 0, st>>>(
+                   g.tasks, w.t0, nw, g.px, g.Lmax, G.E, g.Bx));
         auto tables = [&](int b) {
             k_tables<<<dim3(nw, tables_yblocks(b, G.NR, G.N)), b, tables_smem_bytes(b, G.N, g.Lmax), st>>>(
                 g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec,
@@ -768,7 +799,10 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
                 LAUNCH(plan, KC_COXMUNK, coxmunk(cb));
             }
         }
-        LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+        if (w.any_water)
+            LAUNCH(plan, KC_COXMUNK, k_rww<<<dim3(G.NR, w.p1 - w.p0), 256,
+                                             iface_smem_bytes(g.Mmax, g.nphi_ww, 0), st>>>(
+                       g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.nphi_ww, g.srf));
         const dim3 sgrid(w.n_simt, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         const int mtiles = (w.Kmax + 127) / 128, ltiles = (w.Kmax + 31) / 32;
         const size_t tc_smem = tc_smem_bytes(G);
@@ -776,7 +810,24 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         // active list, so tasks that have converged cost nothing.
         const int tc_grid = std::min(w.n_tc * mtiles, g_nsm);
         const int mol_grid = std::min(w.n_mol * ltiles, 4 * g_nsm);
-        const int scan_grid = std::min(nw, 8 * g_nsm);
+        const int scan_grid = std::min(nw, 8 * g_nsm), scan4_grid = std::min(nw, 16 * g_nsm);
+        if (w.any_top) {
+            // skylight first-scatter source of the water column: the source pass
+            // over the unscattered skylight field, every task active, into J
+            const int itd = g.max_orders + 1;
+            LAUNCH(plan, KC_PRIMARY, k_dtop_field<<<nw, 256, 0, st>>>(B, W, G, w.t0));
+            LAUNCH(plan, KC_PRIMARY, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, itd));
+            if (w.n_simt) LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, itd));
+            if (w.n_tc)
+                LAUNCH(plan, KC_SOURCE_TC, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(
+                           B, W, G, w.t0, itd, mtiles));
+            if (w.n_mol && !w.n_tc)
+                LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
+                           B, W, G, w.t0, itd, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
+            CK(cudaMemsetAsync(g.active_cnt + (itd - 1), 0, sizeof(int), st));
+            CK(cudaMemsetAsync(g.mol_cnt + (itd - 1), 0, sizeof(int), st));
+        }
+        LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         for (int it = 2; it <= g.max_orders; ++it) {
             if (w.n_simt)
                 LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
@@ -786,7 +837,12 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             if (w.n_mol && !w.n_tc)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
-            LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, scan_smem_bytes(scan_threads), st>>>(B, W, G, w.t0, it));
+            if (g.Cq)
+                LAUNCH(plan, KC_SCAN, k_scan4<<<scan4_grid, scan4_threads(G), scan4_smem_bytes(scan4_threads(G)), st>>>(
+                           B, W, G, w.t0, it));
+            else
+                LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, scan_smem_bytes(scan_threads), st>>>(
+                           B, W, G, w.t0, it));
             if (capture) {
                 if (it == w.fwd_stop) break;
             } else if ((it - 1) % poll == 0 || it == g.max_orders) {
@@ -798,6 +854,8 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         if (capture && w.fwd_stop != INT_MAX)
             LAUNCH(plan, KC_EXTRACT, k_stop_check<<<1, 32, 0, st>>>(g.active_cnt + w.fwd_stop, g.err + 1));
         LAUNCH(plan, KC_EXTRACT, k_extract<<<(nw + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw));
+        if (g.edge)
+            LAUNCH(plan, KC_EXTRACT, k_edges<<<(nw * G.NR + 127) / 128, 128, 0, st>>>(B, W, G, w.t0, nw, g.edge));
         if (g.any_lut) LAUNCH(plan, KC_EXTRACT, k_lut_sample<<<nw, 128, 0, st>>>(B, W, make_lut(g), G, w.t0, nw));
         if (g.ncot) {
             const int rc = run_adjoint_wave(plan, g, w, B, W, st, tc_grid, mol_grid, mtiles, ltiles, sgrid, tc_smem,
@@ -862,6 +920,7 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_scan4, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -1439,3 +1498,365 @@ int ocrt_internal_fail(int rc, const char *msg)
 {
     return fail(rc, msg);
 }
+
+// ===================================================================
+// Coupled atmosphere-ocean solve (rt_solve_case_ocean, rt_solver.c:3468-6660)
+// ===================================================================
+namespace {
+
+double snell_down(double mu_air, double n)
+{
+    const double s2 = std::max(0.0, 1.0 - mu_air * mu_air) / (n * n);
+    return s2 >= 1.0 ? 0.0 : std::sqrt(1.0 - s2);
+}
+
+// Water column of one pixel on the host: optical budget, depth policy and
+// layer count (rt_water_rt.c:4405-4440, 5119-5180).
+struct WaterCol {
+    double ext, om_w, om_p, tau, depth;
+    int nt, m_loop;
+};
+
+int water_column(const ocrt_ocean &oc, WaterCol &wc)
+{
+    const double bp = oc.b_particle > 0.0 ? oc.b_particle : 0.0;
+    const double b_rt = oc.b_water + bp;
+    wc.ext = oc.a_total + b_rt;
+    if (!(wc.ext > 0.0)) return fail(OCRT_ERR_ARGS, "water column has no extinction");
+    wc.om_w = oc.b_water / wc.ext;
+    wc.om_p = bp / wc.ext;
+    if (oc.depth_m > 0.0) {
+        wc.tau = wc.ext * oc.depth_m;
+    } else {
+        double gp = 0.0;
+        if (bp > 0.0 && oc.L_particle >= 1) gp = std::min(0.999, std::max(-0.999, oc.beta[1] / 3.0));
+        const double sb = bp + oc.b_water;
+        const double ge = std::min(0.999, std::max(-0.999, sb > 0.0 ? bp * gp / sb : 0.0));
+        double z_req = (oc.tau_base > 0.0 ? oc.tau_base : 20.0) / wc.ext;
+        const double te = oc.a_total + b_rt * std::max(0.0, 1.0 - ge);
+        if (te > 0.0) z_req = std::max(z_req, -std::log(1.0e-8) / te);
+        wc.tau = wc.ext * z_req;
+    }
+    wc.depth = wc.tau / wc.ext;
+    int nt = (int)std::ceil(wc.tau / 0.05);
+    if (oc.n_layers_water > 0 && (oc.depth_m > 0.0 || oc.n_layers_water > nt)) nt = oc.n_layers_water;
+    wc.nt = std::max(nt, 1);
+    const int Lws = std::max(bp > 0.0 ? oc.L_particle : 0, 2);
+    wc.m_loop = std::min(oc.m_max_water, Lws);
+    return OCRT_OK;
+}
+
+int validate_ocean(const ocrt_case &c, const ocrt_opts &o, const ocrt_ocean &oc)
+{
+    if (c.surface != OCRT_SURFACE_OCEAN) return fail(OCRT_ERR_ARGS, "coupled solve needs surface OCRT_SURFACE_OCEAN");
+    if (!(c.wind_speed > 0.0)) return fail(OCRT_ERR_UNSUPPORTED, "coupled solve: flat interface (wind <= 0) not supported");
+    if (o.pssa) return fail(OCRT_ERR_UNSUPPORTED, "coupled solve: IPSS is not applied on this path");
+    if (!(oc.a_total >= 0.0) || !(oc.b_water >= 0.0) || !(oc.b_particle >= 0.0))
+        return fail(OCRT_ERR_ARGS, "water absorption / scattering must be >= 0");
+    if (oc.n_mu_water < 2 || oc.n_mu_water > OCRT_MAX_N) return fail(OCRT_ERR_ARGS, "n_mu_water outside [2, 64]");
+    if (oc.m_max_water < 0 || oc.m_max_water > OCRT_MAX_M) return fail(OCRT_ERR_ARGS, "m_max_water outside [0, 255]");
+    if (oc.max_orders_water < 1 || !(oc.tolerance_water > 0.0)) return fail(OCRT_ERR_ARGS, "bad water SOS control");
+    if (oc.n_layers_water < 0 || oc.n_layers_water > 4096) return fail(OCRT_ERR_ARGS, "n_layers_water outside [0, 4096]");
+    if (!oc.view_as_node) return fail(OCRT_ERR_UNSUPPORTED, "coupled solve: the water view is extracted at its node");
+    if (oc.b_particle > 0.0) {
+        if (oc.L_particle < 1 || oc.L_particle > 1024 || !oc.beta || !oc.gamma || !oc.alpha || !oc.zeta)
+            return fail(OCRT_ERR_ARGS, "hydrosol expansion missing");
+        for (int l = 0; l <= oc.L_particle; ++l)
+            if (!std::isfinite(oc.beta[l]) || !std::isfinite(oc.gamma[l]) || !std::isfinite(oc.alpha[l]) ||
+                !std::isfinite(oc.zeta[l])) return fail(OCRT_ERR_NONFINITE, "non-finite hydrosol moment");
+    }
+    return OCRT_OK;
+}
+
+int ocean_solve(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp, const ocrt_aerosol *aer, int app,
+                const ocrt_ocean *ocs, int ocp, ocrt_result *out, ocrt_ocean_result *wout, cudaStream_t st)
+{
+    if (n <= 0) return OCRT_OK;
+    const int Nw = ocs[0].n_mu_water;
+    std::vector<ocrt_case> ca(n);
+    std::vector<ocrt_opts> oa(n), ow(n);
+    std::vector<ocrt_aerosol> hyd(n);
+    std::vector<WaterCol> wc(n);
+    int nphi = -1;
+    for (int i = 0; i < n; ++i) {
+        const ocrt_opts &o = opp ? opts[i] : opts[0];
+        const ocrt_ocean &oc = ocp ? ocs[i] : ocs[0];
+        int rc = validate_ocean(cases[i], o, oc);
+        if (rc) return rc;
+        if (oc.n_mu_water != Nw) return fail(OCRT_ERR_ARGS, "coupled batch: n_mu_water must be common to the batch");
+        const int np = o.n_phi_surface > 0 ? o.n_phi_surface : 1024;
+        if (nphi >= 0 && np != nphi) return fail(OCRT_ERR_ARGS, "coupled batch: n_phi_surface must be common");
+        nphi = np;
+        ca[i] = cases[i];
+        ca[i].surface = OCRT_SURFACE_BLACK_FRESNEL_OCEAN;
+        if (!(ca[i].n_water > 0.0)) ca[i].n_water = 1.34;
+        oa[i] = o;
+        oa[i].n_mu = Nw;                        // shared node set (rt_solver.c:4006-4010)
+        rc = validate(&ca[i], &oa[i], aer ? (app ? &aer[i] : &aer[0]) : nullptr);
+        if (rc) return rc;
+        if ((rc = water_column(oc, wc[i]))) return rc;
+        ow[i] = oa[i];
+        ow[i].n_layers = wc[i].nt;
+        ow[i].fourier_m_max = wc[i].m_loop;
+        ow[i].max_orders = oc.max_orders_water;
+        ow[i].tolerance = oc.tolerance_water;
+        ow[i].gas = nullptr;
+        ow[i].pssa = 0;
+        memset(&hyd[i], 0, sizeof(ocrt_aerosol));
+        if (oc.b_particle > 0.0) {
+            hyd[i].tau_a = 1.0; hyd[i].ssa_a = 1.0; hyd[i].L_max = oc.L_particle;
+            hyd[i].beta = oc.beta; hyd[i].gamma = oc.gamma; hyd[i].alpha = oc.alpha; hyd[i].zeta = oc.zeta;
+        }
+    }
+    int rc = ensure_init();
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_mu);
+    ocrt_plan plan;
+    plan.n = n;
+    // host side of each pixel
+    std::vector<OceanPix> hop(n);
+    int Ma = 0;
+    for (int i = 0; i < n; ++i) Ma = std::max(Ma, oa[i].fourier_m_max);
+    for (int i = 0; i < n; ++i) {
+        const ocrt_case &c = cases[i];
+        const ocrt_opts &o = oa[i];
+        const ocrt_ocean &oc = ocp ? ocs[i] : ocs[0];
+        const ocrt_aerosol *a = aer ? (app ? &aer[i] : &aer[0]) : nullptr;
+        OceanPix &p = hop[i];
+        memset(&p, 0, sizeof(p));
+        p.mu_sa = std::cos(c.sza_deg * OCRT_PI / 180.0);
+        p.mu_va = std::cos(c.vza_deg * OCRT_PI / 180.0);
+        p.nw = ca[i].n_water;
+        p.mu_sw = snell_down(p.mu_sa, p.nw);
+        p.mu_vw = snell_down(p.mu_va, p.nw);
+        p.raa_deg = c.raa_deg; p.wind = c.wind_speed; p.st = c.sigma_type; p.qc = c.q_convention;
+        double tau_r = 0.0;
+        if (c.pressure_hpa > 0.0)
+            tau_r = o.tau_r_source == OCRT_TAU_R_FROM_INPUT ? c.tau_r_input : bodhaine_tau(c.wavelength_nm, c.pressure_hpa);
+        p.tau_atm = tau_r + ((a && a->tau_a > 0.0) ? a->tau_a : 0.0);
+        if (o.gas) {
+            double tg = 0.0;
+            if ((rc = ocrt_gb_gas_tau(o.gas, c.wavelength_nm, nullptr, &tg))) return rc;
+            p.tau_atm += tg;
+        }
+        p.ext_w = wc[i].ext;
+        p.M = o.fourier_m_max;
+        p.m_loop = wc[i].m_loop;
+        p.pa = i; p.pw = i;
+        p.top_off = (long long)i * (Ma + 1) * Nw * 3;
+        p.ext_off = (long long)i * (Ma + 1) * (Nw + 1) * 3;
+        // distinct water directions: Gauss + refracted view, nadir, refracted sun, air sun
+        std::vector<double> dirs;
+        {
+            std::vector<double> gm(Nw), gww(Nw);
+            // Gauss nodes as the device builds them (only their coincidence matters here)
+            for (int k = 1; k <= Nw; ++k) {
+                double t = std::cos(OCRT_PI * ((double)k - 0.25) / (2.0 * Nw + 0.5));
+                gm[k - 1] = t;
+            }
+            dirs = gm;
+            for (double x : {p.mu_vw, 1.0, p.mu_sw, p.mu_sa}) {
+                bool dup = false;
+                for (double y : dirs) if (std::fabs(x - y) < 1e-12) dup = true;
+                if (!dup) dirs.push_back(x);
+            }
+        }
+        p.n_ring_unique = (int)dirs.size();
+        (void)oc;
+    }
+    // ---- pass 1: atmosphere over the rough surface, bottom field exported ----
+    plan.groups.resize(3);
+    Group &GA = plan.groups[0], &GW = plan.groups[1], &GC = plan.groups[2];
+    for (int i = 0; i < n; ++i) { GA.idx.push_back(i); GW.idx.push_back(i); GC.idx.push_back(i); }
+    GA.N = GW.N = GC.N = Nw;
+    GA.E = GC.E = 1;
+    GW.E = OCRT_MAX_EXTRA;
+    int Mw = 0;
+    for (int i = 0; i < n; ++i) Mw = std::max(Mw, wc[i].m_loop);
+    GW.nphi_ww = std::max(176, 2 * Mw + 16);
+    const Geom GeA = make_geom(Nw, 1), GeW = make_geom(Nw, OCRT_MAX_EXTRA);
+    double *d_top = nullptr, *d_ext3 = nullptr, *d_td = nullptr, *d_view = nullptr, *d_glo = nullptr;
+    OceanPix *d_op = nullptr;
+    ocrt_result *d_out = nullptr;
+    ocrt_ocean_result *d_wout = nullptr;
+    auto cleanup = [&]() {
+        for (Group &g : plan.groups) { dfree(g.edge); free_group(g); }
+        dfree(d_top); dfree(d_ext3); dfree(d_td); dfree(d_view); dfree(d_glo); dfree(d_op); dfree(d_out); dfree(d_wout);
+    };
+    auto atm_patch = [&](int bottom) {
+        return [&, bottom](int q, PixDev &d) {
+            if (bottom) {
+                d.bottom_only = 1;
+                d.ext_off = hop[q].ext_off;
+                d.ext_mmax = std::min(hop[q].M, wc[q].m_loop);
+            }
+        };
+    };
+    if ((rc = build_group(GA, ca.data(), oa.data(), 1, aer, app, nullptr, 0, nullptr, nullptr, atm_patch(0)))) {
+        cleanup();
+        return rc;
+    }
+    rc = alloc(GA.edge, (size_t)GA.T * GeA.NR * OCRT_EDGE);
+    if (!rc) rc = run_group(&plan, GA, st, false);
+    if (rc) { cleanup(); return rc; }
+    // ---- skylight into the water ----
+    if ((rc = up(d_op, hop)) || (rc = alloc(d_td, (size_t)n * (GeA.NR + 1))) ||
+        (rc = alloc(d_top, (size_t)n * (Ma + 1) * Nw * 3))) { cleanup(); return rc; }
+    LAUNCH(&plan, KC_COXMUNK, k_taw_direct<<<dim3(Nw + 1, n), 128, 0, st>>>(d_op, n, GA.px, GA.gmu, Nw, GeA.NR, d_td));
+    LAUNCH(&plan, KC_COXMUNK, k_ocean_prep<<<(n + 127) / 128, 128, 0, st>>>(d_op, n, GA.pix_task0, GA.gmu, GA.gw, Nw,
+                                                                             GeA.NR, GA.edge, d_td));
+    {
+        const size_t smem = iface_smem_bytes(Ma, 128, 3 * (Ma + 1));
+        CK(cudaFuncSetAttribute(k_couple_aw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(smem + 1024, 227 * 1024)));
+        LAUNCH(&plan, KC_COXMUNK, k_couple_aw<<<dim3(Nw, n), 128, smem, st>>>(d_op, n, GA.pix_task0, GA.gmu, GA.gw, Nw,
+                                                                               GeA.NR, GA.edge, d_top));
+    }
+    // ---- pass 2: the water column ----
+    std::vector<ocrt_case> cw(n);
+    for (int i = 0; i < n; ++i) {
+        cw[i] = ca[i];
+        cw[i].surface = OCRT_SURFACE_BLACK;
+        cw[i].pressure_hpa = 0.0;
+    }
+    auto water_patch = [&](int q, PixDev &d) {
+        const OceanPix &p = hop[q];
+        const ocrt_ocean &oc = ocp ? ocs[q] : ocs[0];
+        d.medium = 1;
+        d.mu0 = p.mu_sw; d.mu_view = p.mu_vw;
+        d.xmu[0] = p.mu_vw; d.xmu[1] = 1.0; d.xmu[2] = p.mu_sw; d.xmu[3] = p.mu_sa;
+        d.n_ring = Nw + OCRT_MAX_EXTRA;
+        d.view_slot = Nw;
+        d.tau_total = wc[q].tau;
+        d.w_tau = wc[q].tau; d.w_omega_w = wc[q].om_w; d.w_omega_p = wc[q].om_p;
+        d.depol = OCRT_DEPOL_WATER;
+        // flat Fresnel transmission of the sun's beam: q = T[1,0] / T[0,0] (rt_water_rt.c:5627-5641)
+        {
+            const double n1 = 1.0, n2 = p.nw, mi = p.mu_sa;
+            const double st2 = (n1 / n2) * (n1 / n2) * std::max(0.0, 1.0 - mi * mi);
+            double bq = 0.0;
+            if (st2 < 1.0) {
+                const double mt = std::sqrt(1.0 - st2);
+                const double rs = (n1 * mi - n2 * mt) / (n1 * mi + n2 * mt), rp = (n2 * mi - n1 * mt) / (n2 * mi + n1 * mt);
+                const double ts = 1.0 + rs, tp = (n1 / n2) * (1.0 + rp);
+                const double Ts = ts * ts, Tp = tp * tp;
+                const double qk = p.qc == 1 ? 0.5 * (Tp - Ts) : 0.5 * (Ts - Tp);
+                bq = qk / (0.5 * (Ts + Tp));
+            }
+            d.beam_q = bq;
+        }
+        d.ext_off = p.top_off;
+        d.ext_mmax = p.M;
+        d.surface = OCRT_SURFACE_BLACK;
+        d.wind = p.wind; d.n_water = p.nw; d.sigma_type = p.st; d.q_conv = p.qc;
+        d.mom_off = oc.b_particle > 0.0 ? d.mom_off : -1;
+        if (oc.b_particle <= 0.0) { d.L_aer = -1; d.tau_a = 0.0; }
+    };
+    if ((rc = build_group(GW, cw.data(), ow.data(), 1, hyd.data(), 1, nullptr, 0, nullptr, nullptr, water_patch))) {
+        cleanup();
+        return rc;
+    }
+    GW.ext = d_top;
+    rc = alloc(GW.edge, (size_t)GW.T * GeW.NR * OCRT_EDGE);
+    if (!rc) {
+        CK(cudaFuncSetAttribute(k_rww, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::min<size_t>(iface_smem_bytes(GW.Mmax, GW.nphi_ww, 0) + 1024, 227 * 1024)));
+        rc = run_group(&plan, GW, st, false);
+    }
+    if (rc) { cleanup(); return rc; }
+    // ---- water-leaving radiance on the atmosphere ring and at the view ----
+    {
+        std::vector<double> hg(192);
+        std::vector<double> xg(96), wg(96);
+        // Gauss-Legendre 96 on (0, 1), as the reference's quadrature (rt_quadrature.c:20-61)
+        for (int k = 1; k <= 96; ++k) {
+            double t = std::cos(OCRT_PI * ((double)k - 0.25) / (192.0 + 0.5)), pn = 0, pm = 0, dp = 1;
+            for (int it = 0; it < 100; ++it) {
+                double a = 1.0, b = t;
+                for (int q = 1; q < 192; ++q) { const double cc = ((2.0 * q + 1.0) * t * b - (double)q * a) / (double)(q + 1); a = b; b = cc; }
+                pn = b; pm = a;
+                dp = 192.0 * (t * pn - pm) / (t * t - 1.0);
+                const double step = -pn / dp;
+                t += step;
+                if (std::fabs(step) < 1.0e-15 * (std::fabs(t) + 1.0)) break;
+            }
+            double a = 1.0, b = t;
+            for (int q = 1; q < 192; ++q) { const double cc = ((2.0 * q + 1.0) * t * b - (double)q * a) / (double)(q + 1); a = b; b = cc; }
+            dp = 192.0 * (t * b - a) / (t * t - 1.0);
+            xg[96 - k] = t;
+            wg[96 - k] = 2.0 / ((1.0 - t * t) * dp * dp);
+        }
+        for (int k = 0; k < 96; ++k) { hg[k] = xg[k]; hg[96 + k] = wg[k]; }
+        if ((rc = up(d_glo, hg)) || (rc = alloc(d_ext3, (size_t)n * (Ma + 1) * GeA.NR * 3)) ||
+            (rc = alloc(d_view, (size_t)n * 3 * (OCRT_MAX_M + 1)))) { cleanup(); return rc; }
+        CK(cudaMemsetAsync(d_ext3, 0, sizeof(double) * (size_t)n * (Ma + 1) * GeA.NR * 3, st));
+        CK(cudaMemsetAsync(d_view, 0, sizeof(double) * (size_t)n * 3 * (OCRT_MAX_M + 1), st));
+        LAUNCH(&plan, KC_COXMUNK, k_water_modes<<<(n + 127) / 128, 128, 0, st>>>(d_op, n, GW.px, GW.pix_task0, GeW.NR,
+                                                                                 GW.edge));
+        const int Mc = std::max(Ma, Mw);
+        const size_t extra = 3 * (size_t)(Mc + 1) + GeW.NR + (GeW.NR + 1) / 2 + 1;
+        const size_t smem = iface_smem_bytes(Mc, 128, (int)extra);
+        CK(cudaFuncSetAttribute(k_couple_wa, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(smem + 1024, 227 * 1024)));
+        LAUNCH(&plan, KC_COXMUNK, k_couple_wa<<<dim3(GeA.NR + 1, n), 128, smem, st>>>(
+                   d_op, n, GA.px, GW.px, GW.pix_task0, GA.gmu, Nw, GeA.NR, GeW.NR, GW.edge, d_glo, d_ext3, d_view));
+    }
+    // ---- pass 3: the atmosphere driven by the water-leaving radiance ----
+    if ((rc = build_group(GC, ca.data(), oa.data(), 1, aer, app, nullptr, 0, nullptr, nullptr, atm_patch(1)))) {
+        cleanup();
+        return rc;
+    }
+    GC.ext = d_ext3;
+    if ((rc = run_group(&plan, GC, st, false))) { cleanup(); return rc; }
+    // ---- outputs ----
+    if ((rc = alloc(d_out, n)) || (rc = alloc(d_wout, n))) { cleanup(); return rc; }
+    LAUNCH(&plan, KC_FINAL, k_ocean_final<<<(n + 127) / 128, 128, 0, st>>>(
+               d_op, n, GA.px, GW.px, GW.pix_task0, GA.gmu, GA.gw, Nw, GeW.NR, GW.edge, d_view, d_top, GA.res, GW.res,
+               GC.res, d_out, d_wout));
+    std::vector<ocrt_result> ho(n);
+    std::vector<ocrt_ocean_result> hw(n);
+    CK(cudaMemcpyAsync(ho.data(), d_out, sizeof(ocrt_result) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hw.data(), d_wout, sizeof(ocrt_ocean_result) * n, cudaMemcpyDeviceToHost, st));
+    for (Group &g : plan.groups) {
+        if ((rc = group_flags(&plan, g, st))) { cleanup(); return rc; }
+    }
+    CK(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; ++i) {
+        if (out) out[i] = ho[i];
+        if (wout) wout[i] = hw[i];
+    }
+    cleanup();
+    return OCRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+void ocrt_ocean_default(ocrt_ocean *oc)
+{
+    if (!oc) return;
+    memset(oc, 0, sizeof(*oc));
+    oc->n_mu_water = 48; oc->m_max_water = 2; oc->max_orders_water = 20; oc->tolerance_water = 1e-7;
+    oc->tau_base = 20.0; oc->view_as_node = 1;
+}
+
+int ocrt_gb_solve_batch_ocean(int n, const ocrt_case *cases, const ocrt_opts *opts, int opts_per_case,
+                              const ocrt_aerosol *aer, int aer_per_case, const ocrt_ocean *oc, int oc_per_case,
+                              ocrt_result *out, ocrt_ocean_result *wout, void *stream)
+{
+    if (n < 0 || (n > 0 && (!cases || !opts || !oc))) return fail(OCRT_ERR_ARGS, "bad batch arguments");
+    const int rc = ensure_init();
+    if (rc) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : g_stream;
+    return ocean_solve(n, cases, opts, opts_per_case, aer, aer_per_case, oc, oc_per_case, out, wout, st);
+}
+
+int ocrt_gb_solve_ocean(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer, const ocrt_ocean *oc,
+                        ocrt_result *out, ocrt_ocean_result *wout)
+{
+    if (!cs || !oc || !out) return fail(OCRT_ERR_ARGS, "null case, water column or output");
+    ocrt_opts def;
+    if (!opts) { ocrt_opts_default(&def); opts = &def; }
+    return ocrt_gb_solve_batch_ocean(1, cs, opts, 0, aer, 0, oc, 0, out, wout, nullptr);
+}
+
+} // extern "C"

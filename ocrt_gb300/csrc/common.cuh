@@ -6,14 +6,16 @@
 // pixel range, so all setup that is per pixel-and-mode is built per wave.
 //
 // Direction ring of a pixel (internal order, not the reference's sorted
-// order): slots 0..N-1 are the Gauss nodes in ascending mu, slot N is the
-// zero-weight view node when one is inserted (rt_angle_grid.c:37-73).
-// NR = N + 1 is the padded ring width.  Field columns:
-//     Gauss slot g < N:  c = s * 2N + h * N + g
-//     view slot  g = N:  c = 6N + 2s + h
+// order): slots 0..N-1 are the Gauss nodes in ascending mu, slots N..N+E-1
+// zero-weight directions (rt_angle_grid.c:37-73): in the atmosphere E = 1, the
+// view node when one is inserted; in the water column E = 4, the refracted
+// view, nadir, refracted sun and air-side sun directions (rt_water_rt.c:5236-
+// 5298).  NR = N + E is the padded ring width.  Field columns:
+//     Gauss slot g < N:        c = s * 2N + h * N + g
+//     zero-weight slot g >= N: c = 6N + 6(g - N) + 2s + h
 // (s in {I,Q,U}, h = 0 up / 1 down), so the weighted inputs of the source
 // contraction are exactly columns [0, 6N) -- six 16-byte aligned blocks of N --
-// and the view columns follow.  Field rows are levels k = 0 (TOA) .. nt.
+// and the zero-weight columns follow.  Field rows are levels k = 0 (TOA) .. nt.
 // Source operators are stored output-major, Aop[c_out][c_in] with c_in in
 // [0, 6N) contiguous and NP >= 6N + 6 output rows (multiple of 16).
 #pragma once
@@ -25,6 +27,8 @@
 #define OCRT_MAX_M 255
 #define OCRT_DEPOL 0.0279
 #define OCRT_ZTOP_KM 100.0
+#define OCRT_DEPOL_WATER 0.039   // pure seawater (rt_water_rt.c:2121)
+#define OCRT_MAX_EXTRA 4        // zero-weight ring slots
 
 struct GasDev;
 
@@ -47,6 +51,16 @@ struct PixDev {
     int lut_nv, lut_nr;     // angle-grid LUT size (0 = no LUT)
     long long lut_vo, lut_ro, lut_oo;   // offsets of the grid vza, grid raa and the LUT outputs
     const GasDev *gas;      // device gas tables, nullptr = no gas absorption
+    // ---- coupled atmosphere-ocean (ocrt_gb_solve_ocean) ----
+    int medium;             // 0 atmosphere, 1 water column (top boundary = internal reflection)
+    int bottom_only;        // atmosphere driven only by ext_bottom (no solar primary, no seeds)
+    long long ext_off;      // offset of this pixel's [M+1][NR][3] ext_bottom (atmosphere) or
+                            // skylight top source (water, [M+1][N][3]) in BatchBufs::ext; -1 = none
+    int ext_mmax;           // last mode the boundary source holds
+    double depol;           // molecular depolarisation: 0.0279 air, 0.039 water
+    double beam_q;          // incident-beam polarisation Q/I (water: Fresnel transmission)
+    double xmu[OCRT_MAX_EXTRA];   // cosines of the zero-weight slots N.. (water: set by the host)
+    double w_tau, w_omega_w, w_omega_p;   // water: optical depth, pure-water and hydrosol albedo
     // ---- derived on device (k_pixel_setup) ----
     double mu0, mu_view, tau_r, tau_total;
     int n_ring, view_slot;  // view_slot: ring slot holding mu_view, -1 = interpolate
@@ -78,19 +92,20 @@ struct TaskOut {
 };
 
 struct Geom {
-    int N, NR, LDC;         // LDC: field row stride (floats)
+    int N, E, NR, LDC;      // E zero-weight slots, NR = N + E; LDC: field row stride (floats)
     int CIN;                // 6N weighted input columns (operator row stride)
-    int COUT;               // 6N + 6 output columns
+    int COUT;               // 6N + 6E output columns
     int NP;                 // operator rows, COUT rounded up to 16
 };
 
-__host__ __device__ inline Geom make_geom(int N)
+__host__ __device__ inline Geom make_geom(int N, int E = 1)
 {
     Geom g;
     g.N = N;
-    g.NR = N + 1;
+    g.E = E;
+    g.NR = N + E;
     g.CIN = 6 * N;
-    g.COUT = 6 * N + 6;
+    g.COUT = 6 * N + 6 * E;
     g.LDC = (g.COUT + 7) & ~7;
     g.NP = (g.COUT + 15) & ~15;
     return g;
@@ -98,7 +113,33 @@ __host__ __device__ inline Geom make_geom(int N)
 
 __host__ __device__ inline int col_of(const Geom &g, int s, int h, int slot)
 {
-    return slot < g.N ? s * 2 * g.N + h * g.N + slot : 6 * g.N + 2 * s + h;
+    return slot < g.N ? s * 2 * g.N + h * g.N + slot : 6 * g.N + 6 * (slot - g.N) + 2 * s + h;
+}
+
+// Field column -> (Stokes s, hemisphere h, ring slot g); columns past the
+// zero-weight block decode to slot NR (never a valid ring slot).
+__host__ __device__ inline void decode_col(const Geom &G, int c, int &s, int &h, int &g)
+{
+    const int N = G.N;
+    if (c < 6 * N) {
+        s = c / (2 * N);
+        const int r = c - s * 2 * N;
+        h = r / N;
+        g = r - h * N;
+    } else if (c < G.COUT) {
+        const int v = c - 6 * N, e = v / 6, r = v - 6 * e;
+        s = r >> 1; h = r & 1; g = N + e;
+    } else {
+        s = 0; h = 0; g = G.NR;
+    }
+}
+
+// Cosine of ring slot g (Gauss node or zero-weight direction); slots past the
+// pixel's ring get 1 so that every coefficient stays finite.
+__host__ __device__ inline double ring_mu(const PixDev &d, const double *gmu, int N, int g)
+{
+    if (g >= d.n_ring) return 1.0;
+    return g < N ? gmu[g] : d.xmu[g - N];
 }
 
 // Input column (weighted Gauss direction) -> field column: the identity.
@@ -167,6 +208,16 @@ __device__ inline void cp_async8(float2 *dst_smem, const float2 *src)
 {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ inline void cp_async16_cg(float4 *dst_smem, const float *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ inline void cp_async16_ca(float4 *dst_smem, const float *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }

@@ -9,15 +9,28 @@
 __global__ void k_gauss(int N, double *mu, double *w, float *pw);
 __global__ void k_pixel_setup(PixDev *px, int P, int N, const double *gmu);
 __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double *xd, double *yd, double *z);
+__global__ void k_levels_water(const PixDev *px, int P, double *h, double *ch, double *xd, double *yd, double *z);
 __global__ void k_level_mix(const PixDev *px, int P, const double *z, double *xd, double *yd);
-__global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const double *h,
+__global__ void k_coef(const PixDev *px, int P, int N, int NR, const double *gmu, const double *h,
                        float *Tc, float *Ca, float *Cb);
+__global__ void k_coef_quads(const PixDev *px, int P, int N, int NR, const float *Tc, const float *Ca, const float *Cb,
+                             float *Cq);
 __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt);
-__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx);
+__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, int E, float *Bx);
 // k_scan: levels in flight per column (cp.async ring depth, a power of two)
 // and its dynamic shared memory: J, the total's FP32 head and 3 coefficients per slot.
 #define SCAN_DEPTH 8
 inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (4 + 4 + 12); }
+// k_scan4: four Gauss columns of one (Stokes, hemisphere) per thread, moved
+// as 16-byte copies; the zero-weight columns one per thread.  It applies when
+// N is a multiple of 4.
+#define SCAN4_DEPTH 8
+__host__ __device__ inline int scan4_threads(const Geom &G) { return ((6 * G.N / 4 + 6 * G.E + 31) / 32) * 32; }
+inline size_t scan4_smem_bytes(int threads) { return (size_t)SCAN4_DEPTH * 5 * threads * 16; }
+__host__ __device__ inline long long coef_quad_off(long long coef_off, int N, int NR)
+{
+    return coef_off / NR * 3 * N;
+}
 // k_adj_scan: cotangent rows per block (they share the transport coefficients)
 #define ADJ_RB 3
 inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 4) + 12); }
@@ -103,11 +116,13 @@ struct BatchBufs {
     const float *pw;       // [2N]: (float)(2 pi mu_i w_i) for m = 0, then (float)(pi mu_i w_i)
     const double *h, *ch, *xd, *yd, *z;
     const float *Tc, *Ca, *Cb;
+    const float *Cq;       // Gauss-slot transport weights in quads for k_scan4 (k_coef_quads), or nullptr
     const float *frs;
     const float *Eatt;     // rough direct-beam attenuation [lev_off*NR + k*NR + g]
     const float *lvf;      // [lev_off + k][3]: x_k, y_k, direct beam ch_k rounded to FP32
     int *active_cnt;       // [max_orders + 2]: tasks still active after order it
     int *mol_cnt;          // [max_orders + 2]: molecular (m <= 2) tasks still active after order it
+    const double *ext;     // per-pixel boundary sources at PixDev::ext_off (coupled ocean), or nullptr
     int *alist[2];         // ping-pong active-task lists (wave-local ids); order it reads alist[it & 1]
     int *mlist[2];         // same for the molecular tasks
     int *work;             // [max_orders + 2][4] work counters of the persistent kernels
@@ -183,6 +198,7 @@ bool tc_supported(const Geom &G);
 size_t tc_adj_smem_bytes(const Geom &G);
 bool tc_adj_supported(const Geom &G);
 __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
+__global__ void k_scan4(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 __global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int ltiles,
                               const float *Bp, const float *Br, const float *Bt, int L);
 inline size_t mol_smem_bytes(const Geom &G) { return sizeof(float) * (4 * G.N + G.COUT * 24 + 32 * G.CIN + 32 * 25); }
@@ -196,3 +212,43 @@ __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z
 __global__ void k_finalize(const PixDev *px, int P, const TaskState *state, const TaskOut *tout,
                            const double *gmu, const double *gw, const double *h,
                            const double *kappa, const double *tau_dir, ocrt_result *res);
+
+// ocean.cu — coupled atmosphere-ocean solve
+#define OCRT_EDGE 12      // doubles per (task, ring slot) of k_edges
+// One coupled pixel: its place in the three passes and the scalars of the
+// interface coupling.
+struct OceanPix {
+    // ---- host ----
+    double mu_sa, mu_va, mu_sw, mu_vw, raa_deg, nw, wind, tau_atm, ext_w;
+    int st, qc, M, m_loop;        // atmosphere modes; water modes solved (min(m_max_water, L))
+    int pa, pw;                   // pixel index in the atmosphere groups / the water group
+    int n_ring_unique;            // distinct water directions (Gauss + zero-weight)
+    long long top_off;            // skylight top source [M+1][N][3] in the water group's ext buffer
+    long long ext_off;            // water-leaving bottom source [M+1][NRa][3] in the pass-3 ext buffer
+    // ---- device ----
+    double T_dir, F_boa, F_w, Ed_sky_w, Ed_sky_a;
+    int m_view, m_nodes;          // last water mode with a view sample / with node values
+};
+__global__ void k_edges(BatchBufs B, WaveBufs W, Geom G, int t0, int nw, double *edge);
+__global__ void k_rww(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
+                      const double *gmu, int nphi, float *srf);
+__global__ void k_taw_direct(const OceanPix *op, int P, const PixDev *pxa, const double *gmu, int N, int NRa, double *td);
+__global__ void k_ocean_prep(OceanPix *op, int P, const int *task0_a, const double *gmu, const double *gw, int N,
+                             int NRa, const double *edge_a, const double *td);
+__global__ void k_couple_aw(const OceanPix *op, int P, const int *task0_a, const double *gmu, const double *gw,
+                            int N, int NRa, const double *edge_a, double *top);
+__global__ void k_dtop_field(BatchBufs B, WaveBufs W, Geom G, int t0);
+__global__ void k_water_modes(OceanPix *op, int P, const PixDev *pxw, const int *task0_w, int NRw, const double *edge_w);
+__global__ void k_couple_wa(const OceanPix *op, int P, const PixDev *pxa, const PixDev *pxw, const int *task0_w,
+                            const double *gmu, int N, int NRa, int NRw, const double *edge_w, const double *glo,
+                            double *ext3, double *view);
+__global__ void k_ocean_final(const OceanPix *op, int P, const PixDev *pxa, const PixDev *pxw, const int *task0_w,
+                              const double *gmu, const double *gw, int N, int NRw, const double *edge_w,
+                              const double *view, const double *top, const ocrt_result *r1, const ocrt_result *rw,
+                              const ocrt_result *r3, ocrt_result *out, ocrt_ocean_result *wout);
+// shared-memory bytes of the interface-projection kernels for M modes
+inline size_t iface_smem_bytes(int M, int nphi, int extra_doubles)
+{
+    return sizeof(float) * ((size_t)(M + 1) * nphi * 2 + (size_t)nphi * 9 + (((size_t)(M + 1) * 9 + 1) & ~(size_t)1)) +
+           sizeof(double) * (size_t)extra_doubles;
+}

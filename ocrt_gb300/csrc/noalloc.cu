@@ -132,6 +132,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     d.nphi = opts->n_phi_surface > 0 ? opts->n_phi_surface : 1024;
     d.mom_off = -1; d.L_aer = -1;
     d.gas = opts->gas ? opts->gas->dev : nullptr;
+    d.depol = OCRT_DEPOL; d.ext_off = -1;
     if (aer) { d.mom_off = 0; d.L_aer = aer->L_max; d.tau_a = aer->tau_a; d.ssa_a = aer->ssa_a; }
     d.L = M > 2 ? M : 2;
     if (d.L_aer > d.L) d.L = d.L_aer;
@@ -224,7 +225,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_LAUNCH(k_levels<<<dim3(2, 1), 256, 0, st>>>(px, 1, h, ch, xd, yd, z));
     NA_LAUNCH(k_level_mix<<<dim3(2, 1), 256, 0, st>>>(px, 1, z, xd, yd));
     if (opts->gas) NA_LAUNCH(k_gas_apply<<<1, 256, 0, st>>>(px, 1, h, ch, xd, yd, z, tabs));
-    NA_LAUNCH(k_coef<<<dim3(16, 1), 256, 0, st>>>(px, 1, N, gmu, h, Tc, Ca, Cb));
+    NA_LAUNCH(k_coef<<<dim3(16, 1), 256, 0, st>>>(px, 1, N, NR, gmu, h, Tc, Ca, Cb));
     NA_LAUNCH(k_basis_gauss<<<T, 64, 0, st>>>(N, M, L, gmu, Bp, Br, Bt));
     if (rough) {
         NA_LAUNCH(k_cs_table<<<T + 1, 256, 0, st>>>(M, d.nphi, cst));
@@ -238,7 +239,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
 
     BatchBufs B;
     B.px = px; B.tasks = tasks; B.state = state; B.tout = tout; B.gmu = gmu; B.gw = gw; B.pw = pwt;
-    B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.frs = frs; B.Eatt = Eatt; B.lvf = lvf;
+    B.h = h; B.ch = ch; B.xd = xd; B.yd = yd; B.z = z; B.Tc = Tc; B.Ca = Ca; B.Cb = Cb; B.Cq = nullptr; B.frs = frs; B.Eatt = Eatt; B.lvf = lvf;
     B.active_cnt = active; B.err = err; B.mol_cnt = molcnt; B.work = work; B.molV = nullptr;
     B.alist[0] = alist0; B.alist[1] = alist1; B.mlist[0] = mlist0; B.mlist[1] = mlist1;
     WaveBufs W;
@@ -253,7 +254,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_CK(cudaMemsetAsync(active, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
         NA_CK(cudaMemsetAsync(molcnt, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
         NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
-        NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, Bx));
+        NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, 1, Bx));
         NA_LAUNCH(k_tables<<<dim3(nw, tables_yblocks(256, G.NR, G.N)), 256, tables_smem_bytes(256, G.N, L), st>>>(
             tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec, nullptr, 1));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));

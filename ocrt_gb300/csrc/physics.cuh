@@ -206,6 +206,23 @@ __device__ inline void fresnel_R(T mu_i, T nw, int qconv, T *M)
     M[0] = T(0.5) * (Rs + Rp); M[1] = q; M[3] = q; M[4] = T(0.5) * (Rs + Rp); M[8] = rs * rp;
 }
 
+// Water-side reflection Mueller at incidence mu_i from the water (n_w -> 1),
+// identity beyond the critical angle (shared/surface.c:385-422 with n1 = n_w).
+template <typename T>
+__device__ inline void fresnel_R_water(T mu_i, T nw, int qconv, T *M)
+{
+#pragma unroll
+    for (int i = 0; i < 9; ++i) M[i] = T(0);
+    const T st2 = nw * nw * fmax(T(0), T(1) - mu_i * mu_i);
+    if (st2 >= T(1)) { M[0] = M[4] = M[8] = T(1); return; }
+    const T mt = sqrt(T(1) - st2);
+    const T rs = (nw * mu_i - mt) / (nw * mu_i + mt);
+    const T rp = (mu_i - nw * mt) / (mu_i + nw * mt);
+    const T Rs = rs * rs, Rp = rp * rp;
+    const T q = qconv == 1 ? T(0.5) * (Rp - Rs) : T(0.5) * (Rs - Rp);
+    M[0] = T(0.5) * (Rs + Rp); M[1] = q; M[3] = q; M[4] = T(0.5) * (Rs + Rp); M[8] = rs * rp;
+}
+
 __host__ __device__ inline double slope_variance(double ws, int sigma_type)
 {
     if (sigma_type == 1) return 0.003 + 0.00512 * fmax(0.01, ws);
@@ -252,9 +269,12 @@ __device__ inline double sancer_lambda_ds2(double mu, double slen)
 // algebraically identical to cos(omega) = sqrt((1 - cosTheta)/2) and
 // tan^2(beta) = (1 - cos^2 beta)/cos^2 beta of the reference; near the specular
 // peak the reference form loses ~eps/sigma^2 in FP32.
+// water_side: the internal reflection of an upward beam at the underside of
+// the surface (shared/surface.c:1136-1238): the same facet geometry, slope
+// density and shadowing, with the water-to-air facet Fresnel matrix.
 template <typename T>
 __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T shalf2, T sig2, T lam,
-                                 T nw, int qconv, T *R, T *tb2_out = nullptr)
+                                 T nw, int qconv, T *R, T *tb2_out = nullptr, bool water_side = false)
 {
 #pragma unroll
     for (int i = 0; i < 9; ++i) R[i] = T(0);
@@ -289,7 +309,8 @@ __device__ inline void coxmunk_R(T mu_out, T mu_in_dn, T cphi, T sphi, T shalf2,
         if (nn < T(1e-12)) { c2 = T(1); si2 = T(0); } else { c2 /= nn; si2 /= nn; }
     }
     T MF[9];
-    fresnel_R<T>(cw, nw, qconv, MF);
+    if (water_side) fresnel_R_water<T>(cw, nw, qconv, MF);
+    else fresnel_R<T>(cw, nw, qconv, MF);
     const T cb2 = cb * cb;
     const T tb2 = Bt / A2;
     if (tb2_out) *tb2_out = tb2;

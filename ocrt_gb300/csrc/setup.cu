@@ -46,8 +46,16 @@ __global__ void k_pixel_setup(PixDev *px, int P, int N, const double *gmu)
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     PixDev &d = px[p];
+    if (d.medium == 1) {
+        // water column: the host sets mu0 (refracted sun), mu_view (refracted
+        // view), the zero-weight slots and the optical depth; no surface below
+        d.view_slot = N;
+        d.surf_on = d.flat = d.rough = 0;
+        return;
+    }
     d.mu0 = cos(d.sza_deg * OCRT_PI / 180.0);
     d.mu_view = cos(d.vza_deg * OCRT_PI / 180.0);
+    d.xmu[0] = d.mu_view;
     double tr;
     if (!(d.pressure_hpa > 0.0)) tr = 0.0;
     else if (d.tau_r_source == 1) tr = d.tau_r_input;
@@ -78,6 +86,7 @@ __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double 
     const int p = blockIdx.y;
     if (p >= P) return;
     const PixDev &d = px[p];
+    if (d.medium == 1) return;
     const int nt = d.nt;
     const double tau = d.tau_total, tr = d.tau_r;
     const int aer = d.mom_off >= 0 && d.tau_a > 0.0;
@@ -124,13 +133,33 @@ __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double 
     }
 }
 
+// Levels of a homogeneous water column (build_inwater_atm, rt_water_rt.c:2163-
+// 2176): h_k = k tau / nt from the surface down, direct beam exp(-h/mu_sw)/2,
+// hydrosol and pure-water scattering fractions constant.
+__global__ void k_levels_water(const PixDev *px, int P, double *h, double *ch, double *xd, double *yd, double *z)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    if (d.medium != 1) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= d.nt; k += gridDim.x * blockDim.x) {
+        const long long o = d.lev_off + k;
+        const double hk = (double)k * d.w_tau / (double)d.nt;
+        h[o] = hk;
+        ch[o] = 0.5 * exp(-hk / d.mu0);
+        xd[o] = d.w_omega_p;
+        yd[o] = d.w_omega_w;
+        z[o] = 0.0;
+    }
+}
+
 // Layer scattering fractions once every level altitude is known.
 __global__ void k_level_mix(const PixDev *px, int P, const double *z, double *xd, double *yd)
 {
     const int p = blockIdx.y;
     if (p >= P) return;
     const PixDev &d = px[p];
-    if (!(d.mom_off >= 0 && d.tau_a > 0.0)) return;
+    if (d.medium == 1 || !(d.mom_off >= 0 && d.tau_a > 0.0)) return;
     const double tr = d.tau_r, ta = d.tau_a, ah = d.aer_h_km > 0.0 ? d.aer_h_km : 2.0;
     for (int k = 1 + blockIdx.x * blockDim.x + threadIdx.x; k <= d.nt; k += gridDim.x * blockDim.x) {
         const long long o = d.lev_off + k;
@@ -149,19 +178,17 @@ __global__ void k_level_mix(const PixDev *px, int P, const double *z, double *xd
 //   I_k = T I_up + Ca J_k + Cb J_up,  G = (1-T)|mu|/dtau - T, Ca = (1-T-G)/2, Cb = G/2
 // (the reference's slope/intercept form of rt_layer_transport.c:89-99 expanded,
 // which keeps every weight non-negative).  Computed in FP64, stored FP32.
-__global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const double *h,
+__global__ void k_coef(const PixDev *px, int P, int N, int NR, const double *gmu, const double *h,
                        float *Tc, float *Ca, float *Cb)
 {
     const int p = blockIdx.y;
     if (p >= P) return;
     const PixDev &d = px[p];
-    const int NR = N + 1;
     const int total = d.nt * NR;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         const int layer = e / NR, g = e - layer * NR;
         const long long o = d.coef_off + e;
-        double am = g < N ? gmu[g] : d.mu_view;
-        if (g >= d.n_ring) am = 1.0;
+        const double am = ring_mu(d, gmu, N, g);
         const double dtau = h[d.lev_off + layer + 1] - h[d.lev_off + layer];
         const double x = dtau / am;
         const double T = exp(-x);
@@ -169,6 +196,27 @@ __global__ void k_coef(const PixDev *px, int P, int N, const double *gmu, const 
         Tc[o] = (float)T;
         Ca[o] = (float)(0.5 * (1.0 - T - G));
         Cb[o] = (float)(0.5 * G);
+    }
+}
+
+// The Gauss-slot weights regrouped for k_scan4: per (layer, quad of slots
+// g = 4q..4q+3) the four T, then the four Ca, then the four Cb, so that one
+// 16-byte copy brings one weight of four columns.
+__global__ void k_coef_quads(const PixDev *px, int P, int N, int NR, const float *Tc, const float *Ca, const float *Cb,
+                             float *Cq)
+{
+    const int p = blockIdx.y;
+    if (p >= P) return;
+    const PixDev &d = px[p];
+    const int total = d.nt * N, nq = N / 4;
+    const long long qo = coef_quad_off(d.coef_off, N, NR);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        const int layer = e / N, g = e - layer * N;
+        const long long src = d.coef_off + (long long)layer * NR + g;
+        const long long dst = qo + ((long long)(layer * nq + (g >> 2)) * 3) * 4 + (g & 3);
+        Cq[dst] = Tc[src];
+        Cq[dst + 4] = Ca[src];
+        Cq[dst + 8] = Cb[src];
     }
 }
 
@@ -251,17 +299,20 @@ __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp,
     });
 }
 
-// GSF basis at the solar direction (-mu0) and at mu_view for every task of a
-// wave: Bx[((t*2 + which)*3 + comp)*(L+1) + l].
-__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, float *Bx)
+// GSF basis at the solar direction (-mu0) and at the E zero-weight slots for
+// every task of a wave: Bx[((t*(1+E) + which)*3 + comp)*(L+1) + l], which 0 =
+// sun, 1 + e = slot N + e.
+__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, int E, float *Bx)
 {
-    const int tl = blockIdx.x * (blockDim.x / 2) + threadIdx.x / 2;
-    const int which = threadIdx.x & 1;
+    const int W = 1 + E, per = blockDim.x / W;
+    if ((int)threadIdx.x >= per * W) return;
+    const int tl = blockIdx.x * per + threadIdx.x / W;
+    const int which = threadIdx.x % W;
     if (tl >= nt_tasks) return;
     const TaskDev tk = tasks[t0 + tl];
     const PixDev &d = px[tk.pix];
-    const double x = which == 0 ? -d.mu0 : d.mu_view;
-    float *dst = Bx + ((size_t)tl * 2 + which) * 3 * (L + 1);
+    const double x = which == 0 ? -d.mu0 : d.xmu[which - 1];
+    float *dst = Bx + ((size_t)tl * W + which) * 3 * (L + 1);
     for (int l = 0; l <= L; ++l) { dst[l] = 0.f; dst[L + 1 + l] = 0.f; dst[2 * (L + 1) + l] = 0.f; }
     gsf_recur(d.L, tk.m, x, [&](int l, double P, double R, double T) {
         dst[l] = (float)P; dst[L + 1 + l] = (float)R; dst[2 * (L + 1) + l] = (float)T;
@@ -313,18 +364,18 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     const int m = tk.m, N = G.N, n = d.n_ring, Lp = d.L;
     const int aer = d.mom_off >= 0 && d.tau_a > 0.0;
     const int La = aer ? d.L_aer : -1;
-    const float *bx = Bx + (size_t)tl * 2 * 3 * (L + 1);        // [which][comp][l]
+    const float *bx = Bx + (size_t)tl * (1 + G.E) * 3 * (L + 1);        // [which][comp][l]
     const size_t gb = (size_t)m * (L + 1) * N;
-    // basis accessor: slot s in 0..N-1 Gauss, s == N view, s == -1 solar
+    // basis accessor: slot s in 0..N-1 Gauss, s >= N zero-weight slot, s == -1 solar
     auto basis = [&](int comp, int s, int l) -> float {
         if (s < 0) return bx[(size_t)(0 * 3 + comp) * (L + 1) + l];
-        if (s >= N) return bx[(size_t)(1 * 3 + comp) * (L + 1) + l];
+        if (s >= N) return bx[(size_t)((1 + s - N) * 3 + comp) * (L + 1) + l];
         const float *B = comp == 0 ? Bp : (comp == 1 ? Br : Bt);
         return B[gb + (size_t)l * N + s];
     };
     // molecular l = 2 basis with mirror parity p(-x) = (-1)^m p(x), t(-x) = -(-1)^m t(x)
     const float par = (m & 1) ? -1.f : 1.f;
-    const double A = 2.0 * (1.0 - OCRT_DEPOL) / (2.0 + OCRT_DEPOL);
+    const double A = 2.0 * (1.0 - d.depol) / (2.0 + d.depol);
     const float b0 = m == 0 ? 1.f : 0.f, b2 = (float)(0.5 * A), g2 = (float)(-A * sqrt(1.5)), a2 = (float)(3.0 * A);
     const int mol = m <= 2;
     float *Aop = ops + tk.op_off;
@@ -459,13 +510,13 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     if (mine1) emit(E1, O1, i1);
     }
     if (blockIdx.y != 0) return;
-    // tile rows no pair writes: the view rows when the view is a Gauss node,
-    // and the padding rows COUT .. NP - 1
+    // tile rows no pair writes: the rows of unused zero-weight slots (the view
+    // when it is a Gauss node), and the padding rows COUT .. NP - 1
     if (Atile) {
-        const int nz0 = n == N ? 6 : 0, nz = nz0 + (G.NP - G.COUT);
+        const int nz0 = 6 * (G.NR - n), nz = nz0 + (G.NP - G.COUT);
         for (int e = threadIdx.x; e < nz * G.CIN; e += blockDim.x) {
             const int q = e / G.CIN, ci = e - q * G.CIN;
-            tile_put(Atile, G, q < nz0 ? 6 * N + q : G.COUT + (q - nz0), ci, 0.f);
+            tile_put(Atile, G, q < nz0 ? 6 * N + 6 * (n - N) + q : G.COUT + (q - nz0), ci, 0.f);
         }
     }
     // ---- molecular operator (m <= 2) in factored form U[c_out][24] ----
@@ -513,10 +564,10 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
 #pragma unroll
             for (int q = 0; q < 24; ++q) Bop[(size_t)c * 24 + q] = u[q];
         }
-        // the view rows when the view is a Gauss node (the buffer is not cleared
-        // between waves on the tensor-core path)
-        if (n == N)
-            for (int e = threadIdx.x; e < 6 * 24; e += blockDim.x) Bop[(size_t)(6 * N) * 24 + e] = 0.f;
+        // rows of unused zero-weight slots (the view when it is a Gauss node; the
+        // buffer is not cleared between waves on the tensor-core path)
+        for (int e = threadIdx.x; e < 6 * (G.NR - n) * 24; e += blockDim.x)
+            Bop[(size_t)(6 * N + 6 * (n - N)) * 24 + e] = 0.f;
     }
 
     // ---- solar row: primary-source vectors and flat reflected-beam vectors ----
@@ -563,6 +614,34 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
         pm[col_of(G, 1, 1, os)] = mol ? g2 * rmo * p0 : 0.f;
         pm[col_of(G, 2, 0, os)] = mol ? -g2 * to * p0 : 0.f;
         pm[col_of(G, 2, 1, os)] = mol ? -g2 * tmo * p0 : 0.f;
+        if (d.beam_q != 0.0) {
+            // partially polarised incident beam (1, q, 0): the Q-incident solar
+            // column of the phase matrix, aerosol and molecular parts
+            // (rt_primary_source.c:31-55, 72-78, 106-148, 173-182)
+            const float bq = (float)d.beam_q, r0s = basis(1, -1, 2);
+            float e1 = 0.f, o1 = 0.f, e2 = 0.f, o2 = 0.f;
+            for (int l = m; l <= Lp; ++l) {
+                const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
+                const float a1 = basis(2, os, l) * basis(1, -1, l) * al;
+                const float a2_ = basis(1, os, l) * basis(2, -1, l) * ze;
+                if (((l + m) & 1) == 0) { e1 += a1; e2 += a2_; } else { o1 += a1; o2 += a2_; }
+            }
+            const float quP = (e1 + o1) + (e2 + o2), quM = -(e1 - o1) + (e2 - o2);
+            pv[col_of(G, 0, 0, os)] += bq * (Ey[0] + Oy[0]);
+            pv[col_of(G, 0, 1, os)] += bq * (Ey[0] - Oy[0]);
+            pv[col_of(G, 1, 0, os)] += bq * arrP;
+            pv[col_of(G, 1, 1, os)] += bq * arrM;
+            pv[col_of(G, 2, 0, os)] += -bq * quP;
+            pv[col_of(G, 2, 1, os)] += -bq * quM;
+            if (mol) {
+                pm[col_of(G, 0, 0, os)] += bq * g2 * po * r0s;
+                pm[col_of(G, 0, 1, os)] += bq * g2 * pmo * r0s;
+                pm[col_of(G, 1, 0, os)] += bq * a2 * ro * r0s;
+                pm[col_of(G, 1, 1, os)] += bq * a2 * rmo * r0s;
+                pm[col_of(G, 2, 0, os)] += -bq * a2 * to * r0s;
+                pm[col_of(G, 2, 1, os)] += -bq * a2 * tmo * r0s;
+            }
+        }
         if (fv) {
             // flat-surface reflected beam kernels (rt_surface_boundary.c:246-360):
             // side 0 ("top", upward outputs) uses column -o, side 1 uses +o.

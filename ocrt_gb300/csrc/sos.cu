@@ -10,34 +10,12 @@
 //   k_mol_lowrank  molecular part for m <= 2, J += y * U (V F) with the rank-24 factored
 //                  molecular operator.
 //   k_scan         surface boundary condition (rt_surface_boundary.c:137-208),
-//                  up/down formal solution, FP64 order totals, sup-norm residual and
-//                  the convergence test (rt_solver.c:2923-3150).
+//                  up/down formal solution, order totals (double-float at the TOA
+//                  and BOA, FP32 elsewhere), FP32 sup-norm residual and the
+//                  convergence test (rt_solver.c:2178-2197, 2923-3150).
 //   k_extract      TOA view sample and BOA downward samples (rt_solver.c:1010-1076).
 #include "kernels.cuh"
 #include "physics.cuh"
-
-// Field column -> (Stokes s, hemisphere h, ring slot g); columns past the view
-// block decode to slot NR (never a valid ring slot).
-__device__ inline void decode_col(const Geom &G, int c, int &s, int &h, int &g)
-{
-    const int N = G.N;
-    if (c < 6 * N) {
-        s = c / (2 * N);
-        const int r = c - s * 2 * N;
-        h = r / N;
-        g = r - h * N;
-    } else if (c < 6 * N + 6) {
-        const int v = c - 6 * N;
-        s = v >> 1; h = v & 1; g = N;
-    } else {
-        s = 0; h = 0; g = G.NR;
-    }
-}
-
-__device__ inline double ring_mu(const PixDev &d, const double *gmu, int N, int g)
-{
-    return g < N ? gmu[g] : d.mu_view;
-}
 
 // Rough direct-beam seed at level k for upward slot g, Stokes s:
 // (pi or pi/2) mu0 exp(-tau/mu0) exp(-(tau-h_k)/mu_g) R_m(mu_g, mu0)[s,I]
@@ -55,7 +33,7 @@ __device__ inline float seed_scale(const PixDev &d, const TaskDev &tk)
     return (float)((tk.m == 0 ? OCRT_PI : 0.5 * OCRT_PI) * d.mu0 * exp(-d.tau_total / d.mu0));
 }
 
-__global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
+__global__ void __launch_bounds__(512, 1) k_primary(BatchBufs B, WaveBufs W, Geom G, int t0)
 {
     const int tl = blockIdx.x, tg = t0 + tl;
     const TaskDev tk = B.tasks[tg];
@@ -103,12 +81,21 @@ __global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geo
         fm1 = fm[s * NR + g]; fm2 = fm[(s + 3) * NR + g];
     }
     int bad = 0;
-    const float faP = (float)aP, fmP = (float)mP;
+    // an atmosphere driven only by a bottom source has no solar primary and no
+    // surface seeds (rt_solver.c:949-954, rt_surface_boundary.c:553-569)
+    const float faP = d.bottom_only ? 0.f : (float)aP, fmP = d.bottom_only ? 0.f : (float)mP;
     const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
     // rough direct-beam seed (rt_surface_boundary.c:430-493) on upward columns:
     // fs_tdn exp(-(tau-h_k)/mu_g) R_m(mu_g, mu0)[s, I], the attenuation per level from Eatt
-    const bool seeded = d.rough && h == 0;
+    const bool seeded = d.rough && h == 0 && !d.bottom_only;
     const float rs = seeded ? W.srf[tk.srf_off + (size_t)G.NR * G.N * 9 + g * 9 + s * 3] : 0.f;
+    // water column: the skylight's first-scatter source, computed into J by the
+    // source pass over the unscattered skylight field (k_dtop_field)
+    const float *Jdt = (d.medium == 1 && d.ext_off >= 0 && tk.m <= d.ext_mmax) ? W.J + tk.fld_off : nullptr;
+    // atmosphere over the ocean: upward bottom source ext[m][g][s] attenuated
+    // upward, part of order 1 and of the total (rt_surface_boundary.c:495-527)
+    const bool extb = d.medium == 0 && d.ext_off >= 0 && h == 0 && tk.m <= d.ext_mmax;
+    const float exv = extb ? (float)B.ext[d.ext_off + ((size_t)tk.m * G.NR + g) * 3 + s] : 0.f;
     // Step j visits level nt - j (upward) or j (downward); the per-level inputs
     // of PF steps are loaded before the dependent recurrence runs.
     constexpr int PF = 4;
@@ -126,7 +113,7 @@ __global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geo
                     const int e = (h == 0 ? k : k - 1) * NR + g;
                     tv[q] = Tc[e]; av[q] = Ca[e]; bv[q] = Cb[e];
                 }
-                ea[q] = seeded ? B.Eatt[(d.lev_off + k) * NR + g] : 0.f;
+                ea[q] = (seeded || extb) ? B.Eatt[(d.lev_off + k) * NR + g] : 0.f;
             }
         }
 #pragma unroll
@@ -134,7 +121,8 @@ __global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geo
             if (q < cnt) {
                 const int j = j0 + q, k = h == 0 ? nt - j : j;
                 float Jk = lc[q] * (lx[q] * faP + ly[q] * fmP);
-                if (d.flat && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
+                if (Jdt) Jk += Jdt[(size_t)k * G.LDC + c];
+                if (d.flat && !d.bottom_only && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
                     const double beam = sb * exp(hh[k] / d.mu0);
                     Jk += (float)(beam * (RI * (lx[q] * fa1 + ly[q] * fm1) + RQ * (lx[q] * fa2 + ly[q] * fm2)));
                 }
@@ -143,6 +131,7 @@ __global__ void __launch_bounds__(256, 3) k_primary(BatchBufs B, WaveBufs W, Geo
                 Jp = Jk;
                 float2 t = make_float2(I, 0.f);
                 if (seeded) t = df_add(t, fs_tdn * ea[q] * rs);
+                if (extb) t = df_add(t, exv * ea[q]);
                 F[(size_t)k * G.LDC + c] = t.x;
                 Tot[(size_t)k * G.LDC + c] = t.x;
                 if (k == 0 || k == nt) W.Ttl[tot_tail_off(tk, G, k, c)] = t.y;
@@ -372,8 +361,21 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         lo0 = *tl0; loN = *tlN;
     }
     // ---- surface boundary condition from the previous order's BOA downward field
+    // (atmosphere), or the internal reflection at the water surface of the
+    // previous order's upward field at the top (water column, rt_solver.c:2788-2815)
     float bc = 0.f;
-    if (valid && h == 0 && d.surf_on) {
+    const bool water = d.medium == 1;
+    if (valid && water && h == 1) {
+        const float *R = W.srf + tk.srf_off + (size_t)g * N * 9 + s * 3;
+        const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
+        float acc = 0.f;
+        for (int i = 0; i < N; ++i) {
+            const float *Ri = R + (size_t)i * 9;
+            acc += pwm[i] * (Ri[0] * F[col_of(G, 0, 0, i)] + Ri[1] * F[col_of(G, 1, 0, i)] +
+                             Ri[2] * F[col_of(G, 2, 0, i)]);
+        }
+        bc = acc;
+    } else if (valid && h == 0 && d.surf_on) {
         const float *Fbot = F + (size_t)nt * G.LDC;
         auto Fb = [&](int col) -> float { return Fbot[col]; };
         if (d.rough) {
@@ -398,7 +400,7 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
     float mi = 0.f, mt = 0.f;
     int bad = 0;
     if (valid) {
-        float I = h == 0 ? bc : 0.f, Jp = 0.f;
+        float I = (water ? h == 1 : h == 0) ? bc : 0.f, Jp = 0.f;
         for (int j = 0; j <= nt; ++j) {
             cp_async_wait<SCAN_DEPTH - 1>();
             const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
@@ -443,6 +445,190 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
     }
 }
 
+// The same order step as k_scan with four Gauss columns per thread.  Columns
+// s*2N + h*N + 4q .. +3 share the Stokes index and the direction (N is a
+// multiple of 4), so one thread runs their four recurrences side by side and
+// every per-level value arrives as one 16-byte copy: J, the total's head, and
+// T, Ca, Cb of the four ring slots from the quad layout of k_coef_quads.  The
+// zero-weight columns (6E of them) take one thread each with 4-byte copies.
+// Per column the arithmetic is k_scan's, in the same order.
+__global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom G, int t0, int it)
+{
+    __shared__ float2 redf2[32];
+    extern __shared__ float4 scan4_smem[];
+    __shared__ int item_s;
+    const int n_items = B.active_cnt[it - 1];
+    const int tid = threadIdx.x, bs = blockDim.x, N = G.N, NR = G.NR, nq = 6 * N / 4;
+    const bool quad = tid < nq, single = !quad && tid < nq + 6 * G.E;
+    int s = 0, h = 0, g = 0, c = 0;
+    if (quad) { c = 4 * tid; decode_col(G, c, s, h, g); }
+    else if (single) { c = 6 * N + (tid - nq); decode_col(G, c, s, h, g); }
+    float4 *R = scan4_smem;   // [SCAN4_DEPTH][5][bs]: J, total, T, Ca, Cb
+    auto slot = [&](int sl, int f) -> float4 * { return R + ((size_t)sl * 5 + f) * bs + tid; };
+    for (;;) {
+    __syncthreads();
+    if (tid == 0) item_s = atomicAdd(&B.work[it * 4 + 2], 1);
+    __syncthreads();
+    if (item_s >= n_items) return;
+    const int tl = B.alist[it & 1][item_s], tg = t0 + tl;
+    const TaskState st = B.state[tg];
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt;
+    const bool valid = quad || (single && g < d.n_ring);
+    float *F = W.F + tk.fld_off;
+    const float *J = W.J + tk.fld_off;
+    float *Tot = W.Tot + tk.fld_off;
+    const float *Tc = B.Tc + d.coef_off, *Ca = B.Ca + d.coef_off, *Cb = B.Cb + d.coef_off;
+    const float *Cq = B.Cq + coef_quad_off(d.coef_off, N, NR) + (size_t)(g >> 2) * 12;
+    auto issue = [&](int j) {
+        if (j <= nt) {
+            const int k = h == 0 ? nt - j : j, sl = j & (SCAN4_DEPTH - 1);
+            const size_t o = (size_t)k * G.LDC + c;
+            const int layer = h == 0 ? k : k - 1;
+            if (quad) {
+                cp_async16_cg(slot(sl, 0), J + o);
+                cp_async16_cg(slot(sl, 1), Tot + o);
+                if (j > 0) {
+                    const float *q = Cq + (size_t)layer * (N / 4) * 12;
+                    cp_async16_ca(slot(sl, 2), q);
+                    cp_async16_ca(slot(sl, 3), q + 4);
+                    cp_async16_ca(slot(sl, 4), q + 8);
+                }
+            } else {
+                cp_async4(&slot(sl, 0)->x, J + o);
+                cp_async4(&slot(sl, 1)->x, Tot + o);
+                if (j > 0) {
+                    const int e = layer * NR + g;
+                    cp_async4(&slot(sl, 2)->x, Tc + e);
+                    cp_async4(&slot(sl, 3)->x, Ca + e);
+                    cp_async4(&slot(sl, 4)->x, Cb + e);
+                }
+            }
+        }
+        cp_async_commit();
+    };
+    const int ncol = quad ? 4 : 1;
+    float *tl0 = W.Ttl + tot_tail_off(tk, G, 0, c), *tlN = W.Ttl + tot_tail_off(tk, G, nt, c);
+    float lo0[4] = {0.f, 0.f, 0.f, 0.f}, loN[4] = {0.f, 0.f, 0.f, 0.f};
+    if (valid) {
+#pragma unroll
+        for (int j = 0; j < SCAN4_DEPTH; ++j) issue(j);
+        for (int q = 0; q < ncol; ++q) { lo0[q] = tl0[q]; loN[q] = tlN[q]; }
+    }
+    // boundary condition of each column (as in k_scan)
+    float bc[4] = {0.f, 0.f, 0.f, 0.f};
+    const bool water = d.medium == 1;
+    if (valid && ((water && h == 1) || (!water && h == 0 && d.surf_on))) {
+        const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
+        for (int q = 0; q < ncol; ++q) {
+            const int gq = g + q;
+            if (water || d.rough) {
+                // water: internal reflection of the previous order's upward field at
+                // the top; atmosphere: rough reflection of the downward field at the bottom
+                const float *Rm = W.srf + tk.srf_off + (size_t)gq * N * 9 + s * 3;
+                const float *Fr = water ? F : F + (size_t)nt * G.LDC;
+                const int hin = water ? 0 : 1;
+                float acc = 0.f;
+                for (int i = 0; i < N; ++i) {
+                    const float *Ri = Rm + (size_t)i * 9;
+                    acc += pwm[i] * (Ri[0] * Fr[col_of(G, 0, hin, i)] + Ri[1] * Fr[col_of(G, 1, hin, i)] +
+                                     Ri[2] * Fr[col_of(G, 2, hin, i)]);
+                }
+                bc[q] = acc;
+            } else {
+                const float *Fbot = F + (size_t)nt * G.LDC;
+                const float *MF = B.frs + ((size_t)tk.pix * NR + gq) * 9 + s * 3;
+                bc[q] = MF[0] * Fbot[col_of(G, 0, 1, gq)] + MF[1] * Fbot[col_of(G, 1, 1, gq)] +
+                        MF[2] * Fbot[col_of(G, 2, 1, gq)];
+            }
+        }
+    }
+    __syncthreads();
+    float mi = 0.f, mt = 0.f;
+    int bad = 0;
+    if (valid && quad) {
+        const bool start = water ? h == 1 : h == 0;
+        float4 I = start ? make_float4(bc[0], bc[1], bc[2], bc[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 Jp = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 0; j <= nt; ++j) {
+            cp_async_wait<SCAN4_DEPTH - 1>();
+            const int k = h == 0 ? nt - j : j, sl = j & (SCAN4_DEPTH - 1);
+            const float4 jv = *slot(sl, 0), ov = *slot(sl, 1);
+            if (j > 0) {
+                const float4 T = *slot(sl, 2), A = *slot(sl, 3), Bw = *slot(sl, 4);
+                I.x = T.x * I.x + A.x * jv.x + Bw.x * Jp.x;
+                I.y = T.y * I.y + A.y * jv.y + Bw.y * Jp.y;
+                I.z = T.z * I.z + A.z * jv.z + Bw.z * Jp.z;
+                I.w = T.w * I.w + A.w * jv.w + Bw.w * Jp.w;
+            }
+            Jp = jv;
+            const size_t o = (size_t)k * G.LDC + c;
+            *reinterpret_cast<float4 *>(F + o) = I;
+            float4 t;
+            if (k == 0 || k == nt) {
+                const bool top = k == 0;
+                float *tp = top ? tl0 : tlN;
+                const float2 a = df_add(make_float2(ov.x, top ? lo0[0] : loN[0]), I.x);
+                const float2 b = df_add(make_float2(ov.y, top ? lo0[1] : loN[1]), I.y);
+                const float2 e = df_add(make_float2(ov.z, top ? lo0[2] : loN[2]), I.z);
+                const float2 f = df_add(make_float2(ov.w, top ? lo0[3] : loN[3]), I.w);
+                tp[0] = a.y; tp[1] = b.y; tp[2] = e.y; tp[3] = f.y;
+                t = make_float4(a.x, b.x, e.x, f.x);
+            } else {
+                t = make_float4(ov.x + I.x, ov.y + I.y, ov.z + I.z, ov.w + I.w);
+            }
+            *reinterpret_cast<float4 *>(Tot + o) = t;
+            mi = fmaxf(mi, fmaxf(fmaxf(fabsf(I.x), fabsf(I.y)), fmaxf(fabsf(I.z), fabsf(I.w))));
+            mt = fmaxf(mt, fmaxf(fmaxf(fabsf(t.x), fabsf(t.y)), fmaxf(fabsf(t.z), fabsf(t.w))));
+            issue(j + SCAN4_DEPTH);
+        }
+        cp_async_wait<0>();
+        bad = !(isfinite(I.x) && isfinite(I.y) && isfinite(I.z) && isfinite(I.w));
+    } else if (valid) {
+        float I = (water ? h == 1 : h == 0) ? bc[0] : 0.f, Jp = 0.f;
+        for (int j = 0; j <= nt; ++j) {
+            cp_async_wait<SCAN4_DEPTH - 1>();
+            const int k = h == 0 ? nt - j : j, sl = j & (SCAN4_DEPTH - 1);
+            const float jv = slot(sl, 0)->x, ov = slot(sl, 1)->x;
+            if (j > 0) I = slot(sl, 2)->x * I + slot(sl, 3)->x * jv + slot(sl, 4)->x * Jp;
+            Jp = jv;
+            const size_t o = (size_t)k * G.LDC + c;
+            F[o] = I;
+            float t;
+            if (k == 0 || k == nt) {
+                const float2 td = df_add(make_float2(ov, k == 0 ? lo0[0] : loN[0]), I);
+                t = td.x;
+                *(k == 0 ? tl0 : tlN) = td.y;
+            } else {
+                t = ov + I;
+            }
+            Tot[o] = t;
+            mi = fmaxf(mi, fabsf(I));
+            mt = fmaxf(mt, fabsf(t));
+            issue(j + SCAN4_DEPTH);
+        }
+        cp_async_wait<0>();
+        bad = !isfinite(I);
+    }
+    if (bad) atomicExch(B.err, -2);
+    const float2 mm = block_maxf2(mi, mt, redf2);
+    mi = mm.x; mt = mm.y;
+    if (tid == 0) {
+        TaskState ns = st;
+        ns.orders = it;
+        ns.resid = mt > 0.f ? (double)(mi / mt) : 0.0;
+        if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
+        else if (it >= d.max_orders) ns.active = 0;
+        B.state[tg] = ns;
+        if (ns.active) {
+            B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
+            if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
+        }
+    }
+    }
+}
+
 // Linear interpolation between the bracketing Gauss nodes (rt_solver.c:386-403).
 __device__ inline void bracket(const double *gmu, int n, double mu, int &lo, int &hi, double &t)
 {
@@ -466,7 +652,7 @@ __global__ void k_extract(BatchBufs B, WaveBufs W, Geom G, int t0, int nt_tasks)
     const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
     auto up0 = [&](int s, int g) -> double {
         double v = tot_value(W, tk, G, 0, nt, col_of(G, s, 0, g));
-        if (d.rough) v -= (double)rough_seed(tk, W, B, d, G, fs_tdn, 0, g, s);
+        if (d.rough && !d.bottom_only) v -= (double)rough_seed(tk, W, B, d, G, fs_tdn, 0, g, s);
         return v;
     };
     auto dn = [&](int g) -> double { return tot_value(W, tk, G, nt, nt, col_of(G, 0, 1, g)); };

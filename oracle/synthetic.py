@@ -56,3 +56,31 @@ def batched_forward_pixels(n=4096, seed=20261203 + 3):
     }
     p["tau_r"] = tau_rayleigh_powerlaw(p["wavelength"])
     return p
+
+
+BANDS_8 = np.array([412.0, 443.0, 490.0, 510.0, 555.0, 670.0, 765.0, 865.0])
+
+
+def pure_water_b_synthetic(wl_nm):
+    """Synthetic pure-water scattering b_w ~ 0.0019 (550/lambda)^4.32 per metre
+    (the shape of the published seawater scattering curve, not its table)."""
+    return 0.0019 * (550.0 / np.asarray(wl_nm, dtype=np.float64)) ** 4.32
+
+
+def coupled_ocean_pixels(n_geom, seed=20261203 + 5):
+    """Config 5 distribution: n_geom geometries x the 8 bands; per pixel-band
+    a U[0.02, 0.5] and total b U[0.01, 1.0] per metre (pure water b_w plus a
+    hydrosol carrying the rest), wind U[1, 12] m/s."""
+    rng = np.random.default_rng(seed)
+    sza, vza, raa = rng.uniform(0.0, 70.0, n_geom), rng.uniform(0.0, 60.0, n_geom), rng.uniform(0.0, 180.0, n_geom)
+    wind = rng.uniform(1.0, 12.0, n_geom)
+    rows = []
+    for i in range(n_geom):
+        for wl in BANDS_8:
+            a = rng.uniform(0.02, 0.5)
+            b = rng.uniform(0.01, 1.0)
+            bw = float(pure_water_b_synthetic(wl))
+            rows.append({"sza": sza[i], "vza": vza[i], "raa": raa[i], "wind": wind[i], "wavelength": float(wl),
+                         "tau_r": float(tau_rayleigh_powerlaw(wl)), "a": a, "b_water": min(bw, b),
+                         "b_particle": max(0.0, b - bw)})
+    return rows

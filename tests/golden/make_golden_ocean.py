@@ -9,6 +9,11 @@ reference used (a_total, b_w) are part of that output and become the inputs
 of the library's ocrt_ocean for the same case.  Recipes R26 and R28 of the
 reference's manual are included with their published values.
 
+It also writes tests/golden/water_iop/: the rows of the reference's pure-water
+tables (inputs/water_iop) that bracket every case's wavelength, so that the
+library's pure-water model (ocrt_gb300/water_iop.py) is checked against the
+a_total and b_total the reference printed without shipping the full tables.
+
 Only runnable where the reference sources exist (the CLI reads its tables
 from code/OCRT_C/inputs); the JSON it writes is committed.
 
@@ -32,10 +37,10 @@ GAS_OFF = sum([[f"--gas-column-{g}", "0"] for g in ("h2o", "o3", "no2", "o2", "c
 def cases():
     out = []
 
-    def add(name, sza, vza, raa, wl, wind, adom=0.0, n_mu_water=None, m_max=None, n_layers=None, note=""):
+    def add(name, sza, vza, raa, wl, wind, adom=0.0, n_mu_water=None, m_max=None, n_layers=None, T=20.0, note=""):
         out.append({"name": name, "sza_deg": sza, "vza_deg": vza, "raa_deg": raa, "wavelength_nm": wl,
                     "wind_speed": wind, "adom440": adom, "n_mu_water": n_mu_water, "m_max": m_max,
-                    "n_layers": n_layers, "note": note})
+                    "n_layers": n_layers, "T_water": T, "note": note})
 
     add("R26", 40.0, 30.0, 90.0, 555.0, 3.0, note="recipe R26: pure seawater under a molecular atmosphere")
     add("R28", 40.0, 30.0, 90.0, 555.0, 3.0, adom=0.1, note="recipe R28: CDOM absorption added")
@@ -45,6 +50,8 @@ def cases():
     add("modes4_n24", 30.0, 40.0, 60.0, 490.0, 4.0, n_mu_water=24, m_max=4,
         note="24 water nodes shared by the atmosphere, Fourier modes 0..4 in both media")
     add("nadir_view_n16", 50.0, 0.0, 0.0, 555.0, 2.0, n_mu_water=16, m_max=3, n_layers=30)
+    add("warm_water_t28", 45.0, 20.0, 100.0, 687.5, 5.0, n_mu_water=16, m_max=2, n_layers=30, T=28.0,
+        note="28 C water: the temperature term of a_w; a wavelength between table rows")
     return out
 
 
@@ -52,7 +59,7 @@ def run(spec):
     args = [CLI, "--surface", "ocean", "--sza", str(spec["sza_deg"]), "--vza", str(spec["vza_deg"]),
             "--raa", str(spec["raa_deg"]), "--wavelength", str(spec["wavelength_nm"]), "--pressure", "1013.25",
             "--wind-speed", str(spec["wind_speed"]), "--n-water", "1.34", *GAS_OFF,
-            "--water-model", "ocrt", "--water-temperature", "20", "--water-salinity", "35",
+            "--water-model", "ocrt", "--water-temperature", str(spec["T_water"]), "--water-salinity", "35",
             "--ocrt-chl", "0", "--ocrt-tsm", "0", "--ocrt-adom440", str(spec["adom440"])]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     if spec["n_mu_water"]:
@@ -73,6 +80,30 @@ def run(spec):
             except ValueError:
                 pass
     return vals
+
+
+def reduce_tables(wavelengths):
+    """Copy the pure-water table rows within 2 nm of each wavelength."""
+    src = os.path.join(REF_WD, "inputs", "water_iop")
+    dst = os.path.join(HERE, "water_iop")
+    os.makedirs(dst, exist_ok=True)
+    for name in ("water_coef_z09_1nm.txt", "psi_T_rottgers2014_OCRT.txt"):
+        keep = []
+        with open(os.path.join(src, name)) as fh:
+            body = False
+            for line in fh:
+                if line.startswith("/end_header"):
+                    body = True
+                    continue
+                if not body or not line.strip() or line.startswith("#"):
+                    continue
+                wl = float(line.split()[0])
+                if any(abs(wl - w) <= 2.0 for w in wavelengths):
+                    keep.append(line)
+        with open(os.path.join(dst, name), "w") as fh:
+            fh.write(f"# rows of the reference's inputs/water_iop/{name} within 2 nm of the fixture wavelengths\n")
+            fh.write("/end_header\n")
+            fh.writelines(keep)
 
 
 def main():
@@ -101,6 +132,7 @@ def main():
     }
     with open(OUT, "w") as fh:
         json.dump(doc, fh, indent=1)
+    reduce_tables(sorted({r["wavelength_nm"] for r in rows}))
     print("wrote", OUT)
 
 

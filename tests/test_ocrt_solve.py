@@ -1,15 +1,72 @@
 """ocrt_gb300.ocrt_solve keeps the reference's Python entry signatures
-(code/OCRT_Python/ocrt_solve.py:131-206, :279-410) for the R2/R3 reflectances
-that are on this path."""
+(code/OCRT_Python/ocrt_solve.py:131-206, :279-410) for the R1/R2/R3
+reflectances; R1 runs the coupled solve over pure seawater plus CDOM, whose
+IOPs (ocrt_gb300/water_iop.py) are checked against the a_total and b_total
+the reference printed for every coupled fixture."""
+import os
+
 import pytest
+
+from _helpers import assert_parity, load_golden_ocean
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WATER = os.path.join(HERE, "golden", "water_iop")
 
 
 def test_unavailable_parts_raise():
     from ocrt_gb300.ocrt_solve import solve_reflectances
-    with pytest.raises(NotImplementedError, match="R1"):
+    with pytest.raises(NotImplementedError, match="constituent"):
         solve_reflectances(555, 30, 30, 90, 3, 1.2, 3.5, 0.04, 0.1, "HG:0.7,0.95", which=("R1",), gas_on=False)
     with pytest.raises(NotImplementedError, match=".mie"):
         solve_reflectances(555, 30, 30, 90, 3, 0, 0, 0, 0.1, "C50", which=("R3",), gas_on=False)
+
+
+def test_pure_water_iops_match_reference():
+    """a_w(lambda, T) + a_cdom and b_w of every coupled fixture, including a
+    28 C case (the psi_T term) and a wavelength between table rows."""
+    from ocrt_gb300.water_iop import PureWater
+    pw = PureWater(WATER)
+    for spec in load_golden_ocean()["cases"]:
+        ref = spec["reference"]
+        a, b = pw.iops(spec["wavelength_nm"], spec["T_water"], spec["adom440"])
+        assert a == pytest.approx(ref["a_total"], rel=1e-9), spec["name"]
+        assert b == pytest.approx(ref["b_total"], rel=1e-9), spec["name"]
+        assert pw.a_w(spec["wavelength_nm"], spec["T_water"]) == pytest.approx(ref["a_w"], rel=1e-9)
+        assert a - pw.a_w(spec["wavelength_nm"], spec["T_water"]) == pytest.approx(ref["a_dom"], rel=1e-6, abs=1e-15)
+
+
+def test_pure_water_tables_do_not_extrapolate(tmp_path):
+    from ocrt_gb300.water_iop import PureWater
+    pw = PureWater(WATER)
+    with pytest.raises(ValueError, match="outside"):
+        pw.a_w(300.0)
+    bad = tmp_path / "water_coef_z09_1nm.txt"
+    bad.write_text("/end_header\n500 0.1 0.002\n499 0.1 0.002\n")
+    with pytest.raises(ValueError, match="increasing"):
+        PureWater(str(tmp_path))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["R26", "R28", "warm_water_t28"])
+def test_r1_matches_reference(gpu, monkeypatch, name):
+    """R1 from the pure-water tables, with the reference CLI's settings of
+    each fixture, reproduces the reference's coupled TOA reflectance and Rrs."""
+    from ocrt_gb300 import ocrt_solve
+    spec = next(s for s in load_golden_ocean()["cases"] if s["name"] == name)
+    monkeypatch.setenv("OCRT_GB_WATER_IOP", WATER)
+    ocrt_solve._STATE.pop("pw", None)
+    m = spec["m_max"] if spec["m_max"] is not None else 2
+    out = ocrt_solve.solve_reflectances(spec["wavelength_nm"], spec["sza_deg"], spec["vza_deg"], spec["raa_deg"],
+                                        spec["wind_speed"], 0.0, 0.0, spec["adom440"], 0.0, "HG:0.7,0.95",
+                                        which=("R1",), n_mu_water=spec["n_mu_water"] or 48, fourier_m_max=m,
+                                        nt_atm=spec["n_layers"] or 40, max_it_water=20, gas_on=False,
+                                        water_temperature_c=spec["T_water"])
+    ocrt_solve._STATE.pop("pw", None)
+    ref = spec["reference"]
+    assert_parity({"rho_I": out["rho_TOA_I"], "rho_Q": out["rho_TOA_Q"], "rho_U": out["rho_TOA_U"]},
+                  {"rho_I": ref["TOA_rho_I"], "rho_Q": ref["TOA_rho_Q"], "rho_U": ref["TOA_rho_U"]}, name)
+    assert out["Rrs"] == pytest.approx(ref["Rrs0plus_I"], rel=1e-4)
+    assert out["rrs0minus"] == pytest.approx(ref["rrs0minus_I"], rel=1e-4)
 
 
 @pytest.mark.gpu
