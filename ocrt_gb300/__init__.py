@@ -328,7 +328,9 @@ def set_timing(enable):
 
 
 def autotune_summary():
-    """Block sizes the launch-shape autotuner picked, one dict per shape."""
+    """Launch choices the autotuners picked, one dict per shape: block sizes of
+    the setup kernels, and the transport-scan implementation (with its time
+    per level-column in ns for each candidate)."""
     L = lib()
     n = L.ocrt_gb_autotune_summary(None, 0)
     buf = C.create_string_buffer(n + 1)
@@ -337,8 +339,9 @@ def autotune_summary():
     for line in buf.value.decode().splitlines():
         head, ms = line.split(" ms:")
         kern, key, best = head.split(" ")
-        out.append({"kernel": kern, "key": [int(x) for x in key[4:].split(",")], "best": int(best[5:]),
-                    "ms": {int(a): float(b) for a, b in (t.split("=") for t in ms.split())}})
+        lab = lambda v: int(v) if v.lstrip("-").isdigit() else v   # noqa: E731 (block sizes or scan names)
+        out.append({"kernel": kern, "key": [int(x) for x in key[4:].split(",")], "best": lab(best[5:]),
+                    "ms": {lab(a): float(b) for a, b in (t.split("=") for t in ms.split())}})
     return out
 
 

@@ -46,6 +46,7 @@ struct TuneRec {
     std::vector<int> key;
     int best = 256;
     std::vector<std::pair<int, float>> ms;
+    const char *const *labels = nullptr;   // names of the choices (printed instead of their numbers)
 };
 std::map<std::pair<std::string, std::vector<int>>, size_t> g_tune_idx;
 std::vector<TuneRec> g_tune;
@@ -186,11 +187,70 @@ bool force_simt()
 
 // OCRT_GB_SCAN=column keeps the one-column-per-thread scan where the
 // four-column one applies (N a multiple of 4).
+// Transport-scan implementations.  All run each column's recurrence with
+// the same arithmetic in the same order, so any of them (and any mix across
+// orders) gives identical results; they differ in how the per-level inputs
+// reach the threads.
+enum ScanKind { SK_COLUMN, SK_QUAD, SK_TMA_8_3, SK_TMA_8_4, SK_TMA_4_6, SK_TMA_16_2, SK_N };
+const char *sk_names[SK_N] = {"column", "quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2"};
+const int sk_ch[SK_N] = {0, 0, 8, 8, 4, 16};
+const int sk_ns[SK_N] = {0, 0, 3, 4, 6, 2};
+inline int sk_map_index(int ch) { return ch == 4 ? 0 : ch == 8 ? 1 : 2; }
+
+// Resident blocks per SM of a chunked-scan variant at this geometry (0: does
+// not fit); the persistent grid is that times the SM count.
+int scan_tma_blocks(int kind, const Geom &G)
+{
+    static std::map<std::vector<int>, int> cache;
+    const std::vector<int> key = {kind, G.N, G.E};
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    const void *fn = scan_tma_fn(sk_ch[kind], sk_ns[kind]);
+    int nb = 0;
+    const int th = scan_tma_threads(G);
+    if (th > 256 ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, th, scan_tma_smem_bytes(G, sk_ch[kind], sk_ns[kind])) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        nb = 0;
+    }
+    cache[key] = nb;
+    return nb;
+}
+
 bool scan4_allowed(int N)
 {
     const char *e = getenv("OCRT_GB_SCAN");
     return N % 4 == 0 && !(e && strcmp(e, "column") == 0);
 }
+
+
+// OCRT_GB_SCAN names one implementation (column, quad, tma8x3, ...); unset,
+// the scan autotuner picks one.  Returns -1 when unset or unknown.
+int scan_forced()
+{
+    const char *e = getenv("OCRT_GB_SCAN");
+    if (!e) return -1;
+    if (strcmp(e, "tma") == 0) return SK_TMA_8_3;
+    for (int k = 0; k < SK_N; ++k)
+        if (strcmp(e, sk_names[k]) == 0) return k;
+    return -1;
+}
+
+// Online scan autotuner.  The scan updates the order state, so a candidate
+// cannot be re-run on the same input; instead, on eager executes of a shape
+// key that has no choice yet, successive orders rotate through the
+// candidates, each order's scan is timed with CUDA events, and the time is
+// divided by the order's level-columns (the scan's work, counted on the
+// device as tasks are queued).  Once every candidate has two orders the
+// fastest per level-column is kept for the process.
+struct ScanTune {
+    std::vector<int> cand;
+    double ms[SK_N] = {0}, lev[SK_N] = {0};
+    int n[SK_N] = {0};
+    int best = -1;
+};
+std::map<std::vector<int>, ScanTune> g_scan_tune;
 
 struct Group {
     int N = 0, E = 1, P = 0, T = 0;   // E zero-weight ring slots (1 atmosphere, 4 water column)
@@ -218,7 +278,9 @@ struct Group {
     double *h = nullptr, *ch = nullptr, *xd = nullptr, *yd = nullptr, *z = nullptr;
     double *tabs = nullptr;   // per-layer gas absorption depths (level-array layout), any_gas only
     float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
-    float *Cq = nullptr;                  // Gauss-slot weights in quads (k_scan4), nullptr when the column scan runs
+    float *Cq = nullptr;                  // transport weights in quads (k_scan4, k_scan_tma), nullptr when the column scan runs
+    ScanMaps smap[3];                     // k_scan_tma tensor maps for level chunks of 4, 8, 16
+    bool smap_ok = false;
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
     double *lam = nullptr;
     float *Eatt = nullptr, *lvf = nullptr;
@@ -470,7 +532,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.h, g.nlev)) || (rc = alloc(g.ch, g.nlev)) || (rc = alloc(g.xd, g.nlev)) ||
         (rc = alloc(g.yd, g.nlev)) || (rc = alloc(g.z, g.nlev)) || (rc = alloc(g.tabs, g.any_gas ? g.nlev : 1)) ||
         (rc = alloc(g.Tc, g.ncoef)) || (rc = alloc(g.Ca, g.ncoef)) || (rc = alloc(g.Cb, g.ncoef)) ||
-        (scan4_allowed(g.N) && (rc = alloc(g.Cq, g.ncoef / G.NR * 3 * (size_t)g.N))) ||
+        (scan4_allowed(g.N) && (rc = alloc(g.Cq, g.ncoef / G.NR * (size_t)coef_quad_width(G.NR)))) ||
         (rc = alloc(g.Bp, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Br, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
         (rc = alloc(g.Bt, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * g.N)) ||
@@ -515,6 +577,13 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     // m <= 2 molecular operator when the geometry allows it, CUDA cores
     // otherwise.  The per-order task lists themselves are built on the device
     // (k_primary, k_scan). ----
+    // tensor maps of the chunked scan over this group's J / total buffers
+    if (g.Cq && scan_tma_supported(G)) {
+        g.smap_ok = true;
+        const int chs[3] = {4, 8, 16};
+        for (int i = 0; i < 3 && g.smap_ok; ++i)
+            g.smap_ok = scan_tma_maps(G, chs[i], g.J, g.Tot, g.wave_fld, g.Cq, g.ncoef / G.NR, &g.smap[i]) == 0;
+    }
     g.use_tc = tc_supported(G) && !force_simt();
     if (g.use_tc && (rc = alloc(g.opt, 2 * g.wave_ops))) return rc;
     if (g.use_tc && (rc = alloc(g.molV, (size_t)3 * 32 * G.CIN))) return rc;
@@ -746,6 +815,40 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     W.fvec = g.any_flat ? g.fvec : nullptr; W.srf = g.srf;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
     const int poll = 4;
+    // ---- transport-scan implementation: forced, tuned, or being tuned ----
+    std::vector<int> scan_cands;
+    if (!g.Cq) {
+        scan_cands.push_back(SK_COLUMN);
+    } else {
+        scan_cands.push_back(SK_QUAD);
+        if (g.smap_ok)
+            for (int k = SK_TMA_8_3; k < SK_N; ++k)
+                if (scan_tma_blocks(k, G) > 0) scan_cands.push_back(k);
+    }
+    int scan_pick = -1;
+    ScanTune *stune = nullptr;
+    std::vector<int> stune_key;
+    {
+        const int forced = scan_forced();
+        int kmax = 0;
+        for (const Wave &w : g.waves) kmax = std::max(kmax, w.Kmax);
+        const std::vector<int> key = {G.N, G.E, kmax};
+        const int dflt = scan_cands.size() > 1 ? scan_cands[1] : scan_cands[0];
+        if (forced >= 0 && std::find(scan_cands.begin(), scan_cands.end(), forced) != scan_cands.end()) {
+            scan_pick = forced;
+        } else if (scan_cands.size() == 1 || !autotune_enabled()) {
+            scan_pick = dflt;
+        } else {
+            ScanTune &t = g_scan_tune[key];
+            if (t.cand.empty()) t.cand = scan_cands;
+            if (t.best >= 0) scan_pick = t.best;
+            else if (capture) scan_pick = dflt;
+            else stune = &t;
+        }
+        if (stune) stune_key = key;
+    }
+    struct ScanTrial { int kind, it; cudaEvent_t e0, e1; };
+    std::vector<ScanTrial> scan_trials;
     for (Wave &w : g.waves) {
         const int nw = w.t1 - w.t0;
         if (!capture) w.fwd_stop = INT_MAX;
@@ -837,18 +940,81 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             if (w.n_mol && !w.n_tc)
                 LAUNCH(plan, KC_MOL, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                            B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
-            if (g.Cq)
-                LAUNCH(plan, KC_SCAN, k_scan4<<<scan4_grid, scan4_threads(G), scan4_smem_bytes(scan4_threads(G)), st>>>(
-                           B, W, G, w.t0, it));
-            else
-                LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, scan_smem_bytes(scan_threads), st>>>(
-                           B, W, G, w.t0, it));
+            {
+                int kind = scan_pick;
+                const bool tuning = kind < 0;
+                if (tuning) kind = stune->cand[(it - 2) % stune->cand.size()];
+                cudaEvent_t te0 = nullptr, te1 = nullptr;
+                if (tuning) {
+                    CK(cudaEventCreate(&te0));
+                    CK(cudaEventCreate(&te1));
+                    CK(cudaEventRecord(te0, st));
+                }
+                switch (kind) {
+                case SK_COLUMN:
+                    LAUNCH(plan, KC_SCAN, k_scan<<<scan_grid, scan_threads, scan_smem_bytes(scan_threads), st>>>(
+                               B, W, G, w.t0, it));
+                    break;
+                case SK_QUAD:
+                    LAUNCH(plan, KC_SCAN, k_scan4<<<scan4_grid, scan4_threads(G),
+                                                     scan4_smem_bytes(scan4_threads(G)), st>>>(B, W, G, w.t0, it));
+                    break;
+                default: {
+                    const int ch = sk_ch[kind], ns = sk_ns[kind];
+                    const ScanMaps &sm = g.smap[sk_map_index(ch)];
+                    const int grid = std::min(nw, scan_tma_blocks(kind, G) * g_nsm);
+                    LAUNCH(plan, KC_SCAN, scan_tma_launch(ch, ns, grid, st, B, W, G, w.t0, it, sm));
+                }
+                }
+                if (tuning) {
+                    CK(cudaEventRecord(te1, st));
+                    scan_trials.push_back({kind, it, te0, te1});
+                }
+            }
             if (capture) {
                 if (it == w.fwd_stop) break;
             } else if ((it - 1) % poll == 0 || it == g.max_orders) {
                 CK(cudaMemcpyAsync(g_pinned, g.active_cnt + it, sizeof(int), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
                 if (*g_pinned == 0) { w.fwd_stop = it; break; }
+            }
+        }
+        if (stune && !scan_trials.empty()) {
+            // scan autotuner: per-candidate time over the level-columns its orders scanned
+            std::vector<int> wk(4 * ((size_t)g.max_orders + 2));
+            CK(cudaMemcpyAsync(wk.data(), g.work, sizeof(int) * wk.size(), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (const ScanTrial &t : scan_trials) {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, t.e0, t.e1) != cudaSuccess) cudaGetLastError();
+                const double lev = (double)wk[(size_t)t.it * 4 + 3] * G.COUT;
+                if (lev > 0 && ms > 0.f) {
+                    stune->ms[t.kind] += ms;
+                    stune->lev[t.kind] += lev;
+                    stune->n[t.kind]++;
+                }
+                cudaEventDestroy(t.e0);
+                cudaEventDestroy(t.e1);
+            }
+            scan_trials.clear();
+            bool all = true;
+            for (int k : stune->cand) all = all && stune->n[k] >= 2;
+            if (all) {
+                TuneRec r;
+                r.kernel = "transport_scan";
+                r.key = stune_key;
+                r.labels = sk_names;
+                double bestv = 0;
+                for (int k : stune->cand) {
+                    const double v = stune->ms[k] / stune->lev[k] * 1e6;   // ns per level-column
+                    r.ms.push_back({k, (float)v});
+                    if (stune->best < 0 || v < bestv) { bestv = v; stune->best = k; }
+                }
+                r.best = stune->best;
+                g_tune_idx[std::make_pair(r.kernel, r.key)] = g_tune.size();
+                g_tune.push_back(r);
+                scan_pick = stune->best;
+                stune = nullptr;
             }
         }
         if (capture && w.fwd_stop != INT_MAX)
@@ -921,6 +1087,7 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan4, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(scan_tma_init());
     CK(cudaFuncSetAttribute(k_adj_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -1235,10 +1402,11 @@ int ocrt_gb_autotune_summary(char *buf, int len)
         t += r.kernel;
         t += " key=";
         for (size_t i = 0; i < r.key.size(); ++i) t += (i ? "," : "") + std::to_string(r.key[i]);
-        t += " best=" + std::to_string(r.best) + " ms:";
+        t += " best=" + (r.labels ? std::string(r.labels[r.best]) : std::to_string(r.best)) + " ms:";
         for (const auto &m : r.ms) {
-            char b[48];
-            snprintf(b, sizeof(b), " %d=%.4f", m.first, m.second);
+            char b[64];
+            if (r.labels) snprintf(b, sizeof(b), " %s=%.6g", r.labels[m.first], m.second);
+            else snprintf(b, sizeof(b), " %d=%.4f", m.first, m.second);
             t += b;
         }
         t += "\n";

@@ -27,10 +27,26 @@ inline size_t scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads
 #define SCAN4_DEPTH 8
 __host__ __device__ inline int scan4_threads(const Geom &G) { return ((6 * G.N / 4 + 6 * G.E + 31) / 32) * 32; }
 inline size_t scan4_smem_bytes(int threads) { return (size_t)SCAN4_DEPTH * 5 * threads * 16; }
+// Transport weights in quads (k_coef_quads): per layer, per quad of ring
+// slots g = 4q..4q+3 (the ring padded to NRq = NR rounded up to 4, padding
+// zero), four T, then four Ca, then four Cb: 3 * NRq floats per layer.
+__host__ __device__ inline int coef_quad_width(int NR) { return 3 * ((NR + 3) & ~3); }
 __host__ __device__ inline long long coef_quad_off(long long coef_off, int N, int NR)
 {
-    return coef_off / NR * 3 * N;
+    (void)N;
+    return coef_off / NR * coef_quad_width(NR);
 }
+// k_scan_tma (scan_tma.cu): zero-weight columns fetched per level (6E rounded
+// up to 4), weight-row width, block size (one thread per field column plus
+// one producer warp), and the tensor maps it reads through.
+__host__ __device__ inline int scan_tma_zw(const Geom &G) { return (6 * G.E + 3) & ~3; }
+__host__ __device__ inline int scan_tma_cw(const Geom &G) { return coef_quad_width(G.NR); }
+__host__ __device__ inline int scan_tma_threads(const Geom &G) { return ((G.COUT + 31) / 32) * 32 + 32; }
+struct ScanMaps {
+    CUtensorMap jg, tg;    // Gauss columns of J / the total head: {N, 2 (h), 3 (s), rows}
+    CUtensorMap jz, tz;    // zero-weight columns: {LDC, rows}
+    CUtensorMap cq;        // transport weights in quads: {3 * NRq, layers}
+};
 // k_adj_scan: cotangent rows per block (they share the transport coefficients)
 #define ADJ_RB 3
 inline size_t adj_scan_smem_bytes(int threads) { return (size_t)SCAN_DEPTH * threads * (ADJ_RB * (4 + 4) + 12); }
@@ -199,6 +215,17 @@ size_t tc_adj_smem_bytes(const Geom &G);
 bool tc_adj_supported(const Geom &G);
 __global__ void k_scan(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 __global__ void k_scan4(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
+// k_scan_tma<CH, NS> (levels per chunk, ring stages) instances: (8, 3), (8, 4), (4, 6), (16, 2)
+const void *scan_tma_fn(int ch, int ns);
+cudaError_t scan_tma_launch(int ch, int ns, int grid, cudaStream_t st, const BatchBufs &B, const WaveBufs &W,
+                            const Geom &G, int t0, int it, const ScanMaps &M);
+cudaError_t scan_tma_init();   // dynamic shared-memory limits of the instances
+size_t scan_tma_smem_bytes(const Geom &G, int CH, int NS);
+// tensor maps over the wave's J and total buffers (fld_floats floats) and the
+// quad weight table (layers rows); 0 on success
+int scan_tma_maps(const Geom &G, int CH, float *J, float *Tot, size_t fld_floats, const float *Cq, size_t layers,
+                  ScanMaps *M);
+bool scan_tma_supported(const Geom &G);
 __global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int ltiles,
                               const float *Bp, const float *Br, const float *Bt, int L);
 inline size_t mol_smem_bytes(const Geom &G) { return sizeof(float) * (4 * G.N + G.COUT * 24 + 32 * G.CIN + 32 * 25); }

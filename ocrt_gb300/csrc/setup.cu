@@ -199,24 +199,26 @@ __global__ void k_coef(const PixDev *px, int P, int N, int NR, const double *gmu
     }
 }
 
-// The Gauss-slot weights regrouped for k_scan4: per (layer, quad of slots
-// g = 4q..4q+3) the four T, then the four Ca, then the four Cb, so that one
-// 16-byte copy brings one weight of four columns.
+// The transport weights regrouped in quads for k_scan4 and k_scan_tma: per
+// (layer, quad of ring slots g = 4q..4q+3) the four T, then the four Ca, then
+// the four Cb, so that one 16-byte copy brings one weight of four columns and
+// one layer is a row of coef_quad_width(NR) floats; slots past NR are zero.
 __global__ void k_coef_quads(const PixDev *px, int P, int N, int NR, const float *Tc, const float *Ca, const float *Cb,
                              float *Cq)
 {
     const int p = blockIdx.y;
     if (p >= P) return;
     const PixDev &d = px[p];
-    const int total = d.nt * N, nq = N / 4;
+    const int NRq = (NR + 3) & ~3, total = d.nt * NRq;
     const long long qo = coef_quad_off(d.coef_off, N, NR);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        const int layer = e / N, g = e - layer * N;
+        const int layer = e / NRq, g = e - layer * NRq;
         const long long src = d.coef_off + (long long)layer * NR + g;
-        const long long dst = qo + ((long long)(layer * nq + (g >> 2)) * 3) * 4 + (g & 3);
-        Cq[dst] = Tc[src];
-        Cq[dst + 4] = Ca[src];
-        Cq[dst + 8] = Cb[src];
+        const long long dst = qo + (long long)layer * 3 * NRq + (g >> 2) * 12 + (g & 3);
+        const bool in = g < NR;
+        Cq[dst] = in ? Tc[src] : 0.f;
+        Cq[dst + 4] = in ? Ca[src] : 0.f;
+        Cq[dst + 8] = in ? Cb[src] : 0.f;
     }
 }
 

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(512, 1) k_primary(BatchBufs B, WaveBufs W, Geo
         B.state[tg] = st;
         if (st.active) {
             B.alist[0][atomicAdd(&B.active_cnt[1], 1)] = tl;
+            atomicAdd(&B.work[2 * 4 + 3], d.nt + 1);   // level rows queued for order 2 (scan autotuner)
             if (tk.has_mol) B.mlist[0][atomicAdd(&B.mol_cnt[1], 1)] = tl;
         }
     }
@@ -439,6 +440,7 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         B.state[tg] = ns;
         if (ns.active) {
             B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
+            atomicAdd(&B.work[(it + 1) * 4 + 3], d.nt + 1);
             if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
         }
     }
@@ -490,7 +492,7 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
                 cp_async16_cg(slot(sl, 0), J + o);
                 cp_async16_cg(slot(sl, 1), Tot + o);
                 if (j > 0) {
-                    const float *q = Cq + (size_t)layer * (N / 4) * 12;
+                    const float *q = Cq + (size_t)layer * coef_quad_width(NR);
                     cp_async16_ca(slot(sl, 2), q);
                     cp_async16_ca(slot(sl, 3), q + 4);
                     cp_async16_ca(slot(sl, 4), q + 8);
@@ -623,6 +625,7 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
         B.state[tg] = ns;
         if (ns.active) {
             B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
+            atomicAdd(&B.work[(it + 1) * 4 + 3], d.nt + 1);
             if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
         }
     }

@@ -123,6 +123,10 @@ def test_autotune_changes_no_result(gpu):
     kinds = {s["kernel"] for s in summ}
     assert "k_tables" in kinds and "k_coxmunk" in kinds
     for s in summ:
-        assert s["best"] in (128, 256, 512)
+        # block sizes of the setup kernels; scan implementations by name
+        if s["kernel"] == "transport_scan":
+            assert s["best"] in ("quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2")
+        else:
+            assert s["best"] in (128, 256, 512)
         assert s["best"] in s["ms"] and all(v > 0 for v in s["ms"].values())
         assert s["ms"][s["best"]] == min(s["ms"].values())

@@ -1,7 +1,10 @@
-"""The four-column transport scan (k_scan4, N a multiple of 4) against the
-one-column scan (k_scan, OCRT_GB_SCAN=column): per column both run the same
-recurrence in the same order, so a batch, the coupled ocean solve and the
-adjoint give the same numbers either way."""
+"""The transport-scan implementations against the one-column scan (k_scan,
+OCRT_GB_SCAN=column): the four-column scan (k_scan4) and the chunked scans
+fed by tensor-map copies (k_scan_tma with 8, 4 or 16 levels per chunk) run
+each column's recurrence with the same arithmetic in the same order, so a
+batch, the coupled ocean solve and the scan autotuner (which rotates the
+implementations across the orders of its first execute) give the same
+numbers as the column scan."""
 import numpy as np
 import pytest
 
@@ -22,10 +25,15 @@ def _batch(A, N, n=6, seed=5):
     return cases, opts, aers
 
 
+SCANS = ["quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2"]
+
+
 @pytest.mark.parametrize("N", [8, 24, 32])
-def test_scan4_equals_column_scan(gpu, monkeypatch, N):
+@pytest.mark.parametrize("scan", SCANS)
+def test_scan_equals_column_scan(gpu, monkeypatch, N, scan):
     from ocrt_gb300 import _abi as A
     cases, opts, aers = _batch(A, N)
+    monkeypatch.setenv("OCRT_GB_SCAN", scan)
     quad = gpu.solve_batch(cases, opts, aers)
     monkeypatch.setenv("OCRT_GB_SCAN", "column")
     col = gpu.solve_batch(cases, opts, aers)
@@ -33,16 +41,42 @@ def test_scan4_equals_column_scan(gpu, monkeypatch, N):
         np.testing.assert_allclose(quad[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
 
 
-def test_scan4_equals_column_scan_coupled_ocean(gpu, monkeypatch):
-    """The water column's top boundary (internal reflection) in both scans."""
+@pytest.mark.parametrize("scan", ["quad", "tma8x3"])
+def test_scan_equals_column_scan_coupled_ocean(gpu, monkeypatch, scan):
+    """The water column's top boundary (internal reflection, four zero-weight
+    ring slots) in every scan."""
     from ocrt_gb300 import _abi as A
     from synthetic import hg_aerosol_moments
     c = A.default_case(surface="ocean", sza_deg=35.0, vza_deg=25.0, raa_deg=60.0, wavelength_nm=490.0, wind_speed=6.0)
     o = A.default_opts(fourier_m_max=4, n_layers=30)
     oc = A.OceanHolder(0.08, 0.003, 0.2, hg_aerosol_moments(0.92, 80), n_mu_water=16, m_max_water=4, depth_m=50.0,
                        n_layers_water=60, max_orders_water=200)
+    monkeypatch.setenv("OCRT_GB_SCAN", scan)
     quad = gpu.solve_ocean(c, o, oc)
     monkeypatch.setenv("OCRT_GB_SCAN", "column")
     col = gpu.solve_ocean(c, o, oc)
     for k in ("rho_I", "rho_Q", "rho_U", "Rrs_0plus_I", "Ed_0minus", "Lu_0minus_I", "Kd_0minus"):
         assert quad[k] == pytest.approx(col[k], rel=1e-12, abs=1e-15), k
+
+
+def test_scan_autotuner_matches_column_scan(gpu, monkeypatch):
+    """With no implementation named, the first execute of a new shape rotates
+    the scans across its orders and keeps the fastest; the results equal the
+    column scan's, and the choice is listed by the autotune summary."""
+    from ocrt_gb300 import _abi as A
+    monkeypatch.delenv("OCRT_GB_SCAN", raising=False)
+    monkeypatch.delenv("OCRT_GB_AUTOTUNE", raising=False)
+    cases, opts, aers = _batch(A, 20, n=5, seed=11)
+    for o in opts:
+        o.n_layers = 77          # a level count no other test uses: a fresh tuning key
+        o.max_orders = 400
+    tuned = gpu.solve_batch(cases, opts, aers)
+    again = gpu.solve_batch(cases, opts, aers)
+    monkeypatch.setenv("OCRT_GB_SCAN", "column")
+    col = gpu.solve_batch(cases, opts, aers)
+    for k in ("rho_I", "rho_Q", "rho_U", "T_diff_dn_hemi", "order_modes"):
+        np.testing.assert_allclose(tuned[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
+        np.testing.assert_allclose(again[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
+    recs = [r for r in gpu.autotune_summary() if r["kernel"] == "transport_scan" and r["key"][:2] == [20, 1]]
+    assert recs, gpu.autotune_summary()
+    assert recs[0]["best"] in ("quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2")
