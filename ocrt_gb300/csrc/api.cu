@@ -288,6 +288,7 @@ struct Group {
     double *kappa = nullptr, *taudir = nullptr;
     int *active_cnt = nullptr, *mol_cnt = nullptr, *work = nullptr, *err = nullptr;
     int *alist[2] = {nullptr, nullptr}, *mlist[2] = {nullptr, nullptr};   // device-built active-task lists
+    unsigned char *aflag = nullptr;       // per wave task: queued for the next order (k_compact sorts the lists)
     float *F = nullptr, *J = nullptr, *ops = nullptr;
     float *opt = nullptr;    // pre-split operator tiles of the tensor-core pass (2 x wave_ops floats)
     float *molV = nullptr;   // [3][32][CIN] molecular input factors V_m of the tensor-core pass
@@ -368,7 +369,7 @@ void free_group(Group &g)
 {
     void *ptrs[] = {g.px, g.tasks, g.state, g.tout, g.res, g.pix_task0, g.gmu, g.gw, g.pw, g.h, g.ch, g.xd, g.yd, g.z,
                     g.tabs, g.Tc, g.Ca, g.Cb, g.Cq, g.Bp, g.Br, g.Bt, g.cs, g.frs, g.Eatt, g.lvf, g.lam, g.mb, g.mg, g.ma, g.mz, g.kappa, g.taudir,
-                    g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1],
+                    g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1], g.aflag,
                     g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.Ttl,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
@@ -545,6 +546,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.work, 4 * ((size_t)g.max_orders + 2))) || (rc = alloc(g.err, 2)) ||
         (rc = alloc(g.alist[0], g.wave_tasks)) || (rc = alloc(g.alist[1], g.wave_tasks)) ||
         (rc = alloc(g.mlist[0], g.wave_tasks)) || (rc = alloc(g.mlist[1], g.wave_tasks)) ||
+        (rc = alloc(g.aflag, g.wave_tasks)) ||
         (rc = alloc(g.F, g.wave_fld)) || (rc = alloc(g.J, g.wave_fld)) ||
         (rc = alloc(g.Tot, g.wave_fld)) || (rc = alloc(g.Ttl, g.wave_tail)) ||
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
@@ -809,6 +811,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     B.alist[0] = g.alist[0]; B.alist[1] = g.alist[1]; B.mlist[0] = g.mlist[0]; B.mlist[1] = g.mlist[1];
     B.molV = g.molV;
     B.ext = g.ext;
+    B.aflag = g.aflag;
     WaveBufs W;
     W.F = g.F; W.J = g.J; W.Tot = g.Tot; W.Ttl = g.Ttl; W.ops = g.ops; W.opt = g.use_tc ? g.opt : nullptr;
     W.pvec = g.pvec;
@@ -860,6 +863,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.mol_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.work, 0, sizeof(int) * 4 * ((size_t)g.max_orders + 2), st));
+        CK(cudaMemsetAsync(g.aflag, 0, (size_t)nw, st));
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 128 / (1 + G.E) - 1) / (128 / (1 + G.E)), 128, 0, st>>>(
                    g.tasks, w.t0, nw, g.px, g.Lmax, G.E, g.Bx));
         auto tables = [&](int b) {
@@ -931,6 +935,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             CK(cudaMemsetAsync(g.mol_cnt + (itd - 1), 0, sizeof(int), st));
         }
         LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+        LAUNCH(plan, KC_PRIMARY, k_compact<<<1, COMPACT_THREADS, 0, st>>>(B, w.t0, nw, 2));
         for (int it = 2; it <= g.max_orders; ++it) {
             if (w.n_simt)
                 LAUNCH(plan, KC_SOURCE, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
@@ -970,6 +975,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
                     CK(cudaEventRecord(te1, st));
                     scan_trials.push_back({kind, it, te0, te1});
                 }
+                LAUNCH(plan, KC_SCAN, k_compact<<<1, COMPACT_THREADS, 0, st>>>(B, w.t0, nw, it + 1));
             }
             if (capture) {
                 if (it == w.fwd_stop) break;

@@ -145,7 +145,29 @@ struct BatchBufs {
     int *err;              // device error word
     const float *molV;     // [3][32][CIN]: V_m[4b + f][bN + i] = w_i {1, P2m, R2m, T2m}(mu_i), rows 24..31 zero
                            // (the adjoint's tensor-core pass contracts the transposed molecular term with it)
+    unsigned char *aflag = nullptr;  // per wave task: 1 = active in the next order, 3 = active and molecular; k_compact
+                           // turns the flags into task-ordered lists.  nullptr: tasks are appended to the lists
+                           // directly (in completion order).
 };
+
+// Queue wave task tl for order itn (after the order that just ran, or after
+// the primary for itn = 2): a flag for k_compact, or a direct append.  The
+// work counter [itn][3] sums the level rows queued (the scan autotuner's work
+// measure).
+__device__ inline void queue_next(const BatchBufs &B, int itn, int tl, int has_mol, int levels)
+{
+    if (B.aflag) {
+        B.aflag[tl] = has_mol ? 3 : 1;
+        return;
+    }
+    B.alist[itn & 1][atomicAdd(&B.active_cnt[itn - 1], 1)] = tl;
+    if (has_mol) B.mlist[itn & 1][atomicAdd(&B.mol_cnt[itn - 1], 1)] = tl;
+    atomicAdd(&B.work[itn * 4 + 3], levels);
+}
+// k_compact: the flagged tasks of a wave (nw of them) in task order into the
+// lists of order itn, their counts and level rows; clears the flags.  One block.
+#define COMPACT_THREADS 1024
+__global__ void k_compact(BatchBufs B, int t0, int nw, int itn);
 
 // adjoint.cu
 struct AdjBufs {

@@ -281,11 +281,7 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
             if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
             else if (it >= d.max_orders) ns.active = 0;
             B.state[tg] = ns;
-            if (ns.active) {
-                B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
-                atomicAdd(&B.work[(it + 1) * 4 + 3], nt + 1);   // level rows queued for the next order
-                if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
-            }
+            if (ns.active) queue_next(B, it + 1, tl, tk.has_mol, nt + 1);
         }
         if (abort_s) break;
     }
@@ -381,7 +377,7 @@ int scan_tma_maps(const Geom &G, int CH, float *J, float *Tot, size_t fld_floats
     const auto F32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const auto NI = CU_TENSOR_MAP_INTERLEAVE_NONE;
     const auto NSW = CU_TENSOR_MAP_SWIZZLE_NONE;
-    const auto L2P = CU_TENSOR_MAP_L2_PROMOTION_L2_128B;
+    const auto L2P = CU_TENSOR_MAP_L2_PROMOTION_NONE;
     const auto OOB = CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE;
     if (enc(&M->jg, F32, 4, J, gd, gs, gb, es, NI, NSW, L2P, OOB) != CUDA_SUCCESS) return -2;
     if (enc(&M->tg, F32, 4, Tot, gd, gs, gb, es, NI, NSW, L2P, OOB) != CUDA_SUCCESS) return -2;

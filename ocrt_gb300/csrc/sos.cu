@@ -47,11 +47,7 @@ __global__ void __launch_bounds__(512, 1) k_primary(BatchBufs B, WaveBufs W, Geo
         st.pad_ = 0;
         st.resid = 0.0;
         B.state[tg] = st;
-        if (st.active) {
-            B.alist[0][atomicAdd(&B.active_cnt[1], 1)] = tl;
-            atomicAdd(&B.work[2 * 4 + 3], d.nt + 1);   // level rows queued for order 2 (scan autotuner)
-            if (tk.has_mol) B.mlist[0][atomicAdd(&B.mol_cnt[1], 1)] = tl;
-        }
+        if (st.active) queue_next(B, 2, tl, tk.has_mol, d.nt + 1);
     }
     if (c >= G.COUT) return;
     int s, h, g;
@@ -438,11 +434,7 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
         else if (it >= d.max_orders) ns.active = 0;
         B.state[tg] = ns;
-        if (ns.active) {
-            B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
-            atomicAdd(&B.work[(it + 1) * 4 + 3], d.nt + 1);
-            if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
-        }
+        if (ns.active) queue_next(B, it + 1, tl, tk.has_mol, d.nt + 1);
     }
     }
 }
@@ -623,11 +615,7 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
         if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
         else if (it >= d.max_orders) ns.active = 0;
         B.state[tg] = ns;
-        if (ns.active) {
-            B.alist[(it + 1) & 1][atomicAdd(&B.active_cnt[it], 1)] = tl;
-            atomicAdd(&B.work[(it + 1) * 4 + 3], d.nt + 1);
-            if (tk.has_mol) B.mlist[(it + 1) & 1][atomicAdd(&B.mol_cnt[it], 1)] = tl;
-        }
+        if (ns.active) queue_next(B, it + 1, tl, tk.has_mol, d.nt + 1);
     }
     }
 }
@@ -735,5 +723,64 @@ __global__ void k_mol_vtab(Geom G, int L, const float *Bp, const float *Br, cons
             v = f == 0 ? w : w * (f == 1 ? Bp[gb + i] : (f == 2 ? Br[gb + i] : Bt[gb + i]));
         }
         Vm[e] = v;
+    }
+}
+
+// Flags -> task-ordered lists.  Queueing by completion order scatters the
+// modes of one pixel over the next order's list; in task order the CTAs
+// that run at the same time work on neighbouring tasks (the modes of a few
+// pixels), which share the pixel's transport weights in L2, and the level
+// tiles of one task's source contraction share its operator tiles.
+__global__ void __launch_bounds__(COMPACT_THREADS) k_compact(BatchBufs B, int t0, int nw, int itn)
+{
+    __shared__ int sa[COMPACT_THREADS / 32], sm[COMPACT_THREADS / 32], sl[COMPACT_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    // thread tid owns tasks [b, e)
+    const int per = (nw + COMPACT_THREADS - 1) / COMPACT_THREADS;
+    const int b = min(nw, tid * per), e = min(nw, b + per);
+    int na = 0, nm = 0, lev = 0;
+    for (int i = b; i < e; ++i) {
+        const unsigned char f = B.aflag[i];
+        if (f) {
+            ++na;
+            nm += f >> 1;
+            lev += B.px[B.tasks[t0 + i].pix].nt + 1;
+        }
+    }
+    // inclusive prefix sums over the warp, then over the warp totals
+    int xa = na, xm = nm;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ya = __shfl_up_sync(0xffffffffu, xa, o), ym = __shfl_up_sync(0xffffffffu, xm, o);
+        if (lane >= o) { xa += ya; xm += ym; }
+    }
+    int ls = lev;
+    for (int o = 16; o > 0; o >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, o);
+    if (lane == 31) { sa[w] = xa; sm[w] = xm; }
+    if (lane == 0) sl[w] = ls;
+    __syncthreads();
+    if (w == 0) {
+        int ta = sa[lane], tm = sm[lane], tlv = sl[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ya = __shfl_up_sync(0xffffffffu, ta, o), ym = __shfl_up_sync(0xffffffffu, tm, o);
+            if (lane >= o) { ta += ya; tm += ym; }
+        }
+        for (int o = 16; o > 0; o >>= 1) tlv += __shfl_xor_sync(0xffffffffu, tlv, o);
+        sa[lane] = ta; sm[lane] = tm;
+        if (lane == 31) {
+            B.active_cnt[itn - 1] = ta;
+            B.mol_cnt[itn - 1] = tm;
+        }
+        if (lane == 0) B.work[itn * 4 + 3] = tlv;
+    }
+    __syncthreads();
+    int oa = (w ? sa[w - 1] : 0) + xa - na, om = (w ? sm[w - 1] : 0) + xm - nm;
+    int *al = B.alist[itn & 1], *ml = B.mlist[itn & 1];
+    for (int i = b; i < e; ++i) {
+        const unsigned char f = B.aflag[i];
+        if (f) {
+            al[oa++] = i;
+            if (f >> 1) ml[om++] = i;
+            B.aflag[i] = 0;
+        }
     }
 }
