@@ -92,7 +92,7 @@ struct TaskOut {
 };
 
 struct Geom {
-    int N, E, NR, LDC;      // E zero-weight slots, NR = N + E; LDC: field row stride (floats)
+    int N, E, NR, LDC;      // E zero-weight slots, NR = N + E; LDC: field row stride (floats, multiple of 32)
     int CIN;                // 6N weighted input columns (operator row stride)
     int COUT;               // 6N + 6E output columns
     int NP;                 // operator rows, COUT rounded up to 16
@@ -106,7 +106,10 @@ __host__ __device__ inline Geom make_geom(int N, int E = 1)
     g.NR = N + E;
     g.CIN = 6 * N;
     g.COUT = 6 * N + 6 * E;
-    g.LDC = (g.COUT + 7) & ~7;
+    // field rows start on 128-byte lines: the scan and the source contraction
+    // read rows in runs of 32 columns, and a run that straddles two lines
+    // costs DRAM two lines
+    g.LDC = (g.COUT + 31) & ~31;
     g.NP = (g.COUT + 15) & ~15;
     return g;
 }
