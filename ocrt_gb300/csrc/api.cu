@@ -218,6 +218,13 @@ int scan_tma_blocks(int kind, const Geom &G)
     return nb;
 }
 
+// OCRT_GB_PRIMARY=column keeps the one-column-per-thread order-1 kernel.
+bool primary_column()
+{
+    const char *e = getenv("OCRT_GB_PRIMARY");
+    return e && strcmp(e, "column") == 0;
+}
+
 bool scan4_allowed(int N)
 {
     const char *e = getenv("OCRT_GB_SCAN");
@@ -934,7 +941,10 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             CK(cudaMemsetAsync(g.active_cnt + (itd - 1), 0, sizeof(int), st));
             CK(cudaMemsetAsync(g.mol_cnt + (itd - 1), 0, sizeof(int), st));
         }
-        LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+        if (g.Cq && !w.any_flat && !primary_column())
+            LAUNCH(plan, KC_PRIMARY, k_primary4<<<nw, scan4_threads(G), 0, st>>>(B, W, G, w.t0));
+        else
+            LAUNCH(plan, KC_PRIMARY, k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
         LAUNCH(plan, KC_PRIMARY, k_compact<<<1, COMPACT_THREADS, 0, st>>>(B, w.t0, nw, 2));
         for (int it = 2; it <= g.max_orders; ++it) {
             if (w.n_simt)

@@ -202,6 +202,7 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
 size_t adj_mol_smem_bytes(const Geom &G);
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
+__global__ void k_primary4(BatchBufs B, WaveBufs W, Geom G, int t0);   // N % 4 == 0, no flat surface, quad weights
 
 // lut.cu (angle-grid LUT mode)
 struct LutBufs {

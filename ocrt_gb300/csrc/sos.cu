@@ -138,6 +138,137 @@ __global__ void __launch_bounds__(512, 1) k_primary(BatchBufs B, WaveBufs W, Geo
     if (bad) atomicExch(B.err, -2);
 }
 
+// Order 1 with four Gauss columns per thread (columns s*2N + h*N + 4q .. +3,
+// N a multiple of 4) and one zero-weight column per thread, for groups with
+// no flat surface.  Per column the arithmetic is k_primary's in the same
+// order; the per-level weights come from the quad table (16-byte loads for a
+// quad), and the field and total rows are written as 16-byte stores.
+template <int WD>
+__device__ __forceinline__ void primary_cols(const BatchBufs &B, const WaveBufs &W, const Geom &G, const TaskDev &tk,
+                                             const PixDev &d, int tl, int c, int s, int h, int g, int &bad)
+{
+    const int nt = d.nt, NR = G.NR, N = G.N;
+    const float *pv = W.pvec + (size_t)tl * 2 * G.LDC + c;
+    float faP[WD], fmP[WD], rs[WD], exv[WD];
+    const bool seeded = d.rough && h == 0 && !d.bottom_only;
+    const bool extb = d.medium == 0 && d.ext_off >= 0 && h == 0 && tk.m <= d.ext_mmax;
+    const float fs_tdn = d.rough ? seed_scale(d, tk) : 0.f;
+#pragma unroll
+    for (int u = 0; u < WD; ++u) {
+        faP[u] = d.bottom_only ? 0.f : pv[u];
+        fmP[u] = d.bottom_only ? 0.f : pv[G.LDC + u];
+        rs[u] = seeded ? W.srf[tk.srf_off + (size_t)NR * N * 9 + (g + u) * 9 + s * 3] : 0.f;
+        exv[u] = extb ? (float)B.ext[d.ext_off + ((size_t)tk.m * NR + g + u) * 3 + s] : 0.f;
+    }
+    const float *Jdt = (d.medium == 1 && d.ext_off >= 0 && tk.m <= d.ext_mmax) ? W.J + tk.fld_off + c : nullptr;
+    float *Fp = W.F + tk.fld_off + c, *Tp = W.Tot + tk.fld_off + c;
+    const int cw = coef_quad_width(NR);
+    const float *cq = B.Cq + coef_quad_off(d.coef_off, N, NR) + (g >> 2) * 12 + (g & 3);
+    const float *lvb = B.lvf + 3 * d.lev_off;
+    const float *eab = B.Eatt + d.lev_off * NR + g;
+    float I[WD], Jp[WD];
+#pragma unroll
+    for (int u = 0; u < WD; ++u) { I[u] = 0.f; Jp[u] = 0.f; }
+    constexpr int PF = WD == 4 ? 2 : 4;
+    for (int j0 = 0; j0 <= nt; j0 += PF) {
+        const int cnt = nt - j0 + 1 < PF ? nt - j0 + 1 : PF;
+        float lx[PF], ly[PF], lc[PF], tv[PF][WD], av[PF][WD], bv[PF][WD], ea[PF][WD], jd[PF][WD];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            if (q < cnt) {
+                const int j = j0 + q, k = h == 0 ? nt - j : j;
+                const float *lv = lvb + 3 * k;
+                lx[q] = lv[0]; ly[q] = lv[1]; lc[q] = lv[2];
+                if (j > 0) {
+                    const float *w = cq + (size_t)(h == 0 ? k : k - 1) * cw;
+                    if (WD == 4) {
+                        const float4 t4 = *reinterpret_cast<const float4 *>(w);
+                        const float4 a4 = *reinterpret_cast<const float4 *>(w + 4);
+                        const float4 b4 = *reinterpret_cast<const float4 *>(w + 8);
+                        tv[q][0] = t4.x; tv[q][WD > 1 ? 1 : 0] = t4.y; tv[q][WD > 2 ? 2 : 0] = t4.z; tv[q][WD - 1] = t4.w;
+                        av[q][0] = a4.x; av[q][WD > 1 ? 1 : 0] = a4.y; av[q][WD > 2 ? 2 : 0] = a4.z; av[q][WD - 1] = a4.w;
+                        bv[q][0] = b4.x; bv[q][WD > 1 ? 1 : 0] = b4.y; bv[q][WD > 2 ? 2 : 0] = b4.z; bv[q][WD - 1] = b4.w;
+                    } else {
+                        tv[q][0] = w[0]; av[q][0] = w[4]; bv[q][0] = w[8];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < WD; ++u) ea[q][u] = (seeded || extb) ? eab[(size_t)k * NR + u] : 0.f;
+                if (Jdt) {
+                    if (WD == 4) {
+                        const float4 x = *reinterpret_cast<const float4 *>(Jdt + (size_t)k * G.LDC);
+                        jd[q][0] = x.x; jd[q][WD > 1 ? 1 : 0] = x.y; jd[q][WD > 2 ? 2 : 0] = x.z; jd[q][WD - 1] = x.w;
+                    } else {
+                        jd[q][0] = Jdt[(size_t)k * G.LDC];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            if (q < cnt) {
+                const int j = j0 + q, k = h == 0 ? nt - j : j;
+                float tx[WD], ty[WD];
+#pragma unroll
+                for (int u = 0; u < WD; ++u) {
+                    float Jk = lc[q] * (lx[q] * faP[u] + ly[q] * fmP[u]);
+                    if (Jdt) Jk += jd[q][u];
+                    if (!isfinite(Jk)) bad = 1;
+                    if (j > 0) I[u] = tv[q][u] * I[u] + av[q][u] * Jk + bv[q][u] * Jp[u];
+                    Jp[u] = Jk;
+                    float2 t = make_float2(I[u], 0.f);
+                    if (seeded) t = df_add(t, fs_tdn * ea[q][u] * rs[u]);
+                    if (extb) t = df_add(t, exv[u] * ea[q][u]);
+                    tx[u] = t.x; ty[u] = t.y;
+                }
+                const size_t o = (size_t)k * G.LDC;
+                if (WD == 4) {
+                    const float4 v = make_float4(tx[0], tx[WD > 1 ? 1 : 0], tx[WD > 2 ? 2 : 0], tx[WD - 1]);
+                    *reinterpret_cast<float4 *>(Fp + o) = v;
+                    *reinterpret_cast<float4 *>(Tp + o) = v;
+                } else {
+                    Fp[o] = tx[0];
+                    Tp[o] = tx[0];
+                }
+                if (k == 0 || k == nt) {
+#pragma unroll
+                    for (int u = 0; u < WD; ++u) W.Ttl[tot_tail_off(tk, G, k, c + u)] = ty[u];
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 4) k_primary4(BatchBufs B, WaveBufs W, Geom G, int t0)
+{
+    const int tl = blockIdx.x, tg = t0 + tl;
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int tid = threadIdx.x, N = G.N, nq = 6 * N / 4;
+    if (tid == 0) {
+        TaskState st;
+        st.orders = 1;
+        st.active = d.max_orders > 1;
+        st.converged = d.max_orders <= 1;
+        st.pad_ = 0;
+        st.resid = 0.0;
+        B.state[tg] = st;
+        if (st.active) queue_next(B, 2, tl, tk.has_mol, d.nt + 1);
+    }
+    int bad = 0;
+    int s, h, g;
+    if (tid < nq) {
+        const int c = 4 * tid;
+        decode_col(G, c, s, h, g);
+        primary_cols<4>(B, W, G, tk, d, tl, c, s, h, g, bad);
+    } else if (tid < nq + 6 * G.E) {
+        const int c = 6 * N + (tid - nq);
+        decode_col(G, c, s, h, g);
+        if (g < d.n_ring) primary_cols<1>(B, W, G, tk, d, tl, c, s, h, g, bad);
+    }
+    if (bad) atomicExch(B.err, -2);
+}
+
 // Tiled SIMT GEMM: per task, J[k][c] = x_k * sum_i F[k][col(i)] A[i][c] + y_k * (... B ...).
 // Tile 64 levels x 64 output columns, 256 threads, 4x4 outputs per thread.
 #define ST_K 16

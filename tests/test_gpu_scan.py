@@ -11,12 +11,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _batch(A, N, n=6, seed=5):
+def _batch(A, N, n=6, seed=5, surfaces=("black_fresnel_ocean", "black", "flat")):
     from synthetic import hg_aerosol_moments
     rng = np.random.default_rng(seed)
     cases, opts, aers = [], [], []
     for i in range(n):
-        cases.append(A.default_case(surface=["black_fresnel_ocean", "black", "flat"][i % 3],
+        cases.append(A.default_case(surface=surfaces[i % len(surfaces)],
                                     sza_deg=rng.uniform(0, 70), vza_deg=rng.uniform(0, 60), raa_deg=rng.uniform(0, 180),
                                     wavelength_nm=rng.choice([443.0, 555.0, 865.0]), wind_speed=rng.uniform(1, 10)))
         opts.append(A.default_opts(n_mu=N, n_layers=int(rng.choice([20, 37, 60])), fourier_m_max=int(rng.integers(2, 9)),
@@ -80,3 +80,17 @@ def test_scan_autotuner_matches_column_scan(gpu, monkeypatch):
     recs = [r for r in gpu.autotune_summary() if r["kernel"] == "transport_scan" and r["key"][:2] == [20, 1]]
     assert recs, gpu.autotune_summary()
     assert recs[0]["best"] in ("quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2")
+
+
+@pytest.mark.parametrize("N", [8, 32])
+def test_primary4_equals_column_primary(gpu, monkeypatch, N):
+    """The four-column order-1 kernel (no flat surface in the batch: rough
+    ocean with its direct-beam seeds, black) against the one-column one."""
+    from ocrt_gb300 import _abi as A
+    cases, opts, aers = _batch(A, N, surfaces=("black_fresnel_ocean", "black"))
+    monkeypatch.setenv("OCRT_GB_SCAN", "quad")
+    quad = gpu.solve_batch(cases, opts, aers)
+    monkeypatch.setenv("OCRT_GB_PRIMARY", "column")
+    col = gpu.solve_batch(cases, opts, aers)
+    for k in ("rho_I", "rho_Q", "rho_U", "T_diff_dn_hemi", "order_modes"):
+        np.testing.assert_allclose(quad[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
