@@ -84,7 +84,14 @@ typedef struct {
     const ocrt_gas *gas;     /* NULL => no gas absorption (abs_state, rt_atm.c:437) */
 } ocrt_opts;
 
-/* ---- aerosol expansion (rt_aerosol_input_t moment path, rt_solver.h:94-114) */
+/* ---- aerosol (rt_aerosol_input_t, rt_solver.h:94-114) ------------------
+ * The moment expansion drives every element of the aerosol phase matrix.
+ * With use_value_kernel set, the intensity-to-intensity phase table is
+ * instead the direct azimuth integral (720 midpoints) of the tabulated P11,
+ * linear in the scattering angle (rt_solver.c:188-235), and IPSS weights the
+ * aerosol single scattering with the same table (rt_ipss.c:81-146); the
+ * polarised elements stay on the moments.  Zero-filled trailing fields give
+ * the moment path. */
 typedef struct {
     double tau_a;            /* column AOD at the wavelength */
     double ssa_a;            /* aerosol single-scattering albedo [0,1] */
@@ -93,6 +100,10 @@ typedef struct {
     const double *gamma;     /* [L_max+1] */
     const double *alpha;     /* [L_max+1] */
     const double *zeta;      /* [L_max+1] */
+    int    use_value_kernel; /* 0: moment kernel; 1: value kernel from the phase table below */
+    int    n_ang_phase;      /* table size (>= 2 when use_value_kernel) */
+    const double *theta_phase;                     /* [n_ang_phase] scattering angles, degrees, ascending */
+    const double *P11_phase, *P12_phase, *P33_phase; /* [n_ang_phase], normalised so (1/2) int P11 dmu = 1 */
 } ocrt_aerosol;
 
 /* ---- per-case output (solve-path fields of rt_result_t, rt_types.h:496-651) */
@@ -332,6 +343,48 @@ int  ocrt_gb_gas_columns(const ocrt_gas *gas, double *column_eff, double *column
  * altitudes in km (z_km, opts.n_layers + 1 entries, level 0 = TOA). */
 int  ocrt_gb_layer_gas(const ocrt_case *cs, const ocrt_opts *opts, const ocrt_aerosol *aer,
                        double *tau_abs, double *z_km);
+
+/* ---- aerosol models from .mie tables ------------------------------------
+ * ocrt_gb_mie_read replaces read_mie_file (shared/mie_io.c:174-327): the
+ * OPAC layout (angle count, free header, spectral rows of wavelength [um]
+ * and six columns, then the P11, P12 and P33 blocks with an optional TETA
+ * line naming a separate phase-wavelength grid).  ocrt_gb_mie_prepare
+ * replaces rt_aerosol_runtime_prepare (rt_aerosol_runtime.c:13-285) for the
+ * CLI's aerosol protocol (main.c:3296-3343, 3646-3686): the AOD given at
+ * aod_ref_nm is carried to the wavelength by the table's extinction ratio,
+ * SSA is interpolated linearly, P11/P12/P33 by PCHIP in wavelength; the
+ * real-angle log10-linear forward-peak truncation (rt_aerosol.c:403-552) with
+ * its mass-conserving tau/SSA renormalisation; vector moments to L_max from
+ * a 4096-point PCHIP-densified angle grid (rt_aerosol.c:119-213, 649-774);
+ * and the phase table normalised by beta_0 and ordered by ascending angle
+ * for the value kernel.  The prepared aerosol (ocrt_mie_aerosol) owns the
+ * arrays that the filled ocrt_aerosol points into. */
+typedef struct ocrt_mie ocrt_mie;
+typedef struct ocrt_mie_aerosol ocrt_mie_aerosol;
+typedef struct {
+    int    L_max;                /* moment order (CLI default 80) */
+    int    use_loglin_trunc;     /* 1 (CLI default): log10-linear truncation */
+    double loglin_mu1, loglin_mu2, loglin_threshold;   /* 0.8, 0.94, 0.1 */
+    int    use_value_kernel;     /* 1 (CLI default): value kernel for the I-I table */
+} ocrt_mie_opts;
+typedef struct {
+    double aod_ref, aod_ref_nm;          /* the given AOD and its wavelength */
+    double aod_target, extinction_ratio; /* AOD at the wavelength = aod_ref * extinction_ratio */
+    double ssa_raw;                      /* interpolated SSA before truncation */
+    double trunc_A;                      /* truncation coefficient A (0: none) */
+    double tau_a_eff, ssa_a_eff;         /* after the truncation renormalisation */
+} ocrt_mie_diag;
+void ocrt_mie_opts_default(ocrt_mie_opts *o);
+int  ocrt_gb_mie_read(const char *path, ocrt_mie **out);
+void ocrt_gb_mie_free(ocrt_mie *m);
+/* Table sizes: angles, spectral wavelengths, phase wavelengths (any may be NULL). */
+int  ocrt_gb_mie_shape(const ocrt_mie *m, int *n_ang, int *n_wl, int *n_phase_wl);
+/* OCRT_ERR_ARGS when the wavelength or aod_ref_nm lies outside the table's
+ * grids, the table does not span 0..180 degrees, or aod_ref <= 0. */
+int  ocrt_gb_mie_prepare(const ocrt_mie *m, double wavelength_nm, double aod_ref, double aod_ref_nm,
+                         const ocrt_mie_opts *opts, ocrt_mie_aerosol **out, ocrt_aerosol *aer,
+                         ocrt_mie_diag *diag);
+void ocrt_gb_mie_aerosol_free(ocrt_mie_aerosol *a);
 
 /* ---- coupled atmosphere-ocean (rt_solve_case_ocean, rt_solver.h:145-149) -
  * Three successive-orders solves joined at a rough (Cox-Munk) air-water

@@ -10,7 +10,8 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Lut, LutHolder, Ocean, OceanHolder,
+from ._abi import (Aerosol, AerosolHolder, Case, Diag, Grad, Layers, LayersHolder, Lut, LutHolder, MieDiag, MieOpts,
+                   Ocean, OceanHolder,
                    OceanResult, Opts, Result, default_case, default_opts, lut_grid_reference_cli, ocean_result_dict,
                    result_dict, RESULT_FIELDS)
 
@@ -27,6 +28,8 @@ EXPORTS = [
     "ocrt_gb_solve_case_lut", "ocrt_gb_solve_batch_lut", "ocrt_gb_plan_graph_ready", "ocrt_gb_autotune_summary",
     "ocrt_gb_gas_create", "ocrt_gb_gas_destroy", "ocrt_gb_gas_tau", "ocrt_gb_gas_columns", "ocrt_gb_layer_gas",
     "ocrt_ocean_default", "ocrt_gb_solve_ocean", "ocrt_gb_solve_batch_ocean",
+    "ocrt_mie_opts_default", "ocrt_gb_mie_read", "ocrt_gb_mie_free", "ocrt_gb_mie_shape", "ocrt_gb_mie_prepare",
+    "ocrt_gb_mie_aerosol_free",
 ]
 
 
@@ -93,6 +96,16 @@ def lib():
     L.ocrt_gb_solve_batch_ocean.argtypes = [C.c_int, C.POINTER(Case), C.POINTER(Opts), C.c_int, C.POINTER(Aerosol),
                                             C.c_int, C.POINTER(Ocean), C.c_int, C.POINTER(Result),
                                             C.POINTER(OceanResult), C.c_void_p]
+    L.ocrt_mie_opts_default.argtypes = [C.POINTER(MieOpts)]
+    L.ocrt_mie_opts_default.restype = None
+    L.ocrt_gb_mie_read.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    L.ocrt_gb_mie_free.argtypes = [C.c_void_p]
+    L.ocrt_gb_mie_free.restype = None
+    L.ocrt_gb_mie_shape.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.ocrt_gb_mie_prepare.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.POINTER(MieOpts),
+                                      C.POINTER(C.c_void_p), C.POINTER(Aerosol), C.POINTER(MieDiag)]
+    L.ocrt_gb_mie_aerosol_free.argtypes = [C.c_void_p]
+    L.ocrt_gb_mie_aerosol_free.restype = None
     _lib = L
     return L
 
@@ -115,7 +128,7 @@ def solve_case(case, opts=None, aerosol=None, diag=False):
                 "view_I_m": (C.c_double * n)(), "view_Q_m": (C.c_double * n)(),
                 "view_U_m": (C.c_double * n)()}
         d = Diag(**{k: C.cast(v, Diag._fields_[i][1]) for i, (k, v) in enumerate(arrs.items())})
-    a = aerosol.struct if isinstance(aerosol, AerosolHolder) else aerosol
+    a = aerosol.struct if hasattr(aerosol, "struct") else aerosol
     _check(L.ocrt_gb_solve_case(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
                                 C.byref(r), C.byref(d) if d is not None else None))
     out = result_dict(r)
@@ -155,10 +168,10 @@ def _arrays(cases, opts, aerosols):
     if aerosols is None:
         aa, app = None, 0
     elif isinstance(aerosols, (list, tuple)):
-        structs = [a.struct if isinstance(a, AerosolHolder) else a for a in aerosols]
+        structs = [a.struct if hasattr(a, "struct") else a for a in aerosols]
         aa, app = (Aerosol * n)(*structs), 1
     else:
-        s = aerosols.struct if isinstance(aerosols, AerosolHolder) else aerosols
+        s = aerosols.struct if hasattr(aerosols, "struct") else aerosols
         aa, app = (Aerosol * 1)(s), 0
     return n, ca, oa, opp, aa, app
 
@@ -177,7 +190,7 @@ def layer_defaults(case, opts, aerosol=None):
     L = lib()
     n = opts.n_layers
     dt, ss = np.zeros(n), np.zeros(n)
-    a = aerosol.struct if isinstance(aerosol, AerosolHolder) else aerosol
+    a = aerosol.struct if hasattr(aerosol, "struct") else aerosol
     _check(L.ocrt_gb_layer_defaults(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
                                     dt.ctypes.data_as(C.POINTER(C.c_double)),
                                     ss.ctypes.data_as(C.POINTER(C.c_double))))
@@ -240,7 +253,7 @@ def layer_gas(case, opts, aerosol=None):
     L = lib()
     n = opts.n_layers
     ta, z = np.zeros(n), np.zeros(n + 1)
-    a = aerosol.struct if isinstance(aerosol, AerosolHolder) else aerosol
+    a = aerosol.struct if hasattr(aerosol, "struct") else aerosol
     _check(L.ocrt_gb_layer_gas(C.byref(case), C.byref(opts), C.byref(a) if a is not None else None,
                                ta.ctypes.data_as(C.POINTER(C.c_double)), z.ctypes.data_as(C.POINTER(C.c_double))))
     return ta, z
@@ -424,3 +437,65 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class MieAerosol:
+    """A .mie aerosol prepared at one wavelength (ocrt_gb_mie_prepare): .struct
+    is the ocrt_aerosol to pass to the solves, .diag the preparation's
+    diagnostics.  The native object owning the arrays lives as long as this."""
+
+    def __init__(self, handle, struct, diag):
+        self._h, self.struct, self.diag = handle, struct, diag
+
+    @property
+    def L_max(self):
+        return self.struct.L_max
+
+    def arrays(self):
+        """Moments and phase table as numpy copies."""
+        s = self.struct
+        L, n = s.L_max + 1, s.n_ang_phase
+        out = {k: np.ctypeslib.as_array(getattr(s, k), (L,)).copy() for k in ("beta", "gamma", "alpha", "zeta")}
+        for k in ("theta_phase", "P11_phase", "P12_phase", "P33_phase"):
+            out[k] = np.ctypeslib.as_array(getattr(s, k), (n,)).copy()
+        return out
+
+    def __del__(self):
+        if self._h and _lib is not None:
+            _lib.ocrt_gb_mie_aerosol_free(self._h)
+            self._h = None
+
+
+class MieModel:
+    """An aerosol model read from a .mie table (ocrt_gb_mie_read)."""
+
+    def __init__(self, path):
+        L = lib()
+        self._h = C.c_void_p()
+        _check(L.ocrt_gb_mie_read(os.fsencode(path), C.byref(self._h)))
+        self.path = path
+
+    def shape(self):
+        a, w, p = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().ocrt_gb_mie_shape(self._h, C.byref(a), C.byref(w), C.byref(p)))
+        return a.value, w.value, p.value
+
+    def prepare(self, wavelength_nm, aod_ref, aod_ref_nm=555.0, L_max=80, value_kernel=True, loglin=True):
+        """The aerosol at a wavelength, the CLI's protocol by default: AOD given
+        at aod_ref_nm, log10-linear truncation, moments to L_max = 80, value
+        kernel for the intensity table."""
+        L = lib()
+        o = MieOpts()
+        L.ocrt_mie_opts_default(C.byref(o))
+        o.L_max = int(L_max)
+        o.use_value_kernel = 1 if value_kernel else 0
+        o.use_loglin_trunc = 1 if loglin else 0
+        h, aer, dg = C.c_void_p(), Aerosol(), MieDiag()
+        _check(L.ocrt_gb_mie_prepare(self._h, float(wavelength_nm), float(aod_ref), float(aod_ref_nm), C.byref(o),
+                                     C.byref(h), C.byref(aer), C.byref(dg)))
+        return MieAerosol(h, aer, {f: getattr(dg, f) for f, _ in MieDiag._fields_})
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ocrt_gb_mie_free(self._h)
+            self._h = None

@@ -58,7 +58,20 @@ class Aerosol(C.Structure):
         ("tau_a", C.c_double), ("ssa_a", C.c_double), ("L_max", C.c_int),
         ("beta", C.POINTER(C.c_double)), ("gamma", C.POINTER(C.c_double)),
         ("alpha", C.POINTER(C.c_double)), ("zeta", C.POINTER(C.c_double)),
+        ("use_value_kernel", C.c_int), ("n_ang_phase", C.c_int),
+        ("theta_phase", C.POINTER(C.c_double)), ("P11_phase", C.POINTER(C.c_double)),
+        ("P12_phase", C.POINTER(C.c_double)), ("P33_phase", C.POINTER(C.c_double)),
     ]
+
+
+class MieOpts(C.Structure):
+    _fields_ = [("L_max", C.c_int), ("use_loglin_trunc", C.c_int), ("loglin_mu1", C.c_double),
+                ("loglin_mu2", C.c_double), ("loglin_threshold", C.c_double), ("use_value_kernel", C.c_int)]
+
+
+class MieDiag(C.Structure):
+    _fields_ = [(f, C.c_double) for f in ("aod_ref", "aod_ref_nm", "aod_target", "extinction_ratio", "ssa_raw",
+                                          "trunc_A", "tau_a_eff", "ssa_a_eff")]
 
 
 class Result(C.Structure):
@@ -169,9 +182,11 @@ def default_opts(**kw):
 
 
 class AerosolHolder:
-    """Keeps the moment arrays alive while an Aerosol struct points into them."""
+    """Keeps the moment arrays (and, for the value kernel, the phase table:
+    ascending angles in degrees and P11, P12, P33) alive while an Aerosol
+    struct points into them."""
 
-    def __init__(self, tau_a, ssa_a, beta, gamma, alpha, zeta):
+    def __init__(self, tau_a, ssa_a, beta, gamma, alpha, zeta, phase=None, value_kernel=None):
         import numpy as np
         self.arrays = [np.ascontiguousarray(np.asarray(a, dtype=np.float64))
                        for a in (beta, gamma, alpha, zeta)]
@@ -179,6 +194,12 @@ class AerosolHolder:
         ptrs = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self.arrays]
         self.struct = Aerosol(tau_a=float(tau_a), ssa_a=float(ssa_a), L_max=L,
                               beta=ptrs[0], gamma=ptrs[1], alpha=ptrs[2], zeta=ptrs[3])
+        if phase is not None:
+            self.phase = [np.ascontiguousarray(np.asarray(a, dtype=np.float64)) for a in phase]
+            pp = [a.ctypes.data_as(C.POINTER(C.c_double)) for a in self.phase]
+            self.struct.use_value_kernel = 1 if value_kernel is None else int(value_kernel)
+            self.struct.n_ang_phase = len(self.phase[0])
+            self.struct.theta_phase, self.struct.P11_phase, self.struct.P12_phase, self.struct.P33_phase = pp
 
     @property
     def L_max(self):

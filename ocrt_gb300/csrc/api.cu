@@ -144,6 +144,19 @@ int validate(const ocrt_case *cs, const ocrt_opts *op, const ocrt_aerosol *aer)
         for (int l = 0; l <= aer->L_max; ++l)
             if (!std::isfinite(aer->beta[l]) || !std::isfinite(aer->gamma[l]) || !std::isfinite(aer->alpha[l]) ||
                 !std::isfinite(aer->zeta[l])) return fail(OCRT_ERR_NONFINITE, "non-finite aerosol moment");
+        if (aer->use_value_kernel && aer->tau_a > 0.0) {
+            const int n = aer->n_ang_phase;
+            if (n < 2 || n > 8192 || !aer->theta_phase || !aer->P11_phase)
+                return fail(OCRT_ERR_ARGS, "value kernel: phase table of 2 .. 8192 angles required");
+            for (int i = 0; i < n; ++i) {
+                if (!std::isfinite(aer->theta_phase[i]) || !std::isfinite(aer->P11_phase[i]))
+                    return fail(OCRT_ERR_NONFINITE, "value kernel: non-finite phase table");
+                if (i && !(aer->theta_phase[i] > aer->theta_phase[i - 1]))
+                    return fail(OCRT_ERR_ARGS, "value kernel: phase angles must ascend strictly");
+            }
+            if (cs->surface == OCRT_SURFACE_FLAT || (cs->surface == OCRT_SURFACE_BLACK_FRESNEL_OCEAN && !(cs->wind_speed > 0.0)))
+                return fail(OCRT_ERR_UNSUPPORTED, "value kernel with a flat surface is not on the GB300 path");
+        }
     }
     double tau_r;
     if (!(cs->pressure_hpa > 0.0)) tau_r = 0.0;
@@ -287,6 +300,14 @@ struct Group {
     float *Tc = nullptr, *Ca = nullptr, *Cb = nullptr;
     float *Cq = nullptr;                  // transport weights in quads (k_scan4, k_scan_tma), nullptr when the column scan runs
     ScanMaps smap[3];                     // k_scan_tma tensor maps for level chunks of 4, 8, 16
+    // aerosol value kernel: tables of every such pixel (ascending degrees, P11),
+    // and the wave's I-I tables from k_value_pfm ([wave pixel][m][N + 1][2 NR])
+    bool any_vk = false;
+    int vk_nmax = 0;
+    double *vk_th = nullptr, *vk_p11 = nullptr;
+    float *vkV = nullptr;
+    long long vk_stride = 0;
+    int wave_pix = 0;
     bool smap_ok = false;
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
     double *lam = nullptr;
@@ -380,7 +401,7 @@ void free_group(Group &g)
                     g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.Ttl,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
-                    g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out};
+                    g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out, g.vk_th, g.vk_p11, g.vkV};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -396,7 +417,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     const Geom G = make_geom(g.N, g.E);
     g.G = G;
     g.P = (int)g.idx.size();
-    std::vector<double> mb, mgv, ma, mz;
+    std::vector<double> mb, mgv, ma, mz, vth, vp11;
     size_t lev = 0, coef = 0;
     int task = 0;
     for (int q = 0; q < g.P; ++q) {
@@ -450,6 +471,14 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
             for (int l = 0; l <= a->L_max; ++l) {
                 mb.push_back(a->beta[l]); mgv.push_back(a->gamma[l]); ma.push_back(a->alpha[l]); mz.push_back(a->zeta[l]);
             }
+            if (a->use_value_kernel && a->n_ang_phase > 1) {
+                d.vk_n = a->n_ang_phase;
+                d.vk_off = (long long)vth.size();
+                vth.insert(vth.end(), a->theta_phase, a->theta_phase + a->n_ang_phase);
+                vp11.insert(vp11.end(), a->P11_phase, a->P11_phase + a->n_ang_phase);
+                g.any_vk = true;
+                g.vk_nmax = std::max(g.vk_nmax, d.vk_n);
+            }
         }
         d.L = std::max(std::max(d.M, 2), d.L_aer);
         d.lev_off = (long long)lev; lev += d.nt + 1;
@@ -491,6 +520,7 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         g.wave_fld = std::max(g.wave_fld, w.fld); g.wave_ops = std::max(g.wave_ops, w.ops);
         g.wave_tail = std::max(g.wave_tail, w.tail);
         g.wave_srf = std::max(g.wave_srf, w.srf); g.wave_tasks = std::max(g.wave_tasks, w.t1 - w.t0);
+        g.wave_pix = std::max(g.wave_pix, w.p1 - w.p0);
     };
     for (int q = 0; q < g.P; ++q) {
         const PixDev &d = g.hpx[q];
@@ -503,6 +533,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         if (ncot > 0)   // adjoint fields, dR/dW, per-task partials
             pb += (size_t)ncot * (pf * 12 + nm * (G.NR * 3 * 4 + sizeof(TaskState) + (3 * K + 4) * 8)) + ps * 4 +
                   nm * (size_t)2 * (G.CIN + 32) * ((G.COUT + 31) & ~31) * 4;
+        if (g.any_vk)   // the value kernel's tables of the pixel
+            pb += (size_t)(g.Mmax + 1) * (G.N + 1) * 2 * G.NR * 4;
         if (q > w.p0 && bytes + pb > budget) {
             close(q);
             w = Wave{q, 0, d.task0, 0, 0, 0, 0, 0, false, false};
@@ -562,6 +594,12 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.Bx, (size_t)g.wave_tasks * 3 * (1 + G.E) * (g.Lmax + 1))))
         return rc;
     if (g.any_layers && ((rc = up(g.ldt, ldt)) || (rc = up(g.lss, lss)))) return rc;
+    if (g.any_vk) {
+        g.vk_stride = (long long)(g.Mmax + 1) * (G.N + 1) * 2 * G.NR;
+        if ((rc = up(g.vk_th, vth)) || (rc = up(g.vk_p11, vp11)) ||
+            (rc = alloc(g.vkV, (size_t)g.wave_pix * g.vk_stride)))
+            return rc;
+    }
     if (g.any_lut && ((rc = up(g.lut_vza, hlv)) || (rc = up(g.lut_raa, hlr)) ||
                       (rc = alloc(g.lut_samp, (size_t)g.T * g.lut_nvmax * 4)) ||
                       (rc = alloc(g.lut_kappa, (size_t)g.lut_ntot)) || (rc = alloc(g.lut_out, 6 * (size_t)g.lut_ntot))))
@@ -873,10 +911,14 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         CK(cudaMemsetAsync(g.aflag, 0, (size_t)nw, st));
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 128 / (1 + G.E) - 1) / (128 / (1 + G.E)), 128, 0, st>>>(
                    g.tasks, w.t0, nw, g.px, g.Lmax, G.E, g.Bx));
+        if (g.any_vk)
+            LAUNCH(plan, KC_TABLES, k_value_pfm<<<dim3(((G.N + 1) * 2 * G.NR + 127) / 128, w.p1 - w.p0), 128,
+                                                  value_kernel_smem_bytes(g.vk_nmax), st>>>(
+                       g.px, w.p0, G, g.gmu, g.vk_th, g.vk_p11, g.vkV, g.vk_stride));
         auto tables = [&](int b) {
             k_tables<<<dim3(nw, tables_yblocks(b, G.NR, G.N)), b, tables_smem_bytes(b, G.N, g.Lmax), st>>>(
                 g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec,
-                W.fvec, W.opt, (!g.use_tc || g.ncot > 0) ? 1 : 0);
+                W.fvec, W.opt, (!g.use_tc || g.ncot > 0) ? 1 : 0, g.any_vk ? g.vkV : nullptr, w.p0, g.vk_stride);
         };
         int tb = 256;
         int rc = tuned_block("k_tables", (const void *)k_tables, {G.N, g.Lmax, g.Mmax}, !capture, st, tables, &tb);
@@ -1050,11 +1092,12 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         for (const PixDev &d : g.hpx) maxnt = std::max(maxnt, d.nt);
         const size_t smem = sizeof(double) * (6 * (size_t)maxnt + 6) + sizeof(int) * ((size_t)maxnt + 1);
         LAUNCH(plan, KC_IPSS, k_ipss<<<P, 256, smem, st>>>(g.px, P, g.h, g.z, g.xd, g.yd,
-                                                           g.any_gas ? g.tabs : nullptr, g.mb, g.kappa, g.taudir));
+                                                           g.any_gas ? g.tabs : nullptr, g.mb, g.vk_th, g.vk_p11,
+                                                           g.kappa, g.taudir));
         if (g.any_lut)
             LAUNCH(plan, KC_IPSS, k_ipss_lut<<<dim3(std::min(g.lut_ptmax, 2048), P), 256, smem, st>>>(
-                       g.px, P, g.h, g.z, g.xd, g.yd, g.any_gas ? g.tabs : nullptr, g.mb, g.lut_vza, g.lut_raa,
-                       g.lut_kappa));
+                       g.px, P, g.h, g.z, g.xd, g.yd, g.any_gas ? g.tabs : nullptr, g.mb, g.vk_th, g.vk_p11,
+                       g.lut_vza, g.lut_raa, g.lut_kappa));
     }
     if (g.any_lut)
         LAUNCH(plan, KC_FINAL, k_lut_final<<<dim3((g.lut_ptmax + 127) / 128, P), 128, 0, st>>>(g.px, P, make_lut(g),
@@ -1101,6 +1144,7 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_coxmunk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(cudaFuncSetAttribute(k_value_pfm, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan4, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(scan_tma_init());
@@ -1768,6 +1812,8 @@ int ocean_solve(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp, c
         int rc = validate_ocean(cases[i], o, oc);
         if (rc) return rc;
         if (oc.n_mu_water != Nw) return fail(OCRT_ERR_ARGS, "coupled batch: n_mu_water must be common to the batch");
+        if (aer && (app ? aer[i] : aer[0]).use_value_kernel)
+            return fail(OCRT_ERR_UNSUPPORTED, "coupled solve: the aerosol value kernel is not on the GB300 path");
         const int np = o.n_phi_surface > 0 ? o.n_phi_surface : 1024;
         if (nphi >= 0 && np != nphi) return fail(OCRT_ERR_ARGS, "coupled batch: n_phi_surface must be common");
         nphi = np;

@@ -61,6 +61,9 @@ struct PixDev {
     double beam_q;          // incident-beam polarisation Q/I (water: Fresnel transmission)
     double xmu[OCRT_MAX_EXTRA];   // cosines of the zero-weight slots N.. (water: set by the host)
     double w_tau, w_omega_w, w_omega_p;   // water: optical depth, pure-water and hydrosol albedo
+    // ---- aerosol value kernel (rt_solver.c:188-235): tabulated P11, ascending angle ----
+    int vk_n;               // table entries; 0 = the I-I aerosol table from the moments
+    long long vk_off;       // offset of the table in the group's angle / P11 arrays
     // ---- derived on device (k_pixel_setup) ----
     double mu0, mu_view, tau_r, tau_total;
     int n_ring, view_slot;  // view_slot: ring slot holding mu_view, -1 = interpolate

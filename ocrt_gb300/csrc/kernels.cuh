@@ -64,7 +64,13 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
-                         float *ops, float *pvec, float *fvec, float *opt, int plain);
+                         float *ops, float *pvec, float *fvec, float *opt, int plain,
+                         const float *V, int vp0, long long vstride);
+// value.cu: the aerosol value kernel's I-I tables V[pixel - p0][m][row][column]
+// (rows: sun, Gauss nodes; columns: ring slots at +mu, then at -mu)
+__global__ void k_value_pfm(const PixDev *px, int p0, Geom G, const double *gmu, const double *vk_th,
+                            const double *vk_p11, float *V, long long vstride);
+size_t value_kernel_smem_bytes(int n_ang);
 // coxmunk_tc.cu: Cox-Munk Fourier kernels with the azimuth projection on tcgen05.
 // pairs: (outgoing slot, incoming slot) list of the ring (Gauss pairs with
 // outgoing > incoming left out: the reciprocal pair writes them).
@@ -217,8 +223,8 @@ struct LutBufs {
 __global__ void k_lut_sample(BatchBufs B, WaveBufs W, LutBufs Lb, Geom G, int t0, int nw);
 __global__ void k_lut_final(const PixDev *px, int P, LutBufs Lb, const int *pix_task0);
 __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
-                           const double *yd, const double *tabs, const double *mb, const double *lut_vza,
-                           const double *lut_raa, double *lut_kappa);
+                           const double *yd, const double *tabs, const double *mb, const double *vk_th,
+                           const double *vk_p11, const double *lut_vza, const double *lut_raa, double *lut_kappa);
 __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
@@ -258,7 +264,7 @@ __global__ void k_stop_check(const int *active_after_last, int *flag);
 // post.cu
 __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
                        const double *xd, const double *yd, const double *tabs,
-                       const double *mb, double *kappa, double *tau_dir);
+                       const double *mb, const double *vk_th, const double *vk_p11, double *kappa, double *tau_dir);
 __global__ void k_finalize(const PixDev *px, int P, const TaskState *state, const TaskOut *tout,
                            const double *gmu, const double *gw, const double *h,
                            const double *kappa, const double *tau_dir, ocrt_result *res);

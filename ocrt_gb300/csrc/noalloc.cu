@@ -93,6 +93,9 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     int rc = ocrt_internal_validate(cs, opts, aer_in);
     if (rc) return rc;
     const ocrt_aerosol *aer = (aer_in && aer_in->tau_a > 0.0) ? aer_in : nullptr;
+    if (aer && aer->use_value_kernel)
+        return ocrt_internal_fail(OCRT_ERR_UNSUPPORTED, "noalloc: the aerosol value kernel needs its table buffers; "
+                                                        "use ocrt_gb_solve_case");
     if (opts->n_mu > NA_MAX_N || opts->n_layers > NA_MAX_LAYERS || opts->fourier_m_max > NA_MAX_M ||
         (aer && aer->L_max > NA_MAX_L) || opts->max_orders > NA_MAX_ORDERS)
         return ocrt_internal_fail(OCRT_ERR_ARGS, "noalloc: case exceeds the static-scratch limits "
@@ -256,7 +259,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
         NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, 1, Bx));
         NA_LAUNCH(k_tables<<<dim3(nw, tables_yblocks(256, G.NR, G.N)), 256, tables_smem_bytes(256, G.N, L), st>>>(
-            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec, nullptr, 1));
+            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec, nullptr, 1, nullptr, 0, 0));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= opts->max_orders; ++it) {
@@ -276,8 +279,8 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     }
     if (opts->pssa) {
         const size_t smem = sizeof(double) * (6 * (size_t)nt + 6) + sizeof(int) * ((size_t)nt + 1);
-        NA_LAUNCH(k_ipss<<<1, 256, smem, st>>>(px, 1, h, z, xd, yd, opts->gas ? tabs : nullptr, mb, kappa,
-                                               taudir));
+        NA_LAUNCH(k_ipss<<<1, 256, smem, st>>>(px, 1, h, z, xd, yd, opts->gas ? tabs : nullptr, mb, nullptr, nullptr,
+                                               kappa, taudir));
     }
     NA_LAUNCH(k_finalize<<<1, 32, 0, st>>>(px, 1, state, tout, gmu, gw, h, kappa, taudir, res));
     int dev_err = 0;

@@ -57,7 +57,8 @@ __device__ double ipss_tau_sun(const double *he, const double *beta, int nl, dou
 // block; thread 0 writes *kappa and, when tau_dir is non-null, the direct-beam
 // slant depth to the surface.
 __device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, const double *h, const double *z,
-                           const double *xd, const double *yd, const double *tabs, const double *mb, double *kappa,
+                           const double *xd, const double *yd, const double *tabs, const double *mb,
+                           const double *vk_th, const double *vk_p11, double *kappa,
                            double *tau_dir)
 {
     extern __shared__ double sm[];
@@ -91,13 +92,32 @@ __device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, cons
         const double sn = sqrt(fmax(0.0, 1.0 - d.mu0 * d.mu0));
         const double ct = sn * sin(tv) * cos(fp) - d.mu0 * cos(tv);
         PR = 1.0 + (1.0 - OCRT_DEPOL) / (2.0 + OCRT_DEPOL) * 0.5 * (3.0 * ct * ct - 1.0);
-        double p0 = 1.0, p1 = ct, s = mb[d.mom_off];
-        if (d.L_aer >= 1) s += mb[d.mom_off + 1] * p1;
-        for (int l = 2; l <= d.L_aer; ++l) {
-            const double p2 = ((2.0 * l - 1.0) * ct * p1 - (l - 1.0) * p0) / l;
-            s += mb[d.mom_off + l] * p2; p0 = p1; p1 = p2;
+        if (d.vk_n > 1 && vk_th) {
+            // the value kernel's table, linear in the angle (rt_ipss.c:131-146)
+            const double *th = vk_th + d.vk_off, *pv = vk_p11 + d.vk_off;
+            const int n = d.vk_n;
+            const double t = acos(fmax(-1.0, fmin(1.0, ct))) * 180.0 / OCRT_PI;
+            if (t <= th[0]) {
+                PA = pv[0];
+            } else if (t >= th[n - 1]) {
+                PA = pv[n - 1];
+            } else {
+                int lo = 0, hi = n - 1;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (th[mid] <= t) lo = mid; else hi = mid;
+                }
+                PA = pv[lo] + (t - th[lo]) / (th[hi] - th[lo]) * (pv[hi] - pv[lo]);
+            }
+        } else {
+            double p0 = 1.0, p1 = ct, s = mb[d.mom_off];
+            if (d.L_aer >= 1) s += mb[d.mom_off + 1] * p1;
+            for (int l = 2; l <= d.L_aer; ++l) {
+                const double p2 = ((2.0 * l - 1.0) * ct * p1 - (l - 1.0) * p0) / l;
+                s += mb[d.mom_off + l] * p2; p0 = p1; p1 = p2;
+            }
+            PA = s > 0.0 ? s : 0.0;
         }
-        PA = s > 0.0 ? s : 0.0;
     }
     for (int j = threadIdx.x; j < nl; j += blockDim.x) {
         const int k = nl - 1 - j;
@@ -191,7 +211,7 @@ __device__ void ipss_block(const PixDev &d, double vza_deg, double raa_deg, cons
 
 __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z,
                        const double *xd, const double *yd, const double *tabs,
-                       const double *mb, double *kappa, double *tau_dir)
+                       const double *mb, const double *vk_th, const double *vk_p11, double *kappa, double *tau_dir)
 {
     const int p = blockIdx.x;
     if (p >= P) return;
@@ -200,13 +220,13 @@ __global__ void k_ipss(const PixDev *px, int P, const double *h, const double *z
         if (threadIdx.x == 0) { kappa[p] = 1.0; tau_dir[p] = -1.0; }
         return;
     }
-    ipss_block(d, d.vza_deg, d.raa_deg, h, z, xd, yd, tabs, mb, &kappa[p], &tau_dir[p]);
+    ipss_block(d, d.vza_deg, d.raa_deg, h, z, xd, yd, tabs, mb, vk_th, vk_p11, &kappa[p], &tau_dir[p]);
 }
 
 // IPSS kappa at every (vza, raa) of each pixel's LUT grid: block (point, pixel).
 __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const double *z, const double *xd,
-                           const double *yd, const double *tabs, const double *mb, const double *lut_vza,
-                           const double *lut_raa, double *lut_kappa)
+                           const double *yd, const double *tabs, const double *mb, const double *vk_th,
+                           const double *vk_p11, const double *lut_vza, const double *lut_raa, double *lut_kappa)
 {
     const int p = blockIdx.y;
     if (p >= P) return;
@@ -219,7 +239,8 @@ __global__ void k_ipss_lut(const PixDev *px, int P, const double *h, const doubl
             continue;
         }
         const int iv = pt / d.lut_nr, ir = pt - iv * d.lut_nr;
-        ipss_block(d, lut_vza[d.lut_vo + iv], lut_raa[d.lut_ro + ir], h, z, xd, yd, tabs, mb, kout, nullptr);
+        ipss_block(d, lut_vza[d.lut_vo + iv], lut_raa[d.lut_ro + ir], h, z, xd, yd, tabs, mb, vk_th, vk_p11, kout,
+                   nullptr);
         __syncthreads();
     }
 }

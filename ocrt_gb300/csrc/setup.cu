@@ -357,7 +357,8 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
-                         float *ops, float *pvec, float *fvec, float *opt, int plain)
+                         float *ops, float *pvec, float *fvec, float *opt, int plain,
+                         const float *V, int vp0, long long vstride)
 {
     const int tl = blockIdx.x;
     if (tl >= nt_tasks) return;
@@ -380,6 +381,9 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     const double A = 2.0 * (1.0 - d.depol) / (2.0 + d.depol);
     const float b0 = m == 0 ? 1.f : 0.f, b2 = (float)(0.5 * A), g2 = (float)(-A * sqrt(1.5)), a2 = (float)(3.0 * A);
     const int mol = m <= 2;
+    // aerosol value kernel: the I-I table of this mode from k_value_pfm
+    const float *Vm = (V && d.vk_n > 1) ? V + (size_t)(tk.pix - vp0) * vstride + (size_t)m * (N + 1) * 2 * G.NR
+                                        : nullptr;
     float *Aop = ops + tk.op_off;
     float *Atile = opt ? opt + 2 * tk.op_off : nullptr;     // tensor-core tiles of the aerosol operator
     float *Bop = tk.mol_off >= 0 ? ops + tk.mol_off : nullptr;
@@ -496,6 +500,10 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
         for (int q = 0; q < 4; ++q) { St[q] = Ea[9 + q] + Oa[9 + q]; Dt[q] = Ea[9 + q] - Oa[9 + q]; }
         float c[18];
         c[0] = S[0];             c[1] = D[0];               // pfm[i][+-o]
+        if (Vm) {                                           // the value kernel's table instead
+            c[0] = Vm[(size_t)(1 + i) * 2 * G.NR + os];
+            c[1] = Vm[(size_t)(1 + i) * 2 * G.NR + G.NR + os];
+        }
         c[2] = S[2];             c[3] = -D[2];              // gt[i][+-o]
         c[4] = St[0];            c[5] = -Dt[0];             // gt[o][+-i]
         c[6] = S[1];             c[7] = D[1];               // gr[i][+-o]
@@ -598,7 +606,7 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
             for (int q = 0; q < 2; ++q) (ev ? Ey[q] : Oy[q]) += vy[q];
         }
         // row 0 (solar) tables at column +o (S) and -o (sigma D)
-        const float pfmP = E[0] + O[0], pfmM = E[0] - O[0];
+        const float pfmP = Vm ? Vm[os] : E[0] + O[0], pfmM = Vm ? Vm[G.NR + os] : E[0] - O[0];
         const float grP = E[1] + O[1], grM = E[1] - O[1];
         const float gtP = E[2] + O[2], gtM = -(E[2] - O[2]);
         const float arrP = (E[3] + O[3]) + (E[4] + O[4]), arrM = -(E[3] - O[3]) + (E[4] - O[4]);

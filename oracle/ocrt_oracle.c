@@ -746,6 +746,21 @@ static int mode_alloc(mode_t_ *md, int n, int L)
     return 0;
 }
 
+/* Tabulated P11 at a scattering-angle cosine, linear in the angle in
+ * degrees, clamped to the end values (rt_solver.c:190-202, rt_ipss.c:131-146). */
+static double aer_p11_table(const ocrt_aerosol *a, double cth)
+{
+    if (cth > 1.0) cth = 1.0; else if (cth < -1.0) cth = -1.0;
+    const double t = acos(cth) * 180.0 / PI;
+    const double *th = a->theta_phase, *P = a->P11_phase;
+    const int n = a->n_ang_phase;
+    if (t <= th[0]) return P[0];
+    if (t >= th[n - 1]) return P[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (th[mid] <= t) lo = mid; else hi = mid; }
+    return P[lo] + (t - th[lo]) / (th[hi] - th[lo]) * (P[hi] - P[lo]);
+}
+
 /* rm: signed ring [2n+1] (index j+n), moments may be NULL (pure Rayleigh). */
 static void mode_build(mode_t_ *md, int m, const double *rm,
                        const ocrt_aerosol *aer)
@@ -793,6 +808,22 @@ static void mode_build(mode_t_ *md, int m, const double *rm,
             }
             TAB(md->pfm, n, j, k) = s_p; TAB(md->gr, n, j, k) = s_r; TAB(md->gt, n, j, k) = s_t;
             TAB(md->arr, n, j, k) = s_rr; TAB(md->art, n, j, k) = s_rt; TAB(md->att, n, j, k) = s_tt;
+        }
+    }
+    if (aer->use_value_kernel && aer->n_ang_phase > 1) {
+        /* value kernel (rt_solver.c:188-235): the I-I table by direct azimuth
+         * integration of the tabulated P11 over 720 midpoints */
+        for (int j = 0; j <= n; ++j) {
+            const double mj = rm[RIDX(n, j)], sj = sqrt(fmax(0.0, 1.0 - mj * mj));
+            for (int k = -n; k <= n; ++k) {
+                const double mk = rm[RIDX(n, k)], sk = sqrt(fmax(0.0, 1.0 - mk * mk));
+                double acc = 0.0;
+                for (int q = 0; q < 720; ++q) {
+                    const double phi = 2.0 * PI * ((double)q + 0.5) / 720.0;
+                    acc += aer_p11_table(aer, mj * mk + sj * sk * cos(phi)) * cos((double)m * phi);
+                }
+                TAB(md->pfm, n, j, k) = acc / 720.0;
+            }
         }
     }
 }
@@ -1273,6 +1304,7 @@ static double ipss_tau_sun(ipss_t *g, const double *r0)
 static double ipss_phase_aer(const ipss_t *g, double ct)
 {
     const ocrt_aerosol *a = g->aer;
+    if (a->use_value_kernel && a->n_ang_phase > 1) return aer_p11_table(a, ct);
     double p0 = 1.0, p1 = ct, s = a->beta[0];
     if (a->L_max >= 1) s += a->beta[1] * p1;
     for (int l = 2; l <= a->L_max; ++l) {

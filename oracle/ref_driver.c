@@ -26,6 +26,8 @@
 #include "rt_raa_convention.h"
 #include "shared/surface.h"
 #include "rt_absorption.h"
+#include "rt_aerosol_runtime.h"
+#include "shared/mie_io.h"
 #include "../include/ocrt_gb300.h"
 
 #define OCRT_PI_ 3.14159265358979323846
@@ -123,7 +125,10 @@ int ocrt_ref_solve_case(const ocrt_case *c, const ocrt_opts *o, const ocrt_aeros
         ai.tau_a = a->tau_a; ai.ssa_a = a->ssa_a; ai.L_max = a->L_max;
         ai.betal_aer = a->beta; ai.gammal_aer = a->gamma;
         ai.alphal_aer = a->alpha; ai.zetal_aer = a->zeta;
-        ai.use_value_kernel = 0;
+        ai.use_value_kernel = a->use_value_kernel;
+        ai.n_ang_phase = a->n_ang_phase;
+        ai.theta_phase = a->theta_phase;
+        ai.P11_phase = a->P11_phase; ai.P12_phase = a->P12_phase; ai.P33_phase = a->P33_phase;
         rc = rt_solve_case_pol_aerosol(&cs, &op, &ai, &r);
     } else {
         rc = rt_solve_case_pol(&cs, &op, &r);
@@ -272,5 +277,45 @@ int ocrt_ref_solve_case_lut(const ocrt_case *c, const ocrt_opts *o, const ocrt_a
     out->rho_I = r.rho_I; out->rho_Q = r.rho_Q; out->rho_U = r.rho_U;
     out->n_orders_used = r.n_orders_used; out->converged = r.converged;
     lut->T_dir_dn = L.T_dir_dn; lut->T_diff_dn_hemi = L.T_diff_dn_hemi;
+    return 0;
+}
+
+/* The reference's .mie pipeline (read_mie_file + rt_aerosol_runtime_prepare
+ * with the CLI's log-linear truncation options, main.c:3646-3670); outputs
+ * copied into the caller's arrays: scal = {tau_a, ssa_a, A, ssa_raw,
+ * aod_target, extinction_ratio, n_ang}, moments [L_max + 1], phase table
+ * [n_ang] (cap entries at most). */
+int ocrt_ref_mie_prepare(const char *path, double wl_nm, double aod_ref, double aod_ref_nm, int L_max,
+                         int use_loglin, int use_value_kernel, double *scal, double *beta, double *gamma,
+                         double *alpha, double *zeta, double *theta, double *p11, double *p12, double *p33,
+                         int cap)
+{
+    mie_data_t mie;
+    memset(&mie, 0, sizeof(mie));
+    if (read_mie_file(path, &mie) != 0) return -1;
+    rt_aerosol_runtime_options_t ro;
+    memset(&ro, 0, sizeof(ro));
+    ro.aer_L_max = L_max;
+    ro.use_loglin_trunc = use_loglin;
+    ro.loglin_mu1 = 0.8; ro.loglin_mu2 = 0.94; ro.loglin_threshold = 0.1;
+    ro.use_value_kernel = use_value_kernel;
+    rt_aerosol_input_t aer;
+    rt_aerosol_runtime_diag_t dg;
+    memset(&dg, 0, sizeof(dg));
+    const int rc = rt_aerosol_runtime_prepare(&mie, wl_nm, aod_ref, aod_ref_nm, &ro, &aer, &dg);
+    mie_data_free(&mie);
+    if (rc) return -2;
+    scal[0] = aer.tau_a; scal[1] = aer.ssa_a; scal[2] = dg.f_fwd; scal[3] = dg.ssa_raw;
+    scal[4] = dg.aod_target; scal[5] = dg.extinction_ratio; scal[6] = aer.n_ang_phase;
+    for (int l = 0; l <= L_max; ++l) {
+        beta[l] = aer.betal_aer[l]; gamma[l] = aer.gammal_aer[l];
+        alpha[l] = aer.alphal_aer[l]; zeta[l] = aer.zetal_aer[l];
+    }
+    const int n = aer.n_ang_phase < cap ? aer.n_ang_phase : cap;
+    for (int i = 0; i < n; ++i) {
+        theta[i] = aer.theta_phase[i]; p11[i] = aer.P11_phase[i];
+        p12[i] = aer.P12_phase[i]; p33[i] = aer.P33_phase[i];
+    }
+    rt_aerosol_runtime_free(&aer);
     return 0;
 }
