@@ -17,13 +17,18 @@
  * --batch FILE solves every row of a CSV (header sza,vza,raa,wavelength and
  * optional wind,aod) in one device pass and prints one line per row.
  *
- * Aerosol: the reference reads FR631 .mie models (--aer NAME), which are not
- * part of this path; an aerosol enters as the synthetic expansion of the
- * moment API (rt_solver.h:94-114): --aod TAU (at the case wavelength),
- * --aer-hg-g G (Henyey-Greenstein beta_l = (2l+1) g^l), --aer-ssa W,
- * --aer-l-max L, with gamma_2 and alpha_2 at 0.3 x the Rayleigh-form values.
- * When an aerosol is on and --n-layers is not given, 400 layers are used
- * (main.c:3342-3345).
+ * Aerosol from a .mie model (main.c:2603-2640, 3279-3345, 3646-3686):
+ * --mie PATH with --aod-555 TAU or --aod-865 TAU (or --aod TAU at
+ * --aod-ref-wavelength NM, default 555) gives the reference's protocol: the
+ * AOD carried to the case wavelength by the model's extinction ratio, the
+ * log10-linear forward-peak truncation, moments to --aer-l-max (default 80),
+ * the value kernel for the intensity phase table, Fourier modes 0..16 when
+ * --m-max is not given.  Without --mie an aerosol enters as the synthetic
+ * expansion of the moment API (rt_solver.h:94-114): --aod TAU (at the case
+ * wavelength), --aer-hg-g G (Henyey-Greenstein beta_l = (2l+1) g^l),
+ * --aer-ssa W, --aer-l-max L, with gamma_2 and alpha_2 at 0.3 x the
+ * Rayleigh-form values.  When an aerosol is on and --n-layers is not given,
+ * 400 layers are used (main.c:3342-3345).
  *
  * Gas absorption is on by default, as in the reference (main.c:1950-1960):
  * the AFGL atmosphere (--atm-profile, default usstd76) and the six
@@ -54,6 +59,7 @@ static int usage(void)
     fprintf(stderr,
             "usage: ocrt --surface black|flat|black_fresnel_ocean [--sza D] [--vza D --raa D] [--wavelength NM]\n"
             "            [--wind-speed MS] [--n-water N] [--pressure HPA | --rayleigh on|off | --tau-r TAU]\n"
+            "            [--mie PATH --aod-555 TAU|--aod-865 TAU|--aod TAU [--aod-ref-wavelength NM]]\n"
             "            [--aod TAU --aer-hg-g G --aer-ssa W --aer-l-max L --aer-h-km H] [--pssa]\n"
             "            [--decouple-sunglint] [--n-layers K] [--m-max M] [--n-mu N] [--sos-max-orders K]\n"
             "            [--sos-tolerance T] [--lut-vza-step D --lut-raa-step D --lut-vza-max D --lut-output F]\n"
@@ -90,7 +96,11 @@ static void hg_moments(double g, int L, moments_t *m)
     if (L >= 2) { m->g[2] = 0.3 * (-A * sqrt(1.5)); m->a[2] = 0.3 * 3.0 * A; }
 }
 
-static void print_single(const ocrt_case *c, const ocrt_result *r, double aod)
+/* the aerosol's AOD as the output line reports it: at the reference
+ * wavelength, that wavelength, at the band, and their ratio */
+typedef struct { double ref, ref_nm, band, ratio; } aod_line_t;
+
+static void print_single(const ocrt_case *c, const ocrt_result *r, aod_line_t a)
 {
     /* rt_io_print_single, non-ocean branch: quantities this path does not
      * produce (the water signal and the upward diffuse view transmittance)
@@ -108,7 +118,7 @@ static void print_single(const ocrt_case *c, const ocrt_result *r, double aod)
            r->T_dir_dn, r->T_diff_dn_hemi, r->T_total_dn_hemi, r->T_diff_dn_dir,
            r->T_dir_up_view, 0.0, 0.0, 0.0, 0,
            r->T_sg_up_dir, r->T_total_up_dir,
-           aod, c->wavelength_nm, aod, aod > 0.0 ? 1.0 : 0.0,
+           a.ref, a.ref_nm, a.band, a.ratio,
            r->tau_R_total, c->sza_deg, c->vza_deg, c->raa_deg, c->wavelength_nm, r->n_orders_used, r->converged);
 }
 
@@ -160,7 +170,11 @@ static int run_batch(const char *path, const ocrt_case *base, const ocrt_opts *o
     const int any_aer = L >= 2;
     const int rc = ocrt_gb_solve_batch(n, cs, o, 0, any_aer ? as : NULL, any_aer ? 1 : 0, res, NULL);
     if (rc) { fprintf(stderr, "error: ocrt_gb_solve_batch rc=%d: %s\n", rc, ocrt_gb_last_error()); return 1; }
-    for (int i = 0; i < n; ++i) print_single(&cs[i], &res[i], any_aer ? as[i].tau_a : 0.0);
+    for (int i = 0; i < n; ++i) {
+        const double ta = any_aer ? as[i].tau_a : 0.0;
+        const aod_line_t al = {ta, cs[i].wavelength_nm, ta, ta > 0.0 ? 1.0 : 0.0};
+        print_single(&cs[i], &res[i], al);
+    }
     free(cs); free(as); free(res);
     return 0;
 }
@@ -170,8 +184,9 @@ int main(int argc, char **argv)
     ocrt_case c; ocrt_case_default(&c);
     ocrt_opts o; ocrt_opts_default(&o);
     int have_surface = 0, have_vza = 0, have_raa = 0, have_nl = 0, have_lut = 0;
-    double aod = 0.0, hg_g = 0.7, ssa = 0.95;
-    int L = 120;
+    double aod = 0.0, hg_g = 0.7, ssa = 0.95, aod_ref_nm = 555.0;
+    int L = 120, have_L = 0, have_m = 0;
+    const char *mie_path = NULL;
     double vstep = 2.5, rstep = 2.5, vmax = 85.0;
     const char *lut_out = NULL, *batch = NULL;
     static const char *const profiles[7] = {"usstd76", "tropical", "mlsumm", "mlwint", "sasumm", "sawint", "userdef"};
@@ -232,14 +247,23 @@ int main(int argc, char **argv)
             else { fprintf(stderr, "error: --rayleigh must be on|off\n"); return 2; }
         }
         else if (!strcmp(a, "--tau-r")) { c.tau_r_input = need_d(argc, argv, &i); o.tau_r_source = OCRT_TAU_R_FROM_INPUT; }
-        else if (!strcmp(a, "--aod") || !strcmp(a, "--aod-band")) aod = need_d(argc, argv, &i);
+        else if (!strcmp(a, "--aod")) aod = need_d(argc, argv, &i);
+        else if (!strcmp(a, "--aod-555")) { aod = need_d(argc, argv, &i); aod_ref_nm = 555.0; }
+        else if (!strcmp(a, "--aod-865")) { aod = need_d(argc, argv, &i); aod_ref_nm = 865.0; }
+        else if (!strcmp(a, "--aod-ref-wavelength")) aod_ref_nm = need_d(argc, argv, &i);
+        else if (!strcmp(a, "--aod-band")) {
+            fprintf(stderr, "error: --aod-band was removed because band-specific AOD breaks spectral consistency; "
+                            "use --aod-555 or --aod-865\n");
+            return 2;
+        }
+        else if (!strcmp(a, "--mie")) mie_path = need_s(argc, argv, &i);
         else if (!strcmp(a, "--aer-hg-g")) hg_g = need_d(argc, argv, &i);
         else if (!strcmp(a, "--aer-ssa")) ssa = need_d(argc, argv, &i);
-        else if (!strcmp(a, "--aer-l-max")) L = (int)need_d(argc, argv, &i);
+        else if (!strcmp(a, "--aer-l-max")) { L = (int)need_d(argc, argv, &i); have_L = 1; }
         else if (!strcmp(a, "--aer-h-km")) o.aer_h_km = need_d(argc, argv, &i);
         else if (!strcmp(a, "--aer")) {
-            fprintf(stderr, "error: --aer %s: FR631 .mie aerosol models are not part of this solve path; "
-                            "use --aod with --aer-hg-g/--aer-ssa/--aer-l-max\n", need_s(argc, argv, &i));
+            fprintf(stderr, "error: --aer %s: name the aerosol model file with --mie PATH (.mie)\n",
+                    need_s(argc, argv, &i));
             return 2;
         }
         else if (!strcmp(a, "--n-mu")) {
@@ -251,7 +275,7 @@ int main(int argc, char **argv)
             }
         }
         else if (!strcmp(a, "--n-layers")) { o.n_layers = (int)need_d(argc, argv, &i); have_nl = 1; }
-        else if (!strcmp(a, "--m-max")) o.fourier_m_max = (int)need_d(argc, argv, &i);
+        else if (!strcmp(a, "--m-max")) { o.fourier_m_max = (int)need_d(argc, argv, &i); have_m = 1; }
         else if (!strcmp(a, "--sos-max-orders") || !strcmp(a, "--max-orders")) {
             o.max_orders = (int)need_d(argc, argv, &i);
             if (o.max_orders != 20 && !advanced_on()) {
@@ -307,8 +331,15 @@ int main(int argc, char **argv)
         fprintf(stderr, "error: conflicting mode flags: single geometry (--vza/--raa) vs LUT grid. Pick one.\n");
         return 2;
     }
+    if (mie_path && !(aod > 0.0)) {
+        fprintf(stderr, "error: aerosol options require --aod-555/--aod-865 > 0 "
+                        "(aerosol is disabled at the default --aod-555 0)\n");
+        return 2;
+    }
     const int aer_on = aod > 0.0;
     if (aer_on && !have_nl) o.n_layers = 400;
+    if (mie_path && !have_m) o.fourier_m_max = 16;      /* main.c:3286-3293 */
+    if (mie_path && !have_L) L = 80;                   /* main.c:3297-3302 */
     if (!aer_on && have_nl && o.n_layers != 40 && !advanced_on()) {
         fprintf(stderr, "error: --n-layers %d differs from the validated default 40 (requires OCRT_ADVANCED=1)\n",
                 o.n_layers);
@@ -339,18 +370,36 @@ int main(int argc, char **argv)
     moments_t mom = {0};
     ocrt_aerosol aer;
     memset(&aer, 0, sizeof aer);
-    if (aer_on) {
+    aod_line_t al = {aod, c.wavelength_nm, aod, aer_on ? 1.0 : 0.0};
+    ocrt_mie *model = NULL;
+    ocrt_mie_aerosol *prep = NULL;
+    if (aer_on && mie_path) {
+        ocrt_mie_opts mo;
+        ocrt_mie_opts_default(&mo);
+        mo.L_max = L;
+        ocrt_mie_diag md;
+        if (ocrt_gb_mie_read(mie_path, &model) ||
+            ocrt_gb_mie_prepare(model, c.wavelength_nm, aod, aod_ref_nm, &mo, &prep, &aer, &md)) {
+            fprintf(stderr, "error: %s\n", ocrt_gb_last_error());
+            return 1;
+        }
+        al.ref = aod; al.ref_nm = aod_ref_nm; al.band = md.aod_target; al.ratio = md.extinction_ratio;
+    } else if (aer_on) {
         if (L < 2) { fprintf(stderr, "error: --aer-l-max must be >= 2\n"); return 2; }
         hg_moments(hg_g, L, &mom);
         aer.tau_a = aod; aer.ssa_a = ssa; aer.L_max = L;
         aer.beta = mom.b; aer.gamma = mom.g; aer.alpha = mom.a; aer.zeta = mom.z;
+    }
+    if (batch && mie_path) {
+        fprintf(stderr, "error: --batch takes the synthetic aerosol expansion (--aod with --aer-hg-g), not --mie\n");
+        return 2;
     }
     if (batch) return run_batch(batch, &c, &o, aer_on ? &aer : NULL, hg_g, ssa, aer_on ? L : 0);
     ocrt_result r;
     if (single) {
         const int rc = ocrt_gb_solve_case(&c, &o, aer_on ? &aer : NULL, &r, NULL);
         if (rc) { fprintf(stderr, "error: solve rc=%d: %s\n", rc, ocrt_gb_last_error()); return 1; }
-        print_single(&c, &r, aod);
+        print_single(&c, &r, al);
         return 0;
     }
     /* LUT grid mode (main.c:3790-3884); the base solve uses vza = raa = 0 */

@@ -18,10 +18,14 @@ its own water IOPs passes water_iop=(a_total, b_water).  gas_on (default True, a
 US76 atmosphere and the six cross-section tables once (ocrt_solve.py:41-45)
 from $OCRT_GB_INPUTS/afgl_atm and $OCRT_GB_INPUTS/xsec, or inputs/afgl_atm and
 inputs/xsec under the working directory, and folds the per-layer absorption
-into every solve.  The reference's aerosol comes from FR631 `.mie`
-models named by aer_name; here aer_name is a synthetic expansion spec
-"HG:g,ssa[,L]" (Henyey-Greenstein beta_l = (2l+1) g^l with the Rayleigh-form
-gamma_2/alpha_2 x 0.3) and aod865 is the AOD at the row's wavelength.
+into every solve.  The aerosol, as in the reference (ocrt_solve.py:48-53,
+143-147), is the .mie model named by aer_name (a path, or a name resolved as
+<name>.mie under $OCRT_GB_MIE_DIR or data/) with aod865 its AOD at 865 nm,
+prepared at the row's wavelength by the library (ocrt_gb_mie_prepare: the
+log10-linear truncation, moments to L = 80, the value kernel); aer_name may
+instead be a synthetic expansion spec "HG:g,ssa[,L]" (Henyey-Greenstein
+beta_l = (2l+1) g^l with the Rayleigh-form gamma_2/alpha_2 x 0.3), where
+aod865 is the AOD at the row's wavelength.
 """
 import argparse
 import csv
@@ -53,10 +57,24 @@ def _absorption():
     return _STATE["ab"]
 
 
-def _hg(spec, aod):
+def _mie_model(name):
+    """The .mie model of aer_name, read once per process."""
+    from . import MieModel
+    key = ("mie", name)
+    if key not in _STATE:
+        path = name
+        if not os.path.exists(path):
+            fn = name if name.endswith(".mie") else name + ".mie"
+            path = os.path.join(os.environ.get("OCRT_GB_MIE_DIR") or "data", fn)
+        _STATE[key] = MieModel(path)
+    return _STATE[key]
+
+
+def _hg(spec, aod, wl_nm=None, value_kernel=True):
     if not isinstance(spec, str) or not spec.upper().startswith("HG:"):
-        raise NotImplementedError("aerosol models from FR631 .mie files are not on this path; "
-                                  "use aer_name='HG:g,ssa[,L]'")
+        if wl_nm is None:
+            raise ValueError("a .mie aerosol needs the wavelength")
+        return _mie_model(spec).prepare(wl_nm, aod, 865.0, L_max=80, value_kernel=value_kernel)
     parts = [float(x) for x in spec[3:].split(",")]
     g, ssa = parts[0], parts[1]
     L = int(parts[2]) if len(parts) > 2 else 80
@@ -83,7 +101,7 @@ def _rows_to_cases(rows, which, fourier_m_max, nt_atm, pressure_hpa, max_it=100,
             out.append(("R3", r, A.default_case(**base),
                         A.default_opts(n_mu=24, n_layers=nt_atm, fourier_m_max=fourier_m_max, max_orders=max_it,
                                        gas=g),
-                        _hg(r["aer_name"], r["aod865"])))
+                        _hg(r["aer_name"], r["aod865"], r["wl_nm"])))
     return out
 
 
@@ -113,7 +131,9 @@ def _solve_r1(rows, outs, fourier_m_max, nt_atm, pressure_hpa, gas, n_mu_water, 
                                     wind_speed=r["wind"], surface="ocean", pressure_hpa=pressure_hpa))
         opts.append(A.default_opts(n_layers=nt_atm, fourier_m_max=fourier_m_max, max_orders=100, gas=g))
         oceans.append(_water_column(r, n_mu_water, fourier_m_max, max_it_water))
-        aers.append(_hg(r["aer_name"], r["aod865"]) if r["aod865"] > 0.0 else _NO_AEROSOL)
+        # the coupled solve takes the moment kernel (the value kernel is not on that path)
+        aers.append(_hg(r["aer_name"], r["aod865"], r["wl_nm"], value_kernel=False) if r["aod865"] > 0.0
+                    else _NO_AEROSOL)
     res = solve_batch_ocean(cases, opts, oceans, aers)
     for o, x in zip(outs, res):
         o["rho_TOA_I"], o["rho_TOA_Q"], o["rho_TOA_U"] = x["rho_I"], x["rho_Q"], x["rho_U"]

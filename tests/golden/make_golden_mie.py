@@ -8,9 +8,12 @@ main.c:3646-3670) give the effective AOD and SSA, the truncation coefficient,
 the vector moments and the normalised phase table (every 20th angle kept);
 for each solve, rt_solve_case_pol_aerosol runs the prepared aerosol with the
 value kernel (the CLI's aerosol default, main.c:3338-3341) and with the
-moment kernel.  Both go through oracle/ref_driver.c in oracle/_ref.
+moment kernel.  Both go through oracle/ref_driver.c in oracle/_ref.  The
+reference CLI itself (oracle/_ref/ocrt, gases off) runs two whole .mie
+commands whose output lines are kept.
 
-    OCRT_REF_ROOT=<reference checkout> make -C oracle all && python tests/golden/make_golden_mie.py
+    OCRT_REF_ROOT=<reference checkout> make -C oracle all && \\
+        OCRT_REF_ROOT=<reference checkout> python tests/golden/make_golden_mie.py
 """
 import ctypes as C
 import json
@@ -55,6 +58,31 @@ SOLVES = [
      "opts": {"n_mu": 16, "n_layers": 40, "fourier_m_max": 10, "max_orders": 200},
      "note": "near-backscatter geometry, where the moment and value kernels differ most"},
 ]
+
+
+# the reference CLI on a .mie model (main.c's aerosol protocol); gases off
+CLI_RUNS = [
+    {"name": "cli_peaked_490", "args": ["--mie", "tests/golden/mie/synth_peaked.mie", "--aod-555", "0.2",
+                                        "--surface", "black_fresnel_ocean", "--wind-speed", "5", "--sza", "40",
+                                        "--vza", "30", "--raa", "60", "--wavelength", "490"]},
+    {"name": "cli_hg_865_pssa", "args": ["--mie", "tests/golden/mie/synth_hg.mie", "--aod-865", "0.08",
+                                         "--surface", "black", "--sza", "55", "--vza", "10", "--raa", "170",
+                                         "--wavelength", "865", "--pssa"]},
+]
+GAS_OFF = sum([[f"--gas-column-{g}", "0"] for g in ("h2o", "o3", "no2", "o2", "co2", "ch4")], [])
+
+
+def ref_cli(spec):
+    import subprocess
+    wd = os.path.join(os.environ.get("OCRT_REF_ROOT", ""), "code", "OCRT_C")
+    args = [os.path.join(ROOT, "oracle", "_ref", "ocrt")] + \
+        [os.path.join(ROOT, a) if a.startswith("tests/") else a for a in spec["args"]] + GAS_OFF
+    r = subprocess.run(args, capture_output=True, text=True, cwd=wd, timeout=600)
+    assert r.returncode == 0, r.stderr
+    fields = r.stdout.split()
+    kv = {f.split("=")[0]: float(f.split("=")[1]) for f in fields[3:] if "=" in f}
+    kv["rho"] = [float(x) for x in fields[:3]]
+    return kv
 
 
 def ref_prepare(lib, spec):
@@ -109,9 +137,15 @@ def main():
             out[kernel] = res
         rows.append({**spec, "reference": out})
         print(spec["name"], "value", out["value"]["rho_I"], "moment", out["moment"]["rho_I"])
+    cli = []
+    for spec in CLI_RUNS:
+        kv = ref_cli(spec)
+        cli.append({**spec, "reference": kv})
+        print(spec["name"], kv["rho"])
     doc = {"source": "reference read_mie_file + rt_aerosol_runtime_prepare + rt_solve_case_pol_aerosol, "
-                     "built from code/OCRT_C/src by oracle/Makefile, driven by oracle/ref_driver.c",
-           "models": "tests/golden/mie (make_synthetic_mie.py)", "prepared": prepared, "solves": rows}
+                     "built from code/OCRT_C/src by oracle/Makefile, driven by oracle/ref_driver.c; "
+                     "cli: the reference CLI (oracle/_ref/ocrt) with every gas column at 0",
+           "models": "tests/golden/mie (make_synthetic_mie.py)", "prepared": prepared, "solves": rows, "cli": cli}
     with open(OUT, "w") as fh:
         json.dump(doc, fh, indent=1)
     print("wrote", OUT)

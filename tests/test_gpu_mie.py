@@ -75,3 +75,46 @@ def test_gpu_value_kernel_unsupported_paths(gpu):
                                               C.byref(A.default_opts(n_mu=16, n_layers=30)), C.byref(a.struct),
                                               C.byref(r), None)
     assert rc == A.OCRT_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("spec", DOC["cli"], ids=[s["name"] for s in DOC["cli"]])
+def test_cli_mie_matches_reference_cli(spec):
+    """The ocrt command on a .mie model (--mie, --aod-555 / --aod-865, the
+    reference's aerosol protocol, gases off) against the reference CLI's line."""
+    import subprocess
+    root = os.path.dirname(HERE)
+    binp = os.path.join(root, "ocrt_gb300", "bin", "ocrt")
+    if not os.path.exists(binp):
+        pytest.skip("ocrt CLI not built")
+    gas_off = sum([[f"--gas-column-{g}", "0"] for g in ("h2o", "o3", "no2", "o2", "co2", "ch4")], [])
+    args = [os.path.join(root, a) if a.startswith("tests/") else a for a in spec["args"]]
+    env = dict(os.environ, OCRT_GB_INPUTS=os.path.join(HERE, "golden", "gas_data"))
+    env.pop("OCRT_ADVANCED", None)
+    r = subprocess.run([binp, *args, *gas_off], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr
+    fields = r.stdout.split()
+    rho = [float(x) for x in fields[:3]]
+    kv = {f.split("=")[0]: float(f.split("=")[1]) for f in fields[3:] if "=" in f}
+    ref = spec["reference"]
+    assert_parity({"rho_I": rho[0], "rho_Q": rho[1], "rho_U": rho[2]},
+                  {"rho_I": ref["rho"][0], "rho_Q": ref["rho"][1], "rho_U": ref["rho"][2]}, spec["name"])
+    for k in ("AOD_ref", "AOD_ref_nm", "AOD_band", "AOD_ext_ratio"):
+        assert kv[k] == pytest.approx(ref[k], rel=1e-6), k
+    assert kv["T_dir_dn"] == pytest.approx(ref["T_dir_dn"], rel=1e-6)
+
+
+def test_ocrt_solve_with_mie_model(gpu):
+    """ocrt_solve's aer_name as a .mie model: R3 with aod865 equals a direct
+    solve of the aerosol the library prepares (AOD given at 865 nm)."""
+    from ocrt_gb300.ocrt_solve import solve_reflectances
+    path = os.path.join(MIE, "synth_peaked.mie")
+    out = solve_reflectances(490.0, 35.0, 25.0, 70.0, 4.0, 0, 0, 0, 0.12, path, which=("R3",), gas_on=False)
+    a = gpu.MieModel(path).prepare(490.0, 0.12, 865.0, L_max=80)
+    c = A.default_case(surface="black_fresnel_ocean", sza_deg=35.0, vza_deg=25.0, raa_deg=70.0, wavelength_nm=490.0,
+                       wind_speed=4.0, decouple_sunglint=1)
+    row = out[0] if isinstance(out, list) else out
+    assert a.diag["aod_ref_nm"] == 865.0 and a.struct.use_value_kernel == 1
+    o = A.default_opts(n_mu=24, n_layers=400, fourier_m_max=16, max_orders=100)
+    direct = gpu.solve_case(c, o, a)
+    assert row["rho_RA_black_I"] == pytest.approx(direct["rho_I"], rel=1e-5)
+    assert row["rho_RA_black_Q"] == pytest.approx(direct["rho_Q"], abs=1e-6)

@@ -17,7 +17,8 @@ def test_unavailable_parts_raise():
     from ocrt_gb300.ocrt_solve import solve_reflectances
     with pytest.raises(NotImplementedError, match="constituent"):
         solve_reflectances(555, 30, 30, 90, 3, 1.2, 3.5, 0.04, 0.1, "HG:0.7,0.95", which=("R1",), gas_on=False)
-    with pytest.raises(NotImplementedError, match=".mie"):
+    import ocrt_gb300 as og
+    with pytest.raises(og.OcrtError, match="cannot open"):      # data/C50.mie: the FR631 tables are not here
         solve_reflectances(555, 30, 30, 90, 3, 0, 0, 0, 0.1, "C50", which=("R3",), gas_on=False)
 
 
