@@ -231,6 +231,13 @@ int scan_tma_blocks(int kind, const Geom &G)
     return nb;
 }
 
+// OCRT_GB_ADJ_SCAN=column keeps the adjoint's per-thread copy-ring scan.
+bool adj_scan_column()
+{
+    const char *e = getenv("OCRT_GB_ADJ_SCAN");
+    return e && strcmp(e, "column") == 0;
+}
+
 // OCRT_GB_PRIMARY=column keeps the one-column-per-thread order-1 kernel.
 bool primary_column()
 {
@@ -309,6 +316,8 @@ struct Group {
     long long vk_stride = 0;
     int wave_pix = 0;
     bool smap_ok = false;
+    AdjScanMaps amap;                     // k_adj_scan_tma tensor maps over the adjoint buffers
+    bool amap_ok = false;
     float *Bp = nullptr, *Br = nullptr, *Bt = nullptr, *cs = nullptr, *frs = nullptr;
     double *lam = nullptr;
     float *Eatt = nullptr, *lvf = nullptr;
@@ -631,6 +640,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         for (int i = 0; i < 3 && g.smap_ok; ++i)
             g.smap_ok = scan_tma_maps(G, chs[i], g.J, g.Tot, g.wave_fld, g.Cq, g.ncoef / G.NR, &g.smap[i]) == 0;
     }
+    if (g.smap_ok && g.ncot > 0 && g.AF && !adj_scan_column())
+        g.amap_ok = adj_scan_tma_maps(G, g.AF, g.ATot, g.wave_fld * g.ncot, g.Cq, g.ncoef / G.NR, &g.amap) == 0;
     g.use_tc = tc_supported(G) && !force_simt();
     if (g.use_tc && (rc = alloc(g.opt, 2 * g.wave_ops))) return rc;
     if (g.use_tc && (rc = alloc(g.molV, (size_t)3 * 32 * G.CIN))) return rc;
@@ -778,8 +789,12 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     const int surf_threads = ((3 * G.N + 31) / 32) * 32;
     if (!capture) w.adj_stop = INT_MAX;
     for (int j = 1; j <= g.max_orders; ++j) {
-        LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB), scan_threads,
-                                              adj_scan_smem_bytes(scan_threads), st>>>(B, A, G, w.t0, j));
+        if (g.amap_ok)
+            LAUNCH(plan, KC_ADJ_SCAN, adj_scan_tma_launch(nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB), st, B, A, G, w.t0, j,
+                                                          g.amap));
+        else
+            LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB), scan_threads,
+                                                  adj_scan_smem_bytes(scan_threads), st>>>(B, A, G, w.t0, j));
         if (capture) {
             if (j == w.adj_stop) break;
         } else if ((j - 1) % 4 == 0 || j == g.max_orders) {

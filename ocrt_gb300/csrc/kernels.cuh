@@ -255,6 +255,19 @@ size_t scan_tma_smem_bytes(const Geom &G, int CH, int NS);
 int scan_tma_maps(const Geom &G, int CH, float *J, float *Tot, size_t fld_floats, const float *Cq, size_t layers,
                   ScanMaps *M);
 bool scan_tma_supported(const Geom &G);
+// the adjoint's transposed scan fed the same way (scan_tma.cu): maps over the
+// adjoint field and total buffers and the weight rows in boxes of 5 levels
+struct AdjScanMaps {
+    CUtensorMap ag, tg;    // Gauss columns of the adjoint field / adjoint total
+    CUtensorMap az, tz;    // zero-weight columns
+    CUtensorMap cq;        // transport weights, 5 layers per box
+};
+struct AdjBufs;
+int adj_scan_tma_maps(const Geom &G, float *AF, float *ATot, size_t adj_floats, const float *Cq, size_t layers,
+                      AdjScanMaps *M);
+size_t adj_scan_tma_smem_bytes(const Geom &G, int CH, int NS);
+cudaError_t adj_scan_tma_launch(int grid, cudaStream_t st, const BatchBufs &B, const AdjBufs &A, const Geom &G,
+                                int t0, int j, const AdjScanMaps &M);
 __global__ void k_mol_lowrank(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int ltiles,
                               const float *Bp, const float *Br, const float *Bt, int L);
 inline size_t mol_smem_bytes(const Geom &G) { return sizeof(float) * (4 * G.N + G.COUT * 24 + 32 * G.CIN + 32 * 25); }

@@ -297,6 +297,241 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
     }
 }
 
+// ===========================================================================
+// The adjoint's transposed transport (k_adj_scan in adjoint.cu: the same
+// recurrences run the other way, nu = a + T nu', muJ = Ca nu + Cb nu', the
+// adjoint total and its convergence norms) fed the same way.  One block per
+// (task, group of up to ADJ_RB cotangent rows); per ring stage and direction
+// the adjoint field and the adjoint total boxes of every active row and the
+// weight rows of the chunk's CH levels plus one (the transposed recurrence
+// reads T and Cb of one layer and Ca of the next).  Per column and row the
+// arithmetic is k_adj_scan's, in the same order.
+// ===========================================================================
+namespace {
+
+struct AstLayout {
+    uint32_t g, z, cf, dir, stage;   // one row's Gauss box, zero-weight box; weights; per direction
+};
+
+__host__ __device__ inline AstLayout ast_layout(const Geom &G, int CH)
+{
+    AstLayout L;
+    L.g = al128((uint32_t)(CH * 3 * G.N * 4));
+    L.z = al128((uint32_t)(CH * scan_tma_zw(G) * 4));
+    L.cf = al128((uint32_t)((CH + 1) * scan_tma_cw(G) * 4));
+    // per active row: field Gauss, total Gauss, field zero-weight, total zero-weight
+    L.dir = ADJ_RB * (2 * L.g + 2 * L.z) + L.cf;
+    L.stage = 2 * L.dir;
+    return L;
+}
+
+} // namespace
+
+size_t adj_scan_tma_smem_bytes(const Geom &G, int CH, int NS)
+{
+    return (size_t)ast_layout(G, CH).stage * NS + 128 + 256;
+}
+
+template <int CH, int NS>
+__global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A, Geom G, int t0, int j,
+                                                         const __grid_constant__ AdjScanMaps M)
+{
+    extern __shared__ unsigned char ast_raw[];
+    __shared__ float2 redf2[32];
+    __shared__ int abort_raw;
+    volatile int &abort_s = abort_raw;
+    unsigned char *base = (unsigned char *)(((uintptr_t)ast_raw + 127) & ~(uintptr_t)127);
+    const AstLayout Ly = ast_layout(G, CH);
+    uint64_t *full = (uint64_t *)(base + (size_t)Ly.stage * NS), *empty = full + NS;
+    const int tid = threadIdx.x, lane = tid & 31, nthr = blockDim.x;
+    const int ncw = nthr / 32 - 1;
+    const bool producer = tid == nthr - 32;
+    const int N = G.N, NR = G.NR, ZW = scan_tma_zw(G), CW = scan_tma_cw(G);
+    const int nrg = (A.ncot + ADJ_RB - 1) / ADJ_RB;
+    const int tl = blockIdx.x / nrg, r0 = (blockIdx.x - tl * nrg) * ADJ_RB, tg = t0 + tl;
+    const int nr = min(ADJ_RB, A.ncot - r0);
+    bool act[ADJ_RB];
+    int nact = 0;
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) {
+        act[q] = q < nr && A.st[tl * A.ncot + r0 + q].active;
+        nact += act[q] ? 1 : 0;
+    }
+    if (nact == 0) return;                                // block-uniform
+    const TaskDev tk = B.tasks[tg];
+    const PixDev &d = B.px[tk.pix];
+    const int nt = d.nt, nq = (nt + CH) / CH;
+    if (tid == 0) {
+        for (int i = 0; i < NS; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], ncw); }
+        abort_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    // first level row of each active row's adjoint field: (fld_off ncot + r K LDC) / LDC
+    int rrow[ADJ_RB];
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q)
+        rrow[q] = (int)((tk.fld_off * A.ncot) / G.LDC) + (r0 + (q < nr ? q : 0)) * tk.K;
+    const int lay0 = (int)(d.coef_off / NR);
+    const uint32_t TX = 2u * (uint32_t)CH * 4u * (uint32_t)nact * (uint32_t)(2 * 3 * N + 2 * ZW) +
+                        2u * (uint32_t)(CH + 1) * 4u * (uint32_t)CW;
+    uint32_t issued = 0;
+    auto issue = [&](int q) -> bool {
+        const uint32_t pos = issued, sl = pos % NS;
+        if (pos >= (uint32_t)NS && !mbar_wait(&empty[sl], ((pos / NS) - 1) & 1)) return false;
+        unsigned char *stg = base + (size_t)sl * Ly.stage;
+        mbar_expect_tx(&full[sl], TX);
+#pragma unroll
+        for (int dd = 0; dd < 2; ++dd) {
+            unsigned char *db = stg + dd * Ly.dir;
+            // direction 0 (upward columns) walks k = 0 .. nt, direction 1 k = nt .. 0
+            const int r = dd == 0 ? q * CH : nt - q * CH - CH + 1;       // first level of the box
+            const int ly = dd == 0 ? q * CH - 1 : nt - q * CH - CH;      // first layer of the weight box
+            int slot = 0;
+#pragma unroll
+            for (int rq = 0; rq < ADJ_RB; ++rq) {
+                if (!act[rq]) continue;
+                unsigned char *rb = db + (size_t)slot * (2 * Ly.g + 2 * Ly.z);
+                tma4(rb, &M.ag, 0, dd, 0, rrow[rq] + r, &full[sl]);
+                tma4(rb + Ly.g, &M.tg, 0, dd, 0, rrow[rq] + r, &full[sl]);
+                tma2(rb + 2 * Ly.g, &M.az, 6 * N, rrow[rq] + r, &full[sl]);
+                tma2(rb + 2 * Ly.g + Ly.z, &M.tz, 6 * N, rrow[rq] + r, &full[sl]);
+                ++slot;
+            }
+            tma2(db + ADJ_RB * (2 * Ly.g + 2 * Ly.z), &M.cq, 0, lay0 + ly, &full[sl]);
+        }
+        issued = pos + 1;
+        return true;
+    };
+    if (producer) {
+        for (int q = 0; q < (nq < NS ? nq : NS); ++q)
+            if (!issue(q)) { abort_s = 1; break; }
+    }
+    // column of this thread
+    const int c = tid;
+    int s = 0, h = 0, g = 0;
+    const bool col = c < G.COUT;
+    if (col) decode_col(G, c, s, h, g);
+    const bool valid = col && g < d.n_ring;
+    const bool gauss = g < N;
+    const uint32_t voff = gauss ? (uint32_t)(s * N + g) * 4u : (uint32_t)(c - 6 * N) * 4u;
+    const uint32_t vrow = gauss ? (uint32_t)(3 * N) * 4u : (uint32_t)ZW * 4u;
+    const uint32_t cofs = (uint32_t)(((g >> 2) * 12 + (g & 3)) * 4), crow = (uint32_t)CW * 4u;
+    float *a[ADJ_RB], *At[ADJ_RB], *mj[ADJ_RB];
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) {
+        const size_t off = (size_t)tk.fld_off * A.ncot + (size_t)(r0 + (q < nr ? q : 0)) * tk.K * G.LDC;
+        a[q] = A.AF + off; At[q] = A.ATot + off; mj[q] = A.AJ + off;
+    }
+    float mi[ADJ_RB], mt[ADJ_RB], nup[ADJ_RB];
+#pragma unroll
+    for (int q = 0; q < ADJ_RB; ++q) { mi[q] = 0.f; mt[q] = 0.f; nup[q] = 0.f; }
+    if (producer) {
+        for (int q = NS; q < nq && !abort_s; ++q)
+            if (!issue(q)) { abort_s = 1; break; }
+    } else if (tid < ncw * 32) {
+        // the view columns are outputs only: the transposed source never
+        // writes them, so they are cleared here once read
+        const bool clear = c >= G.CIN;
+        for (int q = 0; q < nq; ++q) {
+            const uint32_t pos = (uint32_t)q, sl = pos % NS;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[sl], (pos / NS) & 1));
+            if (!ok) { abort_s = 1; break; }
+            const unsigned char *db = base + (size_t)sl * Ly.stage + h * Ly.dir;
+            const unsigned char *vc = db + ADJ_RB * (2 * Ly.g + 2 * Ly.z) + cofs;
+            if (valid) {
+                for (int jj = 0; jj < CH; ++jj) {
+                    const int step = q * CH + jj;
+                    if (step > nt) break;
+                    const int k = h == 0 ? step : nt - step;
+                    const int rbx = h == 0 ? jj : CH - 1 - jj;                 // box row of level k
+                    // weight rows: T, Cb of layer kt and Ca of layer ka
+                    const int kt = h == 0 ? k - 1 : k, ka = h == 0 ? k : k - 1;
+                    const int rt = h == 0 ? jj : CH - jj, ra = h == 0 ? jj + 1 : CH - jj - 1;
+                    const bool ht = kt >= 0 && kt < nt, ha = ka >= 0 && ka < nt;
+                    const float tv = ht ? *(const float *)(vc + rt * crow) : 0.f;
+                    const float cb = ht ? *(const float *)(vc + rt * crow + 32) : 0.f;
+                    const float ca = ha ? *(const float *)(vc + ra * crow + 16) : 0.f;
+                    const bool has_a = h == 0 || k > 0;
+                    const size_t o = (size_t)k * G.LDC + c;
+                    int slot = 0;
+#pragma unroll
+                    for (int rq = 0; rq < ADJ_RB; ++rq) {
+                        if (!act[rq]) continue;
+                        const unsigned char *rb = db + (size_t)slot * (2 * Ly.g + 2 * Ly.z);
+                        ++slot;
+                        const unsigned char *va = rb + (gauss ? 0 : 2 * Ly.g) + voff;
+                        const unsigned char *vt = rb + (gauss ? Ly.g : 2 * Ly.g + Ly.z) + voff;
+                        const float av = has_a ? *(const float *)(va + rbx * vrow) : 0.f;
+                        if (has_a) {
+                            const float t = *(const float *)(vt + rbx * vrow) + av;
+                            At[rq][o] = t;
+                            if (clear) a[rq][o] = 0.f;
+                            mi[rq] = fmaxf(mi[rq], fabsf(av));
+                            mt[rq] = fmaxf(mt[rq], fabsf(t));
+                        }
+                        const float nu = av + tv * nup[rq];
+                        mj[rq][o] = ca * nu + cb * nup[rq];
+                        nup[rq] = nu;
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[sl]);
+        }
+        if (valid && h == 0 && d.surf_on)
+#pragma unroll
+            for (int rq = 0; rq < ADJ_RB; ++rq)
+                if (act[rq]) A.bc[(size_t)(tl * A.ncot + r0 + rq) * NR * 3 + g * 3 + s] = nup[rq];
+    }
+    __syncthreads();
+    if (abort_s) {
+        if (tid == 0) atomicExch(B.err, OCRT_ERR_DEVICE);
+        if (producer)
+            for (uint32_t p = issued > (uint32_t)NS ? issued - NS : 0; p < issued; ++p)
+                (void)mbar_wait(&full[p % NS], (p / NS) & 1);
+        return;
+    }
+#pragma unroll
+    for (int rq = 0; rq < ADJ_RB; ++rq) {
+        if (!act[rq]) continue;                    // block-uniform
+        const float2 mm = stm_maxf2(mi[rq], mt[rq], redf2);
+        if (threadIdx.x == 0) {
+            const int ta = tl * A.ncot + r0 + rq;
+            TaskState ns = A.st[ta];
+            ns.orders = j;
+            ns.resid = mm.y > 0.f ? (double)(mm.x / mm.y) : 0.0;
+            if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
+            else if (j >= d.max_orders) ns.active = 0;
+            A.st[ta] = ns;
+            if (ns.active) atomicAdd(&A.acnt[j], 1);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t adj_scan_tma_launch(int grid, cudaStream_t st, const BatchBufs &B, const AdjBufs &A, const Geom &G,
+                                int t0, int j, const AdjScanMaps &M)
+{
+    const int th = scan_tma_threads(G);
+    k_adj_scan_tma<4, 4><<<grid, th, adj_scan_tma_smem_bytes(G, 4, 4), st>>>(B, A, G, t0, j, M);
+    return cudaGetLastError();
+}
+
+int adj_scan_tma_maps(const Geom &G, float *AF, float *ATot, size_t adj_floats, const float *Cq, size_t layers,
+                      AdjScanMaps *M)
+{
+    ScanMaps f, t;
+    // the field maps of the forward scan over the adjoint buffers (4-level chunks)
+    if (scan_tma_maps(G, 4, AF, ATot, adj_floats, Cq, layers, &f)) return -1;
+    M->ag = f.jg; M->tg = f.tg; M->az = f.jz; M->tz = f.tz;
+    // weight rows: a box one row taller than the chunk
+    if (scan_tma_maps(G, 5, AF, ATot, adj_floats, Cq, layers, &t)) return -1;
+    M->cq = t.cq;
+    return 0;
+}
+
 // ---- host: launch, function handles ----
 const void *scan_tma_fn(int ch, int ns)
 {
@@ -328,7 +563,7 @@ cudaError_t scan_tma_init()
             cudaFuncSetAttribute(scan_tma_fn(x[0], x[1]), cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return cudaFuncSetAttribute(k_adj_scan_tma<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 // ---- host: tensor maps over the wave buffers ----

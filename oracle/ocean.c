@@ -544,6 +544,7 @@ static int water_solve(water_t *W)
     if (!(ext > 0.0)) return -1;
     const double om_w = oc->b_water / ext, om_p = bp / ext;
     ocrt_aerosol par_s, *par = NULL;
+    memset(&par_s, 0, sizeof(par_s));      /* moment path: no value-kernel table */
     if (bp > 0.0 && oc->beta) {
         par_s.tau_a = 0.0; par_s.ssa_a = 1.0; par_s.L_max = oc->L_particle;
         par_s.beta = oc->beta; par_s.gamma = oc->gamma; par_s.alpha = oc->alpha; par_s.zeta = oc->zeta;

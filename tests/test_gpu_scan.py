@@ -94,3 +94,29 @@ def test_primary4_equals_column_primary(gpu, monkeypatch, N):
     col = gpu.solve_batch(cases, opts, aers)
     for k in ("rho_I", "rho_Q", "rho_U", "T_diff_dn_hemi", "order_modes"):
         np.testing.assert_allclose(quad[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
+
+
+@pytest.mark.parametrize("N", [8, 32])
+def test_adjoint_scan_tma_equals_column_scan(gpu, monkeypatch, N):
+    """The adjoint's transposed scan fed by tensor-map copies against its
+    per-thread copy-ring form: the same recurrences in the same order, so the
+    gradients agree bit for bit (3 cotangent rows, mixed geometries, two
+    surfaces, uneven layers)."""
+    from ocrt_gb300 import _abi as A
+    from synthetic import hg_aerosol_moments
+    rng = np.random.default_rng(21)
+    cs, aers = [], []
+    for i in range(4):
+        cs.append(A.default_case(surface=["black_fresnel_ocean", "black"][i % 2], sza_deg=rng.uniform(10, 70),
+                                 vza_deg=rng.uniform(0, 60), raa_deg=rng.uniform(0, 180), wind_speed=rng.uniform(2, 9),
+                                 wavelength_nm=float(rng.choice([443.0, 555.0]))))
+        aers.append(A.AerosolHolder(rng.uniform(0.05, 0.3), 0.93, *hg_aerosol_moments(0.7, 30)))
+    o = A.default_opts(n_mu=N, n_layers=37, fourier_m_max=6, max_orders=300)
+    eye = np.broadcast_to(np.eye(3), (4, 3, 3)).copy()
+    monkeypatch.delenv("OCRT_GB_ADJ_SCAN", raising=False)
+    r1, g1 = gpu.solve_batch_adjoint(cs, o, aers, None, eye)
+    monkeypatch.setenv("OCRT_GB_ADJ_SCAN", "column")
+    r2, g2 = gpu.solve_batch_adjoint(cs, o, aers, None, eye)
+    for k in ("d_dtau", "d_ssa", "d_wind"):
+        np.testing.assert_allclose(g1[k], g2[k], rtol=1e-12, atol=1e-18, err_msg=k)
+    np.testing.assert_allclose(r1["rho_I"], r2["rho_I"], rtol=1e-13)
