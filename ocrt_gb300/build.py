@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libocrt_gb300.so")
 SOURCES = ["setup.cu", "sos.cu", "post.cu", "api.cu", "noalloc.cu", "tc_gemm.cu", "adjoint.cu", "lut.cu",
-           "coxmunk_tc.cu", "gas.cu", "ocean.cu", "scan_tma.cu", "mie.cu", "value.cu"]
+           "coxmunk_tc.cu", "gas.cu", "ocean.cu", "scan_tma.cu", "mie.cu", "value.cu", "tables_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"]
 

@@ -192,6 +192,13 @@ bool force_simt_coxmunk()
     return e && strcmp(e, "simt") == 0;
 }
 
+// OCRT_GB_TABLES=simt keeps the phase tables on the CUDA cores (k_tables alone).
+bool force_simt_tables()
+{
+    const char *e = getenv("OCRT_GB_TABLES");
+    return e && strcmp(e, "simt") == 0;
+}
+
 bool force_simt()
 {
     const char *e = getenv("OCRT_GB_SOURCE_KERNEL");
@@ -328,6 +335,11 @@ struct Group {
     unsigned char *aflag = nullptr;       // per wave task: queued for the next order (k_compact sorts the lists)
     float *F = nullptr, *J = nullptr, *ops = nullptr;
     float *opt = nullptr;    // pre-split operator tiles of the tensor-core pass (2 x wave_ops floats)
+    bool tabs_tc = false;    // phase tables on tcgen05 (k_tables_tc)
+    float *gtab = nullptr;   // its Gauss bases in the chunk order (k_basis_perm)
+    float *atab = nullptr;   // and the Gauss rows of its A tiles, split and swizzled
+    double *gcoef = nullptr; // GSF recurrence step coefficients per (m, l) (k_gsf_coefs)
+    float *sprod = nullptr;  // its sun-outgoing products per wave task [N][16]
     float *molV = nullptr;   // [3][32][CIN] molecular input factors V_m of the tensor-core pass
     short2 *cmpairs = nullptr;   // (outgoing, incoming) slot pairs of the tensor-core Cox-Munk kernel
     float *cstiles = nullptr;    // its cos/sin B tiles, split and swizzled
@@ -410,7 +422,8 @@ void free_group(Group &g)
                     g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.Ttl,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
                     g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
-                    g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out, g.vk_th, g.vk_p11, g.vkV};
+                    g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out, g.vk_th, g.vk_p11, g.vkV, g.gtab,
+                    g.atab, g.sprod, g.gcoef};
     for (void *p : ptrs) dfree(p);
 }
 
@@ -600,7 +613,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
         (rc = alloc(g.ops, g.wave_ops)) || (rc = alloc(g.pvec, (size_t)g.wave_tasks * 2 * G.LDC)) ||
         (rc = alloc(g.fvec, g.any_flat ? (size_t)g.wave_tasks * 24 * G.NR : 1)) ||
         (rc = alloc(g.srf, g.wave_srf)) ||
-        (rc = alloc(g.Bx, (size_t)g.wave_tasks * 3 * (1 + G.E) * (g.Lmax + 1))))
+        (rc = alloc(g.Bx, (size_t)g.wave_tasks * 3 * (1 + G.E) * (g.Lmax + 1))) ||
+        (rc = alloc(g.gcoef, (size_t)(g.Mmax + 1) * (g.Lmax + 1) * 5)))
         return rc;
     if (g.any_layers && ((rc = up(g.ldt, ldt)) || (rc = up(g.lss, lss)))) return rc;
     if (g.any_vk) {
@@ -645,6 +659,11 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     g.use_tc = tc_supported(G) && !force_simt();
     if (g.use_tc && (rc = alloc(g.opt, 2 * g.wave_ops))) return rc;
     if (g.use_tc && (rc = alloc(g.molV, (size_t)3 * 32 * G.CIN))) return rc;
+    g.tabs_tc = g.use_tc && tables_tc_supported(G, g.Lmax) && !force_simt_tables();
+    if (g.tabs_tc && ((rc = alloc(g.gtab, tables_tc_gt_floats(G.N, g.Mmax, g.Lmax))) ||
+                      (rc = alloc(g.atab, tables_tc_at_floats(g.Mmax, g.Lmax))) ||
+                      (rc = alloc(g.sprod, (size_t)g.wave_tasks * G.N * 16))))
+        return rc;
     // Cox-Munk pairs for the tensor-core projection: ring slots o < NR, incoming
     // Gauss slots and the sun (i = N); Gauss pairs with o > i are written by
     // their reciprocal pair
@@ -848,7 +867,12 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
     LAUNCH(plan, KC_SETUP, k_coef<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, G.NR, g.gmu, g.h, g.Tc, g.Ca, g.Cb));
     if (g.Cq)
         LAUNCH(plan, KC_SETUP, k_coef_quads<<<dim3(16, P), 256, 0, st>>>(g.px, P, g.N, G.NR, g.Tc, g.Ca, g.Cb, g.Cq));
-    LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt));
+    LAUNCH(plan, KC_SETUP, k_gsf_coefs<<<g.Mmax + 1, 128, 0, st>>>(g.Mmax, g.Lmax, g.gcoef));
+    LAUNCH(plan, KC_SETUP, k_basis_gauss<<<g.Mmax + 1, 64, 0, st>>>(g.N, g.Mmax, g.Lmax, g.gmu, g.Bp, g.Br, g.Bt,
+                                                                   g.gcoef));
+    if (g.tabs_tc)
+        LAUNCH(plan, KC_SETUP, k_basis_perm<<<dim3(8, g.Mmax + 1), 256, 0, st>>>(g.N, g.Mmax, g.Lmax, g.Bp, g.Br, g.Bt,
+                                                                                g.gtab, g.atab));
     if (g.use_tc)
         LAUNCH(plan, KC_SETUP, k_mol_vtab<<<std::min(g.Mmax, 2) + 1, 256, 0, st>>>(G, g.Lmax, g.Bp, g.Br, g.Bt, g.gw,
                                                                                   g.molV));
@@ -925,20 +949,35 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         CK(cudaMemsetAsync(g.work, 0, sizeof(int) * 4 * ((size_t)g.max_orders + 2), st));
         CK(cudaMemsetAsync(g.aflag, 0, (size_t)nw, st));
         LAUNCH(plan, KC_TABLES, k_basis_pix<<<(nw + 128 / (1 + G.E) - 1) / (128 / (1 + G.E)), 128, 0, st>>>(
-                   g.tasks, w.t0, nw, g.px, g.Lmax, G.E, g.Bx));
+                   g.tasks, w.t0, nw, g.px, g.Lmax, G.E, g.Bx, g.gcoef));
         if (g.any_vk)
             LAUNCH(plan, KC_TABLES, k_value_pfm<<<dim3(((G.N + 1) * 2 * G.NR + 127) / 128, w.p1 - w.p0), 128,
                                                   value_kernel_smem_bytes(g.vk_nmax), st>>>(
                        g.px, w.p0, G, g.gmu, g.vk_th, g.vk_p11, g.vkV, g.vk_stride));
-        auto tables = [&](int b) {
-            k_tables<<<dim3(nw, tables_yblocks(b, G.NR, G.N)), b, tables_smem_bytes(b, G.N, g.Lmax), st>>>(
-                g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops, g.pvec,
-                W.fvec, W.opt, (!g.use_tc || g.ncot > 0) ? 1 : 0, g.any_vk ? g.vkV : nullptr, w.p0, g.vk_stride);
-        };
-        int tb = 256;
-        int rc = tuned_block("k_tables", (const void *)k_tables, {G.N, g.Lmax, g.Mmax}, !capture, st, tables, &tb);
-        if (rc) return rc;
-        LAUNCH(plan, KC_TABLES, tables(tb));
+        const int plain_ops = (!g.use_tc || g.ncot > 0) ? 1 : 0;
+        int rc = 0;
+        if (g.tabs_tc) {
+            // the aerosol operator and the sun-outgoing products on tcgen05, then
+            // the molecular operator and the solar row
+            LAUNCH(plan, KC_TABLES, k_tables_tc<<<std::min(nw, g_nsm), tables_tc_threads(),
+                                                  tables_tc_smem_bytes(G, g.Lmax), st>>>(
+                       g.tasks, w.t0, nw, g.px, G, g.Lmax, g.gtab, g.atab, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops, W.opt,
+                       plain_ops, g.any_vk ? g.vkV : nullptr, w.p0, g.vk_stride, g.sprod, g.err));
+            LAUNCH(plan, KC_TABLES, k_tables<<<dim3(nw, 1), 64, tables_smem_bytes(64, G.N, g.Lmax), st>>>(
+                       g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz,
+                       g.ops, g.pvec, W.fvec, W.opt, plain_ops, g.any_vk ? g.vkV : nullptr, w.p0, g.vk_stride,
+                       g.sprod));
+        } else {
+            auto tables = [&](int b) {
+                k_tables<<<dim3(nw, tables_yblocks(b, G.NR, G.N)), b, tables_smem_bytes(b, G.N, g.Lmax), st>>>(
+                    g.tasks, w.t0, nw, g.px, G, g.Lmax, g.Bp, g.Br, g.Bt, g.Bx, g.gw, g.mb, g.mg, g.ma, g.mz, g.ops,
+                    g.pvec, W.fvec, W.opt, plain_ops, g.any_vk ? g.vkV : nullptr, w.p0, g.vk_stride, nullptr);
+            };
+            int tb = 256;
+            rc = tuned_block("k_tables", (const void *)k_tables, {G.N, g.Lmax, g.Mmax}, !capture, st, tables, &tb);
+            if (rc) return rc;
+            LAUNCH(plan, KC_TABLES, tables(tb));
+        }
         if (g.use_tc)
             LAUNCH(plan, KC_TABLES, k_mol_dense<<<nw, 256, 0, st>>>(g.tasks, w.t0, nw, G, g.Lmax, g.Bp, g.Br, g.Bt,
                                                                      g.gw, g.ops, g.opt));
@@ -1159,6 +1198,7 @@ int ocrt_gb_init(int device)
     CK(cudaFuncSetAttribute(k_coxmunk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_ipss, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    CK(tables_tc_init());
     CK(cudaFuncSetAttribute(k_value_pfm, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_scan4, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

@@ -15,8 +15,13 @@ __global__ void k_coef(const PixDev *px, int P, int N, int NR, const double *gmu
                        float *Tc, float *Ca, float *Cb);
 __global__ void k_coef_quads(const PixDev *px, int P, int N, int NR, const float *Tc, const float *Ca, const float *Cb,
                              float *Cq);
-__global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt);
-__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, int E, float *Bx);
+// gcoef (k_gsf_coefs, (M + 1) (L + 1) 5 doubles) or nullptr: the recurrences'
+// step coefficients, tabulated once per group instead of per direction
+__global__ void k_gsf_coefs(int M, int L, double *gcoef);
+__global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt,
+                              const double *gcoef);
+__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, int E, float *Bx,
+                            const double *gcoef);
 // k_scan: levels in flight per column (cp.async ring depth, a power of two)
 // and its dynamic shared memory: J, the total's FP32 head and 3 coefficients per slot.
 #define SCAN_DEPTH 8
@@ -65,7 +70,25 @@ __global__ void k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDe
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
                          float *ops, float *pvec, float *fvec, float *opt, int plain,
-                         const float *V, int vp0, long long vstride);
+                         const float *V, int vp0, long long vstride, const float *sprod);
+// tables_tc.cu: phase tables and the aerosol operator tiles with the sums over
+// l on tcgen05 (the pair part of k_tables; k_tables then runs with sprod for
+// the molecular operator and the solar row).  GT: the Gauss bases in the chunk
+// order, AT: the Gauss rows of the A tiles split and swizzled (k_basis_perm,
+// grid (blocks, M + 1)); sprod[task][N][16]: the S and D sums of the eight
+// sun-outgoing products of every Gauss slot.
+__global__ void k_basis_perm(int N, int M, int L, const float *Bp, const float *Br, const float *Bt, float *GT,
+                             float *AT);
+__global__ void k_tables_tc(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
+                            const float *GT, const float *AT, const float *Bx, const double *gw, const double *mb,
+                            const double *mg, const double *ma, const double *mz, float *ops, float *opt, int plain,
+                            const float *V, int vp0, long long vstride, float *sprod, int *err);
+size_t tables_tc_smem_bytes(const Geom &G, int L);
+size_t tables_tc_gt_floats(int N, int M, int L);
+size_t tables_tc_at_floats(int M, int L);
+bool tables_tc_supported(const Geom &G, int L);
+int tables_tc_threads();
+cudaError_t tables_tc_init();
 // value.cu: the aerosol value kernel's I-I tables V[pixel - p0][m][row][column]
 // (rows: sun, Gauss nodes; columns: ring slots at +mu, then at -mu)
 __global__ void k_value_pfm(const PixDev *px, int p0, Geom G, const double *gmu, const double *vk_th,

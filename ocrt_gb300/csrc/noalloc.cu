@@ -229,7 +229,7 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
     NA_LAUNCH(k_level_mix<<<dim3(2, 1), 256, 0, st>>>(px, 1, z, xd, yd));
     if (opts->gas) NA_LAUNCH(k_gas_apply<<<1, 256, 0, st>>>(px, 1, h, ch, xd, yd, z, tabs));
     NA_LAUNCH(k_coef<<<dim3(16, 1), 256, 0, st>>>(px, 1, N, NR, gmu, h, Tc, Ca, Cb));
-    NA_LAUNCH(k_basis_gauss<<<T, 64, 0, st>>>(N, M, L, gmu, Bp, Br, Bt));
+    NA_LAUNCH(k_basis_gauss<<<T, 64, 0, st>>>(N, M, L, gmu, Bp, Br, Bt, nullptr));
     if (rough) {
         NA_LAUNCH(k_cs_table<<<T + 1, 256, 0, st>>>(M, d.nphi, cst));
         NA_LAUNCH(k_seed_att<<<dim3(8, 1), 256, 0, st>>>(px, 1, N, gmu, h, Eatt));
@@ -257,9 +257,10 @@ extern "C" int ocrt_gb_solve_case_noalloc(const ocrt_case *cs, const ocrt_opts *
         NA_CK(cudaMemsetAsync(active, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
         NA_CK(cudaMemsetAsync(molcnt, 0, sizeof(int) * ((size_t)opts->max_orders + 2), st));
         NA_CK(cudaMemsetAsync(work, 0, sizeof(int) * 4 * ((size_t)opts->max_orders + 2), st));
-        NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, 1, Bx));
+        NA_LAUNCH(k_basis_pix<<<(nw + 63) / 64, 128, 0, st>>>(tasks, t0, nw, px, L, 1, Bx, nullptr));
         NA_LAUNCH(k_tables<<<dim3(nw, tables_yblocks(256, G.NR, G.N)), 256, tables_smem_bytes(256, G.N, L), st>>>(
-            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec, nullptr, 1, nullptr, 0, 0));
+            tasks, t0, nw, px, G, L, Bp, Br, Bt, Bx, gw, mb, mg, ma, mz, ops, pvec, W.fvec, nullptr, 1, nullptr, 0, 0,
+            nullptr));
         NA_LAUNCH(k_primary<<<nw, scan_threads, 0, st>>>(B, W, G, t0));
         const dim3 sgrid(nw, (K + ST_M_TILE - 1) / ST_M_TILE, (G.COUT + ST_N_TILE - 1) / ST_N_TILE);
         for (int it = 2; it <= opts->max_orders; ++it) {

@@ -140,10 +140,25 @@ __host__ __device__ inline double gsf_diag_norm(int m)
     return v;
 }
 
+// The x-independent coefficients of the step l -> l + 1 (l >= max(2, m)):
+// c = {f, b, sc, dc, cc} of the scalar and spin-2 three-term recurrences.
+__host__ __device__ inline void gsf_step_coefs(int l, int m, double *c)
+{
+    c[0] = (2.0 * l + 1.0) / sqrt((double)(l + m + 1) * (double)(l - m + 1));
+    c[1] = sqrt((double)(l + m) * (double)(l - m)) / (2.0 * l + 1.0);
+    c[2] = (double)(l + 1) * (double)(2 * l + 1) /
+           sqrt((double)(l + 3) * (double)(l - 1) * (double)(l + m + 1) * (double)(l - m + 1));
+    c[3] = sqrt((double)(l + 2) * (double)(l - 2) * (double)(l + m) * (double)(l - m)) /
+           ((double)l * (double)(2 * l + 1));
+    c[4] = 2.0 * (double)m / ((double)l * (double)(l + 1));
+}
+
 // Runs the scalar and spin-2 recurrences for one direction cosine x and
-// hands every degree l = 0..L to sink(l, P, R, T).
+// hands every degree l = 0..L to sink(l, P, R, T).  ctab, when given, holds
+// gsf_step_coefs(l, m) at ctab[5 l] (k_gsf_coefs), so the steps need no
+// square root or division.
 template <class Sink>
-__device__ inline void gsf_recur(int L, int m, double x, Sink sink)
+__device__ inline void gsf_recur(int L, int m, double x, Sink sink, const double *ctab = nullptr)
 {
     double p0 = 0, p1 = 0, r0 = 0, r1 = 0, t0 = 0, t1 = 0;   // degree l-1 and l
     // degrees below the start are zero
@@ -175,14 +190,15 @@ __device__ inline void gsf_recur(int L, int m, double x, Sink sink)
     if (l0 - 1 <= L) sink(l0 - 1, p0, r0, t0);
     if (l0 <= L) sink(l0, p1, r1, t1);
     for (int l = l0; l < L; ++l) {
-        const double f = (2.0 * l + 1.0) / sqrt((double)(l + m + 1) * (double)(l - m + 1));
-        const double b = sqrt((double)(l + m) * (double)(l - m)) / (2.0 * l + 1.0);
+        double k[5];
+        if (ctab) {
+#pragma unroll
+            for (int q = 0; q < 5; ++q) k[q] = ctab[5 * l + q];
+        } else {
+            gsf_step_coefs(l, m, k);
+        }
+        const double f = k[0], b = k[1], sc = k[2], dc = k[3], cc = k[4];
         const double p2 = f * (x * p1 - b * p0);
-        const double sc = (double)(l + 1) * (double)(2 * l + 1) /
-            sqrt((double)(l + 3) * (double)(l - 1) * (double)(l + m + 1) * (double)(l - m + 1));
-        const double dc = sqrt((double)(l + 2) * (double)(l - 2) * (double)(l + m) * (double)(l - m)) /
-                          ((double)l * (double)(2 * l + 1));
-        const double cc = 2.0 * (double)m / ((double)l * (double)(l + 1));
         const double r2 = sc * (x * r1 - cc * t1 - dc * r0);
         const double t2 = sc * (x * t1 - cc * r1 - dc * t0);
         p0 = p1; p1 = p2; r0 = r1; r1 = r2; t0 = t1; t1 = t2;

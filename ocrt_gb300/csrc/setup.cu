@@ -12,6 +12,7 @@
 //   k_flat_fresnel   flat-surface diagonal Mueller kernels    (rt_surface_boundary.c:86-103)
 #include "kernels.cuh"
 #include "physics.cuh"
+#include "tables.cuh"
 
 __global__ void k_gauss(int N, double *mu, double *w, float *pw)
 {
@@ -289,7 +290,8 @@ __global__ void k_coef_deriv(const PixDev *px, int P, int N, const double *gmu, 
     }
 }
 
-__global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt)
+__global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp, float *Br, float *Bt,
+                              const double *gcoef)
 {
     const int m = blockIdx.x, g = threadIdx.x;
     if (m > M || g >= N) return;
@@ -298,13 +300,25 @@ __global__ void k_basis_gauss(int N, int M, int L, const double *gmu, float *Bp,
         Bp[base + (size_t)l * N + g] = (float)P;
         Br[base + (size_t)l * N + g] = (float)R;
         Bt[base + (size_t)l * N + g] = (float)T;
-    });
+    }, gcoef ? gcoef + (size_t)m * (L + 1) * 5 : nullptr);
+}
+
+// Step coefficients of the GSF recurrences for every (m, l) of a group:
+// gcoef[(m * (L + 1) + l) * 5 ..] = gsf_step_coefs(l, m) for max(2, m) <= l < L.
+__global__ void k_gsf_coefs(int M, int L, double *gcoef)
+{
+    const int m = blockIdx.x;
+    if (m > M) return;
+    const int l0 = m < 2 ? 2 : m;
+    for (int l = l0 + threadIdx.x; l < L; l += blockDim.x)
+        gsf_step_coefs(l, m, gcoef + ((size_t)m * (L + 1) + l) * 5);
 }
 
 // GSF basis at the solar direction (-mu0) and at the E zero-weight slots for
 // every task of a wave: Bx[((t*(1+E) + which)*3 + comp)*(L+1) + l], which 0 =
 // sun, 1 + e = slot N + e.
-__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, int E, float *Bx)
+__global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, int L, int E, float *Bx,
+                            const double *gcoef)
 {
     const int W = 1 + E, per = blockDim.x / W;
     if ((int)threadIdx.x >= per * W) return;
@@ -318,47 +332,21 @@ __global__ void k_basis_pix(const TaskDev *tasks, int t0, int nt_tasks, const Pi
     for (int l = 0; l <= L; ++l) { dst[l] = 0.f; dst[L + 1 + l] = 0.f; dst[2 * (L + 1) + l] = 0.f; }
     gsf_recur(d.L, tk.m, x, [&](int l, double P, double R, double T) {
         dst[l] = (float)P; dst[L + 1 + l] = (float)R; dst[2 * (L + 1) + l] = (float)T;
-    });
-}
-
-// Writes the 36 operator entries of one (outgoing o, incoming Gauss i) pair
-// from the 18 direction-pair coefficients of rt_sos_operator.c:54-72
-// (order: ii_s ii_c iu_s iu_c iuT_s iuT_c iq_s iq_c iqT_s iqT_c qq_s qq_c
-//  qu_s qu_c quT_s quT_c uu_s uu_c), with the quadrature weight folded in.
-// The signs are those of the contraction in rt_sos_operator.c:387-406.
-template <class Store>
-__device__ inline void put_pair(Store st, const Geom &G, int o, int i, float w, const float *c)
-{
-    enum { II_S, II_C, IU_S, IU_C, IUT_S, IUT_C, IQ_S, IQ_C, IQT_S, IQT_C, QQ_S, QQ_C,
-           QU_S, QU_C, QUT_S, QUT_C, UU_S, UU_C };
-    auto at = [&](int so, int ho, int si, int hi, float v) { st(col_of(G, so, ho, o), (si * 2 + hi) * G.N + i, v); };
-    // I up / down
-    at(0, 0, 0, 0, w * c[II_S]);   at(0, 0, 1, 0, w * c[IQT_S]);  at(0, 0, 2, 0, -w * c[IUT_S]);
-    at(0, 0, 0, 1, w * c[II_C]);   at(0, 0, 1, 1, w * c[IQT_C]);  at(0, 0, 2, 1, -w * c[IUT_C]);
-    at(0, 1, 0, 0, w * c[II_C]);   at(0, 1, 1, 0, w * c[IQT_C]);  at(0, 1, 2, 0, w * c[IUT_C]);
-    at(0, 1, 0, 1, w * c[II_S]);   at(0, 1, 1, 1, w * c[IQT_S]);  at(0, 1, 2, 1, w * c[IUT_S]);
-    // Q up / down
-    at(1, 0, 0, 0, w * c[IQ_S]);   at(1, 0, 1, 0, w * c[QQ_S]);   at(1, 0, 2, 0, -w * c[QU_S]);
-    at(1, 0, 0, 1, w * c[IQ_C]);   at(1, 0, 1, 1, w * c[QQ_C]);   at(1, 0, 2, 1, w * c[QU_C]);
-    at(1, 1, 0, 0, w * c[IQ_C]);   at(1, 1, 1, 0, w * c[QQ_C]);   at(1, 1, 2, 0, -w * c[QU_C]);
-    at(1, 1, 0, 1, w * c[IQ_S]);   at(1, 1, 1, 1, w * c[QQ_S]);   at(1, 1, 2, 1, w * c[QU_S]);
-    // U up / down (leading minus of rt_sos_operator.c:399-406 folded in)
-    at(2, 0, 0, 0, -w * c[IU_S]);  at(2, 0, 1, 0, -w * c[QUT_S]); at(2, 0, 2, 0, w * c[UU_S]);
-    at(2, 0, 0, 1, w * c[IU_C]);   at(2, 0, 1, 1, -w * c[QUT_C]); at(2, 0, 2, 1, w * c[UU_C]);
-    at(2, 1, 0, 0, -w * c[IU_C]);  at(2, 1, 1, 0, w * c[QUT_C]);  at(2, 1, 2, 0, w * c[UU_C]);
-    at(2, 1, 0, 1, w * c[IU_S]);   at(2, 1, 1, 1, w * c[QUT_S]);  at(2, 1, 2, 1, w * c[UU_S]);
+    }, gcoef ? gcoef + (size_t)tk.m * (L + 1) * 5 : nullptr);
 }
 
 // One block per task.  Phase tables by contraction over l in FP32 with the
 // even/odd parity split giving the mirrored columns; then the packed aerosol
 // operator (and molecular operator for m <= 2), the primary-source vectors and
-// the flat-surface reflected-beam vectors.
+// the flat-surface reflected-beam vectors.  With sprod (k_tables_tc has run)
+// only the second part: the tensor-core kernel wrote the aerosol operator and
+// the sun-outgoing products of the Gauss slots.
 __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G, int L,
                          const float *Bp, const float *Br, const float *Bt, const float *Bx,
                          const double *gw,
                          const double *mb, const double *mg, const double *ma, const double *mz,
                          float *ops, float *pvec, float *fvec, float *opt, int plain,
-                         const float *V, int vp0, long long vstride)
+                         const float *V, int vp0, long long vstride, const float *sprod)
 {
     const int tl = blockIdx.x;
     if (tl >= nt_tasks) return;
@@ -412,7 +400,7 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     float *Xs = Ys + 8 * PO * TB_LC;                              // [3][TB_LC][N]
     const int hN = (N + 1) / 2;
     const int nslot = n * hN, e0 = blockIdx.y * blockDim.x;
-    if (e0 < nslot) {
+    if (!sprod && e0 < nslot) {
     const int e1 = min(e0 + (int)blockDim.x, nslot);
     const int o_lo = e0 / hN, nor = (e1 - 1) / hN - o_lo + 1;
     const int e = e0 + threadIdx.x;
@@ -493,25 +481,14 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     }
     // tables: value at +col = S, at -col = sigma * D with sigma from the column basis
     auto emit = [&](const float *Ea, const float *Oa, int i) {
-        float S[9], D[9], St[4], Dt[4];
+        float S[13], D[13], c[18];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) { S[q] = Ea[q] + Oa[q]; D[q] = Ea[q] - Oa[q]; }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) { St[q] = Ea[9 + q] + Oa[9 + q]; Dt[q] = Ea[9 + q] - Oa[9 + q]; }
-        float c[18];
-        c[0] = S[0];             c[1] = D[0];               // pfm[i][+-o]
+        for (int q = 0; q < 13; ++q) { S[q] = Ea[q] + Oa[q]; D[q] = Ea[q] - Oa[q]; }
+        pair_coefs(S, D, c);
         if (Vm) {                                           // the value kernel's table instead
             c[0] = Vm[(size_t)(1 + i) * 2 * G.NR + os];
             c[1] = Vm[(size_t)(1 + i) * 2 * G.NR + G.NR + os];
         }
-        c[2] = S[2];             c[3] = -D[2];              // gt[i][+-o]
-        c[4] = St[0];            c[5] = -Dt[0];             // gt[o][+-i]
-        c[6] = S[1];             c[7] = D[1];               // gr[i][+-o]
-        c[8] = St[1];            c[9] = Dt[1];              // gr[o][+-i]
-        c[10] = S[3] + S[4];     c[11] = -D[3] + D[4];      // arr[i][+-o]
-        c[12] = S[5] + S[6];     c[13] = D[5] - D[6];       // art[i][+-o]
-        c[14] = St[2] + St[3];   c[15] = Dt[2] - Dt[3];     // art[o][+-i]
-        c[16] = S[7] + S[8];     c[17] = -D[7] + D[8];      // att[i][+-o]
         const float w = (float)gw[i];
         if (plain) put_pair([&](int r, int ci, float v) { Aop[(size_t)r * G.CIN + ci] = v; }, G, os, i, w, c);
         if (Atile) put_pair([&](int r, int ci, float v) { tile_put(Atile, G, r, ci, v); }, G, os, i, w, c);
@@ -522,7 +499,7 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     if (blockIdx.y != 0) return;
     // tile rows no pair writes: the rows of unused zero-weight slots (the view
     // when it is a Gauss node), and the padding rows COUT .. NP - 1
-    if (Atile) {
+    if (Atile && !sprod) {
         const int nz0 = 6 * (G.NR - n), nz = nz0 + (G.NP - G.COUT);
         for (int e = threadIdx.x; e < nz * G.CIN; e += blockDim.x) {
             const int q = e / G.CIN, ci = e - q * G.CIN;
@@ -584,32 +561,72 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
     // pvec[tl][2][LDC]: [0] aerosol part, [1] molecular part of J1 / (ch * fraction)
     float *pv = pvec + (size_t)tl * 2 * G.LDC;
     float *fv = fvec ? fvec + (size_t)tl * 2 * 2 * 6 * G.NR : nullptr;   // [side][aer/mol][6][NR]
+    // with sprod, the zero-weight slots' sun-outgoing products are summed by a
+    // warp each (lane: l = m + lane + 32 j, whose parity is the lane's), into
+    // vprod[e] = {S[8], D[8]}
+    __shared__ float vprod[4][16];
+    if (sprod) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+        for (int e = warp; e < n - N && e < 4; e += nwarp) {
+            const int os = N + e;
+            float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int l = m + lane; l <= Lp; l += 32) {
+                const float be = smom[l], ga = smom[(Lp + 1) + l];
+                const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
+                const float P0 = basis(0, -1, l), R0 = basis(1, -1, l), T0 = basis(2, -1, l);
+                const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
+                a[0] += P0 * Po * be; a[1] += P0 * Ro * ga; a[2] += P0 * To * ga; a[3] += T0 * To * ze;
+                a[4] += R0 * Ro * al; a[5] += Po * R0 * ga; a[6] += To * R0 * al; a[7] += Ro * T0 * ze;
+            }
+            const float sg = (lane & 1) ? -1.f : 1.f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float sv = a[q], dv = sg * a[q];
+#pragma unroll
+                for (int k = 16; k >= 1; k >>= 1) {
+                    sv += __shfl_xor_sync(0xffffffffu, sv, k);
+                    dv += __shfl_xor_sync(0xffffffffu, dv, k);
+                }
+                if (lane == 0) { vprod[e][q] = sv; vprod[e][8 + q] = dv; }
+            }
+        }
+        __syncthreads();
+    }
     for (int o = threadIdx.x; o < n; o += blockDim.x) {
         const int os = o;
-        float E[6] = {0}, O[6] = {0};      // PP b, PR g, PT g, TT z, RR a, TR a | plus transposed pair
-        float Ex[3] = {0}, Ox[3] = {0};    // RT z, TT a, RR z
-        float Ey[2] = {0}, Oy[2] = {0};    // P_o R_0 g  (gr pair),  T_o R_0 a + R_o T_0 z (art pair)
-        for (int l = m; l <= Lp; ++l) {
-            const float be = smom[l], ga = smom[(Lp + 1) + l];
-            const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
-            const float P0 = basis(0, -1, l), R0 = basis(1, -1, l), T0 = basis(2, -1, l);
-            const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
-            const float v[6] = {P0 * Po * be, P0 * Ro * ga, P0 * To * ga, T0 * To * ze, R0 * Ro * al, T0 * Ro * al};
-            const float vx[3] = {R0 * To * ze, T0 * To * al, R0 * Ro * ze};
-            const float vy[2] = {Po * R0 * ga, To * R0 * al + Ro * T0 * ze};
-            const bool ev = ((l + m) & 1) == 0;
+        // the eight sun-outgoing products (0 sun incoming): sums over l of
+        //   0 P0 Po beta   1 P0 Ro gamma   2 P0 To gamma   3 T0 To zeta
+        //   4 R0 Ro alpha  5 R0 Po gamma   6 R0 To alpha   7 T0 Ro zeta
+        // S over all l, D with the sign (-1)^(l+m); from k_tables_tc for the
+        // Gauss slots when it ran, else summed here
+        float S[8], D[8];
+        if (sprod) {
+            const float *sp = o < N ? sprod + ((size_t)tl * N + o) * 16 : vprod[o - N];
 #pragma unroll
-            for (int q = 0; q < 6; ++q) (ev ? E[q] : O[q]) += v[q];
+            for (int q = 0; q < 8; ++q) { S[q] = sp[q]; D[q] = sp[8 + q]; }
+        } else {
+            float E[8] = {0}, O[8] = {0};
+            for (int l = m; l <= Lp; ++l) {
+                const float be = smom[l], ga = smom[(Lp + 1) + l];
+                const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
+                const float P0 = basis(0, -1, l), R0 = basis(1, -1, l), T0 = basis(2, -1, l);
+                const float Po = basis(0, os, l), Ro = basis(1, os, l), To = basis(2, os, l);
+                const float v[8] = {P0 * Po * be, P0 * Ro * ga, P0 * To * ga, T0 * To * ze,
+                                    R0 * Ro * al, Po * R0 * ga, To * R0 * al, Ro * T0 * ze};
+                const bool ev = ((l + m) & 1) == 0;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) (ev ? Ex[q] : Ox[q]) += vx[q];
+                for (int q = 0; q < 8; ++q) (ev ? E[q] : O[q]) += v[q];
+            }
 #pragma unroll
-            for (int q = 0; q < 2; ++q) (ev ? Ey[q] : Oy[q]) += vy[q];
+            for (int q = 0; q < 8; ++q) { S[q] = E[q] + O[q]; D[q] = E[q] - O[q]; }
         }
         // row 0 (solar) tables at column +o (S) and -o (sigma D)
-        const float pfmP = Vm ? Vm[os] : E[0] + O[0], pfmM = Vm ? Vm[G.NR + os] : E[0] - O[0];
-        const float grP = E[1] + O[1], grM = E[1] - O[1];
-        const float gtP = E[2] + O[2], gtM = -(E[2] - O[2]);
-        const float arrP = (E[3] + O[3]) + (E[4] + O[4]), arrM = -(E[3] - O[3]) + (E[4] - O[4]);
+        const float pfmP = Vm ? Vm[os] : S[0], pfmM = Vm ? Vm[G.NR + os] : D[0];
+        const float grP = S[1], grM = D[1];
+        const float gtP = S[2], gtM = -D[2];
+        const float arrP = S[3] + S[4], arrM = -D[3] + D[4];
+        // T_o R_0 alpha (sigma -) + R_o T_0 zeta (sigma +)
+        const float quP = S[6] + S[7], quM = -D[6] + D[7];
         // primary source (rt_primary_source.c:59-77, 163-177), U sign folded in
         const float p0 = basis(0, -1, 2);
         const float po = basis(0, os, 2), ro = basis(1, os, 2), to = basis(2, os, 2);
@@ -629,16 +646,8 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
             // column of the phase matrix, aerosol and molecular parts
             // (rt_primary_source.c:31-55, 72-78, 106-148, 173-182)
             const float bq = (float)d.beam_q, r0s = basis(1, -1, 2);
-            float e1 = 0.f, o1 = 0.f, e2 = 0.f, o2 = 0.f;
-            for (int l = m; l <= Lp; ++l) {
-                const float al = smom[2 * (Lp + 1) + l], ze = smom[3 * (Lp + 1) + l];
-                const float a1 = basis(2, os, l) * basis(1, -1, l) * al;
-                const float a2_ = basis(1, os, l) * basis(2, -1, l) * ze;
-                if (((l + m) & 1) == 0) { e1 += a1; e2 += a2_; } else { o1 += a1; o2 += a2_; }
-            }
-            const float quP = (e1 + o1) + (e2 + o2), quM = -(e1 - o1) + (e2 - o2);
-            pv[col_of(G, 0, 0, os)] += bq * (Ey[0] + Oy[0]);
-            pv[col_of(G, 0, 1, os)] += bq * (Ey[0] - Oy[0]);
+            pv[col_of(G, 0, 0, os)] += bq * S[5];
+            pv[col_of(G, 0, 1, os)] += bq * D[5];
             pv[col_of(G, 1, 0, os)] += bq * arrP;
             pv[col_of(G, 1, 1, os)] += bq * arrM;
             pv[col_of(G, 2, 0, os)] += -bq * quP;
@@ -657,21 +666,6 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
             // side 0 ("top", upward outputs) uses column -o, side 1 uses +o.
             // comps: P, R, T, RT(transpose gr), RR, TR(transpose art)
             const float r0 = basis(1, -1, 2);
-            const float gyP = Ey[0] + Oy[0], gyM = Ey[0] - Oy[0];          // P_o R0 g: col basis P_o -> sigma +
-            // T_o R0 a (sigma -) + R_o T0 z (sigma +): need separate parity -> recompute below
-            float tr_p = 0.f, tr_m = 0.f;
-            {
-                float e1 = 0, o1 = 0, e2 = 0, o2 = 0;
-                for (int l = m; l <= Lp; ++l) {
-                    const float al = l <= La ? (float)ma[d.mom_off + l] : 0.f;
-                    const float ze = l <= La ? (float)mz[d.mom_off + l] : 0.f;
-                    const float a1 = basis(2, os, l) * basis(1, -1, l) * al;
-                    const float a2_ = basis(1, os, l) * basis(2, -1, l) * ze;
-                    if (((l + m) & 1) == 0) { e1 += a1; e2 += a2_; } else { o1 += a1; o2 += a2_; }
-                }
-                tr_p = (e1 + o1) + (e2 + o2);
-                tr_m = -(e1 - o1) + (e2 - o2);
-            }
             for (int side = 0; side < 2; ++side) {
                 const bool neg = side == 0;
                 float *fa = fv + ((size_t)(side * 2 + 0) * 6) * G.NR;
@@ -679,9 +673,9 @@ __global__ void __launch_bounds__(256, 2) k_tables(const TaskDev *tasks, int t0,
                 fa[0 * G.NR + os] = neg ? pfmM : pfmP;
                 fa[1 * G.NR + os] = neg ? grM : grP;
                 fa[2 * G.NR + os] = neg ? gtM : gtP;
-                fa[3 * G.NR + os] = neg ? gyM : gyP;
+                fa[3 * G.NR + os] = neg ? D[5] : S[5];
                 fa[4 * G.NR + os] = neg ? arrM : arrP;
-                fa[5 * G.NR + os] = neg ? tr_m : tr_p;
+                fa[5 * G.NR + os] = neg ? quM : quP;
                 const float pd = neg ? pmo : po, rd = neg ? rmo : ro, td = neg ? tmo : to;
                 fm[0 * G.NR + os] = mol ? b0 + b2 * pd * p0 : 0.f;
                 fm[1 * G.NR + os] = mol ? g2 * rd * p0 : 0.f;

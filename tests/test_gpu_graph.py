@@ -111,12 +111,12 @@ def test_graph_replay_adjoint_plan(gpu):
 
 
 def test_autotune_changes_no_result(gpu):
-    # the CUDA-core Cox-Munk kernel is the autotuned one (the tensor-core
-    # kernel has a fixed shape), so this test selects it
+    # the CUDA-core Cox-Munk and phase-table kernels are the autotuned ones
+    # (the tensor-core kernels have a fixed shape), so this test selects them
     cs, os_, aa = _batch(16, seed=44, n_mu=16, m_max=5)
-    with _env(OCRT_GB_AUTOTUNE="0", OCRT_GB_COXMUNK="simt"):
+    with _env(OCRT_GB_AUTOTUNE="0", OCRT_GB_COXMUNK="simt", OCRT_GB_TABLES="simt"):
         r0 = gpu.solve_batch(cs, os_, aa)
-    with _env(OCRT_GB_COXMUNK="simt"):
+    with _env(OCRT_GB_COXMUNK="simt", OCRT_GB_TABLES="simt"):
         r1 = gpu.solve_batch(cs, os_, aa)
     assert np.array_equal(r0, r1)
     summ = gpu.autotune_summary()
