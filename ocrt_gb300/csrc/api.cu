@@ -995,7 +995,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
             };
             if (g.cmpairs) {
                 const int per = coxmunk_tc_pairs_per_cta();
-                LAUNCH(plan, KC_COXMUNK, k_coxmunk_tc<<<dim3((g.ncmpairs + per - 1) / per, np), coxmunk_tc_threads(),
+                LAUNCH(plan, KC_COXMUNK, k_coxmunk_tc<<<dim3((g.ncmpairs + per - 1) / per, np), coxmunk_tc_threads(dw),
                                                          coxmunk_tc_smem_bytes(g.Mmax, dw), st>>>(
                            g.tasks, g.px, w.p0, g.pix_task0, G, g.gmu, g.cs, g.cstiles, g.Mmax, g.lam,
                            dw ? g.lamd : nullptr, g.srf, dw ? g.srfW : nullptr, g.cmpairs, g.ncmpairs, dw ? 1 : 0,

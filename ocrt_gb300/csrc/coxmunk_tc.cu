@@ -12,7 +12,9 @@
 // into a second accumulator.
 //
 // K is swept in chunks of 32 azimuth nodes (one 128-byte swizzle row).  For a
-// chunk every thread evaluates two Mueller matrices on the CUDA cores (FP32,
+// chunk every thread evaluates two Mueller matrices (one in the wind-derivative
+// variant, whose larger stages leave room for one CTA per SM: 448 threads hide
+// the evaluation's latency there) on the CUDA cores (FP32,
 // the same coxmunk_R as the CUDA-core kernel) and stores the tf32 (hi, lo)
 // split into the SWIZZLE_128B K-major A tiles, while a TMA bulk copy brings the
 // chunk's B tiles (the cos/sin table already split and swizzled once per
@@ -31,6 +33,7 @@ using namespace tcg;
 
 #define CMT_P 14            // pairs per CTA (9 rows each)
 #define CMT_THREADS 224     // CMT_P x CMT_KC / 2: two Mueller evaluations per thread and chunk
+#define CMT_THREADS_DW 448  // CMT_P x CMT_KC: one per thread with the wind derivative (one CTA per SM)
 #define CMT_KC 32           // azimuth nodes per chunk
 
 // Pair constants of the Mueller evaluation (coxmunk_R in physics.cuh with
@@ -145,7 +148,7 @@ __global__ void k_cs_tiles(int Mtab, int nphi, const float *cs_tab, float *tiles
     }
 }
 
-__global__ void __launch_bounds__(CMT_THREADS)
+__global__ void __launch_bounds__(CMT_THREADS_DW)
 k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G, const double *gmu,
              const float *cs_tab, const float *cs_tiles, int Mtab, const double *lamv, const double *lamd,
              float *srf, float *srfW, const short2 *pairs, int npairs, int dw, int *err)
@@ -214,7 +217,7 @@ k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task
         pio[3 * tid + 2] = ok && o < N && i < N && o < i;
     }
     const int task_first = pix_task0[p];
-    for (int m = tid; m <= M; m += CMT_THREADS) soff[m] = tasks[task_first + m].srf_off;
+    for (int m = tid; m <= M; m += blockDim.x) soff[m] = tasks[task_first + m].srf_off;
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -250,7 +253,7 @@ k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task
             bulk_g2s(bH, cs_tiles + (size_t)c * 2 * NN * CMT_KC, 2 * B_BYTES, &bfull[s]);
         }
         // A: Mueller entries of (pair, node); row = 9 pair + entry, K = node in the chunk
-        for (int x = tid; x < CMT_P * CMT_KC; x += CMT_THREADS) {
+        for (int x = tid; x < CMT_P * CMT_KC; x += blockDim.x) {
             const int pp = x / CMT_KC, qq = x - pp * CMT_KC, q = q0 + qq;
             float R[9], tb2 = 0.f;
             if (pio[3 * pp] >= 0) {
@@ -268,7 +271,7 @@ k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task
             }
         }
         // rows 126 and 127 are zero
-        for (int x = tid; x < 2 * CMT_KC; x += CMT_THREADS) {
+        for (int x = tid; x < 2 * CMT_KC; x += blockDim.x) {
             const int row = 126 + x / CMT_KC, qq = x % CMT_KC;
             const uint32_t off = (uint32_t)row * 128u + ((uint32_t)((qq >> 2) ^ (row & 7)) << 4) + (uint32_t)(qq & 3) * 4u;
             split_st(aH, aL, off, 0.f);
@@ -370,4 +373,4 @@ bool coxmunk_tc_supported(int Mtab, int nphi, bool dw)
 
 int coxmunk_tc_pairs_per_cta() { return CMT_P; }
 
-int coxmunk_tc_threads() { return CMT_THREADS; }
+int coxmunk_tc_threads(bool dw) { return dw ? CMT_THREADS_DW : CMT_THREADS; }

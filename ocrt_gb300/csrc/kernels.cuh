@@ -106,7 +106,7 @@ size_t coxmunk_tc_smem_bytes(int Mtab, bool dw);
 size_t coxmunk_tc_tiles_floats(int Mtab, int nphi);
 bool coxmunk_tc_supported(int Mtab, int nphi, bool dw);
 int coxmunk_tc_pairs_per_cta();
-int coxmunk_tc_threads();
+int coxmunk_tc_threads(bool dw);
 __global__ void k_coxmunk(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
                           const double *gmu, const float *cs_tab, int Mtab, const double *lamv, float *srf);
 __global__ void k_coxmunk_dw(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task0, Geom G,
