@@ -339,7 +339,10 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
             if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
             else if (j >= d.max_orders) ns.active = 0;
             A.st[ta] = ns;
-            if (ns.active) atomicAdd(&A.acnt[j], 1);
+            if (ns.active) {
+                atomicAdd(&A.acnt[j], 1);
+                A.aflag[tl] = 1;                           // the task stays on the next order's list
+            }
         }
     }
 }
@@ -473,26 +476,75 @@ size_t adj_mol_smem_bytes(const Geom &G)
 
 // a_{j+1}[nt][(s', down, i)] += pw_i sum_{g, s} R_m(g, i)[s][s'] mu_bc[g][s]
 // (transpose of the rough-surface boundary operator).  Threads over (s', i).
-__global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0)
+// Surface term of adjoint order j for the rows still active after the
+// order's scan: blocks stride over the (listed task, row) items of list j + 1.
+__global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int j)
 {
-    const int ta = blockIdx.x, tl = ta / A.ncot, r = ta - tl * A.ncot, tg = t0 + tl;
-    if (!A.st[ta].active) return;
-    const TaskDev tk = B.tasks[tg];
-    const PixDev &d = B.px[tk.pix];
-    if (!d.rough) return;
     const int N = G.N, NR = G.NR;
     const int e = threadIdx.x;
     if (e >= 3 * N) return;
     const int sp = e / N, i = e - sp * N;
-    const float *mb = A.bc + (size_t)ta * NR * 3;
-    const float *R = W.srf + tk.srf_off;
-    const float pw = B.pw[(tk.m == 0 ? 0 : N) + i];
-    float acc = 0.f;
-    for (int g = 0; g < d.n_ring; ++g) {
-        const float *Rg = R + ((size_t)g * N + i) * 9 + sp;
-        acc += Rg[0] * mb[g * 3 + 0] + Rg[3] * mb[g * 3 + 1] + Rg[6] * mb[g * 3 + 2];
+    const int n_items = A.lcnt[j + 1] * A.ncot;
+    const int *lst = A.alist[(j + 1) & 1];
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const int li = item / A.ncot, r = item - li * A.ncot, tl = lst[li], ta = tl * A.ncot + r, tg = t0 + tl;
+        if (!A.st[ta].active) continue;
+        const TaskDev tk = B.tasks[tg];
+        const PixDev &d = B.px[tk.pix];
+        if (!d.rough) continue;
+        const float *mb = A.bc + (size_t)ta * NR * 3;
+        const float *R = W.srf + tk.srf_off;
+        const float pw = B.pw[(tk.m == 0 ? 0 : N) + i];
+        float acc = 0.f;
+        for (int g = 0; g < d.n_ring; ++g) {
+            const float *Rg = R + ((size_t)g * N + i) * 9 + sp;
+            acc += Rg[0] * mb[g * 3 + 0] + Rg[3] * mb[g * 3 + 1] + Rg[6] * mb[g * 3 + 2];
+        }
+        A.AF[adj_off(tk, G, A.ncot, r) + (size_t)d.nt * G.LDC + col_of(G, sp, 1, i)] += pw * acc;
     }
-    A.AF[adj_off(tk, G, A.ncot, r) + (size_t)d.nt * G.LDC + col_of(G, sp, 1, i)] += pw * acc;
+}
+
+// List of order 1: every task of the wave.
+__global__ void k_adj_list_all(AdjBufs A, int nw)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) A.alist[1][i] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) A.lcnt[1] = nw;
+}
+
+// The flagged tasks (a row active after the scan of order j) in task order
+// into list j + 1 and its count; clears the flags.  One block.
+__global__ void __launch_bounds__(COMPACT_THREADS) k_compact_adj(AdjBufs A, int nw, int j)
+{
+    __shared__ int sa[COMPACT_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int per = (nw + COMPACT_THREADS - 1) / COMPACT_THREADS;
+    const int b = min(nw, tid * per), e = min(nw, b + per);
+    int na = 0;
+    for (int i = b; i < e; ++i) na += A.aflag[i] ? 1 : 0;
+    int xa = na;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ya = __shfl_up_sync(0xffffffffu, xa, o);
+        if (lane >= o) xa += ya;
+    }
+    if (lane == 31) sa[w] = xa;
+    __syncthreads();
+    if (w == 0) {
+        int ta = sa[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int ya = __shfl_up_sync(0xffffffffu, ta, o);
+            if (lane >= o) ta += ya;
+        }
+        sa[lane] = ta;
+        if (lane == 31) A.lcnt[j + 1] = ta;
+    }
+    __syncthreads();
+    int oa = (w ? sa[w - 1] : 0) + xa - na;
+    int *al = A.alist[(j + 1) & 1];
+    for (int i = b; i < e; ++i)
+        if (A.aflag[i]) {
+            al[oa++] = i;
+            A.aflag[i] = 0;
+        }
 }
 
 // Final pass per adjoint task: the transposed transport of the adjoint total

@@ -362,6 +362,7 @@ struct Group {
     long long lut_ntot = 0;
     double *lut_vza = nullptr, *lut_raa = nullptr, *lut_samp = nullptr, *lut_kappa = nullptr, *lut_out = nullptr;
     int *acnt = nullptr, *awork = nullptr;
+    int *alcnt = nullptr, *aswork = nullptr, *adjlist[2] = {nullptr, nullptr};   // adjoint active-task lists
     float *opsT = nullptr;   // transposed aerosol operators for the tcgen05 adjoint source
     bool use_tc_adj = false;
     int gstride = 0, kstride = 0, grad_stride = 0;
@@ -421,7 +422,7 @@ void free_group(Group &g)
                     g.active_cnt, g.mol_cnt, g.work, g.alist[0], g.alist[1], g.mlist[0], g.mlist[1], g.aflag,
                     g.err, g.F, g.J, g.ops, g.opt, g.molV, g.cmpairs, g.cstiles, g.pvec, g.fvec, g.srf, g.Bx, g.Tot, g.Ttl,
                     g.ldt, g.lss, g.cot, g.lamd, g.ATot, g.gout, g.grad, g.dTc, g.dCa, g.dCb, g.srfW, g.AF, g.AJ,
-                    g.Abc, g.Ast, g.acnt, g.awork, g.opsT,
+                    g.Abc, g.Ast, g.acnt, g.awork, g.opsT, g.alcnt, g.aswork, g.adjlist[0], g.adjlist[1],
                     g.lut_vza, g.lut_raa, g.lut_samp, g.lut_kappa, g.lut_out, g.vk_th, g.vk_p11, g.vkV, g.gtab,
                     g.atab, g.sprod, g.gcoef};
     for (void *p : ptrs) dfree(p);
@@ -639,6 +640,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
             (rc = alloc(g.ATot, g.wave_fld * ncot)) ||
             (rc = alloc(g.Abc, na * G.NR * 3)) || (rc = alloc(g.Ast, na)) ||
             (rc = alloc(g.acnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.awork, (size_t)g.max_orders + 2)) ||
+            (rc = alloc(g.alcnt, (size_t)g.max_orders + 2)) || (rc = alloc(g.aswork, (size_t)g.max_orders + 2)) ||
+            (rc = alloc(g.adjlist[0], g.wave_tasks)) || (rc = alloc(g.adjlist[1], g.wave_tasks)) ||
             (rc = alloc(g.gout, na * g.gstride)) ||
             (rc = alloc(g.grad, (size_t)g.P * ncot * g.grad_stride)))
             return rc;
@@ -767,6 +770,7 @@ AdjBufs make_adj(Group &g)
     A.cot = g.cot; A.gout = g.gout; A.gstride = g.gstride; A.kstride = g.kstride;
     A.dTc = g.dTc; A.dCa = g.dCa; A.dCb = g.dCb; A.srfW = g.srfW; A.grad = g.grad; A.grad_stride = g.grad_stride;
     A.awork = g.awork;
+    A.aflag = g.aflag; A.alist[0] = g.adjlist[0]; A.alist[1] = g.adjlist[1]; A.lcnt = g.alcnt; A.swork = g.aswork;
     return A;
 }
 
@@ -795,6 +799,9 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
     CK(cudaMemsetAsync(g.awork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+    CK(cudaMemsetAsync(g.alcnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+    CK(cudaMemsetAsync(g.aswork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
+    CK(cudaMemsetAsync(g.aflag, 0, (size_t)nw, st));
     const int KP = (G.COUT + 31) & ~31;
     const int amt = (g.ncot * w.Kmax + 127) / 128;
     if (g.use_tc_adj) {
@@ -804,16 +811,18 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     }
     const AdjBufs A = make_adj(g);
     LAUNCH(plan, KC_ADJ_OTHER, k_adj_init<<<(na + 127) / 128, 128, 0, st>>>(B, A, G, w.t0, na));
+    LAUNCH(plan, KC_ADJ_OTHER, k_adj_list_all<<<(nw + 255) / 256, 256, 0, st>>>(A, nw));
     const dim3 agrid(na, (w.Kmax + ST_M_TILE - 1) / ST_M_TILE, (G.LDC + ST_N_TILE - 1) / ST_N_TILE);
     const int surf_threads = ((3 * G.N + 31) / 32) * 32;
     if (!capture) w.adj_stop = INT_MAX;
     for (int j = 1; j <= g.max_orders; ++j) {
+        const int nitem = nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB);
         if (g.amap_ok)
-            LAUNCH(plan, KC_ADJ_SCAN, adj_scan_tma_launch(nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB), st, B, A, G, w.t0, j,
-                                                          g.amap));
+            LAUNCH(plan, KC_ADJ_SCAN, adj_scan_tma_launch(std::min(nitem, 2 * g_nsm), st, B, A, G, w.t0, j, g.amap));
         else
-            LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<nw * ((g.ncot + ADJ_RB - 1) / ADJ_RB), scan_threads,
-                                                  adj_scan_smem_bytes(scan_threads), st>>>(B, A, G, w.t0, j));
+            LAUNCH(plan, KC_ADJ_SCAN, k_adj_scan<<<nitem, scan_threads, adj_scan_smem_bytes(scan_threads), st>>>(
+                       B, A, G, w.t0, j));
+        LAUNCH(plan, KC_ADJ_SCAN, k_compact_adj<<<1, COMPACT_THREADS, 0, st>>>(A, nw, j));
         if (capture) {
             if (j == w.adj_stop) break;
         } else if ((j - 1) % 4 == 0 || j == g.max_orders) {
@@ -830,7 +839,8 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_mol<<<dim3(na, ltiles), 256, adj_mol_smem_bytes(G), st>>>(
                        B, W, A, G, w.t0, g.Bp, g.Br, g.Bt, g.Lmax));
         if (w.any_rough)
-            LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<na, surf_threads, 0, st>>>(B, W, A, G, w.t0));
+            LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<std::min(na, 8 * g_nsm), surf_threads, 0, st>>>(B, W, A, G,
+                                                                                                  w.t0, j));
     }
     if (capture && w.adj_stop != INT_MAX)
         LAUNCH(plan, KC_ADJ_OTHER, k_stop_check<<<1, 32, 0, st>>>(g.acnt + w.adj_stop, g.err + 1));

@@ -210,6 +210,14 @@ struct AdjBufs {
     TaskState *st;         // per adjoint task
     int *acnt;             // [max_orders + 2] adjoint tasks still active after order j
     int *awork;            // [max_orders + 2] work counters of the persistent transposed source
+    // active-task lists: alist[j & 1] holds the lcnt[j] wave tasks with a row
+    // active at the start of order j (in task order, k_compact_adj from aflag,
+    // which the adjoint scan of order j - 1 sets); the transposed source and
+    // surface of order j read list j + 1 (rows still active after the scan)
+    unsigned char *aflag;
+    int *alist[2];
+    int *lcnt;             // [max_orders + 2]
+    int *swork;            // [max_orders + 2] work counters of the persistent adjoint scan
     const double *cot;     // [P][ncot][3]
     double *gout;          // per adjoint task partials, gstride doubles (3 arrays of kstride + 2 scalars)
     int gstride, kstride;
@@ -225,7 +233,9 @@ __global__ void k_adj_scan(BatchBufs B, AdjBufs A, Geom G, int t0, int j);
 __global__ void k_adj_source(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
 __global__ void k_adj_mol(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0,
                           const float *Bp, const float *Br, const float *Bt, int L);
-__global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0);
+__global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int j);
+__global__ void k_adj_list_all(AdjBufs A, int nw);
+__global__ void k_compact_adj(AdjBufs A, int nw, int j);
 __global__ void k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb);
 __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, int t0);
 size_t adj_mol_smem_bytes(const Geom &G);

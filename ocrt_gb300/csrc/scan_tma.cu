@@ -300,8 +300,11 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
 // ===========================================================================
 // The adjoint's transposed transport (k_adj_scan in adjoint.cu: the same
 // recurrences run the other way, nu = a + T nu', muJ = Ca nu + Cb nu', the
-// adjoint total and its convergence norms) fed the same way.  One block per
-// (task, group of up to ADJ_RB cotangent rows); per ring stage and direction
+// adjoint total and its convergence norms) fed the same way.  Persistent:
+// blocks pull (task, group of up to ADJ_RB cotangent rows) items of the
+// order's active-task list (k_compact_adj) from a work counter, and a task
+// with a row still active after the order is flagged for the next list; per
+// ring stage and direction
 // the adjoint field and the adjoint total boxes of every active row and the
 // weight rows of the chunk's CH levels plus one (the transposed recurrence
 // reads T and Cb of one layer and Ca of the next).  Per column and row the
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
 {
     extern __shared__ unsigned char ast_raw[];
     __shared__ float2 redf2[32];
-    __shared__ int abort_raw;
+    __shared__ int item_s, abort_raw;
     volatile int &abort_s = abort_raw;
     unsigned char *base = (unsigned char *)(((uintptr_t)ast_raw + 127) & ~(uintptr_t)127);
     const AstLayout Ly = ast_layout(G, CH);
@@ -348,7 +351,24 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
     const bool producer = tid == nthr - 32;
     const int N = G.N, NR = G.NR, ZW = scan_tma_zw(G), CW = scan_tma_cw(G);
     const int nrg = (A.ncot + ADJ_RB - 1) / ADJ_RB;
-    const int tl = blockIdx.x / nrg, r0 = (blockIdx.x - tl * nrg) * ADJ_RB, tg = t0 + tl;
+    // items: (task of this order's active list, group of ADJ_RB rows)
+    const int n_items = A.lcnt[j] * nrg;
+    const int *lst = A.alist[j & 1];
+    if (tid == 0) {
+        for (int i = 0; i < NS; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], ncw); }
+        abort_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    uint32_t issued = 0, consumed = 0;                   // ring positions issued / consumed by this CTA
+    __syncthreads();
+    for (;;) {
+    __syncthreads();
+    if (tid == 0) item_s = abort_s ? n_items : atomicAdd(&A.swork[j], 1);
+    __syncthreads();
+    if (item_s >= n_items) break;
+    const int li = item_s / nrg;
+    const int tl = lst[li], r0 = (item_s - li * nrg) * ADJ_RB, tg = t0 + tl;
     const int nr = min(ADJ_RB, A.ncot - r0);
     bool act[ADJ_RB];
     int nact = 0;
@@ -357,17 +377,10 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
         act[q] = q < nr && A.st[tl * A.ncot + r0 + q].active;
         nact += act[q] ? 1 : 0;
     }
-    if (nact == 0) return;                                // block-uniform
+    if (nact == 0) continue;                              // block-uniform
     const TaskDev tk = B.tasks[tg];
     const PixDev &d = B.px[tk.pix];
     const int nt = d.nt, nq = (nt + CH) / CH;
-    if (tid == 0) {
-        for (int i = 0; i < NS; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], ncw); }
-        abort_s = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
     // first level row of each active row's adjoint field: (fld_off ncot + r K LDC) / LDC
     int rrow[ADJ_RB];
 #pragma unroll
@@ -376,7 +389,6 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
     const int lay0 = (int)(d.coef_off / NR);
     const uint32_t TX = 2u * (uint32_t)CH * 4u * (uint32_t)nact * (uint32_t)(2 * 3 * N + 2 * ZW) +
                         2u * (uint32_t)(CH + 1) * 4u * (uint32_t)CW;
-    uint32_t issued = 0;
     auto issue = [&](int q) -> bool {
         const uint32_t pos = issued, sl = pos % NS;
         if (pos >= (uint32_t)NS && !mbar_wait(&empty[sl], ((pos / NS) - 1) & 1)) return false;
@@ -435,7 +447,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
         // writes them, so they are cleared here once read
         const bool clear = c >= G.CIN;
         for (int q = 0; q < nq; ++q) {
-            const uint32_t pos = (uint32_t)q, sl = pos % NS;
+            const uint32_t pos = consumed + (uint32_t)q, sl = pos % NS;
             const bool ok = __all_sync(0xffffffffu, mbar_wait(&full[sl], (pos / NS) & 1));
             if (!ok) { abort_s = 1; break; }
             const unsigned char *db = base + (size_t)sl * Ly.stage + h * Ly.dir;
@@ -485,14 +497,9 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
             for (int rq = 0; rq < ADJ_RB; ++rq)
                 if (act[rq]) A.bc[(size_t)(tl * A.ncot + r0 + rq) * NR * 3 + g * 3 + s] = nup[rq];
     }
+    consumed += (uint32_t)nq;
     __syncthreads();
-    if (abort_s) {
-        if (tid == 0) atomicExch(B.err, OCRT_ERR_DEVICE);
-        if (producer)
-            for (uint32_t p = issued > (uint32_t)NS ? issued - NS : 0; p < issued; ++p)
-                (void)mbar_wait(&full[p % NS], (p / NS) & 1);
-        return;
-    }
+    if (abort_s) break;
 #pragma unroll
     for (int rq = 0; rq < ADJ_RB; ++rq) {
         if (!act[rq]) continue;                    // block-uniform
@@ -505,9 +512,21 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
             if (ns.resid < d.tol) { ns.converged = 1; ns.active = 0; }
             else if (j >= d.max_orders) ns.active = 0;
             A.st[ta] = ns;
-            if (ns.active) atomicAdd(&A.acnt[j], 1);
+            if (ns.active) {
+                atomicAdd(&A.acnt[j], 1);
+                A.aflag[tl] = 1;                           // the task stays on the next order's list
+            }
         }
         __syncthreads();
+    }
+    }
+    if (abort_s) {
+        if (tid == 0) atomicExch(B.err, OCRT_ERR_DEVICE);
+        // copies issued but not consumed still land in this block's shared
+        // memory: wait for them (bounded) before the block exits
+        if (producer)
+            for (uint32_t p = issued > (uint32_t)NS ? issued - NS : 0; p < issued; ++p)
+                (void)mbar_wait(&full[p % NS], (p / NS) & 1);
     }
 }
 

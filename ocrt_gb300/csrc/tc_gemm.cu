@@ -85,10 +85,12 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
     // epilogue transpose tiles: [4 warps][32 rows][TC_TP floats]
     float *tpose = (float *)(base + 2 * STAGE + 256);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n_items = (ADJ ? nw : B.active_cnt[it - 1]) * mtiles;
-    const int *alist = ADJ ? nullptr : B.alist[it & 1];
+    // the adjoint's order it reads the tasks with a row still active after its
+    // scan: list it + 1
+    const int n_items = (ADJ ? AB.lcnt[it + 1] : B.active_cnt[it - 1]) * mtiles;
+    const int *alist = ADJ ? AB.alist[(it + 1) & 1] : B.alist[it & 1];
     int *counter = ADJ ? &AB.awork[it] : &B.work[it * 4];
-    auto task_of = [&](int li) -> int { return ADJ ? li : alist[li]; };
+    auto task_of = [&](int li) -> int { return alist[li]; };
 
     if (warp == 2) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
