@@ -839,7 +839,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
             LAUNCH(plan, KC_ADJ_SOURCE, k_adj_mol<<<dim3(na, ltiles), 256, adj_mol_smem_bytes(G), st>>>(
                        B, W, A, G, w.t0, g.Bp, g.Br, g.Bt, g.Lmax));
         if (w.any_rough)
-            LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<std::min(na, 8 * g_nsm), surf_threads, 0, st>>>(B, W, A, G,
+            LAUNCH(plan, KC_ADJ_OTHER, k_adj_surface<<<std::min(na, 32 * g_nsm), surf_threads, 0, st>>>(B, W, A, G,
                                                                                                   w.t0, j));
     }
     if (capture && w.adj_stop != INT_MAX)

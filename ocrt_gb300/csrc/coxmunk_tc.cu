@@ -373,4 +373,4 @@ bool coxmunk_tc_supported(int Mtab, int nphi, bool dw)
 
 int coxmunk_tc_pairs_per_cta() { return CMT_P; }
 
-int coxmunk_tc_threads(bool dw) { return dw ? CMT_THREADS_DW : CMT_THREADS; }
+int coxmunk_tc_threads(bool dw) { (void)dw; return CMT_THREADS_DW; }
