@@ -336,6 +336,7 @@ struct Group {
     float *F = nullptr, *J = nullptr, *ops = nullptr;
     float *opt = nullptr;    // pre-split operator tiles of the tensor-core pass (2 x wave_ops floats)
     bool tabs_tc = false;    // phase tables on tcgen05 (k_tables_tc)
+    bool keep_tot = false;   // keep the order totals at every level (set before build_group)
     float *gtab = nullptr;   // its Gauss bases in the chunk order (k_basis_perm)
     float *atab = nullptr;   // and the Gauss rows of its A tiles, split and swizzled
     double *gcoef = nullptr; // GSF recurrence step coefficients per (m, l) (k_gsf_coefs)
@@ -439,6 +440,8 @@ int build_group(Group &g, const ocrt_case *cases, const ocrt_opts *opts, int opp
     std::vector<double> ldt, lss, hcot, hlv, hlr;
     const Geom G = make_geom(g.N, g.E);
     g.G = G;
+    // forward-only plans keep the order totals at the output levels alone
+    g.G.tot_all = (ncot > 0 || g.keep_tot) ? 1 : 0;
     g.P = (int)g.idx.size();
     std::vector<double> mb, mgv, ma, mz, vth, vp11;
     size_t lev = 0, coef = 0;
@@ -1962,6 +1965,8 @@ int ocean_solve(int n, const ocrt_case *cases, const ocrt_opts *opts, int opp, c
     // ---- pass 1: atmosphere over the rough surface, bottom field exported ----
     plan.groups.resize(3);
     Group &GA = plan.groups[0], &GW = plan.groups[1], &GC = plan.groups[2];
+    // the interface coupling reads the totals at level 1 (k_edges)
+    GA.keep_tot = GW.keep_tot = GC.keep_tot = true;
     for (int i = 0; i < n; ++i) { GA.idx.push_back(i); GW.idx.push_back(i); GC.idx.push_back(i); }
     GA.N = GW.N = GC.N = Nw;
     GA.E = GC.E = 1;

@@ -99,6 +99,10 @@ struct Geom {
     int CIN;                // 6N weighted input columns (operator row stride)
     int COUT;               // 6N + 6E output columns
     int NP;                 // operator rows, COUT rounded up to 16
+    // 1: the order totals are kept at every level (the adjoint reads them,
+    // the coupled ocean reads level 1); 0: only at the TOA and BOA output
+    // levels, the interior ones neither read nor written
+    int tot_all;
 };
 
 __host__ __device__ inline Geom make_geom(int N, int E = 1)
@@ -114,6 +118,7 @@ __host__ __device__ inline Geom make_geom(int N, int E = 1)
     // costs DRAM two lines
     g.LDC = (g.COUT + 31) & ~31;
     g.NP = (g.COUT + 15) & ~15;
+    g.tot_all = 1;
     return g;
 }
 

@@ -242,6 +242,17 @@ size_t adj_mol_smem_bytes(const Geom &G);
 
 __global__ void k_primary(BatchBufs B, WaveBufs W, Geom G, int t0);
 __global__ void k_primary4(BatchBufs B, WaveBufs W, Geom G, int t0);   // N % 4 == 0, no flat surface, quad weights
+// The order-1 source and transport step with the rounding sequence fixed
+// (no contraction left to the compiler), so k_primary and k_primary4 give the
+// same bits: J = ch (x fa + y fm), I' = T I + Ca J + Cb J'.
+__device__ __forceinline__ float prim_source(float lc, float lx, float ly, float fa, float fm)
+{
+    return __fmul_rn(lc, __fmaf_rn(lx, fa, __fmul_rn(ly, fm)));
+}
+__device__ __forceinline__ float prim_step(float T, float I, float A, float J, float Bw, float Jp)
+{
+    return __fmaf_rn(T, I, __fmaf_rn(A, J, __fmul_rn(Bw, Jp)));
+}
 
 // lut.cu (angle-grid LUT mode)
 struct LutBufs {

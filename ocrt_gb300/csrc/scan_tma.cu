@@ -59,10 +59,11 @@ __host__ __device__ inline StmLayout stm_layout(const Geom &G, int CH)
 }
 
 // bytes the tensor copies of one stage deliver (boxes are always whole, the
-// out-of-range part zero-filled)
-__host__ __device__ inline uint32_t stm_stage_tx(const Geom &G, int CH)
+// out-of-range part zero-filled), with or without the total's boxes
+__host__ __device__ inline uint32_t stm_stage_tx(const Geom &G, int CH, bool tot = true)
 {
-    return 2u * (uint32_t)CH * 4u * (uint32_t)(2 * 3 * G.N + 2 * scan_tma_zw(G) + scan_tma_cw(G));
+    const int nt = tot ? 2 : 1;
+    return 2u * (uint32_t)CH * 4u * (uint32_t)(nt * 3 * G.N + nt * scan_tma_zw(G) + scan_tma_cw(G));
 }
 
 __device__ __forceinline__ void tma2(void *dst, const CUtensorMap *m, int x, int y, uint64_t *bar)
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
     const int ncw = nthr / 32 - 1;                       // column warps; the last warp's lane 0 produces
     const bool producer = tid == nthr - 32;
     const int N = G.N, NR = G.NR, ZW = scan_tma_zw(G), CW = scan_tma_cw(G);
-    const uint32_t TX = stm_stage_tx(G, CH);
+    const uint32_t TX = stm_stage_tx(G, CH), TXJ = stm_stage_tx(G, CH, false);
     const int n_items = B.active_cnt[it - 1];
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], ncw); }
@@ -168,16 +169,19 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
             const uint32_t pos = issued, sl = pos % NS;
             if (pos >= (uint32_t)NS && !mbar_wait(&empty[sl], ((pos / NS) - 1) & 1)) return false;
             unsigned char *stg = base + (size_t)sl * Ly.stage;
-            mbar_expect_tx(&full[sl], TX);
+            // the total's boxes only where it is kept: the first and last chunk
+            // hold the output levels of both directions
+            const bool wt = G.tot_all || q == 0 || q == nq - 1;
+            mbar_expect_tx(&full[sl], wt ? TX : TXJ);
 #pragma unroll
             for (int dd = 0; dd < 2; ++dd) {
                 unsigned char *db = stg + dd * Ly.dir;
                 const int r = dd == 0 ? nt - q * CH - CH + 1 : q * CH;       // first level row of the box
                 const int ly = dd == 0 ? r : q * CH - 1;                      // first layer of the box
                 tma4(db + Ly.jg, &M.jg, 0, dd, 0, row0 + r, &full[sl]);
-                tma4(db + Ly.tg, &M.tg, 0, dd, 0, row0 + r, &full[sl]);
+                if (wt) tma4(db + Ly.tg, &M.tg, 0, dd, 0, row0 + r, &full[sl]);
                 tma2(db + Ly.jz, &M.jz, 6 * N, row0 + r, &full[sl]);
-                tma2(db + Ly.tz, &M.tz, 6 * N, row0 + r, &full[sl]);
+                if (wt) tma2(db + Ly.tz, &M.tz, 6 * N, row0 + r, &full[sl]);
                 tma2(db + Ly.cf, &M.cq, 0, lay0 + ly, &full[sl]);
             }
             issued = pos + 1;
@@ -246,7 +250,6 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
                         const int r = h == 0 ? CH - 1 - jj : jj;   // box row of level k (and of its layer)
                         const int k = h == 0 ? nt - j : j;
                         const float jv = *(const float *)(vj + r * vrow);
-                        const float ov = *(const float *)(vt + r * vrow);
                         if (j > 0) {
                             const float *cw = (const float *)(vc + r * crow);
                             I = cw[0] * I + cw[4] * jv + cw[8] * Jp;
@@ -254,17 +257,16 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
                         Jp = jv;
                         const size_t o = (size_t)k * G.LDC + c;
                         F[o] = I;
-                        float t;
                         if (k == 0 || k == nt) {
+                            const float ov = *(const float *)(vt + r * vrow);
                             const float2 td = df_add(make_float2(ov, k == 0 ? lo0 : loN), I);
-                            t = td.x;
+                            Tot[o] = td.x;
                             *(k == 0 ? tl0 : tlN) = td.y;
-                        } else {
-                            t = ov + I;
+                            mt = fmaxf(mt, fabsf(td.x));
+                        } else if (G.tot_all) {
+                            Tot[o] = *(const float *)(vt + r * vrow) + I;
                         }
-                        Tot[o] = t;
                         mi = fmaxf(mi, fabsf(I));
-                        mt = fmaxf(mt, fabsf(t));
                     }
                 }
                 __syncwarp();

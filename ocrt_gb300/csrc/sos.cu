@@ -117,20 +117,20 @@ __global__ void __launch_bounds__(512, 1) k_primary(BatchBufs B, WaveBufs W, Geo
         for (int q = 0; q < PF; ++q) {
             if (q < cnt) {
                 const int j = j0 + q, k = h == 0 ? nt - j : j;
-                float Jk = lc[q] * (lx[q] * faP + ly[q] * fmP);
-                if (Jdt) Jk += Jdt[(size_t)k * G.LDC + c];
+                float Jk = prim_source(lc[q], lx[q], ly[q], faP, fmP);
+                if (Jdt) Jk = __fadd_rn(Jk, Jdt[(size_t)k * G.LDC + c]);
                 if (d.flat && !d.bottom_only && ((h == 0 && k < nt) || (h == 1 && k >= 1))) {
                     const double beam = sb * exp(hh[k] / d.mu0);
                     Jk += (float)(beam * (RI * (lx[q] * fa1 + ly[q] * fm1) + RQ * (lx[q] * fa2 + ly[q] * fm2)));
                 }
                 if (!isfinite(Jk)) bad = 1;
-                if (j > 0) I = tv[q] * I + av[q] * Jk + bv[q] * Jp;
+                if (j > 0) I = prim_step(tv[q], I, av[q], Jk, bv[q], Jp);
                 Jp = Jk;
                 float2 t = make_float2(I, 0.f);
-                if (seeded) t = df_add(t, fs_tdn * ea[q] * rs);
-                if (extb) t = df_add(t, exv * ea[q]);
+                if (seeded) t = df_add(t, __fmul_rn(__fmul_rn(fs_tdn, ea[q]), rs));
+                if (extb) t = df_add(t, __fmul_rn(exv, ea[q]));
                 F[(size_t)k * G.LDC + c] = t.x;
-                Tot[(size_t)k * G.LDC + c] = t.x;
+                if (G.tot_all || k == 0 || k == nt) Tot[(size_t)k * G.LDC + c] = t.x;
                 if (k == 0 || k == nt) W.Ttl[tot_tail_off(tk, G, k, c)] = t.y;
             }
         }
@@ -211,24 +211,25 @@ __device__ __forceinline__ void primary_cols(const BatchBufs &B, const WaveBufs 
                 float tx[WD], ty[WD];
 #pragma unroll
                 for (int u = 0; u < WD; ++u) {
-                    float Jk = lc[q] * (lx[q] * faP[u] + ly[q] * fmP[u]);
-                    if (Jdt) Jk += jd[q][u];
+                    float Jk = prim_source(lc[q], lx[q], ly[q], faP[u], fmP[u]);
+                    if (Jdt) Jk = __fadd_rn(Jk, jd[q][u]);
                     if (!isfinite(Jk)) bad = 1;
-                    if (j > 0) I[u] = tv[q][u] * I[u] + av[q][u] * Jk + bv[q][u] * Jp[u];
+                    if (j > 0) I[u] = prim_step(tv[q][u], I[u], av[q][u], Jk, bv[q][u], Jp[u]);
                     Jp[u] = Jk;
                     float2 t = make_float2(I[u], 0.f);
-                    if (seeded) t = df_add(t, fs_tdn * ea[q][u] * rs[u]);
-                    if (extb) t = df_add(t, exv[u] * ea[q][u]);
+                    if (seeded) t = df_add(t, __fmul_rn(__fmul_rn(fs_tdn, ea[q][u]), rs[u]));
+                    if (extb) t = df_add(t, __fmul_rn(exv[u], ea[q][u]));
                     tx[u] = t.x; ty[u] = t.y;
                 }
                 const size_t o = (size_t)k * G.LDC;
+                const bool wt = G.tot_all || k == 0 || k == nt;
                 if (WD == 4) {
                     const float4 v = make_float4(tx[0], tx[WD > 1 ? 1 : 0], tx[WD > 2 ? 2 : 0], tx[WD - 1]);
                     *reinterpret_cast<float4 *>(Fp + o) = v;
-                    *reinterpret_cast<float4 *>(Tp + o) = v;
+                    if (wt) *reinterpret_cast<float4 *>(Tp + o) = v;
                 } else {
                     Fp[o] = tx[0];
-                    Tp[o] = tx[0];
+                    if (wt) Tp[o] = tx[0];
                 }
                 if (k == 0 || k == nt) {
 #pragma unroll
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
             const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
             const size_t o = (size_t)k * G.LDC + c;
             cp_async4(Js + sl * bs + c, J + o);
-            cp_async4(Ts + sl * bs + c, Tot + o);
+            if (G.tot_all || k == 0 || k == nt) cp_async4(Ts + sl * bs + c, Tot + o);
             if (j > 0) {
                 const int e = (h == 0 ? k : k - 1) * NR + g;
                 cp_async4(Cs + (sl * 3 + 0) * bs + c, Tc + e);
@@ -523,8 +524,8 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
         }
     }
     __syncthreads();
-    // sup norms in FP32: the order field is FP32, and the total's head carries
-    // the total to 2^-24 relative
+    // sup norms in FP32: the order field over every level; the total over
+    // the output levels (TOA and BOA), whose heads carry it to 2^-24 relative
     float mi = 0.f, mt = 0.f;
     int bad = 0;
     if (valid) {
@@ -533,23 +534,21 @@ __global__ void __launch_bounds__(512, 2) k_scan(BatchBufs B, WaveBufs W, Geom G
             cp_async_wait<SCAN_DEPTH - 1>();
             const int k = h == 0 ? nt - j : j, sl = j & (SCAN_DEPTH - 1);
             const float jv = Js[sl * bs + c];
-            const float ov = Ts[sl * bs + c];
             if (j > 0)
                 I = Cs[(sl * 3 + 0) * bs + c] * I + Cs[(sl * 3 + 1) * bs + c] * jv + Cs[(sl * 3 + 2) * bs + c] * Jp;
             Jp = jv;
             const size_t o = (size_t)k * G.LDC + c;
             F[o] = I;
-            float t;
             if (k == 0 || k == nt) {
+                const float ov = Ts[sl * bs + c];
                 const float2 td = df_add(make_float2(ov, k == 0 ? lo0 : loN), I);
-                t = td.x;
+                Tot[o] = td.x;
                 *(k == 0 ? tl0 : tlN) = td.y;
-            } else {
-                t = ov + I;
+                mt = fmaxf(mt, fabsf(td.x));
+            } else if (G.tot_all) {
+                Tot[o] = Ts[sl * bs + c] + I;
             }
-            Tot[o] = t;
             mi = fmaxf(mi, fabsf(I));
-            mt = fmaxf(mt, fabsf(t));
             issue(j + SCAN_DEPTH);
         }
         cp_async_wait<0>();
@@ -611,9 +610,10 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
             const int k = h == 0 ? nt - j : j, sl = j & (SCAN4_DEPTH - 1);
             const size_t o = (size_t)k * G.LDC + c;
             const int layer = h == 0 ? k : k - 1;
+            const bool wt = G.tot_all || k == 0 || k == nt;
             if (quad) {
                 cp_async16_cg(slot(sl, 0), J + o);
-                cp_async16_cg(slot(sl, 1), Tot + o);
+                if (wt) cp_async16_cg(slot(sl, 1), Tot + o);
                 if (j > 0) {
                     const float *q = Cq + (size_t)layer * coef_quad_width(NR);
                     cp_async16_ca(slot(sl, 2), q);
@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
                 }
             } else {
                 cp_async4(&slot(sl, 0)->x, J + o);
-                cp_async4(&slot(sl, 1)->x, Tot + o);
+                if (wt) cp_async4(&slot(sl, 1)->x, Tot + o);
                 if (j > 0) {
                     const int e = layer * NR + g;
                     cp_async4(&slot(sl, 2)->x, Tc + e);
@@ -690,7 +690,6 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
             Jp = jv;
             const size_t o = (size_t)k * G.LDC + c;
             *reinterpret_cast<float4 *>(F + o) = I;
-            float4 t;
             if (k == 0 || k == nt) {
                 const bool top = k == 0;
                 float *tp = top ? tl0 : tlN;
@@ -699,13 +698,13 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
                 const float2 e = df_add(make_float2(ov.z, top ? lo0[2] : loN[2]), I.z);
                 const float2 f = df_add(make_float2(ov.w, top ? lo0[3] : loN[3]), I.w);
                 tp[0] = a.y; tp[1] = b.y; tp[2] = e.y; tp[3] = f.y;
-                t = make_float4(a.x, b.x, e.x, f.x);
-            } else {
-                t = make_float4(ov.x + I.x, ov.y + I.y, ov.z + I.z, ov.w + I.w);
+                const float4 t = make_float4(a.x, b.x, e.x, f.x);
+                *reinterpret_cast<float4 *>(Tot + o) = t;
+                mt = fmaxf(mt, fmaxf(fmaxf(fabsf(t.x), fabsf(t.y)), fmaxf(fabsf(t.z), fabsf(t.w))));
+            } else if (G.tot_all) {
+                *reinterpret_cast<float4 *>(Tot + o) = make_float4(ov.x + I.x, ov.y + I.y, ov.z + I.z, ov.w + I.w);
             }
-            *reinterpret_cast<float4 *>(Tot + o) = t;
             mi = fmaxf(mi, fmaxf(fmaxf(fabsf(I.x), fabsf(I.y)), fmaxf(fabsf(I.z), fabsf(I.w))));
-            mt = fmaxf(mt, fmaxf(fmaxf(fabsf(t.x), fabsf(t.y)), fmaxf(fabsf(t.z), fabsf(t.w))));
             issue(j + SCAN4_DEPTH);
         }
         cp_async_wait<0>();
@@ -720,17 +719,15 @@ __global__ void __launch_bounds__(128, 4) k_scan4(BatchBufs B, WaveBufs W, Geom 
             Jp = jv;
             const size_t o = (size_t)k * G.LDC + c;
             F[o] = I;
-            float t;
             if (k == 0 || k == nt) {
                 const float2 td = df_add(make_float2(ov, k == 0 ? lo0[0] : loN[0]), I);
-                t = td.x;
+                Tot[o] = td.x;
                 *(k == 0 ? tl0 : tlN) = td.y;
-            } else {
-                t = ov + I;
+                mt = fmaxf(mt, fabsf(td.x));
+            } else if (G.tot_all) {
+                Tot[o] = ov + I;
             }
-            Tot[o] = t;
             mi = fmaxf(mi, fabsf(I));
-            mt = fmaxf(mt, fabsf(t));
             issue(j + SCAN4_DEPTH);
         }
         cp_async_wait<0>();
