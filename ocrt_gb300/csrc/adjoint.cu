@@ -15,7 +15,9 @@
 // checkpoints per mode: the order total F_tot and the last order's field
 // (their difference is the field that was scattered), not every order.
 //
-//   k_adj_prep      Xs = F_tot - F_last into the field buffer (the scattered field)
+//   k_adj_prep      Xs = F_tot - F_last into the field buffer (the scattered field),
+//                   where a CUDA-core source pass reads it; the tensor-core pass
+//                   (k_source_tc_xs) and k_adj_grad form it from the total instead
 //   k_fill_all      every task active, for one extra source pass J_tot = S Xs
 //   k_adj_init      a_1 = e: the output weights at the TOA view column(s)
 //   k_adj_scan      transposed transport of a_j (recurrences run the other way),
@@ -200,6 +202,10 @@ __global__ void k_adj_init(BatchBufs B, AdjBufs A, Geom G, int t0, int nadj)
     double w[3];
     mode_weights(d, tk.m, A.cot + ((size_t)tk.pix * A.ncot + r) * 3, w);
     float *a = A.AF + adj_off(tk, G, A.ncot, r);
+    // The adjoint buffers are not cleared per execute: order 1 reads a_1 at
+    // the TOA row alone (every other level of a_1 is zero), so that row is
+    // written here in full.
+    for (int c = 0; c < G.LDC; ++c) a[c] = 0.f;
     if (d.view_slot >= 0) {
         for (int s = 0; s < 3; ++s) a[col_of(G, s, 0, d.view_slot)] = (float)w[s];
     } else {
@@ -304,9 +310,11 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
 #pragma unroll
             for (int q = 0; q < ADJ_RB; ++q) {
                 if (!act[q]) continue;
-                const float av = has_a ? As[(sl * ADJ_RB + q) * bs + c] : 0.f;
+                // order 1: a_1 is zero below the TOA row and the total starts
+                // at a_1 (neither buffer is cleared beforehand)
+                const float av = has_a && (j > 1 || k == 0) ? As[(sl * ADJ_RB + q) * bs + c] : 0.f;
                 if (has_a) {
-                    const float t = Ts[(sl * ADJ_RB + q) * bs + c] + av;
+                    const float t = (j > 1 ? Ts[(sl * ADJ_RB + q) * bs + c] : 0.f) + av;
                     At[q][o] = t;
                     if (clear) a[q][o] = 0.f;
                     mi[q] = fmaxf(mi[q], fabsf(av));
@@ -323,6 +331,13 @@ __global__ void __launch_bounds__(512, 1) k_adj_scan(BatchBufs B, AdjBufs A, Geo
 #pragma unroll
             for (int q = 0; q < ADJ_RB; ++q)
                 if (act[q]) A.bc[(size_t)(tl * A.ncot + r0 + q) * NR * 3 + g * 3 + s] = nup[q];
+    } else if (j == 1 && c < G.LDC) {
+        // columns no order writes (unused ring slots, the row padding): zero
+        // once, as the transposed source reads whole muJ rows
+#pragma unroll
+        for (int q = 0; q < ADJ_RB; ++q)
+            if (act[q])
+                for (int k = 0; k <= nt; ++k) mj[q][(size_t)k * G.LDC + c] = 0.f;
     }
 #pragma unroll
     for (int q = 0; q < ADJ_RB; ++q) {
@@ -562,7 +577,8 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact_adj(AdjBufs A, int 
 // so every warp runs one direction.  Per-warp level sums sit in shared memory
 // [warp][3][nt + 1] and are added in warp order, so the result does not
 // depend on scheduling.
-__global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb)
+__global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb,
+                                                  int xs_in_f)
 {
     // One block per (task, group of rb <= ADJ_RB cotangent rows): the forward
     // totals, sources and coefficients a level's terms need are loaded once
@@ -712,14 +728,18 @@ __global__ void __launch_bounds__(512) k_adj_grad(BatchBufs B, WaveBufs W, AdjBu
 #pragma unroll
     for (int r = 0; r < ADJ_RB; ++r) { gW[r] = 0.0; gS[r] = 0.0; }
     if (valid && h == 0 && d.rough) {
-        const float *Xb = W.F + tk.fld_off + (size_t)nt * G.LDC;
+        // the scattered field at the BOA: in F when k_adj_prep ran, else
+        // formed as k_adj_prep forms it
+        const float *Fb = W.F + tk.fld_off + (size_t)nt * G.LDC, *Tb = W.Tot + tk.fld_off + (size_t)nt * G.LDC;
+        const float *Lb = W.Ttl + tk.tail_off + G.LDC;
+        auto Xb = [&](int cc) -> float { return xs_in_f ? Fb[cc] : (Tb[cc] - Fb[cc]) + Lb[cc]; };
         const float *RW = A.srfW + tk.srf_off + (size_t)g * N * 9 + s * 3;
         const float *pwm = B.pw + (tk.m == 0 ? 0 : N);
         float accf = 0.f;          // FP32 like the boundary condition it differentiates
         for (int i = 0; i < N; ++i) {
             const float *Ri = RW + (size_t)i * 9;
-            accf += pwm[i] * (Ri[0] * Xb[col_of(G, 0, 1, i)] + Ri[1] * Xb[col_of(G, 1, 1, i)] +
-                              Ri[2] * Xb[col_of(G, 2, 1, i)]);
+            accf += pwm[i] * (Ri[0] * Xb(col_of(G, 0, 1, i)) + Ri[1] * Xb(col_of(G, 1, 1, i)) +
+                              Ri[2] * Xb(col_of(G, 2, 1, i)));
         }
         const double acc = accf;
         const double tdn = exp(-d.tau_total / d.mu0);
@@ -777,13 +797,28 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
         psm[k] = v;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double acc = 0.0;
-        psm[nt + 1] = 0.0;
-        for (int k = nt; k >= 0; --k) { acc += psm[k]; psm[k] = acc; }     // psm[k] = sum_{k' >= k}
+    if (threadIdx.x < 32) {
+        // warp 0: the suffix sums and the per-pixel terms, modes over lanes
+        const unsigned full = 0xffffffffu;
+        const int lane = threadIdx.x;
+        // psm[k] = sum_{k' >= k} psm[k']: each lane takes a contiguous segment
+        // of levels, the segment totals are combined by a warp suffix scan
+        const int L1 = nt + 1, seg = (L1 + 31) / 32;
+        const int k0 = min(L1, lane * seg), k1 = min(L1, k0 + seg);
+        double part = 0.0;
+        for (int k = k1 - 1; k >= k0; --k) part += psm[k];
+        double incl = part;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double v = __shfl_down_sync(full, incl, o);
+            if (lane + o < 32) incl += v;
+        }
+        double acc = __shfl_down_sync(full, incl, 1);
+        if (lane == 31) acc = 0.0;
+        for (int k = k1 - 1; k >= k0; --k) { acc += psm[k]; psm[k] = acc; }
+        if (lane == 0) psm[nt + 1] = 0.0;
         // direct terms: the removed view seed and the sunglint
         double dt = 0.0, dw = 0.0, seed_sum = 0.0, gw_sum = 0.0;
-        for (int m = 0; m <= M; ++m) {
+        for (int m = lane; m <= M; m += 32) {
             seed_sum += gout(m)[3 * A.kstride + 1];
             gw_sum += gout(m)[3 * A.kstride + 0];
         }
@@ -798,7 +833,7 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
                 bracket_a(B.gmu, N, d.mu_view, lo, hi, t);
                 cols[0] = lo; cw[0] = 1.0 - t; cols[1] = hi; cw[1] = t; nc = 2;
             }
-            for (int m = 0; m <= M; ++m) {
+            for (int m = lane; m <= M; m += 32) {
                 const TaskDev &tk = B.tasks[d.task0 + m];
                 double w[3];
                 mode_weights(d, m, cot, w);
@@ -817,24 +852,31 @@ __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, 
                     }
                 }
             }
-            if (!d.decouple) {
-                const double phi_v = (d.raa_deg - 180.0) * OCRT_PI / 180.0;
-                const double mv = d.vza_deg > 0.0 ? d.mu_view : 1.0;
-                double gl[3];
-                sunglint(d, mv, phi_v, d.tau_total, gl);
-                const double yg = cot[0] * gl[0] + cot[1] * gl[1] - cot[2] * gl[2];
-                dt -= yg * (1.0 / d.mu0 + 1.0 / mv);
-                PixDev dp = d, dm = d;
-                const double hW = 1e-5 * d.wind;
-                dp.wind = d.wind + hW; dm.wind = d.wind - hW;
-                double gp[3], gm[3];
-                sunglint(dp, mv, phi_v, d.tau_total, gp);
-                sunglint(dm, mv, phi_v, d.tau_total, gm);
-                dw += (cot[0] * (gp[0] - gm[0]) + cot[1] * (gp[1] - gm[1]) - cot[2] * (gp[2] - gm[2])) / (2.0 * hW);
-            }
         }
-        dir[0] = dt;
-        dir[1] = dw;
+        for (int o = 16; o > 0; o >>= 1) {
+            dt += __shfl_xor_sync(full, dt, o);
+            dw += __shfl_xor_sync(full, dw, o);
+        }
+        if (d.rough && !d.decouple) {
+            // lanes 0, 1, 2: the sunglint at W, W + h, W - h
+            const double phi_v = (d.raa_deg - 180.0) * OCRT_PI / 180.0;
+            const double mv = d.vza_deg > 0.0 ? d.mu_view : 1.0;
+            const double hW = 1e-5 * d.wind;
+            double gl[3] = {0.0, 0.0, 0.0};
+            if (lane < 3) {
+                PixDev dv = d;
+                dv.wind = lane == 0 ? d.wind : lane == 1 ? d.wind + hW : d.wind - hW;
+                sunglint(dv, mv, phi_v, d.tau_total, gl);
+            }
+            const double yv = cot[0] * gl[0] + cot[1] * gl[1] - cot[2] * gl[2];
+            const double yp = __shfl_sync(full, yv, 1), ym = __shfl_sync(full, yv, 2);
+            dt -= yv * (1.0 / d.mu0 + 1.0 / mv);
+            dw += (yp - ym) / (2.0 * hW);
+        }
+        if (lane == 0) {
+            dir[0] = dt;
+            dir[1] = dw;
+        }
     }
     __syncthreads();
     double *out = A.grad + ((size_t)q * A.ncot + r) * A.grad_stride;

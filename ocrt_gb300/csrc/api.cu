@@ -785,20 +785,25 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     const Geom G = g.G;
     const int nw = w.t1 - w.t0, na = nw * g.ncot;
     const int scan_threads = ((G.COUT + 31) / 32) * 32;
-    // the scattered field Xs = F_tot - F_last and its source S Xs = J_tot - J_1
-    LAUNCH(plan, KC_ADJ_TOTALS, k_adj_prep<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
+    // the scattered field Xs = F_tot - F_last and its source S Xs = J_tot - J_1;
+    // the tensor-core pass forms Xs from the total as it loads the rows, the
+    // CUDA-core passes read it from F (k_adj_prep)
+    const bool xs_in_f = w.n_simt > 0 || w.n_tc == 0;
+    if (xs_in_f) LAUNCH(plan, KC_ADJ_TOTALS, k_adj_prep<<<nw, scan_threads, 0, st>>>(B, W, G, w.t0));
     const int it = g.max_orders + 1;
     LAUNCH(plan, KC_ADJ_TOTALS, k_fill_all<<<1, 256, 0, st>>>(B, w.t0, nw, it));
     if (w.n_simt) LAUNCH(plan, KC_ADJ_TOTALS, k_source_simt<<<sgrid, 256, 0, st>>>(B, W, G, w.t0, it));
-    if (w.n_tc)
+    if (w.n_tc && xs_in_f)
         LAUNCH(plan, KC_ADJ_TOTALS, k_source_tc<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(B, W, G, w.t0, it, mtiles));
+    else if (w.n_tc)
+        LAUNCH(plan, KC_ADJ_TOTALS,
+               k_source_tc_xs<<<tc_grid, tc_fwd_threads(), tc_smem, st>>>(B, W, G, w.t0, it, mtiles));
     if (w.n_mol && !w.n_tc)
         LAUNCH(plan, KC_ADJ_TOTALS, k_mol_lowrank<<<mol_grid, 256, mol_smem_bytes(G), st>>>(
                    B, W, G, w.t0, it, ltiles, g.Bp, g.Br, g.Bt, g.Lmax));
-    // adjoint successive orders
-    CK(cudaMemsetAsync(g.AF, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.AJ, 0, sizeof(float) * w.fld * g.ncot, st));
-    CK(cudaMemsetAsync(g.ATot, 0, sizeof(float) * w.fld * g.ncot, st));
+    // adjoint successive orders (the adjoint field, source and total are not
+    // cleared: k_adj_init writes a_1's TOA row, order 1 reads no other row of
+    // a_1 nor the total, and its scan zeroes the muJ columns no order writes)
     CK(cudaMemsetAsync(g.Abc, 0, sizeof(float) * (size_t)na * G.NR * 3, st));
     CK(cudaMemsetAsync(g.acnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
     CK(cudaMemsetAsync(g.awork, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
@@ -852,7 +857,7 @@ int run_adjoint_wave(ocrt_plan *plan, Group &g, Wave &w, const BatchBufs &B, con
     const size_t row_smem = sizeof(float) * 3 * ((size_t)g.ntmax + 1) * (grad_threads / 32);
     const int grad_rb = std::max(1, std::min({ADJ_RB, g.ncot, (int)((200 * 1024) / row_smem)}));
     LAUNCH(plan, KC_ADJ_GRAD, k_adj_grad<<<nw * ((g.ncot + grad_rb - 1) / grad_rb), grad_threads, row_smem * grad_rb, st>>>(
-               B, W, A, G, w.t0, grad_rb));
+               B, W, A, G, w.t0, grad_rb, xs_in_f ? 1 : 0));
     LAUNCH(plan, KC_ADJ_GRAD, k_adj_pixel<<<(w.p1 - w.p0) * g.ncot, 256, sizeof(double) * (g.ntmax + 2), st>>>(
                B, W, A, G, w.p0, w.t0));
     return OCRT_OK;
@@ -953,8 +958,9 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         const int nw = w.t1 - w.t0;
         if (!capture) w.fwd_stop = INT_MAX;
         // the plain operators are read only off the forward tensor-core path; the
-        // molecular factors it reads are written in full by k_tables
-        if (!g.use_tc || g.ncot > 0) CK(cudaMemsetAsync(g.ops, 0, sizeof(float) * w.ops, st));
+        // molecular factors it reads are written in full by k_tables, and
+        // k_tables_tc writes every row of the plain operator it keeps
+        if (!g.use_tc || (g.ncot > 0 && !g.tabs_tc)) CK(cudaMemsetAsync(g.ops, 0, sizeof(float) * w.ops, st));
         CK(cudaMemsetAsync(g.pvec, 0, sizeof(float) * (size_t)nw * 2 * G.LDC, st));
         if (g.any_flat) CK(cudaMemsetAsync(g.fvec, 0, sizeof(float) * (size_t)nw * 24 * G.NR, st));
         CK(cudaMemsetAsync(g.active_cnt, 0, sizeof(int) * ((size_t)g.max_orders + 2), st));
@@ -1218,6 +1224,7 @@ int ocrt_gb_init(int device)
     CK(scan_tma_init());
     CK(cudaFuncSetAttribute(k_adj_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_source_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    CK(cudaFuncSetAttribute(k_source_tc_xs, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     CK(cudaFuncSetAttribute(k_mol_lowrank, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_mol, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     CK(cudaFuncSetAttribute(k_adj_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

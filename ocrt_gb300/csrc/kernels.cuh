@@ -236,7 +236,7 @@ __global__ void k_adj_mol(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0,
 __global__ void k_adj_surface(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int j);
 __global__ void k_adj_list_all(AdjBufs A, int nw);
 __global__ void k_compact_adj(AdjBufs A, int nw, int j);
-__global__ void k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb);
+__global__ void k_adj_grad(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int t0, int rb, int xs_in_f);
 __global__ void k_adj_pixel(BatchBufs B, WaveBufs W, AdjBufs A, Geom G, int p0, int t0);
 size_t adj_mol_smem_bytes(const Geom &G);
 
@@ -273,6 +273,7 @@ __global__ void k_source_simt(BatchBufs B, WaveBufs W, Geom G, int t0, int it);
 
 // tc_gemm.cu (tcgen05 source contraction for modes without a molecular term)
 __global__ void k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
+__global__ void k_source_tc_xs(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles);
 __global__ void k_adj_source_tc(BatchBufs B, WaveBufs W, AdjBufs AB, Geom G, int t0, int it, int mtiles, int nw);
 __global__ void k_op_transpose(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);
 __global__ void k_mol_utrans(const TaskDev *tasks, int t0, int nw, Geom G, const float *ops, float *opsT);

@@ -477,9 +477,11 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
                         ++slot;
                         const unsigned char *va = rb + (gauss ? 0 : 2 * Ly.g) + voff;
                         const unsigned char *vt = rb + (gauss ? Ly.g : 2 * Ly.g + Ly.z) + voff;
-                        const float av = has_a ? *(const float *)(va + rbx * vrow) : 0.f;
+                        // order 1: a_1 is zero below the TOA row and the total
+                        // starts at a_1 (neither buffer is cleared beforehand)
+                        const float av = has_a && (j > 1 || k == 0) ? *(const float *)(va + rbx * vrow) : 0.f;
                         if (has_a) {
-                            const float t = *(const float *)(vt + rbx * vrow) + av;
+                            const float t = (j > 1 ? *(const float *)(vt + rbx * vrow) : 0.f) + av;
                             At[rq][o] = t;
                             if (clear) a[rq][o] = 0.f;
                             mi[rq] = fmaxf(mi[rq], fabsf(av));
@@ -489,6 +491,17 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
                         mj[rq][o] = ca * nu + cb * nup[rq];
                         nup[rq] = nu;
                     }
+                }
+            } else if (j == 1 && c < G.LDC) {
+                // columns no order writes (unused ring slots, the row
+                // padding): zero once, as the transposed source reads whole
+                // muJ rows
+                for (int jj = 0; jj < CH; ++jj) {
+                    const int step = q * CH + jj;
+                    if (step > nt) break;
+#pragma unroll
+                    for (int rq = 0; rq < ADJ_RB; ++rq)
+                        if (act[rq]) mj[rq][(size_t)step * G.LDC + c] = 0.f;
                 }
             }
             __syncwarp();

@@ -441,6 +441,16 @@ k_tables_tc(const TaskDev *tasks, int t0, int nt_tasks, const PixDev *px, Geom G
                     hi[(size_t)G.NP * 32 + lane] = 0.f;
                 }
             }
+            // and the plain operator's rows of the unused slots (its buffer is
+            // not cleared beforehand)
+            if (plain) {
+                float *Aop = ops + tk.op_off;
+                const int nz0 = 6 * (G.NR - n), nkt = G.CIN / 32;
+                for (int y = ew; y < nz0 * nkt; y += TT_EW) {
+                    const int q = y / nkt, kt = y - q * nkt;
+                    Aop[(size_t)(6 * N + 6 * (n - N) + q) * G.CIN + kt * 32 + lane] = 0.f;
+                }
+            }
             tt_bar(1, TT_EW * 32);                                   // table reads done
         }
     }

@@ -62,7 +62,10 @@ using namespace tcg;
 //   epilogue a[row][cin] = x_k D[row][cin] + y_k sum_f V[4b+f][cin]
 //   D[row][CIN + 4b + f] (cin = bN + i) for cin < CIN; items = every task of
 //   the wave x tiles, skipped when none of its rows is active.
-template <bool ADJ>
+// XS = true (forward form only): the A rows are the adjoint's scattered field
+//   Xs = F_tot - F_last formed while loading, (Tot - F) plus the total's tail
+//   at the TOA and BOA rows, in the same FP32 operations k_adj_prep applies.
+template <bool ADJ, bool XS = false>
 __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBufs &W, const AdjBufs &AB,
                                                const Geom &G, int t0, int it, int mtiles, int nw)
 {
@@ -134,7 +137,7 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
         // NKT and Bm (dense molecular operator) for NKT .. nkt - 1
         // Bt / Btm: the pre-split operator tiles (forward: aerosol, dense
         // molecular; adjoint: transposed operator with U^T rows), tile row count tr
-        struct Opnd { const float *Ab, *Bt, *Btm; int nra, nbi, nkt; };
+        struct Opnd { const float *Ab, *Bt, *Btm, *Tb, *Tl; int nra, nbi, nkt, r0, nt; };
         const int tr = ADJ ? NB + 32 : NB;
         // K tile kt of the item into registers: A rows 0 .. nra - 1 of the item
         // (zero past the task and past a_cols), B rows 0 .. nbi - 1
@@ -146,6 +149,21 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
 #pragma unroll
             for (int i = 0; i < TC_AQ; ++i)
                 ra[i] = acol && r8 + 16 * i < o.nra ? __ldg(pa + (size_t)i * 4 * G.LDC) : make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (XS) {
+                const float4 *pt = reinterpret_cast<const float4 *>(o.Tb + (size_t)r8 * G.LDC + col);
+#pragma unroll
+                for (int i = 0; i < TC_AQ; ++i) {
+                    if (!(acol && r8 + 16 * i < o.nra)) continue;
+                    const float4 t = __ldg(pt + (size_t)i * 4 * G.LDC);
+                    float4 x = make_float4(t.x - ra[i].x, t.y - ra[i].y, t.z - ra[i].z, t.w - ra[i].w);
+                    const int k = o.r0 + r8 + 16 * i;
+                    if (k == 0 || k == o.nt) {
+                        const float4 lo = __ldg(reinterpret_cast<const float4 *>(o.Tl + (k == 0 ? 0 : G.LDC) + col));
+                        x.x = x.x + lo.x; x.y = x.y + lo.y; x.z = x.z + lo.z; x.w = x.w + lo.w;
+                    }
+                    ra[i] = x;
+                }
+            }
         };
         // split into tf32 (hi, lo) and store at byte offset off of the hi and lo tiles
         auto put = [&](unsigned char *hi, unsigned char *lo, uint32_t off, float4 v) {
@@ -203,6 +221,10 @@ __device__ __forceinline__ void source_tc_body(const BatchBufs &B, const WaveBuf
             o.Bt = ADJ ? AB.opsT + (size_t)tl * 2 * tr * b_ld : W.opt + 2 * tk.op_off;
             o.Btm = dbl ? W.opt + 2 * tk.uv_off : o.Bt;
             o.nkt = dbl ? 2 * NKT : NKT;
+            o.Tb = XS ? W.Tot + tk.fld_off + (size_t)r0 * G.LDC : nullptr;
+            o.Tl = XS ? W.Ttl + tk.tail_off : nullptr;
+            o.r0 = r0;
+            o.nt = tk.K - 1;
             return o;
         };
         if (pt == 0) fetch_publish(0);
@@ -442,6 +464,15 @@ k_source_tc(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles)
 {
     AdjBufs none{};
     source_tc_body<false>(B, W, none, G, t0, it, mtiles, 0);
+}
+
+// The adjoint's source of the scattered field, S Xs with Xs = F_tot - F_last
+// formed from the forward total and the last order while the rows load.
+__global__ void __launch_bounds__(TC_FWD_THREADS, 1)
+k_source_tc_xs(BatchBufs B, WaveBufs W, Geom G, int t0, int it, int mtiles)
+{
+    AdjBufs none{};
+    source_tc_body<false, true>(B, W, none, G, t0, it, mtiles, 0);
 }
 
 // Transposed contraction of the adjoint for adjoint order `it` (work counter
