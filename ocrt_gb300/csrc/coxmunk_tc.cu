@@ -12,15 +12,18 @@
 // into a second accumulator.
 //
 // K is swept in chunks of 32 azimuth nodes (one 128-byte swizzle row).  For a
-// chunk every thread evaluates two Mueller matrices (one in the wind-derivative
-// variant, whose larger stages leave room for one CTA per SM: 448 threads hide
-// the evaluation's latency there) on the CUDA cores (FP32,
-// the same coxmunk_R as the CUDA-core kernel) and stores the tf32 (hi, lo)
+// chunk every one of the 448 threads evaluates one Mueller matrix on the CUDA
+// cores (FP32, the same coxmunk_R as the CUDA-core kernel) and stores the tf32 (hi, lo)
 // split into the SWIZZLE_128B K-major A tiles, while a TMA bulk copy brings the
 // chunk's B tiles (the cos/sin table already split and swizzled once per
 // group by k_cs_tiles).  One thread then issues the three kind::tf32 MMAs per
-// 8-node slice (hi*hi + hi*lo + lo*hi).  Two stages: the MMAs of chunk c run
-// while chunk c + 1 is evaluated.  Gauss-Gauss pairs are evaluated once per
+// 8-node slice (hi*hi + hi*lo + lo*hi).  Two stages in the plain variant: the
+// MMAs of chunk c run while chunk c + 1 is evaluated.  The wind-derivative
+// variant's stage (four A tiles) is too large for two stages at two CTAs per
+// SM, so it keeps one: a CTA's MMAs and its next chunk's evaluation
+// alternate, and the second CTA on the SM fills the gaps (two CTAs of one
+// stage ran faster than one CTA of two: the evaluation, not the MMA, is the
+// long phase).  Gauss-Gauss pairs are evaluated once per
 // reciprocal couple and written both ways, as in k_coxmunk.  Every wait is
 // bounded by TC_WAIT_NS.
 #include <cuda.h>
@@ -33,7 +36,7 @@ using namespace tcg;
 
 #define CMT_P 14            // pairs per CTA (9 rows each)
 #define CMT_THREADS 224     // CMT_P x CMT_KC / 2: two Mueller evaluations per thread and chunk
-#define CMT_THREADS_DW 448  // CMT_P x CMT_KC: one per thread with the wind derivative (one CTA per SM)
+#define CMT_THREADS_DW 448  // CMT_P x CMT_KC: one Mueller evaluation per thread and chunk
 #define CMT_KC 32           // azimuth nodes per chunk
 
 // Pair constants of the Mueller evaluation (coxmunk_R in physics.cuh with
@@ -163,7 +166,8 @@ k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task
     const uint32_t A_BYTES = 128 * CMT_KC * 4, B_BYTES = (uint32_t)NN * CMT_KC * 4;
     const uint32_t STAGE = (dw ? 4u : 2u) * A_BYTES + 2u * B_BYTES;
     unsigned char *base = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *mma_done = (uint64_t *)(base + 2 * STAGE);         // [2]
+    const int NSTG = dw ? 1 : 2;                                 // operand stages (see above)
+    uint64_t *mma_done = (uint64_t *)(base + NSTG * STAGE);      // [2]
     uint64_t *fin = mma_done + 2;
     uint64_t *bfull = fin + 1;                                   // [2] B tiles of the stage landed
     uint32_t *tslot = (uint32_t *)(bfull + 2);
@@ -233,15 +237,15 @@ k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task
     const uint32_t idesc = idesc_tf32(128, NN);
     const int nchunk = half / CMT_KC;
     for (int c = 0; c < nchunk; ++c) {
-        const int s = c & 1;
+        const int s = dw ? 0 : (c & 1);
         unsigned char *sp = base + (size_t)s * STAGE;
         unsigned char *aH = sp, *aL = sp + A_BYTES;
         unsigned char *tH = sp + 2 * A_BYTES, *tL = sp + 3 * A_BYTES;             // R tan^2(beta) (wind derivative)
         unsigned char *bH = sp + (dw ? 4 : 2) * A_BYTES, *bL = bH + B_BYTES;
-        if (c >= 2) {
-            // every thread waits (bounded) for the MMAs that read this stage two
-            // chunks ago; the barrier makes the abort decision block-uniform
-            if (!mbar_wait(&mma_done[s], ((c >> 1) - 1) & 1)) *abort_flag = 1;
+        if (c >= NSTG) {
+            // every thread waits (bounded) for the MMAs that read this stage
+            // NSTG chunks ago; the barrier makes the abort decision block-uniform
+            if (!mbar_wait(&mma_done[s], ((c / NSTG) - 1) & 1)) *abort_flag = 1;
             __syncthreads();
             if (*abort_flag) break;
         }
@@ -281,7 +285,7 @@ k_coxmunk_tc(const TaskDev *tasks, const PixDev *px, int p0, const int *pix_task
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
-            const bool bok = mbar_wait(&bfull[s], (c >> 1) & 1);
+            const bool bok = mbar_wait(&bfull[s], (c / NSTG) & 1);
             if (!bok) *abort_flag = 1;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t sa_h = smem_u32(aH), sa_l = smem_u32(aL), st_h = smem_u32(tH), st_l = smem_u32(tL);
@@ -357,7 +361,7 @@ size_t coxmunk_tc_smem_bytes(int Mtab, bool dw)
 {
     const size_t NN = 2 * (size_t)((Mtab + 1 + 7) & ~7);
     const size_t stage = (dw ? 4 : 2) * (size_t)128 * CMT_KC * 4 + 2 * NN * CMT_KC * 4;
-    return 1024 + 2 * stage + 64 + 2 * 4 * CMT_P + 3 * 4 * CMT_P + sizeof(CmPair) * CMT_P + 16 + 8 * ((size_t)Mtab + 1);
+    return 1024 + (dw ? 1 : 2) * stage + 64 + 2 * 4 * CMT_P + 3 * 4 * CMT_P + sizeof(CmPair) * CMT_P + 16 + 8 * ((size_t)Mtab + 1);
 }
 
 size_t coxmunk_tc_tiles_floats(int Mtab, int nphi)
