@@ -211,10 +211,12 @@ bool force_simt()
 // the same arithmetic in the same order, so any of them (and any mix across
 // orders) gives identical results; they differ in how the per-level inputs
 // reach the threads.
-enum ScanKind { SK_COLUMN, SK_QUAD, SK_TMA_8_3, SK_TMA_8_4, SK_TMA_4_6, SK_TMA_16_2, SK_N };
-const char *sk_names[SK_N] = {"column", "quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2"};
-const int sk_ch[SK_N] = {0, 0, 8, 8, 4, 16};
-const int sk_ns[SK_N] = {0, 0, 3, 4, 6, 2};
+// The deeper rings (8x5, 4x10) fit three blocks per SM only where the order
+// totals stay at the output levels (smaller stages).
+enum ScanKind { SK_COLUMN, SK_QUAD, SK_TMA_8_3, SK_TMA_8_4, SK_TMA_4_6, SK_TMA_16_2, SK_TMA_8_5, SK_TMA_4_10, SK_N };
+const char *sk_names[SK_N] = {"column", "quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2", "tma8x5", "tma4x10"};
+const int sk_ch[SK_N] = {0, 0, 8, 8, 4, 16, 8, 4};
+const int sk_ns[SK_N] = {0, 0, 3, 4, 6, 2, 5, 10};
 inline int sk_map_index(int ch) { return ch == 4 ? 0 : ch == 8 ? 1 : 2; }
 
 // Resident blocks per SM of a chunked-scan variant at this geometry (0: does
@@ -222,7 +224,7 @@ inline int sk_map_index(int ch) { return ch == 4 ? 0 : ch == 8 ? 1 : 2; }
 int scan_tma_blocks(int kind, const Geom &G)
 {
     static std::map<std::vector<int>, int> cache;
-    const std::vector<int> key = {kind, G.N, G.E};
+    const std::vector<int> key = {kind, G.N, G.E, G.tot_all};
     const auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     const void *fn = scan_tma_fn(sk_ch[kind], sk_ns[kind]);
@@ -937,7 +939,7 @@ int run_group(ocrt_plan *plan, Group &g, cudaStream_t st, bool capture)
         const int forced = scan_forced();
         int kmax = 0;
         for (const Wave &w : g.waves) kmax = std::max(kmax, w.Kmax);
-        const std::vector<int> key = {G.N, G.E, kmax};
+        const std::vector<int> key = {G.N, G.E, kmax, G.tot_all};
         const int dflt = scan_cands.size() > 1 ? scan_cands[1] : scan_cands[0];
         if (forced >= 0 && std::find(scan_cands.begin(), scan_cands.end(), forced) != scan_cands.end()) {
             scan_pick = forced;

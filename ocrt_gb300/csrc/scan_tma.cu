@@ -46,14 +46,22 @@ struct StmLayout {
 
 __host__ __device__ inline uint32_t al128(uint32_t v) { return (v + 127u) & ~127u; }
 
+// Per direction: the source J's Gauss and zero-weight boxes, the order
+// total's (only where every level keeps its total, G.tot_all; otherwise the
+// two output rows of the total are read directly) and the weight box.
 __host__ __device__ inline StmLayout stm_layout(const Geom &G, int CH)
 {
     StmLayout L;
     const uint32_t gb = al128((uint32_t)(CH * 3 * G.N * 4));
     const uint32_t zb = al128((uint32_t)(CH * scan_tma_zw(G) * 4));
     const uint32_t cb = al128((uint32_t)(CH * scan_tma_cw(G) * 4));
-    L.jg = 0; L.tg = gb; L.jz = 2 * gb; L.tz = 2 * gb + zb; L.cf = 2 * gb + 2 * zb;
-    L.dir = 2 * gb + 2 * zb + cb;
+    if (G.tot_all) {
+        L.jg = 0; L.tg = gb; L.jz = 2 * gb; L.tz = 2 * gb + zb; L.cf = 2 * gb + 2 * zb;
+        L.dir = 2 * gb + 2 * zb + cb;
+    } else {
+        L.jg = 0; L.jz = gb; L.cf = gb + zb; L.tg = L.tz = 0;
+        L.dir = gb + zb + cb;
+    }
     L.stage = 2 * L.dir;
     return L;
 }
@@ -169,9 +177,8 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
             const uint32_t pos = issued, sl = pos % NS;
             if (pos >= (uint32_t)NS && !mbar_wait(&empty[sl], ((pos / NS) - 1) & 1)) return false;
             unsigned char *stg = base + (size_t)sl * Ly.stage;
-            // the total's boxes only where it is kept: the first and last chunk
-            // hold the output levels of both directions
-            const bool wt = G.tot_all || q == 0 || q == nq - 1;
+            // the total's boxes only where every level keeps it
+            const bool wt = G.tot_all != 0;
             mbar_expect_tx(&full[sl], wt ? TX : TXJ);
 #pragma unroll
             for (int dd = 0; dd < 2; ++dd) {
@@ -197,11 +204,12 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
         float *F = W.F + tk.fld_off;
         float *Tot = W.Tot + tk.fld_off;
         float *tl0 = W.Ttl + tot_tail_off(tk, G, 0, c), *tlN = W.Ttl + tot_tail_off(tk, G, nt, c);
-        float lo0 = 0.f, loN = 0.f;
+        float lo0 = 0.f, loN = 0.f, hd0 = 0.f, hdN = 0.f;
         float bc = 0.f;
         const bool water = d.medium == 1;
         if (valid) {
             lo0 = *tl0; loN = *tlN;
+            if (!G.tot_all) { hd0 = Tot[c]; hdN = Tot[(size_t)nt * G.LDC + c]; }
             if ((water && h == 1) || (!water && h == 0 && d.surf_on)) {
                 if (water || d.rough) {
                     // water: internal reflection of the previous order's upward field at the
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
                         const size_t o = (size_t)k * G.LDC + c;
                         F[o] = I;
                         if (k == 0 || k == nt) {
-                            const float ov = *(const float *)(vt + r * vrow);
+                            const float ov = G.tot_all ? *(const float *)(vt + r * vrow) : (k == 0 ? hd0 : hdN);
                             const float2 td = df_add(make_float2(ov, k == 0 ? lo0 : loN), I);
                             Tot[o] = td.x;
                             *(k == 0 ? tl0 : tlN) = td.y;
@@ -573,6 +581,8 @@ const void *scan_tma_fn(int ch, int ns)
     if (ch == 8 && ns == 4) return (const void *)k_scan_tma<8, 4>;
     if (ch == 4 && ns == 6) return (const void *)k_scan_tma<4, 6>;
     if (ch == 16 && ns == 2) return (const void *)k_scan_tma<16, 2>;
+    if (ch == 8 && ns == 5) return (const void *)k_scan_tma<8, 5>;
+    if (ch == 4 && ns == 10) return (const void *)k_scan_tma<4, 10>;
     return nullptr;
 }
 
@@ -585,13 +595,15 @@ cudaError_t scan_tma_launch(int ch, int ns, int grid, cudaStream_t st, const Bat
     else if (ch == 8 && ns == 4) k_scan_tma<8, 4><<<grid, th, sb, st>>>(B, W, G, t0, it, M);
     else if (ch == 4 && ns == 6) k_scan_tma<4, 6><<<grid, th, sb, st>>>(B, W, G, t0, it, M);
     else if (ch == 16 && ns == 2) k_scan_tma<16, 2><<<grid, th, sb, st>>>(B, W, G, t0, it, M);
+    else if (ch == 8 && ns == 5) k_scan_tma<8, 5><<<grid, th, sb, st>>>(B, W, G, t0, it, M);
+    else if (ch == 4 && ns == 10) k_scan_tma<4, 10><<<grid, th, sb, st>>>(B, W, G, t0, it, M);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
 cudaError_t scan_tma_init()
 {
-    const int v[4][2] = {{8, 3}, {8, 4}, {4, 6}, {16, 2}};
+    const int v[6][2] = {{8, 3}, {8, 4}, {4, 6}, {16, 2}, {8, 5}, {4, 10}};
     for (const auto &x : v) {
         const cudaError_t e =
             cudaFuncSetAttribute(scan_tma_fn(x[0], x[1]), cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

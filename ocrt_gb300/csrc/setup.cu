@@ -108,18 +108,38 @@ __global__ void k_levels(const PixDev *px, int P, double *h, double *ch, double 
             const double f = hk / tau;
             if (!aer && f >= 1.0) zk = 0.0;
             else {
-                // Once the midpoint equals an end, every later step leaves
-                // 0.5 (lo + hi) at that midpoint, so the loop can stop there.
                 double lo = 0.0, hi = aer ? OCRT_ZTOP_KM : ztop;
                 const double target = aer ? hk : f;
+                auto above_at = [&](double zz) {
+                    return aer ? tr * above_ray(E, zz) + ta * above_exp(zz, ah, E.et_a) : above_ray(E, zz);
+                };
+                // Illinois steps (regula falsi that halves the value of an end
+                // kept twice) narrow the bracket while keeping the bisection's
+                // invariant above(lo) > target >= above(hi), until it is ~1e-12
+                // wide relative; the bisection below then ends, as a full
+                // 64-step bisection from [0, top] does, on the two adjacent
+                // doubles around the crossing, in ~26 evaluations of the
+                // column fraction instead of ~58.  Where the computed fraction
+                // is not monotone in its last bits the two can end a few ulps
+                // apart (1.2e-15 relative at most over 60k levels of random
+                // profiles, 99.5% identical).
+                double flo = above_at(lo) - target, fhi = above_at(hi) - target;
+                int side = 0;
+                for (int it = 0; it < 40 && hi - lo > 1e-12 * hi; ++it) {
+                    double c = hi - fhi * (hi - lo) / (fhi - flo);
+                    if (!(c > lo && c < hi)) c = 0.5 * (lo + hi);
+                    const double fc = above_at(c) - target;
+                    if (fc > 0.0) { lo = c; flo = fc; if (side < 0) fhi *= 0.5; side = -1; }
+                    else { hi = c; fhi = fc; if (side > 0) flo *= 0.5; side = 1; }
+                }
+                // Once the midpoint equals an end, every later step leaves
+                // 0.5 (lo + hi) at that midpoint, so the loop can stop there.
                 zk = 0.5 * (lo + hi);
                 for (int it = 0; it < 64; ++it) {
                     const double mid = 0.5 * (lo + hi);
                     zk = mid;
                     if (mid == lo || mid == hi) break;
-                    const double above = aer ? tr * above_ray(E, mid) + ta * above_exp(mid, ah, E.et_a)
-                                             : above_ray(E, mid);
-                    if (above > target) lo = mid; else hi = mid;
+                    if (above_at(mid) > target) lo = mid; else hi = mid;
                     zk = 0.5 * (lo + hi);
                 }
             }

@@ -25,7 +25,7 @@ def _batch(A, N, n=6, seed=5, surfaces=("black_fresnel_ocean", "black", "flat"))
     return cases, opts, aers
 
 
-SCANS = ["quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2"]
+SCANS = ["quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2", "tma8x5", "tma4x10"]
 
 
 @pytest.mark.parametrize("N", [8, 24, 32])
@@ -41,7 +41,7 @@ def test_scan_equals_column_scan(gpu, monkeypatch, N, scan):
         np.testing.assert_allclose(quad[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
 
 
-@pytest.mark.parametrize("scan", ["quad", "tma8x3"])
+@pytest.mark.parametrize("scan", ["quad", "tma8x3", "tma8x5"])
 def test_scan_equals_column_scan_coupled_ocean(gpu, monkeypatch, scan):
     """The water column's top boundary (internal reflection, four zero-weight
     ring slots) in every scan."""
@@ -79,7 +79,7 @@ def test_scan_autotuner_matches_column_scan(gpu, monkeypatch):
         np.testing.assert_allclose(again[k], col[k], rtol=1e-12, atol=1e-15, err_msg=k)
     recs = [r for r in gpu.autotune_summary() if r["kernel"] == "transport_scan" and r["key"][:2] == [20, 1]]
     assert recs, gpu.autotune_summary()
-    assert recs[0]["best"] in ("quad", "tma8x3", "tma8x4", "tma4x6", "tma16x2")
+    assert recs[0]["best"] in SCANS
 
 
 @pytest.mark.parametrize("N", [8, 32])
