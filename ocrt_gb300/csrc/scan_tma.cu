@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
 {
     extern __shared__ unsigned char stm_raw[];
     __shared__ float2 redf2[32];
-    __shared__ int item_s, abort_raw;
+    __shared__ int item_s, item_nx, abort_raw;
     volatile int &abort_s = abort_raw;
     unsigned char *base = (unsigned char *)(((uintptr_t)stm_raw + 127) & ~(uintptr_t)127);
     const StmLayout Ly = stm_layout(G, CH);
@@ -160,10 +160,18 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
     const uint32_t vrow = gauss ? (uint32_t)(3 * N) * 4u : (uint32_t)ZW * 4u;
     const uint32_t cofs = (uint32_t)(((g >> 2) * 12 + (g & 3)) * 4), crow = (uint32_t)CW * 4u;
     uint32_t issued = 0, consumed = 0;                   // chunks issued / consumed by this CTA (ring position)
+    // The producer fetches the items: the first one here, each next one as
+    // soon as the current item's chunks are all issued, and it then issues
+    // the next item's first chunks into the ring slots the consumers free
+    // while they finish the current item (run-ahead), so a new item's first
+    // copies are in flight before the consumers reach it.  pre = chunks of
+    // the current item already issued that way (producer only).
+    int pre = 0;
+    if (producer) item_nx = atomicAdd(&B.work[it * 4 + 2], 1);
     __syncthreads();
     for (;;) {
         __syncthreads();
-        if (tid == 0) item_s = abort_s ? n_items : atomicAdd(&B.work[it * 4 + 2], 1);
+        if (tid == 0) item_s = abort_s ? n_items : item_nx;
         __syncthreads();
         if (item_s >= n_items) break;
         const int tl = B.alist[it & 1][item_s], tg = t0 + tl;
@@ -172,8 +180,9 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
         const PixDev &d = B.px[tk.pix];
         const int nt = d.nt, nq = (nt + CH) / CH;        // ceil((nt + 1) / CH) chunks of steps j = 0 .. nt
         const int row0 = (int)(tk.fld_off / G.LDC), lay0 = (int)(d.coef_off / NR);
-        // ---- producer: issue chunk q of this task into ring position issued ----
-        auto issue = [&](int q) -> bool {
+        // ---- producer: issue chunk q of a task (levels nt_, first field row
+        // row0_, first layer lay0_) into ring position issued ----
+        auto issue_of = [&](int q, int nt_, int row0_, int lay0_) -> bool {
             const uint32_t pos = issued, sl = pos % NS;
             if (pos >= (uint32_t)NS && !mbar_wait(&empty[sl], ((pos / NS) - 1) & 1)) return false;
             unsigned char *stg = base + (size_t)sl * Ly.stage;
@@ -183,20 +192,21 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
 #pragma unroll
             for (int dd = 0; dd < 2; ++dd) {
                 unsigned char *db = stg + dd * Ly.dir;
-                const int r = dd == 0 ? nt - q * CH - CH + 1 : q * CH;       // first level row of the box
+                const int r = dd == 0 ? nt_ - q * CH - CH + 1 : q * CH;      // first level row of the box
                 const int ly = dd == 0 ? r : q * CH - 1;                      // first layer of the box
-                tma4(db + Ly.jg, &M.jg, 0, dd, 0, row0 + r, &full[sl]);
-                if (wt) tma4(db + Ly.tg, &M.tg, 0, dd, 0, row0 + r, &full[sl]);
-                tma2(db + Ly.jz, &M.jz, 6 * N, row0 + r, &full[sl]);
-                if (wt) tma2(db + Ly.tz, &M.tz, 6 * N, row0 + r, &full[sl]);
-                tma2(db + Ly.cf, &M.cq, 0, lay0 + ly, &full[sl]);
+                tma4(db + Ly.jg, &M.jg, 0, dd, 0, row0_ + r, &full[sl]);
+                if (wt) tma4(db + Ly.tg, &M.tg, 0, dd, 0, row0_ + r, &full[sl]);
+                tma2(db + Ly.jz, &M.jz, 6 * N, row0_ + r, &full[sl]);
+                if (wt) tma2(db + Ly.tz, &M.tz, 6 * N, row0_ + r, &full[sl]);
+                tma2(db + Ly.cf, &M.cq, 0, lay0_ + ly, &full[sl]);
             }
             issued = pos + 1;
             return true;
         };
+        auto issue = [&](int q) -> bool { return issue_of(q, nt, row0, lay0); };
         const int npre = nq < NS ? nq : NS;
         if (producer) {
-            for (int q = 0; q < npre; ++q)
+            for (int q = pre; q < npre; ++q)
                 if (!issue(q)) { abort_s = 1; break; }
         }
         // ---- boundary condition from the previous order's field (as in k_scan) ----
@@ -237,8 +247,23 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
         float mi = 0.f, mt = 0.f;
         int bad = 0;
         if (producer) {
-            for (int q = npre; q < nq && !abort_s; ++q)
+            for (int q = npre > pre ? npre : pre; q < nq && !abort_s; ++q)
                 if (!issue(q)) { abort_s = 1; break; }
+            // run-ahead: the next item and its first chunks; the slots they
+            // take are freed by the consumers' progress through this item,
+            // which needs nothing more from the producer
+            pre = 0;
+            item_nx = abort_s ? n_items : atomicAdd(&B.work[it * 4 + 2], 1);
+            if (item_nx < n_items) {
+                const TaskDev tn = B.tasks[t0 + B.alist[it & 1][item_nx]];
+                const PixDev &dn = B.px[tn.pix];
+                const int nqn = (dn.nt + CH) / CH, npn = nqn < NS ? nqn : NS;
+                const int r0n = (int)(tn.fld_off / G.LDC), l0n = (int)(dn.coef_off / NR);
+                for (int q = 0; q < npn && !abort_s; ++q) {
+                    if (!issue_of(q, dn.nt, r0n, l0n)) { abort_s = 1; break; }
+                    pre = q + 1;
+                }
+            }
         } else if (tid < ncw * 32) {
             float I = (water ? h == 1 : h == 0) ? bc : 0.f, Jp = 0.f;
             for (int q = 0; q < nq; ++q) {
