@@ -90,6 +90,8 @@ __device__ __forceinline__ void tma4(void *dst, const CUtensorMap *m, int c0, in
                  : "memory");
 }
 
+// Block maxima of (a, b), valid in thread 0.  One barrier: the caller
+// passes a barrier between a thread 0 read of red and the next call.
 __device__ inline float2 stm_maxf2(float a, float b, float2 *red)
 {
     for (int o = 16; o > 0; o >>= 1) {
@@ -97,17 +99,11 @@ __device__ inline float2 stm_maxf2(float a, float b, float2 *red)
         b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
     }
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
     if (l == 0) red[w] = make_float2(a, b);
     __syncthreads();
-    if (w == 0) {
+    if (threadIdx.x == 0) {
         const int nw = (blockDim.x + 31) >> 5;
-        const float2 v = l < nw ? red[l] : make_float2(0.f, 0.f);
-        a = v.x; b = v.y;
-        for (int o = 16; o > 0; o >>= 1) {
-            a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
-            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
-        }
+        for (int i = 1; i < nw; ++i) { a = fmaxf(a, red[i].x); b = fmaxf(b, red[i].y); }
     }
     return make_float2(a, b);
 }
@@ -125,7 +121,7 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
 {
     extern __shared__ unsigned char stm_raw[];
     __shared__ float2 redf2[32];
-    __shared__ int item_s, item_nx, abort_raw;
+    __shared__ int item_nx, abort_raw;
     volatile int &abort_s = abort_raw;
     unsigned char *base = (unsigned char *)(((uintptr_t)stm_raw + 127) & ~(uintptr_t)127);
     const StmLayout Ly = stm_layout(G, CH);
@@ -170,11 +166,11 @@ __global__ void __launch_bounds__(256, 3) k_scan_tma(BatchBufs B, WaveBufs W, Ge
     if (producer) item_nx = atomicAdd(&B.work[it * 4 + 2], 1);
     __syncthreads();
     for (;;) {
-        __syncthreads();
-        if (tid == 0) item_s = abort_s ? n_items : item_nx;
-        __syncthreads();
-        if (item_s >= n_items) break;
-        const int tl = B.alist[it & 1][item_s], tg = t0 + tl;
+        // item_nx was written before the previous item's reduction barrier and
+        // is rewritten only after this item's boundary-condition barrier
+        const int item_c = __syncthreads_or(abort_s != 0) ? n_items : item_nx;
+        if (item_c >= n_items) break;
+        const int tl = B.alist[it & 1][item_c], tg = t0 + tl;
         const TaskState st = B.state[tg];
         const TaskDev tk = B.tasks[tg];
         const PixDev &d = B.px[tk.pix];
