@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
                                                          const __grid_constant__ AdjScanMaps M)
 {
     extern __shared__ unsigned char ast_raw[];
-    __shared__ float2 redf2[32];
+    __shared__ float2 redr[32][ADJ_RB];
     __shared__ int item_s, abort_raw;
     volatile int &abort_s = abort_raw;
     unsigned char *base = (unsigned char *)(((uintptr_t)ast_raw + 127) & ~(uintptr_t)127);
@@ -544,11 +544,28 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
     consumed += (uint32_t)nq;
     __syncthreads();
     if (abort_s) break;
+    // every row's maxima in one block reduction: lane 0 of each warp stores
+    // its warp's (mi, mt) per row, one barrier, thread 0 finishes (the values
+    // are non-negative, so 0 starts the maximum)
+#pragma unroll
+    for (int rq = 0; rq < ADJ_RB; ++rq) {
+        float a = mi[rq], b = mt[rq];
+        for (int o = 16; o > 0; o >>= 1) {
+            a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
+        if (lane == 0) redr[tid >> 5][rq] = make_float2(a, b);
+    }
+    __syncthreads();
 #pragma unroll
     for (int rq = 0; rq < ADJ_RB; ++rq) {
         if (!act[rq]) continue;                    // block-uniform
-        const float2 mm = stm_maxf2(mi[rq], mt[rq], redf2);
         if (threadIdx.x == 0) {
+            float2 mm = make_float2(0.f, 0.f);
+            for (int w = 0; w < (nthr >> 5); ++w) {
+                mm.x = fmaxf(mm.x, redr[w][rq].x);
+                mm.y = fmaxf(mm.y, redr[w][rq].y);
+            }
             const int ta = tl * A.ncot + r0 + rq;
             TaskState ns = A.st[ta];
             ns.orders = j;
@@ -561,7 +578,6 @@ __global__ void __launch_bounds__(256, 2) k_adj_scan_tma(BatchBufs B, AdjBufs A,
                 A.aflag[tl] = 1;                           // the task stays on the next order's list
             }
         }
-        __syncthreads();
     }
     }
     if (abort_s) {
